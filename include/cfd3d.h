@@ -1,0 +1,174 @@
+/*
+ * cfd3d.h -- C ABI of the GB300-native pseudo-iteration engine (libcfd3d_gb300.so).
+ *
+ * The engine replaces one hot path of kwonhwi1/3dcode: the per-pseudo-iteration
+ * LU-SGS update `t_update%timeinteg` (src/update_module.f90:37-52, implementation
+ * `lusgs` :455-733) together with the convergence residual `t_resi%setqres/residual`
+ * (src/residual_module.f90:94-186), as called from `solve_equation`
+ * (src/solve_module.f90:133-136).  A Fortran caller binds these entry points through
+ * ISO_C_BINDING; Python binds them through ctypes.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  All arrays are FP64 in the reference's Fortran
+ *    storage order (first index fastest).
+ *  - Block sizes imax/jmax/kmax are NODE counts per direction, exactly as the
+ *    reference's grid module reads them (src/grid_module.f90:107-116); interior cells
+ *    are i = 2..imax, the padded cell range is -1..imax+3 (src/variable_module.f90:69-71).
+ *  - Every entry point returns CFD3D_OK (0) or a CFD3D_ERR_* code; the message of the
+ *    last failure is available through cfd3d_last_error().  No exception crosses the ABI.
+ *  - One host thread per handle.  The handle owns every device buffer, its CUDA stream
+ *    and its CUDA graphs; host arrays stay owned by the caller.
+ */
+#ifndef CFD3D_H
+#define CFD3D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+#define CFD3D_OK               0
+#define CFD3D_ERR_ARG          1   /* bad argument or unsupported option            */
+#define CFD3D_ERR_CUDA         2   /* a CUDA runtime call failed                     */
+#define CFD3D_ERR_NONFINITE    3   /* NaN/Inf detected in the updated state          */
+#define CFD3D_ERR_VOLUME       4   /* zero or negative cell volume in the grid       */
+#define CFD3D_ERR_TIMEOUT      5   /* a bounded device wait ran out                  */
+#define CFD3D_ERR_DESCRIPTOR   6   /* inconsistent block / BC / connection descriptor */
+#define CFD3D_ERR_NOMEM        7   /* device allocation failed                       */
+#define CFD3D_ERR_NODEVICE     8   /* no CUDA device is visible                      */
+
+/* ---- arithmetic forms ---------------------------------------------------------- */
+#define CFD3D_FP64   0   /* every kernel in FP64 (the reference's arithmetic)        */
+#define CFD3D_MIXED  1   /* FP32 reconstruction/limiter/flux, FP64 EOS mixture,
+                            accumulation, diagonal inversion and update             */
+
+/* ---- boundary-condition kinds (names of the CGNS BC families the reference
+ *      dispatches on, src/bc_module.f90:221-335) -------------------------------- */
+#define CFD3D_BC_WALL         1   /* BCWall: inviscid / viscous / SST wall by iturb   */
+#define CFD3D_BC_SYMMETRY     2   /* BCSymmetryPlane                                  */
+#define CFD3D_BC_FARFIELD     3   /* BCFarfield (characteristic, with EOS)            */
+#define CFD3D_BC_EXTRAPOLATE  4   /* BCExtrapolate / BCOutflowSupersonic              */
+#define CFD3D_BC_DEGENERATE   5   /* BCDegeneratePoint / BCDegenerateLine             */
+#define CFD3D_BC_INFLOW       6   /* BCInflow (the reference's routine is a no-op)    */
+
+/* Solver configuration: the fields of the reference's input.inp
+ * (src/config_module.f90:100-119, documented in bin/input_templet.inp:34-66). */
+typedef struct cfd3d_config {
+  int    nsteady, npmax, ntmax, bond;   /* 0 steady, 1 BDF1, 2 BDF2                */
+  double dt_phy;
+  int    iturb, ides;                   /* -3 Euler, -2 laminar, 0 k-omega SST      */
+  int    nscheme, nmuscl, nlim;         /* flux, reconstruction, limiter            */
+  int    timemethod, local, prec;       /* 3 = LU-SGS; local -1/0/1; prec 0/1/2     */
+  double cfl;
+  int    fluid, ngas;                   /* 1 stiffened water, 2 IAPWS-97; 1 ideal gas */
+  int    ncav;                          /* 0 none, 1 Merkle ... 5 Lee               */
+  double c_v, c_c;
+  double pref, uref, aoa, aos, tref, y1ref, y2ref;   /* aoa, aos in degrees       */
+  double l_chord, l_character, scale, l_domain;
+  /* extensions (0 keeps the reference's behaviour) */
+  int    fix_cav_clamp;   /* 1: clamp r_c by rho*y1 and r_v by rho*(1-y1-y2)
+                             instead of the reference's temperature-indexed clamp */
+  int    precision;       /* CFD3D_FP64 or CFD3D_MIXED                            */
+  double kinf, oinf;      /* >0: replace the SST free-stream k / omega that
+                             config%setref derives (src/config_module.f90:186-189) */
+} cfd3d_config;
+
+/* A boundary patch: CGNS PointRange in 1-based NODE indices
+ * (imin, jmin, kmin, imax, jmax, kmax), one index pair collapsed to a face. */
+typedef struct cfd3d_bc_patch {
+  int type;
+  int pnts[6];
+} cfd3d_bc_patch;
+
+/* A point-matched 1-to-1 interface, as cg_1to1_read_f returns it: own range,
+ * donor range (1-based node indices) and the transform vector. */
+typedef struct cfd3d_connection {
+  int donor;            /* 0-based block index of the neighbouring block */
+  int pnts[6];
+  int pnts_donor[6];
+  int transform[3];
+} cfd3d_connection;
+
+typedef struct cfd3d_block_desc {
+  int imax, jmax, kmax;             /* node counts                                   */
+  const double *xyz;                /* node coordinates x(3, imax, jmax, kmax)        */
+  int nbc;
+  const cfd3d_bc_patch *bc;
+  int ncon;
+  const cfd3d_connection *con;
+} cfd3d_block_desc;
+
+typedef struct cfd3d_handle cfd3d_handle;
+
+/* Build the engine: config%construct + grid%construct + variable%construct +
+ * update%construct (src/main.f90:15-35).  Computes the metrics, the wall distance,
+ * the BC/edge/corner ghost programs and the halo copy lists, and allocates every
+ * device buffer.  Replaces: src/config_module.f90:90-165, src/grid_module.f90:75-332,
+ * src/update_module.f90:77-178, src/bc_module.f90:71-1188. */
+int  cfd3d_create(const cfd3d_config *cfg, int nblocks, const cfd3d_block_desc *blocks,
+                  cfd3d_handle **out);
+void cfd3d_destroy(cfd3d_handle *h);
+const char *cfd3d_last_error(const cfd3d_handle *h);
+
+/* Derived sizes (config%getnpv/getndv/getntv/getnqq, grid%getngrd). */
+int  cfd3d_sizes(const cfd3d_handle *h, int *npv, int *ndv, int *ntv, int *nqq, int *ngrd);
+
+/* Initial state: t_ini_initial + set_others (src/initial_module.f90:678-771).
+ * pv_interior == NULL gives the uniform free stream; otherwise it holds
+ * pv(npv, 2:imax, 2:jmax, 2:kmax) (k and omega are taken from it when iturb = 0). */
+int  cfd3d_initialize(cfd3d_handle *h, int block, const double *pv_interior);
+
+/* Copy a full padded state in/out: pv(npv,-1:imax+3,..), dv(ndv,..), tv(ntv,..),
+ * qq(npv,nqq,2:imax,..) and (out only) rcav(2,2:imax,..).  Any pointer may be NULL.
+ * Replaces the accessors t_variable%getpv/setpv.. (src/variable_module.f90:22-39). */
+int  cfd3d_upload_state(cfd3d_handle *h, int block, const double *pv, const double *dv,
+                        const double *tv, const double *qq);
+int  cfd3d_download_state(cfd3d_handle *h, int block, double *pv, double *dv, double *tv,
+                          double *qq, double *rcav);
+
+/* One pseudo-iteration: resi%setqres + update%timeinteg (LU-SGS) + resi%residual
+ * (src/solve_module.f90:134-136).  Outputs the solution time, the L2 norms
+ * res_l2[npv] of the state change, and the location (block,i,j,k) of the largest
+ * pressure change.  Any output pointer may be NULL. */
+int  cfd3d_iterate(cfd3d_handle *h, int nt_phy, int nt, double timeprev, double *time_out,
+                   double *res_l2, int *resmax_loc);
+
+/* niter pseudo-iterations back to back on the device (CUDA-graph replays), with one
+ * host synchronisation at the end; res_l2 receives the norms of the last one. */
+int  cfd3d_iterate_n(cfd3d_handle *h, int niter, int nt_phy, int nt0, double timeprev,
+                     double *time_out, double *res_l2);
+
+/* Physical-time BDF history shift: solve%unsteadyupdate (src/solve_module.f90:155-183). */
+int  cfd3d_unsteady_shift(cfd3d_handle *h);
+
+/* Ghost fill + residual only (bc%setbc + rhs%calrhs, src/rhs_module.f90:260-643) on the
+ * current state, without updating it: res(npv,2:imax,..), icav(4,..), itt(4,..),
+ * omega_cut(2:imax,..).  Pointers may be NULL. */
+int  cfd3d_residual(cfd3d_handle *h, int block, double *res, double *icav, double *itt,
+                    double *omega_cut);
+
+/* Grid metrics as the reference stores them: cx(3,1:imax,1:jmax+1,1:kmax+1),
+ * ex(3,1:imax+1,1:jmax,1:kmax+1), tx(3,1:imax+1,1:jmax+1,1:kmax),
+ * grd(ngrd,1:imax+1,1:jmax+1,1:kmax+1) (src/grid_module.f90:609-1241). */
+int  cfd3d_grid_metrics(cfd3d_handle *h, int block, double *cx, double *ex, double *tx,
+                        double *grd);
+
+/* Pointwise mixture EOS on the device: eos%deteos_simple (with_prop = 0) or
+ * eos%deteos with transport properties (with_prop = 1)
+ * (src/eos_module.f90:1064-1234).  Host arrays of n points; dv is dv(18, n),
+ * tv is tv(2, n) (may be NULL when with_prop = 0). */
+int  cfd3d_eos_eval(int fluid, int ngas, int with_prop, int64_t n, const double *p,
+                    const double *t, const double *y1, const double *y2, double *dv,
+                    double *tv);
+
+/* Device-side statistics of the last iterate call: how many EOS evaluations took
+ * the reference's "alternative calculation for snd2" branch
+ * (src/eos_module.f90:1104-1111), and the kernel launches of one iteration. */
+int  cfd3d_stats(const cfd3d_handle *h, int64_t *snd2_fallbacks, int *launches_per_iter);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFD3D_H */
