@@ -1,0 +1,1321 @@
+// engine.cu -- kernels of one LU-SGS pseudo-iteration and the C ABI (include/cfd3d.h).
+//
+// One iteration (the reference's `lusgs`, src/update_module.f90:455-733, plus the
+// residual of src/residual_module.f90:110-186) is a fixed sequence of launches on the
+// handle's stream, captured once into a CUDA graph and replayed:
+//
+//   k_timestep            local time step + global minimum   (timestep_module.f90:127-212)
+//   k_ghost x3            boundary program: faces+halos, edges, corners (bc_module.f90:1235-1396)
+//   k_face_flux x3        inviscid + viscous face fluxes per direction (rhs_module.f90:282-538)
+//   k_rhs                 flux differences + cavitation / SST / dual-time sources (:540-642)
+//   k_sweep (fwd) x S     forward LU-SGS sweep, one launch per hyperplane i+j+k = s
+//   k_sweep (bwd) x S     backward sweep                          (update_module.f90:486-670)
+//   k_update              pv += dq, clipping, EOS with transport, residual partial sums (:672-700)
+//   k_eddy                SST eddy viscosity                      (:701-732)
+//   k_finish              residual norms, max location, solution time
+//
+// All blocks of a multi-block case advance together in every launch; the LU-SGS
+// operator stays block-local (dq outside a block is zero), as in the reference.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include "engine.cuh"
+
+namespace cfd {
+
+// ------------------------------------------------------------------ index helpers
+__device__ __forceinline__ int find_block_interior(const BlockGeom* B, int nb, long long t) {
+  int b = 0;
+  while (b + 1 < nb && t >= B[b + 1].int_off) ++b;
+  return b;
+}
+__device__ __forceinline__ int find_block_cell(const BlockGeom* B, int nb, long long g) {
+  int b = 0;
+  while (b + 1 < nb && g >= B[b + 1].off) ++b;
+  return b;
+}
+__device__ __forceinline__ long long interior_cell(const BlockGeom& B, long long loc, int& i, int& j, int& k) {
+  int ni = B.imax - 1, nj = B.jmax - 1;
+  i = (int)(loc % ni) + 2;
+  long long r = loc / ni;
+  j = (int)(r % nj) + 2;
+  k = (int)(r / nj) + 2;
+  return B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1));
+}
+
+struct Cell {
+  double pv[NPVM], dv[NDV], tv[3];
+};
+
+__device__ __forceinline__ void load_cell(const DevPtr& d, const Par& c, long long g, Cell& x) {
+  const long long n = d.ncell;
+  for (int v = 0; v < c.npv; ++v) x.pv[v] = d.pv[v * n + g];
+  for (int v = 0; v < NDV; ++v) x.dv[v] = d.dv[v * n + g];
+  x.tv[0] = x.tv[1] = x.tv[2] = 0.0;
+  for (int v = 0; v < c.ntv; ++v) x.tv[v] = d.tv[v * n + g];
+}
+__device__ __forceinline__ void store_cell(const DevPtr& d, const Par& c, long long g, const Cell& x) {
+  const long long n = d.ncell;
+  for (int v = 0; v < c.npv; ++v) d.pv[v * n + g] = x.pv[v];
+  for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = x.dv[v];
+  for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = x.tv[v];
+}
+__device__ __forceinline__ void face_vec(const DevPtr& d, int plane, long long g, double* o) {
+  o[0] = d.gm[(plane + 0) * d.ncell + g];
+  o[1] = d.gm[(plane + 1) * d.ncell + g];
+  o[2] = d.gm[(plane + 2) * d.ncell + g];
+}
+
+// ------------------------------------------------------------------ pointwise EOS
+__global__ void k_eos_points(int fluid, int with_prop, long long n, const double* __restrict__ p,
+                             const double* __restrict__ t, const double* __restrict__ y1,
+                             const double* __restrict__ y2, double* __restrict__ dv, double* __restrict__ tv,
+                             unsigned long long* fb) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double d[NDV], tt[2] = {0.0, 0.0};
+  deteos(fluid, with_prop, p[q], t[q], y1[q], y2[q], d, tt, fb);
+  for (int v = 0; v < NDV; ++v) dv[NDV * q + v] = d[v];
+  if (tv) { tv[2 * q] = tt[0]; tv[2 * q + 1] = tt[1]; }
+}
+
+// ------------------------------------------------------------------ initial state
+// set_others (src/initial_module.f90:707-771) on the uploaded interior pv
+__global__ void k_init(DevPtr d, Par c, int b) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const BlockGeom& B = d.blk[b];
+  if (t >= (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1)) return;
+  int i, j, k;
+  long long g = interior_cell(B, t, i, j, k);
+  const long long n = d.ncell;
+  double pv[NPVM], dv[NDV], tv[3] = {0.0, 0.0, 0.0};
+  for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
+  deteos(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
+  if (c.iturb == 0) tv[2] = c.emutref;
+  for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
+  for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
+  if (c.nqq) {
+    double q[NPVM];
+    q[0] = dv[0]; q[1] = dv[0] * pv[1]; q[2] = dv[0] * pv[2]; q[3] = dv[0] * pv[3];
+    q[4] = dv[0] * (dv[1] + 0.5 * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3])) - pv[0] - c.pref;
+    for (int v = 5; v < c.npv; ++v) q[v] = dv[0] * pv[v];
+    for (int v = 0; v < c.npv; ++v) { d.qq[v * n + g] = q[v]; d.qq[(c.npv + v) * n + g] = q[v]; }
+  }
+  if (c.ncav) { d.rcav[g] = 0.0; d.rcav[n + g] = 0.0; }
+}
+
+// BDF history shift (solve%unsteadyupdate, src/solve_module.f90:155-183)
+__global__ void k_unsteady_shift(DevPtr d, Par c) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= d.nint) return;
+  int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
+  long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
+  const long long n = d.ncell;
+  double pv[NPVM];
+  for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
+  double r = d.dv[g], h = d.dv[n + g];
+  for (int v = 0; v < c.npv; ++v) d.qq[(c.npv + v) * n + g] = d.qq[v * n + g];
+  d.qq[g] = r;
+  d.qq[n + g] = r * pv[1];
+  d.qq[2 * n + g] = r * pv[2];
+  d.qq[3 * n + g] = r * pv[3];
+  d.qq[4 * n + g] = r * (h + 0.5 * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3])) - pv[0] - c.pref;
+  for (int v = 5; v < c.npv; ++v) d.qq[v * n + g] = r * pv[v];
+}
+
+// ------------------------------------------------------------------ local time step
+__global__ void k_timestep(DevPtr d, Par c) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double dtv = 1.0e10;
+  if (t < d.nint) {
+    int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
+    const BlockGeom& B = d.blk[b];
+    long long g = interior_cell(B, t - B.int_off, i, j, k);
+    if (c.local == -1) {
+      dtv = c.cfl;
+    } else {
+      const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+      double u = d.pv[n + g], v = d.pv[2 * n + g], w = d.pv[3 * n + g];
+      double dv[NDV];
+      for (int q = 0; q < NDV; ++q) dv[q] = d.dv[q * n + g];
+      double tv[3] = {0.0, 0.0, 0.0};
+      for (int q = 0; q < c.ntv; ++q) tv[q] = d.tv[q * n + g];
+      double vol = d.gm[GM_GRD * n + g];
+      double cs[3][3];
+      for (int q = 0; q < 3; ++q) {
+        cs[0][q] = 0.5 * (d.gm[(GM_CX + q) * n + g - 1] + d.gm[(GM_CX + q) * n + g]);
+        cs[1][q] = 0.5 * (d.gm[(GM_EX + q) * n + g - sj] + d.gm[(GM_EX + q) * n + g]);
+        cs[2][q] = 0.5 * (d.gm[(GM_TX + q) * n + g - sk] + d.gm[(GM_TX + q) * n + g]);
+      }
+      double sndp2 = sndp2_of<double>(c, dv[5], u * u + v * v + w * w);
+      double qf = sndp2 / dv[5];
+      double eig = 0.0, ss = 0.0;
+      for (int q = 0; q < 3; ++q) {
+        double uc = fabs(cs[q][0] * u + cs[q][1] * v + cs[q][2] * w);
+        double s = cs[q][0] * cs[q][0] + cs[q][1] * cs[q][1] + cs[q][2] * cs[q][2];
+        double up = uc * (1.0 + qf);
+        double dd = sqrt(uc * uc * (1.0 - qf) * (1.0 - qf) + 4.0 * sndp2 * s);
+        eig += 0.5 * (up + dd);
+        ss += s;
+      }
+      double ev = eigenvis_of(c, dv, tv) * ss / vol;
+      dtv = c.cfl * vol / (eig + 4.0 * ev);
+    }
+    d.dt[g] = dtv;
+  }
+  // block minimum -> one atomic per CTA (positive doubles order like their bit patterns)
+  for (int o = 16; o > 0; o >>= 1) dtv = fmin(dtv, __shfl_xor_sync(0xffffffffu, dtv, o));
+  __shared__ double wmin[32];
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = dtv;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double m = (threadIdx.x < (blockDim.x >> 5)) ? wmin[threadIdx.x] : 1.0e10;
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) atomicMin(&d.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+// ------------------------------------------------------------------ boundary program
+__global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int nops) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nops) return;
+  const GhostOp op = ops[q];
+  const long long n = d.ncell;
+  Cell x;
+  switch (op.kind) {
+    case G_COPY:
+    case G_EXTRAP:
+      load_cell(d, c, op.src, x);
+      store_cell(d, c, op.dst, x);
+      return;
+    case G_WALL_VISCOUS:
+      load_cell(d, c, op.src, x);
+      x.pv[1] = -x.pv[1]; x.pv[2] = -x.pv[2]; x.pv[3] = -x.pv[3];
+      store_cell(d, c, op.dst, x);
+      return;
+    case G_WALL_KW: {
+      load_cell(d, c, op.src, x);
+      double vis_b = d.tv[op.bnd], rho_b = d.dv[op.bnd], y5 = d.gm[(GM_GRD + 4) * n + op.bnd];
+      double om = 1600.0 * vis_b / rho_b / (y5 * y5) - x.pv[8];
+      x.pv[1] = -x.pv[1]; x.pv[2] = -x.pv[2]; x.pv[3] = -x.pv[3]; x.pv[7] = -x.pv[7]; x.pv[8] = om;
+      x.tv[2] = -x.tv[2];
+      store_cell(d, c, op.dst, x);
+      return;
+    }
+    case G_SYMMETRY: {
+      load_cell(d, c, op.src, x);
+      double nx[3];
+      face_vec(d, op.fplane, op.fidx, nx);
+      for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;
+      double us = d.pv[n + op.bnd], vs = d.pv[2 * n + op.bnd], ws = d.pv[3 * n + op.bnd];
+      double un = (us * nx[0] + vs * nx[1] + ws * nx[2]) / (nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
+      x.pv[1] = 2.0 * (us - nx[0] * un) - x.pv[1];
+      x.pv[2] = 2.0 * (vs - nx[1] * un) - x.pv[2];
+      x.pv[3] = 2.0 * (ws - nx[2] * un) - x.pv[3];
+      store_cell(d, c, op.dst, x);
+      return;
+    }
+    case G_FARFIELD: {
+      load_cell(d, c, op.src, x);
+      double nx[3];
+      face_vec(d, op.fplane, op.fidx, nx);
+      for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;
+      double pb[NPVM];
+      for (int v = 0; v < c.npv; ++v) pb[v] = d.pv[v * n + op.bnd];
+      double rb = d.dv[op.bnd], c2b = d.dv[5 * n + op.bnd];
+      double dl = 1.0 / sqrt(nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
+      double vel = (pb[1] * nx[0] + pb[2] * nx[1] + pb[3] * nx[2]) * dl;
+      double mach = vel / sqrt(c2b);
+      double a = sqrt(sndp2_of<double>(c, c2b, vel * vel));
+      // free-stream state bcinfo%pv with bcinfo%pressure = pref
+      double bp[NPVM];
+      bp[0] = c.pref; bp[1] = c.uref_vec[0]; bp[2] = c.uref_vec[1]; bp[3] = c.uref_vec[2];
+      bp[4] = c.tref; bp[5] = c.y1ref; bp[6] = c.y2ref; bp[7] = c.kref; bp[8] = c.oref;
+      double* pv = x.pv;
+      if (mach >= 0.0) {
+        if (mach < 1.0) {
+          pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
+          for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (pb[1 + q3] + nx[q3] * (pb[0] + bp[0] - c.pref) / rb / a * dl) - pv[1 + q3];
+        }
+      } else if (mach <= -1.0) {
+        pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
+        for (int v = 1; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
+        pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
+        pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
+      } else {
+        double var = c.pref - bp[0] + pb[0] - rb * a * (nx[0] * (bp[1] - pb[1]) + nx[1] * (bp[2] - pb[2]) + nx[2] * (bp[3] - pb[3])) * dl;
+        pv[0] = var - pv[0];
+        for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (bp[1 + q3] + nx[q3] * 0.5 * var / rb / a * dl) - pv[1 + q3];
+        for (int v = 4; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
+        pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
+        pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
+      }
+      deteos(c.fluid, c.with_prop, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      store_cell(d, c, op.dst, x);
+      return;
+    }
+    case G_WALLWALL:
+    case G_WALLWALL_KW4:
+    case G_WALLWALL_KW8: {
+      load_cell(d, c, op.src, x);
+      double ppv[NPVM];
+      for (int v = 0; v < c.npv; ++v) ppv[v] = -x.pv[v];
+      for (int m = 0; m < 6; ++m) {
+        if (op.nb[m] < 0) break;
+        for (int v = 0; v < c.npv; ++v) ppv[v] -= d.pv[v * n + op.nb[m]];
+      }
+      x.pv[1] = ppv[1]; x.pv[2] = ppv[2]; x.pv[3] = ppv[3];
+      if (op.kind == G_WALLWALL) {
+        if (c.npv > 7) { x.pv[7] = ppv[7]; x.pv[8] = ppv[8]; }
+      } else {
+        double y5 = d.gm[(GM_GRD + 4) * n + op.src];
+        double var = 800.0 * x.tv[0] / x.dv[0] / (y5 * y5);
+        x.pv[7] = ppv[7];
+        x.pv[8] = ((op.kind == G_WALLWALL_KW8) ? 8.0 : 4.0) * var + ppv[8];
+      }
+      store_cell(d, c, op.dst, x);
+      return;
+    }
+    case G_NOWALL3:
+    case G_NOWALL7: {
+      double pv[NPVM], tv[3] = {0.0, 0.0, 0.0};
+      for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + op.src];
+      for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + op.src];
+      for (int m = 0; m < 6; ++m) {
+        if (op.nb[m] < 0) break;
+        for (int v = 0; v < c.npv; ++v) pv[v] += d.pv[v * n + op.nb[m]];
+        for (int v = 0; v < c.ntv; ++v) tv[v] += d.tv[v * n + op.nb[m]];
+      }
+      double f = (op.kind == G_NOWALL7) ? 1.0 / 7.0 : 1.0 / 3.0;
+      for (int v = 0; v < c.npv; ++v) x.pv[v] = f * pv[v];
+      for (int v = 0; v < 3; ++v) x.tv[v] = f * tv[v];
+      deteos(c.fluid, c.with_prop, x.pv[0] + c.pref, x.pv[4], x.pv[5], x.pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      store_cell(d, c, op.dst, x);
+      return;
+    }
+    default:
+      return;
+  }
+}
+
+// ------------------------------------------------------------------ face fluxes
+// stencil cell l (0..37) of a face at left cell g: normal stride sn, transverse s1, s2
+__device__ __forceinline__ long long stencil_cell(int l, long long g, long long sn, long long s1, long long s2) {
+  if (l < 18) {
+    int a = l & 1, t1 = (l >> 1) % 3 - 1, t2 = l / 6 - 1;
+    return g + a * sn + t1 * s1 + t2 * s2;
+  }
+  if (l < 36) {
+    int m = (l - 18) % 9;
+    int a = (l < 27) ? -1 : 2;
+    int t1 = m % 3 - 1, t2 = m / 3 - 1;
+    return g + a * sn + t1 * s1 + t2 * s2;
+  }
+  return g + ((l == 36) ? -2 : 3) * sn;
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // flat face numbering per direction: block-major, then (k, j, i) of the left cell
+  int b = 0;
+  while (b + 1 < d.nblk && t >= d.blk[b + 1].face_off[DIR]) ++b;
+  const BlockGeom& B = d.blk[b];
+  long long loc = t - B.face_off[DIR];
+  int fi_, fj, fk;  // extents of the face set
+  if (DIR == 0) { fi_ = B.imax; fj = B.jmax - 1; fk = B.kmax - 1; }
+  else if (DIR == 1) { fi_ = B.imax - 1; fj = B.jmax; fk = B.kmax - 1; }
+  else { fi_ = B.imax - 1; fj = B.jmax - 1; fk = B.kmax; }
+  if (loc < 0 || loc >= (long long)fi_ * fj * fk) return;
+  int i = (int)(loc % fi_) + (DIR == 0 ? 1 : 2);
+  long long r = loc / fi_;
+  int j = (int)(r % fj) + (DIR == 1 ? 1 : 2);
+  int k = (int)(r / fj) + (DIR == 2 ? 1 : 2);
+  const long long n = d.ncell;
+  const long long si = 1, sj = B.ni, sk = (long long)B.ni * B.nj;
+  const long long g = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
+  long long sn, s1, s2;
+  if (DIR == 0) { sn = si; s1 = sj; s2 = sk; }
+  else if (DIR == 1) { sn = sj; s1 = sk; s2 = si; }
+  else { sn = sk; s1 = si; s2 = sj; }
+  const int fplane = (DIR == 0) ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
+  double nx[3];
+  face_vec(d, fplane, g, nx);
+  const int npv = c.npv;
+  FaceState L, R;
+  const long long gr = g + sn;
+  if (c.nmuscl > 0) {
+    double c9[NPVM], c10[NPVM];
+    for (int v = 0; v < npv; ++v) {
+      double x[38];
+#pragma unroll
+      for (int l = 0; l < 38; ++l) x[l] = d.pv[v * n + stencil_cell(l, g, sn, s1, s2)];
+      muscl_var<double>(c, x, L.pv[v], R.pv[v]);
+      c9[v] = x[8]; c10[v] = x[9];
+    }
+    muscl_clip<double>(c, c9, c10, L.pv, R.pv);
+    double dl_[NDV], dr_[NDV];
+    deteos_simple(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], dl_, &d.sc->snd2_fallbacks);
+    deteos_simple(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], dr_, &d.sc->snd2_fallbacks);
+    L.rho = dl_[0]; L.h = dl_[1]; L.c2 = dl_[5];
+    R.rho = dr_[0]; R.h = dr_[1]; R.c2 = dr_[5];
+  } else {
+    for (int v = 0; v < npv; ++v) { L.pv[v] = d.pv[v * n + g]; R.pv[v] = d.pv[v * n + gr]; }
+    L.rho = d.dv[g]; L.h = d.dv[n + g]; L.c2 = d.dv[5 * n + g];
+    R.rho = d.dv[gr]; R.h = d.dv[n + gr]; R.c2 = d.dv[5 * n + gr];
+  }
+  double sdst[18];
+  if (c.nscheme == 2 || c.nscheme == 3) {
+#pragma unroll
+    for (int l = 0; l < 18; ++l) sdst[l] = d.pv[stencil_cell(l, g, sn, s1, s2)];
+  }
+  double fx[NPVM];
+  inviscid_flux(c, nx, L, R, sdst, fx, &d.sc->snd2_fallbacks);
+  double* fi = d.fi + (long long)DIR * npv * n;
+  for (int v = 0; v < npv; ++v) fi[v * n + g] = fx[v];
+  if (c.iturb == -3) return;
+  // ---- viscous flux (vsflux_laminar / vsflux_turbulent)
+  const bool turb = (c.iturb == 0);
+  const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);   // faces normal to t1
+  const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);   // faces normal to t2
+  double ev[3], tvv[3];
+  for (int q = 0; q < 3; ++q) {
+    const double* P = d.gm + (ep + q) * n;
+    ev[q] = 0.25 * (P[g - s1] + P[g - s1 + sn] + P[g] + P[g + sn]);
+    const double* T = d.gm + (tp + q) * n;
+    tvv[q] = 0.25 * (T[g - s2] + T[g - s2 + sn] + T[g] + T[g + sn]);
+  }
+  double vol = 2.0 / (d.gm[GM_GRD * n + g] + d.gm[GM_GRD * n + gr]);
+  double tvl[3] = {0, 0, 0}, tvr[3] = {0, 0, 0};
+  for (int q = 0; q < c.ntv; ++q) { tvl[q] = d.tv[q * n + g]; tvr[q] = d.tv[q * n + gr]; }
+  double vis = 0.5 * (tvl[0] + tvr[0]);
+  double con = 0.5 * (tvl[1] + tvr[1]);
+  double emut = 0.0, tcon = 0.0;
+  if (turb) {
+    emut = 0.5 * (tvl[2] + tvr[2]);
+    tcon = 0.5 * (tvl[2] * d.dv[11 * n + g] + tvr[2] * d.dv[11 * n + gr]) / 0.9;
+  }
+  const int vars[6] = {1, 2, 3, 4, 7, 8};
+  double gx[6], gy[6], gz[6], cc[6];
+  const int nv = turb ? 6 : 4;
+  for (int q = 0; q < nv; ++q) {
+    const double* P = d.pv + vars[q] * n;
+    double x[18];
+#pragma unroll
+    for (int l = 0; l < 18; ++l) x[l] = P[stencil_cell(l, g, sn, s1, s2)];
+    double dn = x[9] - x[8];
+    double de = 0.0625 * (-x[0] - x[1] + x[4] + x[5] + 2.0 * (-x[6] - x[7] + x[10] + x[11]) - x[12] - x[13] + x[16] + x[17]);
+    double dt = 0.0625 * (-x[0] - x[1] + x[12] + x[13] + 2.0 * (-x[2] - x[3] + x[14] + x[15]) - x[4] - x[5] + x[16] + x[17]);
+    gx[q] = (dn * nx[0] + de * ev[0] + dt * tvv[0]) * vol;
+    gy[q] = (dn * nx[1] + de * ev[1] + dt * tvv[1]) * vol;
+    gz[q] = (dn * nx[2] + de * ev[2] + dt * tvv[2]) * vol;
+    cc[q] = 0.5 * (x[8] + x[9]);
+  }
+  const double c23 = 2.0 / 3.0;
+  double mu = turb ? (vis + emut) : vis;
+  double div = gx[0] + gy[1] + gz[2];
+  double txx = mu * (2.0 * gx[0] - c23 * div), tyy = mu * (2.0 * gy[1] - c23 * div), tzz = mu * (2.0 * gz[2] - c23 * div);
+  double txy = mu * (gy[0] + gx[1]), txz = mu * (gz[0] + gx[2]), tyz = mu * (gz[1] + gy[2]);
+  double kc = turb ? (con + tcon) : con;
+  double uc = cc[0], vc = cc[1], wc = cc[2];
+  double fv[NPVM];
+  fv[0] = 0.0;
+  fv[1] = txx * nx[0] + txy * nx[1] + txz * nx[2];
+  fv[2] = txy * nx[0] + tyy * nx[1] + tyz * nx[2];
+  fv[3] = txz * nx[0] + tyz * nx[1] + tzz * nx[2];
+  fv[4] = nx[0] * (uc * txx + vc * txy + wc * txz + kc * gx[3]) + nx[1] * (uc * txy + vc * tyy + wc * tyz + kc * gy[3]) +
+          nx[2] * (uc * txz + vc * tyz + wc * tzz + kc * gz[3]);
+  fv[5] = 0.0;
+  fv[6] = 0.0;
+  if (turb) {
+    double pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
+    double rho = 0.5 * (d.dv[g] + d.dv[gr]);
+    double ydns = 0.5 * (d.gm[(GM_GRD + 4) * n + g] + d.gm[(GM_GRD + 4) * n + gr]);
+    double kf = cc[4], of = cc[5];
+    double cdkw = fmax(1.712 * rho / of * pkw, 1.0e-10);
+    double term1 = sqrt(kf) / (0.09 * of * ydns);
+    double term2 = 500.0 * vis / rho / (of * ydns * ydns);
+    double term3 = (3.424 * rho * kf) / (cdkw * ydns * ydns);
+    double arg1 = fmin(fmax(term1, term2), term3);
+    double a2 = arg1 * arg1;
+    double bigf = tanh(a2 * a2);
+    double tdk = bigf * 0.85 + (1.0 - bigf) * 1.0;
+    double tdo = bigf * 0.5 + (1.0 - bigf) * 0.856;
+    fv[7] = (vis + emut * tdk) * (gx[4] * nx[0] + gy[4] * nx[1] + gz[4] * nx[2]);
+    fv[8] = (vis + emut * tdo) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
+  }
+  double* fvp = d.fv + (long long)DIR * npv * n;
+  for (int v = 0; v < npv; ++v) fvp[v * n + g] = fv[v];
+}
+
+// ------------------------------------------------------------------ residual + sources
+__global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= d.nint) return;
+  int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
+  const BlockGeom& B = d.blk[b];
+  long long g = interior_cell(B, t - B.int_off, i, j, k);
+  const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+  const int npv = c.npv;
+  const bool vis = c.iturb != -3;
+  const long long st[3] = {1, sj, sk};
+  double res[NPVM];
+  for (int v = 0; v < npv; ++v) {
+    double r = 0.0;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double* F = d.fi + ((long long)q * npv + v) * n;
+      if (q == 0) r = -(F[g] - F[g - st[q]]);
+      else r = r - (F[g] - F[g - st[q]]);
+      if (vis) {
+        const double* V = d.fv + ((long long)q * npv + v) * n;
+        r = r + (V[g] - V[g - st[q]]);
+      }
+    }
+    res[v] = r;
+  }
+  double pv2[NPVM], dv[NDV];
+  for (int v = 0; v < npv; ++v) pv2[v] = d.pv[v * n + g];
+  for (int v = 0; v < NDV; ++v) dv[v] = d.dv[v * n + g];
+  const double vol = d.gm[GM_GRD * n + g];
+  if (c.ncav) {
+    CavOut o = cavsource(c, pv2, dv, vol);
+    res[5] = res[5] + o.r_v - o.r_c;
+    for (int q = 0; q < 4; ++q) d.icav[q * n + g] = o.icav[q];
+    d.rcav[g] = o.r_c;
+    d.rcav[n + g] = o.r_v;
+  }
+  if (c.iturb == 0) {
+    // cell-centred gradients of u, v, w, k, omega (turbsource kwsst, :269-383)
+    const long long nbr[6] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk};
+    double fa[6][3];
+    for (int q = 0; q < 3; ++q) {
+      fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
+      fa[2][q] = d.gm[(GM_EX + q) * n + g - sj]; fa[3][q] = d.gm[(GM_EX + q) * n + g];
+      fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
+    }
+    const int gv[5] = {1, 2, 3, 7, 8};
+    double gr[5][3];
+    double ivol = 1.0 / vol;
+    for (int q = 0; q < 5; ++q) {
+      const double* P = d.pv + gv[q] * n;
+      double c0 = P[g];
+      double v1 = 0.5 * (P[nbr[0]] + c0), v2 = 0.5 * (P[nbr[1]] + c0), v3 = 0.5 * (P[nbr[2]] + c0);
+      double v4 = 0.5 * (P[nbr[3]] + c0), v5 = 0.5 * (P[nbr[4]] + c0), v6 = 0.5 * (P[nbr[5]] + c0);
+      for (int e = 0; e < 3; ++e)
+        gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
+    }
+    double tv[3];
+    for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
+    const double c23 = 2.0 / 3.0, c59 = 5.0 / 9.0;
+    double kk = pv2[7], oo = pv2[8];
+    double dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
+    double dvdx = gr[1][0], dvdy = gr[1][1], dvdz = gr[1][2];
+    double dwdx = gr[2][0], dwdy = gr[2][1], dwdz = gr[2][2];
+    double strain = 2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + sq(dudy + dvdx) + sq(dudz + dwdx) + sq(dvdz + dwdy);
+    double div = dudx + dvdy + dwdz;
+    double prod = tv[2] * (strain - c23 * div * div) - c23 * dv[0] * kk * div;
+    prod = fmin(prod, 0.9 * dv[0] * kk * oo);
+    d.ocut[g] = sqrt(strain - c23 * div * div);
+    double pkw = gr[3][0] * gr[4][0] + gr[3][1] * gr[4][1] + gr[3][2] * gr[4][2];
+    double y5 = d.gm[(GM_GRD + 4) * n + g];
+    double cdkw = fmax(1.712 * dv[0] / oo * pkw, 1.0e-10);
+    double term1 = sqrt(kk) / (0.09 * oo * y5);
+    double term2 = 500.0 * tv[0] / dv[0] / (oo * y5 * y5);
+    double term3 = (3.424 * dv[0] * kk) / (cdkw * y5 * y5);
+    double arg1 = fmin(fmax(term1, term2), term3);
+    double a2 = arg1 * arg1;
+    double bigf = tanh(a2 * a2);
+    double talpha = bigf * c59 + (1.0 - bigf) * 0.44;
+    double tbeta = bigf * 0.075 + (1.0 - bigf) * 0.0828;
+    double ki = 1.0 / kk, oi = 1.0 / oo, ei = 1.0 / tv[2];
+    double tl = sqrt(kk) / 9.0 / oo * 100.0;
+    double dest = dv[0] * pow(kk, 1.5) / tl;
+    res[7] = res[7] + (prod - dest) * vol;
+    res[8] = res[8] + (talpha * dv[0] * ei * prod - tbeta * dv[0] * oo * oo + 1.712 * (1.0 - bigf) * dv[0] * oi * pkw) * vol;
+    double dpdk = prod * ki;
+    double dpdo = -((prod + c23 * dv[0] * kk * div) * oi);
+    double it0 = dpdk - dest * ki, it1 = dpdo - dest * oi, it2 = 0.0;
+    double it3 = talpha * dv[0] * ei * dpdo + talpha * dv[0] * ei * prod * oi - 2.0 * tbeta * dv[0] * oo -
+                 1.712 * (1.0 - bigf) * dv[0] * oi * oi * pkw;
+    double tr = it0 + it3, de = it0 * it3 - it1 * it2;
+    double sd = sqrt(fmax(0.25 * tr * tr - de, 0.0));
+    double l1 = copysign(1.0, 0.5 * tr + sd), l2 = copysign(1.0, 0.5 * tr - sd);
+    double f1 = (1.0 - 0.5 * (1.0 - l1)) - 0.5 * (1.0 - l1);
+    double f2 = (1.0 - 0.5 * (1.0 - l2)) - 0.5 * (1.0 - l2);
+    d.itt[g] = it0 * f1; d.itt[n + g] = it1 * f1; d.itt[2 * n + g] = it2 * f2; d.itt[3 * n + g] = it3 * f2;
+  }
+  if (c.nsteady >= 1) {
+    double bb = (c.nsteady == 1) ? 1.0 : 0.75;
+    double fx[NPVM];
+    fx[0] = dv[0];
+    fx[1] = dv[0] * pv2[1]; fx[2] = dv[0] * pv2[2]; fx[3] = dv[0] * pv2[3];
+    fx[4] = dv[0] * (dv[1] + 0.5 * (pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3])) - (pv2[0] + c.pref);
+    for (int v = 5; v < npv; ++v) fx[v] = dv[0] * pv2[v];
+    for (int v = 0; v < npv; ++v) {
+      double q1 = d.qq[v * n + g], q2 = d.qq[(npv + v) * n + g];
+      double s = (double)c.nsteady * (bb * fx[v] - q1) + 0.5 * ((double)c.nsteady - 1.0) * q2;
+      res[v] = res[v] - s * vol / c.dt_phy;
+    }
+  }
+  for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
+}
+
+// ------------------------------------------------------------------ LU-SGS sweeps
+__device__ __forceinline__ void load_nbr(const DevPtr& d, const Par& c, long long g, double* pv, double* dv,
+                                         double* tv, double& vol) {
+  const long long n = d.ncell;
+  for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
+  for (int v = 0; v < 12; ++v) dv[v] = d.dv[v * n + g];
+  tv[0] = tv[1] = tv[2] = 0.0;
+  for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
+  vol = d.gm[GM_GRD * n + g];
+}
+
+template <bool FWD>
+__global__ void __launch_bounds__(128) k_sweep(DevPtr d, Par c, const int* __restrict__ cells, long long p0, long long p1) {
+  long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= p1) return;
+  const long long g = cells[t];
+  const int b = find_block_cell(d.blk, d.nblk, g);
+  const BlockGeom& B = d.blk[b];
+  const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+  long long rel = g - B.off;
+  const int i = (int)(rel % B.ni) - 1;
+  const int j = (int)((rel / B.ni) % B.nj) - 1;
+  const int k = (int)(rel / sk) - 1;
+  const int npv = c.npv;
+  double acc[NPVM];
+  if (FWD) for (int v = 0; v < npv; ++v) acc[v] = d.res[v * n + g];
+  else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * n + g];
+  const long long strides[3] = {1, sj, sk};
+  const int pos[3] = {i, j, k};
+  const int lim[3] = {B.imax, B.jmax, B.kmax};
+  const int plane[3] = {GM_CX, GM_EX, GM_TX};
+#pragma unroll 1
+  for (int q = 0; q < 3; ++q) {
+    // forward: lower neighbour across face (g - s); backward: upper neighbour across face (g)
+    const bool interior = FWD ? (pos[q] - 1 >= 2) : (pos[q] + 1 <= lim[q]);
+    if (!interior) continue;  // dq is zero outside the block
+    const long long nb = FWD ? g - strides[q] : g + strides[q];
+    const long long fidx = FWD ? nb : g;
+    double nx[3];
+    face_vec(d, plane[q], fidx, nx);
+    double pv[NPVM], dv[12], tv[3], vol, dq[NPVM];
+    load_nbr(d, c, nb, pv, dv, tv, vol);
+    for (int v = 0; v < npv; ++v) dq[v] = d.dqs[v * n + nb];
+    if (FWD) jac_apply(c, nx, vol, pv, dv, tv, 1.0, dq, acc, 1.0);
+    else jac_apply(c, nx, vol, pv, dv, tv, -1.0, dq, acc, -1.0);
+  }
+  if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * n + g] = acc[v];
+  // diagonal block
+  double pv[NPVM], dv[NDV], tv[3] = {0.0, 0.0, 0.0};
+  for (int v = 0; v < npv; ++v) pv[v] = d.pv[v * n + g];
+  for (int v = 0; v < 14; ++v) dv[v] = d.dv[v * n + g];
+  for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
+  double fc[18];
+  for (int q = 0; q < 3; ++q) {
+    fc[q] = d.gm[(GM_CX + q) * n + g - 1]; fc[3 + q] = d.gm[(GM_CX + q) * n + g];
+    fc[6 + q] = d.gm[(GM_EX + q) * n + g - sj]; fc[9 + q] = d.gm[(GM_EX + q) * n + g];
+    fc[12 + q] = d.gm[(GM_TX + q) * n + g - sk]; fc[15 + q] = d.gm[(GM_TX + q) * n + g];
+  }
+  double ic[4] = {0, 0, 0, 0}, it[4] = {0, 0, 0, 0};
+  if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
+  if (c.iturb == 0) for (int q = 0; q < 4; ++q) it[q] = d.itt[q * n + g];
+  Diag D;
+  diag_prepare(c, pv, dv, tv, fc, d.gm[GM_GRD * n + g], d.dt[g], ic, it, D);
+  double x[NPVM];
+  diag_solve(c, D, pv, dv, acc, x);
+  for (int v = 0; v < npv; ++v) d.dqs[v * n + g] = x[v];
+}
+
+// ------------------------------------------------------------------ update + residual
+__global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int npv = c.npv;
+  double sq_[NPVM];
+  for (int v = 0; v < NPVM; ++v) sq_[v] = 0.0;
+  double dpmax = -1.0;
+  long long dpidx = -1;
+  int bad = 0;
+  if (t < d.nint) {
+    int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
+    long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
+    const long long n = d.ncell;
+    double old[NPVM], p[NPVM];
+    for (int v = 0; v < npv; ++v) { old[v] = d.pv[v * n + g]; p[v] = old[v] + d.dqs[v * n + g]; }
+    p[0] = fmax(-c.pref + 1.0e1, p[0]);
+    p[5] = fmin(1.0, fmax(0.0, p[5]));
+    p[6] = fmin(1.0, fmax(0.0, p[6]));
+    if (c.iturb == 0) {
+      p[7] = fmax(p[7], 1.0e-16);
+      p[8] = fmax(fmax(p[8], 1.0e-16), d.ocut[g]);
+    }
+    double dv[NDV], tv[3] = {0.0, 0.0, 0.0};
+    for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
+    deteos(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
+    for (int v = 0; v < npv; ++v) {
+      d.pv[v * n + g] = p[v];
+      double df = fabs(old[v] - p[v]);
+      sq_[v] = df * df;
+      if (!isfinite(p[v])) bad = 1;
+    }
+    for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
+    for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
+    dpmax = fabs(old[0] - p[0]);
+    dpidx = t;
+  }
+  if (bad) atomicExch(&d.sc->nonfinite, 1);
+  // per-CTA partial sums (deterministic order: warp shuffles then warps in order)
+  __shared__ double sh[4][NPVM + 2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int v = 0; v < npv; ++v) {
+    double s = sq_[v];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[w][v] = s;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double om = __shfl_down_sync(0xffffffffu, dpmax, o);
+    long long oi = __shfl_down_sync(0xffffffffu, dpidx, o);
+    if (om > dpmax || (om == dpmax && oi >= 0 && (dpidx < 0 || oi < dpidx))) { dpmax = om; dpidx = oi; }
+  }
+  if (lane == 0) { sh[w][NPVM] = dpmax; sh[w][NPVM + 1] = __longlong_as_double(dpidx); }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double* out = d.partial + (long long)blockIdx.x * (NPVM + 2);
+    double m = -1.0;
+    long long mi = -1;
+    for (int v = 0; v < npv; ++v) {
+      double s = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += sh[q][v];
+      out[v] = s;
+    }
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      double om = sh[q][NPVM];
+      long long oi = __double_as_longlong(sh[q][NPVM + 1]);
+      if (om > m || (om == m && oi >= 0 && (mi < 0 || oi < mi))) { m = om; mi = oi; }
+    }
+    out[NPVM] = m;
+    out[NPVM + 1] = __longlong_as_double(mi);
+  }
+}
+
+__global__ void k_eddy(DevPtr d, Par c) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= d.nint) return;
+  int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
+  const BlockGeom& B = d.blk[b];
+  long long g = interior_cell(B, t - B.int_off, i, j, k);
+  const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+  const long long nbr[6] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk};
+  double fa[6][3];
+  for (int q = 0; q < 3; ++q) {
+    fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
+    fa[2][q] = d.gm[(GM_EX + q) * n + g - sj]; fa[3][q] = d.gm[(GM_EX + q) * n + g];
+    fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
+  }
+  double vol = d.gm[GM_GRD * n + g], ivol = 1.0 / vol;
+  double gr[3][3];
+  for (int q = 0; q < 3; ++q) {
+    const double* P = d.pv + (1 + q) * n;
+    double c0 = P[g];
+    double v1 = 0.5 * (P[nbr[0]] + c0), v2 = 0.5 * (P[nbr[1]] + c0), v3 = 0.5 * (P[nbr[2]] + c0);
+    double v4 = 0.5 * (P[nbr[3]] + c0), v5 = 0.5 * (P[nbr[4]] + c0), v6 = 0.5 * (P[nbr[5]] + c0);
+    for (int e = 0; e < 3; ++e)
+      gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
+  }
+  double kk = d.pv[7 * n + g], oo = d.pv[8 * n + g], rho = d.dv[g], mu = d.tv[g];
+  double y5 = d.gm[(GM_GRD + 4) * n + g];
+  double term1 = sqrt(kk) / (0.09 * oo * y5);
+  double term2 = 500.0 * mu / rho / (oo * y5 * y5);
+  double arg2 = fmax(2.0 * term1, term2);
+  double bigf2 = tanh(arg2 * arg2);
+  double sij = gr[0][0] * gr[0][0] + gr[1][1] * gr[1][1] + gr[2][2] * gr[2][2] +
+               0.5 * (sq(gr[0][1] + gr[1][0]) + sq(gr[0][2] + gr[2][0]) + sq(gr[1][2] + gr[2][1]));
+  double sss = sqrt(2.0 * sij);
+  d.tv[2 * n + g] = 0.31 * rho * kk / fmax(0.31 * oo, sss * bigf2);
+}
+
+__global__ void k_finish(DevPtr d, Par c, int nparts) {
+  __shared__ double s[NPVM];
+  const int npv = c.npv;
+  if (threadIdx.x < npv) {
+    double acc = 0.0;
+    for (int q = 0; q < nparts; ++q) acc += d.partial[(long long)q * (NPVM + 2) + threadIdx.x];
+    s[threadIdx.x] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Scalars* sc = d.sc;
+    for (int v = 0; v < npv; ++v) sc->res[v] = sqrt(s[v]);
+    double m = -1.0;
+    long long mi = -1;
+    for (int q = 0; q < nparts; ++q) {
+      double om = d.partial[(long long)q * (NPVM + 2) + NPVM];
+      long long oi = __double_as_longlong(d.partial[(long long)q * (NPVM + 2) + NPVM + 1]);
+      if (om > m || (om == m && oi >= 0 && (mi < 0 || oi < mi))) { m = om; mi = oi; }
+    }
+    sc->resmax = m;
+    sc->resmax_cell = (m > 1.0e-12) ? mi : -1;
+    sc->time_acc += __longlong_as_double((long long)sc->dtmin_bits);
+    sc->dtmin_bits = (unsigned long long)__double_as_longlong(1.0e10);
+  }
+}
+
+// ------------------------------------------------------------------ layout conversion
+// Fortran AoS a(nv, -1:imax+3, ...) of one block <-> SoA planes
+__global__ void k_aos_to_soa(const double* __restrict__ a, int nv, long long ncb, double* __restrict__ soa,
+                             long long ncell, long long off) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= ncb) return;
+  for (int v = 0; v < nv; ++v) soa[v * ncell + off + q] = a[q * nv + v];
+}
+__global__ void k_soa_to_aos(const double* __restrict__ soa, int nv, long long ncb, double* __restrict__ a,
+                             long long ncell, long long off) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= ncb) return;
+  for (int v = 0; v < nv; ++v) a[q * nv + v] = soa[v * ncell + off + q];
+}
+// interior AoS a(nv, 2:imax, 2:jmax, 2:kmax) of one block <-> SoA planes
+__global__ void k_interior_io(double* __restrict__ a, int nv, BlockGeom B, double* __restrict__ soa, long long ncell,
+                              int to_soa) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  if (q >= nint) return;
+  int i, j, k;
+  long long g = interior_cell(B, q, i, j, k);
+  for (int v = 0; v < nv; ++v) {
+    if (to_soa) soa[v * ncell + g] = a[q * nv + v];
+    else a[q * nv + v] = soa[v * ncell + g];
+  }
+}
+
+}  // namespace cfd
+
+// =====================================================================================
+//                                     C ABI
+// =====================================================================================
+using namespace cfd;
+
+struct cfd3d_handle {
+  Engine E;
+  double* staging = nullptr;
+  size_t staging_bytes = 0;
+};
+
+namespace {
+
+inline unsigned nblk_of(long long n, int T) { return (unsigned)((n + T - 1) / T); }
+
+int ensure_staging(cfd3d_handle* h, size_t bytes) {
+  Engine& E = h->E;
+  if (h->staging_bytes >= bytes) return CFD3D_OK;
+  cudaFree(h->staging);
+  h->staging = nullptr;
+  h->staging_bytes = 0;
+  CFD_CUDA(cudaMalloc(&h->staging, bytes));
+  h->staging_bytes = bytes;
+  return CFD3D_OK;
+}
+
+// the launch sequence of one iteration (captured into the graph); `mark` (optional)
+// records an event after each stage for the stage profile
+void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
+  const DevPtr& d = E.d;
+  const Par& c = E.par;
+  cudaStream_t s = E.st;
+  const int T = 128;
+  int n = 0;
+  auto stage = [&](int q) { if (mark) cudaEventRecord(mark[q], s); };
+  stage(0);
+  if (full) { k_timestep<<<nblk_of(E.nint, 256), 256, 0, s>>>(d, c); ++n; }
+  stage(1);
+  for (int p = 0; p < 3; ++p)
+    if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
+  stage(2);
+  k_face_flux<0><<<nblk_of(E.nface[0], T), T, 0, s>>>(d, c);
+  k_face_flux<1><<<nblk_of(E.nface[1], T), T, 0, s>>>(d, c);
+  k_face_flux<2><<<nblk_of(E.nface[2], T), T, 0, s>>>(d, c);
+  stage(3);
+  k_rhs<<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+  stage(4);
+  n += 4;
+  if (!full) { E.launches_per_iter = n; return; }
+  const int np = (int)E.plane_off.size() - 1;
+  for (int q = 0; q < np; ++q) {
+    long long a = E.plane_off[q], b = E.plane_off[q + 1];
+    if (b > a) { k_sweep<true><<<nblk_of(b - a, T), T, 0, s>>>(d, c, E.d_planes, a, b); ++n; }
+  }
+  stage(5);
+  for (int q = np - 1; q >= 0; --q) {
+    long long a = E.plane_off[q], b = E.plane_off[q + 1];
+    if (b > a) { k_sweep<false><<<nblk_of(b - a, T), T, 0, s>>>(d, c, E.d_planes, a, b); ++n; }
+  }
+  stage(6);
+  k_update<<<E.red_grid, T, 0, s>>>(d, c);
+  ++n;
+  stage(7);
+  if (c.iturb == 0) { k_eddy<<<nblk_of(E.nint, T), T, 0, s>>>(d, c); ++n; }
+  k_finish<<<1, 32, 0, s>>>(d, c, E.red_grid);
+  ++n;
+  stage(8);
+  E.launches_per_iter = n;
+}
+
+int build_graph(Engine& E) {
+  if (E.graph_ready) return CFD3D_OK;
+  cudaGraph_t g;
+  CFD_CUDA(cudaStreamBeginCapture(E.st, cudaStreamCaptureModeThreadLocal));
+  launch_iteration(E, true);
+  CFD_CUDA(cudaStreamEndCapture(E.st, &g));
+  CFD_CUDA(cudaGraphInstantiate(&E.graph, g, 0));
+  cudaGraphDestroy(g);
+  E.graph_ready = 1;
+  return CFD3D_OK;
+}
+
+int read_scalars(Engine& E, Scalars& s) {
+  CFD_CUDA(cudaMemcpyAsync(&s, E.d.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, E.st));
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  return CFD3D_OK;
+}
+
+bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
+  std::memset(&c, 0, sizeof(c));
+  if (in->timemethod != 3) { err = "timemethod must be 3 (LU-SGS)"; return false; }
+  if (in->iturb == -3) { c.npv = 7; c.ntv = 0; }
+  else if (in->iturb == -2) { c.npv = 7; c.ntv = 2; }
+  else if (in->iturb == 0) { c.npv = 9; c.ntv = 3; }
+  else { err = "iturb must be -3, -2 or 0"; return false; }
+  if (in->iturb == 0 && in->ides != 0) { err = "only ides = 0 is supported"; return false; }
+  if (in->fluid != 1 && in->fluid != 2) { err = "fluid must be 1 (stiffened) or 2 (IAPWS-97)"; return false; }
+  if (in->ngas != 1) { err = "ngas must be 1 (ideal gas)"; return false; }
+  if (in->nscheme < 1 || in->nscheme > 4 || in->nmuscl < 0 || in->nmuscl > 2 || in->nlim < 0 || in->nlim > 10) {
+    err = "nscheme/nmuscl/nlim out of range"; return false;
+  }
+  if (in->ncav < 0 || in->ncav > 5) { err = "ncav out of range"; return false; }
+  if (in->local < -1 || in->local > 1) { err = "local out of range"; return false; }
+  if (in->prec < 0 || in->prec > 2) { err = "prec out of range"; return false; }
+  if (in->nsteady >= 1 && !(in->dt_phy > 0.0)) { err = "dual time stepping needs dt_phy > 0"; return false; }
+  c.nqq = in->nsteady >= 1 ? 2 : 0;
+  c.ngrd = (in->iturb == 0) ? 5 : 4;
+  c.nsteady = in->nsteady; c.iturb = in->iturb; c.nscheme = in->nscheme; c.nmuscl = in->nmuscl; c.nlim = in->nlim;
+  c.local = in->local; c.prec = in->prec; c.fluid = in->fluid; c.ncav = in->ncav; c.fix_cav_clamp = in->fix_cav_clamp;
+  c.with_prop = (in->iturb != -3);
+  c.dt_phy = in->dt_phy; c.cfl = in->cfl; c.c_v = in->c_v; c.c_c = in->c_c; c.pref = in->pref; c.uref = in->uref;
+  const double pi = std::atan(1.0) * 4.0;
+  c.str = in->l_character / pi / in->dt_phy;
+  c.l_chord = in->l_chord;
+  double aoa = in->aoa * pi / 180.0, aos = in->aos * pi / 180.0;
+  c.uref_vec[0] = in->uref * std::cos(aos) * std::cos(aoa);
+  c.uref_vec[1] = in->uref * std::cos(aos) * std::sin(aoa);
+  c.uref_vec[2] = in->uref * std::sin(aos);
+  c.tref = in->tref; c.y1ref = in->y1ref; c.y2ref = in->y2ref;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cfd3d_last_error(const cfd3d_handle* h) { return h ? h->E.err.c_str() : "null handle"; }
+
+int cfd3d_eos_eval(int fluid, int ngas, int with_prop, int64_t n, const double* p, const double* t, const double* y1,
+                   const double* y2, double* dv, double* tv) {
+  if (n <= 0 || !p || !t || !y1 || !y2 || !dv || (fluid != 1 && fluid != 2) || ngas != 1) return CFD3D_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CFD3D_ERR_NODEVICE;
+  double *dp = nullptr, *dt = nullptr, *dy1 = nullptr, *dy2 = nullptr, *ddv = nullptr, *dtv = nullptr;
+  unsigned long long* fb = nullptr;
+  size_t b = (size_t)n * 8;
+  int rc = CFD3D_OK;
+  if (cudaMalloc(&dp, b) || cudaMalloc(&dt, b) || cudaMalloc(&dy1, b) || cudaMalloc(&dy2, b) ||
+      cudaMalloc(&ddv, b * NDV) || cudaMalloc(&dtv, b * 2) || cudaMalloc(&fb, 8)) {
+    rc = CFD3D_ERR_NOMEM;
+  } else {
+    cudaMemcpy(dp, p, b, cudaMemcpyHostToDevice);
+    cudaMemcpy(dt, t, b, cudaMemcpyHostToDevice);
+    cudaMemcpy(dy1, y1, b, cudaMemcpyHostToDevice);
+    cudaMemcpy(dy2, y2, b, cudaMemcpyHostToDevice);
+    cudaMemset(fb, 0, 8);
+    k_eos_points<<<(unsigned)((n + 127) / 128), 128>>>(fluid, with_prop, n, dp, dt, dy1, dy2, ddv, dtv, fb);
+    if (cudaMemcpy(dv, ddv, b * NDV, cudaMemcpyDeviceToHost) != cudaSuccess) rc = CFD3D_ERR_CUDA;
+    if (tv && with_prop && cudaMemcpy(tv, dtv, b * 2, cudaMemcpyDeviceToHost) != cudaSuccess) rc = CFD3D_ERR_CUDA;
+  }
+  cudaFree(dp); cudaFree(dt); cudaFree(dy1); cudaFree(dy2); cudaFree(ddv); cudaFree(dtv); cudaFree(fb);
+  return rc;
+}
+
+int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* blocks, cfd3d_handle** out) {
+  if (!out) return CFD3D_ERR_ARG;
+  *out = nullptr;
+  cfd3d_handle* h = new (std::nothrow) cfd3d_handle();
+  if (!h) return CFD3D_ERR_NOMEM;
+  *out = h;
+  Engine& E = h->E;
+  if (!cfg || nblocks < 1 || nblocks > MAXBLK || !blocks) { E.err = "bad arguments"; return CFD3D_ERR_ARG; }
+  E.cfg = *cfg;
+  if (!make_par(cfg, E.par, E.err)) return CFD3D_ERR_ARG;
+  for (int b = 0; b < nblocks; ++b) {
+    const cfd3d_block_desc& d = blocks[b];
+    for (int q = 0; q < d.nbc; ++q) {
+      const int* p = d.bc[q].pnts;
+      int nmax[3] = {d.imax, d.jmax, d.kmax}, faces = 0;
+      for (int a = 0; a < 3; ++a)
+        if (p[a] == p[3 + a] && (p[a] == 1 || p[a] == nmax[a])) ++faces;
+      if (faces != 1) { E.err = "bc patch is not a block face"; return CFD3D_ERR_DESCRIPTOR; }
+    }
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { E.err = "no CUDA device"; return CFD3D_ERR_NODEVICE; }
+  // block layout
+  long long off = 0, ioff = 0, foff[3] = {0, 0, 0};
+  for (int b = 0; b < nblocks; ++b) {
+    const cfd3d_block_desc& d = blocks[b];
+    if (d.imax < 4 || d.jmax < 4 || d.kmax < 4 || !d.xyz) { E.err = "block too small or no coordinates"; return CFD3D_ERR_DESCRIPTOR; }
+    BlockGeom G{};
+    G.imax = d.imax; G.jmax = d.jmax; G.kmax = d.kmax;
+    G.ni = d.imax + 5; G.nj = d.jmax + 5; G.nk = d.kmax + 5;
+    G.off = off; G.int_off = ioff;
+    for (int q = 0; q < 3; ++q) G.face_off[q] = foff[q];
+    off += (long long)G.ni * G.nj * G.nk;
+    ioff += (long long)(d.imax - 1) * (d.jmax - 1) * (d.kmax - 1);
+    foff[0] += (long long)d.imax * (d.jmax - 1) * (d.kmax - 1);
+    foff[1] += (long long)(d.imax - 1) * d.jmax * (d.kmax - 1);
+    foff[2] += (long long)(d.imax - 1) * (d.jmax - 1) * d.kmax;
+    E.blk.push_back(G);
+  }
+  if (off >= (1ll << 31)) { E.err = "case too large for 32-bit cell indices"; return CFD3D_ERR_ARG; }
+  E.ncell = off; E.nint = ioff;
+  for (int q = 0; q < 3; ++q) E.nface[q] = foff[q];
+  CFD_CUDA(cudaStreamCreateWithFlags(&E.st, cudaStreamNonBlocking));
+  // device buffers
+  const Par& c = E.par;
+  const long long n = E.ncell;
+  auto alloc = [&](double*& p, long long planes) -> bool {
+    if (planes <= 0) { p = nullptr; return true; }
+    if (cudaMalloc(&p, (size_t)planes * n * 8) != cudaSuccess) return false;
+    cudaMemset(p, 0, (size_t)planes * n * 8);
+    return true;
+  };
+  bool ok = alloc(E.d.pv, c.npv) && alloc(E.d.dv, NDV) && alloc(E.d.tv, std::max(c.ntv, 1)) &&
+            alloc(E.d.gm, GM_GRD + c.ngrd) && alloc(E.d.res, c.npv) && alloc(E.d.icav, 4) && alloc(E.d.itt, 4) &&
+            alloc(E.d.ocut, 1) && alloc(E.d.dt, 1) && alloc(E.d.rcav, 2) && alloc(E.d.qq, std::max(2 * c.npv * (c.nqq ? 1 : 0), 1)) &&
+            alloc(E.d.dqs, c.npv) && alloc(E.d.dcv, c.npv) && alloc(E.d.fi, 3 * c.npv) &&
+            alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
+  if (!ok) { E.err = "device allocation failed"; return CFD3D_ERR_NOMEM; }
+  E.d.ncell = n;
+  E.d.nint = E.nint;
+  E.d.nblk = nblocks;
+  BlockGeom* dblk = nullptr;
+  CFD_CUDA(cudaMalloc(&dblk, sizeof(BlockGeom) * nblocks));
+  CFD_CUDA(cudaMemcpy(dblk, E.blk.data(), sizeof(BlockGeom) * nblocks, cudaMemcpyHostToDevice));
+  E.d.blk = dblk;
+  CFD_CUDA(cudaMalloc(&E.d.sc, sizeof(Scalars)));
+  Scalars s0{};
+  s0.time_acc = 0.0;
+  double big = 1.0e10;
+  std::memcpy(&s0.dtmin_bits, &big, 8);
+  CFD_CUDA(cudaMemcpy(E.d.sc, &s0, sizeof(Scalars), cudaMemcpyHostToDevice));
+  E.red_grid = (int)nblk_of(E.nint, 128);
+  CFD_CUDA(cudaMalloc(&E.d.partial, (size_t)E.red_grid * (NPVM + 2) * 8));
+  // reference state: deteos at (pref, tref, y1ref, y2ref), then config%setref
+  {
+    double hp[4] = {cfg->pref, cfg->tref, cfg->y1ref, cfg->y2ref};
+    double dvr[NDV], tvr[2] = {0.0, 0.0};
+    int rc = cfd3d_eos_eval(cfg->fluid, cfg->ngas, c.with_prop, 1, &hp[0], &hp[1], &hp[2], &hp[3], dvr, tvr);
+    if (rc != CFD3D_OK) { E.err = "reference-state EOS failed"; return rc; }
+    E.par.rhoref = dvr[0];
+    if (c.iturb == 0) {
+      E.par.oref = 10.0 * cfg->uref / cfg->l_domain;
+      E.par.emutref = std::pow(10.0, -5) * tvr[0];
+      E.par.kref = E.par.emutref / E.par.rhoref * E.par.oref;
+      if (cfg->kinf > 0) E.par.kref = cfg->kinf;
+      if (cfg->oinf > 0) E.par.oref = cfg->oinf;
+    }
+  }
+  if (!setup_geometry(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
+  if (!setup_ghost_program(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
+  setup_planes(E);
+  CFD_CUDA(cudaDeviceSynchronize());
+  return CFD3D_OK;
+}
+
+void cfd3d_destroy(cfd3d_handle* h) {
+  if (!h) return;
+  Engine& E = h->E;
+  if (E.graph) cudaGraphExecDestroy(E.graph);
+  double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
+                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
+  for (double* p : bufs) cudaFree(p);
+  cudaFree((void*)E.d.blk);
+  cudaFree(E.d.sc);
+  for (int p = 0; p < 3; ++p) cudaFree(E.d_ops[p]);
+  cudaFree(E.d_planes);
+  if (E.st) cudaStreamDestroy(E.st);
+  delete h;
+}
+
+int cfd3d_sizes(const cfd3d_handle* h, int* npv, int* ndv, int* ntv, int* nqq, int* ngrd) {
+  if (!h) return CFD3D_ERR_ARG;
+  const Par& c = h->E.par;
+  if (npv) *npv = c.npv;
+  if (ndv) *ndv = NDV;
+  if (ntv) *ntv = c.ntv;
+  if (nqq) *nqq = c.nqq;
+  if (ngrd) *ngrd = c.ngrd;
+  return CFD3D_OK;
+}
+
+int cfd3d_initialize(cfd3d_handle* h, int block, const double* pv_interior) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
+  const BlockGeom& B = E.blk[block];
+  const Par& c = E.par;
+  long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  std::vector<double> host;
+  const double* src = pv_interior;
+  if (!src) {
+    host.resize((size_t)nint * c.npv);
+    for (long long q = 0; q < nint; ++q) {
+      double* p = &host[(size_t)q * c.npv];
+      p[0] = 0.0; p[1] = c.uref_vec[0]; p[2] = c.uref_vec[1]; p[3] = c.uref_vec[2];
+      p[4] = c.tref; p[5] = c.y1ref; p[6] = c.y2ref;
+      if (c.npv > 7) { p[7] = c.kref; p[8] = c.oref; }
+    }
+    src = host.data();
+  }
+  int rc = ensure_staging(h, (size_t)nint * c.npv * 8);
+  if (rc) return rc;
+  CFD_CUDA(cudaMemcpyAsync(h->staging, src, (size_t)nint * c.npv * 8, cudaMemcpyHostToDevice, E.st));
+  k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, c.npv, B, E.d.pv, E.ncell, 1);
+  k_init<<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block);
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  // reset the solution-time accumulator of the local time step
+  Scalars s;
+  if ((rc = read_scalars(E, s))) return rc;
+  s.time_acc = 0.0;
+  CFD_CUDA(cudaMemcpy(E.d.sc, &s, sizeof(Scalars), cudaMemcpyHostToDevice));
+  return CFD3D_OK;
+}
+
+int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const double* dv, const double* tv, const double* qq) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
+  const BlockGeom& B = E.blk[block];
+  const Par& c = E.par;
+  long long ncb = (long long)B.ni * B.nj * B.nk;
+  long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  int rc = ensure_staging(h, (size_t)ncb * NDV * 8);
+  if (rc) return rc;
+  struct { const double* a; int nv; double* dst; } items[3] = {{pv, c.npv, E.d.pv}, {dv, NDV, E.d.dv}, {tv, c.ntv, E.d.tv}};
+  for (auto& it : items) {
+    if (!it.a || it.nv == 0) continue;
+    CFD_CUDA(cudaMemcpyAsync(h->staging, it.a, (size_t)ncb * it.nv * 8, cudaMemcpyHostToDevice, E.st));
+    k_aos_to_soa<<<nblk_of(ncb, 256), 256, 0, E.st>>>(h->staging, it.nv, ncb, it.dst, E.ncell, B.off);
+  }
+  if (qq && c.nqq) {
+    CFD_CUDA(cudaMemcpyAsync(h->staging, qq, (size_t)nint * 2 * c.npv * 8, cudaMemcpyHostToDevice, E.st));
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, 2 * c.npv, B, E.d.qq, E.ncell, 1);
+  }
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  return CFD3D_OK;
+}
+
+int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, double* tv, double* qq, double* rcav) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
+  const BlockGeom& B = E.blk[block];
+  const Par& c = E.par;
+  long long ncb = (long long)B.ni * B.nj * B.nk;
+  long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  int rc = ensure_staging(h, (size_t)ncb * NDV * 8);
+  if (rc) return rc;
+  struct { double* a; int nv; double* src; } items[3] = {{pv, c.npv, E.d.pv}, {dv, NDV, E.d.dv}, {tv, c.ntv, E.d.tv}};
+  for (auto& it : items) {
+    if (!it.a || it.nv == 0) continue;
+    k_soa_to_aos<<<nblk_of(ncb, 256), 256, 0, E.st>>>(it.src, it.nv, ncb, h->staging, E.ncell, B.off);
+    CFD_CUDA(cudaMemcpyAsync(it.a, h->staging, (size_t)ncb * it.nv * 8, cudaMemcpyDeviceToHost, E.st));
+    CFD_CUDA(cudaStreamSynchronize(E.st));
+  }
+  if (qq && c.nqq) {
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, 2 * c.npv, B, E.d.qq, E.ncell, 0);
+    CFD_CUDA(cudaMemcpyAsync(qq, h->staging, (size_t)nint * 2 * c.npv * 8, cudaMemcpyDeviceToHost, E.st));
+    CFD_CUDA(cudaStreamSynchronize(E.st));
+  }
+  if (rcav) {
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, 2, B, E.d.rcav, E.ncell, 0);
+    CFD_CUDA(cudaMemcpyAsync(rcav, h->staging, (size_t)nint * 2 * 8, cudaMemcpyDeviceToHost, E.st));
+    CFD_CUDA(cudaStreamSynchronize(E.st));
+  }
+  return CFD3D_OK;
+}
+
+static int finish_iteration(cfd3d_handle* h, int nt_phy, double timeprev, double* time_out, double* res_l2, int* loc) {
+  Engine& E = h->E;
+  Scalars s;
+  int rc = read_scalars(E, s);
+  if (rc) return rc;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { E.err = cudaGetErrorString(e); return CFD3D_ERR_CUDA; }
+  double t = (E.par.nsteady == 0) ? s.time_acc + timeprev : E.par.dt_phy * (double)nt_phy;
+  if (time_out) *time_out = t;
+  if (res_l2) for (int v = 0; v < E.par.npv; ++v) res_l2[v] = s.res[v];
+  if (loc) {
+    loc[0] = -1; loc[1] = loc[2] = loc[3] = 0;
+    if (s.resmax_cell >= 0) {
+      long long q = s.resmax_cell;
+      int b = 0;
+      while (b + 1 < (int)E.blk.size() && q >= E.blk[b + 1].int_off) ++b;
+      const BlockGeom& B = E.blk[b];
+      long long l = q - B.int_off;
+      int ni = B.imax - 1, nj = B.jmax - 1;
+      loc[0] = b; loc[1] = (int)(l % ni) + 2; loc[2] = (int)((l / ni) % nj) + 2; loc[3] = (int)(l / ((long long)ni * nj)) + 2;
+    }
+  }
+  if (s.nonfinite) {
+    E.err = "non-finite value in the updated state";
+    int zero = 0;
+    cudaMemcpy(&E.d.sc->nonfinite, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    return CFD3D_ERR_NONFINITE;
+  }
+  return CFD3D_OK;
+}
+
+int cfd3d_iterate(cfd3d_handle* h, int nt_phy, int nt, double timeprev, double* time_out, double* res_l2, int* loc) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  (void)nt;
+  int rc = build_graph(E);
+  if (rc) return rc;
+  CFD_CUDA(cudaGraphLaunch(E.graph, E.st));
+  return finish_iteration(h, nt_phy, timeprev, time_out, res_l2, loc);
+}
+
+int cfd3d_iterate_n(cfd3d_handle* h, int niter, int nt_phy, int nt0, double timeprev, double* time_out, double* res_l2) {
+  if (!h || niter < 1) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  (void)nt0;
+  int rc = build_graph(E);
+  if (rc) return rc;
+  for (int q = 0; q < niter; ++q) CFD_CUDA(cudaGraphLaunch(E.graph, E.st));
+  return finish_iteration(h, nt_phy, timeprev, time_out, res_l2, nullptr);
+}
+
+int cfd3d_unsteady_shift(cfd3d_handle* h) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (!E.par.nqq) return CFD3D_OK;
+  k_unsteady_shift<<<nblk_of(E.nint, 128), 128, 0, E.st>>>(E.d, E.par);
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  return CFD3D_OK;
+}
+
+int cfd3d_residual(cfd3d_handle* h, int block, double* res, double* icav, double* itt, double* omega_cut) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
+  launch_iteration(E, false);
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  const BlockGeom& B = E.blk[block];
+  long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  int rc = ensure_staging(h, (size_t)nint * 9 * 8);
+  if (rc) return rc;
+  struct { double* a; int nv; double* src; } items[4] = {{res, E.par.npv, E.d.res}, {icav, 4, E.d.icav}, {itt, 4, E.d.itt}, {omega_cut, 1, E.d.ocut}};
+  for (auto& it : items) {
+    if (!it.a) continue;
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, it.nv, B, it.src, E.ncell, 0);
+    CFD_CUDA(cudaMemcpyAsync(it.a, h->staging, (size_t)nint * it.nv * 8, cudaMemcpyDeviceToHost, E.st));
+    CFD_CUDA(cudaStreamSynchronize(E.st));
+  }
+  return CFD3D_OK;
+}
+
+int cfd3d_grid_metrics(cfd3d_handle* h, int block, double* cx, double* ex, double* tx, double* grd) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
+  const BlockGeom& B = E.blk[block];
+  const int ngrd = E.par.ngrd;
+  std::vector<double> gm((size_t)(GM_GRD + ngrd) * B.ni * B.nj * B.nk);
+  long long ncb = (long long)B.ni * B.nj * B.nk;
+  for (int v = 0; v < GM_GRD + ngrd; ++v)
+    CFD_CUDA(cudaMemcpy(&gm[(size_t)v * ncb], E.d.gm + v * E.ncell + B.off, ncb * 8, cudaMemcpyDeviceToHost));
+  const int im = B.imax, jm = B.jmax, km = B.kmax;
+  auto li = [&](int i, int j, int k) { return (size_t)(i + 1) + (size_t)B.ni * ((j + 1) + (size_t)B.nj * (k + 1)); };
+  size_t q = 0;
+  if (cx) for (int k = 1; k <= km + 1; ++k) for (int j = 1; j <= jm + 1; ++j) for (int i = 1; i <= im; ++i) for (int v = 0; v < 3; ++v) cx[q++] = gm[(GM_CX + v) * ncb + li(i, j, k)];
+  q = 0;
+  if (ex) for (int k = 1; k <= km + 1; ++k) for (int j = 1; j <= jm; ++j) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) ex[q++] = gm[(GM_EX + v) * ncb + li(i, j, k)];
+  q = 0;
+  if (tx) for (int k = 1; k <= km; ++k) for (int j = 1; j <= jm + 1; ++j) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) tx[q++] = gm[(GM_TX + v) * ncb + li(i, j, k)];
+  q = 0;
+  if (grd) for (int k = 1; k <= km + 1; ++k) for (int j = 1; j <= jm + 1; ++j) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < ngrd; ++v) grd[q++] = gm[(GM_GRD + v) * ncb + li(i, j, k)];
+  return CFD3D_OK;
+}
+
+int cfd3d_set_device(int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CFD3D_ERR_NODEVICE;
+  if (device < 0 || device >= ndev) return CFD3D_ERR_ARG;
+  return cudaSetDevice(device) == cudaSuccess ? CFD3D_OK : CFD3D_ERR_CUDA;
+}
+
+int cfd3d_time_iterate(cfd3d_handle* h, int niter, double* ms) {
+  if (!h || niter < 1 || !ms) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  int rc = build_graph(E);
+  if (rc) return rc;
+  cudaEvent_t a, b;
+  CFD_CUDA(cudaEventCreate(&a));
+  CFD_CUDA(cudaEventCreate(&b));
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaEventRecord(a, E.st));
+  for (int q = 0; q < niter; ++q) CFD_CUDA(cudaGraphLaunch(E.graph, E.st));
+  CFD_CUDA(cudaEventRecord(b, E.st));
+  CFD_CUDA(cudaEventSynchronize(b));
+  float f = 0.0f;
+  CFD_CUDA(cudaEventElapsedTime(&f, a, b));
+  *ms = f;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  Scalars s;
+  return read_scalars(E, s);
+}
+
+int cfd3d_profile_iterate(cfd3d_handle* h, double* stage_ms) {
+  if (!h || !stage_ms) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  cudaEvent_t ev[9];
+  for (int q = 0; q < 9; ++q) CFD_CUDA(cudaEventCreate(&ev[q]));
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  launch_iteration(E, true, ev);
+  CFD_CUDA(cudaEventSynchronize(ev[8]));
+  for (int q = 0; q < CFD3D_NSTAGES; ++q) {
+    float f = 0.0f;
+    CFD_CUDA(cudaEventElapsedTime(&f, ev[q], ev[q + 1]));
+    stage_ms[q] = f;
+  }
+  for (int q = 0; q < 9; ++q) cudaEventDestroy(ev[q]);
+  CFD_CUDA(cudaGetLastError());
+  return CFD3D_OK;
+}
+
+int cfd3d_stats(const cfd3d_handle* h, int64_t* snd2_fallbacks, int* launches_per_iter) {
+  if (!h) return CFD3D_ERR_ARG;
+  const Engine& E = h->E;
+  Scalars s;
+  if (cudaMemcpy(&s, E.d.sc, sizeof(Scalars), cudaMemcpyDeviceToHost) != cudaSuccess) return CFD3D_ERR_CUDA;
+  if (snd2_fallbacks) *snd2_fallbacks = (int64_t)s.snd2_fallbacks;
+  if (launches_per_iter) *launches_per_iter = E.launches_per_iter;
+  return CFD3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,108 @@
+// engine.cuh -- data layout and host-side engine state shared by the translation units.
+//
+// HBM layout: every block's padded cell box (-1..imax+3 per direction, the reference's
+// storage range, src/variable_module.f90:69-71) is laid end to end in one global cell
+// space of `ncell` entries.  Every field is a structure of arrays: variable v of field f
+// lives at f[v * ncell + g], with g the padded global cell index, so a warp walking i
+// reads consecutive addresses.  Face vectors use the same index: cx(i,j,k) -- the
+// i-face between cells i and i+1 -- is stored at the index of cell (i,j,k).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "../../include/cfd3d.h"
+#include "physics.cuh"
+
+namespace cfd {
+
+constexpr int MAXBLK = 256;
+
+struct BlockGeom {
+  int imax, jmax, kmax;     // node counts
+  int ni, nj, nk;           // padded extents imax+5, ...
+  long long off;            // first padded cell of the block
+  long long int_off;        // first interior cell in the flat interior numbering
+  long long face_off[3];    // first face of each direction in the flat face numbering
+};
+
+// gm planes: face vectors and cell geometry
+enum { GM_CX = 0, GM_EX = 3, GM_TX = 6, GM_GRD = 9 };
+
+enum GhostKind : int {
+  G_COPY = 0, G_EXTRAP, G_WALL_VISCOUS, G_WALL_KW, G_SYMMETRY, G_FARFIELD,
+  G_WALLWALL, G_WALLWALL_KW4, G_WALLWALL_KW8, G_NOWALL3, G_NOWALL7
+};
+
+// one ghost cell write of the compiled boundary program
+struct GhostOp {
+  int kind;
+  int dst;        // written cell
+  int src;        // mirror / origin cell
+  int bnd;        // boundary cell (pv_s / pv_b / wall data)
+  int nb[6];      // neighbour cells (edge / corner fills), -1 = unused
+  int fidx;       // cell index of the face vector
+  int fplane;     // GM_CX / GM_EX / GM_TX
+  float fsign;    // +1 / -1
+  int pad;
+};
+
+// device scalars of one iteration
+struct Scalars {
+  double time_acc;
+  unsigned long long dtmin_bits;
+  double res[NPVM];
+  double resmax;
+  long long resmax_cell;
+  unsigned long long snd2_fallbacks;
+  int nonfinite;
+  int pad;
+};
+
+struct DevPtr {
+  double *pv, *dv, *tv, *gm, *res, *icav, *itt, *ocut, *dt, *rcav, *qq, *dqs, *dcv, *qold, *fi, *fv;
+  const BlockGeom* blk;
+  int nblk;
+  long long ncell;
+  long long nint;
+  Scalars* sc;
+  double* partial;   // per-CTA partial residual sums [gridsize][npv+2]
+};
+
+struct Engine {
+  cfd3d_config cfg;
+  Par par;
+  std::vector<BlockGeom> blk;
+  long long ncell = 0, nint = 0, nface[3] = {0, 0, 0};
+  DevPtr d{};
+  // ghost program: phase 0 faces + halos, 1 edges, 2 corners
+  GhostOp* d_ops[3] = {nullptr, nullptr, nullptr};
+  int nops[3] = {0, 0, 0};
+  int* d_planes = nullptr;
+  std::vector<long long> plane_off;
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_ready = 0;
+  int launches_per_iter = 0;
+  int red_grid = 0;
+  double time_host = 0.0;
+  std::string err;
+  // host copies of the reference state used by the ghost program
+  double pv_ref[NPVM];
+};
+
+// host entry points implemented in setup.cu
+bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks);
+bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks);
+void setup_planes(Engine& E);
+
+#define CFD_CUDA(call)                                                                 \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      E.err = std::string(#call) + ": " + cudaGetErrorString(e_);                      \
+      return CFD3D_ERR_CUDA;                                                           \
+    }                                                                                  \
+  } while (0)
+
+}  // namespace cfd

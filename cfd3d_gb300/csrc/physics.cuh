@@ -1,0 +1,644 @@
+// physics.cuh -- device physics of one pseudo-iteration.
+//
+// Per-point operators of the reference, rewritten for the GPU (one thread per face or
+// cell, operands in registers, SoA state in HBM):
+//   mixture EOS          deteos_simple / deteos_prop     src/eos_module.f90:1064-1234
+//   MUSCL / MLP          tvd, mlp, 11 limiters            src/muscl_module.f90:104-413
+//   inviscid fluxes      roe, roem, ausmpwp, ausmpup      src/flux_module.f90:198-721
+//   viscous fluxes       vsflux_laminar / _turbulent      src/vsflux_module.f90:182-425
+//   cavitation sources   merkle .. lee                    src/cav_module.f90:136-357
+//   SST source, eddy     kwsst / calbigf / no_des         src/turbsource_module.f90:269-414,
+//                                                         src/eddy_module.f90:135-187
+//   dual-time source     unsteadysource                   src/unsteady_module.f90:96-114
+//   diagonal operator    flowonly / flowturball, eigen    src/lhs_module.f90:346-534
+//   split Jacobians      flowonly / flowturball           src/jacobian_module.f90:182-403
+// The split Jacobian is applied matrix-free: its rows are rank-one updates of row 1 plus
+// a diagonal, so A*dq costs O(npv) instead of the reference's O(npv^2).
+#pragma once
+#include "iapws.cuh"
+
+namespace cfd {
+
+constexpr int NPVM = 9;
+constexpr int NDV = 18;
+
+// solver parameters, passed by value to every kernel
+struct Par {
+  int npv, ntv, nqq, ngrd;
+  int nsteady, iturb, nscheme, nmuscl, nlim, local, prec, fluid, ncav, fix_cav_clamp, with_prop;
+  double dt_phy, cfl, c_v, c_c, pref, uref, str, rhoref, l_chord;
+  double kref, oref, emutref;
+  double uref_vec[3], tref, y1ref, y2ref;   // free-stream state bcinfo%pv (src/bc_module.f90:133-146)
+};
+
+__device__ __forceinline__ double sq(double x) { return x * x; }
+
+template <class R>
+__device__ __forceinline__ R sndp2_of(const Par& c, R snd2, R u2) {
+  if (c.prec == 0) return snd2;
+  if (c.prec == 1) return fmin(snd2, fmax(u2, R(c.uref * c.uref)));
+  return fmin(snd2, fmax(fmax(u2, R(c.uref * c.uref)), R(c.str * c.str)));
+}
+template <class R>
+__device__ __forceinline__ R sndp2_du_of(const Par& c, R snd2, R u2) {
+  if (c.prec == 0) return snd2;
+  return fmin(snd2, fmax(u2, R(c.uref * c.uref)));
+}
+
+// ------------------------------------------------------------------ mixture EOS
+struct EosCount { unsigned long long* fallbacks; };
+
+template <class T>
+__device__ __forceinline__ void phase_l(int fluid, T p, T t, Phase<T>& e) {
+  if (fluid == 1) stiffened(p, t, e); else iapws_l(p, t, e);
+}
+template <class T>
+__device__ __forceinline__ void phase_v(int fluid, T p, T t, Phase<T>& e) {
+  if (fluid == 1) ideal_gas(p, t, e); else iapws_v(p, t, e);
+}
+
+__device__ __forceinline__ void mixture(const Phase<double>& l, const Phase<double>& v, const Phase<double>& g,
+                                        double y1, double y2, double* dv, unsigned long long* fallbacks) {
+  dv[2] = l.rho; dv[3] = v.rho; dv[4] = g.rho;
+  double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+  double yl = 1.0 - y1 - y2;
+  double irho = yl * irhol + y1 * irhov + y2 * irhog;
+  dv[0] = 1.0 / irho;
+  dv[1] = yl * l.h + y1 * v.h + y2 * g.h;
+  double r2 = dv[0] * dv[0];
+  double il2 = irhol * irhol, iv2 = irhov * irhov, ig2 = irhog * irhog;
+  dv[6] = r2 * (yl * il2 * l.drdp + y1 * iv2 * v.drdp + y2 * ig2 * g.drdp);
+  dv[7] = r2 * (yl * il2 * l.drdt + y1 * iv2 * v.drdt + y2 * ig2 * g.drdt);
+  dv[8] = r2 * (irhol - irhov);
+  dv[9] = r2 * (irhol - irhog);
+  dv[10] = yl * l.dhdp + y1 * v.dhdp + y2 * g.dhdp;
+  dv[11] = yl * l.dhdt + y1 * v.dhdt + y2 * g.dhdt;
+  dv[12] = v.h - l.h;
+  dv[13] = g.h - l.h;
+  dv[5] = dv[0] * dv[11] / (dv[0] * dv[6] * dv[11] + dv[7] * (1.0 - dv[0] * dv[10]));
+  if (dv[5] <= 0.0) {  // the reference's "alternative calculation for snd2"
+    if (fallbacks) atomicAdd(fallbacks, 1ull);
+    double ic2l = (dv[2] * l.drdp * l.dhdt + l.drdt * (1.0 - dv[2] * l.dhdp)) / (dv[2] * l.dhdt);
+    double ic2v = (dv[3] * v.drdp * v.dhdt + v.drdt * (1.0 - dv[3] * v.dhdp)) / (dv[3] * v.dhdt);
+    double ic2g = (dv[4] * g.drdp * g.dhdt + g.drdt * (1.0 - dv[4] * g.dhdp)) / (dv[4] * g.dhdt);
+    dv[5] = 1.0 / (r2 * (yl * ic2l * il2 + y1 * ic2v * iv2 + y2 * ic2g * ig2));
+  }
+  dv[14] = v.drdp; dv[15] = v.drdt; dv[16] = l.drdp; dv[17] = l.drdt;
+}
+
+// eos%deteos_simple
+__device__ __forceinline__ void deteos_simple(int fluid, double p, double t, double y1, double y2, double* dv,
+                                              unsigned long long* fb) {
+  Phase<double> l, v, g;
+  phase_l(fluid, p, t, l);
+  phase_v(fluid, p, t, v);
+  ideal_gas(p, t, g);
+  mixture(l, v, g, y1, y2, dv, fb);
+}
+
+// eos%deteos: with transport properties when with_prop (tv(1:2) written), else simple
+__device__ __forceinline__ void deteos(int fluid, int with_prop, double p, double t, double y1, double y2,
+                                       double* dv, double* tv, unsigned long long* fb) {
+  Phase<double> l, v, g;
+  phase_l(fluid, p, t, l);
+  phase_v(fluid, p, t, v);
+  ideal_gas(p, t, g);
+  mixture(l, v, g, y1, y2, dv, fb);
+  if (with_prop) {
+    double lv, lc, vv, vc;
+    if (fluid == 1) {
+      lv = stiffened_vis(t); lc = 4598.0 * lv;
+      vv = ideal_vis(t); vc = 1395.333333 * vv;
+    } else {
+      iapws_transport(t, l.rho, lv, lc);
+      iapws_transport(t, v.rho, vv, vc);
+    }
+    double gv = ideal_vis(t), gc = 1395.333333 * gv;
+    double yl = 1.0 - y1 - y2;
+    double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+    tv[0] = dv[0] * (lv * yl * irhol + vv * y1 * irhov + gv * y2 * irhog);
+    tv[1] = dv[0] * (lc * yl * irhol + vc * y1 * irhov + gc * y2 * irhog);
+  }
+}
+
+// ------------------------------------------------------------------ MUSCL / MLP
+template <class R>
+__device__ __forceinline__ R limiter(int nlim, R r, R r1, R r2, R alp) {
+  R c;
+  switch (nlim) {
+    case 0: return R(1);
+    case 1: return fmax(R(0), fmin(R(1), r));
+    case 2: return fmax(fmax(R(0), fmin(R(1), alp * r)), fmin(alp, r));
+    case 3: c = (r + fabs(r)) / (R(1) + fabs(r)); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 4: c = (R(1) + r) / R(2); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 5: c = (r * r + r) / (R(1) + r * r); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
+    case 6: c = fmin(R(1.5), alp); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
+    case 7: c = (R(1) + R(2) * r) / R(3); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 8: c = (R(-2) * r1 + R(11) + R(24) * r - R(3) * r2) / R(30); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 9: return (R(1) + R(2) * r) / R(3);
+    default: return (R(-2) * r1 + R(11) + R(24) * r - R(3) * r2) / R(30);
+  }
+}
+
+// stencil x[l] is the reference's x(l+1, k) for one variable k (38 cells)
+template <class R>
+__device__ __forceinline__ void muscl_var(const Par& c, const R* x, R& xl, R& xr) {
+  const R eps = R(1.0e-30), eps2 = R(1.0e-3);
+  R dq = x[9] - x[8];
+  R dqm = x[8] - x[22];
+  R dqm1 = x[22] - x[36];
+  R dqp = x[31] - x[9];
+  R dqp1 = x[37] - x[31];
+  R dqmm = R(1) / (dqm + eps);
+  R r0 = dq * dqmm, r10 = dqm1 * dqmm, r20 = dqp * dqmm;
+  R dqpp = R(1) / (dqp + eps);
+  R r1 = dq * dqpp, r11 = dqp1 * dqpp, r21 = dqm * dqpp;
+  R alp0 = R(2), alp1 = R(2);
+  if (c.nmuscl == 2) {
+    R rxy_l = fabs((x[10] - x[6]) / (x[9] - x[22] + eps));
+    R rxz_l = fabs((x[14] - x[2]) / (x[9] - x[22] + eps));
+    R rxy_r = fabs((x[11] - x[7]) / (x[31] - x[8] + eps));
+    R rxz_r = fabs((x[15] - x[3]) / (x[31] - x[8] + eps));
+    // min/max over the 3x3 planes: A = cells 0..17 (both face sides), L = i-1 plane (18..26),
+    // R = i+2 plane (27..35); "even" = the 9 cells of the left side (0,2,..,16), "odd" right side
+    R mA = x[0], MA = x[0], mE = x[0], ME = x[0], mO = x[1], MO = x[1];
+#pragma unroll
+    for (int l = 1; l < 18; ++l) { mA = fmin(mA, x[l]); MA = fmax(MA, x[l]); }
+#pragma unroll
+    for (int l = 2; l < 18; l += 2) { mE = fmin(mE, x[l]); ME = fmax(ME, x[l]); }
+#pragma unroll
+    for (int l = 3; l < 18; l += 2) { mO = fmin(mO, x[l]); MO = fmax(MO, x[l]); }
+    R mL = x[18], ML = x[18], mR = x[27], MR = x[27];
+#pragma unroll
+    for (int l = 19; l < 27; ++l) { mL = fmin(mL, x[l]); ML = fmax(ML, x[l]); }
+#pragma unroll
+    for (int l = 28; l < 36; ++l) { mR = fmin(mR, x[l]); MR = fmax(MR, x[l]); }
+    R qmin, qmax;
+    if (rxy_l < eps2 && rxz_l < eps2) { qmin = fmin(mA, mL); qmax = fmax(MA, ML); }
+    else if (x[9] - x[22] > R(0)) { qmax = MA; qmin = fmin(mE, mL); }
+    else { qmin = mA; qmax = fmax(ME, ML); }
+    R qml = fmin(fabs(qmax - x[8]), fabs(qmin - x[8]));
+    if (rxy_r < eps2 && rxz_r < eps2) { qmin = fmin(mA, mR); qmax = fmax(MA, MR); }
+    else if (x[31] - x[8] > R(0)) { qmax = fmax(MO, MR); qmin = mA; }
+    else { qmin = fmin(mO, mR); qmax = MA; }
+    R qmr = fmin(fabs(qmax - x[9]), fabs(qmin - x[9]));
+    alp0 = R(2) * fmax(R(1), r0) / (fabs(dq) + eps) / (R(1) + rxy_l + rxz_l) * qml;
+    if (fabs(dq) <= eps) alp1 = R(2) * fmax(R(1), dqp / eps) * fabs(dqpp) / (R(1) + rxy_r + rxz_r) * qmr;
+    else alp1 = R(2) * fmax(R(1), R(1) / r1) * fabs(dqpp) / (R(1) + rxy_r + rxz_r) * qmr;
+    alp0 = fmax(R(1), fmin(R(2), alp0));
+    alp1 = fmax(R(1), fmin(R(2), alp1));
+  }
+  xl = x[8] + R(0.5) * limiter<R>(c.nlim, r0, r10, r20, alp0) * dqm;
+  xr = x[9] - R(0.5) * limiter<R>(c.nlim, r1, r11, r21, alp1) * dqp;
+}
+
+// post-clipping of the reconstructed states (muscl_module.f90:136-158)
+template <class R>
+__device__ __forceinline__ void muscl_clip(const Par& c, const R* c9, const R* c10, R* xl, R* xr) {
+  xl[0] = fmax(R(-c.pref + 10.0), xl[0]);
+  xr[0] = fmax(R(-c.pref + 10.0), xr[0]);
+  if (xl[5] < R(0) || xl[5] > R(1)) xl[5] = c9[5];
+  if (xr[5] < R(0) || xr[5] > R(1)) xr[5] = c10[5];
+  if (xl[6] < R(0) || xl[6] > R(1)) xl[6] = c9[6];
+  if (xr[6] < R(0) || xr[6] > R(1)) xr[6] = c10[6];
+  if (xl[5] + xl[6] > R(1)) { xl[5] = c9[5]; xl[6] = c9[6]; }
+  if (xr[5] + xr[6] > R(1)) { xr[5] = c10[5]; xr[6] = c10[6]; }
+  if (c.npv > 7) {
+    if (xl[7] < R(0) && c9[7] > R(0)) xl[7] = c9[7];
+    if (xr[7] < R(0) && c10[7] > R(0)) xr[7] = c10[7];
+    if (xl[8] < R(0) && c9[8] > R(0)) xl[8] = c9[8];
+    if (xr[8] < R(0) && c10[8] > R(0)) xr[8] = c10[8];
+  }
+}
+
+// ------------------------------------------------------------------ inviscid fluxes
+// L/R face states: pv (npv), rho, h(static), snd2 in dv slots [0], [1], [5]
+struct FaceState { double pv[NPVM]; double rho, h, c2; };
+
+__device__ __forceinline__ double sdst_ratio_min(const double* s) {
+  double v = fmin(s[8] / s[9], s[9] / s[8]);
+  v = fmin(v, fmin(s[10] / s[8], s[8] / s[10]));
+  v = fmin(v, fmin(s[8] / s[6], s[6] / s[8]));
+  v = fmin(v, fmin(s[8] / s[2], s[2] / s[8]));
+  v = fmin(v, fmin(s[8] / s[14], s[14] / s[8]));
+  v = fmin(v, fmin(s[9] / s[11], s[11] / s[9]));
+  v = fmin(v, fmin(s[9] / s[7], s[7] / s[9]));
+  v = fmin(v, fmin(s[3] / s[9], s[9] / s[3]));
+  v = fmin(v, fmin(s[9] / s[15], s[15] / s[9]));
+  return v;
+}
+
+// returns the face flux fx (npv) for the unnormalised area vector n
+__device__ inline void inviscid_flux(const Par& c, const double* n, const FaceState& L, const FaceState& Rs,
+                              const double* sdst_in, double* fx, unsigned long long* fb) {
+  const int npv = c.npv;
+  double dl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  if (dl == 0.0) {
+    for (int k = 0; k < npv; ++k) fx[k] = 0.0;
+    return;
+  }
+  double nx = n[0] / dl, ny = n[1] / dl, nz = n[2] / dl;
+  const double* pl = L.pv;
+  const double* pr = Rs.pv;
+  double uull = nx * pl[1] + ny * pl[2] + nz * pl[3];
+  double uurr = nx * pr[1] + ny * pr[2] + nz * pr[3];
+  double srl = sqrt(L.rho), srr = sqrt(Rs.rho);
+  double ravg_d = 1.0 / (srl + srr);
+  double ravg[NPVM];
+  ravg[0] = 0.5 * (pl[0] + pr[0]);
+  ravg[4] = 0.5 * (pl[4] + pr[4]);
+  for (int k = 1; k <= 3; ++k) ravg[k] = (srl * pl[k] + srr * pr[k]) * ravg_d;
+  for (int k = 5; k < npv; ++k) ravg[k] = (srl * pl[k] + srr * pr[k]) * ravg_d;
+  double hl = L.h + 0.5 * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]);
+  double hr = Rs.h + 0.5 * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]);
+  // Roe-average EOS: only the sound speed is used (src/flux_module.f90:237,319,461,588)
+  double rdv[NDV];
+  deteos_simple(c.fluid, ravg[0] + c.pref, ravg[4], ravg[5], ravg[6], rdv, fb);
+  double rc2 = rdv[5];
+  double rrho = sqrt(L.rho * Rs.rho);
+  const double pref = c.pref;
+  if (c.nscheme == 1 || c.nscheme == 2) {
+    double ravg_ht = (srl * hl + srr * hr) * ravg_d;
+    double u2 = ravg[1] * ravg[1] + ravg[2] * ravg[2] + ravg[3] * ravg[3];
+    double uuu = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
+    if (c.nscheme == 1) {
+      double sndp2 = sndp2_of<double>(c, rc2, u2);
+      double q = sndp2 / rc2;
+      double uup = 0.5 * (1.0 + q) * uuu;
+      double ddd = 0.5 * sqrt((1.0 - q) * (1.0 - q) * uuu * uuu + 4.0 * sndp2);
+      double c_star = 0.5 * (fabs(uup + ddd) + fabs(uup - ddd));
+      double m_star = 0.5 * (fabs(uup + ddd) - fabs(uup - ddd)) / ddd;
+      double du = m_star * (uurr - uull) + (c_star - q * fabs(uuu) - 0.5 * (1.0 - q) * uuu * m_star) * (pr[0] - pl[0]) / rrho / sndp2;
+      double dp = m_star * (pr[0] - pl[0]) + (c_star - fabs(uuu) + 0.5 * (1.0 - q) * uuu * m_star) * rrho * (uurr - uull);
+      double au = fabs(uuu);
+      double df0 = au * (Rs.rho - L.rho) + du * rrho;
+      fx[0] = 0.5 * (L.rho * uull + Rs.rho * uurr - df0) * dl;
+      const double nn[3] = {nx, ny, nz};
+      for (int q3 = 0; q3 < 3; ++q3) {
+        double df = au * (Rs.rho * pr[1 + q3] - L.rho * pl[1 + q3]) + du * rrho * ravg[1 + q3] + dp * nn[q3];
+        fx[1 + q3] = 0.5 * (L.rho * uull * pl[1 + q3] + nn[q3] * (pl[0] + pref) + Rs.rho * uurr * pr[1 + q3] +
+                            nn[q3] * (pr[0] + pref) - df) * dl;
+      }
+      double df4 = au * (Rs.rho * hr - pr[0] - L.rho * hl + pl[0]) + du * rrho * ravg_ht + dp * uuu;
+      fx[4] = 0.5 * (L.rho * uull * hl + Rs.rho * uurr * hr - df4) * dl;
+      for (int k = 5; k < npv; ++k) {
+        double df = au * (Rs.rho * pr[k] - L.rho * pl[k]) + du * rrho * ravg[k];
+        fx[k] = 0.5 * (L.rho * uull * pl[k] + Rs.rho * uurr * pr[k] - df) * dl;
+      }
+      return;
+    }
+    // Roe-M
+    double am2rmid_du = sndp2_du_of<double>(c, rc2, u2) / rc2;
+    double am2rmid = sndp2_of<double>(c, rc2, u2) / rc2;
+    double fmid = sqrt(am2rmid) * (2.0 - sqrt(am2rmid));
+    double fmid_du = sqrt(am2rmid_du) * (2.0 - sqrt(am2rmid_du));
+    double amid = sqrt(rc2);
+    double b1 = fmax(fmax(0.0, uuu + amid), uurr + amid);
+    double b2 = fmin(fmin(0.0, uuu - amid), uull - amid);
+    double b1_du = fmax(fmax(0.0, uuu + fmid_du * amid), uurr + fmid_du * amid);
+    double b2_du = fmin(fmin(0.0, uuu - fmid_du * amid), uull - fmid_du * amid);
+    double m_tilde = copysign(1.0, uuu) * fmin(fabs(uuu) / amid, 1.0);
+    double m_tilde_du = copysign(1.0, uuu) * fmin(fabs(uuu) / (fmid_du * amid), 1.0);
+    double sd[18];
+    double add0 = 0.1 * fmin(L.rho * L.c2, Rs.rho * Rs.c2);
+    for (int k = 0; k < 18; ++k) sd[k] = sdst_in[k] + pref + add0;
+    double ff = 1.0 - sdst_ratio_min(sd);
+    ff = (uuu != 0.0) ? pow(fabs(uuu) / amid, ff) : 1.0;
+    double gg = 1.0 - fmin(sd[8] / sd[9], sd[9] / sd[8]);
+    gg = (uuu != 0.0) ? pow(fabs(uuu) / amid, gg) : 1.0;
+    double add = 1.0 + fabs(m_tilde), aaa = 1.0 + fabs(m_tilde_du);
+    double dq[NPVM], fl[NPVM], fr[NPVM], bdq[NPVM];
+    dq[0] = Rs.rho - L.rho;
+    for (int k = 1; k <= 3; ++k) dq[k] = Rs.rho * pr[k] - L.rho * pl[k];
+    dq[4] = Rs.rho * hr - L.rho * hl;
+    for (int k = 5; k < npv; ++k) dq[k] = Rs.rho * pr[k] - L.rho * pl[k];
+    const double nn[3] = {nx, ny, nz};
+    fl[0] = L.rho * uull; fr[0] = Rs.rho * uurr;
+    for (int q3 = 0; q3 < 3; ++q3) {
+      fl[1 + q3] = L.rho * uull * pl[1 + q3] + nn[q3] * (pl[0] + pref);
+      fr[1 + q3] = Rs.rho * uurr * pr[1 + q3] + nn[q3] * (pr[0] + pref);
+    }
+    fl[4] = L.rho * uull * hl; fr[4] = Rs.rho * uurr * hr;
+    for (int k = 5; k < npv; ++k) { fl[k] = L.rho * uull * pl[k]; fr[k] = Rs.rho * uurr * pr[k]; }
+    bdq[0] = dq[0] - ff * (pr[0] - pl[0]) / rc2 / fmid;
+    for (int k = 1; k <= 3; ++k) bdq[k] = bdq[0] * ravg[k] + rrho * (pr[k] - pl[k]);
+    bdq[4] = bdq[0] * ravg_ht + rrho * (hr - hl);
+    for (int k = 5; k < npv; ++k) bdq[k] = bdq[0] * ravg[k] + rrho * (pr[k] - pl[k]);
+    for (int k = 0; k < npv; ++k) fx[k] = (b1 * fl[k] - b2 * fr[k] + b1 * b2 * (dq[k] - gg * bdq[k] / add)) / (b1 - b2) * dl;
+    for (int q3 = 0; q3 < 3; ++q3)
+      fx[1 + q3] = fx[1 + q3] + gg * b1_du * b2_du * rrho * (uurr - uull) * nn[q3] / aaa / (b1_du - b2_du) * dl;
+    return;
+  }
+  // AUSM family
+  double amid = sqrt(rc2);
+  double zmr = uurr / amid, zml = uull / amid;
+  double fmid, fmid1, am2mid;
+  if (c.nscheme == 3) {
+    am2mid = ravg[1] * ravg[1] + ravg[2] * ravg[2] + ravg[3] * ravg[3];
+    double a1 = sndp2_du_of<double>(c, rc2, am2mid) / rc2;
+    double a0 = sndp2_of<double>(c, rc2, am2mid) / rc2;
+    fmid = sqrt(a0) * (2.0 - sqrt(a0));
+    fmid1 = sqrt(a1) * (2.0 - sqrt(a1));
+  } else {
+    double un = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
+    am2mid = un * un;
+    double a0 = sndp2_of<double>(c, rc2, am2mid) / rc2;
+    fmid = sqrt(a0) * (2.0 - sqrt(a0));
+    fmid1 = fmid;
+  }
+  double alpha = 3.0 / 16.0 * (-4.0 + 5.0 * fmid1 * fmid1);
+  alpha = fmax(fmin(alpha, 3.0 / 16.0), -3.0 / 4.0);
+  const double beta = 0.125;
+  double zmmr, pmr, zmpl, ppl;
+  if (fabs(zmr) >= 1.0) { zmmr = 0.5 * (zmr - fabs(zmr)); pmr = 0.5 * (1.0 - zmr / fabs(zmr)); }
+  else {
+    zmmr = -(0.25 * (zmr - 1.0) * (zmr - 1.0)) - beta * sq(zmr * zmr - 1.0);
+    pmr = 0.25 * (zmr - 1.0) * (zmr - 1.0) * (2.0 + zmr) - alpha * zmr * sq(zmr * zmr - 1.0);
+  }
+  if (fabs(zml) >= 1.0) { zmpl = 0.5 * (zml + fabs(zml)); ppl = 0.5 * (1.0 + zml / fabs(zml)); }
+  else {
+    zmpl = 0.25 * (zml + 1.0) * (zml + 1.0) + beta * sq(zml * zml - 1.0);
+    ppl = 0.25 * (zml + 1.0) * (zml + 1.0) * (2.0 - zml) + alpha * zml * sq(zml * zml - 1.0);
+  }
+  double zmpl1, zmmr1, pmid;
+  if (c.nscheme == 3) {
+    double zmid = zmpl + zmmr;
+    pmid = ppl * (pl[0] + pref) + pmr * (pr[0] + pref) - 2.0 * ppl * pmr * rrho * fmid1 * amid * (uurr - uull);
+    double sd[18];
+    double add0 = 0.1 * fmin(L.rho * L.c2, Rs.rho * Rs.c2);
+    for (int k = 0; k < 18; ++k) sd[k] = sdst_in[k] + pref + add0;
+    double m1 = fmin(sd[8] / sd[9], sd[9] / sd[8]);
+    double ww1 = 1.0 - m1 * m1 * m1;
+    double m2 = sdst_ratio_min(sd);
+    double ww2 = 1.0 - m2 * m2;
+    double ww = fmax(ww1, ww2);
+    double pmt = rrho * rc2;
+    double pwl = ((pl[0] + pref + rrho * rc2) / pmt - 1.0) * (1.0 - ww) / fmid;
+    double pwr = ((pr[0] + pref + rrho * rc2) / pmt - 1.0) * (1.0 - ww) / fmid;
+    if (zmid >= 0.0) {
+      pwl = pwl * rrho / L.rho;
+      pwr = pwr * rrho / L.rho;  // both weights scaled by the left density, as the reference does
+      zmpl1 = zmpl + zmmr * ((1.0 - ww) * (1.0 + pwr) - pwl);
+      zmmr1 = zmmr * ww * (1.0 + pwr);
+    } else {
+      pwl = pwl * rrho / Rs.rho;
+      pwr = pwr * rrho / Rs.rho;
+      zmpl1 = zmpl * ww * (1.0 + pwl);
+      zmmr1 = zmmr + zmpl * ((1.0 - ww) * (1.0 + pwl) - pwr);
+    }
+  } else {
+    const double kp = 0.25;
+    double zmid = zmpl + zmmr - kp * fmax(1.0 - am2mid / rc2, 0.0) * (pr[0] - pl[0]) / rrho / rc2 / fmid;
+    pmid = ppl * (pl[0] + pref) + pmr * (pr[0] + pref) - 2.0 * ppl * pmr * rrho * fmid * amid * (uurr - uull);
+    if (zmid > 0.0) { zmpl1 = zmid; zmmr1 = 0.0; } else { zmmr1 = zmid; zmpl1 = 0.0; }
+  }
+  double ml = zmpl1 * amid * L.rho, mr = zmmr1 * amid * Rs.rho;
+  fx[0] = (ml + mr) * dl;
+  fx[1] = (ml * pl[1] + mr * pr[1] + pmid * nx) * dl;
+  fx[2] = (ml * pl[2] + mr * pr[2] + pmid * ny) * dl;
+  fx[3] = (ml * pl[3] + mr * pr[3] + pmid * nz) * dl;
+  fx[4] = (ml * hl + mr * hr) * dl;
+  for (int k = 5; k < npv; ++k) fx[k] = (ml * pl[k] + mr * pr[k]) * dl;
+}
+
+// ------------------------------------------------------------------ cavitation
+struct CavOut { double r_c, r_v, icav[4]; };
+
+__device__ inline CavOut cavsource(const Par& c, const double* pv2, const double* dv, double vol) {
+  CavOut o = {0.0, 0.0, {0.0, 0.0, 0.0, 0.0}};
+  if (pv2[4] >= 647.096) return o;
+  const double dp_ref = 2.0 / (c.rhoref * c.uref * c.uref);
+  const double t_ref = c.uref / c.l_chord;
+  const double P = pv2[0] + c.pref;
+  const double clamp_c = c.fix_cav_clamp ? pv2[5] : pv2[4];
+  const double clamp_v = c.fix_cav_clamp ? (1.0 - pv2[5] - pv2[6]) : (1.0 - pv2[4] - pv2[5]);
+  const double yl = 1.0 - pv2[5] - pv2[6];
+  double r_c, r_v;
+  if (c.ncav == 1) {  // Merkle
+    double pww = h2o_pww(pv2[4]);
+    double rho1 = 1.0 / dv[0];
+    double kc = c.c_c * dv[0] * dp_ref * t_ref, kv = c.c_v * dv[0] * dp_ref * t_ref;
+    double dpc = fmax(P - pww, 0.0), dpv = fmax(pww - P, 0.0);
+    r_c = fmin(c.c_c * dv[0] * pv2[5] * dpc * dp_ref * t_ref, dv[0] * clamp_c);
+    r_v = fmin(c.c_v * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
+    o.r_c = r_c * vol; o.r_v = r_v * vol;
+    if (r_c != 0.0) {
+      o.icav[0] = -(r_c * dv[6] * rho1) - kc * pv2[5];
+      o.icav[1] = -(r_c * dv[7] * rho1);
+      o.icav[2] = -(r_c * dv[8] * rho1) - kc * dpc;
+      o.icav[3] = -(r_c * dv[9] * rho1);
+    }
+    if (r_v != 0.0) {
+      o.icav[0] = r_v * dv[6] * rho1 - kv * yl;
+      o.icav[1] = r_v * dv[7] * rho1;
+      o.icav[2] = r_v * dv[8] * rho1 - kv * dpv;
+      o.icav[3] = r_v * dv[9] * rho1 - kv * dpv;
+    }
+  } else if (c.ncav == 2) {  // Kunz
+    double pww = h2o_pww(pv2[4]);
+    double rho1 = 1.0 / dv[0];
+    double av = dv[0] * pv2[5] / dv[3], ag = dv[0] * pv2[6] / dv[4], al = 1.0 - av - ag;
+    double dpv = fmax(pww - P, 0.0);
+    r_c = fmin(c.c_c * dv[3] * av * sq(al + ag) * t_ref, dv[0] * clamp_c);
+    r_v = fmin(c.c_v * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
+    o.r_c = r_c * vol; o.r_v = r_v * vol;
+    double av1 = 1.0 - 4.0 * av + 3.0 * av * av;
+    o.icav[0] = -(c.c_c * t_ref * (dv[6] * pv2[5] * av1 + 2.0 * av * av * dv[14] * (al + ag)));
+    o.icav[1] = -(c.c_c * t_ref * (dv[7] * pv2[5] * av1 + 2.0 * av * av * dv[15] * (al + ag)));
+    o.icav[2] = -(c.c_c * t_ref * (dv[8] * pv2[5] + dv[0]) * av1);
+    o.icav[3] = -(c.c_c * t_ref * dv[9] * pv2[5] * av1);
+    if (r_v != 0.0) {
+      double kv = c.c_v * dv[0] * dp_ref * t_ref;
+      o.icav[0] = r_v * dv[6] * rho1 - kv * yl;
+      o.icav[1] = r_v * dv[7] * rho1;
+      o.icav[2] = r_v * dv[8] * rho1 - kv * dpv;
+      o.icav[3] = r_v * dv[9] * rho1 - kv * dpv;
+    }
+  } else if (c.ncav == 3) {  // Singhal
+    double pww = h2o_pww(pv2[4]);
+    double sigma = h2o_sigma(pv2[4]);
+    double rho1 = 1.0 / dv[2], rho2 = 1.0 / dv[3];
+    double cc = c.c_c * c.uref / sigma * dv[2] * dv[3], cv = c.c_v * c.uref / sigma * dv[2] * dv[3];
+    r_c = fmin(cc * sqrt(2.0 / 3.0 * fmax(P - pww, 0.0) * rho1) * pv2[5], dv[0] * clamp_c);
+    r_v = fmin(cv * sqrt(2.0 / 3.0 * fmax(pww - P, 0.0) * rho1) * yl, dv[0] * clamp_v);
+    o.r_c = r_c * vol; o.r_v = r_v * vol;
+    if (r_c != 0.0) {
+      o.icav[0] = -(r_c * (dv[14] * rho2 + 0.5 * dv[16] * rho1)) - 0.5 * cc * sqrt(2.0 / 3.0 * rho1) * pv2[5] * pow(P - pww, -0.5);
+      o.icav[1] = -(r_c * (dv[15] * rho2 + 0.5 * dv[17] * rho1));
+      o.icav[2] = -(cc * sqrt(2.0 / 3.0 * fmax(P - pww, 0.0) * rho1));
+      o.icav[3] = 0.0;
+    }
+    if (r_v != 0.0) {
+      o.icav[0] = r_v * (dv[14] * rho2 + 0.5 * dv[16] * rho1) - 0.5 * cv * sqrt(2.0 / 3.0 * rho1) * yl * pow(pww - P, -0.5);
+      o.icav[1] = r_v * (dv[15] * rho2 + 0.5 * dv[17] * rho1);
+      o.icav[2] = -(cv * sqrt(2.0 / 3.0 * fmax(pww - P, 0.0) * rho1));
+      o.icav[3] = o.icav[2];
+    }
+  } else if (c.ncav == 4) {  // Schnerr-Sauer
+    const double pi = 3.14159265358979323846, eta = 1.0e13;
+    double pww = h2o_pww(pv2[4]);
+    double rho1 = 1.0 / dv[0], rho3 = 1.0 / dv[2], rho4 = 1.0 / dv[3];
+    double k0 = 3.0 * pow(4.0 * pi * eta / 3.0, 1.0 / 3.0) * sqrt(2.0 / 3.0);
+    double base = k0 * dv[0] * pow(dv[3], 1.0 / 3.0) * pow(dv[2], -5.0 / 6.0) * pow(yl, 4.0 / 3.0);
+    r_c = fmin(c.c_c * base * pow(pv2[5], 2.0 / 3.0) * sqrt(fmax(P - pww, 0.0)), dv[0] * clamp_c);
+    r_v = fmin(c.c_v * base * pow(pv2[5] + pv2[6], 2.0 / 3.0) * sqrt(fmax(pww - P, 0.0)), dv[0] * clamp_v);
+    o.r_c = r_c * vol; o.r_v = r_v * vol;
+    if (r_c != 0.0) {
+      o.icav[0] = -(r_c * (dv[6] * rho1 + dv[14] * rho4 / 3.0 - 5.0 * dv[16] * rho3 / 6.0 + 0.5 / (P - pww)));
+      o.icav[1] = -(r_c * (dv[7] * rho1 + dv[15] * rho4 / 3.0 - 5.0 * dv[17] * rho3 / 6.0));
+      o.icav[2] = -(r_c * (dv[8] * rho1 + 2.0 / (3.0 * pv2[5]) - 4.0 / (3.0 * yl)));
+      o.icav[3] = -(r_c * (dv[9] * rho1 - 4.0 / (3.0 * yl)));
+    }
+    if (r_v != 0.0) {
+      o.icav[0] = r_v * (dv[6] * rho1 + dv[14] * rho4 / 3.0 - 5.0 * dv[16] * rho3 / 6.0 - 0.5 / (pww - P));
+      o.icav[1] = r_v * (dv[7] * rho1 + dv[15] * rho4 / 3.0 - 5.0 * dv[17] * rho3 / 6.0);
+      o.icav[2] = r_v * (dv[8] * rho1 + 2.0 / (3.0 * (pv2[5] + pv2[6])) - 4.0 / (3.0 * yl));
+      o.icav[3] = r_v * (dv[9] * rho1 + 2.0 / (3.0 * (pv2[5] + pv2[6])) - 4.0 / (3.0 * yl));
+    }
+  } else {  // Lee
+    double tww = h2o_tww(P);
+    double rho1 = 1.0 / dv[0];
+    r_c = fmin(c.c_c * dv[0] * pv2[5] * fmax(tww - pv2[4], 0.0) / tww, dv[0] * clamp_c);
+    r_v = fmin(c.c_v * dv[0] * yl * fmax(pv2[4] - tww, 0.0) / tww, dv[0] * clamp_v);
+    o.r_c = r_c * vol; o.r_v = r_v * vol;
+    if (r_c != 0.0) {
+      o.icav[0] = -(r_c * dv[6] * rho1);
+      o.icav[1] = -(r_c * dv[7] * rho1) + c.c_c * dv[0] * pv2[5] / tww;
+      o.icav[2] = -(r_c * dv[8] * rho1) - c.c_c * dv[0] * fmax(tww - pv2[4], 0.0) / tww;
+      o.icav[3] = -(r_c * dv[9] * rho1);
+    }
+    if (r_v != 0.0) {
+      o.icav[0] = r_v * dv[6] * rho1;
+      o.icav[1] = r_v * dv[7] * rho1 + c.c_v * dv[0] * yl / tww;
+      o.icav[2] = r_v * dv[8] * rho1 - c.c_v * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
+      o.icav[3] = r_v * dv[9] * rho1 - c.c_v * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
+    }
+  }
+  double lam = copysign(1.0, o.icav[2]);
+  double f = (1.0 - 0.5 * (1.0 - lam)) - 0.5 * (1.0 - lam);
+  for (int q = 0; q < 4; ++q) o.icav[q] *= f;
+  return o;
+}
+
+// ------------------------------------------------------------------ diagonal operator
+__device__ __forceinline__ double eigenvis_of(const Par& c, const double* dv, const double* tv) {
+  if (c.iturb == -3) return 0.0;
+  double den = dv[7] + dv[11] * dv[6] * dv[0] - dv[10] * dv[7] * dv[0];
+  if (c.iturb == -2) return fmax(dv[6] * tv[1] / den, 4.0 / 3.0 * tv[0] / dv[0]);
+  return fmax(dv[6] * (tv[1] + dv[11] * tv[2] / 0.9) / den, 4.0 / 3.0 * (tv[0] + tv[2]) / dv[0]);
+}
+
+// everything of lhs%getx that does not depend on the right-hand side
+struct Diag {
+  double a, b1, i_b1, ss, rr, cross, cross1, cross2, ssy1, ssy2, ssh, aaa1, aaa2, mm, c[4], tt, t[4];
+};
+
+__device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, const double* dv, const double* tv,
+                                             const double* fc /* cx1,cx2,ex1,ex2,tx1,tx2 x3 */, double vol,
+                                             double dt, const double* icav, const double* itt, Diag& D) {
+  double uv2 = pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3];
+  double sndp2 = sndp2_of<double>(c, dv[5], uv2);
+  const double cappa = 1.05;
+  double lamda = 0.0, fs = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    double ox = 0.5 * (fc[6 * d + 0] + fc[6 * d + 3]);
+    double oy = 0.5 * (fc[6 * d + 1] + fc[6 * d + 4]);
+    double oz = 0.5 * (fc[6 * d + 2] + fc[6 * d + 5]);
+    double ds = ox * ox + oy * oy + oz * oz;
+    double u = ox * pv[1] + oy * pv[2] + oz * pv[3];
+    double up = 0.5 * (1.0 + sndp2 / dv[5]) * u;
+    double dd = 0.5 * sqrt(u * u * sq(1.0 - sndp2 / dv[5]) + 4.0 * sndp2 * ds);
+    lamda += cappa * (fabs(up) + dd);
+    fs += ds;  // 0.25*(f1+f2)^2 summed over the components
+  }
+  double ev = eigenvis_of(c, dv, tv) * fs;
+  double bb = (c.nsteady == 1) ? 1.0 : 0.75;
+  double a = 1.0 / (vol / dt + lamda);
+  double unst = (c.nsteady >= 1) ? (double)c.nsteady * bb * vol / c.dt_phy : 0.0;
+  double b = (unst + 2.0 * ev / vol) * a;
+  for (int q = 0; q < 4; ++q) { D.c[q] = icav[q] * vol * a; D.t[q] = itt[q] * vol * a; }
+  D.a = a;
+  D.b1 = 1.0 + b;
+  D.i_b1 = 1.0 / (D.b1 * dv[0]);
+  D.ss = dv[0] * dv[11] * (1.0 / sndp2 + b / dv[5]);
+  D.rr = 1.0 / sndp2 - 1.0 / dv[5] + D.b1 * dv[6];
+  double hst = dv[1] + 0.5 * uv2 - uv2;
+  D.cross = dv[13] * dv[8] - dv[12] * dv[9];
+  D.cross1 = dv[12] * dv[7] - dv[11] * dv[8];
+  D.cross2 = dv[13] * dv[7] - dv[11] * dv[9];
+  double dhdp1 = 1.0 - dv[10] * dv[0];
+  D.ssy1 = dv[12] * dv[0] * D.rr + D.b1 * dv[8] * dhdp1;
+  D.ssy2 = dv[13] * dv[0] * D.rr + D.b1 * dv[9] * dhdp1;
+  D.ssh = dv[0] * D.rr * hst - D.b1 * dhdp1 * dv[0];
+  D.aaa1 = dv[8] * hst + dv[12] * dv[0] - D.cross * pv[6];
+  D.aaa2 = dv[7] * hst + dv[11] * dv[0] - D.cross2 * pv[6];
+  D.mm = 1.0 / (D.b1 * dv[0] * (D.ss + D.c[0] * D.cross1) - D.c[1] * D.ssy1 + D.c[2] * D.ss);
+  D.tt = 1.0 / (D.t[1] * D.t[2] - (D.t[0] + D.b1 * dv[0]) * (D.t[3] + D.b1 * dv[0]));
+}
+
+// x = D^-1 res (lhs%getx)
+__device__ __forceinline__ void diag_solve(const Par& c, const Diag& D, const double* pv, const double* dv,
+                                           const double* res, double* x) {
+  const double* C4 = D.c;
+  double uuu = res[1] * pv[1] + res[2] * pv[2] + res[3] * pv[3] - res[4];
+  double coeff1 = res[0] * D.aaa1 + dv[8] * uuu + D.cross * res[6];
+  double coeff2 = res[0] * D.aaa2 + dv[7] * uuu + D.cross2 * res[6];
+  double coeff3 = res[0] * (D.ssh - D.ssy2 * pv[6]) + dv[0] * D.rr * uuu + res[6] * D.ssy2;
+  double r6 = res[6] - res[0] * pv[6];
+  x[0] = (C4[3] * D.cross1 * (res[0] * pv[6] - res[6]) - C4[1] * coeff1 + C4[2] * coeff2 +
+          dv[0] * D.b1 * (coeff2 + D.cross1 * res[5] - D.cross1 * pv[5] * res[0])) * D.mm;
+  x[1] = (res[1] - res[0] * pv[1]) * D.i_b1;
+  x[2] = (res[2] - res[0] * pv[2]) * D.i_b1;
+  x[3] = (res[3] - res[0] * pv[3]) * D.i_b1;
+  x[4] = (C4[3] * D.i_b1 * D.ssy1 * r6 + C4[0] * coeff1 - C4[2] * D.i_b1 * coeff3 -
+          (coeff3 - D.ssy1 * pv[5] * res[0] + res[5] * D.ssy1)) * D.mm;
+  x[5] = (D.ss * (res[5] - res[0] * pv[5]) - C4[3] * D.ss * D.i_b1 * r6 - C4[0] * coeff2 + C4[1] * D.i_b1 * coeff3) * D.mm;
+  x[6] = r6 * D.i_b1;
+  if (c.npv > 7) {
+    double bd = D.b1 * dv[0];
+    double r7 = res[7] - res[0] * pv[7], r8 = res[8] - res[0] * pv[8];
+    x[7] = (r8 * D.t[1] - (bd + D.t[3]) * r7) * D.tt;
+    x[8] = (r7 * D.t[2] - (bd + D.t[0]) * r8) * D.tt;
+  }
+  for (int n = 0; n < c.npv; ++n) x[n] *= D.a;
+}
+
+// acc += sign_acc * A(sign) dq for the neighbour cell state (pv, dv, tv, vol) across face nx
+__device__ __forceinline__ void jac_apply(const Par& c, const double* nx, double vol, const double* pv,
+                                          const double* dv, const double* tv, double sign, const double* dq,
+                                          double* acc, double sign_acc) {
+  const double cappa = 1.05;
+  double ds = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
+  double u = nx[0] * pv[1] + nx[1] * pv[2] + nx[2] * pv[3];
+  double sndp2 = sndp2_of<double>(c, dv[5], pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
+  double up = 0.5 * (1.0 + sndp2 / dv[5]) * u;
+  double d = 0.5 * sqrt(u * u * sq(1.0 - sndp2 / dv[5]) + 4.0 * sndp2 * ds);
+  double lamda = sign * cappa * (fabs(up) + d);
+  double vis = sign * 2.0 * eigenvis_of(c, dv, tv) * ds / vol;
+  double beta = 1.0 / sndp2 - 1.0 / dv[5] + dv[6];
+  double uuu = u + lamda + vis;
+  double lv = lamda + vis;
+  // row 1: a1..a7 (+ g, ge shifts)
+  double r0 = (u * dv[6] + lamda * beta + vis * dv[6]) * dq[0] + nx[0] * dv[0] * dq[1] + nx[1] * dv[0] * dq[2] +
+              nx[2] * dv[0] * dq[3] + (u * dv[7] + lv * dv[7]) * dq[4] + (u * dv[8] + lv * dv[8]) * dq[5] +
+              (u * dv[9] + lv * dv[9]) * dq[6];
+  double ru = dv[0] * uuu;
+  double h = dv[1] + 0.5 * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
+  double y[NPVM];
+  y[0] = r0;
+  y[1] = pv[1] * r0 + nx[0] * dq[0] + ru * dq[1];
+  y[2] = pv[2] * r0 + nx[1] * dq[0] + ru * dq[2];
+  y[3] = pv[3] * r0 + nx[2] * dq[0] + ru * dq[3];
+  y[4] = ru * (dv[10] * dq[0] + pv[1] * dq[1] + pv[2] * dq[2] + pv[3] * dq[3] + dv[11] * dq[4] + dv[12] * dq[5] +
+               dv[13] * dq[6]) + h * r0 - lv * dq[0];
+  y[5] = pv[5] * r0 + ru * dq[5];
+  y[6] = pv[6] * r0 + ru * dq[6];
+  if (c.npv > 7) {
+    y[7] = pv[7] * r0 + ru * dq[7];
+    y[8] = pv[8] * r0 + ru * dq[8];
+  }
+  double s = 0.5 * sign_acc;
+  for (int n = 0; n < c.npv; ++n) acc[n] += s * y[n];
+}
+
+}  // namespace cfd

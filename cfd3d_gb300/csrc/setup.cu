@@ -1,0 +1,674 @@
+// setup.cu -- build-time work of the engine (runs once per cfd3d_create).
+//
+//  * grid metrics: face area vectors, volumes, centroids (calnormal / calvolume,
+//    src/grid_module.f90:609-1241) computed on the host per block, with the reference's
+//    metric halos across 1-to-1 interfaces (:725-940, :1115-1212);
+//  * wall distance (calydns, :350-607) as a two-pass brute-force GPU kernel: an FP32
+//    pass finds each cell's nearest wall-face distance, an FP64 pass re-evaluates only
+//    the faces within a relative margin of it, so the result equals the FP64 minimum;
+//  * the boundary program: the reference's BC, 12 edge, 8 corner and halo descriptors
+//    (src/bc_module.f90:71-1188) compiled into a flat list of ghost-cell operations in
+//    three dependency phases (faces + halos, edges, corners);
+//  * the LU-SGS hyperplane schedule: interior cells of all blocks grouped by
+//    i + j + k, so each sweep stage is one launch over independent cells.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include "engine.cuh"
+
+namespace cfd {
+
+namespace {
+
+struct HBlock {
+  int im, jm, km;
+  std::vector<double> x;   // x(3, 2:im+1, 2:jm+1, 2:km+1)
+  std::vector<double> cx, ex, tx, grd;  // Fortran ranges as in the reference
+  int ngrd;
+  double& X(int v, int i, int j, int k) { return x[v + 3 * ((i - 2) + (size_t)im * ((j - 2) + (size_t)jm * (k - 2)))]; }
+  double& CX(int v, int i, int j, int k) { return cx[v + 3 * ((i - 1) + (size_t)im * ((j - 1) + (size_t)(jm + 1) * (k - 1)))]; }
+  double& EX(int v, int i, int j, int k) { return ex[v + 3 * ((i - 1) + (size_t)(im + 1) * ((j - 1) + (size_t)jm * (k - 1)))]; }
+  double& TX(int v, int i, int j, int k) { return tx[v + 3 * ((i - 1) + (size_t)(im + 1) * ((j - 1) + (size_t)(jm + 1) * (k - 1)))]; }
+  double& G(int v, int i, int j, int k) { return grd[v + ngrd * ((i - 1) + (size_t)(im + 1) * ((j - 1) + (size_t)(jm + 1) * (k - 1)))]; }
+};
+
+struct Con {
+  int donor;
+  int s[3], e[3], sd[3], ed[3];
+  int tm[3][3];
+};
+
+double pyramid(const double* pa, const double* pb, const double* pc, const double* pd, const double* cen) {
+  double cs[3], va[3], vb[3];
+  for (int v = 0; v < 3; ++v) {
+    cs[v] = 0.25 * (pa[v] + pb[v] + pc[v] + pd[v]);
+    va[v] = pc[v] - pa[v];
+    vb[v] = pd[v] - pb[v];
+  }
+  double px = (cen[0] - cs[0]) * (va[1] * vb[2] - va[2] * vb[1]);
+  double py = (cen[1] - cs[1]) * (va[2] * vb[0] - va[0] * vb[2]);
+  double pz = (cen[2] - cs[2]) * (va[0] * vb[1] - va[1] * vb[0]);
+  return std::fabs(px + py + pz);
+}
+
+void face_vectors(HBlock& B, const cfd3d_block_desc& d) {
+  const int im = B.im, jm = B.jm, km = B.km;
+  B.cx.assign(3 * (size_t)im * (jm + 1) * (km + 1), 0.0);
+  B.ex.assign(3 * (size_t)(im + 1) * jm * (km + 1), 0.0);
+  B.tx.assign(3 * (size_t)(im + 1) * (jm + 1) * km, 0.0);
+  auto cross_half = [](const double* a, const double* b, double* out) {
+    out[0] = 0.5 * (a[1] * b[2] - b[1] * a[2]);
+    out[1] = 0.5 * (b[0] * a[2] - a[0] * b[2]);
+    out[2] = 0.5 * (a[0] * b[1] - b[0] * a[1]);
+  };
+  for (int k = 2; k <= km; ++k)
+    for (int j = 2; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i) {
+        double e[3], s[3], o[3];
+        for (int v = 0; v < 3; ++v) {
+          e[v] = B.X(v, i + 1, j + 1, k) - B.X(v, i + 1, j, k + 1);
+          s[v] = B.X(v, i + 1, j + 1, k + 1) - B.X(v, i + 1, j, k);
+        }
+        cross_half(e, s, o);
+        for (int v = 0; v < 3; ++v) B.CX(v, i, j, k) = o[v];
+      }
+  for (int i = 2; i <= im; ++i)
+    for (int k = 2; k <= km; ++k)
+      for (int j = 1; j <= jm; ++j) {
+        double c[3], s[3], o[3];
+        for (int v = 0; v < 3; ++v) {
+          c[v] = B.X(v, i, j + 1, k) - B.X(v, i + 1, j + 1, k + 1);
+          s[v] = B.X(v, i, j + 1, k + 1) - B.X(v, i + 1, j + 1, k);
+        }
+        cross_half(c, s, o);
+        for (int v = 0; v < 3; ++v) B.EX(v, i, j, k) = o[v];
+      }
+  for (int j = 2; j <= jm; ++j)
+    for (int i = 2; i <= im; ++i)
+      for (int k = 1; k <= km; ++k) {
+        double c[3], e[3], o[3];
+        for (int v = 0; v < 3; ++v) {
+          c[v] = B.X(v, i + 1, j, k + 1) - B.X(v, i, j + 1, k + 1);
+          e[v] = B.X(v, i + 1, j + 1, k + 1) - B.X(v, i, j, k + 1);
+        }
+        cross_half(c, e, o);
+        for (int v = 0; v < 3; ++v) B.TX(v, i, j, k) = o[v];
+      }
+  // degenerate patches zero the boundary face vectors (src/grid_module.f90:672-708)
+  for (int n = 0; n < d.nbc; ++n) {
+    if (d.bc[n].type != CFD3D_BC_DEGENERATE) continue;
+    const int* p = d.bc[n].pnts;
+    for (int ax = 0; ax < 3; ++ax) {
+      if (p[ax] != p[3 + ax]) continue;
+      bool mn = (p[ax] == 1);
+      if (ax == 0) { int ii = mn ? 1 : im; for (int k = 1; k <= km + 1; ++k) for (int j = 1; j <= jm + 1; ++j) for (int v = 0; v < 3; ++v) B.CX(v, ii, j, k) = 0.0; }
+      if (ax == 1) { int jj = mn ? 1 : jm; for (int k = 1; k <= km + 1; ++k) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) B.EX(v, i, jj, k) = 0.0; }
+      if (ax == 2) { int kk = mn ? 1 : km; for (int j = 1; j <= jm + 1; ++j) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) B.TX(v, i, j, kk) = 0.0; }
+      break;
+    }
+  }
+  // copy to the ghost edges of the face arrays
+  for (int k = 1; k <= km + 1; ++k) for (int i = 1; i <= im; ++i) for (int v = 0; v < 3; ++v) { B.CX(v, i, 1, k) = B.CX(v, i, 2, k); B.CX(v, i, jm + 1, k) = B.CX(v, i, jm, k); }
+  for (int j = 1; j <= jm + 1; ++j) for (int i = 1; i <= im; ++i) for (int v = 0; v < 3; ++v) { B.CX(v, i, j, 1) = B.CX(v, i, j, 2); B.CX(v, i, j, km + 1) = B.CX(v, i, j, km); }
+  for (int k = 1; k <= km + 1; ++k) for (int j = 1; j <= jm; ++j) for (int v = 0; v < 3; ++v) { B.EX(v, 1, j, k) = B.EX(v, 2, j, k); B.EX(v, im + 1, j, k) = B.EX(v, im, j, k); }
+  for (int j = 1; j <= jm; ++j) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) { B.EX(v, i, j, 1) = B.EX(v, i, j, 2); B.EX(v, i, j, km + 1) = B.EX(v, i, j, km); }
+  for (int k = 1; k <= km; ++k) for (int j = 1; j <= jm + 1; ++j) for (int v = 0; v < 3; ++v) { B.TX(v, 1, j, k) = B.TX(v, 2, j, k); B.TX(v, im + 1, j, k) = B.TX(v, im, j, k); }
+  for (int k = 1; k <= km; ++k) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) { B.TX(v, i, 1, k) = B.TX(v, i, 2, k); B.TX(v, i, jm + 1, k) = B.TX(v, i, jm, k); }
+}
+
+void volumes(HBlock& B) {
+  const int im = B.im, jm = B.jm, km = B.km;
+  B.grd.assign((size_t)B.ngrd * (im + 1) * (jm + 1) * (km + 1), 0.0);
+  for (int k = 2; k <= km; ++k)
+    for (int j = 2; j <= jm; ++j)
+      for (int i = 2; i <= im; ++i) {
+        double cen[3];
+        for (int v = 0; v < 3; ++v)
+          cen[v] = 0.125 * (B.X(v, i, j, k) + B.X(v, i + 1, j, k) + B.X(v, i, j + 1, k) + B.X(v, i, j, k + 1) +
+                            B.X(v, i + 1, j + 1, k) + B.X(v, i, j + 1, k + 1) + B.X(v, i + 1, j, k + 1) +
+                            B.X(v, i + 1, j + 1, k + 1));
+        for (int v = 0; v < 3; ++v) B.G(1 + v, i, j, k) = cen[v];
+        auto P = [&](int a, int b, int c, double* o) { for (int v = 0; v < 3; ++v) o[v] = B.X(v, a, b, c); };
+        double pa[3], pb[3], pc[3], pd[3], s = 0.0;
+        P(i, j, k, pa); P(i + 1, j, k, pb); P(i + 1, j + 1, k, pc); P(i, j + 1, k, pd); s += pyramid(pa, pb, pc, pd, cen);
+        P(i, j, k + 1, pa); P(i + 1, j, k + 1, pb); P(i + 1, j + 1, k + 1, pc); P(i, j + 1, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+        P(i, j, k, pa); P(i + 1, j, k, pb); P(i + 1, j, k + 1, pc); P(i, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+        P(i, j + 1, k, pa); P(i + 1, j + 1, k, pb); P(i + 1, j + 1, k + 1, pc); P(i, j + 1, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+        P(i, j, k, pa); P(i, j + 1, k, pb); P(i, j + 1, k + 1, pc); P(i, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+        P(i + 1, j, k, pa); P(i + 1, j + 1, k, pb); P(i + 1, j + 1, k + 1, pc); P(i + 1, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+        B.G(0, i, j, k) = s / 6.0;
+      }
+  for (int k = 2; k <= km; ++k)
+    for (int i = 2; i <= im; ++i) {
+      B.G(0, i, 1, k) = B.G(0, i, 2, k);
+      B.G(0, i, jm + 1, k) = B.G(0, i, jm, k);
+      for (int v = 1; v <= 3; ++v) {
+        B.G(v, i, 1, k) = 2.0 * B.G(v, i, 2, k) - B.G(v, i, 3, k);
+        B.G(v, i, jm + 1, k) = 2.0 * B.G(v, i, jm, k) - B.G(v, i, jm - 1, k);
+      }
+    }
+  for (int k = 2; k <= km; ++k)
+    for (int j = 1; j <= jm + 1; ++j) {
+      B.G(0, 1, j, k) = B.G(0, 2, j, k);
+      B.G(0, im + 1, j, k) = B.G(0, im, j, k);
+      for (int v = 1; v <= 3; ++v) {
+        B.G(v, 1, j, k) = 2.0 * B.G(v, 2, j, k) - B.G(v, 3, j, k);
+        B.G(v, im + 1, j, k) = 2.0 * B.G(v, im, j, k) - B.G(v, im - 1, j, k);
+      }
+    }
+  for (int j = 1; j <= jm + 1; ++j)
+    for (int i = 1; i <= im + 1; ++i) {
+      B.G(0, i, j, 1) = B.G(0, i, j, 2);
+      B.G(0, i, j, km + 1) = B.G(0, i, j, km);
+      for (int v = 1; v <= 3; ++v) {
+        // the reference extrapolates the k=1 centroids from the fixed cell (3, j, 3)
+        B.G(v, i, j, 1) = 2.0 * B.G(v, i, j, 2) - B.G(v, 3, j, 3);
+        B.G(v, i, j, km + 1) = 2.0 * B.G(v, i, j, km) - B.G(v, i, j, km - 1);
+      }
+    }
+}
+
+inline void cmap(const Con& g, int i, int j, int k, int& ii, int& jj, int& kk) {
+  ii = g.tm[0][0] * (i - g.s[0]) + g.tm[0][1] * (j - g.s[1]) + g.tm[0][2] * (k - g.s[2]) + g.sd[0];
+  jj = g.tm[1][0] * (i - g.s[0]) + g.tm[1][1] * (j - g.s[1]) + g.tm[1][2] * (k - g.s[2]) + g.sd[1];
+  kk = g.tm[2][0] * (i - g.s[0]) + g.tm[2][1] * (j - g.s[1]) + g.tm[2][2] * (k - g.s[2]) + g.sd[2];
+}
+
+bool read_cons(const cfd3d_block_desc& d, int nblocks, std::vector<Con>& out, std::string& err) {
+  for (int n = 0; n < d.ncon; ++n) {
+    const cfd3d_connection& c = d.con[n];
+    if (c.donor < 0 || c.donor >= nblocks) { err = "connection donor out of range"; return false; }
+    Con g{};
+    g.donor = c.donor;
+    for (int q = 0; q < 3; ++q) {
+      int t = c.transform[q];
+      if (t == 0 || std::abs(t) > 3) { err = "bad connection transform"; return false; }
+      g.tm[std::abs(t) - 1][q] = t > 0 ? 1 : -1;
+    }
+    const int* p = c.pnts;
+    const int* pd = c.pnts_donor;
+    bool any = false, anyd = false;
+    for (int m = 0; m < 3; ++m) {
+      if (p[m] == p[3 + m]) {
+        any = true;
+        for (int q = 0; q < 3; ++q) { g.s[q] = p[q]; g.e[q] = p[3 + q]; }
+        if (p[m] == 1) { g.s[m] = p[m] + 1; g.e[m] = p[3 + m] + 1; }
+      }
+      if (pd[m] == pd[3 + m]) {
+        anyd = true;
+        for (int q = 0; q < 3; ++q) { g.sd[q] = pd[q]; g.ed[q] = pd[3 + q]; }
+        if (pd[m] != 1) { g.sd[m] = pd[m] + 1; g.ed[m] = pd[3 + m] + 1; }
+      }
+    }
+    if (!any || !anyd) { err = "connection range is not a face"; return false; }
+    out.push_back(g);
+  }
+  return true;
+}
+
+// ---- wall distance ------------------------------------------------------------------
+__global__ void k_wall_distance(const double* __restrict__ cen, long long ncen, const double* __restrict__ wall,
+                                int nwall, double* __restrict__ out) {
+  extern __shared__ float sw[];
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double cx = 0, cy = 0, cz = 0;
+  if (c < ncen) { cx = cen[3 * c]; cy = cen[3 * c + 1]; cz = cen[3 * c + 2]; }
+  float fx = (float)cx, fy = (float)cy, fz = (float)cz;
+  float best = 3.0e38f;
+  // pass 1: FP32 minimum of the squared distance
+  for (int t0 = 0; t0 < nwall; t0 += blockDim.x) {
+    __syncthreads();
+    int t = t0 + threadIdx.x;
+    if (t < nwall) { sw[3 * threadIdx.x] = (float)wall[3 * t]; sw[3 * threadIdx.x + 1] = (float)wall[3 * t + 1]; sw[3 * threadIdx.x + 2] = (float)wall[3 * t + 2]; }
+    __syncthreads();
+    int nt = min((int)blockDim.x, nwall - t0);
+    for (int q = 0; q < nt; ++q) {
+      float dx = fx - sw[3 * q], dy = fy - sw[3 * q + 1], dz = fz - sw[3 * q + 2];
+      best = fminf(best, dx * dx + dy * dy + dz * dz);
+    }
+  }
+  // pass 2: FP64 distance of every face within the FP32 rounding margin
+  float thr = best * (1.0f + 1.0e-4f) + 1.0e-30f;
+  double ymin = 1.0e6;
+  for (int t0 = 0; t0 < nwall; t0 += blockDim.x) {
+    __syncthreads();
+    int t = t0 + threadIdx.x;
+    if (t < nwall) { sw[3 * threadIdx.x] = (float)wall[3 * t]; sw[3 * threadIdx.x + 1] = (float)wall[3 * t + 1]; sw[3 * threadIdx.x + 2] = (float)wall[3 * t + 2]; }
+    __syncthreads();
+    int nt = min((int)blockDim.x, nwall - t0);
+    for (int q = 0; q < nt; ++q) {
+      float dx = fx - sw[3 * q], dy = fy - sw[3 * q + 1], dz = fz - sw[3 * q + 2];
+      if (dx * dx + dy * dy + dz * dz <= thr) {
+        const double* w = wall + 3 * (size_t)(t0 + q);
+        double yt = sqrt((cx - w[0]) * (cx - w[0]) + (cy - w[1]) * (cy - w[1]) + (cz - w[2]) * (cz - w[2]));
+        if (yt < ymin) ymin = yt;
+      }
+    }
+  }
+  if (c < ncen) out[c] = ymin;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
+  const int ngrd = E.par.ngrd;
+  std::vector<HBlock> H(nblocks);
+  std::vector<std::vector<Con>> cons(nblocks);
+  for (int b = 0; b < nblocks; ++b) {
+    const cfd3d_block_desc& d = blocks[b];
+    HBlock& B = H[b];
+    B.im = d.imax; B.jm = d.jmax; B.km = d.kmax; B.ngrd = ngrd;
+    B.x.resize(3 * (size_t)d.imax * d.jmax * d.kmax);
+    for (size_t q = 0; q < B.x.size(); ++q) B.x[q] = d.xyz[q] * E.cfg.scale;
+    face_vectors(B, d);
+    if (!read_cons(d, nblocks, cons[b], E.err)) return false;
+  }
+  // face-vector halo on the node-based ranges, with orientation signs
+  for (int b = 0; b < nblocks; ++b)
+    for (auto& g : cons[b]) {
+      HBlock& S = H[b];
+      HBlock& D = H[g.donor];
+      int s1 = 1, s2 = 1;
+      if (g.sd[0] == g.ed[0]) { if (g.sd[1] > g.ed[1]) s1 = -1; if (g.sd[2] > g.ed[2]) s2 = -1; }
+      else if (g.sd[1] == g.ed[1]) { if (g.sd[2] > g.ed[2]) s1 = -1; if (g.sd[0] > g.ed[0]) s2 = -1; }
+      else { if (g.sd[0] > g.ed[0]) s1 = -1; if (g.sd[1] > g.ed[1]) s2 = -1; }
+      for (int k = g.s[2]; k <= g.e[2]; ++k)
+        for (int j = g.s[1]; j <= g.e[1]; ++j)
+          for (int i = g.s[0]; i <= g.e[0]; ++i) {
+            int ii, jj, kk;
+            cmap(g, i, j, k, ii, jj, kk);
+            for (int m = 0; m < 3; ++m) {
+              double a, c;
+              if (g.s[0] == g.e[0]) { a = S.EX(m, i, j, k); c = S.TX(m, i, j, k); }
+              else if (g.s[1] == g.e[1]) { a = S.TX(m, i, j, k); c = S.CX(m, i, j, k); }
+              else { a = S.CX(m, i, j, k); c = S.EX(m, i, j, k); }
+              if (g.sd[0] == g.ed[0]) { D.EX(m, ii, jj, kk) = s1 * a; D.TX(m, ii, jj, kk) = s2 * c; }
+              else if (g.sd[1] == g.ed[1]) { D.TX(m, ii, jj, kk) = s1 * a; D.CX(m, ii, jj, kk) = s2 * c; }
+              else { D.CX(m, ii, jj, kk) = s1 * a; D.EX(m, ii, jj, kk) = s2 * c; }
+            }
+          }
+    }
+  // node ranges become cell ranges ("reodering", src/grid_module.f90:926-940)
+  for (auto& cl : cons)
+    for (auto& g : cl)
+      for (int m = 0; m < 3; ++m) {
+        if (g.s[m] != g.e[m]) g.s[m] += 1;
+        if (g.sd[m] != g.ed[m]) {
+          if (g.sd[m] < g.ed[m]) g.sd[m] += 1;
+          else g.ed[m] += 1;
+        }
+      }
+  for (auto& B : H) volumes(B);
+  for (auto& B : H)
+    for (int k = 2; k <= B.km; ++k) for (int j = 2; j <= B.jm; ++j) for (int i = 2; i <= B.im; ++i)
+      if (!(B.G(0, i, j, k) > 0.0)) { E.err = "zero/negative cell volume"; return false; }
+  auto exchange = [&](int var) {
+    for (int b = 0; b < nblocks; ++b)
+      for (auto& g : cons[b])
+        for (int k = g.s[2]; k <= g.e[2]; ++k)
+          for (int j = g.s[1]; j <= g.e[1]; ++j)
+            for (int i = g.s[0]; i <= g.e[0]; ++i) {
+              int ii, jj, kk;
+              cmap(g, i, j, k, ii, jj, kk);
+              H[g.donor].G(var, ii, jj, kk) = H[b].G(var, i, j, k);
+            }
+  };
+  exchange(0);
+  if (ngrd == 5) {
+    // wall-face centres of every block (BCWall patches), then the GPU brute force
+    std::vector<double> wall, cen;
+    for (int b = 0; b < nblocks; ++b) {
+      const cfd3d_block_desc& d = blocks[b];
+      HBlock& B = H[b];
+      for (int n = 0; n < d.nbc; ++n) {
+        if (d.bc[n].type != CFD3D_BC_WALL) continue;
+        const int* p = d.bc[n].pnts;
+        int ax = -1;
+        for (int a = 0; a < 3; ++a) if (p[a] == p[3 + a]) ax = a;
+        int nmax[3] = {B.im, B.jm, B.km};
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) { lo[a] = p[a] + 1; hi[a] = p[3 + a]; }
+        int plane = (p[ax] == 1) ? 2 : nmax[ax] + 1;
+        int t1 = (ax + 1) % 3, t2 = (ax + 2) % 3;
+        if (ax == 1) { t1 = 0; t2 = 2; }
+        for (int b2 = lo[t2]; b2 <= hi[t2]; ++b2)
+          for (int a2 = lo[t1]; a2 <= hi[t1]; ++a2) {
+            int q0[3], q1[3], q2[3], q3[3];
+            q0[ax] = q1[ax] = q2[ax] = q3[ax] = plane;
+            q0[t1] = a2; q0[t2] = b2;
+            q1[t1] = a2 + 1; q1[t2] = b2;
+            q2[t1] = a2; q2[t2] = b2 + 1;
+            q3[t1] = a2 + 1; q3[t2] = b2 + 1;
+            for (int v = 0; v < 3; ++v)
+              wall.push_back(0.25 * (B.X(v, q0[0], q0[1], q0[2]) + B.X(v, q1[0], q1[1], q1[2]) +
+                                     B.X(v, q2[0], q2[1], q2[2]) + B.X(v, q3[0], q3[1], q3[2])));
+          }
+      }
+      for (int k = 2; k <= B.km; ++k) for (int j = 2; j <= B.jm; ++j) for (int i = 2; i <= B.im; ++i)
+        for (int v = 0; v < 3; ++v)
+          cen.push_back(0.125 * (B.X(v, i, j, k) + B.X(v, i + 1, j, k) + B.X(v, i, j + 1, k) + B.X(v, i, j, k + 1) +
+                                 B.X(v, i + 1, j + 1, k) + B.X(v, i, j + 1, k + 1) + B.X(v, i + 1, j, k + 1) +
+                                 B.X(v, i + 1, j + 1, k + 1)));
+    }
+    long long ncen = (long long)cen.size() / 3;
+    std::vector<double> yd(ncen, 1.0e6);
+    int nwall = (int)(wall.size() / 3);
+    if (nwall > 0) {
+      double *dcen = nullptr, *dwall = nullptr, *dy = nullptr;
+      if (cudaMalloc(&dcen, cen.size() * 8) != cudaSuccess || cudaMalloc(&dwall, wall.size() * 8) != cudaSuccess ||
+          cudaMalloc(&dy, ncen * 8) != cudaSuccess) {
+        E.err = "cudaMalloc failed in wall distance"; cudaFree(dcen); cudaFree(dwall); return false;
+      }
+      cudaMemcpy(dcen, cen.data(), cen.size() * 8, cudaMemcpyHostToDevice);
+      cudaMemcpy(dwall, wall.data(), wall.size() * 8, cudaMemcpyHostToDevice);
+      const int T = 256;
+      k_wall_distance<<<(unsigned)((ncen + T - 1) / T), T, 3 * T * sizeof(float)>>>(dcen, ncen, dwall, nwall, dy);
+      cudaError_t e = cudaMemcpy(yd.data(), dy, ncen * 8, cudaMemcpyDeviceToHost);
+      cudaFree(dcen); cudaFree(dwall); cudaFree(dy);
+      if (e != cudaSuccess) { E.err = std::string("wall distance: ") + cudaGetErrorString(e); return false; }
+    }
+    long long q = 0;
+    for (auto& B : H) {
+      for (int k = 2; k <= B.km; ++k) for (int j = 2; j <= B.jm; ++j) for (int i = 2; i <= B.im; ++i) B.G(4, i, j, k) = yd[q++];
+      for (int k = 2; k <= B.km; ++k) for (int i = 2; i <= B.im; ++i) { B.G(4, i, 1, k) = B.G(4, i, 2, k); B.G(4, i, B.jm + 1, k) = B.G(4, i, B.jm, k); }
+      for (int k = 2; k <= B.km; ++k) for (int j = 1; j <= B.jm + 1; ++j) { B.G(4, 1, j, k) = B.G(4, 2, j, k); B.G(4, B.im + 1, j, k) = B.G(4, B.im, j, k); }
+      for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im + 1; ++i) { B.G(4, i, j, 1) = B.G(4, i, j, 2); B.G(4, i, j, B.km + 1) = B.G(4, i, j, B.km); }
+    }
+    exchange(4);
+  }
+  // scatter into the SoA metric planes
+  const long long nc = E.ncell;
+  const int ngm = GM_GRD + ngrd;
+  std::vector<double> gm((size_t)ngm * nc, 0.0);
+  for (int b = 0; b < nblocks; ++b) {
+    HBlock& B = H[b];
+    const BlockGeom& G = E.blk[b];
+    auto gi = [&](int i, int j, int k) { return G.off + (i + 1) + (long long)G.ni * ((j + 1) + (long long)G.nj * (k + 1)); };
+    for (int k = 1; k <= B.km + 1; ++k) for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im; ++i)
+      for (int v = 0; v < 3; ++v) gm[(size_t)(GM_CX + v) * nc + gi(i, j, k)] = B.CX(v, i, j, k);
+    for (int k = 1; k <= B.km + 1; ++k) for (int j = 1; j <= B.jm; ++j) for (int i = 1; i <= B.im + 1; ++i)
+      for (int v = 0; v < 3; ++v) gm[(size_t)(GM_EX + v) * nc + gi(i, j, k)] = B.EX(v, i, j, k);
+    for (int k = 1; k <= B.km; ++k) for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im + 1; ++i)
+      for (int v = 0; v < 3; ++v) gm[(size_t)(GM_TX + v) * nc + gi(i, j, k)] = B.TX(v, i, j, k);
+    for (int k = 1; k <= B.km + 1; ++k) for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im + 1; ++i)
+      for (int v = 0; v < ngrd; ++v) gm[(size_t)(GM_GRD + v) * nc + gi(i, j, k)] = B.G(v, i, j, k);
+  }
+  if (cudaMemcpy(E.d.gm, gm.data(), gm.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+    E.err = "metric upload failed"; return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------------------
+// boundary program
+namespace {
+
+enum Face { F_IMIN, F_IMAX, F_JMIN, F_JMAX, F_KMIN, F_KMAX, F_NOFACE };
+
+struct Bc {
+  int kind;            // GhostKind
+  int type;            // cfd3d BC type (face patches)
+  Face face = F_NOFACE;
+  int s[3], e[3], o[3] = {0, 0, 0}, dir[3] = {0, 0, 0};
+  int nb[6][3];
+  bool farfield_sign = false;
+};
+
+int wall_kind(const Par& c) {
+  if (c.iturb == 0) return G_WALL_KW;
+  if (c.iturb == -2) return G_WALL_VISCOUS;
+  return G_SYMMETRY;  // bcwallinviscid is the symmetry reflection
+}
+
+}  // namespace
+
+bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
+  const Par& c = E.par;
+  std::vector<GhostOp> ops[3];
+  for (int b = 0; b < nblocks; ++b) {
+    const cfd3d_block_desc& d = blocks[b];
+    const BlockGeom& G = E.blk[b];
+    const int im = d.imax, jm = d.jmax, km = d.kmax;
+    auto gi = [&](int i, int j, int k) -> int {
+      return (int)(G.off + (i + 1) + (long long)G.ni * ((j + 1) + (long long)G.nj * (k + 1)));
+    };
+    // ---- face patches (src/bc_module.f90:126-335)
+    std::vector<Bc> bcs;
+    for (int n = 0; n < d.nbc; ++n) {
+      const int* p = d.bc[n].pnts;
+      Bc bi;
+      bi.type = d.bc[n].type;
+      int ax = -1;
+      for (int a = 0; a < 3; ++a) if (p[a] == p[3 + a]) ax = a;
+      if (ax < 0) { E.err = "bc patch is not a face"; return false; }
+      int nmax[3] = {im, jm, km};
+      bool mn = (p[ax] == 1);
+      if (!mn && p[ax] != nmax[ax]) { E.err = "bc patch is not on a block face"; return false; }
+      for (int a = 0; a < 3; ++a) { bi.s[a] = p[a] + 1; bi.e[a] = p[3 + a]; bi.dir[a] = 1; }
+      bi.s[ax] = bi.e[ax] = mn ? 1 : p[ax] + 1;
+      bi.dir[ax] = -1;
+      if (mn) { bi.s[ax] -= 2; bi.o[ax] = 2 * bi.e[ax] + 1; }
+      else { bi.e[ax] += 2; bi.o[ax] = 2 * bi.s[ax] - 1; }
+      bi.face = (Face)(2 * ax + (mn ? 0 : 1));
+      switch (bi.type) {
+        case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
+        case CFD3D_BC_SYMMETRY: bi.kind = G_SYMMETRY; break;
+        case CFD3D_BC_FARFIELD: bi.kind = G_FARFIELD; bi.farfield_sign = true; break;
+        case CFD3D_BC_EXTRAPOLATE: case CFD3D_BC_DEGENERATE: bi.kind = G_EXTRAP; break;
+        case CFD3D_BC_INFLOW: bi.kind = -1; break;
+        default: E.err = "unknown bc type"; return false;
+      }
+      for (int q = 0; q < 6; ++q) for (int r = 0; r < 3; ++r) bi.nb[q][r] = 0;
+      bcs.push_back(bi);
+    }
+    auto is_surf = [&](const int* pnt, std::initializer_list<int> axes) {
+      for (auto& bc : bcs) {
+        if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_SYMMETRY) continue;
+        bool in = true;
+        for (int a : axes) in = in && bc.s[a] <= pnt[a] && bc.e[a] >= pnt[a];
+        if (in) return true;
+      }
+      return false;
+    };
+    // emits the ghost ops of one descriptor into a phase
+    auto emit = [&](const Bc& bi, int phase, int nnb, bool skip_zero_nb) {
+      if (bi.kind < 0) return;
+      for (int k = bi.s[2]; k <= bi.e[2]; ++k)
+        for (int j = bi.s[1]; j <= bi.e[1]; ++j)
+          for (int i = bi.s[0]; i <= bi.e[0]; ++i) {
+            GhostOp op{};
+            op.kind = bi.kind;
+            op.dst = gi(i, j, k);
+            int mi = bi.o[0] + bi.dir[0] * i, mj = bi.o[1] + bi.dir[1] * j, mk = bi.o[2] + bi.dir[2] * k;
+            op.src = gi(mi, mj, mk);
+            op.bnd = op.src;
+            for (int q = 0; q < 6; ++q) op.nb[q] = -1;
+            op.fidx = op.src; op.fplane = GM_CX; op.fsign = 1.0f;
+            if (bi.kind == G_SYMMETRY || bi.kind == G_FARFIELD || bi.kind == G_WALL_KW) {
+              int ii = mi, jj = mj, kk = mk;
+              float s = bi.farfield_sign ? -1.0f : 1.0f;
+              switch (bi.face) {
+                case F_IMIN: ii = bi.o[0] + bi.dir[0] * bi.e[0]; op.fidx = gi(ii - 1, jj, kk); op.fplane = GM_CX; op.fsign = s; break;
+                case F_IMAX: ii = bi.o[0] + bi.dir[0] * bi.s[0]; op.fidx = gi(ii, jj, kk); op.fplane = GM_CX; op.fsign = -s; break;
+                case F_JMIN: jj = bi.o[1] + bi.dir[1] * bi.e[1]; op.fidx = gi(ii, jj - 1, kk); op.fplane = GM_EX; op.fsign = s; break;
+                case F_JMAX: jj = bi.o[1] + bi.dir[1] * bi.s[1]; op.fidx = gi(ii, jj, kk); op.fplane = GM_EX; op.fsign = -s; break;
+                case F_KMIN: kk = bi.o[2] + bi.dir[2] * bi.e[2]; op.fidx = gi(ii, jj, kk - 1); op.fplane = GM_TX; op.fsign = s; break;
+                case F_KMAX: kk = bi.o[2] + bi.dir[2] * bi.s[2]; op.fidx = gi(ii, jj, kk); op.fplane = GM_TX; op.fsign = -s; break;
+                default: break;  // corner 'Kmin'/'Kmax': the boundary cell stays the mirror cell
+              }
+              op.bnd = gi(ii, jj, kk);
+            }
+            int q2 = 0;
+            for (int q = 0; q < nnb; ++q) {
+              const int* nb = bi.nb[q];
+              if (skip_zero_nb && nb[0] == 0 && nb[1] == 0 && nb[2] == 0) continue;
+              op.nb[q2++] = gi(nb[0] + bi.dir[0] * i, nb[1] + bi.dir[1] * j, nb[2] + bi.dir[2] * k);
+            }
+            ops[phase].push_back(op);
+          }
+    };
+    for (auto& bi : bcs) emit(bi, 0, 0, false);
+    // ---- 12 edges (src/bc_module.f90:505-865)
+    struct ED { int s[3], e[3], n1[3], n2[3], n3[3], o[3]; };
+    const ED EDG[12] = {
+        {{-1, -1, 2}, {1, 1, km}, {1, 2, 0}, {2, 1, 0}, {0, 0, 0}, {2, 2, 0}},
+        {{im + 1, -1, 2}, {im + 3, 1, km}, {im + 1, 2, 0}, {im, 1, 0}, {0, 0, 0}, {im, 2, 0}},
+        {{-1, jm + 1, 2}, {1, jm + 3, km}, {1, jm, 0}, {2, jm + 1, 0}, {0, 0, 0}, {2, jm, 0}},
+        {{im + 1, jm + 1, 2}, {im + 3, jm + 3, km}, {im + 1, jm, 0}, {im, jm + 1, 0}, {0, 0, 0}, {im, jm, 0}},
+        {{-1, 2, -1}, {1, jm, 1}, {1, 0, 2}, {0, 0, 0}, {2, 0, 1}, {2, 0, 2}},
+        {{im + 1, 2, -1}, {im + 3, jm, 1}, {im + 1, 0, 2}, {0, 0, 0}, {im, 0, 1}, {im, 0, 2}},
+        {{-1, 2, km + 1}, {1, jm, km + 3}, {1, 0, km}, {0, 0, 0}, {2, 0, km + 1}, {2, 0, km}},
+        {{im + 1, 2, km + 1}, {im + 3, jm, km + 3}, {im + 1, 0, km}, {0, 0, 0}, {im, 0, km + 1}, {im, 0, km}},
+        {{2, -1, -1}, {im, 1, 1}, {0, 0, 0}, {0, 1, 2}, {0, 2, 1}, {0, 2, 2}},
+        {{2, jm + 1, -1}, {im, jm + 3, 1}, {0, 0, 0}, {0, jm + 1, 2}, {0, jm, 1}, {0, jm, 2}},
+        {{2, -1, km + 1}, {im, 1, km + 3}, {0, 0, 0}, {0, 1, km}, {0, 2, km + 1}, {0, 2, km}},
+        {{2, jm + 1, km + 1}, {im, jm + 3, km + 3}, {0, 0, 0}, {0, jm + 1, km}, {0, jm, km + 1}, {0, jm, km}},
+    };
+    for (int m = 0; m < 12; ++m) {
+      Bc e;
+      for (int q = 0; q < 3; ++q) {
+        e.s[q] = EDG[m].s[q]; e.e[q] = EDG[m].e[q]; e.o[q] = EDG[m].o[q]; e.dir[q] = 0;
+        e.nb[0][q] = EDG[m].n1[q]; e.nb[1][q] = EDG[m].n2[q]; e.nb[2][q] = EDG[m].n3[q];
+        e.nb[3][q] = e.nb[4][q] = e.nb[5][q] = 0;
+      }
+      bool s1, s2;
+      int along;
+      if (m < 4) { s1 = is_surf(e.nb[0], {0, 1}); s2 = is_surf(e.nb[1], {0, 1}); along = 2; }
+      else if (m < 8) { s1 = is_surf(e.nb[0], {0, 2}); s2 = is_surf(e.nb[2], {0, 2}); along = 1; }
+      else { s1 = is_surf(e.nb[1], {1, 2}); s2 = is_surf(e.nb[2], {1, 2}); along = 0; }
+      if (s1 && s2) {
+        e.kind = (c.iturb == 0) ? G_WALLWALL_KW4 : G_WALLWALL;
+        e.dir[along] = 1;
+        emit(e, 1, 3, true);
+      } else if (s1 || s2) {
+        e.kind = wall_kind(c);
+        if (m < 4) {
+          if (s1) { e.face = (m == 0 || m == 2) ? F_IMIN : F_IMAX; e.o[0] = e.nb[1][0]; e.o[1] = e.nb[1][1]; }
+          else { e.face = (m == 0 || m == 1) ? F_JMIN : F_JMAX; e.o[0] = e.nb[0][0]; e.o[1] = e.nb[0][1]; }
+        } else if (m < 8) {
+          if (s1) { e.face = (m == 4 || m == 6) ? F_IMIN : F_IMAX; e.o[0] = e.nb[2][0]; e.o[2] = e.nb[2][2]; }
+          else { e.face = (m == 4 || m == 5) ? F_KMIN : F_KMAX; e.o[0] = e.nb[0][0]; e.o[2] = e.nb[0][2]; }
+        } else {
+          if (s1) { e.face = (m == 8 || m == 10) ? F_JMIN : F_JMAX; e.o[1] = e.nb[2][1]; e.o[2] = e.nb[2][2]; }
+          else { e.face = (m == 8 || m == 9) ? F_KMIN : F_KMAX; e.o[1] = e.nb[1][1]; e.o[2] = e.nb[1][2]; }
+        }
+        e.dir[along] = 1;
+        emit(e, 1, 0, false);
+      } else {
+        e.kind = G_NOWALL3;
+        e.dir[along] = 1;
+        emit(e, 1, 3, true);
+      }
+    }
+    // ---- 8 corners (src/bc_module.f90:870-1186)
+    for (int m = 0; m < 8; ++m) {
+      int mi = m & 1, mj = (m >> 1) & 1, mk = (m >> 2) & 1;
+      Bc e;
+      e.s[0] = mi ? im + 1 : -1; e.e[0] = mi ? im + 3 : 1;
+      e.s[1] = mj ? jm + 1 : -1; e.e[1] = mj ? jm + 3 : 1;
+      e.s[2] = mk ? km + 1 : -1; e.e[2] = mk ? km + 3 : 1;
+      int gi_ = mi ? im + 1 : 1, ci = mi ? im : 2;
+      int gj = mj ? jm + 1 : 1, cj = mj ? jm : 2;
+      int gk = mk ? km + 1 : 1, ck = mk ? km : 2;
+      int N[6][3] = {{gi_, cj, ck}, {ci, gj, ck}, {ci, cj, gk}, {ci, gj, gk}, {gi_, cj, gk}, {gi_, gj, ck}};
+      for (int q = 0; q < 6; ++q) for (int r = 0; r < 3; ++r) e.nb[q][r] = N[q][r];
+      e.o[0] = ci; e.o[1] = cj; e.o[2] = ck;
+      bool si = is_surf(e.nb[0], {0, 1, 2}), sj = is_surf(e.nb[1], {0, 1, 2}), sk = is_surf(e.nb[2], {0, 1, 2});
+      auto org = [&](int q) { for (int r = 0; r < 3; ++r) e.o[r] = N[q][r]; };
+      auto setnb = [&](int dst, int src) { for (int r = 0; r < 3; ++r) e.nb[dst][r] = (src < 0) ? 0 : N[src][r]; };
+      int ww = (c.iturb == 0) ? G_WALLWALL_KW4 : G_WALLWALL;
+      if (si && sj && sk) {
+        e.kind = (c.iturb == 0) ? G_WALLWALL_KW8 : G_WALLWALL;
+        emit(e, 2, 6, false);
+      } else if (!si && sj && sk) {
+        org(0); setnb(0, -1); setnb(1, 4); setnb(2, 5); e.kind = ww; emit(e, 2, 3, true);
+      } else if (si && !sj && sk) {
+        org(1); setnb(0, 3); setnb(1, -1); setnb(2, 5); e.kind = ww; emit(e, 2, 3, true);
+      } else if (si && sj && !sk) {
+        org(2); setnb(0, 3); setnb(1, 4); setnb(2, -1); e.kind = ww; emit(e, 2, 3, true);
+      } else if (!si && !sj && sk) {
+        e.face = F_NOFACE;  // the reference's capital-K face label matches no case
+        org(5); e.kind = wall_kind(c);
+        if (e.kind == G_SYMMETRY) { E.err = "corner with only a k-side wall under inviscid walls is undefined in the reference"; return false; }
+        emit(e, 2, 0, false);
+      } else if (si && !sj && !sk) {
+        e.face = (m % 2 == 0) ? F_IMIN : F_IMAX; org(3); e.kind = wall_kind(c); emit(e, 2, 0, false);
+      } else if (!si && sj && !sk) {
+        e.face = (m == 0 || m == 1 || m == 4 || m == 5) ? F_JMIN : F_JMAX; org(4); e.kind = wall_kind(c); emit(e, 2, 0, false);
+      } else {
+        e.kind = G_NOWALL7;
+        emit(e, 2, 6, false);
+      }
+    }
+  }
+  // ---- halos: own 3-deep slab into the donor's ghost cells (src/bc_module.f90:355-463)
+  std::vector<std::vector<Con>> cons(nblocks);
+  for (int b = 0; b < nblocks; ++b) {
+    if (!read_cons(blocks[b], nblocks, cons[b], E.err)) return false;
+    for (auto& g : cons[b])
+      for (int m = 0; m < 3; ++m) {
+        if (g.s[m] != g.e[m]) g.s[m] += 1;
+        if (g.sd[m] != g.ed[m]) { if (g.sd[m] < g.ed[m]) g.sd[m] += 1; else g.ed[m] += 1; }
+      }
+  }
+  for (int b = 0; b < nblocks; ++b) {
+    const BlockGeom& S = E.blk[b];
+    for (auto g : cons[b]) {
+      int ax;
+      if (g.s[1] == g.e[1]) ax = 1;
+      else if (g.s[0] == g.e[0]) ax = 0;
+      else ax = 2;
+      int row = -1, sgn = 0;
+      for (int r = 0; r < 3; ++r) if (g.tm[r][ax] != 0) { row = r; sgn = g.tm[r][ax]; }
+      if (g.s[ax] == 2) { g.e[ax] += 2; g.ed[row] += 2 * sgn; }
+      else { g.s[ax] -= 2; g.sd[row] -= 2 * sgn; }
+      const BlockGeom& D = E.blk[g.donor];
+      for (int k = g.s[2]; k <= g.e[2]; ++k)
+        for (int j = g.s[1]; j <= g.e[1]; ++j)
+          for (int i = g.s[0]; i <= g.e[0]; ++i) {
+            int ii, jj, kk;
+            cmap(g, i, j, k, ii, jj, kk);
+            if (ii < -1 || ii > D.imax + 3 || jj < -1 || jj > D.jmax + 3 || kk < -1 || kk > D.kmax + 3) {
+              E.err = "halo target outside the donor block"; return false;
+            }
+            GhostOp op{};
+            op.kind = G_COPY;
+            op.src = (int)(S.off + (i + 1) + (long long)S.ni * ((j + 1) + (long long)S.nj * (k + 1)));
+            op.dst = (int)(D.off + (ii + 1) + (long long)D.ni * ((jj + 1) + (long long)D.nj * (kk + 1)));
+            op.bnd = op.src;
+            for (int q = 0; q < 6; ++q) op.nb[q] = -1;
+            ops[0].push_back(op);
+          }
+    }
+  }
+  for (int p = 0; p < 3; ++p) {
+    E.nops[p] = (int)ops[p].size();
+    if (E.nops[p] == 0) continue;
+    if (cudaMalloc(&E.d_ops[p], ops[p].size() * sizeof(GhostOp)) != cudaSuccess) { E.err = "cudaMalloc ghost ops"; return false; }
+    cudaMemcpy(E.d_ops[p], ops[p].data(), ops[p].size() * sizeof(GhostOp), cudaMemcpyHostToDevice);
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------------------
+void setup_planes(Engine& E) {
+  long long maxs = 0;
+  for (auto& B : E.blk) maxs = std::max<long long>(maxs, (B.imax - 2) + (B.jmax - 2) + (B.kmax - 2));
+  std::vector<std::vector<int>> pl(maxs + 1);
+  for (auto& B : E.blk)
+    for (int k = 2; k <= B.kmax; ++k)
+      for (int j = 2; j <= B.jmax; ++j)
+        for (int i = 2; i <= B.imax; ++i)
+          pl[(i - 2) + (j - 2) + (k - 2)].push_back((int)(B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1))));
+  std::vector<int> flat;
+  E.plane_off.assign(1, 0);
+  for (auto& p : pl) {
+    flat.insert(flat.end(), p.begin(), p.end());
+    E.plane_off.push_back((long long)flat.size());
+  }
+  cudaMalloc(&E.d_planes, flat.size() * sizeof(int));
+  cudaMemcpy(E.d_planes, flat.data(), flat.size() * sizeof(int), cudaMemcpyHostToDevice);
+}
+
+}  // namespace cfd

@@ -1,0 +1,243 @@
+"""ctypes binding of the engine's C ABI (include/cfd3d.h) and the host driver.
+
+`Engine` wraps one `cfd3d_handle`; `Solver` mirrors the reference's
+`t_solve%solve_equation` (src/solve_module.f90:119-153): physical-time loop, pseudo-time
+loop of `update%timeinteg` + `resi%residual`, convergence test on res(1)/res(2) against
+10^-bond, BDF history shift after each physical step, and the `res.plt` Tecplot log
+(src/residual_module.f90:47-69,168-174).
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is visible, every
+entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from . import build as _build
+
+_lib = None
+
+
+class Cfd3dError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"cfd3d error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    """Load libcfd3d_gb300.so (building it in-tree if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        _build.build()
+    L = C.CDLL(path)
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int)
+    H = C.c_void_p
+    L.cfd3d_create.argtypes = [C.POINTER(abi.Config), C.c_int, C.POINTER(abi.BlockDesc), C.POINTER(H)]
+    L.cfd3d_destroy.argtypes = [H]
+    L.cfd3d_last_error.restype = C.c_char_p
+    L.cfd3d_last_error.argtypes = [H]
+    L.cfd3d_sizes.argtypes = [H, ip, ip, ip, ip, ip]
+    L.cfd3d_initialize.argtypes = [H, C.c_int, dp]
+    L.cfd3d_upload_state.argtypes = [H, C.c_int, dp, dp, dp, dp]
+    L.cfd3d_download_state.argtypes = [H, C.c_int, dp, dp, dp, dp, dp]
+    L.cfd3d_iterate.argtypes = [H, C.c_int, C.c_int, C.c_double, dp, dp, ip]
+    L.cfd3d_iterate_n.argtypes = [H, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]
+    L.cfd3d_unsteady_shift.argtypes = [H]
+    L.cfd3d_residual.argtypes = [H, C.c_int, dp, dp, dp, dp]
+    L.cfd3d_grid_metrics.argtypes = [H, C.c_int, dp, dp, dp, dp]
+    L.cfd3d_eos_eval.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
+    L.cfd3d_stats.argtypes = [H, C.POINTER(C.c_int64), ip]
+    L.cfd3d_time_iterate.argtypes = [H, C.c_int, dp]
+    L.cfd3d_profile_iterate.argtypes = [H, dp]
+    L.cfd3d_set_device.argtypes = [C.c_int]
+    _lib = L
+    return L
+
+
+EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
+           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_iterate", "cfd3d_iterate_n",
+           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_stats",
+           "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device"]
+STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
+
+
+def set_device(dev):
+    """Select the CUDA device for the engines created afterwards on this thread."""
+    rc = lib().cfd3d_set_device(int(dev))
+    if rc:
+        raise Cfd3dError(rc, "cfd3d_set_device failed")
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def eos_eval(p, t, y1, y2, fluid=2, prop=False):
+    """Pointwise mixture EOS on the device: dv (n, 18) and tv (n, 2)."""
+    p, t, y1, y2 = (np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (p, t, y1, y2))
+    n = p.size
+    dv = np.zeros((n, 18))
+    tv = np.zeros((n, 2))
+    rc = lib().cfd3d_eos_eval(fluid, 1, 1 if prop else 0, n, _p(p), _p(t), _p(y1), _p(y2), _p(dv), _p(tv))
+    if rc:
+        raise Cfd3dError(rc, "cfd3d_eos_eval failed")
+    return dv, tv
+
+
+class Engine:
+    """One engine handle over a case (cfd3d_gb300.cases format)."""
+
+    def __init__(self, case, precision=abi.FP64):
+        self.case = case
+        cfgd = dict(case["cfg"])
+        cfgd["precision"] = precision
+        self.cfgd = cfgd
+        self._cfg = abi.config_from_dict(cfgd)
+        self._bs = abi.BlockSet(case["blocks"])
+        h = C.c_void_p()
+        rc = lib().cfd3d_create(C.byref(self._cfg), self._bs.n, self._bs.arr, C.byref(h))
+        self.h = h
+        if rc:
+            msg = lib().cfd3d_last_error(h).decode() if h else "create failed"
+            lib().cfd3d_destroy(h)
+            self.h = None
+            raise Cfd3dError(rc, msg)
+        npv, ndv, ntv, nqq, ngrd = (C.c_int() for _ in range(5))
+        lib().cfd3d_sizes(self.h, C.byref(npv), C.byref(ndv), C.byref(ntv), C.byref(nqq), C.byref(ngrd))
+        self.npv, self.ntv, self.nqq, self.ngrd = npv.value, ntv.value, nqq.value, ngrd.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cfd3d_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _check(self, rc):
+        if rc:
+            raise Cfd3dError(rc, lib().cfd3d_last_error(self.h).decode())
+
+    def initialize(self, pv0=None):
+        for n in range(len(self.case["blocks"])):
+            a = None if pv0 is None else np.ascontiguousarray(pv0[n], dtype=np.float64)
+            self._check(lib().cfd3d_initialize(self.h, n, _p(a)))
+
+    def upload(self, n, pv=None, dv=None, tv=None, qq=None):
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (pv, dv, tv, qq)]
+        self._check(lib().cfd3d_upload_state(self.h, n, *[_p(a) for a in args]))
+
+    def download(self, n, out=None):
+        b = self.case["blocks"][n]
+        if out is None:
+            out = dict(pv=np.zeros(abi.padded_shape(b, self.npv)), dv=np.zeros(abi.padded_shape(b, 18)),
+                       tv=np.zeros(abi.padded_shape(b, max(self.ntv, 1))),
+                       qq=np.zeros(abi.interior_shape(b, max(2 * self.npv * (1 if self.nqq else 0), 1))),
+                       rcav=np.zeros(abi.interior_shape(b, 2)))
+        self._check(lib().cfd3d_download_state(self.h, n, _p(out["pv"]), _p(out["dv"]),
+                                               _p(out["tv"]) if self.ntv else None,
+                                               _p(out["qq"]) if self.nqq else None, _p(out["rcav"])))
+        if self.ntv:
+            out["tv"] = out["tv"][..., :self.ntv]
+        return out
+
+    def download_arrays(self, n, pv=None, dv=None, tv=None, qq=None, rcav=None):
+        """Download into caller-owned contiguous float64 arrays (None skips a field)."""
+        for a in (pv, dv, tv, qq, rcav):
+            assert a is None or (a.dtype == np.float64 and a.flags["C_CONTIGUOUS"])
+        self._check(lib().cfd3d_download_state(self.h, n, _p(pv), _p(dv), _p(tv) if self.ntv else None,
+                                               _p(qq) if self.nqq else None, _p(rcav)))
+
+    def residual(self, n=0):
+        b = self.case["blocks"][n]
+        res = np.zeros(abi.interior_shape(b, self.npv))
+        icav = np.zeros(abi.interior_shape(b, 4))
+        itt = np.zeros(abi.interior_shape(b, 4))
+        oc = np.zeros(abi.interior_shape(b, 1))
+        self._check(lib().cfd3d_residual(self.h, n, _p(res), _p(icav), _p(itt), _p(oc)))
+        return dict(res=res, icav=icav, itt=itt, omega_cut=oc[..., 0])
+
+    def metrics(self, n):
+        b = self.case["blocks"][n]
+        im, jm, km = b["imax"], b["jmax"], b["kmax"]
+        cx = np.zeros((km + 1, jm + 1, im, 3))
+        ex = np.zeros((km + 1, jm, im + 1, 3))
+        tx = np.zeros((km, jm + 1, im + 1, 3))
+        grd = np.zeros((km + 1, jm + 1, im + 1, self.ngrd))
+        self._check(lib().cfd3d_grid_metrics(self.h, n, _p(cx), _p(ex), _p(tx), _p(grd)))
+        return cx, ex, tx, grd
+
+    def iterate(self, nt_phy=1, nt=1, timeprev=0.0):
+        t = C.c_double(0.0)
+        res = np.zeros(self.npv)
+        loc = (C.c_int * 4)()
+        self._check(lib().cfd3d_iterate(self.h, nt_phy, nt, timeprev, C.byref(t), _p(res), loc))
+        return t.value, res, tuple(loc)
+
+    def iterate_n(self, niter, nt_phy=1, nt0=1, timeprev=0.0):
+        t = C.c_double(0.0)
+        res = np.zeros(self.npv)
+        self._check(lib().cfd3d_iterate_n(self.h, niter, nt_phy, nt0, timeprev, C.byref(t), _p(res)))
+        return t.value, res
+
+    def unsteady_shift(self):
+        self._check(lib().cfd3d_unsteady_shift(self.h))
+
+    def time_iterate(self, niter):
+        ms = C.c_double(0.0)
+        self._check(lib().cfd3d_time_iterate(self.h, niter, C.byref(ms)))
+        return ms.value
+
+    def profile_iterate(self):
+        out = np.zeros(len(STAGES))
+        self._check(lib().cfd3d_profile_iterate(self.h, _p(out)))
+        return dict(zip(STAGES, out))
+
+    def stats(self):
+        fb = C.c_int64()
+        nl = C.c_int()
+        self._check(lib().cfd3d_stats(self.h, C.byref(fb), C.byref(nl)))
+        return dict(snd2_fallbacks=fb.value, launches_per_iter=nl.value)
+
+
+class Solver:
+    """The reference's solve loop (src/solve_module.f90:119-153) over an Engine."""
+
+    def __init__(self, case, precision=abi.FP64, log_path=None):
+        self.engine = Engine(case, precision)
+        self.cfg = case["cfg"]
+        self.case = case
+        self.log_path = log_path
+        self.history = []
+
+    def solve(self, npmax=None, ntmax=None, pv0=None):
+        e = self.engine
+        e.initialize(self.case.get("pv0") if pv0 is None else pv0)
+        nsteady = self.cfg.get("nsteady", 0)
+        npmax = npmax or self.cfg.get("npmax", 1)
+        ntmax = ntmax or self.cfg.get("ntmax", 1)
+        bond = 10.0 ** (-self.cfg.get("bond", 12))
+        log = open(self.log_path, "w") if self.log_path else None
+        if log:
+            names = ["nt", "resp", "resu", "resv", "resw", "rest", "resy1", "resy2"] + (["resk", "reso"] if e.npv == 9 else [])
+            log.write(" variables=" + ",".join('"%s"' % x for x in names) + "\n zone t =\"newstart\"\n")
+        time = 0.0
+        for nt_phy in range(1, npmax + 1):
+            for nt in range(1, ntmax + 1):
+                time, res, loc = e.iterate(nt_phy, nt, 0.0)
+                it = ntmax * (nt_phy - 1) + nt
+                self.history.append((it, time, res.copy(), loc))
+                if log:
+                    log.write("%10d" % it + "".join("%30.12f" % r for r in res) + "\n")
+                if res[0] < bond or res[1] < bond:
+                    break
+            if nsteady >= 1:
+                e.unsteady_shift()
+        if log:
+            log.close()
+        return self.history

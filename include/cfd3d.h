@@ -168,6 +168,21 @@ int  cfd3d_eos_eval(int fluid, int ngas, int with_prop, int64_t n, const double 
  * (src/eos_module.f90:1104-1111), and the kernel launches of one iteration. */
 int  cfd3d_stats(const cfd3d_handle *h, int64_t *snd2_fallbacks, int *launches_per_iter);
 
+/* Select the CUDA device used by the handles created afterwards on the calling thread
+ * (one GPU per process; the reference's MPI rank -> GPU mapping). */
+int  cfd3d_set_device(int device);
+
+/* Timing on the handle's own stream (CUDA events, graph replays): milliseconds for
+ * niter back-to-back pseudo-iterations.  No reference counterpart (measurement only). */
+int  cfd3d_time_iterate(cfd3d_handle *h, int niter, double *ms);
+
+/* One pseudo-iteration launched stage by stage with CUDA events between the stages;
+ * stage_ms[CFD3D_NSTAGES] receives: time step, boundary program, face fluxes, residual
+ * + sources, forward sweep, backward sweep, update + EOS, eddy + norms.
+ * No reference counterpart (measurement only). */
+#define CFD3D_NSTAGES 8
+int  cfd3d_profile_iterate(cfd3d_handle *h, double *stage_ms);
+
 #ifdef __cplusplus
 }
 #endif
