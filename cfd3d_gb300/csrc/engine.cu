@@ -561,6 +561,28 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
     }
   }
   for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
+  if (!d.prep) return;
+  // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous term)
+  double tvc[3] = {0.0, 0.0, 0.0};
+  for (int q = 0; q < c.ntv; ++q) tvc[q] = d.tv[q * n + g];
+  double fc[18];
+  for (int q = 0; q < 3; ++q) {
+    fc[q] = d.gm[(GM_CX + q) * n + g - 1]; fc[3 + q] = d.gm[(GM_CX + q) * n + g];
+    fc[6 + q] = d.gm[(GM_EX + q) * n + g - sj]; fc[9 + q] = d.gm[(GM_EX + q) * n + g];
+    fc[12 + q] = d.gm[(GM_TX + q) * n + g - sk]; fc[15 + q] = d.gm[(GM_TX + q) * n + g];
+  }
+  double ic[4] = {0, 0, 0, 0}, it4[4] = {0, 0, 0, 0};
+  if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
+  if (c.iturb == 0) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
+  Diag D;
+  diag_prepare(c, pv2, dv, tvc, fc, vol, d.dt[g], ic, it4, D);
+  double o[NPREP];
+  diag_to_array(D, o);
+  for (int q = 0; q < 6; ++q) o[PREP_SPEC + q] = face_spectral(c, fc + 3 * q, pv2, dv);
+  double sndp2 = sndp2_of<double>(c, dv[5], pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3]);
+  o[PREP_BETA] = 1.0 / sndp2 - 1.0 / dv[5] + dv[6];
+  o[PREP_EVV] = 2.0 * eigenvis_of(c, dv, tvc) / vol;
+  for (int q = 0; q < NPREP; ++q) d.prep[q * n + g] = o[q];
 }
 
 // ------------------------------------------------------------------ LU-SGS sweeps
@@ -568,7 +590,7 @@ __device__ __forceinline__ void load_nbr(const DevPtr& d, const Par& c, long lon
                                          double* tv, double& vol) {
   const long long n = d.ncell;
   for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
-  for (int v = 0; v < 12; ++v) dv[v] = d.dv[v * n + g];
+  for (int v = 0; v < 14; ++v) dv[v] = d.dv[v * n + g];
   tv[0] = tv[1] = tv[2] = 0.0;
   for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
   vol = d.gm[GM_GRD * n + g];
@@ -594,38 +616,30 @@ __global__ void __launch_bounds__(128) k_sweep(DevPtr d, Par c, const int* __res
   const int pos[3] = {i, j, k};
   const int lim[3] = {B.imax, B.jmax, B.kmax};
   const int plane[3] = {GM_CX, GM_EX, GM_TX};
-#pragma unroll 1
+#pragma unroll
   for (int q = 0; q < 3; ++q) {
-    // forward: lower neighbour across face (g - s); backward: upper neighbour across face (g)
+    // forward: lower neighbour, its + face; backward: upper neighbour, its - face
     const bool interior = FWD ? (pos[q] - 1 >= 2) : (pos[q] + 1 <= lim[q]);
     if (!interior) continue;  // dq is zero outside the block
     const long long nb = FWD ? g - strides[q] : g + strides[q];
     const long long fidx = FWD ? nb : g;
     double nx[3];
     face_vec(d, plane[q], fidx, nx);
-    double pv[NPVM], dv[12], tv[3], vol, dq[NPVM];
-    load_nbr(d, c, nb, pv, dv, tv, vol);
-    for (int v = 0; v < npv; ++v) dq[v] = d.dqs[v * n + nb];
-    if (FWD) jac_apply(c, nx, vol, pv, dv, tv, 1.0, dq, acc, 1.0);
-    else jac_apply(c, nx, vol, pv, dv, tv, -1.0, dq, acc, -1.0);
+    double pv[NPVM], dv[14], dq[NPVM];
+    for (int v = 0; v < npv; ++v) { pv[v] = d.pv[v * n + nb]; dq[v] = d.dqs[v * n + nb]; }
+    for (int v = 0; v < 14; ++v) dv[v] = d.dv[v * n + nb];
+    const double spec = d.prep[(PREP_SPEC + 2 * q + (FWD ? 1 : 0)) * n + nb];
+    const double beta = d.prep[PREP_BETA * n + nb];
+    const double evv = d.prep[PREP_EVV * n + nb];
+    jac_apply_pre(npv, nx, pv, dv, spec, beta, evv, FWD ? 1.0 : -1.0, dq, acc);
   }
   if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * n + g] = acc[v];
-  // diagonal block
-  double pv[NPVM], dv[NDV], tv[3] = {0.0, 0.0, 0.0};
+  double pv[NPVM], dv[14], o[PREP_DIAG];
   for (int v = 0; v < npv; ++v) pv[v] = d.pv[v * n + g];
   for (int v = 0; v < 14; ++v) dv[v] = d.dv[v * n + g];
-  for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
-  double fc[18];
-  for (int q = 0; q < 3; ++q) {
-    fc[q] = d.gm[(GM_CX + q) * n + g - 1]; fc[3 + q] = d.gm[(GM_CX + q) * n + g];
-    fc[6 + q] = d.gm[(GM_EX + q) * n + g - sj]; fc[9 + q] = d.gm[(GM_EX + q) * n + g];
-    fc[12 + q] = d.gm[(GM_TX + q) * n + g - sk]; fc[15 + q] = d.gm[(GM_TX + q) * n + g];
-  }
-  double ic[4] = {0, 0, 0, 0}, it[4] = {0, 0, 0, 0};
-  if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
-  if (c.iturb == 0) for (int q = 0; q < 4; ++q) it[q] = d.itt[q * n + g];
+  for (int q = 0; q < PREP_DIAG; ++q) o[q] = d.prep[q * n + g];
   Diag D;
-  diag_prepare(c, pv, dv, tv, fc, d.gm[GM_GRD * n + g], d.dt[g], ic, it, D);
+  diag_from_array(o, D);
   double x[NPVM];
   diag_solve(c, D, pv, dv, acc, x);
   for (int v = 0; v < npv; ++v) d.dqs[v * n + g] = x[v];
@@ -1003,7 +1017,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   bool ok = alloc(E.d.pv, c.npv) && alloc(E.d.dv, NDV) && alloc(E.d.tv, std::max(c.ntv, 1)) &&
             alloc(E.d.gm, GM_GRD + c.ngrd) && alloc(E.d.res, c.npv) && alloc(E.d.icav, 4) && alloc(E.d.itt, 4) &&
             alloc(E.d.ocut, 1) && alloc(E.d.dt, 1) && alloc(E.d.rcav, 2) && alloc(E.d.qq, std::max(2 * c.npv * (c.nqq ? 1 : 0), 1)) &&
-            alloc(E.d.dqs, c.npv) && alloc(E.d.dcv, c.npv) && alloc(E.d.fi, 3 * c.npv) &&
+            alloc(E.d.dqs, c.npv) && alloc(E.d.dcv, c.npv) && alloc(E.d.fi, 3 * c.npv) && alloc(E.d.prep, NPREP) &&
             alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
   if (!ok) { E.err = "device allocation failed"; return CFD3D_ERR_NOMEM; }
   E.d.ncell = n;
@@ -1048,7 +1062,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   Engine& E = h->E;
   if (E.graph) cudaGraphExecDestroy(E.graph);
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
-                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
+                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.prep, E.d.partial, h->staging};
   for (double* p : bufs) cudaFree(p);
   cudaFree((void*)E.d.blk);
   cudaFree(E.d.sc);

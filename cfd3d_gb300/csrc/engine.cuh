@@ -60,7 +60,7 @@ struct Scalars {
 };
 
 struct DevPtr {
-  double *pv, *dv, *tv, *gm, *res, *icav, *itt, *ocut, *dt, *rcav, *qq, *dqs, *dcv, *qold, *fi, *fv;
+  double *pv, *dv, *tv, *gm, *res, *icav, *itt, *ocut, *dt, *rcav, *qq, *dqs, *dcv, *qold, *fi, *fv, *prep;
   const BlockGeom* blk;
   int nblk;
   long long ncell;

@@ -603,6 +603,67 @@ __device__ __forceinline__ void diag_solve(const Par& c, const Diag& D, const do
   for (int n = 0; n < c.npv; ++n) x[n] *= D.a;
 }
 
+// per-cell LU-SGS coefficients computed once per iteration (k_rhs) and read by the sweeps
+constexpr int PREP_DIAG = 23;                 // Diag fields
+constexpr int PREP_SPEC = PREP_DIAG;          // 6 spectral radii 1.05(|u'|+d): i-,i+,j-,j+,k-,k+
+constexpr int PREP_BETA = PREP_SPEC + 6;      // 1/sndp2 - 1/c^2 + drho/dp
+constexpr int PREP_EVV = PREP_BETA + 1;       // 2 * eigenvis / vol
+constexpr int NPREP = PREP_EVV + 1;
+
+__device__ __forceinline__ void diag_to_array(const Diag& D, double* o) {
+  o[0] = D.a; o[1] = D.b1; o[2] = D.i_b1; o[3] = D.ss; o[4] = D.rr; o[5] = D.cross; o[6] = D.cross1;
+  o[7] = D.cross2; o[8] = D.ssy1; o[9] = D.ssy2; o[10] = D.ssh; o[11] = D.aaa1; o[12] = D.aaa2; o[13] = D.mm;
+  for (int q = 0; q < 4; ++q) { o[14 + q] = D.c[q]; o[19 + q] = D.t[q]; }
+  o[18] = D.tt;
+}
+__device__ __forceinline__ void diag_from_array(const double* o, Diag& D) {
+  D.a = o[0]; D.b1 = o[1]; D.i_b1 = o[2]; D.ss = o[3]; D.rr = o[4]; D.cross = o[5]; D.cross1 = o[6];
+  D.cross2 = o[7]; D.ssy1 = o[8]; D.ssy2 = o[9]; D.ssh = o[10]; D.aaa1 = o[11]; D.aaa2 = o[12]; D.mm = o[13];
+  for (int q = 0; q < 4; ++q) { D.c[q] = o[14 + q]; D.t[q] = o[19 + q]; }
+  D.tt = o[18];
+}
+
+// spectral radius of the split Jacobian for one face: 1.05 (|u'| + d)
+__device__ __forceinline__ double face_spectral(const Par& c, const double* nx, const double* pv, const double* dv) {
+  double ds = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
+  double u = nx[0] * pv[1] + nx[1] * pv[2] + nx[2] * pv[3];
+  double sndp2 = sndp2_of<double>(c, dv[5], pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
+  double up = 0.5 * (1.0 + sndp2 / dv[5]) * u;
+  double d = 0.5 * sqrt(u * u * sq(1.0 - sndp2 / dv[5]) + 4.0 * sndp2 * ds);
+  return 1.05 * (fabs(up) + d);
+}
+
+// acc += sign_acc * 0.5 * A dq with the precomputed spectral radius `spec`, beta and
+// evv = 2 eigenvis / vol of the neighbour (same algebra as jac_apply)
+__device__ __forceinline__ void jac_apply_pre(int npv, const double* nx, const double* pv, const double* dv,
+                                              double spec, double beta, double evv, double sign,
+                                              const double* dq, double* acc) {
+  double ds = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
+  double u = nx[0] * pv[1] + nx[1] * pv[2] + nx[2] * pv[3];
+  double lamda = sign * spec;
+  double vis = sign * evv * ds;
+  double uuu = u + lamda + vis;
+  double lv = lamda + vis;
+  double r0 = (u * dv[6] + lamda * beta + vis * dv[6]) * dq[0] + nx[0] * dv[0] * dq[1] + nx[1] * dv[0] * dq[2] +
+              nx[2] * dv[0] * dq[3] + (u * dv[7] + lv * dv[7]) * dq[4] + (u * dv[8] + lv * dv[8]) * dq[5] +
+              (u * dv[9] + lv * dv[9]) * dq[6];
+  double ru = dv[0] * uuu;
+  double h = dv[1] + 0.5 * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
+  double s = 0.5 * sign;  // forward: +A+ ; backward: -A- (sign = -1 for both factors)
+  acc[0] += s * r0;
+  acc[1] += s * (pv[1] * r0 + nx[0] * dq[0] + ru * dq[1]);
+  acc[2] += s * (pv[2] * r0 + nx[1] * dq[0] + ru * dq[2]);
+  acc[3] += s * (pv[3] * r0 + nx[2] * dq[0] + ru * dq[3]);
+  acc[4] += s * (ru * (dv[10] * dq[0] + pv[1] * dq[1] + pv[2] * dq[2] + pv[3] * dq[3] + dv[11] * dq[4] +
+                       dv[12] * dq[5] + dv[13] * dq[6]) + h * r0 - lv * dq[0]);
+  acc[5] += s * (pv[5] * r0 + ru * dq[5]);
+  acc[6] += s * (pv[6] * r0 + ru * dq[6]);
+  if (npv > 7) {
+    acc[7] += s * (pv[7] * r0 + ru * dq[7]);
+    acc[8] += s * (pv[8] * r0 + ru * dq[8]);
+  }
+}
+
 // acc += sign_acc * A(sign) dq for the neighbour cell state (pv, dv, tv, vol) across face nx
 __device__ __forceinline__ void jac_apply(const Par& c, const double* nx, double vol, const double* pv,
                                           const double* dv, const double* tv, double sign, const double* dq,

@@ -100,7 +100,7 @@ def test_iterations_match(oracle, name):
         tg, resg, locg = e.iterate(1, it + 1, 0.0)
         to, reso, loco = o.iterate(1, it + 1, 0.0)
         assert abs(tg - to) <= 1e-9 * abs(to)
-        assert rel_err(resg, reso, floor=1e-300).max() < 1e-7, (it, resg, reso)
+        assert np.allclose(resg, reso, rtol=1e-7, atol=1e-9 * np.abs(reso).max()), (it, resg, reso)
     for b in range(len(c["blocks"])):
         sg = e.download(b)
         so = o.get_state(b)
