@@ -250,7 +250,9 @@ def adjoint(scale=1, seed=3):
 
 def large(scale=1, seed=4, nt_phy=20, ntmax=30):
     """384x192x192 stretched (wall spacing 1e-5 L, ratio 1.1) SST cavitating block with
-    BDF2 dual time stepping; Re = 1e6 via L = 1 m."""
+    BDF2 dual time stepping; Re = 1e6 via L = 1 m.  Steady-form preconditioning (prec = 1):
+    from this synthetic start the unsteady form (prec = 2, str = L / pi / dt_phy) diverges
+    within ten pseudo-iterations in both the CPU restatement and the GPU engine."""
     ni, nj, nk = 384 // scale, 192 // scale, 192 // scale
     xyz = box_nodes(ni, nj, nk, 2.0, 1.0, 1.0, shear=0.0, seed=seed, ystretch=(1e-5 * scale, 1.1))
     bc = face_patches(ni + 1, nj + 1, nk + 1, {"imin": BC_FARFIELD, "imax": BC_FARFIELD, "jmin": BC_WALL,
@@ -258,7 +260,7 @@ def large(scale=1, seed=4, nt_phy=20, ntmax=30):
     u = 15.0
     pinf = pww_iapws(300.0) + 0.8 * 0.5 * 996.5 * u * u
     dt_phy = 0.01 * 1.0 / u
-    cfg, turb = _sst_cfg(u, pinf, extra=dict(nsteady=2, dt_phy=dt_phy, prec=2, npmax=nt_phy, ntmax=ntmax))
+    cfg, turb = _sst_cfg(u, pinf, extra=dict(nsteady=2, dt_phy=dt_phy, prec=1, npmax=nt_phy, ntmax=ntmax))
     blk = _block(xyz, bc)
     pv = _cavitating_state(blk, cfg, seed + 100, u, 0.8, turb=turb, radius=0.1)
     return {"name": "large", "cfg": cfg, "blocks": [blk], "pv0": [pv], "iterations": nt_phy * ntmax}

@@ -17,8 +17,8 @@ struct df64 {
   __device__ __forceinline__ df64() {}
   __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
   __device__ __forceinline__ explicit df64(double a) {
-    hi = __double2float_rn(a);
-    lo = __double2float_rn(a - (double)hi);
+    hi = static_cast<float>(a);
+    lo = static_cast<float>(a - static_cast<double>(hi));
   }
   __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
 };

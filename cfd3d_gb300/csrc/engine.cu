@@ -83,6 +83,7 @@ __global__ void k_eos_points(int fluid, int with_prop, long long n, const double
 
 // ------------------------------------------------------------------ initial state
 // set_others (src/initial_module.f90:707-771) on the uploaded interior pv
+template <bool MX>
 __global__ void k_init(DevPtr d, Par c, int b) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const BlockGeom& B = d.blk[b];
@@ -92,7 +93,7 @@ __global__ void k_init(DevPtr d, Par c, int b) {
   const long long n = d.ncell;
   double pv[NPVM], dv[NDV], tv[3] = {0.0, 0.0, 0.0};
   for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
-  deteos(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
+  deteos<MX>(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
   if (c.iturb == 0) tv[2] = c.emutref;
   for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
   for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
@@ -316,7 +317,7 @@ __device__ __forceinline__ long long stencil_cell(int l, long long g, long long 
   return g + ((l == 36) ? -2 : 3) * sn;
 }
 
-template <int DIR>
+template <int DIR, bool MX>
 __global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   // flat face numbering per direction: block-major, then (k, j, i) of the left cell
@@ -356,11 +357,18 @@ __global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
       c9[v] = x[8]; c10[v] = x[9];
     }
     muscl_clip<double>(c, c9, c10, L.pv, R.pv);
-    double dl_[NDV], dr_[NDV];
-    deteos_simple(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], dl_, &d.sc->snd2_fallbacks);
-    deteos_simple(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], dr_, &d.sc->snd2_fallbacks);
-    L.rho = dl_[0]; L.h = dl_[1]; L.c2 = dl_[5];
-    R.rho = dr_[0]; R.h = dr_[1]; R.c2 = dr_[5];
+    if (c.nscheme == 2 || c.nscheme == 3) {
+      // Roe-M and AUSMPW+ also read the face sound speeds
+      double dl_[NDV], dr_[NDV];
+      deteos_simple<MX>(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], dl_, &d.sc->snd2_fallbacks);
+      deteos_simple<MX>(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], dr_, &d.sc->snd2_fallbacks);
+      L.rho = dl_[0]; L.h = dl_[1]; L.c2 = dl_[5];
+      R.rho = dr_[0]; R.h = dr_[1]; R.c2 = dr_[5];
+    } else {
+      eos_rho_h<MX>(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], L.rho, L.h);
+      eos_rho_h<MX>(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], R.rho, R.h);
+      L.c2 = R.c2 = 0.0;
+    }
   } else {
     for (int v = 0; v < npv; ++v) { L.pv[v] = d.pv[v * n + g]; R.pv[v] = d.pv[v * n + gr]; }
     L.rho = d.dv[g]; L.h = d.dv[n + g]; L.c2 = d.dv[5 * n + g];
@@ -372,7 +380,7 @@ __global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
     for (int l = 0; l < 18; ++l) sdst[l] = d.pv[stencil_cell(l, g, sn, s1, s2)];
   }
   double fx[NPVM];
-  inviscid_flux(c, nx, L, R, sdst, fx, &d.sc->snd2_fallbacks);
+  inviscid_flux<MX>(c, nx, L, R, sdst, fx, &d.sc->snd2_fallbacks);
   double* fi = d.fi + (long long)DIR * npv * n;
   for (int v = 0; v < npv; ++v) fi[v * n + g] = fx[v];
   if (c.iturb == -3) return;
@@ -646,6 +654,7 @@ __global__ void __launch_bounds__(128) k_sweep(DevPtr d, Par c, const int* __res
 }
 
 // ------------------------------------------------------------------ update + residual
+template <bool MX>
 __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int npv = c.npv;
@@ -669,7 +678,7 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
     }
     double dv[NDV], tv[3] = {0.0, 0.0, 0.0};
     for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
-    deteos(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
+    deteos<MX>(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
     for (int v = 0; v < npv; ++v) {
       d.pv[v * n + g] = p[v];
       double df = fabs(old[v] - p[v]);
@@ -849,9 +858,15 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   for (int p = 0; p < 3; ++p)
     if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
   stage(2);
-  k_face_flux<0><<<nblk_of(E.nface[0], T), T, 0, s>>>(d, c);
-  k_face_flux<1><<<nblk_of(E.nface[1], T), T, 0, s>>>(d, c);
-  k_face_flux<2><<<nblk_of(E.nface[2], T), T, 0, s>>>(d, c);
+  if (c.mixed) {
+    k_face_flux<0, true><<<nblk_of(E.nface[0], T), T, 0, s>>>(d, c);
+    k_face_flux<1, true><<<nblk_of(E.nface[1], T), T, 0, s>>>(d, c);
+    k_face_flux<2, true><<<nblk_of(E.nface[2], T), T, 0, s>>>(d, c);
+  } else {
+    k_face_flux<0, false><<<nblk_of(E.nface[0], T), T, 0, s>>>(d, c);
+    k_face_flux<1, false><<<nblk_of(E.nface[1], T), T, 0, s>>>(d, c);
+    k_face_flux<2, false><<<nblk_of(E.nface[2], T), T, 0, s>>>(d, c);
+  }
   stage(3);
   k_rhs<<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
   stage(4);
@@ -868,7 +883,8 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
     if (b > a) { k_sweep<false><<<nblk_of(b - a, T), T, 0, s>>>(d, c, E.d_planes, a, b); ++n; }
   }
   stage(6);
-  k_update<<<E.red_grid, T, 0, s>>>(d, c);
+  if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c);
+  else k_update<false><<<E.red_grid, T, 0, s>>>(d, c);
   ++n;
   stage(7);
   if (c.iturb == 0) { k_eddy<<<nblk_of(E.nint, T), T, 0, s>>>(d, c); ++n; }
@@ -913,6 +929,8 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   if (in->local < -1 || in->local > 1) { err = "local out of range"; return false; }
   if (in->prec < 0 || in->prec > 2) { err = "prec out of range"; return false; }
   if (in->nsteady >= 1 && !(in->dt_phy > 0.0)) { err = "dual time stepping needs dt_phy > 0"; return false; }
+  if (in->precision != CFD3D_FP64 && in->precision != CFD3D_MIXED) { err = "precision must be CFD3D_FP64 or CFD3D_MIXED"; return false; }
+  c.mixed = (in->precision == CFD3D_MIXED);
   c.nqq = in->nsteady >= 1 ? 2 : 0;
   c.ngrd = (in->iturb == 0) ? 5 : 4;
   c.nsteady = in->nsteady; c.iturb = in->iturb; c.nscheme = in->nscheme; c.nmuscl = in->nmuscl; c.nlim = in->nlim;
@@ -1106,7 +1124,8 @@ int cfd3d_initialize(cfd3d_handle* h, int block, const double* pv_interior) {
   if (rc) return rc;
   CFD_CUDA(cudaMemcpyAsync(h->staging, src, (size_t)nint * c.npv * 8, cudaMemcpyHostToDevice, E.st));
   k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, c.npv, B, E.d.pv, E.ncell, 1);
-  k_init<<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block);
+  if (c.mixed) k_init<true><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block);
+  else k_init<false><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block);
   CFD_CUDA(cudaStreamSynchronize(E.st));
   CFD_CUDA(cudaGetLastError());
   // reset the solution-time accumulator of the local time step

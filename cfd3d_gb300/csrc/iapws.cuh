@@ -108,7 +108,7 @@ __device__ __forceinline__ T cpow(T x, T xi) {
 template <class T>
 struct GAcc { T x, xx, y, yy, xy; };
 
-template <class T, const IJN* TAB, size_t K>
+template <class T, const IJN* TAB, size_t K, bool FULL>
 __device__ __forceinline__ void gterm(T x, T xi, T y, T yi, GAcc<T>& a) {
   constexpr int I = TAB[K].i;
   constexpr int J = TAB[K].j;
@@ -118,19 +118,19 @@ __device__ __forceinline__ void gterm(T x, T xi, T y, T yi, GAcc<T>& a) {
   if constexpr (I != 0) {
     T tx = T(double(I)) * t * xi;
     a.x += tx;
-    if constexpr (I != 1) a.xx += T(double(I - 1)) * tx * xi;
-    if constexpr (J != 0) a.xy += T(double(J)) * tx * yi;
+    if constexpr (FULL && I != 1) a.xx += T(double(I - 1)) * tx * xi;
+    if constexpr (FULL && J != 0) a.xy += T(double(J)) * tx * yi;
   }
   if constexpr (J != 0) {
     T ty = T(double(J)) * t * yi;
     a.y += ty;
-    if constexpr (J != 1) a.yy += T(double(J - 1)) * ty * yi;
+    if constexpr (FULL && J != 1) a.yy += T(double(J - 1)) * ty * yi;
   }
 }
 
-template <class T, const IJN* TAB, size_t... K>
+template <class T, const IJN* TAB, bool FULL = true, size_t... K>
 __device__ __forceinline__ void gsum(T x, T xi, T y, T yi, GAcc<T>& a, std::index_sequence<K...>) {
-  (gterm<T, TAB, K>(x, xi, y, yi, a), ...);
+  (gterm<T, TAB, K, FULL>(x, xi, y, yi, a), ...);
 }
 
 template <class T>
@@ -165,55 +165,57 @@ __device__ __forceinline__ double h2o_sigma(double t) {
          2.62005668908913e-13 * t4 + 2.97878955533757e-16 * t5;
 }
 
-// region 1 (liquid)
-template <class T>
+// region 1 (liquid); FULL = false evaluates only rho and h
+template <class T, bool FULL = true>
 __device__ __forceinline__ void iapws_l(T p, T t, Phase<T>& e) {
   T pi = p * T(0.00000006049607);
   T tau = T(1386.0) / t;
   T x = T(7.1) - pi, xi = T(1.0) / x;
   T y = tau - T(1.222), yi = T(1.0) / y;
-  GAcc<T> a = {T(0), T(0), T(0), T(0), T(0)};
-  gsum<T, kR1>(x, xi, y, yi, a, std::make_index_sequence<34>{});
+  GAcc<T> a = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
+  gsum<T, kR1, FULL>(x, xi, y, yi, a, std::make_index_sequence<34>{});
   // d/dpi = -d/dx
   T gp = -a.x, gpp = a.xx, gt = a.y, gtt = a.yy, gpt = -a.xy;
   T gp1 = T(1.0) / gp;
   e.rho = T((double)25.841246054191803727f) * tau * gp1;
   e.h = T(639675.036) * gt;
+  if constexpr (!FULL) return;
   e.drdp = -(gpp * T(1.5632937721834122e-6) * tau * (gp1 * gp1));
   e.drdt = -(e.rho * T(7.215007215007215e-4) * tau) + T((double)0.01864447767257706f) * gpt * (tau * tau * tau) * (gp1 * gp1);
   e.dhdp = T((double)0.03869782431941923775f) * gpt;
   e.dhdt = -(T(461.526) * (tau * tau) * gtt);
 }
 
-// region 2 / metastable vapour
-template <class T>
-__device__ __forceinline__ void iapws_v(T p, T t, Phase<T>& e) {
-  T pww = h2o_pww(t);
+// region 2 / metastable vapour; `meta` = p > p_sat(T) selects the metastable set
+template <class T, bool FULL = true>
+__device__ __forceinline__ void iapws_v_meta(T p, T t, bool meta, Phase<T>& e) {
   T pi = p * T(1e-6);
   T tau = T(540.0) / t;
   T pi1 = T(1.0e6) / p;
   T taui = T(1.0) / tau;
   T y = tau - T(0.5), yi = T(1.0) / y;
-  GAcc<T> id = {T(0), T(0), T(0), T(0), T(0)};
-  GAcc<T> rs = {T(0), T(0), T(0), T(0), T(0)};
-  if (p > pww) {
-    gsum<T, kR2MI>(pi, pi1, tau, taui, id, std::make_index_sequence<9>{});
-    gsum<T, kR2MR>(pi, pi1, y, yi, rs, std::make_index_sequence<13>{});
+  GAcc<T> id = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
+  GAcc<T> rs = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
+  if (meta) {
+    gsum<T, kR2MI, FULL>(pi, pi1, tau, taui, id, std::make_index_sequence<9>{});
+    gsum<T, kR2MR, FULL>(pi, pi1, y, yi, rs, std::make_index_sequence<13>{});
   } else {
-    gsum<T, kR2I>(pi, pi1, tau, taui, id, std::make_index_sequence<9>{});
-    gsum<T, kR2R>(pi, pi1, y, yi, rs, std::make_index_sequence<43>{});
+    gsum<T, kR2I, FULL>(pi, pi1, tau, taui, id, std::make_index_sequence<9>{});
+    gsum<T, kR2R, FULL>(pi, pi1, y, yi, rs, std::make_index_sequence<43>{});
   }
   T g0p = pi1, g0pp = -(pi1 * pi1);
   T gp = g0p + rs.x, gpp = g0pp + rs.xx, gt = id.y + rs.y, gtt = id.yy + rs.yy, gpt = rs.xy;
   T gp1 = T(1.0) / gp;
   e.rho = T(4.01245401527075799) * tau * gp1;
   e.h = T(249224.04) * gt;
+  if constexpr (!FULL) return;
   e.drdp = -(gpp * T(4.01245401527075799e-6) * tau * (gp1 * gp1));
   e.drdt = -(e.rho * T((double)0.00185185185185185185f) * tau) +
            T((double)0.0074304703986495518f) * gpt * (tau * tau * tau) * (gp1 * gp1);
   e.dhdp = T(0.24922404) * gpt;
   e.dhdt = -(T(461.526) * (tau * tau) * gtt);
 }
+
 
 template <class T>
 __device__ __forceinline__ void ideal_gas(T p, T t, Phase<T>& e) {

@@ -16,6 +16,7 @@
 // a diagonal, so A*dq costs O(npv) instead of the reference's O(npv^2).
 #pragma once
 #include "iapws.cuh"
+#include "df64.cuh"
 
 namespace cfd {
 
@@ -26,6 +27,7 @@ constexpr int NDV = 18;
 struct Par {
   int npv, ntv, nqq, ngrd;
   int nsteady, iturb, nscheme, nmuscl, nlim, local, prec, fluid, ncav, fix_cav_clamp, with_prop;
+  int mixed;   // 1: the mixed-precision form (IF97 sums in df64)
   double dt_phy, cfl, c_v, c_c, pref, uref, str, rhoref, l_chord;
   double kref, oref, emutref;
   double uref_vec[3], tref, y1ref, y2ref;   // free-stream state bcinfo%pv (src/bc_module.f90:133-146)
@@ -48,13 +50,39 @@ __device__ __forceinline__ R sndp2_du_of(const Par& c, R snd2, R u2) {
 // ------------------------------------------------------------------ mixture EOS
 struct EosCount { unsigned long long* fallbacks; };
 
-template <class T>
-__device__ __forceinline__ void phase_l(int fluid, T p, T t, Phase<T>& e) {
-  if (fluid == 1) stiffened(p, t, e); else iapws_l(p, t, e);
+// IF97 liquid and vapour phases with the Gibbs sums in df64 on the FP32 pipes; one
+// out-of-line copy per FULL flag keeps the expanded sums out of every caller
+template <bool FULL>
+__device__ __noinline__ void iapws_pair_df64(double p, double t, bool meta, Phase<double>& l, Phase<double>& v) {
+  Phase<df64> lx, vx;
+  const df64 P(p), T(t);
+  iapws_l<df64, FULL>(P, T, lx);
+  iapws_v_meta<df64, FULL>(P, T, meta, vx);
+  l.rho = (double)lx.rho; l.h = (double)lx.h;
+  v.rho = (double)vx.rho; v.h = (double)vx.h;
+  if constexpr (FULL) {
+    l.drdp = (double)lx.drdp; l.drdt = (double)lx.drdt; l.dhdp = (double)lx.dhdp; l.dhdt = (double)lx.dhdt;
+    v.drdp = (double)vx.drdp; v.drdt = (double)vx.drdt; v.dhdp = (double)vx.dhdp; v.dhdt = (double)vx.dhdt;
+  }
 }
-template <class T>
-__device__ __forceinline__ void phase_v(int fluid, T p, T t, Phase<T>& e) {
-  if (fluid == 1) ideal_gas(p, t, e); else iapws_v(p, t, e);
+
+// Phase properties of liquid and vapour.  MX evaluates the IF97 Gibbs sums in df64 (the
+// mixed form); FULL = false evaluates only rho and h.  The metastable branch test
+// p > p_sat(T) is taken in FP64 in both forms so that they select the same term set.
+template <bool MX, bool FULL>
+__device__ __forceinline__ void phases(int fluid, double p, double t, Phase<double>& l, Phase<double>& v) {
+  if (fluid == 1) {
+    stiffened(p, t, l);
+    ideal_gas(p, t, v);
+    return;
+  }
+  const bool meta = p > h2o_pww(t);
+  if constexpr (MX) {
+    iapws_pair_df64<FULL>(p, t, meta, l, v);
+  } else {
+    iapws_l<double, FULL>(p, t, l);
+    iapws_v_meta<double, FULL>(p, t, meta, v);
+  }
 }
 
 __device__ __forceinline__ void mixture(const Phase<double>& l, const Phase<double>& v, const Phase<double>& g,
@@ -87,21 +115,35 @@ __device__ __forceinline__ void mixture(const Phase<double>& l, const Phase<doub
 }
 
 // eos%deteos_simple
+template <bool MX = false>
 __device__ __forceinline__ void deteos_simple(int fluid, double p, double t, double y1, double y2, double* dv,
                                               unsigned long long* fb) {
   Phase<double> l, v, g;
-  phase_l(fluid, p, t, l);
-  phase_v(fluid, p, t, v);
+  phases<MX, true>(fluid, p, t, l, v);
   ideal_gas(p, t, g);
   mixture(l, v, g, y1, y2, dv, fb);
 }
 
+// mixture density and static enthalpy only: all that the Roe and AUSM+-up fluxes read of
+// the reconstructed face states; the same operations as the rho, h of deteos_simple
+template <bool MX = false>
+__device__ __forceinline__ void eos_rho_h(int fluid, double p, double t, double y1, double y2, double& rho, double& h) {
+  Phase<double> l, v, g;
+  phases<MX, false>(fluid, p, t, l, v);
+  ideal_gas(p, t, g);
+  double irhol = 1.0 / l.rho, irhov = 1.0 / v.rho, irhog = 1.0 / g.rho;
+  double yl = 1.0 - y1 - y2;
+  double irho = yl * irhol + y1 * irhov + y2 * irhog;
+  rho = 1.0 / irho;
+  h = yl * l.h + y1 * v.h + y2 * g.h;
+}
+
 // eos%deteos: with transport properties when with_prop (tv(1:2) written), else simple
+template <bool MX = false>
 __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, double t, double y1, double y2,
                                        double* dv, double* tv, unsigned long long* fb) {
   Phase<double> l, v, g;
-  phase_l(fluid, p, t, l);
-  phase_v(fluid, p, t, v);
+  phases<MX, true>(fluid, p, t, l, v);
   ideal_gas(p, t, g);
   mixture(l, v, g, y1, y2, dv, fb);
   if (with_prop) {
@@ -229,6 +271,7 @@ __device__ __forceinline__ double sdst_ratio_min(const double* s) {
 }
 
 // returns the face flux fx (npv) for the unnormalised area vector n
+template <bool MX = false>
 __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceState& L, const FaceState& Rs,
                               const double* sdst_in, double* fx, unsigned long long* fb) {
   const int npv = c.npv;
@@ -253,7 +296,7 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
   double hr = Rs.h + 0.5 * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]);
   // Roe-average EOS: only the sound speed is used (src/flux_module.f90:237,319,461,588)
   double rdv[NDV];
-  deteos_simple(c.fluid, ravg[0] + c.pref, ravg[4], ravg[5], ravg[6], rdv, fb);
+  deteos_simple<MX>(c.fluid, ravg[0] + c.pref, ravg[4], ravg[5], ravg[6], rdv, fb);
   double rc2 = rdv[5];
   double rrho = sqrt(L.rho * Rs.rho);
   const double pref = c.pref;
