@@ -167,6 +167,44 @@ def run_reference(args):
     return 0
 
 
+def fp64_form(case, res_mixed, steps, ncell, ws):
+    """The plain all-FP64 form on the same workload: its throughput, and the error of the
+    mixed form's residual on the initial state, max over cells of |R_mixed - R_fp64|
+    divided by the largest |R_fp64| of the same variable and block."""
+    from cfd3d_gb300 import abi, native
+    e64 = native.Engine(case, precision=abi.FP64)
+    e64.initialize(case["pv0"])
+    err = 0.0
+    per_var = None
+    for n, rm in enumerate(res_mixed):
+        r64 = e64.residual(n)["res"]
+        sc = np.maximum(np.abs(r64).max(axis=(0, 1, 2)), 1e-300)
+        ev = (np.abs(rm - r64) / sc).max(axis=(0, 1, 2))
+        per_var = ev if per_var is None else np.maximum(per_var, ev)
+    err = float(per_var.max())
+    for w in range(2):
+        e64.iterate(1, w + 1, 0.0)
+    ms = e64.time_iterate(steps) / steps
+    e64.close()
+    return {"fp64_form": {"value": ws * ncell / ms / 1e3, "ms_per_step": ms, "steps": steps},
+            "mixed_residual_error": {"max": err, "per_variable": [float(x) for x in per_var],
+                                     "definition": "max over cells of |R_mixed - R_fp64| / max |R_fp64|, "
+                                                   "per variable and block, initial state"}}
+
+
+def combine_ranks(ms_step, ncell, dist=None):
+    """Replicas: the slowest rank's time per step, and the whole job's throughput
+    (every rank advances its own copy of the workload) in Mcell-iter/s."""
+    ws = 1
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+        ws = dist.get_world_size()
+    return ms_step, ws * ncell / ms_step / 1e3
+
+
 def pinned(shape):
     import torch
     t = torch.empty(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
@@ -176,11 +214,13 @@ def pinned(shape):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--case", default="large")
     ap.add_argument("--scale", type=int, default=1)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--fp64-steps", type=int, default=5,
+                    help="iterations of the plain FP64 form timed beside the mixed form (0 skips)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-scale", type=int, default=4)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -205,19 +245,14 @@ def main():
     eng = native.Engine(case, precision=prec)
     eng.initialize(case["pv0"])
     ncell = cases.total_cells(case)
+    res0 = [eng.residual(n)["res"] for n in range(len(case["blocks"]))] if prec == abi.MIXED else None
     for w in range(args.warmup):
         eng.iterate(1, w + 1, 0.0)
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:
         ms = eng.time_iterate(args.steps)
-    ms_step = ms / args.steps
-    if dist:
-        import torch
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = ws * ncell / ms_step / 1e3
+    ms_step, value = combine_ranks(ms / args.steps, ncell, dist)
     stats = eng.stats()
     prof = eng.profile_iterate()
     # ---- end to end through the C ABI with pinned host buffers
@@ -251,12 +286,7 @@ def main():
         eng.iterate(1, args.warmup + s + 1, 0.0)
         for n, keep in enumerate(bufs):
             eng.download_arrays(n, pv=keep["pv"][1], dv=keep["dv"][1], tv=keep["tv"][1] if "tv" in keep else None)
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = ws * ncell / e2e_s / 1e6
+    e2e_ms, e2e_value = combine_ranks((time.perf_counter() - t0) / args.e2e_steps * 1e3, ncell, dist)
     if rank != 0:
         dist.barrier()
         return 0
@@ -281,6 +311,9 @@ def main():
         "gpu_launches": stats["launches_per_iter"] * args.steps,
         "clocks": clk.summary(),
     }
+    if prec == abi.MIXED and args.fp64_steps > 0:
+        line.update(fp64_form(case, res0, args.fp64_steps, ncell, ws))
+        line["speedup_vs_fp64"] = value / line["fp64_form"]["value"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.case, args.ref_scale, args.precision)
     print(json.dumps(line), flush=True)

@@ -1,4 +1,4 @@
-"""Seeded synthetic cases standing in for the five BASELINE configurations.
+"""Seeded synthetic cases standing in for the five benchmark configurations.
 
 The reference ships no grids or datasets (its runs read user-supplied CGNS files), so
 every case here is generated: node coordinates, BC patches in CGNS PointRange form,

@@ -25,26 +25,6 @@
 
 namespace cfd {
 
-// ------------------------------------------------------------------ index helpers
-__device__ __forceinline__ int find_block_interior(const BlockGeom* B, int nb, long long t) {
-  int b = 0;
-  while (b + 1 < nb && t >= B[b + 1].int_off) ++b;
-  return b;
-}
-__device__ __forceinline__ int find_block_cell(const BlockGeom* B, int nb, long long g) {
-  int b = 0;
-  while (b + 1 < nb && g >= B[b + 1].off) ++b;
-  return b;
-}
-__device__ __forceinline__ long long interior_cell(const BlockGeom& B, long long loc, int& i, int& j, int& k) {
-  int ni = B.imax - 1, nj = B.jmax - 1;
-  i = (int)(loc % ni) + 2;
-  long long r = loc / ni;
-  j = (int)(r % nj) + 2;
-  k = (int)(r / nj) + 2;
-  return B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1));
-}
-
 struct Cell {
   double pv[NPVM], dv[NDV], tv[3];
 };
@@ -61,11 +41,6 @@ __device__ __forceinline__ void store_cell(const DevPtr& d, const Par& c, long l
   for (int v = 0; v < c.npv; ++v) d.pv[v * n + g] = x.pv[v];
   for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = x.dv[v];
   for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = x.tv[v];
-}
-__device__ __forceinline__ void face_vec(const DevPtr& d, int plane, long long g, double* o) {
-  o[0] = d.gm[(plane + 0) * d.ncell + g];
-  o[1] = d.gm[(plane + 1) * d.ncell + g];
-  o[2] = d.gm[(plane + 2) * d.ncell + g];
 }
 
 // ------------------------------------------------------------------ pointwise EOS
@@ -301,164 +276,8 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
   }
 }
 
-// ------------------------------------------------------------------ face fluxes
-// stencil cell l (0..37) of a face at left cell g: normal stride sn, transverse s1, s2
-__device__ __forceinline__ long long stencil_cell(int l, long long g, long long sn, long long s1, long long s2) {
-  if (l < 18) {
-    int a = l & 1, t1 = (l >> 1) % 3 - 1, t2 = l / 6 - 1;
-    return g + a * sn + t1 * s1 + t2 * s2;
-  }
-  if (l < 36) {
-    int m = (l - 18) % 9;
-    int a = (l < 27) ? -1 : 2;
-    int t1 = m % 3 - 1, t2 = m / 3 - 1;
-    return g + a * sn + t1 * s1 + t2 * s2;
-  }
-  return g + ((l == 36) ? -2 : 3) * sn;
-}
-
-template <int DIR, bool MX>
-__global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  // flat face numbering per direction: block-major, then (k, j, i) of the left cell
-  int b = 0;
-  while (b + 1 < d.nblk && t >= d.blk[b + 1].face_off[DIR]) ++b;
-  const BlockGeom& B = d.blk[b];
-  long long loc = t - B.face_off[DIR];
-  int fi_, fj, fk;  // extents of the face set
-  if (DIR == 0) { fi_ = B.imax; fj = B.jmax - 1; fk = B.kmax - 1; }
-  else if (DIR == 1) { fi_ = B.imax - 1; fj = B.jmax; fk = B.kmax - 1; }
-  else { fi_ = B.imax - 1; fj = B.jmax - 1; fk = B.kmax; }
-  if (loc < 0 || loc >= (long long)fi_ * fj * fk) return;
-  int i = (int)(loc % fi_) + (DIR == 0 ? 1 : 2);
-  long long r = loc / fi_;
-  int j = (int)(r % fj) + (DIR == 1 ? 1 : 2);
-  int k = (int)(r / fj) + (DIR == 2 ? 1 : 2);
-  const long long n = d.ncell;
-  const long long si = 1, sj = B.ni, sk = (long long)B.ni * B.nj;
-  const long long g = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
-  long long sn, s1, s2;
-  if (DIR == 0) { sn = si; s1 = sj; s2 = sk; }
-  else if (DIR == 1) { sn = sj; s1 = sk; s2 = si; }
-  else { sn = sk; s1 = si; s2 = sj; }
-  const int fplane = (DIR == 0) ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
-  double nx[3];
-  face_vec(d, fplane, g, nx);
-  const int npv = c.npv;
-  FaceState L, R;
-  const long long gr = g + sn;
-  if (c.nmuscl > 0) {
-    double c9[NPVM], c10[NPVM];
-    for (int v = 0; v < npv; ++v) {
-      double x[38];
-#pragma unroll
-      for (int l = 0; l < 38; ++l) x[l] = d.pv[v * n + stencil_cell(l, g, sn, s1, s2)];
-      muscl_var<double>(c, x, L.pv[v], R.pv[v]);
-      c9[v] = x[8]; c10[v] = x[9];
-    }
-    muscl_clip<double>(c, c9, c10, L.pv, R.pv);
-    if (c.nscheme == 2 || c.nscheme == 3) {
-      // Roe-M and AUSMPW+ also read the face sound speeds
-      double dl_[NDV], dr_[NDV];
-      deteos_simple<MX>(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], dl_, &d.sc->snd2_fallbacks);
-      deteos_simple<MX>(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], dr_, &d.sc->snd2_fallbacks);
-      L.rho = dl_[0]; L.h = dl_[1]; L.c2 = dl_[5];
-      R.rho = dr_[0]; R.h = dr_[1]; R.c2 = dr_[5];
-    } else {
-      eos_rho_h<MX>(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], L.rho, L.h);
-      eos_rho_h<MX>(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], R.rho, R.h);
-      L.c2 = R.c2 = 0.0;
-    }
-  } else {
-    for (int v = 0; v < npv; ++v) { L.pv[v] = d.pv[v * n + g]; R.pv[v] = d.pv[v * n + gr]; }
-    L.rho = d.dv[g]; L.h = d.dv[n + g]; L.c2 = d.dv[5 * n + g];
-    R.rho = d.dv[gr]; R.h = d.dv[n + gr]; R.c2 = d.dv[5 * n + gr];
-  }
-  double sdst[18];
-  if (c.nscheme == 2 || c.nscheme == 3) {
-#pragma unroll
-    for (int l = 0; l < 18; ++l) sdst[l] = d.pv[stencil_cell(l, g, sn, s1, s2)];
-  }
-  double fx[NPVM];
-  inviscid_flux<MX>(c, nx, L, R, sdst, fx, &d.sc->snd2_fallbacks);
-  double* fi = d.fi + (long long)DIR * npv * n;
-  for (int v = 0; v < npv; ++v) fi[v * n + g] = fx[v];
-  if (c.iturb == -3) return;
-  // ---- viscous flux (vsflux_laminar / vsflux_turbulent)
-  const bool turb = (c.iturb == 0);
-  const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);   // faces normal to t1
-  const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);   // faces normal to t2
-  double ev[3], tvv[3];
-  for (int q = 0; q < 3; ++q) {
-    const double* P = d.gm + (ep + q) * n;
-    ev[q] = 0.25 * (P[g - s1] + P[g - s1 + sn] + P[g] + P[g + sn]);
-    const double* T = d.gm + (tp + q) * n;
-    tvv[q] = 0.25 * (T[g - s2] + T[g - s2 + sn] + T[g] + T[g + sn]);
-  }
-  double vol = 2.0 / (d.gm[GM_GRD * n + g] + d.gm[GM_GRD * n + gr]);
-  double tvl[3] = {0, 0, 0}, tvr[3] = {0, 0, 0};
-  for (int q = 0; q < c.ntv; ++q) { tvl[q] = d.tv[q * n + g]; tvr[q] = d.tv[q * n + gr]; }
-  double vis = 0.5 * (tvl[0] + tvr[0]);
-  double con = 0.5 * (tvl[1] + tvr[1]);
-  double emut = 0.0, tcon = 0.0;
-  if (turb) {
-    emut = 0.5 * (tvl[2] + tvr[2]);
-    tcon = 0.5 * (tvl[2] * d.dv[11 * n + g] + tvr[2] * d.dv[11 * n + gr]) / 0.9;
-  }
-  const int vars[6] = {1, 2, 3, 4, 7, 8};
-  double gx[6], gy[6], gz[6], cc[6];
-  const int nv = turb ? 6 : 4;
-  for (int q = 0; q < nv; ++q) {
-    const double* P = d.pv + vars[q] * n;
-    double x[18];
-#pragma unroll
-    for (int l = 0; l < 18; ++l) x[l] = P[stencil_cell(l, g, sn, s1, s2)];
-    double dn = x[9] - x[8];
-    double de = 0.0625 * (-x[0] - x[1] + x[4] + x[5] + 2.0 * (-x[6] - x[7] + x[10] + x[11]) - x[12] - x[13] + x[16] + x[17]);
-    double dt = 0.0625 * (-x[0] - x[1] + x[12] + x[13] + 2.0 * (-x[2] - x[3] + x[14] + x[15]) - x[4] - x[5] + x[16] + x[17]);
-    gx[q] = (dn * nx[0] + de * ev[0] + dt * tvv[0]) * vol;
-    gy[q] = (dn * nx[1] + de * ev[1] + dt * tvv[1]) * vol;
-    gz[q] = (dn * nx[2] + de * ev[2] + dt * tvv[2]) * vol;
-    cc[q] = 0.5 * (x[8] + x[9]);
-  }
-  const double c23 = 2.0 / 3.0;
-  double mu = turb ? (vis + emut) : vis;
-  double div = gx[0] + gy[1] + gz[2];
-  double txx = mu * (2.0 * gx[0] - c23 * div), tyy = mu * (2.0 * gy[1] - c23 * div), tzz = mu * (2.0 * gz[2] - c23 * div);
-  double txy = mu * (gy[0] + gx[1]), txz = mu * (gz[0] + gx[2]), tyz = mu * (gz[1] + gy[2]);
-  double kc = turb ? (con + tcon) : con;
-  double uc = cc[0], vc = cc[1], wc = cc[2];
-  double fv[NPVM];
-  fv[0] = 0.0;
-  fv[1] = txx * nx[0] + txy * nx[1] + txz * nx[2];
-  fv[2] = txy * nx[0] + tyy * nx[1] + tyz * nx[2];
-  fv[3] = txz * nx[0] + tyz * nx[1] + tzz * nx[2];
-  fv[4] = nx[0] * (uc * txx + vc * txy + wc * txz + kc * gx[3]) + nx[1] * (uc * txy + vc * tyy + wc * tyz + kc * gy[3]) +
-          nx[2] * (uc * txz + vc * tyz + wc * tzz + kc * gz[3]);
-  fv[5] = 0.0;
-  fv[6] = 0.0;
-  if (turb) {
-    double pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
-    double rho = 0.5 * (d.dv[g] + d.dv[gr]);
-    double ydns = 0.5 * (d.gm[(GM_GRD + 4) * n + g] + d.gm[(GM_GRD + 4) * n + gr]);
-    double kf = cc[4], of = cc[5];
-    double cdkw = fmax(1.712 * rho / of * pkw, 1.0e-10);
-    double term1 = sqrt(kf) / (0.09 * of * ydns);
-    double term2 = 500.0 * vis / rho / (of * ydns * ydns);
-    double term3 = (3.424 * rho * kf) / (cdkw * ydns * ydns);
-    double arg1 = fmin(fmax(term1, term2), term3);
-    double a2 = arg1 * arg1;
-    double bigf = tanh(a2 * a2);
-    double tdk = bigf * 0.85 + (1.0 - bigf) * 1.0;
-    double tdo = bigf * 0.5 + (1.0 - bigf) * 0.856;
-    fv[7] = (vis + emut * tdk) * (gx[4] * nx[0] + gy[4] * nx[1] + gz[4] * nx[2]);
-    fv[8] = (vis + emut * tdo) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
-  }
-  double* fvp = d.fv + (long long)DIR * npv * n;
-  for (int v = 0; v < npv; ++v) fvp[v * n + g] = fv[v];
-}
-
 // ------------------------------------------------------------------ residual + sources
+template <bool MX>
 __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
@@ -474,15 +293,41 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
     double r = 0.0;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-      const double* F = d.fi + ((long long)q * npv + v) * n;
-      if (q == 0) r = -(F[g] - F[g - st[q]]);
-      else r = r - (F[g] - F[g - st[q]]);
+      double f1, f0;
+      if (MX) {
+        const float* F = d.fi32 + ((long long)q * npv + v) * n;
+        f1 = F[g]; f0 = F[g - st[q]];
+      } else {
+        const double* F = d.fi + ((long long)q * npv + v) * n;
+        f1 = F[g]; f0 = F[g - st[q]];
+      }
+      if (q == 0) r = -(f1 - f0);
+      else r = r - (f1 - f0);
       if (vis) {
-        const double* V = d.fv + ((long long)q * npv + v) * n;
-        r = r + (V[g] - V[g - st[q]]);
+        double v1, v0;
+        if (MX) {
+          const float* V = d.fv32 + ((long long)q * npv + v) * n;
+          v1 = V[g]; v0 = V[g - st[q]];
+        } else {
+          const double* V = d.fv + ((long long)q * npv + v) * n;
+          v1 = V[g]; v0 = V[g - st[q]];
+        }
+        r = r + (v1 - v0);
       }
     }
     res[v] = r;
+  }
+  if (MX) {
+    // the uniform pref * n * dl part of the pressure flux, left out of the stored fluxes
+    const int planes[3] = {GM_CX, GM_EX, GM_TX};
+    for (int e = 0; e < 3; ++e) {
+      double s = 0.0;
+      for (int q = 0; q < 3; ++q) {
+        const double* G = d.gm + (planes[q] + e) * n;
+        s += G[g] - G[g - st[q]];
+      }
+      res[1 + e] -= c.pref * s;
+    }
   }
   double pv2[NPVM], dv[NDV];
   for (int v = 0; v < npv; ++v) pv2[v] = d.pv[v * n + g];
@@ -656,14 +501,16 @@ __global__ void __launch_bounds__(128) k_sweep(DevPtr d, Par c, const int* __res
 // ------------------------------------------------------------------ update + residual
 template <bool MX>
 __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // grid-stride over the interior cells: the grid is a fixed multiple of the SM count,
+  // so the per-CTA partials (and the order they are summed in) do not depend on size
   const int npv = c.npv;
   double sq_[NPVM];
   for (int v = 0; v < NPVM; ++v) sq_[v] = 0.0;
   double dpmax = -1.0;
   long long dpidx = -1;
   int bad = 0;
-  if (t < d.nint) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < d.nint; t += stride) {
     int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
     long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
     const long long n = d.ncell;
@@ -682,13 +529,13 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
     for (int v = 0; v < npv; ++v) {
       d.pv[v * n + g] = p[v];
       double df = fabs(old[v] - p[v]);
-      sq_[v] = df * df;
+      sq_[v] += df * df;
       if (!isfinite(p[v])) bad = 1;
     }
     for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
     for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
-    dpmax = fabs(old[0] - p[0]);
-    dpidx = t;
+    double dp = fabs(old[0] - p[0]);
+    if (dp > dpmax) { dpmax = dp; dpidx = t; }   // t increases: ties keep the first cell
   }
   if (bad) atomicExch(&d.sc->nonfinite, 1);
   // per-CTA partial sums (deterministic order: warp shuffles then warps in order)
@@ -761,27 +608,43 @@ __global__ void k_eddy(DevPtr d, Par c) {
   d.tv[2 * n + g] = 0.31 * rho * kk / fmax(0.31 * oo, sss * bigf2);
 }
 
-__global__ void k_finish(DevPtr d, Par c, int nparts) {
-  __shared__ double s[NPVM];
-  const int npv = c.npv;
-  if (threadIdx.x < npv) {
-    double acc = 0.0;
-    for (int q = 0; q < nparts; ++q) acc += d.partial[(long long)q * (NPVM + 2) + threadIdx.x];
-    s[threadIdx.x] = acc;
+// final reduction of the per-CTA partials: 256 threads, fixed assignment and a fixed
+// tree, so the norms are bitwise reproducible from run to run
+constexpr int FIN_T = 256;
+__global__ void __launch_bounds__(FIN_T) k_finish(DevPtr d, Par c, int nparts) {
+  __shared__ double s[FIN_T][NPVM];
+  __shared__ double sm[FIN_T];
+  __shared__ long long si[FIN_T];
+  const int npv = c.npv, tid = threadIdx.x;
+  double acc[NPVM];
+  for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
+  double m = -1.0;
+  long long mi = -1;
+  for (int q = tid; q < nparts; q += FIN_T) {
+    const double* pp = d.partial + (long long)q * (NPVM + 2);
+    for (int v = 0; v < npv; ++v) acc[v] += pp[v];
+    double om = pp[NPVM];
+    long long oi = __double_as_longlong(pp[NPVM + 1]);
+    if (om > m || (om == m && oi >= 0 && (mi < 0 || oi < mi))) { m = om; mi = oi; }
   }
+  for (int v = 0; v < NPVM; ++v) s[tid][v] = acc[v];
+  sm[tid] = m;
+  si[tid] = mi;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    Scalars* sc = d.sc;
-    for (int v = 0; v < npv; ++v) sc->res[v] = sqrt(s[v]);
-    double m = -1.0;
-    long long mi = -1;
-    for (int q = 0; q < nparts; ++q) {
-      double om = d.partial[(long long)q * (NPVM + 2) + NPVM];
-      long long oi = __double_as_longlong(d.partial[(long long)q * (NPVM + 2) + NPVM + 1]);
-      if (om > m || (om == m && oi >= 0 && (mi < 0 || oi < mi))) { m = om; mi = oi; }
+  for (int h = FIN_T / 2; h > 0; h >>= 1) {
+    if (tid < h) {
+      for (int v = 0; v < npv; ++v) s[tid][v] += s[tid + h][v];
+      double om = sm[tid + h];
+      long long oi = si[tid + h];
+      if (om > sm[tid] || (om == sm[tid] && oi >= 0 && (si[tid] < 0 || oi < si[tid]))) { sm[tid] = om; si[tid] = oi; }
     }
-    sc->resmax = m;
-    sc->resmax_cell = (m > 1.0e-12) ? mi : -1;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    Scalars* sc = d.sc;
+    for (int v = 0; v < npv; ++v) sc->res[v] = sqrt(s[0][v]);
+    sc->resmax = sm[0];
+    sc->resmax_cell = (sm[0] > 1.0e-12) ? si[0] : -1;
     sc->time_acc += __longlong_as_double((long long)sc->dtmin_bits);
     sc->dtmin_bits = (unsigned long long)__double_as_longlong(1.0e10);
   }
@@ -858,19 +721,13 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   for (int p = 0; p < 3; ++p)
     if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
   stage(2);
-  if (c.mixed) {
-    k_face_flux<0, true><<<nblk_of(E.nface[0], T), T, 0, s>>>(d, c);
-    k_face_flux<1, true><<<nblk_of(E.nface[1], T), T, 0, s>>>(d, c);
-    k_face_flux<2, true><<<nblk_of(E.nface[2], T), T, 0, s>>>(d, c);
-  } else {
-    k_face_flux<0, false><<<nblk_of(E.nface[0], T), T, 0, s>>>(d, c);
-    k_face_flux<1, false><<<nblk_of(E.nface[1], T), T, 0, s>>>(d, c);
-    k_face_flux<2, false><<<nblk_of(E.nface[2], T), T, 0, s>>>(d, c);
-  }
+  if (c.mixed) launch_face_flux_mixed(E, s);
+  else launch_face_flux(E, s);
   stage(3);
-  k_rhs<<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+  if (c.mixed) k_rhs<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+  else k_rhs<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
   stage(4);
-  n += 4;
+  n += c.mixed ? 5 : 4;
   if (!full) { E.launches_per_iter = n; return; }
   const int np = (int)E.plane_off.size() - 1;
   for (int q = 0; q < np; ++q) {
@@ -888,7 +745,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   ++n;
   stage(7);
   if (c.iturb == 0) { k_eddy<<<nblk_of(E.nint, T), T, 0, s>>>(d, c); ++n; }
-  k_finish<<<1, 32, 0, s>>>(d, c, E.red_grid);
+  k_finish<<<1, FIN_T, 0, s>>>(d, c, E.red_grid);
   ++n;
   stage(8);
   E.launches_per_iter = n;
@@ -1035,8 +892,16 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   bool ok = alloc(E.d.pv, c.npv) && alloc(E.d.dv, NDV) && alloc(E.d.tv, std::max(c.ntv, 1)) &&
             alloc(E.d.gm, GM_GRD + c.ngrd) && alloc(E.d.res, c.npv) && alloc(E.d.icav, 4) && alloc(E.d.itt, 4) &&
             alloc(E.d.ocut, 1) && alloc(E.d.dt, 1) && alloc(E.d.rcav, 2) && alloc(E.d.qq, std::max(2 * c.npv * (c.nqq ? 1 : 0), 1)) &&
-            alloc(E.d.dqs, c.npv) && alloc(E.d.dcv, c.npv) && alloc(E.d.fi, 3 * c.npv) && alloc(E.d.prep, NPREP) &&
-            alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
+            alloc(E.d.dqs, c.npv) && alloc(E.d.dcv, c.npv) && alloc(E.d.prep, NPREP);
+  auto allocf = [&](float*& p, long long planes) -> bool {
+    if (cudaMalloc(&p, (size_t)planes * n * 4) != cudaSuccess) return false;
+    cudaMemset(p, 0, (size_t)planes * n * 4);
+    return true;
+  };
+  if (c.mixed)
+    ok = ok && allocf(E.d.pvf, c.npv) && allocf(E.d.fi32, 3 * c.npv) && allocf(E.d.fv32, (c.iturb == -3) ? 1 : 3 * c.npv);
+  else
+    ok = ok && alloc(E.d.fi, 3 * c.npv) && alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
   if (!ok) { E.err = "device allocation failed"; return CFD3D_ERR_NOMEM; }
   E.d.ncell = n;
   E.d.nint = E.nint;
@@ -1051,7 +916,12 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   double big = 1.0e10;
   std::memcpy(&s0.dtmin_bits, &big, 8);
   CFD_CUDA(cudaMemcpy(E.d.sc, &s0, sizeof(Scalars), cudaMemcpyHostToDevice));
-  E.red_grid = (int)nblk_of(E.nint, 128);
+  {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    E.red_grid = (int)std::min<long long>(nblk_of(E.nint, 128), (long long)std::max(nsm, 1) * 8);
+  }
   CFD_CUDA(cudaMalloc(&E.d.partial, (size_t)E.red_grid * (NPVM + 2) * 8));
   // reference state: deteos at (pref, tref, y1ref, y2ref), then config%setref
   {
@@ -1082,6 +952,8 @@ void cfd3d_destroy(cfd3d_handle* h) {
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
                     E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.prep, E.d.partial, h->staging};
   for (double* p : bufs) cudaFree(p);
+  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32};
+  for (float* p : fbufs) cudaFree(p);
   cudaFree((void*)E.d.blk);
   cudaFree(E.d.sc);
   for (int p = 0; p < 3; ++p) cudaFree(E.d_ops[p]);

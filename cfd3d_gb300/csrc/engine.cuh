@@ -67,6 +67,8 @@ struct DevPtr {
   long long nint;
   Scalars* sc;
   double* partial;   // per-CTA partial residual sums [gridsize][npv+2]
+  // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
+  float *pvf, *fi32, *fv32;
 };
 
 struct Engine {
@@ -90,6 +92,52 @@ struct Engine {
   // host copies of the reference state used by the ghost program
   double pv_ref[NPVM];
 };
+
+// ------------------------------------------------------------------ index helpers
+__device__ __forceinline__ int find_block_interior(const BlockGeom* B, int nb, long long t) {
+  int b = 0;
+  while (b + 1 < nb && t >= B[b + 1].int_off) ++b;
+  return b;
+}
+__device__ __forceinline__ int find_block_cell(const BlockGeom* B, int nb, long long g) {
+  int b = 0;
+  while (b + 1 < nb && g >= B[b + 1].off) ++b;
+  return b;
+}
+__device__ __forceinline__ long long interior_cell(const BlockGeom& B, long long loc, int& i, int& j, int& k) {
+  int ni = B.imax - 1, nj = B.jmax - 1;
+  i = (int)(loc % ni) + 2;
+  long long r = loc / ni;
+  j = (int)(r % nj) + 2;
+  k = (int)(r / nj) + 2;
+  return B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1));
+}
+
+__device__ __forceinline__ void face_vec(const DevPtr& d, int plane, long long g, double* o) {
+  o[0] = d.gm[(plane + 0) * d.ncell + g];
+  o[1] = d.gm[(plane + 1) * d.ncell + g];
+  o[2] = d.gm[(plane + 2) * d.ncell + g];
+}
+
+// stencil cell l (0..37) of a face at left cell g: normal stride sn, transverse s1, s2
+__device__ __forceinline__ long long stencil_cell(int l, long long g, long long sn, long long s1, long long s2) {
+  if (l < 18) {
+    int a = l & 1, t1 = (l >> 1) % 3 - 1, t2 = l / 6 - 1;
+    return g + a * sn + t1 * s1 + t2 * s2;
+  }
+  if (l < 36) {
+    int m = (l - 18) % 9;
+    int a = (l < 27) ? -1 : 2;
+    int t1 = m % 3 - 1, t2 = m / 3 - 1;
+    return g + a * sn + t1 * s1 + t2 * s2;
+  }
+  return g + ((l == 36) ? -2 : 3) * sn;
+}
+
+
+// face-flux launchers (flux.cu: FP64 form; flux_mixed.cu: mixed form)
+void launch_face_flux(const Engine& E, cudaStream_t s);
+void launch_face_flux_mixed(const Engine& E, cudaStream_t s);
 
 // host entry points implemented in setup.cu
 bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks);

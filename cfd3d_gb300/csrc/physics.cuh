@@ -164,6 +164,17 @@ __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, doubl
 }
 
 // ------------------------------------------------------------------ MUSCL / MLP
+// Products and sums without FMA contraction.  A reconstructed state often lands exactly
+// on a clip bound (y1 = 0 next to a cell without vapour, when the MLP factor is exactly 2),
+// and which side of the bound it rounds to selects the clip; the reference is compiled
+// without contraction, so the reconstruction repeats its rounding step for step.
+__device__ __forceinline__ double nmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double nadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double nsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float nmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float nadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float nsub(float a, float b) { return __fsub_rn(a, b); }
+
 template <class R>
 __device__ __forceinline__ R limiter(int nlim, R r, R r1, R r2, R alp) {
   R c;
@@ -173,16 +184,17 @@ __device__ __forceinline__ R limiter(int nlim, R r, R r1, R r2, R alp) {
     case 2: return fmax(fmax(R(0), fmin(R(1), alp * r)), fmin(alp, r));
     case 3: c = (r + fabs(r)) / (R(1) + fabs(r)); return fmax(R(0), fmin(fmin(alp, alp * r), c));
     case 4: c = (R(1) + r) / R(2); return fmax(R(0), fmin(fmin(alp, alp * r), c));
-    case 5: c = (r * r + r) / (R(1) + r * r); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
+    case 5: c = nadd(nmul(r, r), r) / nadd(R(1), nmul(r, r)); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
     case 6: c = fmin(R(1.5), alp); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
-    case 7: c = (R(1) + R(2) * r) / R(3); return fmax(R(0), fmin(fmin(alp, alp * r), c));
-    case 8: c = (R(-2) * r1 + R(11) + R(24) * r - R(3) * r2) / R(30); return fmax(R(0), fmin(fmin(alp, alp * r), c));
-    case 9: return (R(1) + R(2) * r) / R(3);
-    default: return (R(-2) * r1 + R(11) + R(24) * r - R(3) * r2) / R(30);
+    case 7: c = nadd(R(1), nmul(R(2), r)) / R(3); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 8:
+      c = nsub(nadd(nadd(nmul(R(-2), r1), R(11)), nmul(R(24), r)), nmul(R(3), r2)) / R(30);
+      return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 9: return nadd(R(1), nmul(R(2), r)) / R(3);
+    default: return nsub(nadd(nadd(nmul(R(-2), r1), R(11)), nmul(R(24), r)), nmul(R(3), r2)) / R(30);
   }
 }
 
-// stencil x[l] is the reference's x(l+1, k) for one variable k (38 cells)
 template <class R>
 __device__ __forceinline__ void muscl_var(const Par& c, const R* x, R& xl, R& xr) {
   const R eps = R(1.0e-30), eps2 = R(1.0e-3);
@@ -230,8 +242,8 @@ __device__ __forceinline__ void muscl_var(const Par& c, const R* x, R& xl, R& xr
     alp0 = fmax(R(1), fmin(R(2), alp0));
     alp1 = fmax(R(1), fmin(R(2), alp1));
   }
-  xl = x[8] + R(0.5) * limiter<R>(c.nlim, r0, r10, r20, alp0) * dqm;
-  xr = x[9] - R(0.5) * limiter<R>(c.nlim, r1, r11, r21, alp1) * dqp;
+  xl = nadd(x[8], nmul(nmul(R(0.5), limiter<R>(c.nlim, r0, r10, r20, alp0)), dqm));
+  xr = nsub(x[9], nmul(nmul(R(0.5), limiter<R>(c.nlim, r1, r11, r21, alp1)), dqp));
 }
 
 // post-clipping of the reconstructed states (muscl_module.f90:136-158)

@@ -6,7 +6,7 @@
  * `lusgs` :455-733) together with the convergence residual `t_resi%setqres/residual`
  * (src/residual_module.f90:94-186), as called from `solve_equation`
  * (src/solve_module.f90:133-136).  A Fortran caller binds these entry points through
- * ISO_C_BINDING; Python binds them through ctypes.
+ * ISO_C_BINDING interfaces; Python binds them through ctypes.
  *
  * Conventions
  *  - Plain pointers and sizes only.  All arrays are FP64 in the reference's Fortran

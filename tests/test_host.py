@@ -1,0 +1,112 @@
+"""Host-side logic that needs no GPU: the input.inp reader, the synthetic cases, the
+benchmark's byte model and its replica reduction (gloo, two ranks)."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from cfd3d_gb300 import abi, cases
+from cfd3d_gb300.config import read_input, write_input
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+
+def test_input_roundtrip():
+    cfg = cases.make("cavitating", scale=16)["cfg"]
+    back, bad = read_input(write_input(cfg, name="cav"))
+    assert bad == []
+    assert back["name"] == "cav"
+    for k, v in cfg.items():
+        if k in back:
+            assert back[k] == pytest.approx(v, rel=1e-15), k
+
+
+def test_input_flags_unsupported_options():
+    cfg = dict(cases.make("plain_small", scale=16)["cfg"])
+    text = write_input(cfg).splitlines()
+    # gravity / csf value line is the 20th line (10th label/value pair)
+    text[19] = "1 0"
+    _, bad = read_input("\n".join(text) + "\n")
+    assert bad == ["gravity"]
+
+
+def test_fortran_real_literals():
+    cfg = dict(cases.make("plain_small", scale=16)["cfg"])
+    text = write_input(cfg)
+    assert "d" in text  # reals are written as Fortran double literals
+    back, _ = read_input(text.replace("d", "D"))
+    assert back["pref"] == pytest.approx(cfg["pref"])
+
+
+@pytest.mark.parametrize("name,cells", [("plain_small", 64 * 32 * 32), ("cavitating", 128 * 64 * 64),
+                                        ("adjoint", 64 ** 3), ("large", 384 * 192 * 192)])
+def test_case_sizes(name, cells):
+    # generated at 1/8 resolution; the full-size count follows from the divisor
+    c = cases.make(name, scale=8)
+    assert cases.total_cells(c) * 8 ** 3 == cells
+    for b, pv in zip(c["blocks"], c["pv0"]):
+        assert pv.shape == abi.interior_shape(b, abi.sizes(c["cfg"])[0])
+        assert np.all(np.isfinite(pv))
+        assert np.all((pv[..., 5] >= 0.0) & (pv[..., 5] <= 1.0))
+
+
+def test_batched_connections_are_point_matched():
+    c = cases.make("batched", scale=8, nblocks=12)
+    blocks = c["blocks"]
+    for n, b in enumerate(blocks):
+        for con in b["con"]:
+            d = blocks[con["donor"]]
+            back = [cc for cc in d["con"] if cc["donor"] == n]
+            assert len(back) == 1
+            assert tuple(back[0]["pnts"]) == tuple(con["pnts_donor"])
+            # the shared face has the same node coordinates on both sides
+            i0 = con["pnts"][0] - 1
+            j0 = con["pnts_donor"][0] - 1
+            assert np.array_equal(b["xyz"][:, :, i0], d["xyz"][:, :, j0])
+
+
+@pytest.mark.parametrize("name,bytes_", [("plain_small", 728), ("cavitating", 776), ("adjoint", 896),
+                                         ("large", 1040)])
+def test_algorithmic_bytes_per_cell_iteration(name, bytes_):
+    assert bench.algorithmic_bytes(cases.make(name, scale=16)["cfg"]) == bytes_
+
+
+def test_reference_arm_other_ranks_exit_without_work():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference"],
+                       capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode == 0
+    assert r.stdout.strip() == ""
+
+
+def _replica_rank(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms, value = bench.combine_ranks(10.0 * (rank + 1), 1000, dist)
+    out.put((rank, ms, value))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_replica_reduction_two_ranks_gloo():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + (os.getpid() % 2000)
+    procs = [ctx.Process(target=_replica_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    # slowest rank's time, whole-job throughput = 2 replicas x 1000 cells / 20 ms
+    for rank, ms, value in got:
+        assert ms == 20.0
+        assert value == pytest.approx(2 * 1000 / 20.0 / 1e3)
