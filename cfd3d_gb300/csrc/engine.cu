@@ -318,16 +318,20 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
     res[v] = r;
   }
   if (MX) {
-    // the uniform pref * n * dl part of the pressure flux, left out of the stored fluxes
+    // the stored mixed-form fluxes are F - (Phi + pref I).n dl; add the free-stream part
+    // back through the cell's face-vector sum (zero up to the metrics' closure error)
     const int planes[3] = {GM_CX, GM_EX, GM_TX};
+    double sn[3];
     for (int e = 0; e < 3; ++e) {
       double s = 0.0;
       for (int q = 0; q < 3; ++q) {
         const double* G = d.gm + (planes[q] + e) * n;
         s += G[g] - G[g - st[q]];
       }
-      res[1 + e] -= c.pref * s;
+      sn[e] = s;
     }
+    for (int v = 0; v < npv; ++v) res[v] -= c.phi[v][0] * sn[0] + c.phi[v][1] * sn[1] + c.phi[v][2] * sn[2];
+    for (int e = 0; e < 3; ++e) res[1 + e] -= c.pref * sn[e];
   }
   double pv2[NPVM], dv[NDV];
   for (int v = 0; v < npv; ++v) pv2[v] = d.pv[v * n + g];
@@ -727,7 +731,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   if (c.mixed) k_rhs<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
   else k_rhs<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
   stage(4);
-  n += c.mixed ? 5 : 4;
+  n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
   const int np = (int)E.plane_off.size() - 1;
   for (int q = 0; q < np; ++q) {
@@ -899,7 +903,8 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     return true;
   };
   if (c.mixed)
-    ok = ok && allocf(E.d.pvf, c.npv) && allocf(E.d.fi32, 3 * c.npv) && allocf(E.d.fv32, (c.iturb == -3) ? 1 : 3 * c.npv);
+    ok = ok && allocf(E.d.pvf, c.npv) && allocf(E.d.fi32, 3 * c.npv) && allocf(E.d.fv32, (c.iturb == -3) ? 1 : 3 * c.npv) &&
+         allocf(E.d.frec, 2 * 12);
   else
     ok = ok && alloc(E.d.fi, 3 * c.npv) && alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
   if (!ok) { E.err = "device allocation failed"; return CFD3D_ERR_NOMEM; }
@@ -937,6 +942,16 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
       if (cfg->kinf > 0) E.par.kref = cfg->kinf;
       if (cfg->oinf > 0) E.par.oref = cfg->oinf;
     }
+    // mixed form: free-stream flux tensor (gauge pressure) for the stored flux deviations
+    E.par.href = dvr[1];
+    const double* U = E.par.uref_vec;
+    const double H = dvr[1] + 0.5 * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
+    const double sc[NPVM] = {1.0, 0.0, 0.0, 0.0, H, cfg->y1ref, cfg->y2ref, E.par.kref, E.par.oref};
+    for (int e = 0; e < 3; ++e) {
+      const double m = dvr[0] * U[e];
+      for (int v = 0; v < NPVM; ++v) E.par.phi[v][e] = m * sc[v];
+      for (int q = 0; q < 3; ++q) E.par.phi[1 + q][e] = m * U[q];
+    }
   }
   if (!setup_geometry(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
   if (!setup_ghost_program(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
@@ -952,7 +967,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
                     E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.prep, E.d.partial, h->staging};
   for (double* p : bufs) cudaFree(p);
-  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32};
+  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec};
   for (float* p : fbufs) cudaFree(p);
   cudaFree((void*)E.d.blk);
   cudaFree(E.d.sc);

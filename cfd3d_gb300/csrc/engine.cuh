@@ -69,6 +69,7 @@ struct DevPtr {
   double* partial;   // per-CTA partial residual sums [gridsize][npv+2]
   // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
   float *pvf, *fi32, *fv32;
+  float* frec;       // mixed form: reconstructed face states of one direction (2 x 12 planes)
 };
 
 struct Engine {

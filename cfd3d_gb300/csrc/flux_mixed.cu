@@ -1,11 +1,14 @@
 // flux_mixed.cu -- face fluxes of the mixed-precision form (CFD3D_MIXED).
 //
-// k_shadow writes the FP32 gauge shadow pvf = (p - pref, u, v, w, T - tref, y1, y2, k, omega)
-// of every padded cell after the boundary program; k_face_flux_mx then reconstructs,
-// evaluates and stores the face fluxes of one direction in FP32, one thread per face.  The
-// face-state EOS runs through the df64 IF97 sums and an FP64 mixture; the fluxes are stored
-// in fi32 / fv32 (half the bytes of the FP64 form) and accumulated in FP64 by k_rhs.
-// Same faces, stencils and formulas as the FP64 form (flux.cu).
+//   k_shadow          FP32 gauge shadow pvf of every padded cell, after the boundary program
+//   k_recon_mx<DIR>   per face: MUSCL / MLP on pvf, clips, face-state rho and h (df64 IF97
+//                     sums, FP64 mixture), written to the face record frec
+//   k_flux_mx<DIR>    per face: FP32 Roe-average sound speed, inviscid flux with FP64
+//                     leading-order terms, FP32 viscous flux; stores F - Phi.n dl in FP32
+// Splitting reconstruction + EOS from the flux keeps each kernel's code within the
+// instruction cache (the expanded df64 Gibbs sums are large) and its registers low.
+// Same faces, stencils and formulas as the FP64 form (flux.cu); the precision choices are
+// listed in mixed.cuh.
 #include "engine.cuh"
 #include "mixed.cuh"
 
@@ -15,17 +18,21 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c) {
   const long long n = d.ncell;
   const long long total = n * c.npv;
   const long long stride = (long long)gridDim.x * blockDim.x;
+  const double off[NPVM] = {0.0, c.uref_vec[0], c.uref_vec[1], c.uref_vec[2], c.tref, 0.0, 0.0, 0.0, 0.0};
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += stride) {
     const int v = (int)(q / n);
-    double x = d.pv[q];
-    if (v == 4) x -= c.tref;
-    d.pvf[q] = (float)x;
+    d.pvf[q] = (float)(d.pv[q] - off[v]);
   }
 }
 
+// face of direction DIR for thread t: left cell g and the stencil strides
+struct FaceIdx {
+  long long g, sn, s1, s2;
+  bool ok;
+};
 template <int DIR>
-__global__ void __launch_bounds__(128) k_face_flux_mx(DevPtr d, Par c) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__device__ __forceinline__ FaceIdx face_of(const DevPtr& d, long long t) {
+  FaceIdx f{};
   int b = 0;
   while (b + 1 < d.nblk && t >= d.blk[b + 1].face_off[DIR]) ++b;
   const BlockGeom& B = d.blk[b];
@@ -34,87 +41,116 @@ __global__ void __launch_bounds__(128) k_face_flux_mx(DevPtr d, Par c) {
   if (DIR == 0) { fi_ = B.imax; fj = B.jmax - 1; fk = B.kmax - 1; }
   else if (DIR == 1) { fi_ = B.imax - 1; fj = B.jmax; fk = B.kmax - 1; }
   else { fi_ = B.imax - 1; fj = B.jmax - 1; fk = B.kmax; }
-  if (loc < 0 || loc >= (long long)fi_ * fj * fk) return;
+  f.ok = !(loc < 0 || loc >= (long long)fi_ * fj * fk);
+  if (!f.ok) return f;
   int i = (int)(loc % fi_) + (DIR == 0 ? 1 : 2);
   long long r = loc / fi_;
   int j = (int)(r % fj) + (DIR == 1 ? 1 : 2);
   int k = (int)(r / fj) + (DIR == 2 ? 1 : 2);
-  const long long n = d.ncell;
   const long long si = 1, sj = B.ni, sk = (long long)B.ni * B.nj;
-  const long long g = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
-  long long sn, s1, s2;
-  if (DIR == 0) { sn = si; s1 = sj; s2 = sk; }
-  else if (DIR == 1) { sn = sj; s1 = sk; s2 = si; }
-  else { sn = sk; s1 = si; s2 = sj; }
-  const long long gr = g + sn;
-  const int fplane = (DIR == 0) ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
-  float nx[3];
-  for (int q = 0; q < 3; ++q) nx[q] = (float)d.gm[(fplane + q) * n + g];
+  f.g = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
+  if (DIR == 0) { f.sn = si; f.s1 = sj; f.s2 = sk; }
+  else if (DIR == 1) { f.sn = sj; f.s1 = sk; f.s2 = si; }
+  else { f.sn = sk; f.s1 = si; f.s2 = sj; }
+  return f;
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(128) k_recon_mx(DevPtr d, Par c) {
+  const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+  if (!f.ok) return;
+  const long long n = d.ncell, g = f.g, gr = g + f.sn;
   const int npv = c.npv;
   const float* P = d.pvf;
-  FaceStateF L, R;
+  float gl[NPVM], gR[NPVM];
+  double rl, hl, rr, hr;
+  float cl = 0.0f, cr = 0.0f;
   if (c.nmuscl > 0) {
     float c9[NPVM], c10[NPVM];
     for (int v = 0; v < npv; ++v) {
       float x[38];
 #pragma unroll
-      for (int l = 0; l < 38; ++l) x[l] = P[v * n + stencil_cell(l, g, sn, s1, s2)];
-      muscl_var<float>(c, x, L.pv[v], R.pv[v]);
+      for (int l = 0; l < 38; ++l) x[l] = P[v * n + stencil_cell(l, g, f.sn, f.s1, f.s2)];
+      muscl_var<float>(c, x, gl[v], gR[v]);
       c9[v] = x[8]; c10[v] = x[9];
     }
-    muscl_clip<float>(c, c9, c10, L.pv, R.pv);
-    const double pl = c.pref + (double)L.pv[0], tl = c.tref + (double)L.pv[4];
-    const double pr = c.pref + (double)R.pv[0], tr = c.tref + (double)R.pv[4];
+    muscl_clip_mx(c, c9, c10, gl, gR);
+    const double pl = c.pref + (double)gl[0], tl = c.tref + (double)gl[4];
+    const double pr = c.pref + (double)gR[0], tr = c.tref + (double)gR[4];
+    eos_rho_h<true>(c.fluid, pl, tl, gl[5], gl[6], rl, hl);
+    eos_rho_h<true>(c.fluid, pr, tr, gR[5], gR[6], rr, hr);
     if (c.nscheme == 2 || c.nscheme == 3) {
-      double dl_[NDV], dr_[NDV];
-      deteos_simple<true>(c.fluid, pl, tl, L.pv[5], L.pv[6], dl_, &d.sc->snd2_fallbacks);
-      deteos_simple<true>(c.fluid, pr, tr, R.pv[5], R.pv[6], dr_, &d.sc->snd2_fallbacks);
-      L.rho = (float)dl_[0]; L.h = (float)dl_[1]; L.c2 = (float)dl_[5];
-      R.rho = (float)dr_[0]; R.h = (float)dr_[1]; R.c2 = (float)dr_[5];
-    } else {
-      double rl, hl, rr, hr;
-      eos_rho_h<true>(c.fluid, pl, tl, L.pv[5], L.pv[6], rl, hl);
-      eos_rho_h<true>(c.fluid, pr, tr, R.pv[5], R.pv[6], rr, hr);
-      L.rho = (float)rl; L.h = (float)hl; R.rho = (float)rr; R.h = (float)hr;
-      L.c2 = R.c2 = 0.0f;
+      cl = eos_c2_f(c.fluid, (float)pl, (float)tl, gl[5], gl[6], &d.sc->snd2_fallbacks);
+      cr = eos_c2_f(c.fluid, (float)pr, (float)tr, gR[5], gR[6], &d.sc->snd2_fallbacks);
     }
   } else {
-    for (int v = 0; v < npv; ++v) { L.pv[v] = P[v * n + g]; R.pv[v] = P[v * n + gr]; }
-    L.rho = (float)d.dv[g]; L.h = (float)d.dv[n + g]; L.c2 = (float)d.dv[5 * n + g];
-    R.rho = (float)d.dv[gr]; R.h = (float)d.dv[n + gr]; R.c2 = (float)d.dv[5 * n + gr];
+    for (int v = 0; v < npv; ++v) { gl[v] = P[v * n + g]; gR[v] = P[v * n + gr]; }
+    rl = d.dv[g]; hl = d.dv[n + g]; cl = (float)d.dv[5 * n + g];
+    rr = d.dv[gr]; hr = d.dv[n + gr]; cr = (float)d.dv[5 * n + gr];
+  }
+  float* F = d.frec;
+  for (int v = 0; v < npv; ++v) { F[v * n + g] = gl[v]; F[(FREC_SIDE + v) * n + g] = gR[v]; }
+  F[NPVM * n + g] = (float)(rl - c.rhoref);
+  F[(NPVM + 1) * n + g] = (float)(hl - c.href);
+  F[(NPVM + 2) * n + g] = cl;
+  F[(FREC_SIDE + NPVM) * n + g] = (float)(rr - c.rhoref);
+  F[(FREC_SIDE + NPVM + 1) * n + g] = (float)(hr - c.href);
+  F[(FREC_SIDE + NPVM + 2) * n + g] = cr;
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(128) k_flux_mx(DevPtr d, Par c) {
+  const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+  if (!f.ok) return;
+  const long long n = d.ncell, g = f.g, gr = g + f.sn;
+  const long long sn = f.sn, s1 = f.s1, s2 = f.s2;
+  const int npv = c.npv;
+  const float* P = d.pvf;
+  const int fplane = (DIR == 0) ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
+  double nv[3];
+  for (int q = 0; q < 3; ++q) nv[q] = d.gm[(fplane + q) * n + g];
+  FaceMx L, R;
+  {
+    const float* F = d.frec;
+    for (int v = 0; v < npv; ++v) { L.g[v] = F[v * n + g]; R.g[v] = F[(FREC_SIDE + v) * n + g]; }
+    L.rho = c.rhoref + (double)F[NPVM * n + g];
+    L.h = c.href + (double)F[(NPVM + 1) * n + g];
+    L.c2 = F[(NPVM + 2) * n + g];
+    R.rho = c.rhoref + (double)F[(FREC_SIDE + NPVM) * n + g];
+    R.h = c.href + (double)F[(FREC_SIDE + NPVM + 1) * n + g];
+    R.c2 = F[(FREC_SIDE + NPVM + 2) * n + g];
+    for (int q = 0; q < 3; ++q) { L.u[q] = c.uref_vec[q] + (double)L.g[1 + q]; R.u[q] = c.uref_vec[q] + (double)R.g[1 + q]; }
+  }
+  // Roe-average state (sqrt(rho) weights; p and T arithmetic means) and its FP32 sound speed
+  float ravg_u[3], ravg_s[NPVM];
+  float rc2 = 0.0f;
+  {
+    float srl = sqrtf((float)L.rho), srr = sqrtf((float)R.rho);
+    float rd = 1.0f / (srl + srr);
+    for (int q = 0; q < 3; ++q) ravg_u[q] = (float)c.uref_vec[q] + (srl * L.g[1 + q] + srr * R.g[1 + q]) * rd;
+    for (int q = 0; q < NPVM; ++q) ravg_s[q] = 0.0f;
+    for (int q = 5; q < npv; ++q) ravg_s[q] = (srl * L.g[q] + srr * R.g[q]) * rd;
+    if (nv[0] != 0.0 || nv[1] != 0.0 || nv[2] != 0.0) {
+      float pa = (float)(c.pref + 0.5 * ((double)L.g[0] + (double)R.g[0]));
+      float ta = (float)(c.tref + 0.5 * ((double)L.g[4] + (double)R.g[4]));
+      rc2 = eos_c2_f(c.fluid, pa, ta, ravg_s[5], ravg_s[6], &d.sc->snd2_fallbacks);
+    }
   }
   float sdst[18];
   if (c.nscheme == 2 || c.nscheme == 3) {
 #pragma unroll
     for (int l = 0; l < 18; ++l) sdst[l] = P[stencil_cell(l, g, sn, s1, s2)];
   }
-  // Roe-average state; its sound speed comes from the FP64 mixture EOS
-  // (src/flux_module.f90:237,319,461,588)
-  float ravg[NPVM];
-  {
-    float srl = sqrtf(L.rho), srr = sqrtf(R.rho);
-    float rd = 1.0f / (srl + srr);
-    ravg[0] = 0.5f * (L.pv[0] + R.pv[0]);
-    ravg[4] = 0.5f * (L.pv[4] + R.pv[4]);
-    for (int q = 1; q <= 3; ++q) ravg[q] = (srl * L.pv[q] + srr * R.pv[q]) * rd;
-    for (int q = 5; q < npv; ++q) ravg[q] = (srl * L.pv[q] + srr * R.pv[q]) * rd;
-  }
-  float rc2 = 0.0f;
-  if (nx[0] != 0.0f || nx[1] != 0.0f || nx[2] != 0.0f) {
-    double rdv[NDV];
-    deteos_simple<true>(c.fluid, c.pref + (double)ravg[0], c.tref + (double)ravg[4], ravg[5], ravg[6], rdv,
-                        &d.sc->snd2_fallbacks);
-    rc2 = (float)rdv[5];
-  }
-  float fx[NPVM];
-  inviscid_flux_mx(c, nx, L, R, sdst, rc2, ravg, fx);
+  double fx[NPVM];
+  inviscid_flux_mx(c, nv, L, R, sdst, rc2, ravg_u, ravg_s, fx);
   float* fo = d.fi32 + (long long)DIR * npv * n;
-  for (int v = 0; v < npv; ++v) fo[v * n + g] = fx[v];
+  for (int v = 0; v < npv; ++v) fo[v * n + g] = (float)fx[v];
   if (c.iturb == -3) return;
-  // ---- viscous flux (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
+  // ---- viscous flux in FP32 (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
   const bool turb = (c.iturb == 0);
   const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);
   const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);
+  float nx[3] = {(float)nv[0], (float)nv[1], (float)nv[2]};
   float ev[3], tvv[3];
   for (int q = 0; q < 3; ++q) {
     const double* E1 = d.gm + (ep + q) * n;
@@ -134,8 +170,8 @@ __global__ void __launch_bounds__(128) k_face_flux_mx(DevPtr d, Par c) {
   }
   const int vars[6] = {1, 2, 3, 4, 7, 8};
   float gx[6], gy[6], gz[6], cc[6];
-  const int nv = turb ? 6 : 4;
-  for (int q = 0; q < nv; ++q) {
+  const int nvv = turb ? 6 : 4;
+  for (int q = 0; q < nvv; ++q) {
     const float* X = P + vars[q] * n;
     float x[18];
 #pragma unroll
@@ -154,7 +190,8 @@ __global__ void __launch_bounds__(128) k_face_flux_mx(DevPtr d, Par c) {
   float txx = mu * (2.0f * gx[0] - c23 * div), tyy = mu * (2.0f * gy[1] - c23 * div), tzz = mu * (2.0f * gz[2] - c23 * div);
   float txy = mu * (gy[0] + gx[1]), txz = mu * (gz[0] + gx[2]), tyz = mu * (gz[1] + gy[2]);
   float kc = turb ? (con + tcon) : con;
-  float uc = cc[0], vc = cc[1], wc = cc[2];
+  // face-average velocities are full values: the shadow holds u - U
+  float uc = cc[0] + (float)c.uref_vec[0], vc = cc[1] + (float)c.uref_vec[1], wc = cc[2] + (float)c.uref_vec[2];
   float fv[NPVM];
   fv[0] = 0.0f;
   fv[1] = txx * nx[0] + txy * nx[1] + txz * nx[2];
@@ -192,9 +229,12 @@ void launch_face_flux_mixed(const Engine& E, cudaStream_t s) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   k_shadow<<<std::max(nsm, 1) * 8, 256, 0, s>>>(E.d, E.par);
-  k_face_flux_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  k_face_flux_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
-  k_face_flux_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
+  k_recon_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
+  k_flux_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
+  k_recon_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
+  k_flux_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
+  k_recon_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
+  k_flux_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
 }
 
 }  // namespace cfd

@@ -1,24 +1,91 @@
-// mixed.cuh -- FP32 face arithmetic of the mixed-precision form (CFD3D_MIXED).
+// mixed.cuh -- device functions of the mixed-precision form (CFD3D_MIXED).
 //
 // Precision map of the mixed form (the FP64 form keeps everything in FP64):
-//   reconstruction, limiters, inviscid and viscous flux arithmetic, stored fluxes  FP32
-//   IF97 Gibbs sums of liquid and vapour                                         df64
-//   saturation pressure, mixture density / enthalpy / sound speed                FP64
-//   residual accumulation, LU-SGS diagonal block and sweeps, state update         FP64
-// The FP32 arithmetic runs on a gauge shadow of the state, (p - pref, u, v, w, T - tref,
-// y1, y2, k, omega), so that rounding is relative to the variations, not to pref or tref.
-// Stored momentum fluxes leave out the uniform pref * n * dl part of the pressure flux;
-// the residual kernel adds it back in FP64 (it is a pure geometric term).  AUSM-type fluxes
-// carry pref * (P+ + P- - 1), evaluated from the odd parts P -/+ 1/2 so that it keeps its
-// relative accuracy at low Mach numbers.
+//   reconstruction and limiters                                         FP32
+//   flux dissipation, split Mach / pressure corrections, viscous fluxes  FP32
+//   Roe-average sound speed (IF97 + mixture)                             FP32
+//   face-state density and enthalpy: IF97 Gibbs sums                     df64
+//                                    saturation test, mixture            FP64
+//   leading-order (central / upwind-transport) flux terms                FP64
+//   residual accumulation, LU-SGS operator, state update and its EOS     FP64 (IF97 in df64)
+//
+// Three devices keep FP32 rounding relative to the flow's variations rather than to its
+// absolute level:
+//  * the state is reconstructed from a gauge shadow pvf = (p - pref, u - U, v - V, w - W,
+//    T - tref, y1, y2, k, omega), U = (U, V, W) the free-stream velocity;
+//  * face densities and enthalpies travel as rho - rho_ref, h - h_ref and their jumps are
+//    formed from the FP64 values;
+//  * a face stores F - Phi.n dl, its flux minus the flux of the uniform free stream through
+//    the same face.  Every scheme returns Phi.n dl for a uniform state, and Phi.n is linear
+//    in n, so the residual adds - Phi . sum(n dl) back in FP64 (zero up to the metrics'
+//    closure error).
 #pragma once
 #include "physics.cuh"
 
 namespace cfd {
 
-// FP32 face state: gauge primitive variables (p - pref, u, v, w, T - tref, y1, y2, k, omega)
-struct FaceStateF { float pv[NPVM]; float rho, h, c2; };
+// ------------------------------------------------------------------ FP32 sound speed
+// Mixture sound speed at (p, T, y1, y2) with every step in FP32: the Roe-average state's
+// c^2, which only scales dissipation and Mach splitting (src/flux_module.f90:237,319,461,588).
+__device__ __forceinline__ float eos_c2_f(int fluid, float p, float t, float y1, float y2, unsigned long long* fb) {
+  Phase<float> l, v, g;
+  if (fluid == 1) {
+    stiffened<float>(p, t, l);
+    ideal_gas<float>(p, t, v);
+  } else {
+    iapws_l<float, true>(p, t, l);
+    iapws_v_meta<float, true>(p, t, p > h2o_pww<float>(t), v);
+  }
+  ideal_gas<float>(p, t, g);
+  float yl = 1.0f - y1 - y2;
+  float il = 1.0f / l.rho, iv = 1.0f / v.rho, ig = 1.0f / g.rho;
+  float rho = 1.0f / (yl * il + y1 * iv + y2 * ig);
+  float r2 = rho * rho;
+  float d6 = r2 * (yl * il * il * l.drdp + y1 * iv * iv * v.drdp + y2 * ig * ig * g.drdp);
+  float d7 = r2 * (yl * il * il * l.drdt + y1 * iv * iv * v.drdt + y2 * ig * ig * g.drdt);
+  float d10 = yl * l.dhdp + y1 * v.dhdp + y2 * g.dhdp;
+  float d11 = yl * l.dhdt + y1 * v.dhdt + y2 * g.dhdt;
+  float c2 = rho * d11 / (rho * d6 * d11 + d7 * (1.0f - rho * d10));
+  if (c2 <= 0.0f) {  // the reference's "alternative calculation for snd2"
+    if (fb) atomicAdd(fb, 1ull);
+    float cl = (l.rho * l.drdp * l.dhdt + l.drdt * (1.0f - l.rho * l.dhdp)) / (l.rho * l.dhdt);
+    float cv = (v.rho * v.drdp * v.dhdt + v.drdt * (1.0f - v.rho * v.dhdp)) / (v.rho * v.dhdt);
+    float cg = (g.rho * g.drdp * g.dhdt + g.drdt * (1.0f - g.rho * g.dhdp)) / (g.rho * g.dhdt);
+    c2 = 1.0f / (r2 * (yl * cl * il * il + y1 * cv * iv * iv + y2 * cg * ig * ig));
+  }
+  return c2;
+}
 
+// ------------------------------------------------------------------ reconstruction clips
+// muscl_clip for the FP32 reconstruction.  Where the MLP factor is exactly 2 the
+// reconstructed y1 (or y2) equals a neighbour's value, typically exactly 0 at the edge of a
+// vapour region; FP64 evaluates it to 0 while FP32 rounds to +-1e-9 |y|.  A value that is
+// negative only by that rounding is taken as the bound itself (0), so the mixed form makes
+// the same clip decision as the FP64 form instead of resetting the state to the cell value.
+__device__ __forceinline__ float clip_lo0(float x, float cell) {
+  const float tol = 1.0e-5f * fabsf(cell);
+  return (x < 0.0f && x >= -tol) ? 0.0f : x;
+}
+__device__ __forceinline__ void muscl_clip_mx(const Par& c, const float* c9, const float* c10, float* xl, float* xr) {
+  for (int k = 5; k <= 6; ++k) { xl[k] = clip_lo0(xl[k], c9[k]); xr[k] = clip_lo0(xr[k], c10[k]); }
+  muscl_clip<float>(c, c9, c10, xl, xr);
+}
+
+// ------------------------------------------------------------------ face states
+// A reconstructed face state as the flux kernel sees it: gauge primitives in FP32 and the
+// FP64 quantities the leading-order flux terms need.
+struct FaceMx {
+  float g[NPVM];      // gauge primitives (p', u', v', w', T', y1, y2, k, omega)
+  double rho, h;      // mixture density and static enthalpy (FP64)
+  double u[3];        // full velocity (FP64)
+  float c2;           // face sound speed (Roe-M and AUSMPW+ pressure sensor only)
+};
+
+// per-face record written by the reconstruction kernel: for each side
+// g[0..npv-1], rho - rho_ref, h - h_ref, c2
+constexpr int FREC_SIDE = NPVM + 3;
+
+// ------------------------------------------------------------------ inviscid flux
 __device__ __forceinline__ float sdst_ratio_min_f(const float* s) {
   float v = fminf(s[8] / s[9], s[9] / s[8]);
   v = fminf(v, fminf(s[10] / s[8], s[8] / s[10]));
@@ -32,55 +99,79 @@ __device__ __forceinline__ float sdst_ratio_min_f(const float* s) {
   return v;
 }
 
-// inviscid face flux in FP32 with gauge pressures (src/flux_module.f90:198-641).  rc2 is
-// the sound speed of the Roe-average state (FP64 mixture EOS) and ravg that state; the
-// returned momentum flux excludes the geometric pref * n * dl term
-__device__ __forceinline__ void inviscid_flux_mx(const Par& c, const float* n, const FaceStateF& L, const FaceStateF& Rs,
-                                                 const float* sdst_g, float rc2, const float* ravg, float* fx) {
+// Inviscid face flux of the mixed form (src/flux_module.f90:198-641), returned as
+// F - Phi.nv (FP64 values to be stored in FP32).  nv is the unnormalised face vector,
+// sdst the gauge pressures of the 18 stencil cells (schemes 2 and 3), rc2 the FP32
+// sound speed of the Roe-average state, ravg_u its full velocity and ravg_s its
+// primitives (scalars k >= 5 used).
+__device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv, const FaceMx& L, const FaceMx& R,
+                                                 const float* sdst, float rc2, const float* ravg_u,
+                                                 const float* ravg_s, double* fx) {
   const int npv = c.npv;
-  float dl = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-  if (dl == 0.0f) {
-    for (int k = 0; k < npv; ++k) fx[k] = 0.0f;
+  const double dl = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+  if (dl == 0.0) {
+    for (int k = 0; k < npv; ++k) fx[k] = 0.0;
     return;
   }
-  float nx = n[0] / dl, ny = n[1] / dl, nz = n[2] / dl;
-  const float* pl = L.pv;
-  const float* pr = Rs.pv;
-  float uull = nx * pl[1] + ny * pl[2] + nz * pl[3];
-  float uurr = nx * pr[1] + ny * pr[2] + nz * pr[3];
-  float srl = sqrtf(L.rho), srr = sqrtf(Rs.rho);
-  float ravg_d = 1.0f / (srl + srr);
-  float hl = L.h + 0.5f * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]);
-  float hr = Rs.h + 0.5f * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]);
-  float rrho = sqrtf(L.rho * Rs.rho);
-  const float nn[3] = {nx, ny, nz};
+  const double n0 = nv[0] / dl, n1 = nv[1] / dl, n2 = nv[2] / dl;
+  const double nn[3] = {n0, n1, n2};
+  const float nf[3] = {(float)n0, (float)n1, (float)n2};
+  const float* pl = L.g;
+  const float* pr = R.g;
+  // FP64 leading-order quantities
+  const double ull = n0 * L.u[0] + n1 * L.u[1] + n2 * L.u[2];
+  const double urr = n0 * R.u[0] + n1 * R.u[1] + n2 * R.u[2];
+  const double HL = L.h + 0.5 * (L.u[0] * L.u[0] + L.u[1] * L.u[1] + L.u[2] * L.u[2]);
+  const double HR = R.h + 0.5 * (R.u[0] * R.u[0] + R.u[1] * R.u[1] + R.u[2] * R.u[2]);
+  // FP32 copies and accurate jumps
+  const float uull = (float)ull, uurr = (float)urr;
+  const float rl = (float)L.rho, rr = (float)R.rho;
+  const float drho = (float)(R.rho - L.rho);
+  const float dH = (float)(HR - HL);
+  const float dun = (float)(urr - ull);
+  const float ulf[3] = {(float)L.u[0], (float)L.u[1], (float)L.u[2]};
+  const float hlf = (float)HL;
+  float du3[3];
+  for (int q = 0; q < 3; ++q) du3[q] = pr[1 + q] - pl[1 + q];   // gauge differences are the velocity jumps
+  const float dp = pr[0] - pl[0];
+  const float rrho = sqrtf(rl * rr);
+  // free-stream flux through the face, subtracted from every scheme's result
+  double phin[NPVM];
+  for (int k = 0; k < npv; ++k) phin[k] = c.phi[k][0] * nv[0] + c.phi[k][1] * nv[1] + c.phi[k][2] * nv[2];
+
   if (c.nscheme == 1 || c.nscheme == 2) {
-    float ravg_ht = (srl * hl + srr * hr) * ravg_d;
-    float u2 = ravg[1] * ravg[1] + ravg[2] * ravg[2] + ravg[3] * ravg[3];
-    float uuu = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
+    const float u2 = ravg_u[0] * ravg_u[0] + ravg_u[1] * ravg_u[1] + ravg_u[2] * ravg_u[2];
+    const float uuu = nf[0] * ravg_u[0] + nf[1] * ravg_u[1] + nf[2] * ravg_u[2];
+    const float srl = sqrtf(rl), srr = sqrtf(rr);
+    const float ravg_ht = (srl * (float)HL + srr * (float)HR) / (srl + srr);
     if (c.nscheme == 1) {
+      // Roe: central part in FP64, dissipation in FP32
       float sndp2 = sndp2_of<float>(c, rc2, u2);
       float q = sndp2 / rc2;
       float uup = 0.5f * (1.0f + q) * uuu;
       float ddd = 0.5f * sqrtf((1.0f - q) * (1.0f - q) * uuu * uuu + 4.0f * sndp2);
       float c_star = 0.5f * (fabsf(uup + ddd) + fabsf(uup - ddd));
       float m_star = 0.5f * (fabsf(uup + ddd) - fabsf(uup - ddd)) / ddd;
-      float du = m_star * (uurr - uull) + (c_star - q * fabsf(uuu) - 0.5f * (1.0f - q) * uuu * m_star) * (pr[0] - pl[0]) / rrho / sndp2;
-      float dp = m_star * (pr[0] - pl[0]) + (c_star - fabsf(uuu) + 0.5f * (1.0f - q) * uuu * m_star) * rrho * (uurr - uull);
+      float du = m_star * dun + (c_star - q * fabsf(uuu) - 0.5f * (1.0f - q) * uuu * m_star) * dp / rrho / sndp2;
+      float dpp = m_star * dp + (c_star - fabsf(uuu) + 0.5f * (1.0f - q) * uuu * m_star) * rrho * dun;
       float au = fabsf(uuu);
-      fx[0] = 0.5f * (L.rho * uull + Rs.rho * uurr - (au * (Rs.rho - L.rho) + du * rrho)) * dl;
+      const double mL = L.rho * ull, mR = R.rho * urr;
+      fx[0] = 0.5 * (mL + mR - (double)(au * drho + du * rrho));
       for (int q3 = 0; q3 < 3; ++q3) {
-        float df = au * (Rs.rho * pr[1 + q3] - L.rho * pl[1 + q3]) + du * rrho * ravg[1 + q3] + dp * nn[q3];
-        fx[1 + q3] = 0.5f * (L.rho * uull * pl[1 + q3] + nn[q3] * pl[0] + Rs.rho * uurr * pr[1 + q3] + nn[q3] * pr[0] - df) * dl;
+        // rho_R u_R - rho_L u_L = rho_R (u_R - u_L) + (rho_R - rho_L) u_L
+        float df = au * (rr * du3[q3] + drho * ulf[q3]) + du * rrho * ravg_u[q3] + dpp * nf[q3];
+        fx[1 + q3] = 0.5 * (mL * L.u[q3] + mR * R.u[q3] + nn[q3] * ((double)pl[0] + (double)pr[0]) - (double)df);
       }
-      float df4 = au * (Rs.rho * hr - pr[0] - L.rho * hl + pl[0]) + du * rrho * ravg_ht + dp * uuu;
-      fx[4] = 0.5f * (L.rho * uull * hl + Rs.rho * uurr * hr - df4) * dl;
+      float df4 = au * (rr * dH + drho * hlf - dp) + du * rrho * ravg_ht + dpp * uuu;
+      fx[4] = 0.5 * (mL * HL + mR * HR - (double)df4);
       for (int k = 5; k < npv; ++k) {
-        float df = au * (Rs.rho * pr[k] - L.rho * pl[k]) + du * rrho * ravg[k];
-        fx[k] = 0.5f * (L.rho * uull * pl[k] + Rs.rho * uurr * pr[k] - df) * dl;
+        float df = au * (rr * (pr[k] - pl[k]) + drho * pl[k]) + du * rrho * ravg_s[k];
+        fx[k] = 0.5 * (mL * (double)pl[k] + mR * (double)pr[k] - (double)df);
       }
+      for (int k = 0; k < npv; ++k) fx[k] = fx[k] * dl - phin[k];
       return;
     }
+    // Roe-M
     float am2rmid_du = sndp2_du_of<float>(c, rc2, u2) / rc2;
     float am2rmid = sndp2_of<float>(c, rc2, u2) / rc2;
     float fmid = sqrtf(am2rmid) * (2.0f - sqrtf(am2rmid));
@@ -93,46 +184,55 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const float* n, c
     float m_tilde = copysignf(1.0f, uuu) * fminf(fabsf(uuu) / amid, 1.0f);
     float m_tilde_du = copysignf(1.0f, uuu) * fminf(fabsf(uuu) / (fmid_du * amid), 1.0f);
     float sd[18];
-    float add0 = 0.1f * fminf(L.rho * L.c2, Rs.rho * Rs.c2);
-    for (int k = 0; k < 18; ++k) sd[k] = sdst_g[k] + (float)c.pref + add0;
+    float add0 = 0.1f * fminf(rl * L.c2, rr * R.c2);
+    for (int k = 0; k < 18; ++k) sd[k] = sdst[k] + (float)c.pref + add0;
     float ff = 1.0f - sdst_ratio_min_f(sd);
     ff = (uuu != 0.0f) ? powf(fabsf(uuu) / amid, ff) : 1.0f;
     float gg = 1.0f - fminf(sd[8] / sd[9], sd[9] / sd[8]);
     gg = (uuu != 0.0f) ? powf(fabsf(uuu) / amid, gg) : 1.0f;
     float add = 1.0f + fabsf(m_tilde), aaa = 1.0f + fabsf(m_tilde_du);
-    float dq[NPVM], fl[NPVM], fr[NPVM], bdq[NPVM];
-    dq[0] = Rs.rho - L.rho;
-    for (int k = 1; k <= 3; ++k) dq[k] = Rs.rho * pr[k] - L.rho * pl[k];
-    dq[4] = Rs.rho * hr - L.rho * hl;
-    for (int k = 5; k < npv; ++k) dq[k] = Rs.rho * pr[k] - L.rho * pl[k];
-    fl[0] = L.rho * uull; fr[0] = Rs.rho * uurr;
+    // jumps of the conservative variables, and of (1, u, H, y..) for bdq
+    float dq[NPVM], bdq[NPVM];
+    dq[0] = drho;
+    for (int k = 1; k <= 3; ++k) dq[k] = rr * du3[k - 1] + drho * ulf[k - 1];
+    dq[4] = rr * dH + drho * hlf;
+    for (int k = 5; k < npv; ++k) dq[k] = rr * (pr[k] - pl[k]) + drho * pl[k];
+    bdq[0] = dq[0] - ff * dp / rc2 / fmid;
+    for (int k = 1; k <= 3; ++k) bdq[k] = bdq[0] * ravg_u[k - 1] + rrho * du3[k - 1];
+    bdq[4] = bdq[0] * ravg_ht + rrho * dH;
+    for (int k = 5; k < npv; ++k) bdq[k] = bdq[0] * ravg_s[k] + rrho * (pr[k] - pl[k]);
+    // central part (b1 F_L - b2 F_R) / (b1 - b2) in FP64
+    const double B1 = b1, B2 = b2, iB = 1.0 / (B1 - B2);
+    const double mL = L.rho * ull, mR = R.rho * urr;
+    double fl[NPVM], fr[NPVM];
+    fl[0] = mL; fr[0] = mR;
     for (int q3 = 0; q3 < 3; ++q3) {
-      fl[1 + q3] = L.rho * uull * pl[1 + q3] + nn[q3] * pl[0];
-      fr[1 + q3] = Rs.rho * uurr * pr[1 + q3] + nn[q3] * pr[0];
+      fl[1 + q3] = mL * L.u[q3] + nn[q3] * (double)pl[0];
+      fr[1 + q3] = mR * R.u[q3] + nn[q3] * (double)pr[0];
     }
-    fl[4] = L.rho * uull * hl; fr[4] = Rs.rho * uurr * hr;
-    for (int k = 5; k < npv; ++k) { fl[k] = L.rho * uull * pl[k]; fr[k] = Rs.rho * uurr * pr[k]; }
-    bdq[0] = dq[0] - ff * (pr[0] - pl[0]) / rc2 / fmid;
-    for (int k = 1; k <= 3; ++k) bdq[k] = bdq[0] * ravg[k] + rrho * (pr[k] - pl[k]);
-    bdq[4] = bdq[0] * ravg_ht + rrho * (hr - hl);
-    for (int k = 5; k < npv; ++k) bdq[k] = bdq[0] * ravg[k] + rrho * (pr[k] - pl[k]);
-    for (int k = 0; k < npv; ++k) fx[k] = (b1 * fl[k] - b2 * fr[k] + b1 * b2 * (dq[k] - gg * bdq[k] / add)) / (b1 - b2) * dl;
+    fl[4] = mL * HL; fr[4] = mR * HR;
+    for (int k = 5; k < npv; ++k) { fl[k] = mL * (double)pl[k]; fr[k] = mR * (double)pr[k]; }
+    const float wdiss = b1 * b2 / (b1 - b2);
+    for (int k = 0; k < npv; ++k)
+      fx[k] = (B1 * fl[k] - B2 * fr[k]) * iB + (double)(wdiss * (dq[k] - gg * bdq[k] / add));
     for (int q3 = 0; q3 < 3; ++q3)
-      fx[1 + q3] = fx[1 + q3] + gg * b1_du * b2_du * rrho * (uurr - uull) * nn[q3] / aaa / (b1_du - b2_du) * dl;
+      fx[1 + q3] += (double)(gg * b1_du * b2_du * rrho * dun * nf[q3] / aaa / (b1_du - b2_du));
+    for (int k = 0; k < npv; ++k) fx[k] = fx[k] * dl - phin[k];
     return;
   }
-  // AUSM family
-  float amid = sqrtf(rc2);
-  float zmr = uurr / amid, zml = uull / amid;
+  // AUSM family: the interface velocity amid * M_1/2 = (u_L + u_R)/2 + small terms is
+  // assembled in FP64 from its leading part and FP32 corrections
+  const float amid = sqrtf(rc2);
+  const float zmr = uurr / amid, zml = uull / amid;
   float fmid, fmid1, am2mid;
   if (c.nscheme == 3) {
-    am2mid = ravg[1] * ravg[1] + ravg[2] * ravg[2] + ravg[3] * ravg[3];
+    am2mid = ravg_u[0] * ravg_u[0] + ravg_u[1] * ravg_u[1] + ravg_u[2] * ravg_u[2];
     float a1 = sndp2_du_of<float>(c, rc2, am2mid) / rc2;
     float a0 = sndp2_of<float>(c, rc2, am2mid) / rc2;
     fmid = sqrtf(a0) * (2.0f - sqrtf(a0));
     fmid1 = sqrtf(a1) * (2.0f - sqrtf(a1));
   } else {
-    float un = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
+    float un = nf[0] * ravg_u[0] + nf[1] * ravg_u[1] + nf[2] * ravg_u[2];
     am2mid = un * un;
     float a0 = sndp2_of<float>(c, rc2, am2mid) / rc2;
     fmid = sqrtf(a0) * (2.0f - sqrtf(a0));
@@ -141,10 +241,8 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const float* n, c
   float alpha = 3.0f / 16.0f * (-4.0f + 5.0f * fmid1 * fmid1);
   alpha = fmaxf(fminf(alpha, 3.0f / 16.0f), -3.0f / 4.0f);
   const float beta = 0.125f;
-  // split Mach numbers and pressure weights.  In FP32 the sums M+(ML) + M-(MR) and
-  // P+(ML) + P-(MR) - 1 cancel (M+ ~ 3/8 + ML/2, M- ~ -3/8 + MR/2 at low Mach), so they are
-  // formed from their odd parts: dpl = P+(ML) - 1/2, dpr = P-(MR) - 1/2, and for subsonic
-  // ML, MR  M+ + M- = (ML + MR)/2 + (ML - MR)(ML + MR)(1/4 - 2 beta + beta (ML^2 + MR^2)).
+  // split Mach numbers M+(ML), M-(MR) and pressure weights; dpl = P+(ML) - 1/2,
+  // dpr = P-(MR) - 1/2 (the odd parts, no cancellation at low Mach)
   float zmmr, pmr, zmpl, ppl, dpl, dpr;
   const bool subl = fabsf(zml) < 1.0f, subr = fabsf(zmr) < 1.0f;
   if (!subr) {
@@ -167,18 +265,22 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const float* n, c
     dpl = 0.25f * zml * (3.0f - zml * zml) + alpha * zml * s2;
     ppl = 0.5f + dpl;
   }
-  const float zsum = (subl && subr)
-      ? 0.5f * (zml + zmr) + (zml - zmr) * (zml + zmr) * ((0.25f - 2.0f * beta) + beta * (zml * zml + zmr * zmr))
-      : zmpl + zmmr;
-  // gauge interface pressure: P+ pl + P- pr + pref (P+ + P- - 1) - dissipation
-  float pdev = (float)(c.pref * ((double)dpl + (double)dpr));
-  float zmpl1, zmmr1, pmid;
+  // amid * (M+ + M-) = (u_L + u_R)/2 + amid * E for subsonic ML, MR, with
+  // E = (ML - MR)(ML + MR)(1/4 - 2 beta + beta (ML^2 + MR^2))
+  double vsum;
+  if (subl && subr)
+    vsum = 0.5 * (ull + urr) + (double)(amid * ((zml - zmr) * (zml + zmr) * ((0.25f - 2.0f * beta) + beta * (zml * zml + zmr * zmr))));
+  else
+    vsum = (double)(amid * (zmpl + zmmr));
+  // gauge interface pressure: P+ p'L + P- p'R + pref (P+ + P- - 1) - dissipation
+  const float pdev = (float)(c.pref * ((double)dpl + (double)dpr));
+  double ml, mr;
+  float pmid;
   if (c.nscheme == 3) {
-    float zmid = zsum;
-    pmid = ppl * pl[0] + pmr * pr[0] + pdev - 2.0f * ppl * pmr * rrho * fmid1 * amid * (uurr - uull);
+    pmid = ppl * pl[0] + pmr * pr[0] + pdev - 2.0f * ppl * pmr * rrho * fmid1 * amid * dun;
     float sd[18];
-    float add0 = 0.1f * fminf(L.rho * L.c2, Rs.rho * Rs.c2);
-    for (int k = 0; k < 18; ++k) sd[k] = sdst_g[k] + (float)c.pref + add0;
+    float add0 = 0.1f * fminf(rl * L.c2, rr * R.c2);
+    for (int k = 0; k < 18; ++k) sd[k] = sdst[k] + (float)c.pref + add0;
     float m1 = fminf(sd[8] / sd[9], sd[9] / sd[8]);
     float ww1 = 1.0f - m1 * m1 * m1;
     float m2 = sdst_ratio_min_f(sd);
@@ -187,32 +289,31 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const float* n, c
     float wq = (1.0f - ww) / fmid;
     float pwl = ((float)((double)pl[0] + c.pref) / pmt) * wq;
     float pwr = ((float)((double)pr[0] + c.pref) / pmt) * wq;
-    float dpw = ((pr[0] - pl[0]) / pmt) * wq;   // pwr - pwl from the gauge difference
-    if (zmid >= 0.0f) {
-      float sc = rrho / L.rho;
+    float dpw = (dp / pmt) * wq;   // pwr - pwl from the gauge difference
+    if (vsum >= 0.0) {
+      // both weights scaled by the left density, as the reference does
+      float sc = rrho / rl;
       pwl *= sc; pwr *= sc; dpw *= sc;
-      // zmpl + zmmr ((1 - ww)(1 + pwr) - pwl), with zmpl + zmmr taken from zsum
-      zmpl1 = zsum + zmmr * (dpw - ww * (1.0f + pwr));
-      zmmr1 = zmmr * ww * (1.0f + pwr);
+      // M+_1 = (M+ + M-) + M- ((pwr - pwl) - ww (1 + pwr)), M-_1 = M- ww (1 + pwr)
+      ml = L.rho * (vsum + (double)(amid * zmmr * (dpw - ww * (1.0f + pwr))));
+      mr = R.rho * (double)(amid * zmmr * ww * (1.0f + pwr));
     } else {
-      float sc = rrho / Rs.rho;
+      float sc = rrho / rr;
       pwl *= sc; pwr *= sc; dpw *= sc;
-      zmpl1 = zmpl * ww * (1.0f + pwl);
-      zmmr1 = zsum + zmpl * (-dpw - ww * (1.0f + pwl));
+      ml = L.rho * (double)(amid * zmpl * ww * (1.0f + pwl));
+      mr = R.rho * (vsum + (double)(amid * zmpl * (-dpw - ww * (1.0f + pwl))));
     }
   } else {
     const float kp = 0.25f;
-    float zmid = zsum - kp * fmaxf(1.0f - am2mid / rc2, 0.0f) * (pr[0] - pl[0]) / rrho / rc2 / fmid;
-    pmid = ppl * pl[0] + pmr * pr[0] + pdev - 2.0f * ppl * pmr * rrho * fmid * amid * (uurr - uull);
-    if (zmid > 0.0f) { zmpl1 = zmid; zmmr1 = 0.0f; } else { zmmr1 = zmid; zmpl1 = 0.0f; }
+    double vmid = vsum - (double)(amid * kp * fmaxf(1.0f - am2mid / rc2, 0.0f) * dp / rrho / rc2 / fmid);
+    pmid = ppl * pl[0] + pmr * pr[0] + pdev - 2.0f * ppl * pmr * rrho * fmid * amid * dun;
+    if (vmid > 0.0) { ml = L.rho * vmid; mr = 0.0; } else { mr = R.rho * vmid; ml = 0.0; }
   }
-  float ml = zmpl1 * amid * L.rho, mr = zmmr1 * amid * Rs.rho;
-  fx[0] = (ml + mr) * dl;
-  fx[1] = (ml * pl[1] + mr * pr[1] + pmid * nx) * dl;
-  fx[2] = (ml * pl[2] + mr * pr[2] + pmid * ny) * dl;
-  fx[3] = (ml * pl[3] + mr * pr[3] + pmid * nz) * dl;
-  fx[4] = (ml * hl + mr * hr) * dl;
-  for (int k = 5; k < npv; ++k) fx[k] = (ml * pl[k] + mr * pr[k]) * dl;
+  fx[0] = ml + mr;
+  for (int q3 = 0; q3 < 3; ++q3) fx[1 + q3] = ml * L.u[q3] + mr * R.u[q3] + (double)pmid * nn[q3];
+  fx[4] = ml * HL + mr * HR;
+  for (int k = 5; k < npv; ++k) fx[k] = ml * (double)pl[k] + mr * (double)pr[k];
+  for (int k = 0; k < npv; ++k) fx[k] = fx[k] * dl - phin[k];
 }
 
 }  // namespace cfd

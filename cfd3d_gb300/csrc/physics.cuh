@@ -31,6 +31,10 @@ struct Par {
   double dt_phy, cfl, c_v, c_c, pref, uref, str, rhoref, l_chord;
   double kref, oref, emutref;
   double uref_vec[3], tref, y1ref, y2ref;   // free-stream state bcinfo%pv (src/bc_module.f90:133-146)
+  // mixed form: reference density / enthalpy and the gauge flux tensor of the uniform
+  // free stream, phi[v][e] = e-component of the flux of variable v (pressure part omitted)
+  double href;
+  double phi[NPVM][3];
 };
 
 __device__ __forceinline__ double sq(double x) { return x * x; }

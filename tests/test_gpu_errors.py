@@ -1,0 +1,37 @@
+"""Error paths of the C ABI on a GPU, made on the host: a non-finite uploaded state, and
+out-of-range arguments.  Nothing here faults the device; the handle stays usable."""
+import numpy as np
+import pytest
+
+from cfd3d_gb300 import abi, cases, native
+from cfd3d_gb300.native import Cfd3dError
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_nonfinite_state_is_reported_and_the_handle_recovers(precision):
+    c = cases.make("plain_small", scale=8)
+    e = native.Engine(c, precision=precision)
+    e.initialize(c["pv0"])
+    clean = e.download(0)
+    bad = {k: v.copy() for k, v in clean.items()}
+    bad["pv"][5, 5, 5, 0] = np.nan
+    e.upload(0, pv=bad["pv"])
+    with pytest.raises(Cfd3dError) as ei:
+        e.iterate(1, 1, 0.0)
+    assert ei.value.code == abi.ERR_NONFINITE
+    e.upload(0, pv=clean["pv"], dv=clean["dv"], tv=clean["tv"] if e.ntv else None)
+    _, res, _ = e.iterate(1, 2, 0.0)
+    assert np.all(np.isfinite(res))
+
+
+def test_block_index_out_of_range():
+    c = cases.make("plain_small", scale=8)
+    e = native.Engine(c)
+    e.initialize(c["pv0"])
+    lib = native.lib()
+    assert lib.cfd3d_residual(e.h, 3, None, None, None, None) == abi.ERR_ARG
+    assert lib.cfd3d_download_state(e.h, -1, None, None, None, None, None) == abi.ERR_ARG
+    assert b"block" in lib.cfd3d_last_error(e.h)
+    e.residual(0)   # still usable
