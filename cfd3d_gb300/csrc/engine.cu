@@ -519,7 +519,11 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
     long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
     const long long n = d.ncell;
     double old[NPVM], p[NPVM];
-    for (int v = 0; v < npv; ++v) { old[v] = d.pv[v * n + g]; p[v] = old[v] + d.dqs[v * n + g]; }
+    for (int v = 0; v < npv; ++v) {
+      old[v] = d.pv[v * n + g];
+      p[v] = old[v] + d.dqs[v * n + g];
+      if (!isfinite(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
+    }
     p[0] = fmax(-c.pref + 1.0e1, p[0]);
     p[5] = fmin(1.0, fmax(0.0, p[5]));
     p[6] = fmin(1.0, fmax(0.0, p[6]));
@@ -536,7 +540,10 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
       sq_[v] += df * df;
       if (!isfinite(p[v])) bad = 1;
     }
-    for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
+    for (int v = 0; v < NDV; ++v) {
+      d.dv[v * n + g] = dv[v];
+      if (!isfinite(dv[v])) bad = 1;
+    }
     for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
     double dp = fabs(old[0] - p[0]);
     if (dp > dpmax) { dpmax = dp; dpidx = t; }   // t increases: ties keep the first cell
