@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include "engine.cuh"
 
@@ -846,6 +847,53 @@ int cfd3d_eos_eval(int fluid, int ngas, int with_prop, int64_t n, const double* 
   }
   cudaFree(dp); cudaFree(dt); cudaFree(dy1); cudaFree(dy2); cudaFree(ddv); cudaFree(dtv); cudaFree(fb);
   return rc;
+}
+
+// ---- pointwise EOS through a static device buffer (no allocation)
+namespace {
+struct EosScratch {
+  double p[CFD3D_EOS_NOALLOC_MAX], t[CFD3D_EOS_NOALLOC_MAX], y1[CFD3D_EOS_NOALLOC_MAX], y2[CFD3D_EOS_NOALLOC_MAX];
+  double dv[NDV * CFD3D_EOS_NOALLOC_MAX], tv[2 * CFD3D_EOS_NOALLOC_MAX];
+  unsigned long long fallbacks;   // must start at zero: the kernel counts into it
+};
+constexpr int EOS_SCRATCH_DEVICES = 64;
+std::mutex g_eos_scratch_mu;
+EosScratch* g_eos_scratch_ptr[EOS_SCRATCH_DEVICES] = {};
+}  // namespace
+static __device__ __align__(256) EosScratch g_eos_scratch;
+
+int cfd3d_eos_eval_noalloc(int fluid, int ngas, int with_prop, int64_t n, const double* p, const double* t,
+                           const double* y1, const double* y2, double* dv, double* tv) {
+  if (n <= 0 || n > CFD3D_EOS_NOALLOC_MAX || !p || !t || !y1 || !y2 || !dv || (fluid != 1 && fluid != 2) ||
+      ngas != 1)
+    return CFD3D_ERR_ARG;
+  int ndev = 0, dev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CFD3D_ERR_NODEVICE;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= EOS_SCRATCH_DEVICES) return CFD3D_ERR_CUDA;
+  EosScratch* S = nullptr;
+  {
+    // per-device set-up on the first call: the buffer's device address
+    std::lock_guard<std::mutex> lock(g_eos_scratch_mu);
+    if (!g_eos_scratch_ptr[dev]) {
+      void* ptr = nullptr;
+      if (cudaGetSymbolAddress(&ptr, g_eos_scratch) != cudaSuccess || !ptr) return CFD3D_ERR_CUDA;
+      g_eos_scratch_ptr[dev] = static_cast<EosScratch*>(ptr);
+    }
+    S = g_eos_scratch_ptr[dev];
+  }
+  const size_t b = (size_t)n * 8;
+  if (cudaMemcpy(S->p, p, b, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(S->t, t, b, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(S->y1, y1, b, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(S->y2, y2, b, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(&S->fallbacks, 0, sizeof(unsigned long long)) != cudaSuccess)
+    return CFD3D_ERR_CUDA;
+  k_eos_points<<<(unsigned)((n + 127) / 128), 128>>>(fluid, with_prop, n, S->p, S->t, S->y1, S->y2, S->dv, S->tv,
+                                                      &S->fallbacks);
+  if (cudaGetLastError() != cudaSuccess) return CFD3D_ERR_CUDA;
+  if (cudaMemcpy(dv, S->dv, b * NDV, cudaMemcpyDeviceToHost) != cudaSuccess) return CFD3D_ERR_CUDA;
+  if (tv && with_prop && cudaMemcpy(tv, S->tv, b * 2, cudaMemcpyDeviceToHost) != cudaSuccess) return CFD3D_ERR_CUDA;
+  return CFD3D_OK;
 }
 
 int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* blocks, cfd3d_handle** out) {

@@ -52,6 +52,7 @@ def lib():
     L.cfd3d_residual.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_grid_metrics.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_eos_eval.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
+    L.cfd3d_eos_eval_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
     L.cfd3d_stats.argtypes = [H, C.POINTER(C.c_int64), ip]
     L.cfd3d_time_iterate.argtypes = [H, C.c_int, dp]
     L.cfd3d_profile_iterate.argtypes = [H, dp]
@@ -62,7 +63,7 @@ def lib():
 
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
            "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_iterate", "cfd3d_iterate_n",
-           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_stats",
+           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device"]
 STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
 
@@ -87,6 +88,22 @@ def eos_eval(p, t, y1, y2, fluid=2, prop=False):
     rc = lib().cfd3d_eos_eval(fluid, 1, 1 if prop else 0, n, _p(p), _p(t), _p(y1), _p(y2), _p(dv), _p(tv))
     if rc:
         raise Cfd3dError(rc, "cfd3d_eos_eval failed")
+    return dv, tv
+
+
+EOS_NOALLOC_MAX = 4096   # CFD3D_EOS_NOALLOC_MAX
+
+
+def eos_eval_noalloc(p, t, y1, y2, fluid=2, prop=False):
+    """eos_eval through the library's static device buffer (no device allocation);
+    at most EOS_NOALLOC_MAX points per call, calls on one device must not overlap."""
+    p, t, y1, y2 = (np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (p, t, y1, y2))
+    n = p.size
+    dv = np.zeros((n, 18))
+    tv = np.zeros((n, 2))
+    rc = lib().cfd3d_eos_eval_noalloc(fluid, 1, 1 if prop else 0, n, _p(p), _p(t), _p(y1), _p(y2), _p(dv), _p(tv))
+    if rc:
+        raise Cfd3dError(rc, "cfd3d_eos_eval_noalloc failed (n = %d, limit %d)" % (n, EOS_NOALLOC_MAX))
     return dv, tv
 
 
