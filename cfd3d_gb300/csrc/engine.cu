@@ -8,6 +8,7 @@
 //   k_ghost x3            boundary program: faces+halos, edges, corners (bc_module.f90:1235-1396)
 //   k_face_flux x3        inviscid + viscous face fluxes per direction (rhs_module.f90:282-538)
 //   k_rhs                 flux differences + cavitation / SST / dual-time sources (:540-642)
+//   k_gather_rec          sweep records of every cell in plane-major order
 //   k_sweep (fwd) x S     forward LU-SGS sweep, one launch per hyperplane i+j+k = s
 //   k_sweep (bwd) x S     backward sweep                          (update_module.f90:486-670)
 //   k_update              pv += dq, clipping, EOS with transport, residual partial sums (:672-700)
@@ -444,63 +445,78 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
 }
 
 // ------------------------------------------------------------------ LU-SGS sweeps
-__device__ __forceinline__ void load_nbr(const DevPtr& d, const Par& c, long long g, double* pv, double* dv,
-                                         double* tv, double& vol) {
-  const long long n = d.ncell;
-  for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
-  for (int v = 0; v < 14; ++v) dv[v] = d.dv[v * n + g];
-  tv[0] = tv[1] = tv[2] = 0.0;
-  for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
-  vol = d.gm[GM_GRD * n + g];
+// The sweeps work in the plane-major numbering t (setup_planes).  k_gather_rec copies what
+// they read of each cell -- as itself (diagonal block, residual) and as a neighbour (state,
+// split-Jacobian coefficients, + face vectors) -- into sweep records at t, once per
+// iteration; each hyperplane launch then reads its own records and those of the previous
+// (next) plane with coalesced loads.  dcv and dqs live at t as well; k_update reads dqs
+// through pos[g].
+__global__ void __launch_bounds__(256) k_gather_rec(DevPtr d, Par c) {
+  const long long nint = d.nint, n = d.ncell;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int pvi[7] = {1, 2, 3, 5, 6, 7, 8};
+  const int dvi[10] = {0, 1, 6, 7, 8, 9, 10, 11, 12, 13};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nint; t += stride) {
+    const long long g = d.cells[t];
+    double* R = d.rec;
+    for (int q = 0; q < 7; ++q) R[(REC_PV + q) * nint + t] = (pvi[q] < c.npv) ? d.pv[pvi[q] * n + g] : 0.0;
+    for (int q = 0; q < 10; ++q) R[(REC_DV + q) * nint + t] = d.dv[dvi[q] * n + g];
+    R[REC_BETA * nint + t] = d.prep[PREP_BETA * n + g];
+    R[REC_EVV * nint + t] = d.prep[PREP_EVV * n + g];
+    for (int q = 0; q < 6; ++q) R[(REC_SPEC + q) * nint + t] = d.prep[(PREP_SPEC + q) * n + g];
+    for (int q = 0; q < 9; ++q) R[(REC_FACE + q) * nint + t] = d.gm[(GM_CX + q) * n + g];
+    for (int q = 0; q < PREP_DIAG; ++q) R[(REC_DIAG + q) * nint + t] = d.prep[q * n + g];
+    for (int v = 0; v < c.npv; ++v) R[(REC_RES + v) * nint + t] = d.res[v * n + g];
+  }
+}
+
+// a cell's pv / dv as the Jacobian and diagonal routines index them, from its record
+__device__ __forceinline__ void rec_state(const double* R, long long nint, long long t, double* pv, double* dv) {
+  pv[0] = 0.0; pv[4] = 0.0;
+  pv[1] = R[(REC_PV + 0) * nint + t]; pv[2] = R[(REC_PV + 1) * nint + t]; pv[3] = R[(REC_PV + 2) * nint + t];
+  pv[5] = R[(REC_PV + 3) * nint + t]; pv[6] = R[(REC_PV + 4) * nint + t];
+  pv[7] = R[(REC_PV + 5) * nint + t]; pv[8] = R[(REC_PV + 6) * nint + t];
+  dv[0] = R[(REC_DV + 0) * nint + t]; dv[1] = R[(REC_DV + 1) * nint + t];
+  dv[2] = dv[3] = dv[4] = dv[5] = 0.0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) dv[6 + q] = R[(REC_DV + 2 + q) * nint + t];
 }
 
 template <bool FWD>
-__global__ void __launch_bounds__(128) k_sweep(DevPtr d, Par c, const int* __restrict__ cells, long long p0, long long p1) {
-  long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, long long p1) {
+  const long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= p1) return;
-  const long long g = cells[t];
-  const int b = find_block_cell(d.blk, d.nblk, g);
-  const BlockGeom& B = d.blk[b];
-  const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
-  long long rel = g - B.off;
-  const int i = (int)(rel % B.ni) - 1;
-  const int j = (int)((rel / B.ni) % B.nj) - 1;
-  const int k = (int)(rel / sk) - 1;
+  const long long nint = d.nint;
+  const double* R = d.rec;
   const int npv = c.npv;
   double acc[NPVM];
-  if (FWD) for (int v = 0; v < npv; ++v) acc[v] = d.res[v * n + g];
-  else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * n + g];
-  const long long strides[3] = {1, sj, sk};
-  const int pos[3] = {i, j, k};
-  const int lim[3] = {B.imax, B.jmax, B.kmax};
-  const int plane[3] = {GM_CX, GM_EX, GM_TX};
+  if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
+  else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
-    // forward: lower neighbour, its + face; backward: upper neighbour, its - face
-    const bool interior = FWD ? (pos[q] - 1 >= 2) : (pos[q] + 1 <= lim[q]);
-    if (!interior) continue;  // dq is zero outside the block
-    const long long nb = FWD ? g - strides[q] : g + strides[q];
-    const long long fidx = FWD ? nb : g;
-    double nx[3];
-    face_vec(d, plane[q], fidx, nx);
-    double pv[NPVM], dv[14], dq[NPVM];
-    for (int v = 0; v < npv; ++v) { pv[v] = d.pv[v * n + nb]; dq[v] = d.dqs[v * n + nb]; }
-    for (int v = 0; v < 14; ++v) dv[v] = d.dv[v * n + nb];
-    const double spec = d.prep[(PREP_SPEC + 2 * q + (FWD ? 1 : 0)) * n + nb];
-    const double beta = d.prep[PREP_BETA * n + nb];
-    const double evv = d.prep[PREP_EVV * n + nb];
+    // forward: lower neighbour through its + face; backward: upper neighbour through this
+    // cell's + face.  Neighbours outside the block carry dq = 0.
+    const int nb = FWD ? d.nbf[q * nint + t] : d.nbb[q * nint + t];
+    if (nb < 0) continue;
+    const long long fr = FWD ? nb : t;
+    double nx[3], pv[NPVM], dv[14], dq[NPVM];
+    for (int e = 0; e < 3; ++e) nx[e] = R[(REC_FACE + 3 * q + e) * nint + fr];
+    rec_state(R, nint, nb, pv, dv);
+    for (int v = 0; v < npv; ++v) dq[v] = d.dqs[v * nint + nb];
+    const double spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + nb];
+    const double beta = R[REC_BETA * nint + nb];
+    const double evv = R[REC_EVV * nint + nb];
     jac_apply_pre(npv, nx, pv, dv, spec, beta, evv, FWD ? 1.0 : -1.0, dq, acc);
   }
-  if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * n + g] = acc[v];
+  if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
   double pv[NPVM], dv[14], o[PREP_DIAG];
-  for (int v = 0; v < npv; ++v) pv[v] = d.pv[v * n + g];
-  for (int v = 0; v < 14; ++v) dv[v] = d.dv[v * n + g];
-  for (int q = 0; q < PREP_DIAG; ++q) o[q] = d.prep[q * n + g];
+  rec_state(R, nint, t, pv, dv);
+  for (int q = 0; q < PREP_DIAG; ++q) o[q] = R[(REC_DIAG + q) * nint + t];
   Diag D;
   diag_from_array(o, D);
   double x[NPVM];
   diag_solve(c, D, pv, dv, acc, x);
-  for (int v = 0; v < npv; ++v) d.dqs[v * n + g] = x[v];
+  for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
 }
 
 // ------------------------------------------------------------------ update + residual
@@ -519,10 +535,11 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
     int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
     long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
     const long long n = d.ncell;
+    const long long pq = d.pos[g];   // plane-major position of the sweep's dq
     double old[NPVM], p[NPVM];
     for (int v = 0; v < npv; ++v) {
       old[v] = d.pv[v * n + g];
-      p[v] = old[v] + d.dqs[v * n + g];
+      p[v] = old[v] + d.dqs[v * d.nint + pq];
       if (!isfinite(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
     }
     p[0] = fmax(-c.pref + 1.0e1, p[0]);
@@ -741,15 +758,18 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   stage(4);
   n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
+  k_gather_rec<<<E.red_grid, 256, 0, s>>>(d, c);
+  ++n;
   const int np = (int)E.plane_off.size() - 1;
+  const int TS = 64;
   for (int q = 0; q < np; ++q) {
     long long a = E.plane_off[q], b = E.plane_off[q + 1];
-    if (b > a) { k_sweep<true><<<nblk_of(b - a, T), T, 0, s>>>(d, c, E.d_planes, a, b); ++n; }
+    if (b > a) { k_sweep<true><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b); ++n; }
   }
   stage(5);
   for (int q = np - 1; q >= 0; --q) {
     long long a = E.plane_off[q], b = E.plane_off[q + 1];
-    if (b > a) { k_sweep<false><<<nblk_of(b - a, T), T, 0, s>>>(d, c, E.d_planes, a, b); ++n; }
+    if (b > a) { k_sweep<false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b); ++n; }
   }
   stage(6);
   if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c);
@@ -1011,6 +1031,9 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   if (!setup_geometry(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
   if (!setup_ghost_program(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
   setup_planes(E);
+  E.d.cells = E.d_planes; E.d.pos = E.d_pos; E.d.nbf = E.d_nbf; E.d.nbb = E.d_nbb;
+  if (!E.d_planes || !E.d_pos || !E.d_nbf || !E.d_nbb) { E.err = "device allocation failed (sweep maps)"; return CFD3D_ERR_NOMEM; }
+  if (cudaMalloc(&E.d.rec, (size_t)NREC * E.nint * 8) != cudaSuccess) { E.err = "device allocation failed (sweep records)"; return CFD3D_ERR_NOMEM; }
   CFD_CUDA(cudaDeviceSynchronize());
   return CFD3D_OK;
 }
@@ -1028,6 +1051,10 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d.sc);
   for (int p = 0; p < 3; ++p) cudaFree(E.d_ops[p]);
   cudaFree(E.d_planes);
+  cudaFree(E.d_pos);
+  cudaFree(E.d_nbf);
+  cudaFree(E.d_nbb);
+  cudaFree(E.d.rec);
   if (E.st) cudaStreamDestroy(E.st);
   delete h;
 }

@@ -70,6 +70,23 @@ struct DevPtr {
   // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
   float *pvf, *fi32, *fv32;
   float* frec;       // mixed form: reconstructed face states of one direction (2 x 12 planes)
+  // LU-SGS sweep records in plane-major order t (REC_* planes of nint entries); dqs and
+  // dcv are plane-major too
+  double* rec;
+  const int *cells, *pos, *nbf, *nbb;
+};
+
+// sweep record planes: what the sweeps read of a cell, as itself and as a neighbour
+enum {
+  REC_PV = 0,      // pv 1, 2, 3, 5, 6, 7, 8
+  REC_DV = 7,      // dv 0, 1, 6 .. 13
+  REC_BETA = 17,
+  REC_EVV = 18,
+  REC_SPEC = 19,   // 6 face spectral radii
+  REC_FACE = 25,   // the cell's + face vectors cx, ex, tx
+  REC_DIAG = 34,   // 23 values of the closed-form diagonal block
+  REC_RES = 57,    // residual (npv)
+  NREC = 66
 };
 
 struct Engine {
@@ -81,7 +98,11 @@ struct Engine {
   // ghost program: phase 0 faces + halos, 1 edges, 2 corners
   GhostOp* d_ops[3] = {nullptr, nullptr, nullptr};
   int nops[3] = {0, 0, 0};
+  // LU-SGS plane-major numbering (setup_planes): cells[t], pos[g], lower / upper neighbours
   int* d_planes = nullptr;
+  int* d_pos = nullptr;
+  int* d_nbf = nullptr;
+  int* d_nbb = nullptr;
   std::vector<long long> plane_off;
   cudaStream_t st = nullptr;
   cudaGraphExec_t graph = nullptr;

@@ -653,22 +653,56 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
 
 // ---------------------------------------------------------------------------------------
 void setup_planes(Engine& E) {
+  // Hyperplanes (i-2)+(j-2)+(k-2) = s of every block, merged by s; within a plane cells are
+  // ordered by block, k, j.  The sweep works in this plane-major numbering t: cells[t] is
+  // the padded cell, pos[g] its inverse, and nbf / nbb the positions of the three lower /
+  // upper interior neighbours (-1 outside the block).  With the (k, j) order, consecutive t
+  // of plane s have consecutive neighbours in plane s -/+ 1, so the sweep's loads coalesce.
   long long maxs = 0;
   for (auto& B : E.blk) maxs = std::max<long long>(maxs, (B.imax - 2) + (B.jmax - 2) + (B.kmax - 2));
-  std::vector<std::vector<int>> pl(maxs + 1);
+  std::vector<long long> count(maxs + 2, 0);
   for (auto& B : E.blk)
     for (int k = 2; k <= B.kmax; ++k)
       for (int j = 2; j <= B.jmax; ++j)
-        for (int i = 2; i <= B.imax; ++i)
-          pl[(i - 2) + (j - 2) + (k - 2)].push_back((int)(B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1))));
-  std::vector<int> flat;
-  E.plane_off.assign(1, 0);
-  for (auto& p : pl) {
-    flat.insert(flat.end(), p.begin(), p.end());
-    E.plane_off.push_back((long long)flat.size());
+        for (int i = 2; i <= B.imax; ++i) ++count[(i - 2) + (j - 2) + (k - 2) + 1];
+  E.plane_off.assign(maxs + 2, 0);
+  for (long long s = 1; s <= maxs + 1; ++s) E.plane_off[s] = E.plane_off[s - 1] + count[s];
+  const long long nint = E.plane_off[maxs + 1];
+  std::vector<long long> fill(E.plane_off.begin(), E.plane_off.end() - 1);
+  std::vector<int> cells(nint), pos(E.ncell, -1);
+  for (auto& B : E.blk)
+    for (int k = 2; k <= B.kmax; ++k)
+      for (int j = 2; j <= B.jmax; ++j)
+        for (int i = 2; i <= B.imax; ++i) {
+          long long t = fill[(i - 2) + (j - 2) + (k - 2)]++;
+          long long g = B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1));
+          cells[t] = (int)g;
+          pos[g] = (int)t;
+        }
+  std::vector<int> nbf(3 * nint, -1), nbb(3 * nint, -1);
+  for (auto& B : E.blk) {
+    const long long st[3] = {1, B.ni, (long long)B.ni * B.nj};
+    for (int k = 2; k <= B.kmax; ++k)
+      for (int j = 2; j <= B.jmax; ++j)
+        for (int i = 2; i <= B.imax; ++i) {
+          long long g = B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1));
+          const int t = pos[g];
+          const int p3[3] = {i, j, k};
+          const int lim[3] = {B.imax, B.jmax, B.kmax};
+          for (int q = 0; q < 3; ++q) {
+            if (p3[q] - 1 >= 2) nbf[q * nint + t] = pos[g - st[q]];
+            if (p3[q] + 1 <= lim[q]) nbb[q * nint + t] = pos[g + st[q]];
+          }
+        }
   }
-  cudaMalloc(&E.d_planes, flat.size() * sizeof(int));
-  cudaMemcpy(E.d_planes, flat.data(), flat.size() * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMalloc(&E.d_planes, nint * sizeof(int));
+  cudaMemcpy(E.d_planes, cells.data(), nint * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMalloc(&E.d_pos, E.ncell * sizeof(int));
+  cudaMemcpy(E.d_pos, pos.data(), E.ncell * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMalloc(&E.d_nbf, 3 * nint * sizeof(int));
+  cudaMemcpy(E.d_nbf, nbf.data(), 3 * nint * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMalloc(&E.d_nbb, 3 * nint * sizeof(int));
+  cudaMemcpy(E.d_nbb, nbb.data(), 3 * nint * sizeof(int), cudaMemcpyHostToDevice);
 }
 
 }  // namespace cfd
