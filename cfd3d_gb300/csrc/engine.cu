@@ -8,7 +8,6 @@
 //   k_ghost x3            boundary program: faces+halos, edges, corners (bc_module.f90:1235-1396)
 //   k_face_flux x3        inviscid + viscous face fluxes per direction (rhs_module.f90:282-538)
 //   k_rhs                 flux differences + cavitation / SST / dual-time sources (:540-642)
-//   k_gather_rec          sweep records of every cell in plane-major order
 //   k_sweep (fwd) x S     forward LU-SGS sweep, one launch per hyperplane i+j+k = s
 //   k_sweep (bwd) x S     backward sweep                          (update_module.f90:486-670)
 //   k_update              pv += dq, clipping, EOS with transport, residual partial sums (:672-700)
@@ -70,7 +69,8 @@ __global__ void k_init(DevPtr d, Par c, int b) {
   const long long n = d.ncell;
   double pv[NPVM], dv[NDV], tv[3] = {0.0, 0.0, 0.0};
   for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
-  deteos<MX>(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
+  if (MX) deteos_split(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
+  else deteos<false>(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
   if (c.iturb == 0) tv[2] = c.emutref;
   for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
   for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
@@ -420,8 +420,8 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
     }
   }
   for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
-  if (!d.prep) return;
-  // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous term)
+  // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous
+  // term), written with its state and residual as the cell's sweep record at pos[g]
   double tvc[3] = {0.0, 0.0, 0.0};
   for (int q = 0; q < c.ntv; ++q) tvc[q] = d.tv[q * n + g];
   double fc[18];
@@ -435,63 +435,64 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
   if (c.iturb == 0) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
   Diag D;
   diag_prepare(c, pv2, dv, tvc, fc, vol, d.dt[g], ic, it4, D);
-  double o[NPREP];
-  diag_to_array(D, o);
-  for (int q = 0; q < 6; ++q) o[PREP_SPEC + q] = face_spectral(c, fc + 3 * q, pv2, dv);
-  double sndp2 = sndp2_of<double>(c, dv[5], pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3]);
-  o[PREP_BETA] = 1.0 / sndp2 - 1.0 / dv[5] + dv[6];
-  o[PREP_EVV] = 2.0 * eigenvis_of(c, dv, tvc) / vol;
-  for (int q = 0; q < NPREP; ++q) d.prep[q * n + g] = o[q];
+  double o[NREC];
+  for (int q = 0; q < NREC; ++q) o[q] = 0.0;
+  const int pvi[7] = {1, 2, 3, 5, 6, 7, 8};
+  const int dvi[10] = {0, 1, 6, 7, 8, 9, 10, 11, 12, 13};
+  for (int q = 0; q < 7; ++q) o[REC_PV + q] = (pvi[q] < npv) ? pv2[pvi[q]] : 0.0;
+  for (int q = 0; q < 10; ++q) o[REC_DV + q] = dv[dvi[q]];
+  diag_to_array(D, o + REC_DIAG);
+  if (MX) {
+    // the spectral radii only scale the implicit operator: FP32
+    float pvf[NPVM], dvf[6];
+    for (int q = 0; q < NPVM; ++q) pvf[q] = (q < npv) ? (float)pv2[q] : 0.0f;
+    for (int q = 0; q < 6; ++q) dvf[q] = (float)dv[q];
+    for (int q = 0; q < 6; ++q) {
+      const float nf[3] = {(float)fc[3 * q], (float)fc[3 * q + 1], (float)fc[3 * q + 2]};
+      o[REC_SPEC + q] = (double)face_spectral<float>(c, nf, pvf, dvf);
+    }
+  } else {
+    for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = face_spectral<double>(c, fc + 3 * q, pv2, dv);
+  }
+  const double sndp2 = sndp2_of<double>(c, dv[5], pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3]);
+  o[REC_BETA] = 1.0 / sndp2 - 1.0 / dv[5] + dv[6];
+  o[REC_EVV] = 2.0 * eigenvis_of(c, dv, tvc) / vol;
+  for (int e = 0; e < 3; ++e) {
+    o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e];
+  }
+  for (int v = 0; v < npv; ++v) o[REC_RES + v] = res[v];
+  const long long nint = d.nint, tp = d.pos[g];
+  for (int q = 0; q < NREC; ++q) d.rec[q * nint + tp] = o[q];
+  if (MX) for (int q = 0; q < REC_DIAG; ++q) d.recf[q * nint + tp] = (float)o[q];
 }
 
 // ------------------------------------------------------------------ LU-SGS sweeps
-// The sweeps work in the plane-major numbering t (setup_planes).  k_gather_rec copies what
-// they read of each cell -- as itself (diagonal block, residual) and as a neighbour (state,
-// split-Jacobian coefficients, + face vectors) -- into sweep records at t, once per
-// iteration; each hyperplane launch then reads its own records and those of the previous
-// (next) plane with coalesced loads.  dcv and dqs live at t as well; k_update reads dqs
-// through pos[g].
-__global__ void __launch_bounds__(256) k_gather_rec(DevPtr d, Par c) {
-  const long long nint = d.nint, n = d.ncell;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const int pvi[7] = {1, 2, 3, 5, 6, 7, 8};
-  const int dvi[10] = {0, 1, 6, 7, 8, 9, 10, 11, 12, 13};
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nint; t += stride) {
-    const long long g = d.cells[t];
-    double* R = d.rec;
-    for (int q = 0; q < 7; ++q) R[(REC_PV + q) * nint + t] = (pvi[q] < c.npv) ? d.pv[pvi[q] * n + g] : 0.0;
-    for (int q = 0; q < 10; ++q) R[(REC_DV + q) * nint + t] = d.dv[dvi[q] * n + g];
-    R[REC_BETA * nint + t] = d.prep[PREP_BETA * n + g];
-    R[REC_EVV * nint + t] = d.prep[PREP_EVV * n + g];
-    for (int q = 0; q < 6; ++q) R[(REC_SPEC + q) * nint + t] = d.prep[(PREP_SPEC + q) * n + g];
-    for (int q = 0; q < 9; ++q) R[(REC_FACE + q) * nint + t] = d.gm[(GM_CX + q) * n + g];
-    for (int q = 0; q < PREP_DIAG; ++q) R[(REC_DIAG + q) * nint + t] = d.prep[q * n + g];
-    for (int v = 0; v < c.npv; ++v) R[(REC_RES + v) * nint + t] = d.res[v * n + g];
-  }
-}
+// The sweeps work in the plane-major numbering t (setup_planes).  k_rhs writes what they
+// read of each cell -- as itself (diagonal block, residual) and as a neighbour (state,
+// split-Jacobian coefficients, + face vectors) -- as the cell's sweep record at t; each
+// hyperplane launch then reads its own records and those of the previous (next) plane
+// with coalesced loads.  dcv and dqs live at t as well; k_update reads dqs through pos[g].
+// The mixed form reads the neighbour part of the records, and the neighbours' dq, in FP32
+// (recf, dqsf): they only enter the off-diagonal products of the implicit operator.
 
 // a cell's pv / dv as the Jacobian and diagonal routines index them, from its record
-__device__ __forceinline__ void rec_state(const double* R, long long nint, long long t, double* pv, double* dv) {
-  pv[0] = 0.0; pv[4] = 0.0;
+template <class T>
+__device__ __forceinline__ void rec_state(const T* R, long long nint, long long t, T* pv, T* dv) {
+  pv[0] = T(0); pv[4] = T(0);
   pv[1] = R[(REC_PV + 0) * nint + t]; pv[2] = R[(REC_PV + 1) * nint + t]; pv[3] = R[(REC_PV + 2) * nint + t];
   pv[5] = R[(REC_PV + 3) * nint + t]; pv[6] = R[(REC_PV + 4) * nint + t];
   pv[7] = R[(REC_PV + 5) * nint + t]; pv[8] = R[(REC_PV + 6) * nint + t];
   dv[0] = R[(REC_DV + 0) * nint + t]; dv[1] = R[(REC_DV + 1) * nint + t];
-  dv[2] = dv[3] = dv[4] = dv[5] = 0.0;
+  dv[2] = dv[3] = dv[4] = dv[5] = T(0);
 #pragma unroll
   for (int q = 0; q < 8; ++q) dv[6 + q] = R[(REC_DV + 2 + q) * nint + t];
 }
 
-template <bool FWD>
-__global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, long long p1) {
-  const long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= p1) return;
+// the three lower (forward) or upper (backward) neighbours' products, added to acc
+template <bool FWD, class T>
+__device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long long t, const T* R, const T* dqs,
+                                                 T* acc) {
   const long long nint = d.nint;
-  const double* R = d.rec;
-  const int npv = c.npv;
-  double acc[NPVM];
-  if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
-  else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     // forward: lower neighbour through its + face; backward: upper neighbour through this
@@ -499,24 +500,47 @@ __global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, lon
     const int nb = FWD ? d.nbf[q * nint + t] : d.nbb[q * nint + t];
     if (nb < 0) continue;
     const long long fr = FWD ? nb : t;
-    double nx[3], pv[NPVM], dv[14], dq[NPVM];
+    T nx[3], pv[NPVM], dv[14], dq[NPVM];
     for (int e = 0; e < 3; ++e) nx[e] = R[(REC_FACE + 3 * q + e) * nint + fr];
-    rec_state(R, nint, nb, pv, dv);
-    for (int v = 0; v < npv; ++v) dq[v] = d.dqs[v * nint + nb];
-    const double spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + nb];
-    const double beta = R[REC_BETA * nint + nb];
-    const double evv = R[REC_EVV * nint + nb];
-    jac_apply_pre(npv, nx, pv, dv, spec, beta, evv, FWD ? 1.0 : -1.0, dq, acc);
+    rec_state<T>(R, nint, nb, pv, dv);
+    for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? dqs[v * nint + nb] : T(0);
+    const T spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + nb];
+    const T beta = R[REC_BETA * nint + nb];
+    const T evv = R[REC_EVV * nint + nb];
+    jac_apply_pre<T>(npv, nx, pv, dv, spec, beta, evv, FWD ? T(1) : T(-1), dq, acc);
+  }
+}
+
+template <bool FWD, bool MX>
+__global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, long long p1) {
+  const long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= p1) return;
+  const long long nint = d.nint;
+  const double* R = d.rec;
+  const int npv = c.npv;
+  double acc[NPVM];
+  for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
+  if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
+  else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
+  if (MX) {
+    float an[NPVM];
+    for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
+    sweep_neighbours<FWD, float>(d, npv, t, d.recf, d.dqsf, an);
+    for (int v = 0; v < npv; ++v) acc[v] += (double)an[v];
+  } else {
+    sweep_neighbours<FWD, double>(d, npv, t, R, d.dqs, acc);
   }
   if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
   double pv[NPVM], dv[14], o[PREP_DIAG];
-  rec_state(R, nint, t, pv, dv);
+  rec_state<double>(R, nint, t, pv, dv);
   for (int q = 0; q < PREP_DIAG; ++q) o[q] = R[(REC_DIAG + q) * nint + t];
   Diag D;
   diag_from_array(o, D);
   double x[NPVM];
+  for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
   diag_solve(c, D, pv, dv, acc, x);
   for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
+  if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
 }
 
 // ------------------------------------------------------------------ update + residual
@@ -551,7 +575,8 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
     }
     double dv[NDV], tv[3] = {0.0, 0.0, 0.0};
     for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
-    deteos<MX>(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
+    if (MX) deteos_split(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
+    else deteos<false>(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
     for (int v = 0; v < npv; ++v) {
       d.pv[v * n + g] = p[v];
       double df = fabs(old[v] - p[v]);
@@ -758,18 +783,24 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   stage(4);
   n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
-  k_gather_rec<<<E.red_grid, 256, 0, s>>>(d, c);
-  ++n;
   const int np = (int)E.plane_off.size() - 1;
   const int TS = 64;
   for (int q = 0; q < np; ++q) {
     long long a = E.plane_off[q], b = E.plane_off[q + 1];
-    if (b > a) { k_sweep<true><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b); ++n; }
+    if (b > a) {
+      if (c.mixed) k_sweep<true, true><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
+      else k_sweep<true, false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
+      ++n;
+    }
   }
   stage(5);
   for (int q = np - 1; q >= 0; --q) {
     long long a = E.plane_off[q], b = E.plane_off[q + 1];
-    if (b > a) { k_sweep<false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b); ++n; }
+    if (b > a) {
+      if (c.mixed) k_sweep<false, true><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
+      else k_sweep<false, false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
+      ++n;
+    }
   }
   stage(6);
   if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c);
@@ -971,7 +1002,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   bool ok = alloc(E.d.pv, c.npv) && alloc(E.d.dv, NDV) && alloc(E.d.tv, std::max(c.ntv, 1)) &&
             alloc(E.d.gm, GM_GRD + c.ngrd) && alloc(E.d.res, c.npv) && alloc(E.d.icav, 4) && alloc(E.d.itt, 4) &&
             alloc(E.d.ocut, 1) && alloc(E.d.dt, 1) && alloc(E.d.rcav, 2) && alloc(E.d.qq, std::max(2 * c.npv * (c.nqq ? 1 : 0), 1)) &&
-            alloc(E.d.dqs, c.npv) && alloc(E.d.dcv, c.npv) && alloc(E.d.prep, NPREP);
+            alloc(E.d.dqs, c.npv) && alloc(E.d.dcv, c.npv);
   auto allocf = [&](float*& p, long long planes) -> bool {
     if (cudaMalloc(&p, (size_t)planes * n * 4) != cudaSuccess) return false;
     cudaMemset(p, 0, (size_t)planes * n * 4);
@@ -1034,6 +1065,11 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   E.d.cells = E.d_planes; E.d.pos = E.d_pos; E.d.nbf = E.d_nbf; E.d.nbb = E.d_nbb;
   if (!E.d_planes || !E.d_pos || !E.d_nbf || !E.d_nbb) { E.err = "device allocation failed (sweep maps)"; return CFD3D_ERR_NOMEM; }
   if (cudaMalloc(&E.d.rec, (size_t)NREC * E.nint * 8) != cudaSuccess) { E.err = "device allocation failed (sweep records)"; return CFD3D_ERR_NOMEM; }
+  if (c.mixed && (cudaMalloc(&E.d.recf, (size_t)REC_DIAG * E.nint * 4) != cudaSuccess ||
+                  cudaMalloc(&E.d.dqsf, (size_t)c.npv * E.nint * 4) != cudaSuccess)) {
+    E.err = "device allocation failed (sweep records)";
+    return CFD3D_ERR_NOMEM;
+  }
   CFD_CUDA(cudaDeviceSynchronize());
   return CFD3D_OK;
 }
@@ -1043,7 +1079,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   Engine& E = h->E;
   if (E.graph) cudaGraphExecDestroy(E.graph);
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
-                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.prep, E.d.partial, h->staging};
+                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
   for (double* p : bufs) cudaFree(p);
   float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec};
   for (float* p : fbufs) cudaFree(p);
@@ -1055,6 +1091,8 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_nbf);
   cudaFree(E.d_nbb);
   cudaFree(E.d.rec);
+  cudaFree(E.d.recf);
+  cudaFree(E.d.dqsf);
   if (E.st) cudaStreamDestroy(E.st);
   delete h;
 }

@@ -60,7 +60,7 @@ struct Scalars {
 };
 
 struct DevPtr {
-  double *pv, *dv, *tv, *gm, *res, *icav, *itt, *ocut, *dt, *rcav, *qq, *dqs, *dcv, *qold, *fi, *fv, *prep;
+  double *pv, *dv, *tv, *gm, *res, *icav, *itt, *ocut, *dt, *rcav, *qq, *dqs, *dcv, *qold, *fi, *fv;
   const BlockGeom* blk;
   int nblk;
   long long ncell;
@@ -74,6 +74,9 @@ struct DevPtr {
   // dcv are plane-major too
   double* rec;
   const int *cells, *pos, *nbf, *nbb;
+  // mixed form: FP32 copy of the neighbour part of the records (the first REC_DIAG
+  // planes) and FP32 dq
+  float *recf, *dqsf;
 };
 
 // sweep record planes: what the sweeps read of a cell, as itself and as a neighbour

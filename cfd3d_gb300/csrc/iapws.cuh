@@ -149,20 +149,22 @@ __device__ __forceinline__ T h2o_pww(T t) {
   return T(1.0e6) * (q2 * q2);
 }
 
-__device__ __forceinline__ double h2o_tww(double p) {
-  double beta = pow(p / 1.0e6, 0.25);
-  double e = beta * beta - 0.17073846940092e2 * beta + 0.14915108613530e2;
-  double f = 0.11670521452767e4 * (beta * beta) + 0.12020824702470e5 * beta - 0.48232657361591e4;
-  double g = -(0.72421316703206e6 * (beta * beta)) - 0.32325550322333e7 * beta + 0.40511340542057e6;
-  double d = 2.0 * g / (-f - sqrt(f * f - 4.0 * e * g));
-  double s = 0.65017534844798e3 + d;
-  return 0.5 * (0.65017534844798e3 + d - sqrt(s * s - 4.0 * (-0.23855557567849 + 0.65017534844798e3 * d)));
+template <class T>
+__device__ __forceinline__ T h2o_tww(T p) {
+  T beta = pow(p / T(1.0e6), T(0.25));
+  T e = beta * beta - T(0.17073846940092e2) * beta + T(0.14915108613530e2);
+  T f = T(0.11670521452767e4) * (beta * beta) + T(0.12020824702470e5) * beta - T(0.48232657361591e4);
+  T g = -(T(0.72421316703206e6) * (beta * beta)) - T(0.32325550322333e7) * beta + T(0.40511340542057e6);
+  T d = T(2.0) * g / (-f - sqrt(f * f - T(4.0) * e * g));
+  T s = T(0.65017534844798e3) + d;
+  return T(0.5) * (T(0.65017534844798e3) + d - sqrt(s * s - T(4.0) * (T(-0.23855557567849) + T(0.65017534844798e3) * d)));
 }
 
-__device__ __forceinline__ double h2o_sigma(double t) {
-  double t2 = t * t, t3 = t2 * t, t4 = t2 * t2, t5 = t4 * t;
-  return 0.0881130429998226 + 0.0000616475914044782 * t - 4.4860167748009e-7 * t2 + 2.53682468718936e-10 * t3 -
-         2.62005668908913e-13 * t4 + 2.97878955533757e-16 * t5;
+template <class T>
+__device__ __forceinline__ T h2o_sigma(T t) {
+  T t2 = t * t, t3 = t2 * t, t4 = t2 * t2, t5 = t4 * t;
+  return T(0.0881130429998226) + T(0.0000616475914044782) * t - T(4.4860167748009e-7) * t2 +
+         T(2.53682468718936e-10) * t3 - T(2.62005668908913e-13) * t4 + T(2.97878955533757e-16) * t5;
 }
 
 // region 1 (liquid); FULL = false evaluates only rho and h
@@ -241,42 +243,45 @@ __device__ __forceinline__ void stiffened(T p, T t, Phase<T>& e) {
   e.dhdt = T(4186.0);
 }
 
-__device__ __forceinline__ double ideal_vis(double t) {
-  return 1.716e-5 * pow(t / 273.11, 1.5) * 383.67 / (t + 110.56);
+template <class T>
+__device__ __forceinline__ T ideal_vis(T t) {
+  return T(1.716e-5) * pow(t / T(273.11), T(1.5)) * T(383.67) / (t + T(110.56));
 }
-__device__ __forceinline__ double stiffened_vis(double t) {
-  double temp = fmax(273.0, t);
-  double r = 273.0 / temp;
-  return 1.788e-3 * exp(-1.704 - 5.306 * 273.0 / temp + 7.003 * (r * r));
+template <class T>
+__device__ __forceinline__ T stiffened_vis(T t) {
+  T temp = fmax(T(273.0), t);
+  T r = T(273.0) / temp;
+  return T(1.788e-3) * exp(T(-1.704) - T(5.306 * 273.0) / temp + T(7.003) * (r * r));
 }
 
 // IAPWS viscosity and conductivity (critical enhancement off, as in the reference)
-__device__ __forceinline__ void iapws_transport(double t, double rho, double& vis, double& cond) {
-  double tt = t * 0.00154495032985;
-  double rr = fmax(1.0e-3, fmin(1332.4, rho)) * 0.00314699949333;
-  double tt1 = 647.27 / t;
-  double a = tt1 - 1.0, b = rr - 1.0;
-  double st = sqrt(tt);
-  double mu0 = st / (kVisH[0] + kVisH[1] * tt1 + kVisH[2] * (tt1 * tt1) + kVisH[3] * (tt1 * tt1 * tt1));
-  double mu1 = 0.0;
+template <class T>
+__device__ __forceinline__ void iapws_transport(T t, T rho, T& vis, T& cond) {
+  T tt = t * T(0.00154495032985);
+  T rr = fmax(T(1.0e-3), fmin(T(1332.4), rho)) * T(0.00314699949333);
+  T tt1 = T(647.27) / t;
+  T a = tt1 - T(1.0), b = rr - T(1.0);
+  T st = sqrt(tt);
+  T mu0 = st / (T(kVisH[0]) + T(kVisH[1]) * tt1 + T(kVisH[2]) * (tt1 * tt1) + T(kVisH[3]) * (tt1 * tt1 * tt1));
+  T mu1 = T(0.0);
 #pragma unroll
   for (int i = 5; i >= 0; --i) {
-    double row = 0.0;
+    T row = T(0.0);
 #pragma unroll
-    for (int j = 6; j >= 0; --j) row = row * b + kVisHH[i][j];
+    for (int j = 6; j >= 0; --j) row = row * b + T(kVisHH[i][j]);
     mu1 = mu1 * a + row;
   }
-  vis = 55.071e-6 * mu0 * exp(rr * mu1);
-  double lam0 = st / (kConL[0] + kConL[1] * tt1 + kConL[2] * (tt1 * tt1) + kConL[3] * (tt1 * tt1 * tt1));
-  double lam1 = 0.0;
+  vis = T(55.071e-6) * mu0 * exp(rr * mu1);
+  T lam0 = st / (T(kConL[0]) + T(kConL[1]) * tt1 + T(kConL[2]) * (tt1 * tt1) + T(kConL[3]) * (tt1 * tt1 * tt1));
+  T lam1 = T(0.0);
 #pragma unroll
   for (int i = 4; i >= 0; --i) {
-    double row = 0.0;
+    T row = T(0.0);
 #pragma unroll
-    for (int j = 5; j >= 0; --j) row = row * b + kConLL[i][j];
+    for (int j = 5; j >= 0; --j) row = row * b + T(kConLL[i][j]);
     lam1 = lam1 * a + row;
   }
-  cond = 0.4945 * (lam0 * exp(rr * lam1));
+  cond = T(0.4945) * (lam0 * exp(rr * lam1));
 }
 
 }  // namespace cfd

@@ -37,7 +37,22 @@ struct Par {
   double phi[NPVM][3];
 };
 
-__device__ __forceinline__ double sq(double x) { return x * x; }
+template <class T>
+__device__ __forceinline__ T sq(const T& x) { return x * x; }
+
+// the preconditioning speed with the squared reference speed uref2 given, for the
+// adjoint's derivative with respect to the free-stream speed
+template <class R>
+__device__ __forceinline__ R sndp2_u(const Par& c, R snd2, R u2, R uref2) {
+  if (c.prec == 0) return snd2;
+  if (c.prec == 1) return fmin(snd2, fmax(u2, uref2));
+  return fmin(snd2, fmax(fmax(u2, uref2), R(c.str * c.str)));
+}
+template <class R>
+__device__ __forceinline__ R sndp2_du_u(const Par& c, R snd2, R u2, R uref2) {
+  if (c.prec == 0) return snd2;
+  return fmin(snd2, fmax(u2, uref2));
+}
 
 template <class R>
 __device__ __forceinline__ R sndp2_of(const Par& c, R snd2, R u2) {
@@ -89,16 +104,17 @@ __device__ __forceinline__ void phases(int fluid, double p, double t, Phase<doub
   }
 }
 
-__device__ __forceinline__ void mixture(const Phase<double>& l, const Phase<double>& v, const Phase<double>& g,
-                                        double y1, double y2, double* dv, unsigned long long* fallbacks) {
+template <class T>
+__device__ __forceinline__ void mixture(const Phase<T>& l, const Phase<T>& v, const Phase<T>& g, T y1, T y2, T* dv,
+                                        unsigned long long* fallbacks) {
   dv[2] = l.rho; dv[3] = v.rho; dv[4] = g.rho;
-  double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
-  double yl = 1.0 - y1 - y2;
-  double irho = yl * irhol + y1 * irhov + y2 * irhog;
+  T irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+  T yl = 1.0 - y1 - y2;
+  T irho = yl * irhol + y1 * irhov + y2 * irhog;
   dv[0] = 1.0 / irho;
   dv[1] = yl * l.h + y1 * v.h + y2 * g.h;
-  double r2 = dv[0] * dv[0];
-  double il2 = irhol * irhol, iv2 = irhov * irhov, ig2 = irhog * irhog;
+  T r2 = dv[0] * dv[0];
+  T il2 = irhol * irhol, iv2 = irhov * irhov, ig2 = irhog * irhog;
   dv[6] = r2 * (yl * il2 * l.drdp + y1 * iv2 * v.drdp + y2 * ig2 * g.drdp);
   dv[7] = r2 * (yl * il2 * l.drdt + y1 * iv2 * v.drdt + y2 * ig2 * g.drdt);
   dv[8] = r2 * (irhol - irhov);
@@ -110,12 +126,48 @@ __device__ __forceinline__ void mixture(const Phase<double>& l, const Phase<doub
   dv[5] = dv[0] * dv[11] / (dv[0] * dv[6] * dv[11] + dv[7] * (1.0 - dv[0] * dv[10]));
   if (dv[5] <= 0.0) {  // the reference's "alternative calculation for snd2"
     if (fallbacks) atomicAdd(fallbacks, 1ull);
-    double ic2l = (dv[2] * l.drdp * l.dhdt + l.drdt * (1.0 - dv[2] * l.dhdp)) / (dv[2] * l.dhdt);
-    double ic2v = (dv[3] * v.drdp * v.dhdt + v.drdt * (1.0 - dv[3] * v.dhdp)) / (dv[3] * v.dhdt);
-    double ic2g = (dv[4] * g.drdp * g.dhdt + g.drdt * (1.0 - dv[4] * g.dhdp)) / (dv[4] * g.dhdt);
+    T ic2l = (dv[2] * l.drdp * l.dhdt + l.drdt * (1.0 - dv[2] * l.dhdp)) / (dv[2] * l.dhdt);
+    T ic2v = (dv[3] * v.drdp * v.dhdt + v.drdt * (1.0 - dv[3] * v.dhdp)) / (dv[3] * v.dhdt);
+    T ic2g = (dv[4] * g.drdp * g.dhdt + g.drdt * (1.0 - dv[4] * g.dhdp)) / (dv[4] * g.dhdt);
     dv[5] = 1.0 / (r2 * (yl * ic2l * il2 + y1 * ic2v * iv2 + y2 * ic2g * ig2));
   }
   dv[14] = v.drdp; dv[15] = v.drdt; dv[16] = l.drdp; dv[17] = l.drdt;
+}
+
+// Phase properties and the mixture EOS in a generic scalar (the adjoint's dual numbers);
+// the metastable branch is chosen on the values, as in the FP64 form.
+template <class T>
+__device__ __forceinline__ void phases_t(int fluid, T p, T t, Phase<T>& l, Phase<T>& v) {
+  if (fluid == 1) {
+    stiffened<T>(p, t, l);
+    ideal_gas<T>(p, t, v);
+    return;
+  }
+  const bool meta = (double)p > h2o_pww((double)t);
+  iapws_l<T, true>(p, t, l);
+  iapws_v_meta<T, true>(p, t, meta, v);
+}
+template <class T>
+__device__ __forceinline__ void deteos_t(int fluid, int with_prop, T p, T t, T y1, T y2, T* dv, T* tv) {
+  Phase<T> l, v, g;
+  phases_t<T>(fluid, p, t, l, v);
+  ideal_gas<T>(p, t, g);
+  mixture<T>(l, v, g, y1, y2, dv, nullptr);
+  if (with_prop) {
+    T lv, lc, vv, vc;
+    if (fluid == 1) {
+      lv = stiffened_vis<T>(t); lc = 4598.0 * lv;
+      vv = ideal_vis<T>(t); vc = 1395.333333 * vv;
+    } else {
+      iapws_transport<T>(t, l.rho, lv, lc);
+      iapws_transport<T>(t, v.rho, vv, vc);
+    }
+    T gv = ideal_vis<T>(t), gc = 1395.333333 * gv;
+    T yl = 1.0 - y1 - y2;
+    T irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+    tv[0] = dv[0] * (lv * yl * irhol + vv * y1 * irhov + gv * y2 * irhog);
+    tv[1] = dv[0] * (lc * yl * irhol + vc * y1 * irhov + gc * y2 * irhog);
+  }
 }
 
 // eos%deteos_simple
@@ -164,6 +216,45 @@ __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, doubl
     double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
     tv[0] = dv[0] * (lv * yl * irhol + vv * y1 * irhov + gv * y2 * irhog);
     tv[1] = dv[0] * (lc * yl * irhol + vc * y1 * irhov + gc * y2 * irhog);
+  }
+}
+
+// eos%deteos of the mixed form's update: phase densities and enthalpies from df64 IF97 sums
+// (they enter the residual: dual-time source, face states of first-order schemes), their
+// p / T derivatives and the transport properties in FP32 (they only shape the implicit
+// operator, the preconditioning speed and the FP32 viscous fluxes); mixture in FP64.
+__device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p, double t, double y1, double y2,
+                                             double* dv, double* tv, unsigned long long* fb) {
+  Phase<double> l, v, g;
+  const float pf = (float)p, tf = (float)t;
+  if (fluid == 1) {
+    stiffened(p, t, l);
+    ideal_gas(p, t, v);
+  } else {
+    const bool meta = p > h2o_pww(t);
+    iapws_pair_df64<false>(p, t, meta, l, v);
+    Phase<float> lf, vf;
+    iapws_l<float, true>(pf, tf, lf);
+    iapws_v_meta<float, true>(pf, tf, meta, vf);
+    l.drdp = lf.drdp; l.drdt = lf.drdt; l.dhdp = lf.dhdp; l.dhdt = lf.dhdt;
+    v.drdp = vf.drdp; v.drdt = vf.drdt; v.dhdp = vf.dhdp; v.dhdt = vf.dhdt;
+  }
+  ideal_gas(p, t, g);
+  mixture(l, v, g, y1, y2, dv, fb);
+  if (with_prop) {
+    float lv, lc, vv, vc;
+    if (fluid == 1) {
+      lv = stiffened_vis<float>(tf); lc = 4598.0f * lv;
+      vv = ideal_vis<float>(tf); vc = 1395.333333f * vv;
+    } else {
+      iapws_transport<float>(tf, (float)l.rho, lv, lc);
+      iapws_transport<float>(tf, (float)v.rho, vv, vc);
+    }
+    float gv = ideal_vis<float>(tf), gc = 1395.333333f * gv;
+    double yl = 1.0 - y1 - y2;
+    double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+    tv[0] = dv[0] * ((double)lv * yl * irhol + (double)vv * y1 * irhov + (double)gv * y2 * irhog);
+    tv[1] = dv[0] * ((double)lc * yl * irhol + (double)vc * y1 * irhov + (double)gc * y2 * irhog);
   }
 }
 
@@ -662,12 +753,8 @@ __device__ __forceinline__ void diag_solve(const Par& c, const Diag& D, const do
   for (int n = 0; n < c.npv; ++n) x[n] *= D.a;
 }
 
-// per-cell LU-SGS coefficients computed once per iteration (k_rhs) and read by the sweeps
-constexpr int PREP_DIAG = 23;                 // Diag fields
-constexpr int PREP_SPEC = PREP_DIAG;          // 6 spectral radii 1.05(|u'|+d): i-,i+,j-,j+,k-,k+
-constexpr int PREP_BETA = PREP_SPEC + 6;      // 1/sndp2 - 1/c^2 + drho/dp
-constexpr int PREP_EVV = PREP_BETA + 1;       // 2 * eigenvis / vol
-constexpr int NPREP = PREP_EVV + 1;
+// the Diag fields as an array (the sweep record's diagonal part)
+constexpr int PREP_DIAG = 23;
 
 __device__ __forceinline__ void diag_to_array(const Diag& D, double* o) {
   o[0] = D.a; o[1] = D.b1; o[2] = D.i_b1; o[3] = D.ss; o[4] = D.rr; o[5] = D.cross; o[6] = D.cross1;
@@ -683,32 +770,34 @@ __device__ __forceinline__ void diag_from_array(const double* o, Diag& D) {
 }
 
 // spectral radius of the split Jacobian for one face: 1.05 (|u'| + d)
-__device__ __forceinline__ double face_spectral(const Par& c, const double* nx, const double* pv, const double* dv) {
-  double ds = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
-  double u = nx[0] * pv[1] + nx[1] * pv[2] + nx[2] * pv[3];
-  double sndp2 = sndp2_of<double>(c, dv[5], pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
-  double up = 0.5 * (1.0 + sndp2 / dv[5]) * u;
-  double d = 0.5 * sqrt(u * u * sq(1.0 - sndp2 / dv[5]) + 4.0 * sndp2 * ds);
-  return 1.05 * (fabs(up) + d);
+template <class R>
+__device__ __forceinline__ R face_spectral(const Par& c, const R* nx, const R* pv, const R* dv) {
+  R ds = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
+  R u = nx[0] * pv[1] + nx[1] * pv[2] + nx[2] * pv[3];
+  R sndp2 = sndp2_of<R>(c, dv[5], pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
+  R up = R(0.5) * (R(1.0) + sndp2 / dv[5]) * u;
+  R d = R(0.5) * sqrt(u * u * sq(R(1.0) - sndp2 / dv[5]) + R(4.0) * sndp2 * ds);
+  return R(1.05) * (fabs(up) + d);
 }
 
 // acc += sign_acc * 0.5 * A dq with the precomputed spectral radius `spec`, beta and
-// evv = 2 eigenvis / vol of the neighbour (same algebra as jac_apply)
-__device__ __forceinline__ void jac_apply_pre(int npv, const double* nx, const double* pv, const double* dv,
-                                              double spec, double beta, double evv, double sign,
-                                              const double* dq, double* acc) {
-  double ds = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
-  double u = nx[0] * pv[1] + nx[1] * pv[2] + nx[2] * pv[3];
-  double lamda = sign * spec;
-  double vis = sign * evv * ds;
-  double uuu = u + lamda + vis;
-  double lv = lamda + vis;
-  double r0 = (u * dv[6] + lamda * beta + vis * dv[6]) * dq[0] + nx[0] * dv[0] * dq[1] + nx[1] * dv[0] * dq[2] +
-              nx[2] * dv[0] * dq[3] + (u * dv[7] + lv * dv[7]) * dq[4] + (u * dv[8] + lv * dv[8]) * dq[5] +
-              (u * dv[9] + lv * dv[9]) * dq[6];
-  double ru = dv[0] * uuu;
-  double h = dv[1] + 0.5 * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
-  double s = 0.5 * sign;  // forward: +A+ ; backward: -A- (sign = -1 for both factors)
+// evv = 2 eigenvis / vol of the neighbour (same algebra as jac_apply); R = float is the
+// mixed form's neighbour product
+template <class R>
+__device__ __forceinline__ void jac_apply_pre(int npv, const R* nx, const R* pv, const R* dv, R spec, R beta, R evv,
+                                              R sign, const R* dq, R* acc) {
+  R ds = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
+  R u = nx[0] * pv[1] + nx[1] * pv[2] + nx[2] * pv[3];
+  R lamda = sign * spec;
+  R vis = sign * evv * ds;
+  R uuu = u + lamda + vis;
+  R lv = lamda + vis;
+  R r0 = (u * dv[6] + lamda * beta + vis * dv[6]) * dq[0] + nx[0] * dv[0] * dq[1] + nx[1] * dv[0] * dq[2] +
+         nx[2] * dv[0] * dq[3] + (u * dv[7] + lv * dv[7]) * dq[4] + (u * dv[8] + lv * dv[8]) * dq[5] +
+         (u * dv[9] + lv * dv[9]) * dq[6];
+  R ru = dv[0] * uuu;
+  R h = dv[1] + R(0.5) * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
+  R s = R(0.5) * sign;  // forward: +A+ ; backward: -A- (sign = -1 for both factors)
   acc[0] += s * r0;
   acc[1] += s * (pv[1] * r0 + nx[0] * dq[0] + ru * dq[1]);
   acc[2] += s * (pv[2] * r0 + nx[1] * dq[0] + ru * dq[2]);
