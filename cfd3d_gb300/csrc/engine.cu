@@ -204,32 +204,12 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       for (int v = 0; v < c.npv; ++v) pb[v] = d.pv[v * n + op.bnd];
       double rb = d.dv[op.bnd], c2b = d.dv[5 * n + op.bnd];
       double dl = 1.0 / sqrt(nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
-      double vel = (pb[1] * nx[0] + pb[2] * nx[1] + pb[3] * nx[2]) * dl;
-      double mach = vel / sqrt(c2b);
-      double a = sqrt(sndp2_of<double>(c, c2b, vel * vel));
       // free-stream state bcinfo%pv with bcinfo%pressure = pref
       double bp[NPVM];
       bp[0] = c.pref; bp[1] = c.uref_vec[0]; bp[2] = c.uref_vec[1]; bp[3] = c.uref_vec[2];
       bp[4] = c.tref; bp[5] = c.y1ref; bp[6] = c.y2ref; bp[7] = c.kref; bp[8] = c.oref;
       double* pv = x.pv;
-      if (mach >= 0.0) {
-        if (mach < 1.0) {
-          pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
-          for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (pb[1 + q3] + nx[q3] * (pb[0] + bp[0] - c.pref) / rb / a * dl) - pv[1 + q3];
-        }
-      } else if (mach <= -1.0) {
-        pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
-        for (int v = 1; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
-        pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
-        pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
-      } else {
-        double var = c.pref - bp[0] + pb[0] - rb * a * (nx[0] * (bp[1] - pb[1]) + nx[1] * (bp[2] - pb[2]) + nx[2] * (bp[3] - pb[3])) * dl;
-        pv[0] = var - pv[0];
-        for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (bp[1 + q3] + nx[q3] * 0.5 * var / rb / a * dl) - pv[1 + q3];
-        for (int v = 4; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
-        pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
-        pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
-      }
+      farfield_pv<double>(c, nx, dl, pb, rb, c2b, bp, c.uref * c.uref, pv);
       deteos(c.fluid, c.with_prop, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
       store_cell(d, c, op.dst, x);
       return;
@@ -368,32 +348,16 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
     }
     double tv[3];
     for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
-    const double c23 = 2.0 / 3.0, c59 = 5.0 / 9.0;
-    double kk = pv2[7], oo = pv2[8];
-    double dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
-    double dvdx = gr[1][0], dvdy = gr[1][1], dvdz = gr[1][2];
-    double dwdx = gr[2][0], dwdy = gr[2][1], dwdz = gr[2][2];
-    double strain = 2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + sq(dudy + dvdx) + sq(dudz + dwdx) + sq(dvdz + dwdy);
-    double div = dudx + dvdy + dwdz;
-    double prod = tv[2] * (strain - c23 * div * div) - c23 * dv[0] * kk * div;
-    prod = fmin(prod, 0.9 * dv[0] * kk * oo);
-    d.ocut[g] = sqrt(strain - c23 * div * div);
-    double pkw = gr[3][0] * gr[4][0] + gr[3][1] * gr[4][1] + gr[3][2] * gr[4][2];
-    double y5 = d.gm[(GM_GRD + 4) * n + g];
-    double cdkw = fmax(1.712 * dv[0] / oo * pkw, 1.0e-10);
-    double term1 = sqrt(kk) / (0.09 * oo * y5);
-    double term2 = 500.0 * tv[0] / dv[0] / (oo * y5 * y5);
-    double term3 = (3.424 * dv[0] * kk) / (cdkw * y5 * y5);
-    double arg1 = fmin(fmax(term1, term2), term3);
-    double a2 = arg1 * arg1;
-    double bigf = tanh(a2 * a2);
-    double talpha = bigf * c59 + (1.0 - bigf) * 0.44;
-    double tbeta = bigf * 0.075 + (1.0 - bigf) * 0.0828;
-    double ki = 1.0 / kk, oi = 1.0 / oo, ei = 1.0 / tv[2];
-    double tl = sqrt(kk) / 9.0 / oo * 100.0;
-    double dest = dv[0] * pow(kk, 1.5) / tl;
-    res[7] = res[7] + (prod - dest) * vol;
-    res[8] = res[8] + (talpha * dv[0] * ei * prod - tbeta * dv[0] * oo * oo + 1.712 * (1.0 - bigf) * dv[0] * oi * pkw) * vol;
+    const double c23 = 2.0 / 3.0;
+    const double kk = pv2[7], oo = pv2[8];
+    const double y5 = d.gm[(GM_GRD + 4) * n + g];
+    const SstOut<double> so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol);
+    res[7] = res[7] + so.r7;
+    res[8] = res[8] + so.r8;
+    d.ocut[g] = sqrt(so.strain - c23 * so.div * so.div);
+    const double prod = so.prod, dest = so.dest, div = so.div, pkw = so.pkw, bigf = so.bigf;
+    const double talpha = so.talpha, tbeta = so.tbeta;
+    const double ki = 1.0 / kk, oi = 1.0 / oo, ei = 1.0 / tv[2];
     double dpdk = prod * ki;
     double dpdo = -((prod + c23 * dv[0] * kk * div) * oi);
     double it0 = dpdk - dest * ki, it1 = dpdo - dest * oi, it2 = 0.0;

@@ -105,47 +105,15 @@ __global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
     double x[18];
 #pragma unroll
     for (int l = 0; l < 18; ++l) x[l] = P[stencil_cell(l, g, sn, s1, s2)];
-    double dn = x[9] - x[8];
-    double de = 0.0625 * (-x[0] - x[1] + x[4] + x[5] + 2.0 * (-x[6] - x[7] + x[10] + x[11]) - x[12] - x[13] + x[16] + x[17]);
-    double dt = 0.0625 * (-x[0] - x[1] + x[12] + x[13] + 2.0 * (-x[2] - x[3] + x[14] + x[15]) - x[4] - x[5] + x[16] + x[17]);
-    gx[q] = (dn * nx[0] + de * ev[0] + dt * tvv[0]) * vol;
-    gy[q] = (dn * nx[1] + de * ev[1] + dt * tvv[1]) * vol;
-    gz[q] = (dn * nx[2] + de * ev[2] + dt * tvv[2]) * vol;
-    cc[q] = 0.5 * (x[8] + x[9]);
+    face_gradient<double>(x, nx, ev, tvv, vol, gx[q], gy[q], gz[q], cc[q]);
   }
-  const double c23 = 2.0 / 3.0;
-  double mu = turb ? (vis + emut) : vis;
-  double div = gx[0] + gy[1] + gz[2];
-  double txx = mu * (2.0 * gx[0] - c23 * div), tyy = mu * (2.0 * gy[1] - c23 * div), tzz = mu * (2.0 * gz[2] - c23 * div);
-  double txy = mu * (gy[0] + gx[1]), txz = mu * (gz[0] + gx[2]), tyz = mu * (gz[1] + gy[2]);
-  double kc = turb ? (con + tcon) : con;
-  double uc = cc[0], vc = cc[1], wc = cc[2];
-  double fv[NPVM];
-  fv[0] = 0.0;
-  fv[1] = txx * nx[0] + txy * nx[1] + txz * nx[2];
-  fv[2] = txy * nx[0] + tyy * nx[1] + tyz * nx[2];
-  fv[3] = txz * nx[0] + tyz * nx[1] + tzz * nx[2];
-  fv[4] = nx[0] * (uc * txx + vc * txy + wc * txz + kc * gx[3]) + nx[1] * (uc * txy + vc * tyy + wc * tyz + kc * gy[3]) +
-          nx[2] * (uc * txz + vc * tyz + wc * tzz + kc * gz[3]);
-  fv[5] = 0.0;
-  fv[6] = 0.0;
+  double rho = 0.0, ydns = 0.0;
   if (turb) {
-    double pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
-    double rho = 0.5 * (d.dv[g] + d.dv[gr]);
-    double ydns = 0.5 * (d.gm[(GM_GRD + 4) * n + g] + d.gm[(GM_GRD + 4) * n + gr]);
-    double kf = cc[4], of = cc[5];
-    double cdkw = fmax(1.712 * rho / of * pkw, 1.0e-10);
-    double term1 = sqrt(kf) / (0.09 * of * ydns);
-    double term2 = 500.0 * vis / rho / (of * ydns * ydns);
-    double term3 = (3.424 * rho * kf) / (cdkw * ydns * ydns);
-    double arg1 = fmin(fmax(term1, term2), term3);
-    double a2 = arg1 * arg1;
-    double bigf = tanh(a2 * a2);
-    double tdk = bigf * 0.85 + (1.0 - bigf) * 1.0;
-    double tdo = bigf * 0.5 + (1.0 - bigf) * 0.856;
-    fv[7] = (vis + emut * tdk) * (gx[4] * nx[0] + gy[4] * nx[1] + gz[4] * nx[2]);
-    fv[8] = (vis + emut * tdo) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
+    rho = 0.5 * (d.dv[g] + d.dv[gr]);
+    ydns = 0.5 * (d.gm[(GM_GRD + 4) * n + g] + d.gm[(GM_GRD + 4) * n + gr]);
   }
+  double fv[NPVM];
+  vsflux_core<double>(c, nx, gx, gy, gz, cc, vis, con, emut, tcon, rho, ydns, fv);
   double* fvp = d.fv + (long long)DIR * npv * n;
   for (int v = 0; v < npv; ++v) fvp[v * n + g] = fv[v];
 }

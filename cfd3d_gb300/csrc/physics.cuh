@@ -66,6 +66,37 @@ __device__ __forceinline__ R sndp2_du_of(const Par& c, R snd2, R u2) {
   return fmin(snd2, fmax(u2, R(c.uref * c.uref)));
 }
 
+// ------------------------------------------------------------------ far-field ghost state
+// bcfarfield (src/bc_module.f90:2904-3013): the ghost pv from the boundary cell's pressure
+// and velocity pb[0..3], density rb and sound speed c2b and the free-stream state bp, by the
+// sign and size of the normal Mach number; pv holds the mirror cell's values on entry.  nx
+// is the outward face vector, dl its inverse length.  Templated for the adjoint.
+template <class T>
+__device__ __forceinline__ void farfield_pv(const Par& c, const double* nx, double dl, const T* pb, T rb, T c2b,
+                                            const T* bp, T uref2, T* pv) {
+  T vel = (pb[1] * nx[0] + pb[2] * nx[1] + pb[3] * nx[2]) * dl;
+  T mach = vel / sqrt(c2b);
+  T a = sqrt(sndp2_u<T>(c, c2b, vel * vel, uref2));
+  if (mach >= 0.0) {
+    if (mach < 1.0) {
+      pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
+      for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (pb[1 + q3] + nx[q3] * (pb[0] + bp[0] - c.pref) / rb / a * dl) - pv[1 + q3];
+    }
+  } else if (mach <= -1.0) {
+    pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
+    for (int v = 1; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
+    pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
+    pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
+  } else {
+    T var = c.pref - bp[0] + pb[0] - rb * a * (nx[0] * (bp[1] - pb[1]) + nx[1] * (bp[2] - pb[2]) + nx[2] * (bp[3] - pb[3])) * dl;
+    pv[0] = var - pv[0];
+    for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (bp[1 + q3] + nx[q3] * 0.5 * var / rb / a * dl) - pv[1 + q3];
+    for (int v = 4; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
+    pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
+    pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
+  }
+}
+
 // ------------------------------------------------------------------ mixture EOS
 struct EosCount { unsigned long long* fallbacks; };
 
@@ -362,10 +393,14 @@ __device__ __forceinline__ void muscl_clip(const Par& c, const R* c9, const R* c
 
 // ------------------------------------------------------------------ inviscid fluxes
 // L/R face states: pv (npv), rho, h(static), snd2 in dv slots [0], [1], [5]
-struct FaceState { double pv[NPVM]; double rho, h, c2; };
+// L/R face states: pv (npv), rho, h(static), snd2 in dv slots [0], [1], [5]
+template <class T>
+struct FaceStateT { T pv[NPVM]; T rho, h, c2; };
+using FaceState = FaceStateT<double>;
 
-__device__ __forceinline__ double sdst_ratio_min(const double* s) {
-  double v = fmin(s[8] / s[9], s[9] / s[8]);
+template <class T>
+__device__ __forceinline__ T sdst_ratio_min(const T* s) {
+  T v = fmin(s[8] / s[9], s[9] / s[8]);
   v = fmin(v, fmin(s[10] / s[8], s[8] / s[10]));
   v = fmin(v, fmin(s[8] / s[6], s[6] / s[8]));
   v = fmin(v, fmin(s[8] / s[2], s[2] / s[8]));
@@ -377,87 +412,96 @@ __device__ __forceinline__ double sdst_ratio_min(const double* s) {
   return v;
 }
 
-// returns the face flux fx (npv) for the unnormalised area vector n
-template <bool MX = false>
-__device__ inline void inviscid_flux(const Par& c, const double* n, const FaceState& L, const FaceState& Rs,
-                              const double* sdst_in, double* fx, unsigned long long* fb) {
-  const int npv = c.npv;
-  double dl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-  if (dl == 0.0) {
-    for (int k = 0; k < npv; ++k) fx[k] = 0.0;
-    return;
-  }
-  double nx = n[0] / dl, ny = n[1] / dl, nz = n[2] / dl;
-  const double* pl = L.pv;
-  const double* pr = Rs.pv;
-  double uull = nx * pl[1] + ny * pl[2] + nz * pl[3];
-  double uurr = nx * pr[1] + ny * pr[2] + nz * pr[3];
-  double srl = sqrt(L.rho), srr = sqrt(Rs.rho);
-  double ravg_d = 1.0 / (srl + srr);
-  double ravg[NPVM];
+// Roe-average state of a face: sqrt(rho)-weighted velocities and scalars, arithmetic
+// means of p and T (src/flux_module.f90:222-236)
+template <class T>
+__device__ __forceinline__ void roe_state(int npv, const FaceStateT<T>& L, const FaceStateT<T>& Rs, T* ravg) {
+  const T* pl = L.pv;
+  const T* pr = Rs.pv;
+  T srl = sqrt(L.rho), srr = sqrt(Rs.rho);
+  T ravg_d = 1.0 / (srl + srr);
   ravg[0] = 0.5 * (pl[0] + pr[0]);
   ravg[4] = 0.5 * (pl[4] + pr[4]);
   for (int k = 1; k <= 3; ++k) ravg[k] = (srl * pl[k] + srr * pr[k]) * ravg_d;
   for (int k = 5; k < npv; ++k) ravg[k] = (srl * pl[k] + srr * pr[k]) * ravg_d;
-  double hl = L.h + 0.5 * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]);
-  double hr = Rs.h + 0.5 * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]);
-  // Roe-average EOS: only the sound speed is used (src/flux_module.f90:237,319,461,588)
-  double rdv[NDV];
-  deteos_simple<MX>(c.fluid, ravg[0] + c.pref, ravg[4], ravg[5], ravg[6], rdv, fb);
-  double rc2 = rdv[5];
-  double rrho = sqrt(L.rho * Rs.rho);
+}
+
+// The four inviscid fluxes (src/flux_module.f90:198-641) given the Roe-average state
+// ravg, its sound speed rc2 and the squared reference speed uref2; templated on the
+// scalar so that the adjoint evaluates the same code on dual numbers.  n is the
+// unnormalised face vector; fx (npv) is the face flux.
+template <class T>
+__device__ inline void inviscid_flux_core(const Par& c, const double* n, const FaceStateT<T>& L,
+                                          const FaceStateT<T>& Rs, const T* sdst_in, const T* ravg, T rc2,
+                                          T uref2, T* fx) {
+  const int npv = c.npv;
+  double dl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  if (dl == 0.0) {
+    for (int k = 0; k < npv; ++k) fx[k] = T(0.0);
+    return;
+  }
+  double nx = n[0] / dl, ny = n[1] / dl, nz = n[2] / dl;
+  const T* pl = L.pv;
+  const T* pr = Rs.pv;
+  T rrho = sqrt(L.rho * Rs.rho);
   const double pref = c.pref;
+  const T srl = sqrt(L.rho), srr = sqrt(Rs.rho);
+  const T ravg_d = 1.0 / (srl + srr);
+  const T hl = L.h + 0.5 * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]);
+  const T hr = Rs.h + 0.5 * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]);
+  const T uull = nx * pl[1] + ny * pl[2] + nz * pl[3];
+  const T uurr = nx * pr[1] + ny * pr[2] + nz * pr[3];
   if (c.nscheme == 1 || c.nscheme == 2) {
-    double ravg_ht = (srl * hl + srr * hr) * ravg_d;
-    double u2 = ravg[1] * ravg[1] + ravg[2] * ravg[2] + ravg[3] * ravg[3];
-    double uuu = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
+    T ravg_ht = (srl * hl + srr * hr) * ravg_d;
+    T u2 = ravg[1] * ravg[1] + ravg[2] * ravg[2] + ravg[3] * ravg[3];
+    T uuu = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
     if (c.nscheme == 1) {
-      double sndp2 = sndp2_of<double>(c, rc2, u2);
-      double q = sndp2 / rc2;
-      double uup = 0.5 * (1.0 + q) * uuu;
-      double ddd = 0.5 * sqrt((1.0 - q) * (1.0 - q) * uuu * uuu + 4.0 * sndp2);
-      double c_star = 0.5 * (fabs(uup + ddd) + fabs(uup - ddd));
-      double m_star = 0.5 * (fabs(uup + ddd) - fabs(uup - ddd)) / ddd;
-      double du = m_star * (uurr - uull) + (c_star - q * fabs(uuu) - 0.5 * (1.0 - q) * uuu * m_star) * (pr[0] - pl[0]) / rrho / sndp2;
-      double dp = m_star * (pr[0] - pl[0]) + (c_star - fabs(uuu) + 0.5 * (1.0 - q) * uuu * m_star) * rrho * (uurr - uull);
-      double au = fabs(uuu);
-      double df0 = au * (Rs.rho - L.rho) + du * rrho;
+      T sndp2 = sndp2_u<T>(c, rc2, u2, uref2);
+      T q = sndp2 / rc2;
+      T uup = 0.5 * (1.0 + q) * uuu;
+      T ddd = 0.5 * sqrt((1.0 - q) * (1.0 - q) * uuu * uuu + 4.0 * sndp2);
+      T c_star = 0.5 * (fabs(uup + ddd) + fabs(uup - ddd));
+      T m_star = 0.5 * (fabs(uup + ddd) - fabs(uup - ddd)) / ddd;
+      T du = m_star * (uurr - uull) + (c_star - q * fabs(uuu) - 0.5 * (1.0 - q) * uuu * m_star) * (pr[0] - pl[0]) / rrho / sndp2;
+      T dp = m_star * (pr[0] - pl[0]) + (c_star - fabs(uuu) + 0.5 * (1.0 - q) * uuu * m_star) * rrho * (uurr - uull);
+      T au = fabs(uuu);
+      T df0 = au * (Rs.rho - L.rho) + du * rrho;
       fx[0] = 0.5 * (L.rho * uull + Rs.rho * uurr - df0) * dl;
       const double nn[3] = {nx, ny, nz};
       for (int q3 = 0; q3 < 3; ++q3) {
-        double df = au * (Rs.rho * pr[1 + q3] - L.rho * pl[1 + q3]) + du * rrho * ravg[1 + q3] + dp * nn[q3];
+        T df = au * (Rs.rho * pr[1 + q3] - L.rho * pl[1 + q3]) + du * rrho * ravg[1 + q3] + dp * nn[q3];
         fx[1 + q3] = 0.5 * (L.rho * uull * pl[1 + q3] + nn[q3] * (pl[0] + pref) + Rs.rho * uurr * pr[1 + q3] +
                             nn[q3] * (pr[0] + pref) - df) * dl;
       }
-      double df4 = au * (Rs.rho * hr - pr[0] - L.rho * hl + pl[0]) + du * rrho * ravg_ht + dp * uuu;
+      T df4 = au * (Rs.rho * hr - pr[0] - L.rho * hl + pl[0]) + du * rrho * ravg_ht + dp * uuu;
       fx[4] = 0.5 * (L.rho * uull * hl + Rs.rho * uurr * hr - df4) * dl;
       for (int k = 5; k < npv; ++k) {
-        double df = au * (Rs.rho * pr[k] - L.rho * pl[k]) + du * rrho * ravg[k];
+        T df = au * (Rs.rho * pr[k] - L.rho * pl[k]) + du * rrho * ravg[k];
         fx[k] = 0.5 * (L.rho * uull * pl[k] + Rs.rho * uurr * pr[k] - df) * dl;
       }
       return;
     }
     // Roe-M
-    double am2rmid_du = sndp2_du_of<double>(c, rc2, u2) / rc2;
-    double am2rmid = sndp2_of<double>(c, rc2, u2) / rc2;
-    double fmid = sqrt(am2rmid) * (2.0 - sqrt(am2rmid));
-    double fmid_du = sqrt(am2rmid_du) * (2.0 - sqrt(am2rmid_du));
-    double amid = sqrt(rc2);
-    double b1 = fmax(fmax(0.0, uuu + amid), uurr + amid);
-    double b2 = fmin(fmin(0.0, uuu - amid), uull - amid);
-    double b1_du = fmax(fmax(0.0, uuu + fmid_du * amid), uurr + fmid_du * amid);
-    double b2_du = fmin(fmin(0.0, uuu - fmid_du * amid), uull - fmid_du * amid);
-    double m_tilde = copysign(1.0, uuu) * fmin(fabs(uuu) / amid, 1.0);
-    double m_tilde_du = copysign(1.0, uuu) * fmin(fabs(uuu) / (fmid_du * amid), 1.0);
-    double sd[18];
-    double add0 = 0.1 * fmin(L.rho * L.c2, Rs.rho * Rs.c2);
+    T am2rmid_du = sndp2_du_u<T>(c, rc2, u2, uref2) / rc2;
+    T am2rmid = sndp2_u<T>(c, rc2, u2, uref2) / rc2;
+    T fmid = sqrt(am2rmid) * (2.0 - sqrt(am2rmid));
+    T fmid_du = sqrt(am2rmid_du) * (2.0 - sqrt(am2rmid_du));
+    T amid = sqrt(rc2);
+    T b1 = fmax(fmax(0.0, uuu + amid), uurr + amid);
+    T b2 = fmin(fmin(0.0, uuu - amid), uull - amid);
+    T b1_du = fmax(fmax(0.0, uuu + fmid_du * amid), uurr + fmid_du * amid);
+    T b2_du = fmin(fmin(0.0, uuu - fmid_du * amid), uull - fmid_du * amid);
+    T m_tilde = copysign(1.0, uuu) * fmin(fabs(uuu) / amid, 1.0);
+    T m_tilde_du = copysign(1.0, uuu) * fmin(fabs(uuu) / (fmid_du * amid), 1.0);
+    T sd[18];
+    T add0 = 0.1 * fmin(L.rho * L.c2, Rs.rho * Rs.c2);
     for (int k = 0; k < 18; ++k) sd[k] = sdst_in[k] + pref + add0;
-    double ff = 1.0 - sdst_ratio_min(sd);
-    ff = (uuu != 0.0) ? pow(fabs(uuu) / amid, ff) : 1.0;
-    double gg = 1.0 - fmin(sd[8] / sd[9], sd[9] / sd[8]);
-    gg = (uuu != 0.0) ? pow(fabs(uuu) / amid, gg) : 1.0;
-    double add = 1.0 + fabs(m_tilde), aaa = 1.0 + fabs(m_tilde_du);
-    double dq[NPVM], fl[NPVM], fr[NPVM], bdq[NPVM];
+    T ff = 1.0 - sdst_ratio_min<T>(sd);
+    ff = (uuu != 0.0) ? pow(fabs(uuu) / amid, ff) : T(1.0);
+    T gg = 1.0 - fmin(sd[8] / sd[9], sd[9] / sd[8]);
+    gg = (uuu != 0.0) ? pow(fabs(uuu) / amid, gg) : T(1.0);
+    T add = 1.0 + fabs(m_tilde), aaa = 1.0 + fabs(m_tilde_du);
+    T dq[NPVM], fl[NPVM], fr[NPVM], bdq[NPVM];
     dq[0] = Rs.rho - L.rho;
     for (int k = 1; k <= 3; ++k) dq[k] = Rs.rho * pr[k] - L.rho * pl[k];
     dq[4] = Rs.rho * hr - L.rho * hl;
@@ -480,26 +524,26 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
     return;
   }
   // AUSM family
-  double amid = sqrt(rc2);
-  double zmr = uurr / amid, zml = uull / amid;
-  double fmid, fmid1, am2mid;
+  T amid = sqrt(rc2);
+  T zmr = uurr / amid, zml = uull / amid;
+  T fmid, fmid1, am2mid;
   if (c.nscheme == 3) {
     am2mid = ravg[1] * ravg[1] + ravg[2] * ravg[2] + ravg[3] * ravg[3];
-    double a1 = sndp2_du_of<double>(c, rc2, am2mid) / rc2;
-    double a0 = sndp2_of<double>(c, rc2, am2mid) / rc2;
+    T a1 = sndp2_du_u<T>(c, rc2, am2mid, uref2) / rc2;
+    T a0 = sndp2_u<T>(c, rc2, am2mid, uref2) / rc2;
     fmid = sqrt(a0) * (2.0 - sqrt(a0));
     fmid1 = sqrt(a1) * (2.0 - sqrt(a1));
   } else {
-    double un = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
+    T un = nx * ravg[1] + ny * ravg[2] + nz * ravg[3];
     am2mid = un * un;
-    double a0 = sndp2_of<double>(c, rc2, am2mid) / rc2;
+    T a0 = sndp2_u<T>(c, rc2, am2mid, uref2) / rc2;
     fmid = sqrt(a0) * (2.0 - sqrt(a0));
     fmid1 = fmid;
   }
-  double alpha = 3.0 / 16.0 * (-4.0 + 5.0 * fmid1 * fmid1);
+  T alpha = 3.0 / 16.0 * (-4.0 + 5.0 * fmid1 * fmid1);
   alpha = fmax(fmin(alpha, 3.0 / 16.0), -3.0 / 4.0);
   const double beta = 0.125;
-  double zmmr, pmr, zmpl, ppl;
+  T zmmr, pmr, zmpl, ppl;
   if (fabs(zmr) >= 1.0) { zmmr = 0.5 * (zmr - fabs(zmr)); pmr = 0.5 * (1.0 - zmr / fabs(zmr)); }
   else {
     zmmr = -(0.25 * (zmr - 1.0) * (zmr - 1.0)) - beta * sq(zmr * zmr - 1.0);
@@ -510,21 +554,21 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
     zmpl = 0.25 * (zml + 1.0) * (zml + 1.0) + beta * sq(zml * zml - 1.0);
     ppl = 0.25 * (zml + 1.0) * (zml + 1.0) * (2.0 - zml) + alpha * zml * sq(zml * zml - 1.0);
   }
-  double zmpl1, zmmr1, pmid;
+  T zmpl1, zmmr1, pmid;
   if (c.nscheme == 3) {
-    double zmid = zmpl + zmmr;
+    T zmid = zmpl + zmmr;
     pmid = ppl * (pl[0] + pref) + pmr * (pr[0] + pref) - 2.0 * ppl * pmr * rrho * fmid1 * amid * (uurr - uull);
-    double sd[18];
-    double add0 = 0.1 * fmin(L.rho * L.c2, Rs.rho * Rs.c2);
+    T sd[18];
+    T add0 = 0.1 * fmin(L.rho * L.c2, Rs.rho * Rs.c2);
     for (int k = 0; k < 18; ++k) sd[k] = sdst_in[k] + pref + add0;
-    double m1 = fmin(sd[8] / sd[9], sd[9] / sd[8]);
-    double ww1 = 1.0 - m1 * m1 * m1;
-    double m2 = sdst_ratio_min(sd);
-    double ww2 = 1.0 - m2 * m2;
-    double ww = fmax(ww1, ww2);
-    double pmt = rrho * rc2;
-    double pwl = ((pl[0] + pref + rrho * rc2) / pmt - 1.0) * (1.0 - ww) / fmid;
-    double pwr = ((pr[0] + pref + rrho * rc2) / pmt - 1.0) * (1.0 - ww) / fmid;
+    T m1 = fmin(sd[8] / sd[9], sd[9] / sd[8]);
+    T ww1 = 1.0 - m1 * m1 * m1;
+    T m2 = sdst_ratio_min<T>(sd);
+    T ww2 = 1.0 - m2 * m2;
+    T ww = fmax(ww1, ww2);
+    T pmt = rrho * rc2;
+    T pwl = ((pl[0] + pref + rrho * rc2) / pmt - 1.0) * (1.0 - ww) / fmid;
+    T pwr = ((pr[0] + pref + rrho * rc2) / pmt - 1.0) * (1.0 - ww) / fmid;
     if (zmid >= 0.0) {
       pwl = pwl * rrho / L.rho;
       pwr = pwr * rrho / L.rho;  // both weights scaled by the left density, as the reference does
@@ -538,11 +582,11 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
     }
   } else {
     const double kp = 0.25;
-    double zmid = zmpl + zmmr - kp * fmax(1.0 - am2mid / rc2, 0.0) * (pr[0] - pl[0]) / rrho / rc2 / fmid;
+    T zmid = zmpl + zmmr - kp * fmax(1.0 - am2mid / rc2, 0.0) * (pr[0] - pl[0]) / rrho / rc2 / fmid;
     pmid = ppl * (pl[0] + pref) + pmr * (pr[0] + pref) - 2.0 * ppl * pmr * rrho * fmid * amid * (uurr - uull);
     if (zmid > 0.0) { zmpl1 = zmid; zmmr1 = 0.0; } else { zmmr1 = zmid; zmpl1 = 0.0; }
   }
-  double ml = zmpl1 * amid * L.rho, mr = zmmr1 * amid * Rs.rho;
+  T ml = zmpl1 * amid * L.rho, mr = zmmr1 * amid * Rs.rho;
   fx[0] = (ml + mr) * dl;
   fx[1] = (ml * pl[1] + mr * pr[1] + pmid * nx) * dl;
   fx[2] = (ml * pl[2] + mr * pr[2] + pmid * ny) * dl;
@@ -551,26 +595,148 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
   for (int k = 5; k < npv; ++k) fx[k] = (ml * pl[k] + mr * pr[k]) * dl;
 }
 
-// ------------------------------------------------------------------ cavitation
-struct CavOut { double r_c, r_v, icav[4]; };
 
-__device__ inline CavOut cavsource(const Par& c, const double* pv2, const double* dv, double vol) {
-  CavOut o = {0.0, 0.0, {0.0, 0.0, 0.0, 0.0}};
+// FP64 face flux: the Roe-average EOS (only its sound speed is used,
+// src/flux_module.f90:237,319,461,588), then the flux
+template <bool MX = false>
+__device__ inline void inviscid_flux(const Par& c, const double* n, const FaceState& L, const FaceState& Rs,
+                                     const double* sdst_in, double* fx, unsigned long long* fb) {
+  const int npv = c.npv;
+  double dl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  if (dl == 0.0) {
+    for (int k = 0; k < npv; ++k) fx[k] = 0.0;
+    return;
+  }
+  double ravg[NPVM];
+  roe_state<double>(npv, L, Rs, ravg);
+  double rdv[NDV];
+  deteos_simple<MX>(c.fluid, ravg[0] + c.pref, ravg[4], ravg[5], ravg[6], rdv, fb);
+  inviscid_flux_core<double>(c, n, L, Rs, sdst_in, ravg, rdv[5], c.uref * c.uref, fx);
+}
+
+// ------------------------------------------------------------------ SST source
+// k-omega SST production, destruction and cross diffusion of one cell (kwsst + calbigf +
+// no_des, src/turbsource_module.f90:269-414) from the cell gradients gr[q][e] of
+// (u, v, w, k, omega), the cell's k, omega, density, viscosity, eddy viscosity and wall
+// distance.  r7, r8 are the residual contributions; the rest feeds the implicit
+// coefficients.  Templated for the adjoint.
+template <class T>
+struct SstOut { T r7, r8, prod, dest, div, pkw, bigf, talpha, tbeta, strain; };
+
+template <class T>
+__device__ __forceinline__ SstOut<T> sst_source(const T (*gr)[3], T kk, T oo, T rho, T mu, T mut, double y5,
+                                                double vol) {
+  const double c23 = 2.0 / 3.0, c59 = 5.0 / 9.0;
+  SstOut<T> o;
+  T dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
+  T dvdx = gr[1][0], dvdy = gr[1][1], dvdz = gr[1][2];
+  T dwdx = gr[2][0], dwdy = gr[2][1], dwdz = gr[2][2];
+  o.strain = 2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + sq(dudy + dvdx) + sq(dudz + dwdx) + sq(dvdz + dwdy);
+  o.div = dudx + dvdy + dwdz;
+  T prod = mut * (o.strain - c23 * o.div * o.div) - c23 * rho * kk * o.div;
+  o.prod = fmin(prod, 0.9 * rho * kk * oo);
+  o.pkw = gr[3][0] * gr[4][0] + gr[3][1] * gr[4][1] + gr[3][2] * gr[4][2];
+  T cdkw = fmax(1.712 * rho / oo * o.pkw, T(1.0e-10));
+  T term1 = sqrt(kk) / (0.09 * oo * y5);
+  T term2 = 500.0 * mu / rho / (oo * y5 * y5);
+  T term3 = (3.424 * rho * kk) / (cdkw * y5 * y5);
+  T arg1 = fmin(fmax(term1, term2), term3);
+  T a2 = arg1 * arg1;
+  o.bigf = tanh(a2 * a2);
+  o.talpha = o.bigf * c59 + (1.0 - o.bigf) * 0.44;
+  o.tbeta = o.bigf * 0.075 + (1.0 - o.bigf) * 0.0828;
+  T tl = sqrt(kk) / 9.0 / oo * 100.0;
+  o.dest = rho * pow(kk, 1.5) / tl;
+  o.r7 = (o.prod - o.dest) * vol;
+  o.r8 = (o.talpha * rho * (1.0 / mut) * o.prod - o.tbeta * rho * oo * oo + 1.712 * (1.0 - o.bigf) * rho * (1.0 / oo) * o.pkw) * vol;
+  return o;
+}
+
+// ------------------------------------------------------------------ viscous flux
+// Face viscous flux (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
+// from the face gradients g[x|y|z][q] of (u, v, w, T, k, omega) and their face averages
+// cc[q]; vis, con, emut, tcon are the face-averaged transport coefficients, rho the face
+// density, ydns the face wall distance.  Templated for the adjoint.
+template <class T>
+__device__ __forceinline__ void vsflux_core(const Par& c, const double* nx, const T* gx, const T* gy, const T* gz,
+                                            const T* cc, T vis, T con, T emut, T tcon, T rho, double ydns, T* fv) {
+  const bool turb = (c.iturb == 0);
+  const double c23 = 2.0 / 3.0;
+  T mu = turb ? (vis + emut) : vis;
+  T div = gx[0] + gy[1] + gz[2];
+  T txx = mu * (2.0 * gx[0] - c23 * div), tyy = mu * (2.0 * gy[1] - c23 * div), tzz = mu * (2.0 * gz[2] - c23 * div);
+  T txy = mu * (gy[0] + gx[1]), txz = mu * (gz[0] + gx[2]), tyz = mu * (gz[1] + gy[2]);
+  T kc = turb ? (con + tcon) : con;
+  T uc = cc[0], vc = cc[1], wc = cc[2];
+  fv[0] = T(0.0);
+  fv[1] = txx * nx[0] + txy * nx[1] + txz * nx[2];
+  fv[2] = txy * nx[0] + tyy * nx[1] + tyz * nx[2];
+  fv[3] = txz * nx[0] + tyz * nx[1] + tzz * nx[2];
+  fv[4] = nx[0] * (uc * txx + vc * txy + wc * txz + kc * gx[3]) + nx[1] * (uc * txy + vc * tyy + wc * tyz + kc * gy[3]) +
+          nx[2] * (uc * txz + vc * tyz + wc * tzz + kc * gz[3]);
+  fv[5] = T(0.0);
+  fv[6] = T(0.0);
+  if (turb) {
+    T pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
+    T kf = cc[4], of = cc[5];
+    T cdkw = fmax(1.712 * rho / of * pkw, T(1.0e-10));
+    T term1 = sqrt(kf) / (0.09 * of * ydns);
+    T term2 = 500.0 * vis / rho / (of * ydns * ydns);
+    T term3 = (3.424 * rho * kf) / (cdkw * ydns * ydns);
+    T arg1 = fmin(fmax(term1, term2), term3);
+    T a2 = arg1 * arg1;
+    T bigf = tanh(a2 * a2);
+    T tdk = bigf * 0.85 + (1.0 - bigf) * 1.0;
+    T tdo = bigf * 0.5 + (1.0 - bigf) * 0.856;
+    fv[7] = (vis + emut * tdk) * (gx[4] * nx[0] + gy[4] * nx[1] + gz[4] * nx[2]);
+    fv[8] = (vis + emut * tdo) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
+  }
+}
+
+// face gradient of one variable from its 18-cell stencil x (normal difference plus the
+// 1/16-weighted transverse sums, src/vsflux_module.f90:200-230); ev, tv are the averaged
+// transverse face vectors, vol the inverse mean volume
+template <class T>
+__device__ __forceinline__ void face_gradient(const T* x, const double* nx, const double* ev, const double* tv,
+                                              double vol, T& gx, T& gy, T& gz, T& cc) {
+  T dn = x[9] - x[8];
+  T de = 0.0625 * (-x[0] - x[1] + x[4] + x[5] + 2.0 * (-x[6] - x[7] + x[10] + x[11]) - x[12] - x[13] + x[16] + x[17]);
+  T dt = 0.0625 * (-x[0] - x[1] + x[12] + x[13] + 2.0 * (-x[2] - x[3] + x[14] + x[15]) - x[4] - x[5] + x[16] + x[17]);
+  gx = (dn * nx[0] + de * ev[0] + dt * tv[0]) * vol;
+  gy = (dn * nx[1] + de * ev[1] + dt * tv[1]) * vol;
+  gz = (dn * nx[2] + de * ev[2] + dt * tv[2]) * vol;
+  cc = 0.5 * (x[8] + x[9]);
+}
+
+// ------------------------------------------------------------------ cavitation
+template <class T>
+struct CavOutT { T r_c, r_v, icav[4]; };
+using CavOut = CavOutT<double>;
+
+// Mass-transfer rates r_c, r_v (times the volume) and the implicit coefficients icav of the
+// five cavitation models; the free-stream speed uref and the coefficients c_v, c_c are
+// arguments so that the adjoint can differentiate with respect to them.
+template <class T>
+__device__ inline CavOutT<T> cavsource_t(const Par& c, const T* pv2, const T* dv, double vol, T uref, T cvc,
+                                         T ccc) {
+  CavOutT<T> o;
+  o.r_c = T(0.0); o.r_v = T(0.0);
+  for (int q = 0; q < 4; ++q) o.icav[q] = T(0.0);
   if (pv2[4] >= 647.096) return o;
-  const double dp_ref = 2.0 / (c.rhoref * c.uref * c.uref);
-  const double t_ref = c.uref / c.l_chord;
-  const double P = pv2[0] + c.pref;
-  const double clamp_c = c.fix_cav_clamp ? pv2[5] : pv2[4];
-  const double clamp_v = c.fix_cav_clamp ? (1.0 - pv2[5] - pv2[6]) : (1.0 - pv2[4] - pv2[5]);
-  const double yl = 1.0 - pv2[5] - pv2[6];
-  double r_c, r_v;
+  const T dp_ref = 2.0 / (c.rhoref * uref * uref);
+  const T t_ref = uref / c.l_chord;
+  const T P = pv2[0] + c.pref;
+  const T clamp_c = c.fix_cav_clamp ? pv2[5] : pv2[4];
+  const T clamp_v = c.fix_cav_clamp ? (1.0 - pv2[5] - pv2[6]) : (1.0 - pv2[4] - pv2[5]);
+  const T yl = 1.0 - pv2[5] - pv2[6];
+  T r_c, r_v;
   if (c.ncav == 1) {  // Merkle
-    double pww = h2o_pww(pv2[4]);
-    double rho1 = 1.0 / dv[0];
-    double kc = c.c_c * dv[0] * dp_ref * t_ref, kv = c.c_v * dv[0] * dp_ref * t_ref;
-    double dpc = fmax(P - pww, 0.0), dpv = fmax(pww - P, 0.0);
-    r_c = fmin(c.c_c * dv[0] * pv2[5] * dpc * dp_ref * t_ref, dv[0] * clamp_c);
-    r_v = fmin(c.c_v * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
+    T pww = h2o_pww(pv2[4]);
+    T rho1 = 1.0 / dv[0];
+    T kc = ccc * dv[0] * dp_ref * t_ref, kv = cvc * dv[0] * dp_ref * t_ref;
+    T dpc = fmax(P - pww, 0.0), dpv = fmax(pww - P, 0.0);
+    r_c = fmin(ccc * dv[0] * pv2[5] * dpc * dp_ref * t_ref, dv[0] * clamp_c);
+    r_v = fmin(cvc * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
     if (r_c != 0.0) {
       o.icav[0] = -(r_c * dv[6] * rho1) - kc * pv2[5];
@@ -585,30 +751,30 @@ __device__ inline CavOut cavsource(const Par& c, const double* pv2, const double
       o.icav[3] = r_v * dv[9] * rho1 - kv * dpv;
     }
   } else if (c.ncav == 2) {  // Kunz
-    double pww = h2o_pww(pv2[4]);
-    double rho1 = 1.0 / dv[0];
-    double av = dv[0] * pv2[5] / dv[3], ag = dv[0] * pv2[6] / dv[4], al = 1.0 - av - ag;
-    double dpv = fmax(pww - P, 0.0);
-    r_c = fmin(c.c_c * dv[3] * av * sq(al + ag) * t_ref, dv[0] * clamp_c);
-    r_v = fmin(c.c_v * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
+    T pww = h2o_pww(pv2[4]);
+    T rho1 = 1.0 / dv[0];
+    T av = dv[0] * pv2[5] / dv[3], ag = dv[0] * pv2[6] / dv[4], al = 1.0 - av - ag;
+    T dpv = fmax(pww - P, 0.0);
+    r_c = fmin(ccc * dv[3] * av * sq(al + ag) * t_ref, dv[0] * clamp_c);
+    r_v = fmin(cvc * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
-    double av1 = 1.0 - 4.0 * av + 3.0 * av * av;
-    o.icav[0] = -(c.c_c * t_ref * (dv[6] * pv2[5] * av1 + 2.0 * av * av * dv[14] * (al + ag)));
-    o.icav[1] = -(c.c_c * t_ref * (dv[7] * pv2[5] * av1 + 2.0 * av * av * dv[15] * (al + ag)));
-    o.icav[2] = -(c.c_c * t_ref * (dv[8] * pv2[5] + dv[0]) * av1);
-    o.icav[3] = -(c.c_c * t_ref * dv[9] * pv2[5] * av1);
+    T av1 = 1.0 - 4.0 * av + 3.0 * av * av;
+    o.icav[0] = -(ccc * t_ref * (dv[6] * pv2[5] * av1 + 2.0 * av * av * dv[14] * (al + ag)));
+    o.icav[1] = -(ccc * t_ref * (dv[7] * pv2[5] * av1 + 2.0 * av * av * dv[15] * (al + ag)));
+    o.icav[2] = -(ccc * t_ref * (dv[8] * pv2[5] + dv[0]) * av1);
+    o.icav[3] = -(ccc * t_ref * dv[9] * pv2[5] * av1);
     if (r_v != 0.0) {
-      double kv = c.c_v * dv[0] * dp_ref * t_ref;
+      T kv = cvc * dv[0] * dp_ref * t_ref;
       o.icav[0] = r_v * dv[6] * rho1 - kv * yl;
       o.icav[1] = r_v * dv[7] * rho1;
       o.icav[2] = r_v * dv[8] * rho1 - kv * dpv;
       o.icav[3] = r_v * dv[9] * rho1 - kv * dpv;
     }
   } else if (c.ncav == 3) {  // Singhal
-    double pww = h2o_pww(pv2[4]);
-    double sigma = h2o_sigma(pv2[4]);
-    double rho1 = 1.0 / dv[2], rho2 = 1.0 / dv[3];
-    double cc = c.c_c * c.uref / sigma * dv[2] * dv[3], cv = c.c_v * c.uref / sigma * dv[2] * dv[3];
+    T pww = h2o_pww(pv2[4]);
+    T sigma = h2o_sigma(pv2[4]);
+    T rho1 = 1.0 / dv[2], rho2 = 1.0 / dv[3];
+    T cc = ccc * uref / sigma * dv[2] * dv[3], cv = cvc * uref / sigma * dv[2] * dv[3];
     r_c = fmin(cc * sqrt(2.0 / 3.0 * fmax(P - pww, 0.0) * rho1) * pv2[5], dv[0] * clamp_c);
     r_v = fmin(cv * sqrt(2.0 / 3.0 * fmax(pww - P, 0.0) * rho1) * yl, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
@@ -626,12 +792,12 @@ __device__ inline CavOut cavsource(const Par& c, const double* pv2, const double
     }
   } else if (c.ncav == 4) {  // Schnerr-Sauer
     const double pi = 3.14159265358979323846, eta = 1.0e13;
-    double pww = h2o_pww(pv2[4]);
-    double rho1 = 1.0 / dv[0], rho3 = 1.0 / dv[2], rho4 = 1.0 / dv[3];
-    double k0 = 3.0 * pow(4.0 * pi * eta / 3.0, 1.0 / 3.0) * sqrt(2.0 / 3.0);
-    double base = k0 * dv[0] * pow(dv[3], 1.0 / 3.0) * pow(dv[2], -5.0 / 6.0) * pow(yl, 4.0 / 3.0);
-    r_c = fmin(c.c_c * base * pow(pv2[5], 2.0 / 3.0) * sqrt(fmax(P - pww, 0.0)), dv[0] * clamp_c);
-    r_v = fmin(c.c_v * base * pow(pv2[5] + pv2[6], 2.0 / 3.0) * sqrt(fmax(pww - P, 0.0)), dv[0] * clamp_v);
+    T pww = h2o_pww(pv2[4]);
+    T rho1 = 1.0 / dv[0], rho3 = 1.0 / dv[2], rho4 = 1.0 / dv[3];
+    T k0 = 3.0 * pow(4.0 * pi * eta / 3.0, 1.0 / 3.0) * sqrt(2.0 / 3.0);
+    T base = k0 * dv[0] * pow(dv[3], 1.0 / 3.0) * pow(dv[2], -5.0 / 6.0) * pow(yl, 4.0 / 3.0);
+    r_c = fmin(ccc * base * pow(pv2[5], 2.0 / 3.0) * sqrt(fmax(P - pww, 0.0)), dv[0] * clamp_c);
+    r_v = fmin(cvc * base * pow(pv2[5] + pv2[6], 2.0 / 3.0) * sqrt(fmax(pww - P, 0.0)), dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
     if (r_c != 0.0) {
       o.icav[0] = -(r_c * (dv[6] * rho1 + dv[14] * rho4 / 3.0 - 5.0 * dv[16] * rho3 / 6.0 + 0.5 / (P - pww)));
@@ -646,28 +812,32 @@ __device__ inline CavOut cavsource(const Par& c, const double* pv2, const double
       o.icav[3] = r_v * (dv[9] * rho1 + 2.0 / (3.0 * (pv2[5] + pv2[6])) - 4.0 / (3.0 * yl));
     }
   } else {  // Lee
-    double tww = h2o_tww(P);
-    double rho1 = 1.0 / dv[0];
-    r_c = fmin(c.c_c * dv[0] * pv2[5] * fmax(tww - pv2[4], 0.0) / tww, dv[0] * clamp_c);
-    r_v = fmin(c.c_v * dv[0] * yl * fmax(pv2[4] - tww, 0.0) / tww, dv[0] * clamp_v);
+    T tww = h2o_tww(P);
+    T rho1 = 1.0 / dv[0];
+    r_c = fmin(ccc * dv[0] * pv2[5] * fmax(tww - pv2[4], 0.0) / tww, dv[0] * clamp_c);
+    r_v = fmin(cvc * dv[0] * yl * fmax(pv2[4] - tww, 0.0) / tww, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
     if (r_c != 0.0) {
       o.icav[0] = -(r_c * dv[6] * rho1);
-      o.icav[1] = -(r_c * dv[7] * rho1) + c.c_c * dv[0] * pv2[5] / tww;
-      o.icav[2] = -(r_c * dv[8] * rho1) - c.c_c * dv[0] * fmax(tww - pv2[4], 0.0) / tww;
+      o.icav[1] = -(r_c * dv[7] * rho1) + ccc * dv[0] * pv2[5] / tww;
+      o.icav[2] = -(r_c * dv[8] * rho1) - ccc * dv[0] * fmax(tww - pv2[4], 0.0) / tww;
       o.icav[3] = -(r_c * dv[9] * rho1);
     }
     if (r_v != 0.0) {
       o.icav[0] = r_v * dv[6] * rho1;
-      o.icav[1] = r_v * dv[7] * rho1 + c.c_v * dv[0] * yl / tww;
-      o.icav[2] = r_v * dv[8] * rho1 - c.c_v * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
-      o.icav[3] = r_v * dv[9] * rho1 - c.c_v * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
+      o.icav[1] = r_v * dv[7] * rho1 + cvc * dv[0] * yl / tww;
+      o.icav[2] = r_v * dv[8] * rho1 - cvc * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
+      o.icav[3] = r_v * dv[9] * rho1 - cvc * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
     }
   }
-  double lam = copysign(1.0, o.icav[2]);
-  double f = (1.0 - 0.5 * (1.0 - lam)) - 0.5 * (1.0 - lam);
+  T lam = copysign(1.0, o.icav[2]);
+  T f = (1.0 - 0.5 * (1.0 - lam)) - 0.5 * (1.0 - lam);
   for (int q = 0; q < 4; ++q) o.icav[q] *= f;
   return o;
+}
+
+__device__ inline CavOut cavsource(const Par& c, const double* pv2, const double* dv, double vol) {
+  return cavsource_t<double>(c, pv2, dv, vol, c.uref, c.c_v, c.c_c);
 }
 
 // ------------------------------------------------------------------ diagonal operator
