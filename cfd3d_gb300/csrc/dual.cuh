@@ -10,6 +10,7 @@
 // reconstruction's uncontracted arithmetic, so that ties at clip bounds resolve the same way.
 #pragma once
 #include <cmath>
+#include "iapws.cuh"
 
 namespace cfd {
 
@@ -136,5 +137,45 @@ template <int N> __device__ __forceinline__ Dual<N> nadd(const Dual<N>& a, const
 template <int N> __device__ __forceinline__ Dual<N> nsub(const Dual<N>& a, const Dual<N>& b) { return a - b; }
 
 #undef DUAL_LOOP
+
+// IF97 Gibbs sums on dual arguments: g = sum n x^I y^J with its first three derivatives
+// accumulated in FP64 term by term, then each accumulated derivative g_a becomes a dual
+// number with d(g_a) = g_ax dx + g_ay dy.  Exact, and the term loop stays plain FP64.
+template <int N>
+struct GibbsByParts<Dual<N>> {
+  static constexpr bool value = true;
+  template <const IJN* TAB, size_t K>
+  static __device__ __forceinline__ void term(double x, double xi, double y, double yi, double* S) {
+    constexpr int I = TAB[K].i;
+    constexpr int J = TAB[K].j;
+    constexpr double n = TAB[K].n;
+    const double t = n * cpow<I>(x, xi) * cpow<J>(y, yi);
+    constexpr double i1 = I, i2 = double(I) * (I - 1), i3 = double(I) * (I - 1) * (I - 2);
+    constexpr double j1 = J, j2 = double(J) * (J - 1), j3 = double(J) * (J - 1) * (J - 2);
+    if constexpr (I != 0) S[0] += i1 * t * xi;
+    if constexpr (J != 0) S[1] += j1 * t * yi;
+    if constexpr (I != 0 && I != 1) S[2] += i2 * t * (xi * xi);
+    if constexpr (I != 0 && J != 0) S[3] += i1 * j1 * t * (xi * yi);
+    if constexpr (J != 0 && J != 1) S[4] += j2 * t * (yi * yi);
+    if constexpr (I != 0 && I != 1 && I != 2) S[5] += i3 * t * (xi * xi * xi);
+    if constexpr (I != 0 && I != 1 && J != 0) S[6] += i2 * j1 * t * (xi * xi * yi);
+    if constexpr (I != 0 && J != 0 && J != 1) S[7] += i1 * j2 * t * (xi * yi * yi);
+    if constexpr (J != 0 && J != 1 && J != 2) S[8] += j3 * t * (yi * yi * yi);
+  }
+  template <const IJN* TAB, size_t... K>
+  static __device__ __forceinline__ void sum(const Dual<N>& x, const Dual<N>& xi, const Dual<N>& y,
+                                             const Dual<N>& yi, GAcc<Dual<N>>& a) {
+    // S: g_x, g_y, g_xx, g_xy, g_yy, g_xxx, g_xxy, g_xyy, g_yyy
+    double S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    (term<TAB, K>(x.v, xi.v, y.v, yi.v, S), ...);
+    const int from[5][3] = {{0, 2, 3}, {1, 3, 4}, {2, 5, 6}, {3, 6, 7}, {4, 7, 8}};
+    Dual<N>* out[5] = {&a.x, &a.y, &a.xx, &a.xy, &a.yy};
+    for (int q = 0; q < 5; ++q) {
+      Dual<N> r(S[from[q][0]]);
+      for (int i = 0; i < N; ++i) r.d[i] = S[from[q][1]] * x.d[i] + S[from[q][2]] * y.d[i];
+      *out[q] = *out[q] + r;
+    }
+  }
+};
 
 }  // namespace cfd

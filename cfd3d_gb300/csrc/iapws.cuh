@@ -128,9 +128,19 @@ __device__ __forceinline__ void gterm(T x, T xi, T y, T yi, GAcc<T>& a) {
   }
 }
 
+// Scalar types that evaluate the Gibbs sums by parts (the adjoint's dual numbers, which
+// specialise this trait): the sums and their derivatives are accumulated in plain FP64 and
+// the dual results formed once, instead of carrying the derivatives through every term.
+template <class T>
+struct GibbsByParts { static constexpr bool value = false; };
+
 template <class T, const IJN* TAB, bool FULL = true, size_t... K>
 __device__ __forceinline__ void gsum(T x, T xi, T y, T yi, GAcc<T>& a, std::index_sequence<K...>) {
-  (gterm<T, TAB, K, FULL>(x, xi, y, yi, a), ...);
+  if constexpr (GibbsByParts<T>::value) {
+    GibbsByParts<T>::template sum<TAB, K...>(x, xi, y, yi, a);
+  } else {
+    (gterm<T, TAB, K, FULL>(x, xi, y, yi, a), ...);
+  }
 }
 
 template <class T>
