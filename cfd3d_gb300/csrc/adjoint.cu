@@ -255,3 +255,248 @@ __device__ __noinline__ double adj_face_inviscid(const DevPtr& d, const Par& c, 
     for (int l = 0; l < 18; ++l) aadd(&a.gpv[stencil_cell(l, g, sn, s1, s2)], w[S_SDST + l]);
   return w[S_UREF];
 }
+
+// Viscous part of a face: lamV . dV/d(stencil pv of u, v, w, T, k, omega; face-cell dv / tv)
+template <int DIR>
+__device__ __noinline__ void adj_face_viscous(const DevPtr& d, const Par& c, const AdjPtr& a, const double* nx,
+                                              long long g, long long gr, long long sn, long long s1, long long s2,
+                                              const double* lamV) {
+  const long long n = d.ncell;
+  const int npv = c.npv;
+  const bool turb = (c.iturb == 0);
+  const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);
+  const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);
+  double ev[3], tvv[3];
+  for (int q = 0; q < 3; ++q) {
+    const double* P = d.gm + (ep + q) * n;
+    ev[q] = 0.25 * (P[g - s1] + P[g - s1 + sn] + P[g] + P[g + sn]);
+    const double* T = d.gm + (tp + q) * n;
+    tvv[q] = 0.25 * (T[g - s2] + T[g - s2 + sn] + T[g] + T[g + sn]);
+  }
+  const double vol = 2.0 / (d.gm[GM_GRD * n + g] + d.gm[GM_GRD * n + gr]);
+  double tvl[3] = {0, 0, 0}, tvr[3] = {0, 0, 0};
+  for (int q = 0; q < c.ntv; ++q) { tvl[q] = d.tv[q * n + g]; tvr[q] = d.tv[q * n + gr]; }
+  const double vis = 0.5 * (tvl[0] + tvr[0]);
+  const double con = 0.5 * (tvl[1] + tvr[1]);
+  double emut = 0.0, tcon = 0.0, rho = 0.0, ydns = 0.0;
+  const double cpl = d.dv[11 * n + g], cpr = d.dv[11 * n + gr];
+  if (turb) {
+    emut = 0.5 * (tvl[2] + tvr[2]);
+    tcon = 0.5 * (tvl[2] * cpl + tvr[2] * cpr) / 0.9;
+    rho = 0.5 * (d.dv[g] + d.dv[gr]);
+    ydns = 0.5 * (d.gm[(GM_GRD + 4) * n + g] + d.gm[(GM_GRD + 4) * n + gr]);
+  }
+  const int vars[6] = {1, 2, 3, 4, 7, 8};
+  const int nv = turb ? 6 : 4;
+  double gxv[6], gyv[6], gzv[6], ccv[6];
+  for (int q = 0; q < 6; ++q) gxv[q] = gyv[q] = gzv[q] = ccv[q] = 0.0;
+  for (int q = 0; q < nv; ++q) {
+    double x[18];
+    for (int l = 0; l < 18; ++l) x[l] = d.pv[vars[q] * n + stencil_cell(l, g, sn, s1, s2)];
+    face_gradient<double>(x, nx, ev, tvv, vol, gxv[q], gyv[q], gzv[q], ccv[q]);
+  }
+  double w[NS_VIS];
+  for (int q = 0; q < NS_VIS; ++q) w[q] = 0.0;
+  for (int k0 = 0; k0 < NS_VIS; k0 += DC) {
+    DD gx[6], gy[6], gz[6], cc[6];
+    for (int q = 0; q < 6; ++q) {
+      gx[q] = seed(gxv[q], V_GX + q, k0); gy[q] = seed(gyv[q], V_GY + q, k0);
+      gz[q] = seed(gzv[q], V_GZ + q, k0); cc[q] = seed(ccv[q], V_CC + q, k0);
+    }
+    DD fv[NPVM];
+    vsflux_core<DD>(c, nx, gx, gy, gz, cc, seed(vis, V_VIS, k0), seed(con, V_CON, k0), seed(emut, V_MUT, k0),
+                    seed(tcon, V_TCON, k0), seed(rho, V_RHO, k0), ydns, fv);
+    for (int q = 0; q < DC && k0 + q < NS_VIS; ++q) {
+      double acc = 0.0;
+      for (int v = 0; v < npv; ++v) acc += lamV[v] * fv[v].d[q];
+      w[k0 + q] = acc;
+    }
+  }
+  // through the (linear) face gradients and averages to the stencil
+  for (int q = 0; q < nv; ++q) {
+    for (int l = 0; l < 18; ++l) {
+      double cn, ce, ct, cc;
+      grad_coeffs(l, cn, ce, ct, cc);
+      const double dgx = (cn * nx[0] + ce * ev[0] + ct * tvv[0]) * vol;
+      const double dgy = (cn * nx[1] + ce * ev[1] + ct * tvv[1]) * vol;
+      const double dgz = (cn * nx[2] + ce * ev[2] + ct * tvv[2]) * vol;
+      const double gs = w[V_GX + q] * dgx + w[V_GY + q] * dgy + w[V_GZ + q] * dgz + w[V_CC + q] * cc;
+      aadd(&a.gpv[vars[q] * n + stencil_cell(l, g, sn, s1, s2)], gs);
+    }
+  }
+  // face averages of the two cells' transport coefficients, specific heat and density
+  const long long cl[2] = {g, gr};
+  const double mut[2] = {tvl[2], tvr[2]}, cp[2] = {cpl, cpr};
+  for (int s = 0; s < 2; ++s) {
+    const long long q = cl[s];
+    aadd(&a.gdt[GD_VIS * n + q], 0.5 * w[V_VIS]);
+    aadd(&a.gdt[GD_CON * n + q], 0.5 * w[V_CON]);
+    if (turb) {
+      aadd(&a.gdt[GD_MUT * n + q], 0.5 * w[V_MUT] + w[V_TCON] * 0.5 * cp[s] / 0.9);
+      aadd(&a.gdt[GD_CP * n + q], w[V_TCON] * 0.5 * mut[s] / 0.9);
+      aadd(&a.gdt[GD_RHO * n + q], 0.5 * w[V_RHO]);
+    }
+  }
+}
+
+// One thread per face (the face numbering of k_face_flux).  Face g (between cells g and
+// gr = g + sn) enters the residual of g as -F + V and of gr as +F - V.
+template <int DIR>
+__global__ void __launch_bounds__(64) k_adj_face(DevPtr d, Par c, AdjPtr a) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double wpar = 0.0;
+  int b = 0;
+  while (b + 1 < d.nblk && t >= d.blk[b + 1].face_off[DIR]) ++b;
+  const BlockGeom& B = d.blk[b];
+  const long long loc = t - B.face_off[DIR];
+  int fi_, fj, fk;
+  if (DIR == 0) { fi_ = B.imax; fj = B.jmax - 1; fk = B.kmax - 1; }
+  else if (DIR == 1) { fi_ = B.imax - 1; fj = B.jmax; fk = B.kmax - 1; }
+  else { fi_ = B.imax - 1; fj = B.jmax - 1; fk = B.kmax; }
+  if (loc >= 0 && loc < (long long)fi_ * fj * fk) {
+    const int i = (int)(loc % fi_) + (DIR == 0 ? 1 : 2);
+    const long long r = loc / fi_;
+    const int j = (int)(r % fj) + (DIR == 1 ? 1 : 2);
+    const int k = (int)(r / fj) + (DIR == 2 ? 1 : 2);
+    const long long n = d.ncell;
+    const long long si = 1, sj = B.ni, sk = (long long)B.ni * B.nj;
+    const long long g = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
+    long long sn, s1, s2;
+    if (DIR == 0) { sn = si; s1 = sj; s2 = sk; }
+    else if (DIR == 1) { sn = sj; s1 = sk; s2 = si; }
+    else { sn = sk; s1 = si; s2 = sj; }
+    const long long gr = g + sn;
+    double lamF[NPVM], lamV[NPVM];
+    bool any = false;
+    for (int v = 0; v < NPVM; ++v) {
+      lamF[v] = (v < c.npv) ? a.lam[v * n + gr] - a.lam[v * n + g] : 0.0;
+      lamV[v] = -lamF[v];
+      any = any || (lamF[v] != 0.0);
+    }
+    if (any) {
+      const int fplane = (DIR == 0) ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
+      double nx[3];
+      face_vec(d, fplane, g, nx);
+      wpar = adj_face_inviscid(d, c, a, nx, g, gr, sn, s1, s2, lamF);
+      if (c.iturb != -3) adj_face_viscous<DIR>(d, c, a, nx, g, gr, sn, s1, s2, lamV);
+    }
+  }
+  // one atomic per warp for the free-stream-speed gradient
+  for (int o = 16; o > 0; o >>= 1) wpar += __shfl_down_sync(0xffffffffu, wpar, o);
+  if ((threadIdx.x & 31) == 0) aadd(&a.gpar[0], wpar);
+}
+
+// ------------------------------------------------------------------ cell sources
+// Per interior cell: the cavitation source (res(6)), the SST sources (res(8:9)) and the
+// dual-time source, as k_rhs adds them (src/rhs_module.f90:540-642).
+__global__ void __launch_bounds__(64) k_adj_cell(DevPtr d, Par c, AdjPtr a) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double wp[3] = {0.0, 0.0, 0.0};
+  if (t < d.nint) {
+    const int b = find_block_interior(d.blk, d.nblk, t);
+    int i, j, k;
+    const BlockGeom& B = d.blk[b];
+    const long long g = interior_cell(B, t - B.int_off, i, j, k);
+    const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+    const int npv = c.npv;
+    double lam[NPVM], pv2[NPVM], dv[NDV];
+    for (int v = 0; v < NPVM; ++v) {
+      lam[v] = (v < npv) ? a.lam[v * n + g] : 0.0;
+      pv2[v] = (v < npv) ? d.pv[v * n + g] : 0.0;
+    }
+    for (int v = 0; v < NDV; ++v) dv[v] = d.dv[v * n + g];
+    const double vol = d.gm[GM_GRD * n + g];
+    double gp[NPVM], gd[NGD];
+    for (int v = 0; v < NPVM; ++v) gp[v] = 0.0;
+    for (int m = 0; m < NGD; ++m) gd[m] = 0.0;
+    // ---- cavitation: res(6) += r_v - r_c; seeds p, T, y1, y2, rho, rho_l, rho_v, uref, c_v, c_c
+    if (c.ncav && lam[5] != 0.0) {
+      const int pvs[4] = {0, 4, 5, 6};
+      const int dvs[3] = {0, 2, 3};
+      double w[10];
+      for (int k0 = 0; k0 < 10; k0 += DC) {
+        DD p2[NPVM], dd[NDV];
+        for (int v = 0; v < NPVM; ++v) p2[v] = DD(pv2[v]);
+        for (int q = 0; q < NDV; ++q) dd[q] = DD(dv[q]);
+        for (int m = 0; m < 4; ++m) p2[pvs[m]] = seed(pv2[pvs[m]], m, k0);
+        for (int m = 0; m < 3; ++m) dd[dvs[m]] = seed(dv[dvs[m]], 4 + m, k0);
+        const CavOutT<DD> o = cavsource_t<DD>(c, p2, dd, vol, seed(c.uref, 7, k0), seed(c.c_v, 8, k0),
+                                              seed(c.c_c, 9, k0));
+        for (int q = 0; q < DC && k0 + q < 10; ++q) w[k0 + q] = lam[5] * (o.r_v.d[q] - o.r_c.d[q]);
+      }
+      for (int m = 0; m < 4; ++m) gp[pvs[m]] += w[m];
+      gd[GD_RHO] += w[4]; gd[GD_RL] += w[5]; gd[GD_RV] += w[6];
+      wp[0] += w[7]; wp[1] += w[8]; wp[2] += w[9];
+    }
+    // ---- SST: res(8) += r7, res(9) += r8; seeds the 15 cell gradients, k, omega, rho, mu, mu_t
+    if (c.iturb == 0 && (lam[7] != 0.0 || lam[8] != 0.0)) {
+      const long long nbr[6] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk};
+      double fa[6][3];
+      for (int q = 0; q < 3; ++q) {
+        fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
+        fa[2][q] = d.gm[(GM_EX + q) * n + g - sj]; fa[3][q] = d.gm[(GM_EX + q) * n + g];
+        fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
+      }
+      const int gv[5] = {1, 2, 3, 7, 8};
+      double grv[5][3];
+      const double ivol = 1.0 / vol;
+      for (int q = 0; q < 5; ++q) {
+        const double* P = d.pv + gv[q] * n;
+        const double c0 = P[g];
+        const double v1 = 0.5 * (P[nbr[0]] + c0), v2 = 0.5 * (P[nbr[1]] + c0), v3 = 0.5 * (P[nbr[2]] + c0);
+        const double v4 = 0.5 * (P[nbr[3]] + c0), v5 = 0.5 * (P[nbr[4]] + c0), v6 = 0.5 * (P[nbr[5]] + c0);
+        for (int e = 0; e < 3; ++e)
+          grv[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
+      }
+      const double mu = d.tv[g], mut = d.tv[2 * n + g];
+      const double y5 = d.gm[(GM_GRD + 4) * n + g];
+      double w[20];
+      for (int k0 = 0; k0 < 20; k0 += DC) {
+        DD gr[5][3];
+        for (int q = 0; q < 5; ++q)
+          for (int e = 0; e < 3; ++e) gr[q][e] = seed(grv[q][e], 3 * q + e, k0);
+        const SstOut<DD> so = sst_source<DD>(gr, seed(pv2[7], 15, k0), seed(pv2[8], 16, k0), seed(dv[0], 17, k0),
+                                             seed(mu, 18, k0), seed(mut, 19, k0), y5, vol);
+        for (int q = 0; q < DC && k0 + q < 20; ++q) w[k0 + q] = lam[7] * so.r7.d[q] + lam[8] * so.r8.d[q];
+      }
+      // the cell gradients are linear in the face averages 0.5 (P[nbr] + P[g])
+      const double sgn[6] = {-1.0, 1.0, -1.0, 1.0, -1.0, 1.0};
+      for (int q = 0; q < 5; ++q) {
+        double gc = 0.0;
+        for (int m = 0; m < 6; ++m) {
+          double s = 0.0;
+          for (int e = 0; e < 3; ++e) s += w[3 * q + e] * fa[m][e];
+          s *= 0.5 * sgn[m] * ivol;
+          gc += s;
+          aadd(&a.gpv[gv[q] * n + nbr[m]], s);
+        }
+        gp[gv[q]] += gc;
+      }
+      gp[7] += w[15]; gp[8] += w[16];
+      gd[GD_RHO] += w[17]; gd[GD_VIS] += w[18]; gd[GD_MUT] += w[19];
+    }
+    // ---- dual-time source: res -= (nsteady bb Q(pv, dv) - history) vol / dt_phy
+    if (c.nsteady >= 1) {
+      const double bb = (c.nsteady == 1) ? 1.0 : 0.75;
+      const double cst = (double)c.nsteady * bb * vol / c.dt_phy;
+      double mu_[NPVM];
+      for (int v = 0; v < NPVM; ++v) mu_[v] = -cst * lam[v];
+      const double r = dv[0], h = dv[1], u1 = pv2[1], u2 = pv2[2], u3 = pv2[3];
+      double grho = mu_[0] + mu_[1] * u1 + mu_[2] * u2 + mu_[3] * u3 + mu_[4] * (h + 0.5 * (u1 * u1 + u2 * u2 + u3 * u3));
+      for (int v = 5; v < npv; ++v) { grho += mu_[v] * pv2[v]; gp[v] += mu_[v] * r; }
+      gp[1] += mu_[1] * r + mu_[4] * r * u1;
+      gp[2] += mu_[2] * r + mu_[4] * r * u2;
+      gp[3] += mu_[3] * r + mu_[4] * r * u3;
+      gp[0] -= mu_[4];
+      gd[GD_RHO] += grho;
+      gd[GD_H] += mu_[4] * r;
+    }
+    for (int v = 0; v < npv; ++v) aadd(&a.gpv[v * n + g], gp[v]);
+    for (int m = 0; m < NGD; ++m) aadd(&a.gdt[m * n + g], gd[m]);
+  }
+  for (int q = 0; q < 3; ++q) {
+    double s = wp[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) aadd(&a.gpar[q], s);
+  }
+}
