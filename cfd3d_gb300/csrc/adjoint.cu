@@ -500,3 +500,249 @@ __global__ void __launch_bounds__(64) k_adj_cell(DevPtr d, Par c, AdjPtr a) {
     if ((threadIdx.x & 31) == 0) aadd(&a.gpar[q], s);
   }
 }
+
+// ------------------------------------------------------------------ boundary program
+// One ghost operation of k_ghost reversed.  Its destination's gradient is taken and
+// cleared (the ghost value it overwrote reached nothing), then pushed to the cells the
+// operation read.  Within a phase no operation reads another one's destination, so the
+// phases run in reverse order (2, 1, 0) with the operations of a phase in parallel.
+__device__ __forceinline__ void push_cell(const AdjPtr& a, const Par& c, long long n, long long q, const double* gp,
+                                          const double* gd) {
+  for (int v = 0; v < c.npv; ++v) aadd(&a.gpv[v * n + q], gp[v]);
+  for (int m = 0; m < NGD; ++m) aadd(&a.gdt[m * n + q], gd[m]);
+}
+
+__global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict__ ops, int nops) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  double wu = 0.0;
+  if (q < nops) {
+    const GhostOp op = ops[q];
+    const long long n = d.ncell;
+    const int npv = c.npv;
+    double gp[NPVM], gd[NGD];
+    bool any = false;
+    for (int v = 0; v < NPVM; ++v) {
+      gp[v] = 0.0;
+      if (v < npv) { gp[v] = a.gpv[v * n + op.dst]; a.gpv[v * n + op.dst] = 0.0; }
+      any = any || gp[v] != 0.0;
+    }
+    for (int m = 0; m < NGD; ++m) {
+      gd[m] = a.gdt[m * n + op.dst];
+      a.gdt[m * n + op.dst] = 0.0;
+      any = any || gd[m] != 0.0;
+    }
+    if (any) {
+      const long long src = op.src;
+      switch (op.kind) {
+        case G_COPY:
+        case G_EXTRAP:
+          push_cell(a, c, n, src, gp, gd);
+          break;
+        case G_WALL_VISCOUS:
+          gp[1] = -gp[1]; gp[2] = -gp[2]; gp[3] = -gp[3];
+          push_cell(a, c, n, src, gp, gd);
+          break;
+        case G_WALL_KW: {
+          // omega_ghost = 1600 mu_b / rho_b / y5^2 - omega_src
+          const double vis_b = d.tv[op.bnd], rho_b = d.dv[op.bnd], y5 = d.gm[(GM_GRD + 4) * n + op.bnd];
+          const double kw = 1600.0 / (y5 * y5);
+          aadd(&a.gdt[GD_VIS * n + op.bnd], gp[8] * kw / rho_b);
+          aadd(&a.gdt[GD_RHO * n + op.bnd], -gp[8] * kw * vis_b / (rho_b * rho_b));
+          gp[1] = -gp[1]; gp[2] = -gp[2]; gp[3] = -gp[3]; gp[7] = -gp[7]; gp[8] = -gp[8];
+          gd[GD_MUT] = -gd[GD_MUT];
+          push_cell(a, c, n, src, gp, gd);
+          break;
+        }
+        case G_SYMMETRY: {
+          // u_ghost = 2 (u_b - n (u_b . n) / |n|^2) - u_src
+          double nx[3];
+          face_vec(d, op.fplane, op.fidx, nx);
+          for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;
+          const double nn = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
+          for (int jx = 0; jx < 3; ++jx) {
+            double s = 0.0;
+            for (int ix = 0; ix < 3; ++ix) s += gp[1 + ix] * 2.0 * ((ix == jx ? 1.0 : 0.0) - nx[ix] * nx[jx] / nn);
+            aadd(&a.gpv[(1 + jx) * n + op.bnd], s);
+          }
+          gp[1] = -gp[1]; gp[2] = -gp[2]; gp[3] = -gp[3];
+          push_cell(a, c, n, src, gp, gd);
+          break;
+        }
+        case G_FARFIELD: {
+          double nx[3];
+          face_vec(d, op.fplane, op.fidx, nx);
+          for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;
+          const double dl = 1.0 / ::sqrt(nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
+          double sp[NPVM], pb[4], xp[NPVM], bpv[NPVM];
+          for (int v = 0; v < NPVM; ++v) sp[v] = (v < npv) ? d.pv[v * n + src] : 0.0;
+          for (int m = 0; m < 4; ++m) pb[m] = d.pv[m * n + op.bnd];
+          const double rb = d.dv[op.bnd], c2b = d.dv[5 * n + op.bnd];
+          bpv[0] = c.pref; bpv[1] = c.uref_vec[0]; bpv[2] = c.uref_vec[1]; bpv[3] = c.uref_vec[2];
+          bpv[4] = c.tref; bpv[5] = c.y1ref; bpv[6] = c.y2ref; bpv[7] = c.kref; bpv[8] = c.oref;
+          for (int v = 0; v < NPVM; ++v) xp[v] = sp[v];
+          farfield_pv<double>(c, nx, dl, pb, rb, c2b, bpv, c.uref * c.uref, xp);
+          // the ghost's dv and tv(1:2) are its EOS; tv(3) (and tv(1:2) without transport
+          // properties) is the mirror cell's
+          double ge[4];
+          eos_chain(c, xp[0] + bpv[0], xp[4], xp[5], xp[6], gd, ge);
+          gp[0] += ge[0]; gp[4] += ge[1]; gp[5] += ge[2]; gp[6] += ge[3];
+          aadd(&a.gdt[GD_MUT * n + src], gd[GD_MUT]);
+          if (!c.with_prop) { aadd(&a.gdt[GD_VIS * n + src], gd[GD_VIS]); aadd(&a.gdt[GD_CON * n + src], gd[GD_CON]); }
+          // the ghost pv: seeds mirror pv 0..8, boundary p, u, v, w 9..12, rho_b 13, c2_b 14, uref 15
+          double w[16];
+          for (int k0 = 0; k0 < 16; k0 += DC) {
+            DD x[NPVM], pbd[4], bp[NPVM];
+            for (int v = 0; v < NPVM; ++v) x[v] = seed(sp[v], v, k0);
+            for (int m = 0; m < 4; ++m) pbd[m] = seed(pb[m], 9 + m, k0);
+            const DD ur = seed(c.uref, 15, k0);
+            for (int v = 0; v < NPVM; ++v) bp[v] = DD(bpv[v]);
+            if (c.uref != 0.0 && 15 >= k0 && 15 < k0 + DC)
+              for (int e = 0; e < 3; ++e) bp[1 + e].d[15 - k0] = c.uref_vec[e] / c.uref;
+            farfield_pv<DD>(c, nx, dl, pbd, seed(rb, 13, k0), seed(c2b, 14, k0), bp, ur * ur, x);
+            for (int qq = 0; qq < DC && k0 + qq < 16; ++qq) {
+              double s = 0.0;
+              for (int v = 0; v < npv; ++v) s += gp[v] * x[v].d[qq];
+              w[k0 + qq] = s;
+            }
+          }
+          for (int v = 0; v < npv; ++v) aadd(&a.gpv[v * n + src], w[v]);
+          for (int m = 0; m < 4; ++m) aadd(&a.gpv[m * n + op.bnd], w[9 + m]);
+          aadd(&a.gdt[GD_RHO * n + op.bnd], w[13]);
+          aadd(&a.gdt[GD_C2 * n + op.bnd], w[14]);
+          wu += w[15];
+          break;
+        }
+        case G_WALLWALL:
+        case G_WALLWALL_KW4:
+        case G_WALLWALL_KW8: {
+          // modified entries: -(src + sum of neighbours); the rest are the source cell's
+          bool mod[NPVM];
+          for (int v = 0; v < NPVM; ++v) mod[v] = (v >= 1 && v <= 3);
+          if (op.kind != G_WALLWALL || npv > 7) { mod[7] = true; mod[8] = true; }
+          if (op.kind != G_WALLWALL) {
+            // omega_ghost = K 800 mu_src / rho_src / y5^2 + ppv(8)
+            const double y5 = d.gm[(GM_GRD + 4) * n + src];
+            const double kw = ((op.kind == G_WALLWALL_KW8) ? 8.0 : 4.0) * 800.0 / (y5 * y5);
+            const double mu_s = d.tv[src], rho_s = d.dv[src];
+            gd[GD_VIS] += gp[8] * kw / rho_s;
+            gd[GD_RHO] -= gp[8] * kw * mu_s / (rho_s * rho_s);
+          }
+          double gs[NPVM];
+          for (int v = 0; v < NPVM; ++v) gs[v] = mod[v] ? -gp[v] : gp[v];
+          push_cell(a, c, n, src, gs, gd);
+          for (int m = 0; m < 6; ++m) {
+            if (op.nb[m] < 0) break;
+            for (int v = 0; v < npv; ++v)
+              if (mod[v]) aadd(&a.gpv[v * n + op.nb[m]], -gp[v]);
+          }
+          break;
+        }
+        case G_NOWALL3:
+        case G_NOWALL7: {
+          // the ghost is the mean of the source cell and its neighbours, then its EOS
+          const double f = (op.kind == G_NOWALL7) ? 1.0 / 7.0 : 1.0 / 3.0;
+          double sum[NPVM];
+          for (int v = 0; v < NPVM; ++v) sum[v] = (v < npv) ? d.pv[v * n + src] : 0.0;
+          for (int m = 0; m < 6; ++m) {
+            if (op.nb[m] < 0) break;
+            for (int v = 0; v < npv; ++v) sum[v] += d.pv[v * n + op.nb[m]];
+          }
+          double xp[NPVM];
+          for (int v = 0; v < NPVM; ++v) xp[v] = f * sum[v];
+          double ge[4];
+          eos_chain(c, xp[0] + c.pref, xp[4], xp[5], xp[6], gd, ge);
+          gp[0] += ge[0]; gp[4] += ge[1]; gp[5] += ge[2]; gp[6] += ge[3];
+          double gt[NGD];
+          for (int m = 0; m < NGD; ++m) gt[m] = 0.0;
+          gt[GD_MUT] = f * gd[GD_MUT];
+          if (!c.with_prop) { gt[GD_VIS] = f * gd[GD_VIS]; gt[GD_CON] = f * gd[GD_CON]; }
+          double gs[NPVM];
+          for (int v = 0; v < NPVM; ++v) gs[v] = f * gp[v];
+          push_cell(a, c, n, src, gs, gt);
+          for (int m = 0; m < 6; ++m) {
+            if (op.nb[m] < 0) break;
+            push_cell(a, c, n, op.nb[m], gs, gt);
+          }
+          break;
+        }
+        default:
+          break;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) wu += __shfl_down_sync(0xffffffffu, wu, o);
+  if ((threadIdx.x & 31) == 0) aadd(&a.gpar[0], wu);
+}
+
+// ------------------------------------------------------------------ interior EOS
+// dv and tv(1:2) of an interior cell are its EOS: their gradient goes to (p, T, y1, y2)
+__global__ void k_adj_eos(DevPtr d, Par c, AdjPtr a) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= d.nint) return;
+  const int b = find_block_interior(d.blk, d.nblk, t);
+  int i, j, k;
+  const long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
+  const long long n = d.ncell;
+  double gd[NGD];
+  bool any = false;
+  for (int m = 0; m < NGD; ++m) {
+    gd[m] = (m == GD_MUT) ? 0.0 : a.gdt[m * n + g];
+    any = any || gd[m] != 0.0;
+  }
+  if (!any) return;
+  double ge[4];
+  eos_chain(c, d.pv[g] + c.pref, d.pv[4 * n + g], d.pv[5 * n + g], d.pv[6 * n + g], gd, ge);
+  a.gpv[g] += ge[0];
+  a.gpv[4 * n + g] += ge[1];
+  a.gpv[5 * n + g] += ge[2];
+  a.gpv[6 * n + g] += ge[3];
+}
+
+// ------------------------------------------------------------------ host side
+namespace {
+inline unsigned adj_blocks(long long n, int T) { return (unsigned)((n + T - 1) / T); }
+}
+
+int adjoint_buffers(Engine& E) {
+  const size_t n = (size_t)E.ncell;
+  const int npv = E.par.npv;
+  if (!E.adj_lam) {
+    if (cudaMalloc(&E.adj_lam, n * npv * 8) != cudaSuccess || cudaMalloc(&E.adj_gpv, n * npv * 8) != cudaSuccess ||
+        cudaMalloc(&E.adj_gdt, n * NGD * 8) != cudaSuccess || cudaMalloc(&E.adj_gpar, 4 * 8) != cudaSuccess) {
+      E.err = "device allocation failed (adjoint buffers)";
+      return CFD3D_ERR_NOMEM;
+    }
+  }
+  cudaMemsetAsync(E.adj_lam, 0, n * npv * 8, E.st);
+  cudaMemsetAsync(E.adj_gpv, 0, n * npv * 8, E.st);
+  cudaMemsetAsync(E.adj_gdt, 0, n * NGD * 8, E.st);
+  cudaMemsetAsync(E.adj_gpar, 0, 4 * 8, E.st);
+  return CFD3D_OK;
+}
+
+void adjoint_free(Engine& E) {
+  cudaFree(E.adj_lam); cudaFree(E.adj_gpv); cudaFree(E.adj_gdt); cudaFree(E.adj_gpar);
+  E.adj_lam = E.adj_gpv = E.adj_gdt = E.adj_gpar = nullptr;
+}
+
+// the reverse pass; the cotangent is in adj_lam and the ghost cells hold the values of the
+// forward boundary program
+int adjoint_launch(Engine& E) {
+  const DevPtr& d = E.d;
+  const Par& c = E.par;
+  cudaStream_t s = E.st;
+  const AdjPtr a{E.adj_lam, E.adj_gpv, E.adj_gdt, E.adj_gpar};
+  const int TF = 64;
+  k_adj_face<0><<<adj_blocks(E.nface[0], TF), TF, 0, s>>>(d, c, a);
+  k_adj_face<1><<<adj_blocks(E.nface[1], TF), TF, 0, s>>>(d, c, a);
+  k_adj_face<2><<<adj_blocks(E.nface[2], TF), TF, 0, s>>>(d, c, a);
+  k_adj_cell<<<adj_blocks(E.nint, 64), 64, 0, s>>>(d, c, a);
+  for (int p = 2; p >= 0; --p)
+    if (E.nops[p]) k_adj_ghost<<<adj_blocks(E.nops[p], 64), 64, 0, s>>>(d, c, a, E.d_ops[p], E.nops[p]);
+  k_adj_eos<<<adj_blocks(E.nint, 64), 64, 0, s>>>(d, c, a);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { E.err = std::string("adjoint launch: ") + cudaGetErrorString(e); return CFD3D_ERR_CUDA; }
+  return CFD3D_OK;
+}
+
+}  // namespace cfd
