@@ -1057,6 +1057,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d.rec);
   cudaFree(E.d.recf);
   cudaFree(E.d.dqsf);
+  adjoint_free(E);
   if (E.st) cudaStreamDestroy(E.st);
   delete h;
 }
@@ -1237,6 +1238,47 @@ int cfd3d_residual(cfd3d_handle* h, int block, double* res, double* icav, double
     if (!it.a) continue;
     k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, it.nv, B, it.src, E.ncell, 0);
     CFD_CUDA(cudaMemcpyAsync(it.a, h->staging, (size_t)nint * it.nv * 8, cudaMemcpyDeviceToHost, E.st));
+    CFD_CUDA(cudaStreamSynchronize(E.st));
+  }
+  return CFD3D_OK;
+}
+
+int cfd3d_residual_vjp(cfd3d_handle* h, const double* cot, double* g_state, double* g_params) {
+  if (!h || !cot) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  const Par& c = E.par;
+  long long maxint = 0;
+  for (const BlockGeom& B : E.blk) maxint = std::max(maxint, (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1));
+  int rc = ensure_staging(h, (size_t)maxint * c.npv * 8);
+  if (rc) return rc;
+  if ((rc = adjoint_buffers(E))) return rc;
+  // the cotangent, block after block, into the padded interior
+  size_t off = 0;
+  for (const BlockGeom& B : E.blk) {
+    const long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+    CFD_CUDA(cudaMemcpyAsync(h->staging, cot + off, (size_t)nint * c.npv * 8, cudaMemcpyHostToDevice, E.st));
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, c.npv, B, E.adj_lam, E.ncell, 1);
+    CFD_CUDA(cudaStreamSynchronize(E.st));
+    off += (size_t)nint * c.npv;
+  }
+  // the forward boundary program: the ghost values the residual sees
+  for (int p = 0; p < 3; ++p)
+    if (E.nops[p]) k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, E.st>>>(E.d, c, E.d_ops[p], E.nops[p]);
+  if ((rc = adjoint_launch(E))) return rc;
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  if (g_state) {
+    off = 0;
+    for (const BlockGeom& B : E.blk) {
+      const long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+      k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, c.npv, B, E.adj_gpv, E.ncell, 0);
+      CFD_CUDA(cudaMemcpyAsync(g_state + off, h->staging, (size_t)nint * c.npv * 8, cudaMemcpyDeviceToHost, E.st));
+      CFD_CUDA(cudaStreamSynchronize(E.st));
+      off += (size_t)nint * c.npv;
+    }
+  }
+  if (g_params) {
+    CFD_CUDA(cudaMemcpyAsync(g_params, E.adj_gpar, 3 * 8, cudaMemcpyDeviceToHost, E.st));
     CFD_CUDA(cudaStreamSynchronize(E.st));
   }
   return CFD3D_OK;

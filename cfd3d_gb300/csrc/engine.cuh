@@ -116,6 +116,9 @@ struct Engine {
   std::string err;
   // host copies of the reference state used by the ghost program
   double pv_ref[NPVM];
+  // discrete adjoint (allocated by the first cfd3d_residual_vjp): padded cotangent and
+  // gradients, and the three parameter gradients
+  double *adj_lam = nullptr, *adj_gpv = nullptr, *adj_gdt = nullptr, *adj_gpar = nullptr;
 };
 
 // ------------------------------------------------------------------ index helpers
@@ -163,6 +166,11 @@ __device__ __forceinline__ long long stencil_cell(int l, long long g, long long 
 // face-flux launchers (flux.cu: FP64 form; flux_mixed.cu: mixed form)
 void launch_face_flux(const Engine& E, cudaStream_t s);
 void launch_face_flux_mixed(const Engine& E, cudaStream_t s);
+// discrete adjoint (adjoint.cu): buffers (allocated once, zeroed per call), the reverse
+// pass, and release
+int adjoint_buffers(Engine& E);
+int adjoint_launch(Engine& E);
+void adjoint_free(Engine& E);
 
 // host entry points implemented in setup.cu
 bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks);

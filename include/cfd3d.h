@@ -149,6 +149,17 @@ int  cfd3d_unsteady_shift(cfd3d_handle *h);
 int  cfd3d_residual(cfd3d_handle *h, int block, double *res, double *icav, double *itt,
                     double *omega_cut);
 
+/* Discrete adjoint of the FP64 residual: the vector-Jacobian product of R(pv), the
+ * residual of cfd3d_residual on the current state as a function of the interior pv of all
+ * blocks, with each interior cell's dv and tv(1:2) its EOS (as the update sets them) and
+ * the eddy viscosity tv(3) and the history qq held.  cot and g_state are res-shaped,
+ * (npv,2:imax,2:jmax,2:kmax) per block, blocks concatenated in order: g_state = (dR/dpv)^T cot.
+ * g_params[3] = cot . dR/d(uref, c_v, c_c), uref the free-stream speed at fixed angles and
+ * fixed k_inf / omega_inf.  Limiter, clip and flux switches are recomputed from the state;
+ * nothing is taped.  g_state and g_params may be NULL.  No counterpart in the reference:
+ * it serves gradient checks of the residual. */
+int  cfd3d_residual_vjp(cfd3d_handle *h, const double *cot, double *g_state, double *g_params);
+
 /* Grid metrics as the reference stores them: cx(3,1:imax,1:jmax+1,1:kmax+1),
  * ex(3,1:imax+1,1:jmax,1:kmax+1), tx(3,1:imax+1,1:jmax+1,1:kmax),
  * grd(ngrd,1:imax+1,1:jmax+1,1:kmax+1) (src/grid_module.f90:609-1241). */
