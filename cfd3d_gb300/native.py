@@ -51,6 +51,7 @@ def lib():
     L.cfd3d_unsteady_shift.argtypes = [H]
     L.cfd3d_residual.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_grid_metrics.argtypes = [H, C.c_int, dp, dp, dp, dp]
+    L.cfd3d_residual_vjp.argtypes = [H, dp, dp, dp]
     L.cfd3d_eos_eval.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
     L.cfd3d_eos_eval_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
     L.cfd3d_stats.argtypes = [H, C.POINTER(C.c_int64), ip]
@@ -63,7 +64,7 @@ def lib():
 
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
            "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_iterate", "cfd3d_iterate_n",
-           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
+           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device"]
 STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
 
@@ -178,6 +179,26 @@ class Engine:
         oc = np.zeros(abi.interior_shape(b, 1))
         self._check(lib().cfd3d_residual(self.h, n, _p(res), _p(icav), _p(itt), _p(oc)))
         return dict(res=res, icav=icav, itt=itt, omega_cut=oc[..., 0])
+
+    def residual_vjp(self, cot):
+        """Discrete adjoint of the FP64 residual on the current state.
+
+        cot: one residual-shaped array per block (interior_shape(block, npv)).  Returns
+        (g, g_params): g = (dR/dpv)^T cot per block, same shapes, and g_params =
+        cot . dR/d(uref, c_v, c_c)."""
+        blocks = self.case["blocks"]
+        shapes = [abi.interior_shape(b, self.npv) for b in blocks]
+        flat = np.concatenate([np.ascontiguousarray(c, dtype=np.float64).reshape(-1) for c in cot])
+        assert flat.size == sum(int(np.prod(s)) for s in shapes)
+        out = np.zeros_like(flat)
+        gpar = np.zeros(3)
+        self._check(lib().cfd3d_residual_vjp(self.h, _p(flat), _p(out), _p(gpar)))
+        g, off = [], 0
+        for s in shapes:
+            m = int(np.prod(s))
+            g.append(out[off:off + m].reshape(s))
+            off += m
+        return g, gpar
 
     def metrics(self, n):
         b = self.case["blocks"][n]
