@@ -266,6 +266,51 @@ def large(scale=1, seed=4, nt_phy=20, ntmax=30):
     return {"name": "large", "cfg": cfg, "blocks": [blk], "pv0": [pv], "iterations": nt_phy * ntmax}
 
 
+def split_i(case, nparts):
+    """The single-block case cut along i into nparts point-matched blocks (1-to-1
+    connections, identity transforms): the reference's decomposition of a block over
+    MPI ranks, one block per rank (what its CPU build runs on several cores)."""
+    assert len(case["blocks"]) == 1
+    b = case["blocks"][0]
+    imax = b["imax"]
+    ncells = imax - 1
+    nparts = max(1, min(nparts, ncells // 4))
+    cuts = [round(q * ncells / nparts) for q in range(nparts + 1)]
+    blocks, pv0 = [], []
+    J, K = b["jmax"], b["kmax"]
+    for q in range(nparts):
+        c0, c1 = cuts[q], cuts[q + 1]          # cells c0..c1-1 (0-based), nodes c0+1..c1+1
+        I = c1 - c0 + 1
+        xyz = b["xyz"][:, :, c0:c1 + 1, :].copy()
+        bc = []
+        for kind, pn in b["bc"]:
+            i1, j1, k1, i2, j2, k2 = pn
+            if i1 == i2:   # an i-face patch: the first or the last part
+                if i1 == 1 and q == 0:
+                    bc.append((kind, (1, j1, k1, 1, j2, k2)))
+                elif i1 == imax and q == nparts - 1:
+                    bc.append((kind, (I, j1, k1, I, j2, k2)))
+                continue
+            lo, hi = max(i1, c0 + 1), min(i2, c1 + 1)
+            if lo < hi:
+                bc.append((kind, (lo - c0, j1, k1, hi - c0, j2, k2)))
+        con = []
+        if q > 0:
+            nip = cuts[q] - cuts[q - 1] + 1
+            con.append({"donor": q - 1, "pnts": (1, 1, 1, 1, J, K), "pnts_donor": (nip, 1, 1, nip, J, K),
+                        "transform": (1, 2, 3)})
+        if q < nparts - 1:
+            con.append({"donor": q + 1, "pnts": (I, 1, 1, I, J, K), "pnts_donor": (1, 1, 1, 1, J, K),
+                        "transform": (1, 2, 3)})
+        blocks.append(_block(xyz, bc, con))
+        pv0.append(case["pv0"][0][:, :, c0:c1, :].copy())
+    out = dict(case)
+    out["blocks"] = blocks
+    out["pv0"] = pv0
+    out["name"] = f"{case['name']} in {nparts} blocks along i"
+    return out
+
+
 CASES = {"plain_small": plain_small, "cavitating": cavitating, "batched": batched, "adjoint": adjoint,
          "large": large}
 
