@@ -18,8 +18,8 @@ roofline   algorithmic bytes per cell-iteration (persisted pv/dv/tv, metrics, LU
            the measured HBM copy bandwidth; per-stage times come from an event-instrumented
            iteration.
 cpu_baseline  the CPU oracle (C++ FP64 restatement of the reference) on a bounded sample
-           of the same workload (the case at 1/4 resolution), single thread -- one block,
-           so one rank of the reference.
+           of the same workload (the case at 1/2 resolution), cut into one block per host
+           thread -- the reference's MPI decomposition, one rank per core.
 N > 1      replicas: one independent engine per GPU (the case does not shard without
            changing the block-Jacobi operator); barrier + max over ranks; value is the sum.
 """
@@ -114,38 +114,52 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_baseline(case_name, scale, precision_label, iters=1):
-    """Oracle throughput on a bounded sample (the case at 1/scale resolution)."""
+def host_threads():
+    """host cores this process may run on"""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_sample(case_name, scale, threads):
+    """The CPU oracle on the workload at 1/scale resolution, cut into `threads` blocks
+    along i and run one block per thread: the reference's MPI decomposition, one rank per
+    host core."""
     from cfd3d_gb300 import cases
     from oracle import oracle_py
-    c = cases.make(case_name, scale=scale, **({"fix_cav_clamp": 1} if case_name in ("cavitating",) else {}))
+    c = cases.make(case_name, scale=scale)
     c["cfg"]["fix_cav_clamp"] = 1
-    o = oracle_py.Oracle(c, threads=1)
+    if threads > 1 and len(c["blocks"]) == 1:
+        c = cases.split_i(c, threads)
+    nb = len(c["blocks"])
+    o = oracle_py.Oracle(c, threads=min(threads, nb))
     o.initialize(c["pv0"])
+    return o, cases.total_cells(c), nb
+
+
+def cpu_baseline(case_name, scale, threads, iters=2):
+    """Oracle throughput on a bounded sample of the same workload."""
+    o, ncell, nb = reference_sample(case_name, scale, threads)
     o.iterate(1, 1, 0.0)
     t0 = time.perf_counter()
     for it in range(iters):
         o.iterate(1, it + 2, 0.0)
     dt = time.perf_counter() - t0
-    ncell = cases.total_cells(c)
-    return {"value": ncell * iters / dt / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{case_name} at 1/{scale} resolution ({ncell} cells), {iters} pseudo-iteration(s), "
-                      f"CPU oracle single thread, {dt:.2f} s"}
+    return {"value": ncell * iters / dt / 1e6, "unit": UNIT, "cores": min(threads, nb), "kind": "port",
+            "sample": f"{case_name} at 1/{scale} resolution ({ncell} cells) in {nb} blocks, {iters} "
+                      f"pseudo-iterations, CPU oracle (C++ FP64 restatement of the reference), one block "
+                      f"per thread, {dt:.2f} s"}
 
 
 def run_reference(args):
-    """--impl reference: the reference's algorithm on the host cores (CPU oracle)."""
+    """--impl reference: the reference's algorithm on the host cores (CPU oracle), the
+    workload at 1/ref_scale resolution decomposed over all host threads."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from cfd3d_gb300 import cases
-    from oracle import oracle_py
-    scale = args.ref_scale
-    c = cases.make(args.case, scale=scale)
-    c["cfg"]["fix_cav_clamp"] = 1
-    o = oracle_py.Oracle(c, threads=1)
-    o.initialize(c["pv0"])
-    ncell = cases.total_cells(c)
+    threads = args.ref_threads or host_threads()
+    o, ncell, nb = reference_sample(args.case, args.ref_scale, threads)
     for w in range(args.warmup):
         o.iterate(1, w + 1, 0.0)
     t0 = time.perf_counter()
@@ -153,14 +167,17 @@ def run_reference(args):
         o.iterate(1, args.warmup + s + 1, 0.0)
     dt = time.perf_counter() - t0
     value = ncell * args.steps / dt / 1e6
+    cores = min(threads, nb)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.case} at 1/{scale} resolution ({ncell} cells)", "cells": ncell},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"{args.case} at 1/{scale} resolution, {args.steps} pseudo-iterations per run, "
-                                   "CPU oracle (C++ FP64 restatement), single thread = one reference rank"},
+        "config": {"workload": f"{args.case} at 1/{args.ref_scale} resolution ({ncell} cells) in {nb} blocks",
+                   "cells": ncell},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.case} at 1/{args.ref_scale} resolution, {nb} blocks along i, "
+                                   f"{args.steps} pseudo-iterations per run, CPU oracle (C++ FP64 restatement), "
+                                   f"one block per thread = one reference MPI rank per core"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -222,7 +239,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=5,
                     help="iterations of the plain FP64 form timed beside the mixed form (0 skips)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ref-scale", type=int, default=4)
+    ap.add_argument("--ref-scale", type=int, default=2,
+                    help="the CPU samples run the workload at 1/ref-scale resolution")
+    ap.add_argument("--ref-threads", type=int, default=0, help="host threads of the CPU samples (0: all)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -315,7 +334,7 @@ def main():
         line.update(fp64_form(case, res0, args.fp64_steps, ncell, ws))
         line["speedup_vs_fp64"] = value / line["fp64_form"]["value"]
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.case, args.ref_scale, args.precision)
+        line["cpu_baseline"] = cpu_baseline(args.case, args.ref_scale, args.ref_threads or host_threads())
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
