@@ -110,3 +110,18 @@ def test_replica_reduction_two_ranks_gloo():
     for rank, ms, value in got:
         assert ms == 20.0
         assert value == pytest.approx(2 * 1000 / 20.0 / 1e3)
+
+
+def test_split_i_decomposition():
+    c = cases.make("large", scale=16)
+    s = cases.split_i(c, 4)
+    assert len(s["blocks"]) == 4
+    assert cases.total_cells(s) == cases.total_cells(c)
+    assert np.array_equal(np.concatenate(s["pv0"], axis=2), c["pv0"][0])
+    # interface nodes are shared; far-field patches only on the outer i faces
+    for q, b in enumerate(s["blocks"]):
+        iface = [bc for bc in b["bc"] if bc[1][0] == bc[1][3]]
+        assert len(iface) == (1 if q in (0, 3) else 0)
+        assert len(b["con"]) == (1 if q in (0, 3) else 2)
+    for a, b in zip(s["blocks"][:-1], s["blocks"][1:]):
+        assert np.array_equal(a["xyz"][:, :, -1, :], b["xyz"][:, :, 0, :])
