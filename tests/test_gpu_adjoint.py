@@ -118,6 +118,7 @@ def test_vjp_state_against_fd_of_gpu_residual(c4):
     s = d["s"]
     entries = _entries(d["pv"].shape[:-1], d["pv"].shape[-1], 27, 1)
     used, errs, rows = _check(lambda p: s.residual([p])[0], d, entries)
+    print(f"GPU residual: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
     assert used >= len(entries) - 3, rows
     assert errs.max() <= TOL, (errs, rows)
 
@@ -147,6 +148,7 @@ def test_vjp_state_against_fd_of_oracle_residual(c4_small):
 
     entries = _entries(d["pv"].shape[:-1], d["pv"].shape[-1], 18, 2)
     used, errs, rows = _check(resid, d, entries)
+    print(f"oracle residual: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
     assert used >= len(entries) - 2, rows
     assert errs.max() <= TOL, (errs, rows)
 
@@ -168,6 +170,7 @@ def test_vjp_parameters_against_fd(c4_small):
             e2.close()
         fd = float(np.sum(lam * (r[0] - r[1])) / (2.0 * h))
         ga = d["gpar"][q]
+        print(f"d/d{name}: vjp {ga:.12e} fd {fd:.12e} relative error {abs(fd - ga) / max(abs(fd), abs(ga)):.2e}")
         assert abs(fd - ga) <= TOL * max(abs(fd), abs(ga)), (name, fd, ga)
 
 
