@@ -52,8 +52,10 @@ __global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
     if (c.nscheme == 2 || c.nscheme == 3) {
       // Roe-M and AUSMPW+ also read the face sound speeds
       double dl_[NDV], dr_[NDV];
-      deteos_simple<false>(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], dl_, &d.sc->snd2_fallbacks);
-      deteos_simple<false>(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], dr_, &d.sc->snd2_fallbacks);
+      deteos_simple<false>(c.fluid, L.pv[0] + c.pref, L.pv[4], L.pv[5], L.pv[6], dl_, &d.sc->snd2_fallbacks,
+                           L.pv[5] != 0.0);
+      deteos_simple<false>(c.fluid, R.pv[0] + c.pref, R.pv[4], R.pv[5], R.pv[6], dr_, &d.sc->snd2_fallbacks,
+                           R.pv[5] != 0.0);
       L.rho = dl_[0]; L.h = dl_[1]; L.c2 = dl_[5];
       R.rho = dr_[0]; R.h = dr_[1]; R.c2 = dr_[5];
     } else {

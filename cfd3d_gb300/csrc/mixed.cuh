@@ -34,7 +34,9 @@ __device__ __forceinline__ float eos_c2_f(int fluid, float p, float t, float y1,
     ideal_gas<float>(p, t, v);
   } else {
     iapws_l<float, true>(p, t, l);
-    iapws_v_meta<float, true>(p, t, p > h2o_pww<float>(t), v);
+    // without vapour every vapour term below carries the factor y1 = 0: skip its sums
+    if (y1 != 0.0f) iapws_v_meta<float, true>(p, t, p > h2o_pww<float>(t), v);
+    else { v.rho = 1.0f; v.h = 0.0f; v.drdp = 0.0f; v.drdt = 0.0f; v.dhdp = 0.0f; v.dhdt = 1.0f; }
   }
   ideal_gas<float>(p, t, g);
   float yl = 1.0f - y1 - y2;

@@ -116,14 +116,34 @@ __device__ __noinline__ void iapws_pair_df64(double p, double t, bool meta, Phas
   }
 }
 
+// the liquid phase alone (df64 sums): the face EOS of a face state without vapour
+template <bool FULL>
+__device__ __noinline__ void iapws_liq_df64(double p, double t, Phase<double>& l) {
+  Phase<df64> lx;
+  iapws_l<df64, FULL>(df64(p), df64(t), lx);
+  l.rho = (double)lx.rho; l.h = (double)lx.h;
+  if constexpr (FULL) { l.drdp = (double)lx.drdp; l.drdt = (double)lx.drdt; l.dhdp = (double)lx.dhdp; l.dhdt = (double)lx.dhdt; }
+}
+
 // Phase properties of liquid and vapour.  MX evaluates the IF97 Gibbs sums in df64 (the
 // mixed form); FULL = false evaluates only rho and h.  The metastable branch test
 // p > p_sat(T) is taken in FP64 in both forms so that they select the same term set.
+// vap = false (a state without vapour, y1 = 0, whose caller needs only the mixture's rho,
+// h or c2): every vapour term of the mixture carries the factor y1 = 0, so the vapour sums
+// (the larger half of the work) are skipped and a neutral vapour phase returned; the
+// mixture's rho, h and c2 come out the same.
 template <bool MX, bool FULL>
-__device__ __forceinline__ void phases(int fluid, double p, double t, Phase<double>& l, Phase<double>& v) {
+__device__ __forceinline__ void phases(int fluid, double p, double t, Phase<double>& l, Phase<double>& v,
+                                       bool vap = true) {
   if (fluid == 1) {
     stiffened(p, t, l);
     ideal_gas(p, t, v);
+    return;
+  }
+  if (!vap) {
+    if constexpr (MX) iapws_liq_df64<FULL>(p, t, l);
+    else iapws_l<double, FULL>(p, t, l);
+    v.rho = 1.0; v.h = 0.0; v.drdp = 0.0; v.drdt = 0.0; v.dhdp = 0.0; v.dhdt = 1.0;
     return;
   }
   const bool meta = p > h2o_pww(t);
@@ -202,11 +222,12 @@ __device__ __forceinline__ void deteos_t(int fluid, int with_prop, T p, T t, T y
 }
 
 // eos%deteos_simple
+// (vap = false: the caller reads only dv(1), dv(2), dv(6) of a state with y1 = 0; see phases)
 template <bool MX = false>
 __device__ __forceinline__ void deteos_simple(int fluid, double p, double t, double y1, double y2, double* dv,
-                                              unsigned long long* fb) {
+                                              unsigned long long* fb, bool vap = true) {
   Phase<double> l, v, g;
-  phases<MX, true>(fluid, p, t, l, v);
+  phases<MX, true>(fluid, p, t, l, v, vap);
   ideal_gas(p, t, g);
   mixture(l, v, g, y1, y2, dv, fb);
 }
@@ -216,7 +237,7 @@ __device__ __forceinline__ void deteos_simple(int fluid, double p, double t, dou
 template <bool MX = false>
 __device__ __forceinline__ void eos_rho_h(int fluid, double p, double t, double y1, double y2, double& rho, double& h) {
   Phase<double> l, v, g;
-  phases<MX, false>(fluid, p, t, l, v);
+  phases<MX, false>(fluid, p, t, l, v, y1 != 0.0);
   ideal_gas(p, t, g);
   double irhol = 1.0 / l.rho, irhov = 1.0 / v.rho, irhog = 1.0 / g.rho;
   double yl = 1.0 - y1 - y2;
@@ -610,7 +631,7 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
   double ravg[NPVM];
   roe_state<double>(npv, L, Rs, ravg);
   double rdv[NDV];
-  deteos_simple<MX>(c.fluid, ravg[0] + c.pref, ravg[4], ravg[5], ravg[6], rdv, fb);
+  deteos_simple<MX>(c.fluid, ravg[0] + c.pref, ravg[4], ravg[5], ravg[6], rdv, fb, ravg[5] != 0.0);
   inviscid_flux_core<double>(c, n, L, Rs, sdst_in, ravg, rdv[5], c.uref * c.uref, fx);
 }
 
