@@ -23,6 +23,7 @@
 #include <mutex>
 #include <new>
 #include "engine.cuh"
+#include "mixed.cuh"
 
 namespace cfd {
 
@@ -336,39 +337,78 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
       fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
     }
     const int gv[5] = {1, 2, 3, 7, 8};
-    double gr[5][3];
-    double ivol = 1.0 / vol;
-    for (int q = 0; q < 5; ++q) {
-      const double* P = d.pv + gv[q] * n;
-      double c0 = P[g];
-      double v1 = 0.5 * (P[nbr[0]] + c0), v2 = 0.5 * (P[nbr[1]] + c0), v3 = 0.5 * (P[nbr[2]] + c0);
-      double v4 = 0.5 * (P[nbr[3]] + c0), v5 = 0.5 * (P[nbr[4]] + c0), v6 = 0.5 * (P[nbr[5]] + c0);
-      for (int e = 0; e < 3; ++e)
-        gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
-    }
     double tv[3];
     for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
     const double c23 = 2.0 / 3.0;
     const double kk = pv2[7], oo = pv2[8];
     const double y5 = d.gm[(GM_GRD + 4) * n + g];
-    const SstOut<double> so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol);
+    SstOut<double> so;
+    if (MX) {
+      // FP32 on the gauge shadow: differences of u - U are exact where u's are not
+      float grf[5][3];
+      const float ivf = (float)(1.0 / vol);
+      for (int q = 0; q < 5; ++q) {
+        const float* P = d.pvf + gv[q] * n;
+        const float c0 = P[g];
+        float vv[6];
+        for (int m = 0; m < 6; ++m) vv[m] = 0.5f * (P[nbr[m]] + c0);
+        for (int e = 0; e < 3; ++e)
+          grf[q][e] = (vv[1] * (float)fa[1][e] + vv[3] * (float)fa[3][e] + vv[5] * (float)fa[5][e] -
+                       vv[0] * (float)fa[0][e] - vv[2] * (float)fa[2][e] - vv[4] * (float)fa[4][e]) * ivf;
+      }
+      const SstOut<float> sf = sst_source_f(grf, (float)kk, (float)oo, (float)dv[0], (float)tv[0], (float)tv[2],
+                                            (float)y5, (float)vol);
+      so.r7 = sf.r7; so.r8 = sf.r8; so.prod = sf.prod; so.dest = sf.dest; so.div = sf.div; so.pkw = sf.pkw;
+      so.bigf = sf.bigf; so.talpha = sf.talpha; so.tbeta = sf.tbeta; so.strain = sf.strain;
+    } else {
+      double gr[5][3];
+      double ivol = 1.0 / vol;
+      for (int q = 0; q < 5; ++q) {
+        const double* P = d.pv + gv[q] * n;
+        double c0 = P[g];
+        double v1 = 0.5 * (P[nbr[0]] + c0), v2 = 0.5 * (P[nbr[1]] + c0), v3 = 0.5 * (P[nbr[2]] + c0);
+        double v4 = 0.5 * (P[nbr[3]] + c0), v5 = 0.5 * (P[nbr[4]] + c0), v6 = 0.5 * (P[nbr[5]] + c0);
+        for (int e = 0; e < 3; ++e)
+          gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
+      }
+      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol);
+    }
     res[7] = res[7] + so.r7;
     res[8] = res[8] + so.r8;
-    d.ocut[g] = sqrt(so.strain - c23 * so.div * so.div);
     const double prod = so.prod, dest = so.dest, div = so.div, pkw = so.pkw, bigf = so.bigf;
     const double talpha = so.talpha, tbeta = so.tbeta;
-    const double ki = 1.0 / kk, oi = 1.0 / oo, ei = 1.0 / tv[2];
-    double dpdk = prod * ki;
-    double dpdo = -((prod + c23 * dv[0] * kk * div) * oi);
-    double it0 = dpdk - dest * ki, it1 = dpdo - dest * oi, it2 = 0.0;
-    double it3 = talpha * dv[0] * ei * dpdo + talpha * dv[0] * ei * prod * oi - 2.0 * tbeta * dv[0] * oo -
-                 1.712 * (1.0 - bigf) * dv[0] * oi * oi * pkw;
-    double tr = it0 + it3, de = it0 * it3 - it1 * it2;
-    double sd = sqrt(fmax(0.25 * tr * tr - de, 0.0));
-    double l1 = copysign(1.0, 0.5 * tr + sd), l2 = copysign(1.0, 0.5 * tr - sd);
-    double f1 = (1.0 - 0.5 * (1.0 - l1)) - 0.5 * (1.0 - l1);
-    double f2 = (1.0 - 0.5 * (1.0 - l2)) - 0.5 * (1.0 - l2);
-    d.itt[g] = it0 * f1; d.itt[n + g] = it1 * f1; d.itt[2 * n + g] = it2 * f2; d.itt[3 * n + g] = it3 * f2;
+    if (MX) {
+      // the implicit coefficients and the omega bound of the update: FP32
+      const float pf = (float)prod, df_ = (float)dest, dvf = (float)div, pkf = (float)pkw, bf = (float)bigf;
+      const float taf = (float)talpha, tbf = (float)tbeta, rho = (float)dv[0], kf = (float)kk, of = (float)oo;
+      d.ocut[g] = (double)sqrtf((float)so.strain - (2.0f / 3.0f) * dvf * dvf);
+      const float ki = 1.0f / kf, oi = 1.0f / of, ei = 1.0f / (float)tv[2];
+      const float dpdk = pf * ki;
+      const float dpdo = -((pf + (2.0f / 3.0f) * rho * kf * dvf) * oi);
+      const float it0 = dpdk - df_ * ki, it1 = dpdo - df_ * oi, it2 = 0.0f;
+      const float it3 = taf * rho * ei * dpdo + taf * rho * ei * pf * oi - 2.0f * tbf * rho * of -
+                        1.712f * (1.0f - bf) * rho * oi * oi * pkf;
+      const float tr = it0 + it3, de = it0 * it3 - it1 * it2;
+      const float sd = sqrtf(fmaxf(0.25f * tr * tr - de, 0.0f));
+      const float l1 = copysignf(1.0f, 0.5f * tr + sd), l2 = copysignf(1.0f, 0.5f * tr - sd);
+      const float f1 = (1.0f - 0.5f * (1.0f - l1)) - 0.5f * (1.0f - l1);
+      const float f2 = (1.0f - 0.5f * (1.0f - l2)) - 0.5f * (1.0f - l2);
+      d.itt[g] = it0 * f1; d.itt[n + g] = it1 * f1; d.itt[2 * n + g] = it2 * f2; d.itt[3 * n + g] = it3 * f2;
+    } else {
+      d.ocut[g] = sqrt(so.strain - c23 * so.div * so.div);
+      const double ki = 1.0 / kk, oi = 1.0 / oo, ei = 1.0 / tv[2];
+      double dpdk = prod * ki;
+      double dpdo = -((prod + c23 * dv[0] * kk * div) * oi);
+      double it0 = dpdk - dest * ki, it1 = dpdo - dest * oi, it2 = 0.0;
+      double it3 = talpha * dv[0] * ei * dpdo + talpha * dv[0] * ei * prod * oi - 2.0 * tbeta * dv[0] * oo -
+                   1.712 * (1.0 - bigf) * dv[0] * oi * oi * pkw;
+      double tr = it0 + it3, de = it0 * it3 - it1 * it2;
+      double sd = sqrt(fmax(0.25 * tr * tr - de, 0.0));
+      double l1 = copysign(1.0, 0.5 * tr + sd), l2 = copysign(1.0, 0.5 * tr - sd);
+      double f1 = (1.0 - 0.5 * (1.0 - l1)) - 0.5 * (1.0 - l1);
+      double f2 = (1.0 - 0.5 * (1.0 - l2)) - 0.5 * (1.0 - l2);
+      d.itt[g] = it0 * f1; d.itt[n + g] = it1 * f1; d.itt[2 * n + g] = it2 * f2; d.itt[3 * n + g] = it3 * f2;
+    }
   }
   if (c.nsteady >= 1) {
     double bb = (c.nsteady == 1) ? 1.0 : 0.75;

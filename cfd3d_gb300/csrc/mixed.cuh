@@ -58,6 +58,38 @@ __device__ __forceinline__ float eos_c2_f(int fluid, float p, float t, float y1,
   return c2;
 }
 
+// ------------------------------------------------------------------ SST source
+// sst_source (physics.cuh) in FP32, for the mixed form: its terms are a part of the k and
+// omega residuals and of their implicit coefficients, which an FP32 evaluation gives to
+// about 1e-6 relative.  Same formulas and order.
+__device__ __forceinline__ SstOut<float> sst_source_f(const float (*gr)[3], float kk, float oo, float rho, float mu,
+                                                      float mut, float y5, float vol) {
+  const float c23 = 2.0f / 3.0f, c59 = 5.0f / 9.0f;
+  SstOut<float> o;
+  float dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
+  float dvdx = gr[1][0], dvdy = gr[1][1], dvdz = gr[1][2];
+  float dwdx = gr[2][0], dwdy = gr[2][1], dwdz = gr[2][2];
+  o.strain = 2.0f * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + sq(dudy + dvdx) + sq(dudz + dwdx) + sq(dvdz + dwdy);
+  o.div = dudx + dvdy + dwdz;
+  float prod = mut * (o.strain - c23 * o.div * o.div) - c23 * rho * kk * o.div;
+  o.prod = fminf(prod, 0.9f * rho * kk * oo);
+  o.pkw = gr[3][0] * gr[4][0] + gr[3][1] * gr[4][1] + gr[3][2] * gr[4][2];
+  float cdkw = fmaxf(1.712f * rho / oo * o.pkw, 1.0e-10f);
+  float term1 = sqrtf(kk) / (0.09f * oo * y5);
+  float term2 = 500.0f * mu / rho / (oo * y5 * y5);
+  float term3 = (3.424f * rho * kk) / (cdkw * y5 * y5);
+  float arg1 = fminf(fmaxf(term1, term2), term3);
+  float a2 = arg1 * arg1;
+  o.bigf = tanhf(a2 * a2);
+  o.talpha = o.bigf * c59 + (1.0f - o.bigf) * 0.44f;
+  o.tbeta = o.bigf * 0.075f + (1.0f - o.bigf) * 0.0828f;
+  float tl = sqrtf(kk) / 9.0f / oo * 100.0f;
+  o.dest = rho * kk * sqrtf(kk) / tl;
+  o.r7 = (o.prod - o.dest) * vol;
+  o.r8 = (o.talpha * rho * (1.0f / mut) * o.prod - o.tbeta * rho * oo * oo + 1.712f * (1.0f - o.bigf) * rho * (1.0f / oo) * o.pkw) * vol;
+  return o;
+}
+
 // ------------------------------------------------------------------ reconstruction clips
 // muscl_clip for the FP32 reconstruction.  Where the MLP factor is exactly 2 the
 // reconstructed y1 (or y2) equals a neighbour's value, typically exactly 0 at the edge of a

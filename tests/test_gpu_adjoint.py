@@ -4,7 +4,7 @@ R(pv) is the FP64 residual with each interior cell's dv and tv(1:2) its EOS and 
 viscosity tv(3) and history held (cfd3d_gb300.adjoint.StateSetter).  The state is the
 cavitating SST block of cases.adjoint (pressure, velocity and vapour fraction noisy) with
 noise added to T, y2, k and omega as well, so that no limiter, min / max or clip sits on
-a tie.  Checks, each at <= 1e-6 relative:
+a tie, and a band of cells below the vapour pressure, where vaporisation is active.  Checks, each at <= 1e-6 relative:
   * entries of (dR/dpv)^T lambda at cells across the block (boundary rows included)
     against lambda . (R(pv + h e) - R(pv - h e)) / 2h of the GPU residual, h = 1e-6 |x|;
   * the same against the oracle's residual (CPU restatement of the reference);
@@ -31,6 +31,10 @@ def _state(scale, seed=11):
     sh = pv.shape[:-1]
     pv[..., 4] = 300.0 + rng.normal(0.0, 0.05, size=sh)
     pv[..., 6] = 1e-7 * (1.0 + 0.1 * rng.normal(size=sh))
+    # a band of cells below the vapour pressure, so that vaporisation (and its c_v) is active
+    band = pv[..., 4].copy()[:, :, : max(sh[2] // 8, 2)]
+    pv[:, :, : band.shape[2], 0] = (cases.pww_iapws(band) * (0.9 + 0.02 * rng.normal(size=band.shape))
+                                    - c["cfg"]["pref"])
     pv[..., 7] *= 1.0 + 0.05 * rng.normal(size=sh)
     pv[..., 8] *= 1.0 + 0.05 * rng.normal(size=sh)
     c["pv0"] = [pv]
@@ -170,6 +174,7 @@ def test_vjp_parameters_against_fd(c4_small):
             e2.close()
         fd = float(np.sum(lam * (r[0] - r[1])) / (2.0 * h))
         ga = d["gpar"][q]
+        assert ga != 0.0, name
         print(f"d/d{name}: vjp {ga:.12e} fd {fd:.12e} relative error {abs(fd - ga) / max(abs(fd), abs(ga)):.2e}")
         assert abs(fd - ga) <= TOL * max(abs(fd), abs(ga)), (name, fd, ga)
 
