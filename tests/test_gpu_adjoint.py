@@ -33,7 +33,7 @@ def _state(scale, seed=11):
     pv[..., 6] = 1e-7 * (1.0 + 0.1 * rng.normal(size=sh))
     # a band of cells below the vapour pressure, so that vaporisation (and its c_v) is active
     band = pv[..., 4].copy()[:, :, : max(sh[2] // 8, 2)]
-    pv[:, :, : band.shape[2], 0] = (cases.pww_iapws(band) * (0.9 + 0.02 * rng.normal(size=band.shape))
+    pv[:, :, : band.shape[2], 0] = (np.vectorize(cases.pww_iapws)(band) * (0.9 + 0.02 * rng.normal(size=band.shape))
                                     - c["cfg"]["pref"])
     pv[..., 7] *= 1.0 + 0.05 * rng.normal(size=sh)
     pv[..., 8] *= 1.0 + 0.05 * rng.normal(size=sh)
