@@ -26,6 +26,9 @@ TOL = 1e-6
 
 def _state(scale, seed=11):
     c = cases.adjoint(scale=scale)
+    # the intended cavitation clamp: with the reference's (temperature-indexed) clamp the
+    # vaporisation rate is its clamp value and does not depend on c_v
+    c["cfg"]["fix_cav_clamp"] = 1
     rng = np.random.default_rng(seed)
     pv = c["pv0"][0].copy()
     sh = pv.shape[:-1]
