@@ -4,7 +4,7 @@ R(pv) is the FP64 residual with each interior cell's dv and tv(1:2) its EOS and 
 viscosity tv(3) and history held (cfd3d_gb300.adjoint.StateSetter).  The state is the
 cavitating SST block of cases.adjoint (pressure, velocity and vapour fraction noisy) with
 noise added to T, y2, k and omega as well, so that no limiter, min / max or clip sits on
-a tie, and a band of cells below the vapour pressure, where vaporisation is active.  Checks, each at <= 1e-6 relative:
+a tie, and a band of cells just below the vapour pressure, where vaporisation is active.  Checks, each at <= 1e-6 relative:
   * entries of (dR/dpv)^T lambda at cells across the block (boundary rows included)
     against lambda . (R(pv + h e) - R(pv - h e)) / 2h of the GPU residual, h = 1e-6 |x|;
   * the same against the oracle's residual (CPU restatement of the reference);
@@ -34,10 +34,11 @@ def _state(scale, seed=11):
     sh = pv.shape[:-1]
     pv[..., 4] = 300.0 + rng.normal(0.0, 0.05, size=sh)
     pv[..., 6] = 1e-7 * (1.0 + 0.1 * rng.normal(size=sh))
-    # a band of cells below the vapour pressure, so that vaporisation (and its c_v) is active
+    # a band of cells 0.2-0.8 % below the vapour pressure: vaporisation is active there and
+    # below its clamp, so that it depends on c_v
     band = pv[..., 4].copy()[:, :, : max(sh[2] // 8, 2)]
-    pv[:, :, : band.shape[2], 0] = (np.vectorize(cases.pww_iapws)(band) * (0.9 + 0.02 * rng.normal(size=band.shape))
-                                    - c["cfg"]["pref"])
+    deficit = 0.002 + 0.006 * rng.random(size=band.shape)
+    pv[:, :, : band.shape[2], 0] = np.vectorize(cases.pww_iapws)(band) * (1.0 - deficit) - c["cfg"]["pref"]
     pv[..., 7] *= 1.0 + 0.05 * rng.normal(size=sh)
     pv[..., 8] *= 1.0 + 0.05 * rng.normal(size=sh)
     c["pv0"] = [pv]
