@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -493,7 +494,7 @@ __device__ __forceinline__ void rec_state(const T* R, long long nint, long long 
 }
 
 // the three lower (forward) or upper (backward) neighbours' products, added to acc
-template <bool FWD, class T>
+template <bool FWD, class T, bool CG = false>
 __device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long long t, const T* R, const T* dqs,
                                                  T* acc) {
   const long long nint = d.nint;
@@ -507,7 +508,8 @@ __device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long 
     T nx[3], pv[NPVM], dv[14], dq[NPVM];
     for (int e = 0; e < 3; ++e) nx[e] = R[(REC_FACE + 3 * q + e) * nint + fr];
     rec_state<T>(R, nint, nb, pv, dv);
-    for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? dqs[v * nint + nb] : T(0);
+    // the dataflow sweep reads dq written during this launch by other CTAs: from L2 (CG)
+    for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? (CG ? __ldcg(dqs + v * nint + nb) : dqs[v * nint + nb]) : T(0);
     const T spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + nb];
     const T beta = R[REC_BETA * nint + nb];
     const T evv = R[REC_EVV * nint + nb];
@@ -515,10 +517,9 @@ __device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long 
   }
 }
 
-template <bool FWD, bool MX>
-__global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, long long p1) {
-  const long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= p1) return;
+// one cell of a sweep: its three neighbours' products, the closed-form D^-1, dq
+template <bool FWD, bool MX, bool CG>
+__device__ __forceinline__ void sweep_cell(const DevPtr& d, const Par& c, long long t) {
   const long long nint = d.nint;
   const double* R = d.rec;
   const int npv = c.npv;
@@ -529,10 +530,10 @@ __global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, lon
   if (MX) {
     float an[NPVM];
     for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
-    sweep_neighbours<FWD, float>(d, npv, t, d.recf, d.dqsf, an);
+    sweep_neighbours<FWD, float, CG>(d, npv, t, d.recf, d.dqsf, an);
     for (int v = 0; v < npv; ++v) acc[v] += (double)an[v];
   } else {
-    sweep_neighbours<FWD, double>(d, npv, t, R, d.dqs, acc);
+    sweep_neighbours<FWD, double, CG>(d, npv, t, R, d.dqs, acc);
   }
   if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
   double pv[NPVM], dv[14], o[PREP_DIAG];
@@ -545,6 +546,56 @@ __global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, lon
   diag_solve(c, D, pv, dv, acc, x);
   for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
   if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
+}
+
+// one launch per hyperplane
+template <bool FWD, bool MX>
+__global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, long long p1) {
+  const long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= p1) return;
+  sweep_cell<FWD, MX, false>(d, c, t);
+}
+
+// Dataflow sweep: one persistent launch per sweep.  CTAs take chunks (runs of at most
+// SW_CH cells of one plane) in plane order -- reversed for the backward sweep -- from a
+// ticket counter.  A cell waits for the done flags of its three lower (upper) neighbours,
+// which belong to earlier tickets, runs the hyperplane kernel's arithmetic and raises its own
+// flag.  Ticket order keeps the waits finite: the earliest unfinished chunk has all its
+// dependencies done, and its CTA is running.  Every wait is bounded by `spin` polls; a wait
+// that runs out records sweep_stall, which also ends every other wait, so the launch
+// completes and the host reports CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose
+// flags are never raised (the stall test).
+template <bool FWD, bool MX>
+__global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long spin, int withhold) {
+  __shared__ int s_q;
+  const long long nint = d.nint;
+  unsigned* ticket = d.tickets + (FWD ? 0 : 1);
+  for (;;) {
+    if (threadIdx.x == 0) s_q = (int)atomicAdd(ticket, 1u);
+    __syncthreads();
+    const int q = s_q;
+    __syncthreads();
+    if (q >= d.nchunk) return;
+    const int ch = FWD ? q : d.nchunk - 1 - q;
+    const long long t = d.chunk_t0[ch] + threadIdx.x;
+    if (t >= d.chunk_t0[ch + 1]) continue;
+    for (int k = 0; k < 3; ++k) {
+      const int nb = FWD ? d.nbf[k * nint + t] : d.nbb[k * nint + t];
+      if (nb < 0) continue;
+      const volatile int* f = d.done + nb;
+      long long it = 0;
+      while (*f == 0) {
+        ++it;
+        if ((it & 255) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
+        if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    sweep_cell<FWD, MX, true>(d, c, t);
+    __threadfence();
+    if (ch != withhold) atomicExch(d.done + t, 1);
+  }
 }
 
 // ------------------------------------------------------------------ update + residual
@@ -764,6 +815,9 @@ int ensure_staging(cfd3d_handle* h, size_t bytes) {
   return CFD3D_OK;
 }
 
+// polls of a neighbour's done flag before a dataflow sweep gives up (about 0.1-0.5 s)
+constexpr long long SWEEP_SPIN = 1ll << 22;
+
 // the launch sequence of one iteration (captured into the graph); `mark` (optional)
 // records an event after each stage for the stage profile
 void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
@@ -787,6 +841,18 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   stage(4);
   n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
+  if (!E.sweep_planes) {
+    // dataflow sweeps: flags and tickets cleared, one persistent launch per sweep
+    cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), s);
+    cudaMemsetAsync(d.done, 0, (size_t)E.nint * sizeof(int), s);
+    if (c.mixed) k_sweep_df<true, true><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
+    else k_sweep_df<true, false><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
+    stage(5);
+    cudaMemsetAsync(d.done, 0, (size_t)E.nint * sizeof(int), s);
+    if (c.mixed) k_sweep_df<false, true><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
+    else k_sweep_df<false, false><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
+    n += 2;
+  } else {
   const int np = (int)E.plane_off.size() - 1;
   const int TS = 64;
   for (int q = 0; q < np; ++q) {
@@ -805,6 +871,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
       else k_sweep<false, false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
       ++n;
     }
+  }
   }
   stage(6);
   if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c);
@@ -1069,6 +1136,21 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   E.d.cells = E.d_planes; E.d.pos = E.d_pos; E.d.nbf = E.d_nbf; E.d.nbb = E.d_nbb;
   if (!E.d_planes || !E.d_pos || !E.d_nbf || !E.d_nbb) { E.err = "device allocation failed (sweep maps)"; return CFD3D_ERR_NOMEM; }
   if (cudaMalloc(&E.d.rec, (size_t)NREC * E.nint * 8) != cudaSuccess) { E.err = "device allocation failed (sweep records)"; return CFD3D_ERR_NOMEM; }
+  if (cudaMalloc(&E.d.done, (size_t)E.nint * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&E.d.tickets, 2 * sizeof(unsigned)) != cudaSuccess) {
+    E.err = "device allocation failed (sweep flags)";
+    return CFD3D_ERR_NOMEM;
+  }
+  {
+    const char* mode = std::getenv("CFD3D_SWEEP");
+    E.sweep_planes = (mode && std::strcmp(mode, "planes") == 0) ? 1 : 0;
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, true>, SW_CH, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, false>, SW_CH, 0);
+    E.sweep_grid = std::max(1, std::min(per * nsm, E.d.nchunk));
+  }
   if (c.mixed && (cudaMalloc(&E.d.recf, (size_t)REC_DIAG * E.nint * 4) != cudaSuccess ||
                   cudaMalloc(&E.d.dqsf, (size_t)c.npv * E.nint * 4) != cudaSuccess)) {
     E.err = "device allocation failed (sweep records)";
@@ -1095,6 +1177,9 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_nbf);
   cudaFree(E.d_nbb);
   cudaFree(E.d.rec);
+  cudaFree(E.d.done);
+  cudaFree(E.d.tickets);
+  cudaFree(E.d_chunk_t0);
   cudaFree(E.d.recf);
   cudaFree(E.d.dqsf);
   adjoint_free(E);
@@ -1224,6 +1309,12 @@ static int finish_iteration(cfd3d_handle* h, int nt_phy, double timeprev, double
       loc[0] = b; loc[1] = (int)(l % ni) + 2; loc[2] = (int)((l / ni) % nj) + 2; loc[3] = (int)(l / ((long long)ni * nj)) + 2;
     }
   }
+  if (s.sweep_stall) {
+    E.err = "a dataflow sweep's wait for a neighbour cell ran out";
+    int zero = 0;
+    cudaMemcpy(&E.d.sc->sweep_stall, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    return CFD3D_ERR_TIMEOUT;
+  }
   if (s.nonfinite) {
     E.err = "non-finite value in the updated state";
     int zero = 0;
@@ -1322,6 +1413,30 @@ int cfd3d_residual_vjp(cfd3d_handle* h, const double* cot, double* g_state, doub
     CFD_CUDA(cudaStreamSynchronize(E.st));
   }
   return CFD3D_OK;
+}
+
+int cfd3d_sweep_stall_test(cfd3d_handle* h) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  const DevPtr& d = E.d;
+  const Par& c = E.par;
+  // fresh sweep records of the current state, then a forward sweep whose first chunk never
+  // raises its flags, with a short poll limit
+  launch_iteration(E, false);
+  CFD_CUDA(cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), E.st));
+  CFD_CUDA(cudaMemsetAsync(d.done, 0, (size_t)E.nint * sizeof(int), E.st));
+  if (c.mixed) k_sweep_df<true, true><<<E.sweep_grid, SW_CH, 0, E.st>>>(d, c, 1 << 12, 0);
+  else k_sweep_df<true, false><<<E.sweep_grid, SW_CH, 0, E.st>>>(d, c, 1 << 12, 0);
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  Scalars sc;
+  int rc = read_scalars(E, sc);
+  if (rc) return rc;
+  if (!sc.sweep_stall) { E.err = "the withheld flags did not stop the sweep's waits"; return CFD3D_OK; }
+  int zero = 0;
+  CFD_CUDA(cudaMemcpy(&E.d.sc->sweep_stall, &zero, sizeof(int), cudaMemcpyHostToDevice));
+  E.err = "a dataflow sweep's wait for a neighbour cell ran out";
+  return CFD3D_ERR_TIMEOUT;
 }
 
 int cfd3d_grid_metrics(cfd3d_handle* h, int block, double* cx, double* ex, double* tx, double* grd) {

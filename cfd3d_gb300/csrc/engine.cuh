@@ -56,7 +56,7 @@ struct Scalars {
   long long resmax_cell;
   unsigned long long snd2_fallbacks;
   int nonfinite;
-  int pad;
+  int sweep_stall;   // a dataflow sweep's wait for a neighbour ran out (the sweep went on)
 };
 
 struct DevPtr {
@@ -74,6 +74,12 @@ struct DevPtr {
   // dcv are plane-major too
   double* rec;
   const int *cells, *pos, *nbf, *nbb;
+  // dataflow sweeps: chunk starts in t (chunks of at most SW_CH cells, never across a
+  // plane; nchunk + 1 entries), per-cell done flags, the two sweeps' chunk tickets
+  const int* chunk_t0;
+  int nchunk;
+  int* done;
+  unsigned* tickets;
   // mixed form: FP32 copy of the neighbour part of the records (the first REC_DIAG
   // planes) and FP32 dq
   float *recf, *dqsf;
@@ -107,6 +113,9 @@ struct Engine {
   int* d_nbf = nullptr;
   int* d_nbb = nullptr;
   std::vector<long long> plane_off;
+  int* d_chunk_t0 = nullptr;   // dataflow sweep chunks (setup_planes)
+  int sweep_grid = 0;          // persistent CTAs of the dataflow sweep
+  int sweep_planes = 0;        // 1: one launch per hyperplane instead (CFD3D_SWEEP=planes)
   cudaStream_t st = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_ready = 0;
@@ -162,6 +171,9 @@ __device__ __forceinline__ long long stencil_cell(int l, long long g, long long 
   return g + ((l == 36) ? -2 : 3) * sn;
 }
 
+
+// cells per chunk of the dataflow sweeps (one CTA's work item)
+constexpr int SW_CH = 64;
 
 // face-flux launchers (flux.cu: FP64 form; flux_mixed.cu: mixed form)
 void launch_face_flux(const Engine& E, cudaStream_t s);

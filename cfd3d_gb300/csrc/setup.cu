@@ -695,6 +695,15 @@ void setup_planes(Engine& E) {
           }
         }
   }
+  // chunks of the dataflow sweeps: each plane cut into runs of at most SW_CH cells
+  std::vector<int> chunks;
+  for (long long s = 0; s + 1 < (long long)E.plane_off.size(); ++s)
+    for (long long t = E.plane_off[s]; t < E.plane_off[s + 1]; t += SW_CH) chunks.push_back((int)t);
+  E.d.nchunk = (int)chunks.size();
+  chunks.push_back((int)nint);
+  cudaMalloc(&E.d_chunk_t0, chunks.size() * sizeof(int));
+  cudaMemcpy(E.d_chunk_t0, chunks.data(), chunks.size() * sizeof(int), cudaMemcpyHostToDevice);
+  E.d.chunk_t0 = E.d_chunk_t0;
   cudaMalloc(&E.d_planes, nint * sizeof(int));
   cudaMemcpy(E.d_planes, cells.data(), nint * sizeof(int), cudaMemcpyHostToDevice);
   cudaMalloc(&E.d_pos, E.ncell * sizeof(int));

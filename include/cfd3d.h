@@ -160,6 +160,13 @@ int  cfd3d_residual(cfd3d_handle *h, int block, double *res, double *icav, doubl
  * it serves gradient checks of the residual. */
 int  cfd3d_residual_vjp(cfd3d_handle *h, const double *cot, double *g_state, double *g_params);
 
+/* Test hook of the dataflow sweeps' bounded waits (no counterpart in the reference): one
+ * forward sweep on the current state's records in which the first chunk of cells never
+ * signals completion, with a short wait limit.  The cells that depend on it give up
+ * waiting, the launch completes and the call returns CFD3D_ERR_TIMEOUT with the device
+ * context intact; the state is not updated. */
+int  cfd3d_sweep_stall_test(cfd3d_handle *h);
+
 /* Grid metrics as the reference stores them: cx(3,1:imax,1:jmax+1,1:kmax+1),
  * ex(3,1:imax+1,1:jmax,1:kmax+1), tx(3,1:imax+1,1:jmax+1,1:kmax),
  * grd(ngrd,1:imax+1,1:jmax+1,1:kmax+1) (src/grid_module.f90:609-1241). */

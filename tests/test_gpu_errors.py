@@ -35,3 +35,35 @@ def test_block_index_out_of_range():
     assert lib.cfd3d_download_state(e.h, -1, None, None, None, None, None) == abi.ERR_ARG
     assert b"block" in lib.cfd3d_last_error(e.h)
     e.residual(0)   # still usable
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_sweep_wait_runs_out_and_the_handle_recovers(precision):
+    """A dataflow sweep in which one chunk of cells never signals: its dependents' bounded
+    waits run out, the launch completes and the host gets CFD3D_ERR_TIMEOUT; the next
+    iteration is normal."""
+    c = cases.make("cavitating", scale=8, fix_cav_clamp=1)
+    e = native.Engine(c, precision=precision)
+    e.initialize(c["pv0"])
+    assert e.sweep_stall_test() == abi.ERR_TIMEOUT
+    e.initialize(c["pv0"])
+    _, res, _ = e.iterate(1, 1, 0.0)
+    assert np.all(np.isfinite(res))
+
+
+def test_dataflow_sweeps_equal_hyperplane_sweeps(monkeypatch):
+    """The dataflow sweeps run each cell's arithmetic on the same inputs as the one-launch-
+    per-hyperplane sweeps: the FP64 states agree bit for bit."""
+    c = cases.make("batched", scale=8)
+    c["cfg"]["fix_cav_clamp"] = 1
+    out = []
+    for mode in ("planes", "dataflow"):
+        monkeypatch.setenv("CFD3D_SWEEP", mode)
+        e = native.Engine(c, precision=abi.FP64)
+        e.initialize(c["pv0"])
+        for it in range(3):
+            e.iterate(1, it + 1, 0.0)
+        out.append([e.download(n)["pv"] for n in range(len(c["blocks"]))])
+        e.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
