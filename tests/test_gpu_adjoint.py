@@ -4,7 +4,8 @@ R(pv) is the FP64 residual with each interior cell's dv and tv(1:2) its EOS and 
 viscosity tv(3) and history held (cfd3d_gb300.adjoint.StateSetter).  The state is the
 cavitating SST block of cases.adjoint (pressure, velocity and vapour fraction noisy) with
 noise added to T, y2, k and omega as well, so that no limiter, min / max or clip sits on
-a tie, and a band of cells just below the vapour pressure, where vaporisation is active.  Checks, each at <= 1e-6 relative:
+a tie, and two bands of cells just below and above the vapour pressure, where vaporisation
+and condensation are active.  Checks, each at <= 1e-6 relative:
   * entries of (dR/dpv)^T lambda at cells across the block (boundary rows included)
     against lambda . (R(pv + h e) - R(pv - h e)) / 2h of the GPU residual, h = 1e-6 |x|;
   * the same against the oracle's residual (CPU restatement of the reference);
@@ -34,11 +35,13 @@ def _state(scale, seed=11):
     sh = pv.shape[:-1]
     pv[..., 4] = 300.0 + rng.normal(0.0, 0.05, size=sh)
     pv[..., 6] = 1e-7 * (1.0 + 0.1 * rng.normal(size=sh))
-    # a band of cells 0.2-0.8 % below the vapour pressure: vaporisation is active there and
-    # below its clamp, so that it depends on c_v
-    band = pv[..., 4].copy()[:, :, : max(sh[2] // 8, 2)]
-    deficit = 0.002 + 0.006 * rng.random(size=band.shape)
-    pv[:, :, : band.shape[2], 0] = np.vectorize(cases.pww_iapws)(band) * (1.0 - deficit) - c["cfg"]["pref"]
+    # two bands of cells 0.2-0.8 % below and above the vapour pressure: vaporisation and
+    # condensation are active there and below their clamps, so that they depend on c_v, c_c
+    w = max(sh[2] // 8, 2)
+    for b0, sgn in ((0, -1.0), (w, 1.0)):
+        band = pv[:, :, b0:b0 + w, 4]
+        dev = 0.002 + 0.006 * rng.random(size=band.shape)
+        pv[:, :, b0:b0 + w, 0] = np.vectorize(cases.pww_iapws)(band) * (1.0 + sgn * dev) - c["cfg"]["pref"]
     pv[..., 7] *= 1.0 + 0.05 * rng.normal(size=sh)
     pv[..., 8] *= 1.0 + 0.05 * rng.normal(size=sh)
     c["pv0"] = [pv]
