@@ -558,43 +558,64 @@ __global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, lon
 
 // Dataflow sweep: one persistent launch per sweep.  CTAs take chunks (runs of at most
 // SW_CH cells of one plane) in plane order -- reversed for the backward sweep -- from a
-// ticket counter.  A cell waits for the done flags of its three lower (upper) neighbours,
-// which belong to earlier tickets, runs the hyperplane kernel's arithmetic and raises its own
-// flag.  Ticket order keeps the waits finite: the earliest unfinished chunk has all its
-// dependencies done, and its CTA is running.  Every wait is bounded by `spin` polls; a wait
-// that runs out records sweep_stall, which also ends every other wait, so the launch
-// completes and the host reports CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose
-// flags are never raised (the stall test).
+// ticket counter.  A chunk's cells need the dq of their lower (upper) neighbours, which lie
+// in a few chunks of the previous (next) plane; the CTA's first thread waits for those
+// chunks' done flags, the CTA runs the hyperplane kernel's arithmetic on its cells, and the
+// first thread raises the chunk's flag.  The needed chunks always hold earlier tickets, so
+// the earliest unfinished chunk never waits and its CTA is running: the waits end.  Each
+// wait is still bounded by `spin` polls; a wait that runs out records sweep_stall, which
+// also ends every other wait, so the launch completes and the host reports
+// CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose flag is never raised (the stall
+// test).
 template <bool FWD, bool MX>
 __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long spin, int withhold) {
-  __shared__ int s_q;
+  __shared__ int s_q, s_lo[SW_CH / 32], s_hi[SW_CH / 32];
   const long long nint = d.nint;
   unsigned* ticket = d.tickets + (FWD ? 0 : 1);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (;;) {
     if (threadIdx.x == 0) s_q = (int)atomicAdd(ticket, 1u);
     __syncthreads();
     const int q = s_q;
-    __syncthreads();
     if (q >= d.nchunk) return;
     const int ch = FWD ? q : d.nchunk - 1 - q;
     const long long t = d.chunk_t0[ch] + threadIdx.x;
-    if (t >= d.chunk_t0[ch + 1]) continue;
-    for (int k = 0; k < 3; ++k) {
-      const int nb = FWD ? d.nbf[k * nint + t] : d.nbb[k * nint + t];
-      if (nb < 0) continue;
-      const volatile int* f = d.done + nb;
-      long long it = 0;
-      while (*f == 0) {
-        ++it;
-        if ((it & 255) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
-        if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
-        __nanosleep(32);
+    const bool live = t < d.chunk_t0[ch + 1];
+    // the range of chunks that hold this chunk's neighbours
+    int lo = 0x7fffffff, hi = -1;
+    if (live)
+      for (int k = 0; k < 3; ++k) {
+        const int nb = FWD ? d.nbf[k * nint + t] : d.nbb[k * nint + t];
+        if (nb < 0) continue;
+        const int cn = d.chunk_of[nb];
+        lo = min(lo, cn);
+        hi = max(hi, cn);
       }
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
     }
+    if (lane == 0) { s_lo[wid] = lo; s_hi[wid] = hi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < SW_CH / 32; ++w) { lo = min(lo, s_lo[w]); hi = max(hi, s_hi[w]); }
+      for (int cn = lo; cn <= hi; ++cn) {
+        const volatile int* f = d.done + cn;
+        long long it = 0;
+        while (*f == 0) {
+          ++it;
+          if ((it & 63) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
+          if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (live) sweep_cell<FWD, MX, true>(d, c, t);
     __threadfence();
-    sweep_cell<FWD, MX, true>(d, c, t);
-    __threadfence();
-    if (ch != withhold) atomicExch(d.done + t, 1);
+    __syncthreads();
+    if (threadIdx.x == 0 && ch != withhold) atomicExch(d.done + ch, 1);
   }
 }
 
@@ -844,11 +865,11 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   if (!E.sweep_planes) {
     // dataflow sweeps: flags and tickets cleared, one persistent launch per sweep
     cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), s);
-    cudaMemsetAsync(d.done, 0, (size_t)E.nint * sizeof(int), s);
+    cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), s);
     if (c.mixed) k_sweep_df<true, true><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
     else k_sweep_df<true, false><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
     stage(5);
-    cudaMemsetAsync(d.done, 0, (size_t)E.nint * sizeof(int), s);
+    cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), s);
     if (c.mixed) k_sweep_df<false, true><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
     else k_sweep_df<false, false><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
     n += 2;
@@ -1136,7 +1157,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   E.d.cells = E.d_planes; E.d.pos = E.d_pos; E.d.nbf = E.d_nbf; E.d.nbb = E.d_nbb;
   if (!E.d_planes || !E.d_pos || !E.d_nbf || !E.d_nbb) { E.err = "device allocation failed (sweep maps)"; return CFD3D_ERR_NOMEM; }
   if (cudaMalloc(&E.d.rec, (size_t)NREC * E.nint * 8) != cudaSuccess) { E.err = "device allocation failed (sweep records)"; return CFD3D_ERR_NOMEM; }
-  if (cudaMalloc(&E.d.done, (size_t)E.nint * sizeof(int)) != cudaSuccess ||
+  if (cudaMalloc(&E.d.done, (size_t)E.d.nchunk * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&E.d.tickets, 2 * sizeof(unsigned)) != cudaSuccess) {
     E.err = "device allocation failed (sweep flags)";
     return CFD3D_ERR_NOMEM;
@@ -1149,7 +1170,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, true>, SW_CH, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, false>, SW_CH, 0);
-    E.sweep_grid = std::max(1, std::min(per * nsm, E.d.nchunk));
+    E.sweep_grid = std::max(1, std::min(std::min(per, 8) * nsm, E.d.nchunk));
   }
   if (c.mixed && (cudaMalloc(&E.d.recf, (size_t)REC_DIAG * E.nint * 4) != cudaSuccess ||
                   cudaMalloc(&E.d.dqsf, (size_t)c.npv * E.nint * 4) != cudaSuccess)) {
@@ -1180,6 +1201,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d.done);
   cudaFree(E.d.tickets);
   cudaFree(E.d_chunk_t0);
+  cudaFree(E.d_chunk_of);
   cudaFree(E.d.recf);
   cudaFree(E.d.dqsf);
   adjoint_free(E);
@@ -1424,7 +1446,7 @@ int cfd3d_sweep_stall_test(cfd3d_handle* h) {
   // raises its flags, with a short poll limit
   launch_iteration(E, false);
   CFD_CUDA(cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), E.st));
-  CFD_CUDA(cudaMemsetAsync(d.done, 0, (size_t)E.nint * sizeof(int), E.st));
+  CFD_CUDA(cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), E.st));
   if (c.mixed) k_sweep_df<true, true><<<E.sweep_grid, SW_CH, 0, E.st>>>(d, c, 1 << 12, 0);
   else k_sweep_df<true, false><<<E.sweep_grid, SW_CH, 0, E.st>>>(d, c, 1 << 12, 0);
   CFD_CUDA(cudaStreamSynchronize(E.st));

@@ -75,8 +75,10 @@ struct DevPtr {
   double* rec;
   const int *cells, *pos, *nbf, *nbb;
   // dataflow sweeps: chunk starts in t (chunks of at most SW_CH cells, never across a
-  // plane; nchunk + 1 entries), per-cell done flags, the two sweeps' chunk tickets
+  // plane; nchunk + 1 entries), the chunk of every t, per-chunk done flags, the two
+  // sweeps' chunk tickets
   const int* chunk_t0;
+  const int* chunk_of;
   int nchunk;
   int* done;
   unsigned* tickets;
@@ -114,6 +116,7 @@ struct Engine {
   int* d_nbb = nullptr;
   std::vector<long long> plane_off;
   int* d_chunk_t0 = nullptr;   // dataflow sweep chunks (setup_planes)
+  int* d_chunk_of = nullptr;
   int sweep_grid = 0;          // persistent CTAs of the dataflow sweep
   int sweep_planes = 0;        // 1: one launch per hyperplane instead (CFD3D_SWEEP=planes)
   cudaStream_t st = nullptr;

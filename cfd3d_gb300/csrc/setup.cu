@@ -704,6 +704,12 @@ void setup_planes(Engine& E) {
   cudaMalloc(&E.d_chunk_t0, chunks.size() * sizeof(int));
   cudaMemcpy(E.d_chunk_t0, chunks.data(), chunks.size() * sizeof(int), cudaMemcpyHostToDevice);
   E.d.chunk_t0 = E.d_chunk_t0;
+  std::vector<int> chunk_of(nint);
+  for (size_t q = 0; q + 1 < chunks.size(); ++q)
+    for (int t = chunks[q]; t < chunks[q + 1]; ++t) chunk_of[t] = (int)q;
+  cudaMalloc(&E.d_chunk_of, nint * sizeof(int));
+  cudaMemcpy(E.d_chunk_of, chunk_of.data(), nint * sizeof(int), cudaMemcpyHostToDevice);
+  E.d.chunk_of = E.d_chunk_of;
   cudaMalloc(&E.d_planes, nint * sizeof(int));
   cudaMemcpy(E.d_planes, cells.data(), nint * sizeof(int), cudaMemcpyHostToDevice);
   cudaMalloc(&E.d_pos, E.ncell * sizeof(int));
