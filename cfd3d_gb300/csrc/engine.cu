@@ -273,7 +273,25 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
   const bool vis = c.iturb != -3;
   const long long st[3] = {1, sj, sk};
   double res[NPVM];
-  for (int v = 0; v < npv; ++v) {
+  if (MX) {
+    // the stored FP32 fluxes are deviations from the free-stream flux: their differences
+    // and sums in FP32 carry rounding of the order of the storage's own (one conversion to
+    // FP64 per variable instead of one per stored value)
+    for (int v = 0; v < npv; ++v) {
+      float r = 0.0f;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float* F = d.fi32 + ((long long)q * npv + v) * n;
+        r -= F[g] - F[g - st[q]];
+        if (vis) {
+          const float* V = d.fv32 + ((long long)q * npv + v) * n;
+          r += V[g] - V[g - st[q]];
+        }
+      }
+      res[v] = (double)r;
+    }
+  }
+  for (int v = 0; v < npv && !MX; ++v) {
     double r = 0.0;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -331,12 +349,6 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
   if (c.iturb == 0) {
     // cell-centred gradients of u, v, w, k, omega (turbsource kwsst, :269-383)
     const long long nbr[6] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk};
-    double fa[6][3];
-    for (int q = 0; q < 3; ++q) {
-      fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
-      fa[2][q] = d.gm[(GM_EX + q) * n + g - sj]; fa[3][q] = d.gm[(GM_EX + q) * n + g];
-      fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
-    }
     const int gv[5] = {1, 2, 3, 7, 8};
     double tv[3];
     for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
@@ -346,22 +358,34 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
     SstOut<double> so;
     if (MX) {
       // FP32 on the gauge shadow: differences of u - U are exact where u's are not
+      float faf[6][3];
+      for (int q = 0; q < 3; ++q) {
+        faf[0][q] = d.gmf[(GM_CX + q) * n + g - 1]; faf[1][q] = d.gmf[(GM_CX + q) * n + g];
+        faf[2][q] = d.gmf[(GM_EX + q) * n + g - sj]; faf[3][q] = d.gmf[(GM_EX + q) * n + g];
+        faf[4][q] = d.gmf[(GM_TX + q) * n + g - sk]; faf[5][q] = d.gmf[(GM_TX + q) * n + g];
+      }
       float grf[5][3];
-      const float ivf = (float)(1.0 / vol);
+      const float ivf = 1.0f / d.gmf[GM_GRD * n + g];
       for (int q = 0; q < 5; ++q) {
         const float* P = d.pvf + gv[q] * n;
         const float c0 = P[g];
         float vv[6];
         for (int m = 0; m < 6; ++m) vv[m] = 0.5f * (P[nbr[m]] + c0);
         for (int e = 0; e < 3; ++e)
-          grf[q][e] = (vv[1] * (float)fa[1][e] + vv[3] * (float)fa[3][e] + vv[5] * (float)fa[5][e] -
-                       vv[0] * (float)fa[0][e] - vv[2] * (float)fa[2][e] - vv[4] * (float)fa[4][e]) * ivf;
+          grf[q][e] = (vv[1] * faf[1][e] + vv[3] * faf[3][e] + vv[5] * faf[5][e] -
+                       vv[0] * faf[0][e] - vv[2] * faf[2][e] - vv[4] * faf[4][e]) * ivf;
       }
       const SstOut<float> sf = sst_source_f(grf, (float)kk, (float)oo, (float)dv[0], (float)tv[0], (float)tv[2],
                                             (float)y5, (float)vol);
       so.r7 = sf.r7; so.r8 = sf.r8; so.prod = sf.prod; so.dest = sf.dest; so.div = sf.div; so.pkw = sf.pkw;
       so.bigf = sf.bigf; so.talpha = sf.talpha; so.tbeta = sf.tbeta; so.strain = sf.strain;
     } else {
+      double fa[6][3];
+      for (int q = 0; q < 3; ++q) {
+        fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
+        fa[2][q] = d.gm[(GM_EX + q) * n + g - sj]; fa[3][q] = d.gm[(GM_EX + q) * n + g];
+        fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
+      }
       double gr[5][3];
       double ivol = 1.0 / vol;
       for (int q = 0; q < 5; ++q) {
@@ -795,6 +819,11 @@ __global__ void k_soa_to_aos(const double* __restrict__ soa, int nv, long long n
   for (int v = 0; v < nv; ++v) a[q * nv + v] = soa[v * ncell + off + q];
 }
 // interior AoS a(nv, 2:imax, 2:jmax, 2:kmax) of one block <-> SoA planes
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, long long m) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < m) b[q] = (float)a[q];
+}
+
 __global__ void k_interior_io(double* __restrict__ a, int nv, BlockGeom B, double* __restrict__ soa, long long ncell,
                               int to_soa) {
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -1152,6 +1181,12 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     }
   }
   if (!setup_geometry(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
+  if (c.mixed) {
+    const long long m = (long long)(GM_GRD + c.ngrd) * E.ncell;
+    if (cudaMalloc(&E.d.gmf, (size_t)m * 4) != cudaSuccess) { E.err = "device allocation failed (gmf)"; return CFD3D_ERR_NOMEM; }
+    k_to_f32<<<nblk_of(m, 256), 256, 0, E.st>>>(E.d.gm, E.d.gmf, m);
+    CFD_CUDA(cudaStreamSynchronize(E.st));
+  }
   if (!setup_ghost_program(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
   setup_planes(E);
   E.d.cells = E.d_planes; E.d.pos = E.d_pos; E.d.nbf = E.d_nbf; E.d.nbb = E.d_nbb;
@@ -1188,7 +1223,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
                     E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
   for (double* p : bufs) cudaFree(p);
-  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec};
+  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf};
   for (float* p : fbufs) cudaFree(p);
   cudaFree((void*)E.d.blk);
   cudaFree(E.d.sc);

@@ -69,6 +69,7 @@ struct DevPtr {
   double* partial;   // per-CTA partial residual sums [gridsize][npv+2]
   // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
   float *pvf, *fi32, *fv32;
+  float* gmf;        // mixed form: FP32 copy of gm (metrics of the FP32 viscous and SST terms)
   float* frec;       // mixed form: reconstructed face states of one direction (2 x 12 planes)
   // LU-SGS sweep records in plane-major order t (REC_* planes of nint entries); dqs and
   // dcv are plane-major too

@@ -150,15 +150,17 @@ __global__ void __launch_bounds__(128) k_flux_mx(DevPtr d, Par c) {
   const bool turb = (c.iturb == 0);
   const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);
   const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);
-  float nx[3] = {(float)nv[0], (float)nv[1], (float)nv[2]};
+  // metrics from their FP32 copy
+  const float* GF = d.gmf;
+  float nx[3] = {GF[(fplane + 0) * n + g], GF[(fplane + 1) * n + g], GF[(fplane + 2) * n + g]};
   float ev[3], tvv[3];
   for (int q = 0; q < 3; ++q) {
-    const double* E1 = d.gm + (ep + q) * n;
-    ev[q] = (float)(0.25 * (E1[g - s1] + E1[g - s1 + sn] + E1[g] + E1[g + sn]));
-    const double* T1 = d.gm + (tp + q) * n;
-    tvv[q] = (float)(0.25 * (T1[g - s2] + T1[g - s2 + sn] + T1[g] + T1[g + sn]));
+    const float* E1 = GF + (ep + q) * n;
+    ev[q] = 0.25f * (E1[g - s1] + E1[g - s1 + sn] + E1[g] + E1[g + sn]);
+    const float* T1 = GF + (tp + q) * n;
+    tvv[q] = 0.25f * (T1[g - s2] + T1[g - s2 + sn] + T1[g] + T1[g + sn]);
   }
-  float vol = (float)(2.0 / (d.gm[GM_GRD * n + g] + d.gm[GM_GRD * n + gr]));
+  float vol = 2.0f / (GF[GM_GRD * n + g] + GF[GM_GRD * n + gr]);
   float tvl[3] = {0, 0, 0}, tvr[3] = {0, 0, 0};
   for (int q = 0; q < c.ntv; ++q) { tvl[q] = (float)d.tv[q * n + g]; tvr[q] = (float)d.tv[q * n + gr]; }
   float vis = 0.5f * (tvl[0] + tvr[0]);
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(128) k_flux_mx(DevPtr d, Par c) {
   if (turb) {
     float pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
     float rho = (float)(0.5 * (d.dv[g] + d.dv[gr]));
-    float ydns = (float)(0.5 * (d.gm[(GM_GRD + 4) * n + g] + d.gm[(GM_GRD + 4) * n + gr]));
+    float ydns = 0.5f * (GF[(GM_GRD + 4) * n + g] + GF[(GM_GRD + 4) * n + gr]);
     float kf = cc[4], of = cc[5];
     float cdkw = fmaxf(1.712f * rho / of * pkw, 1.0e-10f);
     float term1 = sqrtf(kf) / (0.09f * of * ydns);

@@ -147,7 +147,8 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
     for (int k = 0; k < npv; ++k) fx[k] = 0.0;
     return;
   }
-  const double n0 = nv[0] / dl, n1 = nv[1] / dl, n2 = nv[2] / dl;
+  const double idl = 1.0 / dl;
+  const double n0 = nv[0] * idl, n1 = nv[1] * idl, n2 = nv[2] * idl;
   const double nn[3] = {n0, n1, n2};
   const float nf[3] = {(float)n0, (float)n1, (float)n2};
   const float* pl = L.g;
