@@ -23,6 +23,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <type_traits>
 #include "engine.cuh"
 #include "mixed.cuh"
 
@@ -591,12 +592,58 @@ __global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, lon
 // also ends every other wait, so the launch completes and the host reports
 // CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose flag is never raised (the stall
 // test).
+// what a dataflow sweep cell reads of one neighbour before its dq is known
+template <class T>
+struct SweepNb {
+  int nb;
+  T nx[3], pv[NPVM], dv[14], spec, beta, evv;
+};
+
+template <bool FWD, class T>
+__device__ __forceinline__ void sweep_nb_load(const DevPtr& d, long long t, int q, const T* R, SweepNb<T>& s) {
+  const long long nint = d.nint;
+  s.nb = FWD ? d.nbf[q * nint + t] : d.nbb[q * nint + t];
+  if (s.nb < 0) return;
+  const long long fr = FWD ? s.nb : t;
+  for (int e = 0; e < 3; ++e) s.nx[e] = R[(REC_FACE + 3 * q + e) * nint + fr];
+  rec_state<T>(R, nint, s.nb, s.pv, s.dv);
+  s.spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + s.nb];
+  s.beta = R[REC_BETA * nint + s.nb];
+  s.evv = R[REC_EVV * nint + s.nb];
+}
+
+template <bool FWD, class T>
+__device__ __forceinline__ void sweep_nb_apply(const DevPtr& d, int npv, const SweepNb<T>& s, const T* dqs, T* acc) {
+  if (s.nb < 0) return;
+  const long long nint = d.nint;
+  T dq[NPVM];
+  for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? __ldcg(dqs + v * nint + s.nb) : T(0);
+  jac_apply_pre<T>(npv, s.nx, s.pv, s.dv, s.spec, s.beta, s.evv, FWD ? T(1) : T(-1), dq, acc);
+}
+
+// Dataflow sweep: one persistent launch per sweep.  CTAs take chunks (runs of at most
+// SW_CH cells of one plane) in plane order -- reversed for the backward sweep -- from a
+// ticket counter.  A chunk's cells need the dq of their lower (upper) neighbours, which lie
+// in a few chunks of the previous (next) plane.  Each cell first loads everything that
+// does not depend on those dq (its own record, the neighbours' records); then the CTA waits
+// for the needed chunks' done flags (one polling thread per flag), runs the hyperplane
+// kernel's arithmetic and raises its own chunk's flag.  The needed chunks always hold
+// earlier tickets, so the earliest unfinished chunk never waits and its CTA is running:
+// the waits end.  Each wait is still bounded by `spin` polls; a wait that runs out records
+// sweep_stall, which also ends every other wait, so the launch completes and the host
+// reports CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose flag is never raised (the
+// stall test).
 template <bool FWD, bool MX>
 __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long spin, int withhold) {
+  using T = typename std::conditional<MX, float, double>::type;
   __shared__ int s_q, s_lo[SW_CH / 32], s_hi[SW_CH / 32];
   const long long nint = d.nint;
+  const int npv = c.npv;
   unsigned* ticket = d.tickets + (FWD ? 0 : 1);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const T* RN;
+  const T* DQ;
+  if constexpr (MX) { RN = d.recf; DQ = d.dqsf; } else { RN = d.rec; DQ = d.dqs; }
   for (;;) {
     if (threadIdx.x == 0) s_q = (int)atomicAdd(ticket, 1u);
     __syncthreads();
@@ -605,38 +652,64 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
     const int ch = FWD ? q : d.nchunk - 1 - q;
     const long long t = d.chunk_t0[ch] + threadIdx.x;
     const bool live = t < d.chunk_t0[ch + 1];
-    // the range of chunks that hold this chunk's neighbours
+    // ---- loads that do not wait: own record, neighbour records, the needed chunks
+    SweepNb<T> nbs[3];
+    double acc[NPVM], pv[NPVM], dv[14], o[PREP_DIAG];
     int lo = 0x7fffffff, hi = -1;
-    if (live)
+    if (live) {
+      const double* R = d.rec;
+      for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
+      if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
+      else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
+      rec_state<double>(R, nint, t, pv, dv);
+      for (int k = 0; k < PREP_DIAG; ++k) o[k] = R[(REC_DIAG + k) * nint + t];
       for (int k = 0; k < 3; ++k) {
-        const int nb = FWD ? d.nbf[k * nint + t] : d.nbb[k * nint + t];
-        if (nb < 0) continue;
-        const int cn = d.chunk_of[nb];
-        lo = min(lo, cn);
-        hi = max(hi, cn);
+        sweep_nb_load<FWD, T>(d, t, k, RN, nbs[k]);
+        if (nbs[k].nb >= 0) {
+          const int cn = d.chunk_of[nbs[k].nb];
+          lo = min(lo, cn);
+          hi = max(hi, cn);
+        }
       }
-    for (int o = 16; o > 0; o >>= 1) {
-      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    for (int k = 16; k > 0; k >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, k));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, k));
     }
     if (lane == 0) { s_lo[wid] = lo; s_hi[wid] = hi; }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int w = 1; w < SW_CH / 32; ++w) { lo = min(lo, s_lo[w]); hi = max(hi, s_hi[w]); }
-      for (int cn = lo; cn <= hi; ++cn) {
-        const volatile int* f = d.done + cn;
-        long long it = 0;
-        while (*f == 0) {
-          ++it;
-          if ((it & 63) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
-          if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
-          __nanosleep(64);
-        }
+    for (int w = 0; w < SW_CH / 32; ++w) { lo = min(lo, s_lo[w]); hi = max(hi, s_hi[w]); }
+    // ---- wait: thread k polls chunks lo + k, lo + k + SW_CH, ...
+    for (int cn = lo + (int)threadIdx.x; cn <= hi; cn += SW_CH) {
+      const volatile int* f = d.done + cn;
+      long long it = 0;
+      while (*f == 0) {
+        ++it;
+        if ((it & 63) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
+        if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
+        if (it > 8) __nanosleep(32);
       }
-      __threadfence();
     }
+    __threadfence();
     __syncthreads();
-    if (live) sweep_cell<FWD, MX, true>(d, c, t);
+    if (live) {
+      if constexpr (MX) {
+        float an[NPVM];
+        for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
+        for (int k = 0; k < 3; ++k) sweep_nb_apply<FWD, float>(d, npv, nbs[k], DQ, an);
+        for (int v = 0; v < npv; ++v) acc[v] += (double)an[v];
+      } else {
+        for (int k = 0; k < 3; ++k) sweep_nb_apply<FWD, double>(d, npv, nbs[k], DQ, acc);
+      }
+      if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
+      Diag D;
+      diag_from_array(o, D);
+      double x[NPVM];
+      for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
+      diag_solve(c, D, pv, dv, acc, x);
+      for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
+      if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0 && ch != withhold) atomicExch(d.done + ch, 1);
