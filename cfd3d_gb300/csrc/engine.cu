@@ -679,8 +679,9 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
     if (lane == 0) { s_lo[wid] = lo; s_hi[wid] = hi; }
     __syncthreads();
     for (int w = 0; w < SW_CH / 32; ++w) { lo = min(lo, s_lo[w]); hi = max(hi, s_hi[w]); }
-    // ---- wait: thread k polls chunks lo + k, lo + k + SW_CH, ...
-    for (int cn = lo + (int)threadIdx.x; cn <= hi; cn += SW_CH) {
+    // ---- wait: thread k polls chunks lo + k, lo + k + SW_CH, ... (none when no cell of
+    // the chunk has a neighbour: then hi = -1 and lo is not a chunk index)
+    for (int cn = (hi >= 0) ? lo + (int)threadIdx.x : 0; hi >= 0 && cn <= hi; cn += SW_CH) {
       const volatile int* f = d.done + cn;
       long long it = 0;
       while (*f == 0) {
