@@ -53,11 +53,13 @@ def test_sweep_wait_runs_out_and_the_handle_recovers(precision):
 
 def test_dataflow_sweeps_equal_hyperplane_sweeps(monkeypatch):
     """The dataflow sweeps run each cell's arithmetic on the same inputs as the one-launch-
-    per-hyperplane sweeps: the FP64 states agree bit for bit."""
+    per-hyperplane sweeps: the FP64 states agree to rounding (the two kernels may contract
+    multiply-adds differently), and two dataflow runs agree bit for bit (the result does
+    not depend on which CTA took which chunk)."""
     c = cases.make("batched", scale=8)
     c["cfg"]["fix_cav_clamp"] = 1
     out = []
-    for mode in ("planes", "dataflow"):
+    for mode in ("planes", "dataflow", "dataflow"):
         monkeypatch.setenv("CFD3D_SWEEP", mode)
         e = native.Engine(c, precision=abi.FP64)
         e.initialize(c["pv0"])
@@ -65,5 +67,7 @@ def test_dataflow_sweeps_equal_hyperplane_sweeps(monkeypatch):
             e.iterate(1, it + 1, 0.0)
         out.append([e.download(n)["pv"] for n in range(len(c["blocks"]))])
         e.close()
-    for a, b in zip(*out):
-        assert np.array_equal(a, b)
+    for a, b, b2 in zip(*out):
+        scale = np.abs(a).reshape(-1, a.shape[-1]).max(axis=0)
+        assert (np.abs(a - b).reshape(-1, a.shape[-1]).max(axis=0) <= 1e-12 * scale).all()
+        assert np.array_equal(b, b2)
