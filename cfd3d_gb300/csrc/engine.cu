@@ -464,7 +464,8 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
   if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
   if (c.iturb == 0) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
   Diag D;
-  diag_prepare(c, pv2, dv, tvc, fc, vol, d.dt[g], ic, it4, D);
+  const double evis = eigenvis_of(c, dv, tvc);
+  diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D);
   double o[NREC];
   for (int q = 0; q < NREC; ++q) o[q] = 0.0;
   const int pvi[7] = {1, 2, 3, 5, 6, 7, 8};
@@ -484,9 +485,9 @@ __global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
   } else {
     for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = face_spectral<double>(c, fc + 3 * q, pv2, dv);
   }
-  const double sndp2 = sndp2_of<double>(c, dv[5], pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3]);
-  o[REC_BETA] = 1.0 / sndp2 - 1.0 / dv[5] + dv[6];
-  o[REC_EVV] = 2.0 * eigenvis_of(c, dv, tvc) / vol;
+  // beta = 1/sndp2 - 1/c2 + drho/dp = D.rr - (D.b1 - 1) drho/dp
+  o[REC_BETA] = D.rr - (D.b1 - 1.0) * dv[6];
+  o[REC_EVV] = 2.0 * evis / vol;
   for (int e = 0; e < 3; ++e) {
     o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e];
   }

@@ -874,11 +874,16 @@ struct Diag {
   double a, b1, i_b1, ss, rr, cross, cross1, cross2, ssy1, ssy2, ssh, aaa1, aaa2, mm, c[4], tt, t[4];
 };
 
-__device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, const double* dv, const double* tv,
+// evis = eigenvis_of(c, dv, tv), which the caller also needs
+__device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, const double* dv, double evis,
                                              const double* fc /* cx1,cx2,ex1,ex2,tx1,tx2 x3 */, double vol,
                                              double dt, const double* icav, const double* itt, Diag& D) {
+  // (the reference's repeated quotients are formed once: one reciprocal of c2, of the
+  // preconditioned c2 and of the volume; the FP64 pipe is the scarce unit of a GB300)
   double uv2 = pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3];
   double sndp2 = sndp2_of<double>(c, dv[5], uv2);
+  const double idv5 = 1.0 / dv[5], isnd = 1.0 / sndp2;
+  const double qr = sndp2 * idv5, qh = 0.5 * (1.0 + qr), qd = sq(1.0 - qr);
   const double cappa = 1.05;
   double lamda = 0.0, fs = 0.0;
   for (int d = 0; d < 3; ++d) {
@@ -887,22 +892,23 @@ __device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, con
     double oz = 0.5 * (fc[6 * d + 2] + fc[6 * d + 5]);
     double ds = ox * ox + oy * oy + oz * oz;
     double u = ox * pv[1] + oy * pv[2] + oz * pv[3];
-    double up = 0.5 * (1.0 + sndp2 / dv[5]) * u;
-    double dd = 0.5 * sqrt(u * u * sq(1.0 - sndp2 / dv[5]) + 4.0 * sndp2 * ds);
+    double up = qh * u;
+    double dd = 0.5 * sqrt(u * u * qd + 4.0 * sndp2 * ds);
     lamda += cappa * (fabs(up) + dd);
     fs += ds;  // 0.25*(f1+f2)^2 summed over the components
   }
-  double ev = eigenvis_of(c, dv, tv) * fs;
+  const double ivol = 1.0 / vol;
+  double ev = evis * fs;
   double bb = (c.nsteady == 1) ? 1.0 : 0.75;
   double a = 1.0 / (vol / dt + lamda);
   double unst = (c.nsteady >= 1) ? (double)c.nsteady * bb * vol / c.dt_phy : 0.0;
-  double b = (unst + 2.0 * ev / vol) * a;
+  double b = (unst + 2.0 * ev * ivol) * a;
   for (int q = 0; q < 4; ++q) { D.c[q] = icav[q] * vol * a; D.t[q] = itt[q] * vol * a; }
   D.a = a;
   D.b1 = 1.0 + b;
   D.i_b1 = 1.0 / (D.b1 * dv[0]);
-  D.ss = dv[0] * dv[11] * (1.0 / sndp2 + b / dv[5]);
-  D.rr = 1.0 / sndp2 - 1.0 / dv[5] + D.b1 * dv[6];
+  D.ss = dv[0] * dv[11] * (isnd + b * idv5);
+  D.rr = isnd - idv5 + D.b1 * dv[6];
   double hst = dv[1] + 0.5 * uv2 - uv2;
   D.cross = dv[13] * dv[8] - dv[12] * dv[9];
   D.cross1 = dv[12] * dv[7] - dv[11] * dv[8];
