@@ -142,28 +142,31 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
                                                  const float* sdst, float rc2, const float* ravg_u,
                                                  const float* ravg_s, double* fx) {
   const int npv = c.npv;
-  const double dl = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-  if (dl == 0.0) {
+  // The FP64 leading-order terms use the unnormalised face vector nv (|nv| = dl): the
+  // normal velocities unl = nv . u are the fluxes' transport velocities times dl, so no
+  // FP64 square root or division is needed; the FP32 terms use the unit normal and are
+  // scaled by the FP32 length dlf.
+  const float nvf[3] = {(float)nv[0], (float)nv[1], (float)nv[2]};
+  const float dlf = sqrtf(nvf[0] * nvf[0] + nvf[1] * nvf[1] + nvf[2] * nvf[2]);
+  if (dlf == 0.0f) {
     for (int k = 0; k < npv; ++k) fx[k] = 0.0;
     return;
   }
-  const double idl = 1.0 / dl;
-  const double n0 = nv[0] * idl, n1 = nv[1] * idl, n2 = nv[2] * idl;
-  const double nn[3] = {n0, n1, n2};
-  const float nf[3] = {(float)n0, (float)n1, (float)n2};
+  const float idlf = 1.0f / dlf;
+  const float nf[3] = {nvf[0] * idlf, nvf[1] * idlf, nvf[2] * idlf};
   const float* pl = L.g;
   const float* pr = R.g;
   // FP64 leading-order quantities
-  const double ull = n0 * L.u[0] + n1 * L.u[1] + n2 * L.u[2];
-  const double urr = n0 * R.u[0] + n1 * R.u[1] + n2 * R.u[2];
+  const double unl = nv[0] * L.u[0] + nv[1] * L.u[1] + nv[2] * L.u[2];
+  const double unr = nv[0] * R.u[0] + nv[1] * R.u[1] + nv[2] * R.u[2];
   const double HL = L.h + 0.5 * (L.u[0] * L.u[0] + L.u[1] * L.u[1] + L.u[2] * L.u[2]);
   const double HR = R.h + 0.5 * (R.u[0] * R.u[0] + R.u[1] * R.u[1] + R.u[2] * R.u[2]);
-  // FP32 copies and accurate jumps
-  const float uull = (float)ull, uurr = (float)urr;
+  // FP32 copies (unit-normal velocities) and accurate jumps
+  const float uull = (float)unl * idlf, uurr = (float)unr * idlf;
   const float rl = (float)L.rho, rr = (float)R.rho;
   const float drho = (float)(R.rho - L.rho);
   const float dH = (float)(HR - HL);
-  const float dun = (float)(urr - ull);
+  const float dun = (float)(unr - unl) * idlf;
   const float ulf[3] = {(float)L.u[0], (float)L.u[1], (float)L.u[2]};
   const float hlf = (float)HL;
   float du3[3];
@@ -190,20 +193,21 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
       float du = m_star * dun + (c_star - q * fabsf(uuu) - 0.5f * (1.0f - q) * uuu * m_star) * dp / rrho / sndp2;
       float dpp = m_star * dp + (c_star - fabsf(uuu) + 0.5f * (1.0f - q) * uuu * m_star) * rrho * dun;
       float au = fabsf(uuu);
-      const double mL = L.rho * ull, mR = R.rho * urr;
-      fx[0] = 0.5 * (mL + mR - (double)(au * drho + du * rrho));
+      // mass fluxes times dl
+      const double mL = L.rho * unl, mR = R.rho * unr;
+      fx[0] = 0.5 * (mL + mR - (double)(dlf * (au * drho + du * rrho)));
       for (int q3 = 0; q3 < 3; ++q3) {
         // rho_R u_R - rho_L u_L = rho_R (u_R - u_L) + (rho_R - rho_L) u_L
         float df = au * (rr * du3[q3] + drho * ulf[q3]) + du * rrho * ravg_u[q3] + dpp * nf[q3];
-        fx[1 + q3] = 0.5 * (mL * L.u[q3] + mR * R.u[q3] + nn[q3] * ((double)pl[0] + (double)pr[0]) - (double)df);
+        fx[1 + q3] = 0.5 * (mL * L.u[q3] + mR * R.u[q3] + nv[q3] * ((double)pl[0] + (double)pr[0]) - (double)(dlf * df));
       }
       float df4 = au * (rr * dH + drho * hlf - dp) + du * rrho * ravg_ht + dpp * uuu;
-      fx[4] = 0.5 * (mL * HL + mR * HR - (double)df4);
+      fx[4] = 0.5 * (mL * HL + mR * HR - (double)(dlf * df4));
       for (int k = 5; k < npv; ++k) {
         float df = au * (rr * (pr[k] - pl[k]) + drho * pl[k]) + du * rrho * ravg_s[k];
-        fx[k] = 0.5 * (mL * (double)pl[k] + mR * (double)pr[k] - (double)df);
+        fx[k] = 0.5 * (mL * (double)pl[k] + mR * (double)pr[k] - (double)(dlf * df));
       }
-      for (int k = 0; k < npv; ++k) fx[k] = fx[k] * dl - phin[k];
+      for (int k = 0; k < npv; ++k) fx[k] = fx[k] - phin[k];
       return;
     }
     // Roe-M
@@ -237,22 +241,25 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
     bdq[4] = bdq[0] * ravg_ht + rrho * dH;
     for (int k = 5; k < npv; ++k) bdq[k] = bdq[0] * ravg_s[k] + rrho * (pr[k] - pl[k]);
     // central part (b1 F_L - b2 F_R) / (b1 - b2) in FP64
+    // the weights b1 / (b1 - b2), b2 / (b1 - b2) in FP64 from FP32 wave speeds; fluxes
+    // times dl
     const double B1 = b1, B2 = b2, iB = 1.0 / (B1 - B2);
-    const double mL = L.rho * ull, mR = R.rho * urr;
+    const double w1 = B1 * iB, w2 = B2 * iB;
+    const double mL = L.rho * unl, mR = R.rho * unr;
     double fl[NPVM], fr[NPVM];
     fl[0] = mL; fr[0] = mR;
     for (int q3 = 0; q3 < 3; ++q3) {
-      fl[1 + q3] = mL * L.u[q3] + nn[q3] * (double)pl[0];
-      fr[1 + q3] = mR * R.u[q3] + nn[q3] * (double)pr[0];
+      fl[1 + q3] = mL * L.u[q3] + nv[q3] * (double)pl[0];
+      fr[1 + q3] = mR * R.u[q3] + nv[q3] * (double)pr[0];
     }
     fl[4] = mL * HL; fr[4] = mR * HR;
     for (int k = 5; k < npv; ++k) { fl[k] = mL * (double)pl[k]; fr[k] = mR * (double)pr[k]; }
-    const float wdiss = b1 * b2 / (b1 - b2);
+    const float wdiss = dlf * b1 * b2 / (b1 - b2);
     for (int k = 0; k < npv; ++k)
-      fx[k] = (B1 * fl[k] - B2 * fr[k]) * iB + (double)(wdiss * (dq[k] - gg * bdq[k] / add));
+      fx[k] = w1 * fl[k] - w2 * fr[k] + (double)(wdiss * (dq[k] - gg * bdq[k] / add));
     for (int q3 = 0; q3 < 3; ++q3)
-      fx[1 + q3] += (double)(gg * b1_du * b2_du * rrho * dun * nf[q3] / aaa / (b1_du - b2_du));
-    for (int k = 0; k < npv; ++k) fx[k] = fx[k] * dl - phin[k];
+      fx[1 + q3] += (double)(dlf * gg * b1_du * b2_du * rrho * dun * nf[q3] / aaa / (b1_du - b2_du));
+    for (int k = 0; k < npv; ++k) fx[k] = fx[k] - phin[k];
     return;
   }
   // AUSM family: the interface velocity amid * M_1/2 = (u_L + u_R)/2 + small terms is
@@ -302,11 +309,12 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
   }
   // amid * (M+ + M-) = (u_L + u_R)/2 + amid * E for subsonic ML, MR, with
   // E = (ML - MR)(ML + MR)(1/4 - 2 beta + beta (ML^2 + MR^2))
+  // (times dl: vsum is the interface velocity times the face length)
   double vsum;
   if (subl && subr)
-    vsum = 0.5 * (ull + urr) + (double)(amid * ((zml - zmr) * (zml + zmr) * ((0.25f - 2.0f * beta) + beta * (zml * zml + zmr * zmr))));
+    vsum = 0.5 * (unl + unr) + (double)(dlf * amid * ((zml - zmr) * (zml + zmr) * ((0.25f - 2.0f * beta) + beta * (zml * zml + zmr * zmr))));
   else
-    vsum = (double)(amid * (zmpl + zmmr));
+    vsum = (double)(dlf * amid * (zmpl + zmmr));
   // gauge interface pressure: P+ p'L + P- p'R + pref (P+ + P- - 1) - dissipation
   const float pdev = (float)(c.pref * ((double)dpl + (double)dpr));
   double ml, mr;
@@ -330,25 +338,26 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
       float sc = rrho / rl;
       pwl *= sc; pwr *= sc; dpw *= sc;
       // M+_1 = (M+ + M-) + M- ((pwr - pwl) - ww (1 + pwr)), M-_1 = M- ww (1 + pwr)
-      ml = L.rho * (vsum + (double)(amid * zmmr * (dpw - ww * (1.0f + pwr))));
-      mr = R.rho * (double)(amid * zmmr * ww * (1.0f + pwr));
+      ml = L.rho * (vsum + (double)(dlf * amid * zmmr * (dpw - ww * (1.0f + pwr))));
+      mr = R.rho * (double)(dlf * amid * zmmr * ww * (1.0f + pwr));
     } else {
       float sc = rrho / rr;
       pwl *= sc; pwr *= sc; dpw *= sc;
-      ml = L.rho * (double)(amid * zmpl * ww * (1.0f + pwl));
-      mr = R.rho * (vsum + (double)(amid * zmpl * (-dpw - ww * (1.0f + pwl))));
+      ml = L.rho * (double)(dlf * amid * zmpl * ww * (1.0f + pwl));
+      mr = R.rho * (vsum + (double)(dlf * amid * zmpl * (-dpw - ww * (1.0f + pwl))));
     }
   } else {
     const float kp = 0.25f;
-    double vmid = vsum - (double)(amid * kp * fmaxf(1.0f - am2mid / rc2, 0.0f) * dp / rrho / rc2 / fmid);
+    double vmid = vsum - (double)(dlf * amid * kp * fmaxf(1.0f - am2mid / rc2, 0.0f) * dp / rrho / rc2 / fmid);
     pmid = ppl * pl[0] + pmr * pr[0] + pdev - 2.0f * ppl * pmr * rrho * fmid * amid * dun;
     if (vmid > 0.0) { ml = L.rho * vmid; mr = 0.0; } else { mr = R.rho * vmid; ml = 0.0; }
   }
+  // ml, mr are mass fluxes times dl; the pressure acts on the face vector itself
   fx[0] = ml + mr;
-  for (int q3 = 0; q3 < 3; ++q3) fx[1 + q3] = ml * L.u[q3] + mr * R.u[q3] + (double)pmid * nn[q3];
+  for (int q3 = 0; q3 < 3; ++q3) fx[1 + q3] = ml * L.u[q3] + mr * R.u[q3] + (double)pmid * nv[q3];
   fx[4] = ml * HL + mr * HR;
   for (int k = 5; k < npv; ++k) fx[k] = ml * (double)pl[k] + mr * (double)pr[k];
-  for (int k = 0; k < npv; ++k) fx[k] = fx[k] * dl - phin[k];
+  for (int k = 0; k < npv; ++k) fx[k] = fx[k] - phin[k];
 }
 
 }  // namespace cfd
