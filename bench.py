@@ -267,6 +267,7 @@ def main():
     ap.add_argument("--ref-threads", type=int, default=0, help="host threads of the CPU samples (0: all)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -290,6 +291,7 @@ def main():
     res0 = [eng.residual(n)["res"] for n in range(len(case["blocks"]))] if prec == abi.MIXED else None
     for w in range(args.warmup):
         eng.iterate(1, w + 1, 0.0)
+    shapes = eng.autotune(3) if not args.no_autotune else None
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:
@@ -348,7 +350,9 @@ def main():
         "dtype": "f64" if prec == abi.FP64 else "f32+f64", "data": "synthetic",
         "config": {"workload": f"{args.case}: {ncell} cells, SST + IAPWS + Merkle, BDF2, LU-SGS",
                    "cells": ncell, "precision": args.precision, "blocks": len(blocks),
-                   "l2": "working set >> 129 MB L2 (no flush needed)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+                   "l2": "working set >> 129 MB L2 (no flush needed)", "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "launch_shapes": None if shapes is None else {"face_threads": shapes[0], "rhs_threads": shapes[1],
+                                                                 "sweep_ctas_per_sm": shapes[2]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
                      "traffic": RHS_TRAFFIC_PER_CELL * ncell if prec == abi.MIXED else None,

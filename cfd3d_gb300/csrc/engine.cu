@@ -263,7 +263,7 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
 
 // ------------------------------------------------------------------ residual + sources
 template <bool MX>
-__global__ void __launch_bounds__(128) k_rhs(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
   int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
@@ -961,8 +961,8 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   if (c.mixed) launch_face_flux_mixed(E, s);
   else launch_face_flux(E, s);
   stage(3);
-  if (c.mixed) k_rhs<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
-  else k_rhs<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+  if (c.mixed) k_rhs<true><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+  else k_rhs<false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
   stage(4);
   n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
@@ -1064,6 +1064,27 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   return true;
 }
 
+}  // namespace
+
+namespace {
+// ms per call of `fn` (launches on the engine's stream): one untimed call, then `reps`
+// timed between CUDA events
+template <class F>
+float time_calls(Engine& E, int reps, F fn) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  fn();
+  cudaEventRecord(a, E.st);
+  for (int r = 0; r < reps; ++r) fn();
+  cudaEventRecord(b, E.st);
+  cudaEventSynchronize(b);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / (float)std::max(reps, 1);
+}
 }  // namespace
 
 extern "C" {
@@ -1544,6 +1565,78 @@ int cfd3d_residual_vjp(cfd3d_handle* h, const double* cot, double* g_state, doub
     CFD_CUDA(cudaMemcpyAsync(g_params, E.adj_gpar, 3 * 8, cudaMemcpyDeviceToHost, E.st));
     CFD_CUDA(cudaStreamSynchronize(E.st));
   }
+  return CFD3D_OK;
+}
+
+int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
+  if (!h || reps < 1) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  const DevPtr& d = E.d;
+  const Par& c = E.par;
+  launch_iteration(E, false);   // boundary program, fluxes, residual and sweep records
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  const int cands[3] = {64, 128, 256};
+  // threads per CTA of the face kernels
+  int best = E.tpb_face;
+  float tbest = 1e30f;
+  for (int T : cands) {
+    E.tpb_face = T;
+    const float t = time_calls(E, reps, [&] {
+      if (c.mixed) launch_face_flux_mixed(E, E.st);
+      else launch_face_flux(E, E.st);
+    });
+    if (t < tbest) { tbest = t; best = T; }
+  }
+  E.tpb_face = best;
+  // threads per CTA of the residual kernel
+  best = E.tpb_rhs;
+  tbest = 1e30f;
+  for (int T : cands) {
+    const float t = time_calls(E, reps, [&] {
+      if (c.mixed) k_rhs<true><<<nblk_of(E.nint, T), T, 0, E.st>>>(d, c);
+      else k_rhs<false><<<nblk_of(E.nint, T), T, 0, E.st>>>(d, c);
+    });
+    if (t < tbest) { tbest = t; best = T; }
+  }
+  E.tpb_rhs = best;
+  // persistent CTAs per SM of the dataflow sweeps (up to the occupancy limit)
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, true>, SW_CH, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, false>, SW_CH, 0);
+  int bestg = E.sweep_grid;
+  tbest = 1e30f;
+  for (int m = 1; m <= std::max(per, 1); ++m) {
+    if (m > 2 && m % 2) continue;   // 1, 2, 4, 6, ...
+    const int grid = std::max(1, std::min(m * nsm, d.nchunk));
+    const float t = time_calls(E, reps, [&] {
+      cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), E.st);
+      cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), E.st);
+      if (c.mixed) k_sweep_df<true, true><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
+      else k_sweep_df<true, false><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
+      cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), E.st);
+      if (c.mixed) k_sweep_df<false, true><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
+      else k_sweep_df<false, false><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
+    });
+    if (t < tbest) { tbest = t; bestg = grid; }
+  }
+  E.sweep_grid = bestg;
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  Scalars sc;
+  int rc = read_scalars(E, sc);
+  if (rc) return rc;
+  if (sc.sweep_stall) {
+    int zero = 0;
+    CFD_CUDA(cudaMemcpy(&E.d.sc->sweep_stall, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    E.err = "a dataflow sweep's wait for a neighbour cell ran out";
+    return CFD3D_ERR_TIMEOUT;
+  }
+  // the iteration graph is captured again with the new shapes
+  if (E.graph) { cudaGraphExecDestroy(E.graph); E.graph = nullptr; }
+  E.graph_ready = 0;
+  if (choice) { choice[0] = E.tpb_face; choice[1] = E.tpb_rhs; choice[2] = (E.sweep_grid + nsm - 1) / std::max(nsm, 1); }
   return CFD3D_OK;
 }
 

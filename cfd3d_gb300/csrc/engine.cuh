@@ -120,6 +120,9 @@ struct Engine {
   int* d_chunk_of = nullptr;
   int sweep_grid = 0;          // persistent CTAs of the dataflow sweep
   int sweep_planes = 0;        // 1: one launch per hyperplane instead (CFD3D_SWEEP=planes)
+  // launch shapes chosen by cfd3d_autotune: threads per CTA of the face kernels and of the
+  // residual kernel (64, 128 or 256)
+  int tpb_face = 128, tpb_rhs = 128;
   cudaStream_t st = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_ready = 0;

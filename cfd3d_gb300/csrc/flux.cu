@@ -10,7 +10,7 @@ namespace cfd {
 
 // ------------------------------------------------------------------ face fluxes
 template <int DIR>
-__global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256) k_face_flux(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   // flat face numbering per direction: block-major, then (k, j, i) of the left cell
   int b = 0;
@@ -122,8 +122,8 @@ __global__ void __launch_bounds__(128) k_face_flux(DevPtr d, Par c) {
 
 
 void launch_face_flux(const Engine& E, cudaStream_t s) {
-  const int T = 128;
-  auto nb = [](long long n) { return (unsigned)((n + 127) / 128); };
+  const int T = E.tpb_face;
+  auto nb = [T](long long n) { return (unsigned)((n + T - 1) / T); };
   k_face_flux<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
   k_face_flux<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
   k_face_flux<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);

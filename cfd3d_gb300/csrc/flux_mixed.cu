@@ -56,7 +56,7 @@ __device__ __forceinline__ FaceIdx face_of(const DevPtr& d, long long t) {
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(128) k_recon_mx(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
   const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
   if (!f.ok) return;
   const long long n = d.ncell, g = f.g, gr = g + f.sn;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(128) k_recon_mx(DevPtr d, Par c) {
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(128) k_flux_mx(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
   const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
   if (!f.ok) return;
   const long long n = d.ncell, g = f.g, gr = g + f.sn;
@@ -225,8 +225,8 @@ __global__ void __launch_bounds__(128) k_flux_mx(DevPtr d, Par c) {
 }
 
 void launch_face_flux_mixed(const Engine& E, cudaStream_t s) {
-  const int T = 128;
-  auto nb = [](long long n) { return (unsigned)((n + 127) / 128); };
+  const int T = E.tpb_face;
+  auto nb = [T](long long n) { return (unsigned)((n + T - 1) / T); };
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);

@@ -53,6 +53,7 @@ def lib():
     L.cfd3d_grid_metrics.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_residual_vjp.argtypes = [H, dp, dp, dp]
     L.cfd3d_sweep_stall_test.argtypes = [H]
+    L.cfd3d_autotune.argtypes = [H, C.c_int, ip]
     L.cfd3d_eos_eval.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
     L.cfd3d_eos_eval_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
     L.cfd3d_stats.argtypes = [H, C.POINTER(C.c_int64), ip]
@@ -65,7 +66,7 @@ def lib():
 
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
            "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_iterate", "cfd3d_iterate_n",
-           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
+           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device"]
 STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
 
@@ -200,6 +201,13 @@ class Engine:
             g.append(out[off:off + m].reshape(s))
             off += m
         return g, gpar
+
+    def autotune(self, reps=3):
+        """cfd3d_autotune: returns (face threads per CTA, residual threads per CTA, sweep
+        CTAs per SM) chosen by timing on the current state."""
+        ch = (C.c_int * 3)()
+        self._check(lib().cfd3d_autotune(self.h, reps, ch))
+        return tuple(ch)
 
     def sweep_stall_test(self):
         """cfd3d_sweep_stall_test: the status code (CFD3D_ERR_TIMEOUT expected)."""

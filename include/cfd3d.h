@@ -160,6 +160,15 @@ int  cfd3d_residual(cfd3d_handle *h, int block, double *res, double *icav, doubl
  * it serves gradient checks of the residual. */
 int  cfd3d_residual_vjp(cfd3d_handle *h, const double *cot, double *g_state, double *g_params);
 
+/* Launch-shape autotuner (no counterpart in the reference).  On the current state it
+ * times, with CUDA events over `reps` calls each, the face-flux kernels and the residual
+ * kernel at 64, 128 and 256 threads per CTA and the dataflow sweeps at 1, 2, 4, ... persistent
+ * CTAs per SM (up to the occupancy limit), keeps the fastest of each, and re-captures the
+ * iteration graph at the next iteration.  choice (may be NULL) receives the threads per
+ * CTA of the face and residual kernels and the sweep CTAs per SM.  Results do not depend on
+ * the shapes: each thread's arithmetic is unchanged. */
+int  cfd3d_autotune(cfd3d_handle *h, int reps, int *choice);
+
 /* Test hook of the dataflow sweeps' bounded waits (no counterpart in the reference): one
  * forward sweep on the current state's records in which the first chunk of cells never
  * signals completion, with a short wait limit.  The cells that depend on it give up
