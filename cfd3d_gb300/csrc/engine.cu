@@ -107,6 +107,16 @@ __global__ void k_unsteady_shift(DevPtr d, Par c) {
 }
 
 // ------------------------------------------------------------------ local time step
+// the viscous eigenvalue term of eigenvis_of in FP32 (the mixed form's time step)
+__device__ __forceinline__ float eigenvis_f(const Par& c, const float* dv, const float* tv) {
+  if (c.iturb == -3) return 0.0f;
+  const float den = dv[7] + dv[11] * dv[6] * dv[0] - dv[10] * dv[7] * dv[0];
+  if (c.iturb == -2) return fmaxf(dv[6] * tv[1] / den, (4.0f / 3.0f) * tv[0] / dv[0]);
+  return fmaxf(dv[6] * (tv[1] + dv[11] * tv[2] * (1.0f / 0.9f)) / den, (4.0f / 3.0f) * (tv[0] + tv[2]) / dv[0]);
+}
+
+// MX: the local time step only scales the implicit operator -- FP32 on the FP32 metrics
+template <bool MX>
 __global__ void k_timestep(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   double dtv = 1.0e10;
@@ -116,6 +126,33 @@ __global__ void k_timestep(DevPtr d, Par c) {
     long long g = interior_cell(B, t - B.int_off, i, j, k);
     if (c.local == -1) {
       dtv = c.cfl;
+    } else if (MX) {
+      const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+      const float u = (float)d.pv[n + g], v = (float)d.pv[2 * n + g], w = (float)d.pv[3 * n + g];
+      float dvf[12], tvf[3] = {0.0f, 0.0f, 0.0f};
+      for (int q = 0; q < 12; ++q) dvf[q] = (float)d.dv[q * n + g];
+      for (int q = 0; q < c.ntv; ++q) tvf[q] = (float)d.tv[q * n + g];
+      const float* G = d.gmf;
+      const float vol = G[GM_GRD * n + g];
+      float cs[3][3];
+      for (int q = 0; q < 3; ++q) {
+        cs[0][q] = 0.5f * (G[(GM_CX + q) * n + g - 1] + G[(GM_CX + q) * n + g]);
+        cs[1][q] = 0.5f * (G[(GM_EX + q) * n + g - sj] + G[(GM_EX + q) * n + g]);
+        cs[2][q] = 0.5f * (G[(GM_TX + q) * n + g - sk] + G[(GM_TX + q) * n + g]);
+      }
+      const float sndp2 = sndp2_of<float>(c, dvf[5], u * u + v * v + w * w);
+      const float qf = sndp2 / dvf[5];
+      float eig = 0.0f, ss = 0.0f;
+      for (int q = 0; q < 3; ++q) {
+        const float uc = fabsf(cs[q][0] * u + cs[q][1] * v + cs[q][2] * w);
+        const float s2 = cs[q][0] * cs[q][0] + cs[q][1] * cs[q][1] + cs[q][2] * cs[q][2];
+        const float up = uc * (1.0f + qf);
+        const float dd = sqrtf(uc * uc * (1.0f - qf) * (1.0f - qf) + 4.0f * sndp2 * s2);
+        eig += 0.5f * (up + dd);
+        ss += s2;
+      }
+      const float ev = eigenvis_f(c, dvf, tvf) * ss / vol;
+      dtv = (double)((float)c.cfl * vol / (eig + 4.0f * ev));
     } else {
       const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
       double u = d.pv[n + g], v = d.pv[2 * n + g], w = d.pv[3 * n + g];
@@ -801,6 +838,8 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
   }
 }
 
+// MX: FP32, with the velocity gradients formed from u - U (exact differences)
+template <bool MX>
 __global__ void k_eddy(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
@@ -814,6 +853,37 @@ __global__ void k_eddy(DevPtr d, Par c) {
     fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
     fa[2][q] = d.gm[(GM_EX + q) * n + g - sj]; fa[3][q] = d.gm[(GM_EX + q) * n + g];
     fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
+  }
+  if (MX) {
+    const float* G = d.gmf;
+    float fa[6][3];
+    for (int q = 0; q < 3; ++q) {
+      fa[0][q] = G[(GM_CX + q) * n + g - 1]; fa[1][q] = G[(GM_CX + q) * n + g];
+      fa[2][q] = G[(GM_EX + q) * n + g - sj]; fa[3][q] = G[(GM_EX + q) * n + g];
+      fa[4][q] = G[(GM_TX + q) * n + g - sk]; fa[5][q] = G[(GM_TX + q) * n + g];
+    }
+    const float ivol = 1.0f / G[GM_GRD * n + g];
+    float gr[3][3];
+    for (int q = 0; q < 3; ++q) {
+      const double* P = d.pv + (1 + q) * n;
+      const double U = c.uref_vec[q];
+      const float c0 = (float)(P[g] - U);
+      float vv[6];
+      for (int m = 0; m < 6; ++m) vv[m] = 0.5f * ((float)(P[nbr[m]] - U) + c0);
+      for (int e = 0; e < 3; ++e)
+        gr[q][e] = (vv[1] * fa[1][e] + vv[3] * fa[3][e] + vv[5] * fa[5][e] - vv[0] * fa[0][e] - vv[2] * fa[2][e] - vv[4] * fa[4][e]) * ivol;
+    }
+    const float kk = (float)d.pv[7 * n + g], oo = (float)d.pv[8 * n + g], rho = (float)d.dv[g], mu = (float)d.tv[g];
+    const float y5 = G[(GM_GRD + 4) * n + g];
+    const float term1 = sqrtf(kk) / (0.09f * oo * y5);
+    const float term2 = 500.0f * mu / rho / (oo * y5 * y5);
+    const float arg2 = fmaxf(2.0f * term1, term2);
+    const float bigf2 = tanhf(arg2 * arg2);
+    const float sij = gr[0][0] * gr[0][0] + gr[1][1] * gr[1][1] + gr[2][2] * gr[2][2] +
+                      0.5f * (sq(gr[0][1] + gr[1][0]) + sq(gr[0][2] + gr[2][0]) + sq(gr[1][2] + gr[2][1]));
+    const float sss = sqrtf(2.0f * sij);
+    d.tv[2 * n + g] = (double)(0.31f * rho * kk / fmaxf(0.31f * oo, sss * bigf2));
+    return;
   }
   double vol = d.gm[GM_GRD * n + g], ivol = 1.0 / vol;
   double gr[3][3];
@@ -953,7 +1023,11 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   int n = 0;
   auto stage = [&](int q) { if (mark) cudaEventRecord(mark[q], s); };
   stage(0);
-  if (full) { k_timestep<<<nblk_of(E.nint, 256), 256, 0, s>>>(d, c); ++n; }
+  if (full) {
+    if (c.mixed) k_timestep<true><<<nblk_of(E.nint, 256), 256, 0, s>>>(d, c);
+    else k_timestep<false><<<nblk_of(E.nint, 256), 256, 0, s>>>(d, c);
+    ++n;
+  }
   stage(1);
   for (int p = 0; p < 3; ++p)
     if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
@@ -1003,7 +1077,11 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   else k_update<false><<<E.red_grid, T, 0, s>>>(d, c);
   ++n;
   stage(7);
-  if (c.iturb == 0) { k_eddy<<<nblk_of(E.nint, T), T, 0, s>>>(d, c); ++n; }
+  if (c.iturb == 0) {
+    if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+    else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+    ++n;
+  }
   k_finish<<<1, FIN_T, 0, s>>>(d, c, E.red_grid);
   ++n;
   stage(8);
