@@ -125,6 +125,25 @@ __device__ __noinline__ void iapws_liq_df64(double p, double t, Phase<double>& l
   if constexpr (FULL) { l.drdp = (double)lx.drdp; l.drdt = (double)lx.drdt; l.dhdp = (double)lx.dhdp; l.dhdt = (double)lx.dhdt; }
 }
 
+// The mixed form's face-state EOS: 1/rho and h of the liquid (and of the vapour when VAP)
+// from the df64 sums, the reciprocal also taken in df64 (on the FP32 pipes: an FP64
+// division costs a GB300 far more)
+template <bool VAP>
+__device__ __noinline__ void iapws_inv_df64(double p, double t, bool meta, double* il, double* hl, double* iv,
+                                            double* hv) {
+  const df64 P(p), T(t), one(1.0f, 0.0f);
+  Phase<df64> lx;
+  iapws_l<df64, false>(P, T, lx);
+  *il = (double)(one / lx.rho);
+  *hl = (double)lx.h;
+  if constexpr (VAP) {
+    Phase<df64> vx;
+    iapws_v_meta<df64, false>(P, T, meta, vx);
+    *iv = (double)(one / vx.rho);
+    *hv = (double)vx.h;
+  }
+}
+
 // Phase properties of liquid and vapour.  MX evaluates the IF97 Gibbs sums in df64 (the
 // mixed form); FULL = false evaluates only rho and h.  The metastable branch test
 // p > p_sat(T) is taken in FP64 in both forms so that they select the same term set.
@@ -236,6 +255,20 @@ __device__ __forceinline__ void deteos_simple(int fluid, double p, double t, dou
 // the reconstructed face states; the same operations as the rho, h of deteos_simple
 template <bool MX = false>
 __device__ __forceinline__ void eos_rho_h(int fluid, double p, double t, double y1, double y2, double& rho, double& h) {
+  if constexpr (MX) {
+    if (fluid != 1) {
+      // phase reciprocals in df64 (the gas's as t / (p r1)); the mixture sums and its one
+      // reciprocal in FP64
+      double il, hl, iv = 0.0, hv = 0.0;
+      if (y1 != 0.0) iapws_inv_df64<true>(p, t, p > h2o_pww(t), &il, &hl, &iv, &hv);
+      else iapws_inv_df64<false>(p, t, false, &il, &hl, &iv, &hv);
+      const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
+      const double yl = 1.0 - y1 - y2;
+      rho = 1.0 / (yl * il + y1 * iv + y2 * ig);
+      h = yl * hl + y1 * hv + y2 * (1004.64 * t);
+      return;
+    }
+  }
   Phase<double> l, v, g;
   phases<MX, false>(fluid, p, t, l, v, y1 != 0.0);
   ideal_gas(p, t, g);
