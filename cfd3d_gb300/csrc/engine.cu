@@ -630,6 +630,19 @@ __global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, lon
 // also ends every other wait, so the launch completes and the host reports
 // CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose flag is never raised (the stall
 // test).
+// the dataflow sweeps' done flags: a release store by the CTA's first thread after a
+// barrier publishes the whole CTA's dq (release is cumulative over what the barrier
+// ordered before it), an acquire load followed by a barrier makes them visible to all
+// threads of the consuming CTA
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
+
 // what a dataflow sweep cell reads of one neighbour before its dq is known
 template <class T>
 struct SweepNb {
@@ -720,16 +733,14 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
     // ---- wait: thread k polls chunks lo + k, lo + k + SW_CH, ... (none when no cell of
     // the chunk has a neighbour: then hi = -1 and lo is not a chunk index)
     for (int cn = (hi >= 0) ? lo + (int)threadIdx.x : 0; hi >= 0 && cn <= hi; cn += SW_CH) {
-      const volatile int* f = d.done + cn;
       long long it = 0;
-      while (*f == 0) {
+      while (ld_acquire(d.done + cn) == 0) {
         ++it;
         if ((it & 63) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
         if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
         if (it > 8) __nanosleep(32);
       }
     }
-    __threadfence();
     __syncthreads();
     if (live) {
       if constexpr (MX) {
@@ -749,9 +760,8 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
       for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
       if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
     }
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0 && ch != withhold) atomicExch(d.done + ch, 1);
+    if (threadIdx.x == 0 && ch != withhold) st_release(d.done + ch, 1);
   }
 }
 
