@@ -978,6 +978,11 @@ __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, lo
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q < m) b[q] = (float)a[q];
 }
+__global__ void k_lo_f32(const double* __restrict__ a, const float* __restrict__ hi, float* __restrict__ lo,
+                         long long m) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < m) lo[q] = (float)(a[q] - (double)hi[q]);
+}
 
 __global__ void k_interior_io(double* __restrict__ a, int nv, BlockGeom B, double* __restrict__ soa, long long ncell,
                               int to_soa) {
@@ -1363,12 +1368,21 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
       for (int v = 0; v < NPVM; ++v) E.par.phi[v][e] = m * sc[v];
       for (int q = 0; q < 3; ++q) E.par.phi[1 + q][e] = m * U[q];
     }
+    auto split = [](double x, float* o) { o[0] = (float)x; o[1] = (float)(x - (double)o[0]); };
+    split(dvr[0], E.par.rhoref2);
+    split(dvr[1], E.par.href2);
+    for (int e = 0; e < 3; ++e) { split(U[e], E.par.U2[e]); split(dvr[0] * U[e], E.par.m2[e]); }
+    for (int v = 0; v < NPVM; ++v) split((v >= 1 && v <= 3) ? U[v - 1] : sc[v], E.par.sc2[v]);
   }
   if (!setup_geometry(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
   if (c.mixed) {
     const long long m = (long long)(GM_GRD + c.ngrd) * E.ncell;
     if (cudaMalloc(&E.d.gmf, (size_t)m * 4) != cudaSuccess) { E.err = "device allocation failed (gmf)"; return CFD3D_ERR_NOMEM; }
     k_to_f32<<<nblk_of(m, 256), 256, 0, E.st>>>(E.d.gm, E.d.gmf, m);
+    // the face vectors' low parts: gm = gmf + gmlo to ~1e-14 (the df64 flux terms)
+    const long long m9 = (long long)GM_GRD * E.ncell;
+    if (cudaMalloc(&E.d.gmlo, (size_t)m9 * 4) != cudaSuccess) { E.err = "device allocation failed (gmlo)"; return CFD3D_ERR_NOMEM; }
+    k_lo_f32<<<nblk_of(m9, 256), 256, 0, E.st>>>(E.d.gm, E.d.gmf, E.d.gmlo, m9);
     CFD_CUDA(cudaStreamSynchronize(E.st));
   }
   if (!setup_ghost_program(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
@@ -1407,7 +1421,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
                     E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
   for (double* p : bufs) cudaFree(p);
-  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf};
+  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf, E.d.gmlo};
   for (float* p : fbufs) cudaFree(p);
   cudaFree((void*)E.d.blk);
   cudaFree(E.d.sc);

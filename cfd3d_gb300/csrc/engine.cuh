@@ -70,6 +70,7 @@ struct DevPtr {
   // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
   float *pvf, *fi32, *fv32;
   float* gmf;        // mixed form: FP32 copy of gm (metrics of the FP32 viscous and SST terms)
+  float* gmlo;       // mixed form: low parts of the face vectors, gm = gmf + gmlo (df64 terms)
   float* frec;       // mixed form: reconstructed face states of one direction (2 x 12 planes)
   // LU-SGS sweep records in plane-major order t (REC_* planes of nint entries); dqs and
   // dcv are plane-major too

@@ -107,32 +107,34 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
   const int npv = c.npv;
   const float* P = d.pvf;
   const int fplane = (DIR == 0) ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
-  double nv[3];
-  for (int q = 0; q < 3; ++q) nv[q] = d.gm[(fplane + q) * n + g];
+  df64 nv[3];
+  for (int q = 0; q < 3; ++q) nv[q] = df64(d.gmf[(fplane + q) * n + g], d.gmlo[(fplane + q) * n + g]);
   FaceMx L, R;
   {
     const float* F = d.frec;
     for (int v = 0; v < npv; ++v) { L.g[v] = F[v * n + g]; R.g[v] = F[(FREC_SIDE + v) * n + g]; }
-    L.rho = c.rhoref + (double)F[NPVM * n + g];
-    L.h = c.href + (double)F[(NPVM + 1) * n + g];
+    const df64 rref = dfp(c.rhoref2), href = dfp(c.href2);
+    L.rho = rref + dff(F[NPVM * n + g]);
+    L.h = href + dff(F[(NPVM + 1) * n + g]);
     L.c2 = F[(NPVM + 2) * n + g];
-    R.rho = c.rhoref + (double)F[(FREC_SIDE + NPVM) * n + g];
-    R.h = c.href + (double)F[(FREC_SIDE + NPVM + 1) * n + g];
+    R.rho = rref + dff(F[(FREC_SIDE + NPVM) * n + g]);
+    R.h = href + dff(F[(FREC_SIDE + NPVM + 1) * n + g]);
     R.c2 = F[(FREC_SIDE + NPVM + 2) * n + g];
-    for (int q = 0; q < 3; ++q) { L.u[q] = c.uref_vec[q] + (double)L.g[1 + q]; R.u[q] = c.uref_vec[q] + (double)R.g[1 + q]; }
+    for (int q = 0; q < 3; ++q) { L.u[q] = dfp(c.U2[q]) + dff(L.g[1 + q]); R.u[q] = dfp(c.U2[q]) + dff(R.g[1 + q]); }
   }
   // Roe-average state (sqrt(rho) weights; p and T arithmetic means) and its FP32 sound speed
   float ravg_u[3], ravg_s[NPVM];
   float rc2 = 0.0f;
   {
-    float srl = sqrtf((float)L.rho), srr = sqrtf((float)R.rho);
+    float srl = sqrtf(tof(L.rho)), srr = sqrtf(tof(R.rho));
     float rd = 1.0f / (srl + srr);
-    for (int q = 0; q < 3; ++q) ravg_u[q] = (float)c.uref_vec[q] + (srl * L.g[1 + q] + srr * R.g[1 + q]) * rd;
+    for (int q = 0; q < 3; ++q) ravg_u[q] = c.U2[q][0] + (srl * L.g[1 + q] + srr * R.g[1 + q]) * rd;
     for (int q = 0; q < NPVM; ++q) ravg_s[q] = 0.0f;
     for (int q = 5; q < npv; ++q) ravg_s[q] = (srl * L.g[q] + srr * R.g[q]) * rd;
-    if (nv[0] != 0.0 || nv[1] != 0.0 || nv[2] != 0.0) {
-      float pa = (float)(c.pref + 0.5 * ((double)L.g[0] + (double)R.g[0]));
-      float ta = (float)(c.tref + 0.5 * ((double)L.g[4] + (double)R.g[4]));
+    if (nv[0].hi != 0.0f || nv[1].hi != 0.0f || nv[2].hi != 0.0f) {
+      // the FP32 sound speed of the Roe average: FP32 state
+      const float pa = (float)c.pref + 0.5f * (L.g[0] + R.g[0]);
+      const float ta = (float)c.tref + 0.5f * (L.g[4] + R.g[4]);
       rc2 = eos_c2_f(c.fluid, pa, ta, ravg_s[5], ravg_s[6], &d.sc->snd2_fallbacks);
     }
   }
@@ -141,10 +143,10 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
 #pragma unroll
     for (int l = 0; l < 18; ++l) sdst[l] = P[stencil_cell(l, g, sn, s1, s2)];
   }
-  double fx[NPVM];
+  float fx[NPVM];
   inviscid_flux_mx(c, nv, L, R, sdst, rc2, ravg_u, ravg_s, fx);
   float* fo = d.fi32 + (long long)DIR * npv * n;
-  for (int v = 0; v < npv; ++v) fo[v * n + g] = (float)fx[v];
+  for (int v = 0; v < npv; ++v) fo[v * n + g] = fx[v];
   if (c.iturb == -3) return;
   // ---- viscous flux in FP32 (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
   const bool turb = (c.iturb == 0);

@@ -110,10 +110,14 @@ __device__ __forceinline__ void muscl_clip_mx(const Par& c, const float* c9, con
 // FP64 quantities the leading-order flux terms need.
 struct FaceMx {
   float g[NPVM];      // gauge primitives (p', u', v', w', T', y1, y2, k, omega)
-  double rho, h;      // mixture density and static enthalpy (FP64)
-  double u[3];        // full velocity (FP64)
+  df64 rho, h;        // mixture density and static enthalpy (df64, ~1e-14)
+  df64 u[3];          // full velocity (df64: U + u', exact)
   float c2;           // face sound speed (Roe-M and AUSMPW+ pressure sensor only)
 };
+
+__device__ __forceinline__ float tof(df64 a) { return __fadd_rn(a.hi, a.lo); }
+__device__ __forceinline__ df64 dfp(const float* p2) { return df64(p2[0], p2[1]); }
+__device__ __forceinline__ df64 dff(float a) { return df64(a, 0.0f); }
 
 // per-face record written by the reconstruction kernel: for each side
 // g[0..npv-1], rho - rho_ref, h - h_ref, c2
@@ -138,50 +142,53 @@ __device__ __forceinline__ float sdst_ratio_min_f(const float* s) {
 // sdst the gauge pressures of the 18 stencil cells (schemes 2 and 3), rc2 the FP32
 // sound speed of the Roe-average state, ravg_u its full velocity and ravg_s its
 // primitives (scalars k >= 5 used).
-__device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv, const FaceMx& L, const FaceMx& R,
+__device__ __forceinline__ void inviscid_flux_mx(const Par& c, const df64* nv, const FaceMx& L, const FaceMx& R,
                                                  const float* sdst, float rc2, const float* ravg_u,
-                                                 const float* ravg_s, double* fx) {
+                                                 const float* ravg_s, float* fx) {
   const int npv = c.npv;
-  // The FP64 leading-order terms use the unnormalised face vector nv (|nv| = dl): the
-  // normal velocities unl = nv . u are the fluxes' transport velocities times dl, so no
-  // FP64 square root or division is needed; the FP32 terms use the unit normal and are
-  // scaled by the FP32 length dlf.
-  const float nvf[3] = {(float)nv[0], (float)nv[1], (float)nv[2]};
+  // The leading-order terms are df64 (float-float on the FP32 pipes, ~1e-14) on the
+  // unnormalised face vector nv (|nv| = dl): the normal velocities unl = nv . u are the
+  // fluxes' transport velocities times dl, so no square root or division is needed; the
+  // FP32 terms use the unit normal and are scaled by the FP32 length dlf.  The result is
+  // the face flux minus the free-stream flux Phi . nv, rounded once to FP32.
+  const float nvf[3] = {nv[0].hi, nv[1].hi, nv[2].hi};
   const float dlf = sqrtf(nvf[0] * nvf[0] + nvf[1] * nvf[1] + nvf[2] * nvf[2]);
   if (dlf == 0.0f) {
-    for (int k = 0; k < npv; ++k) fx[k] = 0.0;
+    for (int k = 0; k < npv; ++k) fx[k] = 0.0f;
     return;
   }
+  df64 fd[NPVM];
   const float idlf = 1.0f / dlf;
   const float nf[3] = {nvf[0] * idlf, nvf[1] * idlf, nvf[2] * idlf};
   const float* pl = L.g;
   const float* pr = R.g;
-  // FP64 leading-order quantities
-  const double unl = nv[0] * L.u[0] + nv[1] * L.u[1] + nv[2] * L.u[2];
-  const double unr = nv[0] * R.u[0] + nv[1] * R.u[1] + nv[2] * R.u[2];
-  const double HL = L.h + 0.5 * (L.u[0] * L.u[0] + L.u[1] * L.u[1] + L.u[2] * L.u[2]);
-  const double HR = R.h + 0.5 * (R.u[0] * R.u[0] + R.u[1] * R.u[1] + R.u[2] * R.u[2]);
+  // df64 leading-order quantities
+  const df64 unl = nv[0] * L.u[0] + nv[1] * L.u[1] + nv[2] * L.u[2];
+  const df64 unr = nv[0] * R.u[0] + nv[1] * R.u[1] + nv[2] * R.u[2];
+  const df64 half(0.5f, 0.0f);
+  const df64 HL = L.h + half * (L.u[0] * L.u[0] + L.u[1] * L.u[1] + L.u[2] * L.u[2]);
+  const df64 HR = R.h + half * (R.u[0] * R.u[0] + R.u[1] * R.u[1] + R.u[2] * R.u[2]);
   // FP32 copies (unit-normal velocities) and accurate jumps
-  const float uull = (float)unl * idlf, uurr = (float)unr * idlf;
-  const float rl = (float)L.rho, rr = (float)R.rho;
-  const float drho = (float)(R.rho - L.rho);
-  const float dH = (float)(HR - HL);
-  const float dun = (float)(unr - unl) * idlf;
-  const float ulf[3] = {(float)L.u[0], (float)L.u[1], (float)L.u[2]};
-  const float hlf = (float)HL;
+  const float uull = tof(unl) * idlf, uurr = tof(unr) * idlf;
+  const float rl = tof(L.rho), rr = tof(R.rho);
+  const float drho = tof(R.rho - L.rho);
+  const float dH = tof(HR - HL);
+  const float dun = tof(unr - unl) * idlf;
+  const float ulf[3] = {tof(L.u[0]), tof(L.u[1]), tof(L.u[2])};
+  const float hlf = tof(HL);
   float du3[3];
   for (int q = 0; q < 3; ++q) du3[q] = pr[1 + q] - pl[1 + q];   // gauge differences are the velocity jumps
   const float dp = pr[0] - pl[0];
   const float rrho = sqrtf(rl * rr);
-  // free-stream flux through the face, subtracted from every scheme's result
-  double phin[NPVM];
-  for (int k = 0; k < npv; ++k) phin[k] = c.phi[k][0] * nv[0] + c.phi[k][1] * nv[1] + c.phi[k][2] * nv[2];
+  // free-stream flux through the face, Phi . nv = (m . nv) s, subtracted from every
+  // scheme's result (m = rho_ref U, s = (1, U, H_ref, y_ref, k_ref, omega_ref))
+  const df64 mn = dfp(c.m2[0]) * nv[0] + dfp(c.m2[1]) * nv[1] + dfp(c.m2[2]) * nv[2];
 
   if (c.nscheme == 1 || c.nscheme == 2) {
     const float u2 = ravg_u[0] * ravg_u[0] + ravg_u[1] * ravg_u[1] + ravg_u[2] * ravg_u[2];
     const float uuu = nf[0] * ravg_u[0] + nf[1] * ravg_u[1] + nf[2] * ravg_u[2];
     const float srl = sqrtf(rl), srr = sqrtf(rr);
-    const float ravg_ht = (srl * (float)HL + srr * (float)HR) / (srl + srr);
+    const float ravg_ht = (srl * tof(HL) + srr * tof(HR)) / (srl + srr);
     if (c.nscheme == 1) {
       // Roe: central part in FP64, dissipation in FP32
       float sndp2 = sndp2_of<float>(c, rc2, u2);
@@ -194,20 +201,20 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
       float dpp = m_star * dp + (c_star - fabsf(uuu) + 0.5f * (1.0f - q) * uuu * m_star) * rrho * dun;
       float au = fabsf(uuu);
       // mass fluxes times dl
-      const double mL = L.rho * unl, mR = R.rho * unr;
-      fx[0] = 0.5 * (mL + mR - (double)(dlf * (au * drho + du * rrho)));
+      const df64 mL = L.rho * unl, mR = R.rho * unr;
+      fd[0] = half * (mL + mR - dff(dlf * (au * drho + du * rrho)));
       for (int q3 = 0; q3 < 3; ++q3) {
         // rho_R u_R - rho_L u_L = rho_R (u_R - u_L) + (rho_R - rho_L) u_L
         float df = au * (rr * du3[q3] + drho * ulf[q3]) + du * rrho * ravg_u[q3] + dpp * nf[q3];
-        fx[1 + q3] = 0.5 * (mL * L.u[q3] + mR * R.u[q3] + nv[q3] * ((double)pl[0] + (double)pr[0]) - (double)(dlf * df));
+        fd[1 + q3] = half * (mL * L.u[q3] + mR * R.u[q3] + nv[q3] * (dff(pl[0]) + dff(pr[0])) - dff(dlf * df));
       }
       float df4 = au * (rr * dH + drho * hlf - dp) + du * rrho * ravg_ht + dpp * uuu;
-      fx[4] = 0.5 * (mL * HL + mR * HR - (double)(dlf * df4));
+      fd[4] = half * (mL * HL + mR * HR - dff(dlf * df4));
       for (int k = 5; k < npv; ++k) {
         float df = au * (rr * (pr[k] - pl[k]) + drho * pl[k]) + du * rrho * ravg_s[k];
-        fx[k] = 0.5 * (mL * (double)pl[k] + mR * (double)pr[k] - (double)(dlf * df));
+        fd[k] = half * (mL * dff(pl[k]) + mR * dff(pr[k]) - dff(dlf * df));
       }
-      for (int k = 0; k < npv; ++k) fx[k] = fx[k] - phin[k];
+      for (int k = 0; k < npv; ++k) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
       return;
     }
     // Roe-M
@@ -241,25 +248,25 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
     bdq[4] = bdq[0] * ravg_ht + rrho * dH;
     for (int k = 5; k < npv; ++k) bdq[k] = bdq[0] * ravg_s[k] + rrho * (pr[k] - pl[k]);
     // central part (b1 F_L - b2 F_R) / (b1 - b2) in FP64
-    // the weights b1 / (b1 - b2), b2 / (b1 - b2) in FP64 from FP32 wave speeds; fluxes
-    // times dl
-    const double B1 = b1, B2 = b2, iB = 1.0 / (B1 - B2);
-    const double w1 = B1 * iB, w2 = B2 * iB;
-    const double mL = L.rho * unl, mR = R.rho * unr;
-    double fl[NPVM], fr[NPVM];
+    // the weights b1 / (b1 - b2), b2 / (b1 - b2) in df64 from FP32 wave speeds (their
+    // difference is exact in df64); fluxes times dl
+    const df64 iB = dff(1.0f) / two_sum(b1, -b2);
+    const df64 w1 = dff(b1) * iB, w2 = dff(b2) * iB;
+    const df64 mL = L.rho * unl, mR = R.rho * unr;
+    df64 fl[NPVM], fr[NPVM];
     fl[0] = mL; fr[0] = mR;
     for (int q3 = 0; q3 < 3; ++q3) {
-      fl[1 + q3] = mL * L.u[q3] + nv[q3] * (double)pl[0];
-      fr[1 + q3] = mR * R.u[q3] + nv[q3] * (double)pr[0];
+      fl[1 + q3] = mL * L.u[q3] + nv[q3] * dff(pl[0]);
+      fr[1 + q3] = mR * R.u[q3] + nv[q3] * dff(pr[0]);
     }
     fl[4] = mL * HL; fr[4] = mR * HR;
-    for (int k = 5; k < npv; ++k) { fl[k] = mL * (double)pl[k]; fr[k] = mR * (double)pr[k]; }
+    for (int k = 5; k < npv; ++k) { fl[k] = mL * dff(pl[k]); fr[k] = mR * dff(pr[k]); }
     const float wdiss = dlf * b1 * b2 / (b1 - b2);
     for (int k = 0; k < npv; ++k)
-      fx[k] = w1 * fl[k] - w2 * fr[k] + (double)(wdiss * (dq[k] - gg * bdq[k] / add));
+      fd[k] = w1 * fl[k] - w2 * fr[k] + dff(wdiss * (dq[k] - gg * bdq[k] / add));
     for (int q3 = 0; q3 < 3; ++q3)
-      fx[1 + q3] += (double)(dlf * gg * b1_du * b2_du * rrho * dun * nf[q3] / aaa / (b1_du - b2_du));
-    for (int k = 0; k < npv; ++k) fx[k] = fx[k] - phin[k];
+      fd[1 + q3] += dff(dlf * gg * b1_du * b2_du * rrho * dun * nf[q3] / aaa / (b1_du - b2_du));
+    for (int k = 0; k < npv; ++k) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
     return;
   }
   // AUSM family: the interface velocity amid * M_1/2 = (u_L + u_R)/2 + small terms is
@@ -310,14 +317,14 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
   // amid * (M+ + M-) = (u_L + u_R)/2 + amid * E for subsonic ML, MR, with
   // E = (ML - MR)(ML + MR)(1/4 - 2 beta + beta (ML^2 + MR^2))
   // (times dl: vsum is the interface velocity times the face length)
-  double vsum;
+  df64 vsum;
   if (subl && subr)
-    vsum = 0.5 * (unl + unr) + (double)(dlf * amid * ((zml - zmr) * (zml + zmr) * ((0.25f - 2.0f * beta) + beta * (zml * zml + zmr * zmr))));
+    vsum = half * (unl + unr) + dff(dlf * amid * ((zml - zmr) * (zml + zmr) * ((0.25f - 2.0f * beta) + beta * (zml * zml + zmr * zmr))));
   else
-    vsum = (double)(dlf * amid * (zmpl + zmmr));
+    vsum = dff(dlf * amid * (zmpl + zmmr));
   // gauge interface pressure: P+ p'L + P- p'R + pref (P+ + P- - 1) - dissipation
   const float pdev = (float)(c.pref * ((double)dpl + (double)dpr));
-  double ml, mr;
+  df64 ml, mr;
   float pmid;
   if (c.nscheme == 3) {
     pmid = ppl * pl[0] + pmr * pr[0] + pdev - 2.0f * ppl * pmr * rrho * fmid1 * amid * dun;
@@ -333,31 +340,31 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const double* nv,
     float pwl = ((float)((double)pl[0] + c.pref) / pmt) * wq;
     float pwr = ((float)((double)pr[0] + c.pref) / pmt) * wq;
     float dpw = (dp / pmt) * wq;   // pwr - pwl from the gauge difference
-    if (vsum >= 0.0) {
+    if (vsum.hi >= 0.0f) {
       // both weights scaled by the left density, as the reference does
       float sc = rrho / rl;
       pwl *= sc; pwr *= sc; dpw *= sc;
       // M+_1 = (M+ + M-) + M- ((pwr - pwl) - ww (1 + pwr)), M-_1 = M- ww (1 + pwr)
-      ml = L.rho * (vsum + (double)(dlf * amid * zmmr * (dpw - ww * (1.0f + pwr))));
-      mr = R.rho * (double)(dlf * amid * zmmr * ww * (1.0f + pwr));
+      ml = L.rho * (vsum + dff(dlf * amid * zmmr * (dpw - ww * (1.0f + pwr))));
+      mr = R.rho * dff(dlf * amid * zmmr * ww * (1.0f + pwr));
     } else {
       float sc = rrho / rr;
       pwl *= sc; pwr *= sc; dpw *= sc;
-      ml = L.rho * (double)(dlf * amid * zmpl * ww * (1.0f + pwl));
-      mr = R.rho * (vsum + (double)(dlf * amid * zmpl * (-dpw - ww * (1.0f + pwl))));
+      ml = L.rho * dff(dlf * amid * zmpl * ww * (1.0f + pwl));
+      mr = R.rho * (vsum + dff(dlf * amid * zmpl * (-dpw - ww * (1.0f + pwl))));
     }
   } else {
     const float kp = 0.25f;
-    double vmid = vsum - (double)(dlf * amid * kp * fmaxf(1.0f - am2mid / rc2, 0.0f) * dp / rrho / rc2 / fmid);
+    const df64 vmid = vsum - dff(dlf * amid * kp * fmaxf(1.0f - am2mid / rc2, 0.0f) * dp / rrho / rc2 / fmid);
     pmid = ppl * pl[0] + pmr * pr[0] + pdev - 2.0f * ppl * pmr * rrho * fmid * amid * dun;
-    if (vmid > 0.0) { ml = L.rho * vmid; mr = 0.0; } else { mr = R.rho * vmid; ml = 0.0; }
+    if (vmid.hi > 0.0f) { ml = L.rho * vmid; mr = dff(0.0f); } else { mr = R.rho * vmid; ml = dff(0.0f); }
   }
   // ml, mr are mass fluxes times dl; the pressure acts on the face vector itself
-  fx[0] = ml + mr;
-  for (int q3 = 0; q3 < 3; ++q3) fx[1 + q3] = ml * L.u[q3] + mr * R.u[q3] + (double)pmid * nv[q3];
-  fx[4] = ml * HL + mr * HR;
-  for (int k = 5; k < npv; ++k) fx[k] = ml * (double)pl[k] + mr * (double)pr[k];
-  for (int k = 0; k < npv; ++k) fx[k] = fx[k] - phin[k];
+  fd[0] = ml + mr;
+  for (int q3 = 0; q3 < 3; ++q3) fd[1 + q3] = ml * L.u[q3] + mr * R.u[q3] + dff(pmid) * nv[q3];
+  fd[4] = ml * HL + mr * HR;
+  for (int k = 5; k < npv; ++k) fd[k] = ml * dff(pl[k]) + mr * dff(pr[k]);
+  for (int k = 0; k < npv; ++k) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
 }
 
 }  // namespace cfd

@@ -35,6 +35,9 @@ struct Par {
   // free stream, phi[v][e] = e-component of the flux of variable v (pressure part omitted)
   double href;
   double phi[NPVM][3];
+  // the same free-stream constants as float pairs (hi, lo) for the df64 flux terms:
+  // rho_ref, h_ref, U, m = rho_ref U, and s with Phi[v][e] = m[e] s[v]
+  float rhoref2[2], href2[2], U2[3][2], m2[3][2], sc2[NPVM][2];
 };
 
 template <class T>
