@@ -88,6 +88,8 @@ template <int N> __device__ __forceinline__ bool operator>(const Dual<N>& a, dou
 template <int N> __device__ __forceinline__ bool operator<=(const Dual<N>& a, double b) { return a.v <= b; }
 template <int N> __device__ __forceinline__ bool operator>=(const Dual<N>& a, double b) { return a.v >= b; }
 template <int N> __device__ __forceinline__ bool operator!=(const Dual<N>& a, double b) { return a.v != b; }
+template <int N> __device__ __forceinline__ bool operator!=(const Dual<N>& a, const Dual<N>& b) { return a.v != b.v; }
+template <int N> __device__ __forceinline__ bool operator==(const Dual<N>& a, const Dual<N>& b) { return a.v == b.v; }
 template <int N> __device__ __forceinline__ bool operator==(const Dual<N>& a, double b) { return a.v == b; }
 
 // elementary functions

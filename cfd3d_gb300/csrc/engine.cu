@@ -314,9 +314,27 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   if (MX) {
     // the stored FP32 fluxes are deviations from the free-stream flux: their differences
     // and sums in FP32 carry rounding of the order of the storage's own (one conversion to
-    // FP64 per variable instead of one per stored value)
+    // FP64 per variable instead of one per stored value).  The free-stream part adds back
+    // as -(m . sn) s, sn the cell's face-vector sum: zero up to the metrics' closure
+    // error, so it is formed in df64 from the face vectors' float pairs and applied in FP32.
+    float mnc, snf[3];
+    {
+      const int planes[3] = {GM_CX, GM_EX, GM_TX};
+      df64 mn = dff(0.0f);
+      for (int e = 0; e < 3; ++e) {
+        df64 se = dff(0.0f);
+        for (int q = 0; q < 3; ++q) {
+          const long long o1 = (planes[q] + e) * n + g, o0 = o1 - st[q];
+          se = se + (df64(d.gmf[o1], d.gmlo[o1]) - df64(d.gmf[o0], d.gmlo[o0]));
+        }
+        snf[e] = tof(se);
+        mn = mn + dfp(c.m2[e]) * se;
+      }
+      mnc = tof(mn);
+    }
     for (int v = 0; v < npv; ++v) {
-      float r = 0.0f;
+      float r = -(mnc * tof(dfp(c.sc2[v])));
+      if (v >= 1 && v <= 3) r -= (float)c.pref * snf[v - 1];
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
         const float* F = d.fi32 + ((long long)q * npv + v) * n;
@@ -357,32 +375,35 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     }
     res[v] = r;
   }
-  if (MX) {
-    // the stored mixed-form fluxes are F - (Phi + pref I).n dl; add the free-stream part
-    // back through the cell's face-vector sum (zero up to the metrics' closure error)
-    const int planes[3] = {GM_CX, GM_EX, GM_TX};
-    double sn[3];
-    for (int e = 0; e < 3; ++e) {
-      double s = 0.0;
-      for (int q = 0; q < 3; ++q) {
-        const double* G = d.gm + (planes[q] + e) * n;
-        s += G[g] - G[g - st[q]];
-      }
-      sn[e] = s;
-    }
-    for (int v = 0; v < npv; ++v) res[v] -= c.phi[v][0] * sn[0] + c.phi[v][1] * sn[1] + c.phi[v][2] * sn[2];
-    for (int e = 0; e < 3; ++e) res[1 + e] -= c.pref * sn[e];
-  }
+
   double pv2[NPVM], dv[NDV];
   for (int v = 0; v < npv; ++v) pv2[v] = d.pv[v * n + g];
   for (int v = 0; v < NDV; ++v) dv[v] = d.dv[v * n + g];
   const double vol = d.gm[GM_GRD * n + g];
   if (c.ncav) {
-    CavOut o = cavsource(c, pv2, dv, vol);
-    res[5] = res[5] + o.r_v - o.r_c;
-    for (int q = 0; q < 4; ++q) d.icav[q * n + g] = o.icav[q];
-    d.rcav[g] = o.r_c;
-    d.rcav[n + g] = o.r_v;
+    if (MX) {
+      // FP32 source (its rates reach the residual to ~1e-7 of their size) with the
+      // saturation pressure / temperature in FP64
+      double sat[2] = {0.0, 0.0};
+      if (pv2[4] < 647.096) {
+        if (c.ncav == 5) sat[1] = h2o_tww(pv2[0] + c.pref);
+        else sat[0] = h2o_pww(pv2[4]);
+      }
+      float p2f[NPVM], dvf[NDV];
+      for (int q = 0; q < NPVM; ++q) p2f[q] = (float)pv2[q];
+      for (int q = 0; q < NDV; ++q) dvf[q] = (float)dv[q];
+      const CavOutT<float> o = cavsource_t<float>(c, p2f, dvf, vol, (float)c.uref, (float)c.c_v, (float)c.c_c, sat);
+      res[5] = res[5] + (double)o.r_v - (double)o.r_c;
+      for (int q = 0; q < 4; ++q) d.icav[q * n + g] = o.icav[q];
+      d.rcav[g] = o.r_c;
+      d.rcav[n + g] = o.r_v;
+    } else {
+      CavOut o = cavsource(c, pv2, dv, vol);
+      res[5] = res[5] + o.r_v - o.r_c;
+      for (int q = 0; q < 4; ++q) d.icav[q * n + g] = o.icav[q];
+      d.rcav[g] = o.r_c;
+      d.rcav[n + g] = o.r_v;
+    }
   }
   if (c.iturb == 0) {
     // cell-centred gradients of u, v, w, k, omega (turbsource kwsst, :269-383)

@@ -775,52 +775,54 @@ using CavOut = CavOutT<double>;
 // arguments so that the adjoint can differentiate with respect to them.
 template <class T>
 __device__ inline CavOutT<T> cavsource_t(const Par& c, const T* pv2, const T* dv, double vol, T uref, T cvc,
-                                         T ccc) {
+                                         T ccc, const double* sat = nullptr) {
+  // sat (optional): the saturation pressure p_sat(T) and temperature T_sat(P) evaluated in
+  // FP64 by the caller (the mixed form's FP32 source keeps them FP64)
   CavOutT<T> o;
-  o.r_c = T(0.0); o.r_v = T(0.0);
-  for (int q = 0; q < 4; ++q) o.icav[q] = T(0.0);
-  if (pv2[4] >= 647.096) return o;
-  const T dp_ref = 2.0 / (c.rhoref * uref * uref);
-  const T t_ref = uref / c.l_chord;
-  const T P = pv2[0] + c.pref;
+  o.r_c = T(T(0.0)); o.r_v = T(T(0.0));
+  for (int q = 0; q < 4; ++q) o.icav[q] = T(T(0.0));
+  if (pv2[4] >= T(647.096)) return o;
+  const T dp_ref = T(2.0) / (T(c.rhoref) * uref * uref);
+  const T t_ref = uref / T(c.l_chord);
+  const T P = pv2[0] + T(c.pref);
   const T clamp_c = c.fix_cav_clamp ? pv2[5] : pv2[4];
-  const T clamp_v = c.fix_cav_clamp ? (1.0 - pv2[5] - pv2[6]) : (1.0 - pv2[4] - pv2[5]);
-  const T yl = 1.0 - pv2[5] - pv2[6];
+  const T clamp_v = c.fix_cav_clamp ? (T(1.0) - pv2[5] - pv2[6]) : (T(1.0) - pv2[4] - pv2[5]);
+  const T yl = T(1.0) - pv2[5] - pv2[6];
   T r_c, r_v;
   if (c.ncav == 1) {  // Merkle
-    T pww = h2o_pww(pv2[4]);
-    T rho1 = 1.0 / dv[0];
+    T pww = sat ? T(sat[0]) : h2o_pww(pv2[4]);
+    T rho1 = T(1.0) / dv[0];
     T kc = ccc * dv[0] * dp_ref * t_ref, kv = cvc * dv[0] * dp_ref * t_ref;
-    T dpc = fmax(P - pww, 0.0), dpv = fmax(pww - P, 0.0);
+    T dpc = fmax(P - pww, T(0.0)), dpv = fmax(pww - P, T(0.0));
     r_c = fmin(ccc * dv[0] * pv2[5] * dpc * dp_ref * t_ref, dv[0] * clamp_c);
     r_v = fmin(cvc * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
-    if (r_c != 0.0) {
+    if (r_c != T(0.0)) {
       o.icav[0] = -(r_c * dv[6] * rho1) - kc * pv2[5];
       o.icav[1] = -(r_c * dv[7] * rho1);
       o.icav[2] = -(r_c * dv[8] * rho1) - kc * dpc;
       o.icav[3] = -(r_c * dv[9] * rho1);
     }
-    if (r_v != 0.0) {
+    if (r_v != T(0.0)) {
       o.icav[0] = r_v * dv[6] * rho1 - kv * yl;
       o.icav[1] = r_v * dv[7] * rho1;
       o.icav[2] = r_v * dv[8] * rho1 - kv * dpv;
       o.icav[3] = r_v * dv[9] * rho1 - kv * dpv;
     }
   } else if (c.ncav == 2) {  // Kunz
-    T pww = h2o_pww(pv2[4]);
-    T rho1 = 1.0 / dv[0];
-    T av = dv[0] * pv2[5] / dv[3], ag = dv[0] * pv2[6] / dv[4], al = 1.0 - av - ag;
-    T dpv = fmax(pww - P, 0.0);
+    T pww = sat ? T(sat[0]) : h2o_pww(pv2[4]);
+    T rho1 = T(1.0) / dv[0];
+    T av = dv[0] * pv2[5] / dv[3], ag = dv[0] * pv2[6] / dv[4], al = T(1.0) - av - ag;
+    T dpv = fmax(pww - P, T(0.0));
     r_c = fmin(ccc * dv[3] * av * sq(al + ag) * t_ref, dv[0] * clamp_c);
     r_v = fmin(cvc * dv[0] * yl * dpv * dp_ref * t_ref, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
-    T av1 = 1.0 - 4.0 * av + 3.0 * av * av;
-    o.icav[0] = -(ccc * t_ref * (dv[6] * pv2[5] * av1 + 2.0 * av * av * dv[14] * (al + ag)));
-    o.icav[1] = -(ccc * t_ref * (dv[7] * pv2[5] * av1 + 2.0 * av * av * dv[15] * (al + ag)));
+    T av1 = T(1.0) - T(4.0) * av + T(3.0) * av * av;
+    o.icav[0] = -(ccc * t_ref * (dv[6] * pv2[5] * av1 + T(2.0) * av * av * dv[14] * (al + ag)));
+    o.icav[1] = -(ccc * t_ref * (dv[7] * pv2[5] * av1 + T(2.0) * av * av * dv[15] * (al + ag)));
     o.icav[2] = -(ccc * t_ref * (dv[8] * pv2[5] + dv[0]) * av1);
     o.icav[3] = -(ccc * t_ref * dv[9] * pv2[5] * av1);
-    if (r_v != 0.0) {
+    if (r_v != T(0.0)) {
       T kv = cvc * dv[0] * dp_ref * t_ref;
       o.icav[0] = r_v * dv[6] * rho1 - kv * yl;
       o.icav[1] = r_v * dv[7] * rho1;
@@ -828,67 +830,67 @@ __device__ inline CavOutT<T> cavsource_t(const Par& c, const T* pv2, const T* dv
       o.icav[3] = r_v * dv[9] * rho1 - kv * dpv;
     }
   } else if (c.ncav == 3) {  // Singhal
-    T pww = h2o_pww(pv2[4]);
+    T pww = sat ? T(sat[0]) : h2o_pww(pv2[4]);
     T sigma = h2o_sigma(pv2[4]);
-    T rho1 = 1.0 / dv[2], rho2 = 1.0 / dv[3];
+    T rho1 = T(1.0) / dv[2], rho2 = T(1.0) / dv[3];
     T cc = ccc * uref / sigma * dv[2] * dv[3], cv = cvc * uref / sigma * dv[2] * dv[3];
-    r_c = fmin(cc * sqrt(2.0 / 3.0 * fmax(P - pww, 0.0) * rho1) * pv2[5], dv[0] * clamp_c);
-    r_v = fmin(cv * sqrt(2.0 / 3.0 * fmax(pww - P, 0.0) * rho1) * yl, dv[0] * clamp_v);
+    r_c = fmin(cc * sqrt(T(2.0) / T(3.0) * fmax(P - pww, T(0.0)) * rho1) * pv2[5], dv[0] * clamp_c);
+    r_v = fmin(cv * sqrt(T(2.0) / T(3.0) * fmax(pww - P, T(0.0)) * rho1) * yl, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
-    if (r_c != 0.0) {
-      o.icav[0] = -(r_c * (dv[14] * rho2 + 0.5 * dv[16] * rho1)) - 0.5 * cc * sqrt(2.0 / 3.0 * rho1) * pv2[5] * pow(P - pww, -0.5);
-      o.icav[1] = -(r_c * (dv[15] * rho2 + 0.5 * dv[17] * rho1));
-      o.icav[2] = -(cc * sqrt(2.0 / 3.0 * fmax(P - pww, 0.0) * rho1));
-      o.icav[3] = 0.0;
+    if (r_c != T(0.0)) {
+      o.icav[0] = -(r_c * (dv[14] * rho2 + T(0.5) * dv[16] * rho1)) - T(0.5) * cc * sqrt(T(2.0) / T(3.0) * rho1) * pv2[5] * pow(P - pww, -T(0.5));
+      o.icav[1] = -(r_c * (dv[15] * rho2 + T(0.5) * dv[17] * rho1));
+      o.icav[2] = -(cc * sqrt(T(2.0) / T(3.0) * fmax(P - pww, T(0.0)) * rho1));
+      o.icav[3] = T(0.0);
     }
-    if (r_v != 0.0) {
-      o.icav[0] = r_v * (dv[14] * rho2 + 0.5 * dv[16] * rho1) - 0.5 * cv * sqrt(2.0 / 3.0 * rho1) * yl * pow(pww - P, -0.5);
-      o.icav[1] = r_v * (dv[15] * rho2 + 0.5 * dv[17] * rho1);
-      o.icav[2] = -(cv * sqrt(2.0 / 3.0 * fmax(pww - P, 0.0) * rho1));
+    if (r_v != T(0.0)) {
+      o.icav[0] = r_v * (dv[14] * rho2 + T(0.5) * dv[16] * rho1) - T(0.5) * cv * sqrt(T(2.0) / T(3.0) * rho1) * yl * pow(pww - P, -T(0.5));
+      o.icav[1] = r_v * (dv[15] * rho2 + T(0.5) * dv[17] * rho1);
+      o.icav[2] = -(cv * sqrt(T(2.0) / T(3.0) * fmax(pww - P, T(0.0)) * rho1));
       o.icav[3] = o.icav[2];
     }
   } else if (c.ncav == 4) {  // Schnerr-Sauer
     const double pi = 3.14159265358979323846, eta = 1.0e13;
-    T pww = h2o_pww(pv2[4]);
-    T rho1 = 1.0 / dv[0], rho3 = 1.0 / dv[2], rho4 = 1.0 / dv[3];
-    T k0 = 3.0 * pow(4.0 * pi * eta / 3.0, 1.0 / 3.0) * sqrt(2.0 / 3.0);
-    T base = k0 * dv[0] * pow(dv[3], 1.0 / 3.0) * pow(dv[2], -5.0 / 6.0) * pow(yl, 4.0 / 3.0);
-    r_c = fmin(ccc * base * pow(pv2[5], 2.0 / 3.0) * sqrt(fmax(P - pww, 0.0)), dv[0] * clamp_c);
-    r_v = fmin(cvc * base * pow(pv2[5] + pv2[6], 2.0 / 3.0) * sqrt(fmax(pww - P, 0.0)), dv[0] * clamp_v);
+    T pww = sat ? T(sat[0]) : h2o_pww(pv2[4]);
+    T rho1 = T(1.0) / dv[0], rho3 = T(1.0) / dv[2], rho4 = T(1.0) / dv[3];
+    T k0 = T(3.0 * pow(4.0 * pi * eta / 3.0, 1.0 / 3.0) * sqrt(2.0 / 3.0));
+    T base = k0 * dv[0] * pow(dv[3], T(1.0) / T(3.0)) * pow(dv[2], -T(5.0) / T(6.0)) * pow(yl, T(4.0) / T(3.0));
+    r_c = fmin(ccc * base * pow(pv2[5], T(2.0) / T(3.0)) * sqrt(fmax(P - pww, T(0.0))), dv[0] * clamp_c);
+    r_v = fmin(cvc * base * pow(pv2[5] + pv2[6], T(2.0) / T(3.0)) * sqrt(fmax(pww - P, T(0.0))), dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
-    if (r_c != 0.0) {
-      o.icav[0] = -(r_c * (dv[6] * rho1 + dv[14] * rho4 / 3.0 - 5.0 * dv[16] * rho3 / 6.0 + 0.5 / (P - pww)));
-      o.icav[1] = -(r_c * (dv[7] * rho1 + dv[15] * rho4 / 3.0 - 5.0 * dv[17] * rho3 / 6.0));
-      o.icav[2] = -(r_c * (dv[8] * rho1 + 2.0 / (3.0 * pv2[5]) - 4.0 / (3.0 * yl)));
-      o.icav[3] = -(r_c * (dv[9] * rho1 - 4.0 / (3.0 * yl)));
+    if (r_c != T(0.0)) {
+      o.icav[0] = -(r_c * (dv[6] * rho1 + dv[14] * rho4 / T(3.0) - T(5.0) * dv[16] * rho3 / T(6.0) + T(0.5) / (P - pww)));
+      o.icav[1] = -(r_c * (dv[7] * rho1 + dv[15] * rho4 / T(3.0) - T(5.0) * dv[17] * rho3 / T(6.0)));
+      o.icav[2] = -(r_c * (dv[8] * rho1 + T(2.0) / (T(3.0) * pv2[5]) - T(4.0) / (T(3.0) * yl)));
+      o.icav[3] = -(r_c * (dv[9] * rho1 - T(4.0) / (T(3.0) * yl)));
     }
-    if (r_v != 0.0) {
-      o.icav[0] = r_v * (dv[6] * rho1 + dv[14] * rho4 / 3.0 - 5.0 * dv[16] * rho3 / 6.0 - 0.5 / (pww - P));
-      o.icav[1] = r_v * (dv[7] * rho1 + dv[15] * rho4 / 3.0 - 5.0 * dv[17] * rho3 / 6.0);
-      o.icav[2] = r_v * (dv[8] * rho1 + 2.0 / (3.0 * (pv2[5] + pv2[6])) - 4.0 / (3.0 * yl));
-      o.icav[3] = r_v * (dv[9] * rho1 + 2.0 / (3.0 * (pv2[5] + pv2[6])) - 4.0 / (3.0 * yl));
+    if (r_v != T(0.0)) {
+      o.icav[0] = r_v * (dv[6] * rho1 + dv[14] * rho4 / T(3.0) - T(5.0) * dv[16] * rho3 / T(6.0) - T(0.5) / (pww - P));
+      o.icav[1] = r_v * (dv[7] * rho1 + dv[15] * rho4 / T(3.0) - T(5.0) * dv[17] * rho3 / T(6.0));
+      o.icav[2] = r_v * (dv[8] * rho1 + T(2.0) / (T(3.0) * (pv2[5] + pv2[6])) - T(4.0) / (T(3.0) * yl));
+      o.icav[3] = r_v * (dv[9] * rho1 + T(2.0) / (T(3.0) * (pv2[5] + pv2[6])) - T(4.0) / (T(3.0) * yl));
     }
   } else {  // Lee
-    T tww = h2o_tww(P);
-    T rho1 = 1.0 / dv[0];
-    r_c = fmin(ccc * dv[0] * pv2[5] * fmax(tww - pv2[4], 0.0) / tww, dv[0] * clamp_c);
-    r_v = fmin(cvc * dv[0] * yl * fmax(pv2[4] - tww, 0.0) / tww, dv[0] * clamp_v);
+    T tww = sat ? T(sat[1]) : h2o_tww(P);
+    T rho1 = T(1.0) / dv[0];
+    r_c = fmin(ccc * dv[0] * pv2[5] * fmax(tww - pv2[4], T(0.0)) / tww, dv[0] * clamp_c);
+    r_v = fmin(cvc * dv[0] * yl * fmax(pv2[4] - tww, T(0.0)) / tww, dv[0] * clamp_v);
     o.r_c = r_c * vol; o.r_v = r_v * vol;
-    if (r_c != 0.0) {
+    if (r_c != T(0.0)) {
       o.icav[0] = -(r_c * dv[6] * rho1);
       o.icav[1] = -(r_c * dv[7] * rho1) + ccc * dv[0] * pv2[5] / tww;
-      o.icav[2] = -(r_c * dv[8] * rho1) - ccc * dv[0] * fmax(tww - pv2[4], 0.0) / tww;
+      o.icav[2] = -(r_c * dv[8] * rho1) - ccc * dv[0] * fmax(tww - pv2[4], T(0.0)) / tww;
       o.icav[3] = -(r_c * dv[9] * rho1);
     }
-    if (r_v != 0.0) {
+    if (r_v != T(0.0)) {
       o.icav[0] = r_v * dv[6] * rho1;
       o.icav[1] = r_v * dv[7] * rho1 + cvc * dv[0] * yl / tww;
-      o.icav[2] = r_v * dv[8] * rho1 - cvc * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
-      o.icav[3] = r_v * dv[9] * rho1 - cvc * dv[0] * fmax(pv2[4] - tww, 0.0) / tww;
+      o.icav[2] = r_v * dv[8] * rho1 - cvc * dv[0] * fmax(pv2[4] - tww, T(0.0)) / tww;
+      o.icav[3] = r_v * dv[9] * rho1 - cvc * dv[0] * fmax(pv2[4] - tww, T(0.0)) / tww;
     }
   }
   T lam = copysign(1.0, o.icav[2]);
-  T f = (1.0 - 0.5 * (1.0 - lam)) - 0.5 * (1.0 - lam);
+  T f = (T(1.0) - T(0.5) * (T(1.0) - lam)) - T(0.5) * (T(1.0) - lam);
   for (int q = 0; q < 4; ++q) o.icav[q] *= f;
   return o;
 }
