@@ -314,27 +314,9 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   if (MX) {
     // the stored FP32 fluxes are deviations from the free-stream flux: their differences
     // and sums in FP32 carry rounding of the order of the storage's own (one conversion to
-    // FP64 per variable instead of one per stored value).  The free-stream part adds back
-    // as -(m . sn) s, sn the cell's face-vector sum: zero up to the metrics' closure
-    // error, so it is formed in df64 from the face vectors' float pairs and applied in FP32.
-    float mnc, snf[3];
-    {
-      const int planes[3] = {GM_CX, GM_EX, GM_TX};
-      df64 mn = dff(0.0f);
-      for (int e = 0; e < 3; ++e) {
-        df64 se = dff(0.0f);
-        for (int q = 0; q < 3; ++q) {
-          const long long o1 = (planes[q] + e) * n + g, o0 = o1 - st[q];
-          se = se + (df64(d.gmf[o1], d.gmlo[o1]) - df64(d.gmf[o0], d.gmlo[o0]));
-        }
-        snf[e] = tof(se);
-        mn = mn + dfp(c.m2[e]) * se;
-      }
-      mnc = tof(mn);
-    }
+    // FP64 per variable instead of one per stored value)
     for (int v = 0; v < npv; ++v) {
-      float r = -(mnc * tof(dfp(c.sc2[v])));
-      if (v >= 1 && v <= 3) r -= (float)c.pref * snf[v - 1];
+      float r = 0.0f;
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
         const float* F = d.fi32 + ((long long)q * npv + v) * n;
@@ -375,7 +357,23 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     }
     res[v] = r;
   }
-
+  if (MX) {
+    // the stored mixed-form fluxes are F - (Phi + pref I).n dl; add the free-stream part
+    // back through the cell's face-vector sum (zero up to the metrics' closure error).
+    // (In FP64: the same sum from the face vectors' df64 float pairs measured slower.)
+    const int planes[3] = {GM_CX, GM_EX, GM_TX};
+    double sn[3];
+    for (int e = 0; e < 3; ++e) {
+      double s = 0.0;
+      for (int q = 0; q < 3; ++q) {
+        const double* G = d.gm + (planes[q] + e) * n;
+        s += G[g] - G[g - st[q]];
+      }
+      sn[e] = s;
+    }
+    for (int v = 0; v < npv; ++v) res[v] -= c.phi[v][0] * sn[0] + c.phi[v][1] * sn[1] + c.phi[v][2] * sn[2];
+    for (int e = 0; e < 3; ++e) res[1 + e] -= c.pref * sn[e];
+  }
   double pv2[NPVM], dv[NDV];
   for (int v = 0; v < npv; ++v) pv2[v] = d.pv[v * n + g];
   for (int v = 0; v < NDV; ++v) dv[v] = d.dv[v * n + g];

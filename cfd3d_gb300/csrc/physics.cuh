@@ -179,9 +179,12 @@ __device__ __forceinline__ void phases(int fluid, double p, double t, Phase<doub
 
 template <class T>
 __device__ __forceinline__ void mixture(const Phase<T>& l, const Phase<T>& v, const Phase<T>& g, T y1, T y2, T* dv,
-                                        unsigned long long* fallbacks) {
+                                        unsigned long long* fallbacks, T* irh = nullptr) {
+  // irh (optional): the phase reciprocals 1/rho_l, 1/rho_v, 1/rho_g, which the transport
+  // properties reuse (three FP64 divisions fewer)
   dv[2] = l.rho; dv[3] = v.rho; dv[4] = g.rho;
   T irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+  if (irh) { irh[0] = irhol; irh[1] = irhov; irh[2] = irhog; }
   T yl = 1.0 - y1 - y2;
   T irho = yl * irhol + y1 * irhov + y2 * irhog;
   dv[0] = 1.0 / irho;
@@ -225,7 +228,8 @@ __device__ __forceinline__ void deteos_t(int fluid, int with_prop, T p, T t, T y
   Phase<T> l, v, g;
   phases_t<T>(fluid, p, t, l, v);
   ideal_gas<T>(p, t, g);
-  mixture<T>(l, v, g, y1, y2, dv, nullptr);
+  T irh[3];
+  mixture<T>(l, v, g, y1, y2, dv, nullptr, irh);
   if (with_prop) {
     T lv, lc, vv, vc;
     if (fluid == 1) {
@@ -237,7 +241,7 @@ __device__ __forceinline__ void deteos_t(int fluid, int with_prop, T p, T t, T y
     }
     T gv = ideal_vis<T>(t), gc = 1395.333333 * gv;
     T yl = 1.0 - y1 - y2;
-    T irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+    const T irhol = irh[0], irhov = irh[1], irhog = irh[2];
     tv[0] = dv[0] * (lv * yl * irhol + vv * y1 * irhov + gv * y2 * irhog);
     tv[1] = dv[0] * (lc * yl * irhol + vc * y1 * irhov + gc * y2 * irhog);
   }
@@ -289,7 +293,8 @@ __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, doubl
   Phase<double> l, v, g;
   phases<MX, true>(fluid, p, t, l, v);
   ideal_gas(p, t, g);
-  mixture(l, v, g, y1, y2, dv, fb);
+  double irh[3];
+  mixture(l, v, g, y1, y2, dv, fb, irh);
   if (with_prop) {
     double lv, lc, vv, vc;
     if (fluid == 1) {
@@ -301,7 +306,7 @@ __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, doubl
     }
     double gv = ideal_vis(t), gc = 1395.333333 * gv;
     double yl = 1.0 - y1 - y2;
-    double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+    const double irhol = irh[0], irhov = irh[1], irhog = irh[2];
     tv[0] = dv[0] * (lv * yl * irhol + vv * y1 * irhov + gv * y2 * irhog);
     tv[1] = dv[0] * (lc * yl * irhol + vc * y1 * irhov + gc * y2 * irhog);
   }
@@ -328,7 +333,8 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
     v.drdp = vf.drdp; v.drdt = vf.drdt; v.dhdp = vf.dhdp; v.dhdt = vf.dhdt;
   }
   ideal_gas(p, t, g);
-  mixture(l, v, g, y1, y2, dv, fb);
+  double irh[3];
+  mixture(l, v, g, y1, y2, dv, fb, irh);
   if (with_prop) {
     float lv, lc, vv, vc;
     if (fluid == 1) {
@@ -340,7 +346,7 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
     }
     float gv = ideal_vis<float>(tf), gc = 1395.333333f * gv;
     double yl = 1.0 - y1 - y2;
-    double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+    const double irhol = irh[0], irhov = irh[1], irhog = irh[2];
     tv[0] = dv[0] * ((double)lv * yl * irhol + (double)vv * y1 * irhov + (double)gv * y2 * irhog);
     tv[1] = dv[0] * ((double)lc * yl * irhol + (double)vc * y1 * irhov + (double)gc * y2 * irhog);
   }
