@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 
 OK = 0
-ERR_ARG, ERR_CUDA, ERR_NONFINITE, ERR_VOLUME, ERR_TIMEOUT, ERR_DESCRIPTOR, ERR_NOMEM, ERR_NODEVICE = range(1, 9)
+ERR_ARG, ERR_CUDA, ERR_NONFINITE, ERR_VOLUME, ERR_TIMEOUT, ERR_DESCRIPTOR, ERR_NOMEM, ERR_NODEVICE, ERR_IO = range(1, 10)
 
 FP64, MIXED = 0, 1
 

@@ -21,9 +21,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fcntl.h>
 #include <mutex>
 #include <new>
 #include <type_traits>
+#include <unistd.h>
 #include "engine.cuh"
 #include "mixed.cuh"
 
@@ -1558,6 +1560,181 @@ int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, dou
     CFD_CUDA(cudaMemcpyAsync(rcav, h->staging, (size_t)nint * 2 * 8, cudaMemcpyDeviceToHost, E.st));
     CFD_CUDA(cudaStreamSynchronize(E.st));
   }
+  return CFD3D_OK;
+}
+
+// ---- checkpoints ----------------------------------------------------------------------
+// The MPI-IO file of variable%export_variable (src/variable_module.f90:116-182), read back
+// by t_ini_restart%restart (src/initial_module.f90:245-389).  Rank r of the reference owns
+// block r, so the file is the blocks' records in block order; the displacement of a record
+// is the sum of the sizes before it (src/variable_module.f90:80-91).
+namespace {
+
+struct CkptRecord {
+  long long npad, nint;                     // padded and interior cells of the block
+  bool turb, cav;                           // l_turb (iturb >= -1), l_cav (ncav != 0)
+  long long pv_off, emut_off, qq_off, rcav_off, bytes;   // byte offsets within the record
+};
+
+CkptRecord ckpt_record(const Par& c, const BlockGeom& B, bool with_qq) {
+  CkptRecord r;
+  r.npad = (long long)B.ni * B.nj * B.nk;
+  r.nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  r.turb = c.iturb >= -1;
+  r.cav = c.ncav != 0;
+  r.pv_off = 4 + 4 + 8;                      // nt_phy, nt (default integers), time
+  r.emut_off = r.pv_off + 8ll * c.npv * r.npad;
+  r.qq_off = r.emut_off + (r.turb ? 8ll * r.npad : 0);
+  r.rcav_off = r.qq_off + (with_qq ? 8ll * c.nqq * c.npv * r.nint : 0);
+  r.bytes = r.rcav_off + (r.cav ? 16ll * r.nint : 0);
+  return r;
+}
+
+// whole-buffer positional I/O (a single pread/pwrite may move fewer bytes than asked)
+bool pio(int fd, void* buf, long long n, long long off, bool wr) {
+  char* p = (char*)buf;
+  while (n > 0) {
+    const ssize_t k = wr ? pwrite(fd, p, (size_t)std::min(n, 1ll << 30), (off_t)off)
+                         : pread(fd, p, (size_t)std::min(n, 1ll << 30), (off_t)off);
+    if (k <= 0) return false;
+    p += k; off += k; n -= k;
+  }
+  return true;
+}
+
+// interior cells (2:imax, 2:jmax, 2:kmax) of one component of a padded Fortran array
+// a(nv, -1:imax+3, ..) into out(2:imax, ..)
+void padded_to_interior(const BlockGeom& B, const double* a, int nv, int v, double* out) {
+  long long q = 0;
+  for (int k = 2; k <= B.kmax; ++k)
+    for (int j = 2; j <= B.jmax; ++j)
+      for (int i = 2; i <= B.imax; ++i)
+        out[q++] = a[((((long long)(k + 1) * B.nj) + (j + 1)) * B.ni + (i + 1)) * nv + v];
+}
+
+}  // namespace
+
+int cfd3d_checkpoint_write(cfd3d_handle* h, const char* path, int nt_phy, int nt, double time) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  const Par& c = E.par;
+  if (!path) { E.err = "checkpoint path is NULL"; return CFD3D_ERR_ARG; }
+  // mpi_mode_wronly + mpi_mode_create: created when missing, never truncated
+  const int fd = open(path, O_WRONLY | O_CREAT, 0644);
+  if (fd < 0) { E.err = std::string("cannot open checkpoint for writing: ") + path; return CFD3D_ERR_IO; }
+  long long disp = 0;
+  int rc = CFD3D_OK;
+  std::vector<double> pv, tv, qq, rcav, emut;
+  for (int b = 0; b < (int)E.blk.size() && rc == CFD3D_OK; ++b) {
+    const BlockGeom& B = E.blk[b];
+    const CkptRecord r = ckpt_record(c, B, true);
+    pv.assign((size_t)(c.npv * r.npad), 0.0);
+    tv.assign((size_t)(std::max(c.ntv, 1) * r.npad), 0.0);
+    qq.assign((size_t)std::max(2ll * c.npv * r.nint, 1ll), 0.0);
+    rcav.assign((size_t)(2 * r.nint), 0.0);
+    rc = cfd3d_download_state(h, b, pv.data(), nullptr, c.ntv ? tv.data() : nullptr, c.nqq ? qq.data() : nullptr,
+                              rcav.data());
+    if (rc) break;
+    char head[16];
+    const int32_t i2[2] = {(int32_t)nt_phy, (int32_t)nt};
+    memcpy(head, i2, 8);
+    memcpy(head + 8, &time, 8);
+    bool ok = pio(fd, head, 16, disp, true) && pio(fd, pv.data(), 8ll * c.npv * r.npad, disp + r.pv_off, true);
+    if (ok && r.turb) {
+      // emut = tv(3, :, :, :) over the padded range (:141-150)
+      emut.assign((size_t)r.npad, 0.0);
+      if (c.ntv >= 3)
+        for (long long q = 0; q < r.npad; ++q) emut[(size_t)q] = tv[(size_t)(q * c.ntv + 2)];
+      ok = pio(fd, emut.data(), 8ll * r.npad, disp + r.emut_off, true);
+    }
+    if (ok && c.nqq) ok = pio(fd, qq.data(), 8ll * c.nqq * c.npv * r.nint, disp + r.qq_off, true);
+    if (ok && r.cav) ok = pio(fd, rcav.data(), 16ll * r.nint, disp + r.rcav_off, true);
+    if (!ok) { E.err = std::string("checkpoint write failed: ") + path; rc = CFD3D_ERR_IO; }
+    disp += r.bytes;
+  }
+  if (close(fd) != 0 && rc == CFD3D_OK) { E.err = std::string("checkpoint close failed: ") + path; rc = CFD3D_ERR_IO; }
+  return rc;
+}
+
+int cfd3d_checkpoint_read(cfd3d_handle* h, const char* path, int steady_start, int* nps, int* nts,
+                          double* timeprev) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  const Par& c = E.par;
+  if (!path) { E.err = "checkpoint path is NULL"; return CFD3D_ERR_ARG; }
+  const int fd = open(path, O_RDONLY);
+  if (fd < 0) { E.err = std::string("cannot open checkpoint: ") + path; return CFD3D_ERR_IO; }
+  // the steadyini variant (src/initial_module.f90:103-242) reads records without qq
+  const bool with_qq = !steady_start;
+  long long disp = 0;
+  int rc = CFD3D_OK;
+  int32_t head_i[2] = {0, 0};
+  double head_t = 0.0;
+  std::vector<double> pv, buf, interior;
+  for (int b = 0; b < (int)E.blk.size() && rc == CFD3D_OK; ++b) {
+    const BlockGeom& B = E.blk[b];
+    const CkptRecord r = ckpt_record(c, B, with_qq);
+    char head[16];
+    if (!pio(fd, head, 16, disp, false)) { E.err = "checkpoint shorter than the case's blocks"; rc = CFD3D_ERR_IO; break; }
+    int32_t bi[2];
+    double bt;
+    memcpy(bi, head, 8);
+    memcpy(&bt, head + 8, 8);
+    if (b == 0) { head_i[0] = bi[0]; head_i[1] = bi[1]; head_t = bt; }
+    pv.assign((size_t)(c.npv * r.npad), 0.0);
+    if (!pio(fd, pv.data(), 8ll * c.npv * r.npad, disp + r.pv_off, false)) {
+      E.err = "checkpoint shorter than the case's blocks"; rc = CFD3D_ERR_IO; break;
+    }
+    // pv of the interior cells, then dv / tv by the EOS and qq from the state (set_others)
+    interior.assign((size_t)(c.npv * r.nint), 0.0);
+    buf.assign((size_t)r.nint, 0.0);
+    for (int v = 0; v < c.npv; ++v) {
+      padded_to_interior(B, pv.data(), c.npv, v, buf.data());
+      for (long long q = 0; q < r.nint; ++q) interior[(size_t)(q * c.npv + v)] = buf[(size_t)q];
+    }
+    if ((rc = cfd3d_initialize(h, b, interior.data()))) break;
+    // tv(3) = emut, qq and rcav from the file, interior cells only
+    struct Part { bool on; long long off; int nv; bool padded; double* dst; };
+    const Part parts[3] = {
+        {r.turb && c.ntv >= 3, r.emut_off, 1, true, E.d.tv + 2 * E.ncell},
+        {with_qq && c.nqq > 0, r.qq_off, c.nqq * c.npv, false, E.d.qq},
+        {r.cav, r.rcav_off, 2, false, E.d.rcav}};
+    for (const Part& p : parts) {
+      if (!p.on) continue;
+      const long long cnt = p.nv * (p.padded ? r.npad : r.nint);
+      buf.assign((size_t)cnt, 0.0);
+      if (!pio(fd, buf.data(), 8ll * cnt, disp + p.off, false)) {
+        E.err = "checkpoint shorter than the case's blocks"; rc = CFD3D_ERR_IO; break;
+      }
+      if (p.padded) {
+        interior.assign((size_t)r.nint, 0.0);
+        padded_to_interior(B, buf.data(), 1, 0, interior.data());
+        buf.swap(interior);
+      }
+      if ((rc = ensure_staging(h, 8 * (size_t)(p.nv * r.nint)))) break;
+      cudaError_t e = cudaMemcpyAsync(h->staging, buf.data(), 8 * (size_t)(p.nv * r.nint), cudaMemcpyHostToDevice, E.st);
+      if (e != cudaSuccess) { E.err = cudaGetErrorString(e); rc = CFD3D_ERR_CUDA; break; }
+      k_interior_io<<<nblk_of(r.nint, 256), 256, 0, E.st>>>(h->staging, p.nv, B, p.dst, E.ncell, 1);
+      e = cudaStreamSynchronize(E.st);
+      if (e == cudaSuccess) e = cudaGetLastError();
+      if (e != cudaSuccess) { E.err = cudaGetErrorString(e); rc = CFD3D_ERR_CUDA; break; }
+    }
+    disp += r.bytes;
+  }
+  close(fd);
+  if (rc) return rc;
+  // the counters the solve loop restarts from (src/initial_module.f90:238-240,373-381)
+  int p = head_i[0], t = head_i[1];
+  double tp = head_t;
+  if (steady_start) { p = 1; t = 1; tp = 0.0; }
+  else {
+    ++t; ++p;
+    if (c.nsteady >= 1) t = 1;
+    else p = 1;
+  }
+  if (nps) *nps = p;
+  if (nts) *nts = t;
+  if (timeprev) *timeprev = tp;
   return CFD3D_OK;
 }
 

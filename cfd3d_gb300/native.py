@@ -46,6 +46,8 @@ def lib():
     L.cfd3d_initialize.argtypes = [H, C.c_int, dp]
     L.cfd3d_upload_state.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_download_state.argtypes = [H, C.c_int, dp, dp, dp, dp, dp]
+    L.cfd3d_checkpoint_write.argtypes = [H, C.c_char_p, C.c_int, C.c_int, C.c_double]
+    L.cfd3d_checkpoint_read.argtypes = [H, C.c_char_p, C.c_int, ip, ip, dp]
     L.cfd3d_iterate.argtypes = [H, C.c_int, C.c_int, C.c_double, dp, dp, ip]
     L.cfd3d_iterate_n.argtypes = [H, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]
     L.cfd3d_unsteady_shift.argtypes = [H]
@@ -65,7 +67,8 @@ def lib():
 
 
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
-           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_iterate", "cfd3d_iterate_n",
+           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
+           "cfd3d_iterate", "cfd3d_iterate_n",
            "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device"]
 STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
@@ -173,6 +176,17 @@ class Engine:
         self._check(lib().cfd3d_download_state(self.h, n, _p(pv), _p(dv), _p(tv) if self.ntv else None,
                                                _p(qq) if self.nqq else None, _p(rcav)))
 
+    def checkpoint_write(self, path, nt_phy, nt, time):
+        """variable%export_variable: write the state to `path` in the reference's layout."""
+        self._check(lib().cfd3d_checkpoint_write(self.h, os.fsencode(path), nt_phy, nt, float(time)))
+
+    def checkpoint_read(self, path, steady_start=False):
+        """t_ini_restart%restart: load the state from `path`; returns (nps, nts, timeprev)."""
+        nps, nts, tp = C.c_int(), C.c_int(), C.c_double()
+        self._check(lib().cfd3d_checkpoint_read(self.h, os.fsencode(path), 1 if steady_start else 0,
+                                                C.byref(nps), C.byref(nts), C.byref(tp)))
+        return nps.value, nts.value, tp.value
+
     def residual(self, n=0):
         b = self.case["blocks"][n]
         res = np.zeros(abi.interior_shape(b, self.npv))
@@ -266,29 +280,63 @@ class Solver:
         self.log_path = log_path
         self.history = []
 
-    def solve(self, npmax=None, ntmax=None, pv0=None):
+    def solve(self, npmax=None, ntmax=None, pv0=None, export_dir=None, restart=None, steady_start=False):
+        """Run the physical / pseudo-time loops.
+
+        export_dir: write checkpoints out_########.dat there where solve_equation calls
+        variable%export_variable (src/solve_module.f90:127-150): the initial state as
+        out_00000000.dat, then for a steady run every nexport pseudo-iterations and at
+        convergence, for an unsteady run every nexport physical steps (after the history
+        shift, with nt - 1 as its nt).  The tag is nt_phy for unsteady runs, else nt.
+        restart: a checkpoint to start from (iread >= 1) instead of the initial state; the
+        loops resume from the counters it yields.  steady_start reads it as the steadyini
+        variant (no qq section)."""
         e = self.engine
-        e.initialize(self.case.get("pv0") if pv0 is None else pv0)
         nsteady = self.cfg.get("nsteady", 0)
+        if restart is not None:
+            nps, nts, timeprev = e.checkpoint_read(restart, steady_start)
+        else:
+            e.initialize(self.case.get("pv0") if pv0 is None else pv0)
+            nps, nts, timeprev = 1, 1, 0.0
         npmax = npmax or self.cfg.get("npmax", 1)
         ntmax = ntmax or self.cfg.get("ntmax", 1)
+        nexport = max(int(self.cfg.get("nexport", 0) or 0), 0)
         bond = 10.0 ** (-self.cfg.get("bond", 12))
-        log = open(self.log_path, "w") if self.log_path else None
+
+        def export(nt_phy, nt, time):
+            if export_dir is None:
+                return
+            tag = nt_phy if nsteady >= 1 else nt
+            e.checkpoint_write(os.path.join(export_dir, "out_%08d.dat" % tag), nt_phy, nt, time)
+
+        if restart is None:
+            export(0, 0, 0.0)
+        log = open(self.log_path, "a" if restart is not None else "w") if self.log_path else None
         if log:
             names = ["nt", "resp", "resu", "resv", "resw", "rest", "resy1", "resy2"] + (["resk", "reso"] if e.npv == 9 else [])
-            log.write(" variables=" + ",".join('"%s"' % x for x in names) + "\n zone t =\"newstart\"\n")
-        time = 0.0
-        for nt_phy in range(1, npmax + 1):
-            for nt in range(1, ntmax + 1):
-                time, res, loc = e.iterate(nt_phy, nt, 0.0)
+            zone = "restart" if restart is not None else "newstart"
+            log.write(" variables=" + ",".join('"%s"' % x for x in names) + "\n zone t =\"%s\"\n" % zone)
+        time = timeprev
+        for nt_phy in range(nps, npmax + 1):
+            nt = nts
+            for nt in range(nts, ntmax + 1):
+                time, res, loc = e.iterate(nt_phy, nt, timeprev)
                 it = ntmax * (nt_phy - 1) + nt
                 self.history.append((it, time, res.copy(), loc))
                 if log:
                     log.write("%10d" % it + "".join("%30.12f" % r for r in res) + "\n")
                 if res[0] < bond or res[1] < bond:
+                    if nsteady == 0:
+                        export(nt_phy, nt, time)
                     break
+                if nexport and nt % nexport == 0 and nsteady == 0:
+                    export(nt_phy, nt, time)
+            else:
+                nt = ntmax + 1   # a completed Fortran do loop leaves its index one past the end
             if nsteady >= 1:
                 e.unsteady_shift()
+                if nexport and nt_phy % nexport == 0:
+                    export(nt_phy, nt - 1, time)
         if log:
             log.close()
         return self.history

@@ -38,6 +38,7 @@ extern "C" {
 #define CFD3D_ERR_DESCRIPTOR   6   /* inconsistent block / BC / connection descriptor */
 #define CFD3D_ERR_NOMEM        7   /* device allocation failed                       */
 #define CFD3D_ERR_NODEVICE     8   /* no CUDA device is visible                      */
+#define CFD3D_ERR_IO           9   /* a checkpoint file could not be opened, read or written */
 
 /* ---- arithmetic forms ---------------------------------------------------------- */
 #define CFD3D_FP64   0   /* every kernel in FP64 (the reference's arithmetic)        */
@@ -127,6 +128,27 @@ int  cfd3d_upload_state(cfd3d_handle *h, int block, const double *pv, const doub
                         const double *tv, const double *qq);
 int  cfd3d_download_state(cfd3d_handle *h, int block, double *pv, double *dv, double *tv,
                           double *qq, double *rcav);
+
+/* Checkpoint file out_########.dat in the layout of variable%export_variable
+ * (src/variable_module.f90:116-182), native byte order: one record per block, in block
+ * order (rank r of the reference owns block r), each record
+ *   int32 nt_phy, int32 nt, float64 time,
+ *   pv(npv, -1:imax+3, -1:jmax+3, -1:kmax+3),
+ *   emut(-1:imax+3, ..) = tv(3, ..)        when iturb >= -1,
+ *   qq(npv, nqq, 2:imax, 2:jmax, 2:kmax),
+ *   rcav(2, 2:imax, ..)                    when ncav != 0.
+ * The file is created when missing and not truncated (mpi_mode_wronly+mpi_mode_create). */
+int  cfd3d_checkpoint_write(cfd3d_handle *h, const char *path, int nt_phy, int nt, double time);
+
+/* Restart from such a file: t_ini_restart%restart (src/initial_module.f90:245-389).  The
+ * interior pv is read, dv and tv follow from the EOS, tv(3) from emut, qq and rcav from the
+ * file.  Returns the loop counters the solve loop restarts from: nps = nt_phy + 1 and
+ * nts = 1 for unsteady runs, nts = nt + 1 and nps = 1 for steady ones, and the stored time.
+ * steady_start != 0 reads the steadyini variant (:103-242): records without qq, qq rebuilt
+ * from the state, nps = nts = 1, timeprev = 0.  A file shorter than the case's records
+ * returns CFD3D_ERR_IO. */
+int  cfd3d_checkpoint_read(cfd3d_handle *h, const char *path, int steady_start, int *nps, int *nts,
+                           double *timeprev);
 
 /* One pseudo-iteration: resi%setqres + update%timeinteg (LU-SGS) + resi%residual
  * (src/solve_module.f90:134-136).  Outputs the solution time, the L2 norms
