@@ -109,7 +109,8 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
   c.pi = std::atan(1.0) * 4.0;
   c.aoa = in->aoa * c.pi / 180.0; c.aos = in->aos * c.pi / 180.0;
   c.str = c.l_character / c.pi / c.dt_phy;
-  if (in->timemethod != 3) { err = "timemethod must be 3 (LU-SGS)"; return false; }
+  c.timemethod = in->timemethod;
+  if (c.timemethod < 1 || c.timemethod > 3) { err = "timemethod must be 1 (Euler), 2 (RK3) or 3 (LU-SGS)"; return false; }
   if (c.iturb == -3) { c.npv = 7; c.ntv = 0; }
   else if (c.iturb == -2) { c.npv = 7; c.ntv = 2; }
   else if (c.iturb == 0) { c.npv = 9; c.ntv = 3; }
@@ -1076,6 +1077,25 @@ static void jac_apply(const Cfg& c, Block& B, const double* nx, int i, int j, in
     for (int l = 0; l < c.npv; ++l) acc[n] = (sgn_acc > 0) ? acc[n] + a[n][l] * dq[l] : acc[n] - a[n][l] * dq[l];
 }
 
+/* eddy%caleddy over the block after an update (src/update_module.f90:701-732, :300-330) */
+static void eddy_block(const Cfg& c, Block& B) {
+  const int im = B.imax, jm = B.jmax, km = B.kmax;
+  if (c.iturb == 0) {
+    for (int k = 2; k <= km; ++k)
+      for (int j = 2; j <= jm; ++j)
+        for (int i = 2; i <= im; ++i) {
+          double x7[7][NPV_MAX];
+          gather_pv(c, B, i - 1, j, k, x7[0]); gather_pv(c, B, i, j, k, x7[1]); gather_pv(c, B, i + 1, j, k, x7[2]);
+          gather_pv(c, B, i, j - 1, k, x7[3]); gather_pv(c, B, i, j + 1, k, x7[4]);
+          gather_pv(c, B, i, j, k - 1, x7[5]); gather_pv(c, B, i, j, k + 1, x7[6]);
+          double tv[3];
+          for (int m = 0; m < 3; ++m) tv[m] = B.tv(m, i, j, k);
+          B.tv(2, i, j, k) = kwsst_eddy(x7, B.cx.at(i - 1, j, k), B.cx.at(i, j, k), B.ex.at(i, j - 1, k), B.ex.at(i, j, k),
+                                        B.tx.at(i, j, k - 1), B.tx.at(i, j, k), B.grd.at(i, j, k), B.dv.at(i, j, k), tv);
+        }
+  }
+}
+
 static void lusgs_block(const Cfg& c, Block& B) {
   const int im = B.imax, jm = B.jmax, km = B.kmax, npv = c.npv;
   const double zero4[4] = {0, 0, 0, 0};
@@ -1127,20 +1147,46 @@ static void lusgs_block(const Cfg& c, Block& B) {
         deteos(c.eos, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], B.dv.at(i, j, k), tv);
         for (int m = 0; m < c.ntv; ++m) B.tv(m, i, j, k) = tv[m];
       }
-  if (c.iturb == 0) {
-    for (int k = 2; k <= km; ++k)
-      for (int j = 2; j <= jm; ++j)
-        for (int i = 2; i <= im; ++i) {
-          double x7[7][NPV_MAX];
-          gather_pv(c, B, i - 1, j, k, x7[0]); gather_pv(c, B, i, j, k, x7[1]); gather_pv(c, B, i + 1, j, k, x7[2]);
-          gather_pv(c, B, i, j - 1, k, x7[3]); gather_pv(c, B, i, j + 1, k, x7[4]);
-          gather_pv(c, B, i, j, k - 1, x7[5]); gather_pv(c, B, i, j, k + 1, x7[6]);
-          double tv[3];
-          for (int m = 0; m < 3; ++m) tv[m] = B.tv(m, i, j, k);
-          B.tv(2, i, j, k) = kwsst_eddy(x7, B.cx.at(i - 1, j, k), B.cx.at(i, j, k), B.ex.at(i, j - 1, k), B.ex.at(i, j, k),
-                                        B.tx.at(i, j, k - 1), B.tx.at(i, j, k), B.grd.at(i, j, k), B.dv.at(i, j, k), tv);
+  eddy_block(c, B);
+}
+
+/* One stage of eulerex (src/update_module.f90:214-322) or rk3rd (:324-453): pv = a1 rk +
+ * a2 pv + a3 getx(res) with the explicit diagonal solve, the update's clips, deteos and the
+ * eddy viscosity.  rk (the state before the iteration) is kept in dqs at stage 1. */
+static void explicit_block(const Cfg& c, Block& B, int m) {
+  static const double a1[3] = {0.0, 0.75, 1.0 / 3.0}, a2[3] = {1.0, 0.25, 2.0 / 3.0}, a3[3] = {1.0, 0.25, 2.0 / 3.0};
+  const bool rk3 = c.timemethod == 2;
+  const double c1 = rk3 ? a1[m - 1] : 0.0, c2 = rk3 ? a2[m - 1] : 1.0, c3 = rk3 ? a3[m - 1] : 1.0;
+  const int im = B.imax, jm = B.jmax, km = B.kmax, npv = c.npv;
+  const double zero4[4] = {0, 0, 0, 0};
+  double tvb[3];
+  for (int k = 2; k <= km; ++k)
+    for (int j = 2; j <= jm; ++j)
+      for (int i = 2; i <= im; ++i) {
+        double* pv = B.pv.at(i, j, k);
+        double* rk = B.dqs.at(i, j, k);
+        if (m == 1) for (int n = 0; n < npv; ++n) rk[n] = pv[n];
+        LhsIn L;
+        lhs_in(c, B, i, j, k, L, tvb, zero4);
+        double res[NPV_MAX], x[NPV_MAX];
+        for (int n = 0; n < npv; ++n) res[n] = B.res(n, i, j, k);
+        lhs_getx_ex(c, L, res, x);
+        double p[NPV_MAX];
+        for (int n = 0; n < npv; ++n) p[n] = c1 * rk[n] + c2 * pv[n] + c3 * x[n];
+        p[0] = dmax(-c.pref + 1.0e1, p[0]);
+        p[5] = dmin(1.0, dmax(0.0, p[5]));
+        p[6] = dmin(1.0, dmax(0.0, p[6]));
+        if (c.iturb == 0) {
+          p[7] = dmax(p[7], 1.0e-16);
+          p[8] = dmax3(p[8], 1.0e-16, B.omega_cut(0, i, j, k));
         }
-  }
+        for (int n = 0; n < npv; ++n) pv[n] = p[n];
+        double tv[3] = {0, 0, 0};
+        for (int q = 0; q < c.ntv; ++q) tv[q] = B.tv(q, i, j, k);
+        deteos(c.eos, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], B.dv.at(i, j, k), tv);
+        for (int q = 0; q < c.ntv; ++q) B.tv(q, i, j, k) = tv[q];
+      }
+  eddy_block(c, B);
 }
 
 template <class F>
@@ -1325,9 +1371,19 @@ int orc_iterate(void* h, int nt_phy, int nt, double timeprev, double* time_out, 
   O->time_acc = O->time_acc + dtmin;
   double tstep = O->time_acc + timeprev;
   O->time_cur = (c.nsteady == 0) ? tstep : c.dt_phy * (double)nt_phy;
-  setbc(*O);
-  for_blocks(*O, [&](int n) { calrhs_block(c, O->b[n]); });
-  for_blocks(*O, [&](int n) { lusgs_block(c, O->b[n]); });
+  if (c.timemethod == 3) {
+    setbc(*O);
+    for_blocks(*O, [&](int n) { calrhs_block(c, O->b[n]); });
+    for_blocks(*O, [&](int n) { lusgs_block(c, O->b[n]); });
+  } else {
+    /* eulerex: one stage; rk3rd: three, the time step taken at the first only */
+    const int nstage = (c.timemethod == 2) ? 3 : 1;
+    for (int m = 1; m <= nstage; ++m) {
+      setbc(*O);
+      for_blocks(*O, [&](int n) { calrhs_block(c, O->b[n]); });
+      for_blocks(*O, [&](int n) { explicit_block(c, O->b[n], m); });
+    }
+  }
   double res[NPV_MAX] = {0};
   double resmax = 1.0e-12;
   int lb = -1, li = 0, lj = 0, lk = 0;

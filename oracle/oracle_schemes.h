@@ -26,6 +26,7 @@ struct Cfg {
   double l_chord, l_character, scale, l_domain, str, pi;
   double rhoref, visref, kref, oref, emutref;
   int fix_cav_clamp;
+  int timemethod;  /* 1 explicit Euler, 2 RK3, 3 LU-SGS */
   bool with_prop;  /* t_eos_prop (iturb >= -2) vs t_eosonly (Euler) */
   EosSel eos;
 };
@@ -840,6 +841,42 @@ static inline void lhs_getx(const Cfg& cf, const LhsIn& L, const double* res, do
     x[7] = ((res[8] - res[0] * pv[8]) * t[1] - (b1 * dv[0] + t[3]) * (res[7] - res[0] * pv[7])) * tt;
     x[8] = ((res[7] - res[0] * pv[7]) * t[2] - (b1 * dv[0] + t[0]) * (res[8] - res[0] * pv[8])) * tt;
   }
+  for (int n = 0; n < cf.npv; ++n) x[n] = x[n] * a;
+}
+
+/* flowonly_ex / flowturball_ex (src/lhs_module.f90:247-344): the explicit schemes' diagonal
+ * solve, without spectral radii, viscous shift or source couplings; a = dt/vol. */
+static inline void lhs_getx_ex(const Cfg& cf, const LhsIn& L, const double* res, double* x) {
+  const double* pv = L.pv;
+  const double* dv = L.dv;
+  double bb = (cf.nsteady == 1) ? 1.0 : ((cf.nsteady == 2) ? 0.75 : 0.0);
+  double a = L.dt / L.grd[0];
+  double b = (cf.nsteady >= 1) ? (double)cf.nsteady * bb * L.grd[0] / cf.dt_phy * a : 0.0;
+  double b1 = 1.0 + b;
+  double i_b1 = 1.0 / (b1 * dv[0]);
+  double uv2 = sq(pv[1]) + sq(pv[2]) + sq(pv[3]);
+  double ss = dv[0] * dv[11] * (1.0 / sndp2_of(cf, dv[5], uv2) + b / dv[5]);
+  double rr = 1.0 / sndp2_of(cf, dv[5], uv2) - 1.0 / dv[5] + b1 * dv[6];
+  double hst = dv[1] + 0.5 * (sq(pv[1]) + sq(pv[2]) + sq(pv[3])) - uv2;
+  double cross = dv[13] * dv[8] - dv[12] * dv[9];
+  double cross1 = dv[12] * dv[7] - dv[11] * dv[8];
+  double cross2 = dv[13] * dv[7] - dv[11] * dv[9];
+  double dhdp1 = 1.0 - dv[10] * dv[0];
+  double ssy1 = dv[12] * dv[0] * rr + b1 * dv[8] * dhdp1;
+  double ssy2 = dv[13] * dv[0] * rr + b1 * dv[9] * dhdp1;
+  double ssh = dv[0] * rr * hst - b1 * dhdp1 * dv[0];
+  double aaa2 = dv[7] * hst + dv[11] * dv[0] - cross2 * pv[6];
+  double uuu = res[1] * pv[1] + res[2] * pv[2] + res[3] * pv[3] - res[4];
+  double coeff2 = res[0] * aaa2 + dv[7] * uuu + cross2 * res[6];
+  double coeff3 = res[0] * (ssh - ssy2 * pv[6]) + dv[0] * rr * uuu + res[6] * ssy2;
+  double mm = 1.0 / ss;
+  (void)cross;
+  x[0] = (coeff2 + cross1 * res[5] - cross1 * pv[5] * res[0]) * mm;
+  x[1] = (res[1] - res[0] * pv[1]) * i_b1;
+  x[2] = (res[2] - res[0] * pv[2]) * i_b1;
+  x[3] = (res[3] - res[0] * pv[3]) * i_b1;
+  x[4] = -(coeff3 - ssy1 * pv[5] * res[0] + res[5] * ssy1) * mm * i_b1;
+  for (int n = 5; n < cf.npv; ++n) x[n] = (res[n] - res[0] * pv[n]) * i_b1;
   for (int n = 0; n < cf.npv; ++n) x[n] = x[n] * a;
 }
 
