@@ -508,6 +508,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     }
   }
   for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
+  if (c.timemethod != 3) return;   // the explicit schemes need no sweep records
   // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous
   // term), written with its state and residual as the cell's sweep record at pos[g]
   double tvc[3] = {0.0, 0.0, 0.0};
@@ -787,8 +788,13 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
 }
 
 // ------------------------------------------------------------------ update + residual
+// stage > 0: one stage of the explicit schemes instead of the LU-SGS update --
+// eulerex (src/update_module.f90:214-322), pv += getx_ex(res), or stage m of rk3rd
+// (:324-453), pv = a1 rk + a2 pv + a3 getx_ex(res), rk being the state before the
+// iteration (kept in dqs at t by stage 1).  The residual norms measure the change over
+// the whole iteration (they are final after the last stage).
 template <bool MX>
-__global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
+__global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
   // grid-stride over the interior cells: the grid is a fixed multiple of the SM count,
   // so the per-CTA partials (and the order they are summed in) do not depend on size
   const int npv = c.npv;
@@ -802,13 +808,30 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c) {
     int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
     long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
     const long long n = d.ncell;
-    const long long pq = d.pos[g];   // plane-major position of the sweep's dq
     double old[NPVM], p[NPVM];
-    for (int v = 0; v < npv; ++v) {
-      old[v] = d.pv[v * n + g];
-      p[v] = old[v] + d.dqs[v * d.nint + pq];
-      if (!isfinite(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
+    if (stage == 0) {
+      const long long pq = d.pos[g];   // plane-major position of the sweep's dq
+      for (int v = 0; v < npv; ++v) {
+        old[v] = d.pv[v * n + g];
+        p[v] = old[v] + d.dqs[v * d.nint + pq];
+      }
+    } else {
+      double cur[NPVM], dvc[NDV], r[NPVM], x[NPVM];
+      for (int v = 0; v < npv; ++v) { cur[v] = d.pv[v * n + g]; r[v] = d.res[v * n + g]; }
+      for (int v = 0; v < NDV; ++v) dvc[v] = d.dv[v * n + g];
+      getx_explicit(c, cur, dvc, r, d.dt[g], d.gm[GM_GRD * n + g], x);
+      const double a1[3] = {0.0, 0.75, 1.0 / 3.0}, a2[3] = {1.0, 0.25, 2.0 / 3.0};
+      const bool rk3 = c.timemethod == 2;
+      const double c1 = rk3 ? a1[stage - 1] : 0.0, c2 = rk3 ? a2[stage - 1] : 1.0;
+      for (int v = 0; v < npv; ++v) {
+        double* rk = d.dqs + v * d.nint + t;
+        if (stage == 1) *rk = cur[v];
+        old[v] = *rk;
+        p[v] = c1 * old[v] + c2 * cur[v] + c2 * x[v];   // a3 = a2 in both schemes
+      }
     }
+    for (int v = 0; v < npv; ++v)
+      if (!isfinite(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
     p[0] = fmax(-c.pref + 1.0e1, p[0]);
     p[5] = fmin(1.0, fmax(0.0, p[5]));
     p[6] = fmin(1.0, fmax(0.0, p[6]));
@@ -1076,6 +1099,37 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   stage(4);
   n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
+  if (c.timemethod != 3) {
+    // explicit Euler (one stage) or RK3 (three; the time step is taken at the first only):
+    // each stage is boundary program, fluxes, residual, update and eddy viscosity
+    const int nstage = (c.timemethod == 2) ? 3 : 1;
+    for (int m = 1; m <= nstage; ++m) {
+      if (m > 1) {
+        for (int p = 0; p < 3; ++p)
+          if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
+        if (c.mixed) launch_face_flux_mixed(E, s);
+        else launch_face_flux(E, s);
+        if (c.mixed) k_rhs<true><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+        else k_rhs<false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+        n += c.mixed ? 8 : 4;
+      }
+      if (m == nstage) { stage(5); stage(6); }
+      if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c, m);
+      else k_update<false><<<E.red_grid, T, 0, s>>>(d, c, m);
+      ++n;
+      if (m == nstage) stage(7);
+      if (c.iturb == 0) {
+        if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+        else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+        ++n;
+      }
+    }
+    k_finish<<<1, FIN_T, 0, s>>>(d, c, E.red_grid);
+    ++n;
+    stage(8);
+    E.launches_per_iter = n;
+    return;
+  }
   if (!E.sweep_planes) {
     // dataflow sweeps: flags and tickets cleared, one persistent launch per sweep
     cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), s);
@@ -1109,8 +1163,8 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   }
   }
   stage(6);
-  if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c);
-  else k_update<false><<<E.red_grid, T, 0, s>>>(d, c);
+  if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c, 0);
+  else k_update<false><<<E.red_grid, T, 0, s>>>(d, c, 0);
   ++n;
   stage(7);
   if (c.iturb == 0) {
@@ -1144,7 +1198,10 @@ int read_scalars(Engine& E, Scalars& s) {
 
 bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   std::memset(&c, 0, sizeof(c));
-  if (in->timemethod != 3) { err = "timemethod must be 3 (LU-SGS)"; return false; }
+  if (in->timemethod < 1 || in->timemethod > 3) {
+    err = "timemethod must be 1 (explicit Euler), 2 (RK3) or 3 (LU-SGS)"; return false;
+  }
+  c.timemethod = in->timemethod;
   if (in->iturb == -3) { c.npv = 7; c.ntv = 0; }
   else if (in->iturb == -2) { c.npv = 7; c.ntv = 2; }
   else if (in->iturb == 0) { c.npv = 9; c.ntv = 3; }
@@ -1905,7 +1962,7 @@ int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, false>, SW_CH, 0);
   int bestg = E.sweep_grid;
   tbest = 1e30f;
-  for (int m = 1; m <= std::max(per, 1); ++m) {
+  for (int m = 1; c.timemethod == 3 && m <= std::max(per, 1); ++m) {   // (no sweeps in the explicit schemes)
     if (m > 2 && m % 2) continue;   // 1, 2, 4, 6, ...
     const int grid = std::max(1, std::min(m * nsm, d.nchunk));
     const float t = time_calls(E, reps, [&] {

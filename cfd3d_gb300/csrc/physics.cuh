@@ -28,6 +28,7 @@ struct Par {
   int npv, ntv, nqq, ngrd;
   int nsteady, iturb, nscheme, nmuscl, nlim, local, prec, fluid, ncav, fix_cav_clamp, with_prop;
   int mixed;   // 1: the mixed-precision form (IF97 sums in df64)
+  int timemethod;   // 1 explicit Euler, 2 third-order Runge-Kutta, 3 LU-SGS
   double dt_phy, cfl, c_v, c_c, pref, uref, str, rhoref, l_chord;
   double kref, oref, emutref;
   double uref_vec[3], tref, y1ref, y2ref;   // free-stream state bcinfo%pv (src/bc_module.f90:133-146)
@@ -911,6 +912,41 @@ __device__ __forceinline__ double eigenvis_of(const Par& c, const double* dv, co
   double den = dv[7] + dv[11] * dv[6] * dv[0] - dv[10] * dv[7] * dv[0];
   if (c.iturb == -2) return fmax(dv[6] * tv[1] / den, 4.0 / 3.0 * tv[0] / dv[0]);
   return fmax(dv[6] * (tv[1] + dv[11] * tv[2] / 0.9) / den, 4.0 / 3.0 * (tv[0] + tv[2]) / dv[0]);
+}
+
+// flowonly_ex / flowturball_ex (src/lhs_module.f90:247-344): the diagonal solve of the
+// explicit schemes -- lhs%getx without spectral radii, viscous shift or source couplings,
+// scaled by a = dt / vol
+__device__ __forceinline__ void getx_explicit(const Par& c, const double* pv, const double* dv, const double* res,
+                                              double dt, double vol, double* x) {
+  const double a = dt / vol;
+  const double bb = (c.nsteady == 1) ? 1.0 : 0.75;
+  const double b = (c.nsteady >= 1) ? (double)c.nsteady * bb * vol / c.dt_phy * a : 0.0;
+  const double b1 = 1.0 + b;
+  const double i_b1 = 1.0 / (b1 * dv[0]);
+  const double uv2 = pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3];
+  const double isnd = 1.0 / sndp2_of<double>(c, dv[5], uv2), idv5 = 1.0 / dv[5];
+  const double ss = dv[0] * dv[11] * (isnd + b * idv5);
+  const double rr = isnd - idv5 + b1 * dv[6];
+  const double hst = dv[1] + 0.5 * uv2 - uv2;
+  const double cross1 = dv[12] * dv[7] - dv[11] * dv[8];
+  const double cross2 = dv[13] * dv[7] - dv[11] * dv[9];
+  const double dhdp1 = 1.0 - dv[10] * dv[0];
+  const double ssy1 = dv[12] * dv[0] * rr + b1 * dv[8] * dhdp1;
+  const double ssy2 = dv[13] * dv[0] * rr + b1 * dv[9] * dhdp1;
+  const double ssh = dv[0] * rr * hst - b1 * dhdp1 * dv[0];
+  const double aaa2 = dv[7] * hst + dv[11] * dv[0] - cross2 * pv[6];
+  const double uuu = res[1] * pv[1] + res[2] * pv[2] + res[3] * pv[3] - res[4];
+  const double coeff2 = res[0] * aaa2 + dv[7] * uuu + cross2 * res[6];
+  const double coeff3 = res[0] * (ssh - ssy2 * pv[6]) + dv[0] * rr * uuu + res[6] * ssy2;
+  const double mm = 1.0 / ss;
+  x[0] = (coeff2 + cross1 * res[5] - cross1 * pv[5] * res[0]) * mm;
+  x[1] = (res[1] - res[0] * pv[1]) * i_b1;
+  x[2] = (res[2] - res[0] * pv[2]) * i_b1;
+  x[3] = (res[3] - res[0] * pv[3]) * i_b1;
+  x[4] = -(coeff3 - ssy1 * pv[5] * res[0] + res[5] * ssy1) * mm * i_b1;
+  for (int v = 5; v < c.npv; ++v) x[v] = (res[v] - res[0] * pv[v]) * i_b1;
+  for (int v = 0; v < c.npv; ++v) x[v] *= a;
 }
 
 // everything of lhs%getx that does not depend on the right-hand side

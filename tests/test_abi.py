@@ -49,7 +49,7 @@ def test_structs_match_header_layout(tmp_path):
 
 def test_create_rejects_bad_config_without_gpu():
     c = cases.make("plain_small", scale=8)
-    c["cfg"]["timemethod"] = 1
+    c["cfg"]["timemethod"] = 4
     with pytest.raises(native.Cfd3dError) as e:
         native.Engine(c)
     assert e.value.code == abi.ERR_ARG
