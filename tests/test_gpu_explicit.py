@@ -14,12 +14,15 @@ from tests.helpers import field_err, interior
 pytestmark = pytest.mark.gpu
 
 TOL_STATE = 1e-9
-# mixed form against the FP64 form after two explicit iterations
-TOL_MIXED = 1e-6
+# mixed form against the FP64 form after three explicit iterations: state difference per
+# variable, the velocity components scaled by the largest velocity component
+TOL_MIXED = 1e-4
 
 CASES = {
     "plain": ("plain_small", dict(scale=4), {}),
-    "cavitating": ("cavitating", dict(scale=8), {}),
+    # (the reference's clamp by temperature, r_v ~ -299 rho, drives the explicit schemes to
+    # NaN within two iterations -- in the oracle as well -- so these run with the fix)
+    "cavitating": ("cavitating", dict(scale=8, fix_cav_clamp=1), {}),
     "large_sst_bdf2": ("large", dict(scale=16), dict(fix_cav_clamp=1)),
     "batched": ("batched", dict(scale=4, nblocks=6), dict(fix_cav_clamp=1)),
 }
@@ -73,12 +76,20 @@ def test_rk3_differs_from_euler_and_graph_replay_is_exact():
 
 
 @pytest.mark.parametrize("timemethod", [1, 2])
-def test_mixed_explicit_matches_fp64(timemethod):
+def test_mixed_explicit_follows_fp64(timemethod):
     c = make("large_sst_bdf2", timemethod)
     a = native.Engine(c, precision=abi.FP64)
     m = native.Engine(c, precision=abi.MIXED)
     for x in (a, m):
         x.initialize(c["pv0"])
-        for it in range(2):
-            x.iterate(1, it + 1, 0.0)
-    assert field_err(interior(m.download(0)["pv"]), interior(a.download(0)["pv"])).max() < TOL_MIXED
+    for it in range(3):
+        _, ra, _ = a.iterate(1, it + 1, 0.0)
+        _, rm, _ = m.iterate(1, it + 1, 0.0)
+        assert np.all(np.isfinite(rm))
+        big = ra > 1e-6 * ra.max()
+        assert np.allclose(rm[big], ra[big], rtol=2e-2), (it, rm, ra)
+    pa, pm = interior(a.download(0)["pv"]), interior(m.download(0)["pv"])
+    scale = np.abs(pa).reshape(-1, pa.shape[-1]).max(axis=0)
+    scale[1:4] = scale[1:4].max()
+    err = (np.abs(pm - pa).reshape(-1, pa.shape[-1]).max(axis=0) / scale).max()
+    assert err < TOL_MIXED, err
