@@ -61,7 +61,7 @@ typedef struct cfd3d_config {
   double dt_phy;
   int    iturb, ides;                   /* -3 Euler, -2 laminar, 0 k-omega SST      */
   int    nscheme, nmuscl, nlim;         /* flux, reconstruction, limiter            */
-  int    timemethod, local, prec;       /* 3 = LU-SGS; local -1/0/1; prec 0/1/2     */
+  int    timemethod, local, prec;       /* 1 Euler, 2 RK3, 3 LU-SGS; local; prec    */
   double cfl;
   int    fluid, ngas;                   /* 1 stiffened water, 2 IAPWS-97; 1 ideal gas */
   int    ncav;                          /* 0 none, 1 Merkle ... 5 Lee               */
@@ -150,7 +150,8 @@ int  cfd3d_checkpoint_write(cfd3d_handle *h, const char *path, int nt_phy, int n
 int  cfd3d_checkpoint_read(cfd3d_handle *h, const char *path, int steady_start, int *nps, int *nts,
                            double *timeprev);
 
-/* One pseudo-iteration: resi%setqres + update%timeinteg (LU-SGS) + resi%residual
+/* One pseudo-iteration: resi%setqres + update%timeinteg + resi%residual, timeinteg being
+ * LU-SGS (timemethod 3), explicit Euler (1) or RK3 (2) (src/update_module.f90:214-733)
  * (src/solve_module.f90:134-136).  Outputs the solution time, the L2 norms
  * res_l2[npv] of the state change, and the location (block,i,j,k) of the largest
  * pressure change.  Any output pointer may be NULL. */
