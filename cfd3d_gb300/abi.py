@@ -15,6 +15,7 @@ ERR_ARG, ERR_CUDA, ERR_NONFINITE, ERR_VOLUME, ERR_TIMEOUT, ERR_DESCRIPTOR, ERR_N
 FP64, MIXED = 0, 1
 
 BC_WALL, BC_SYMMETRY, BC_FARFIELD, BC_EXTRAPOLATE, BC_DEGENERATE, BC_INFLOW = range(1, 7)
+BC_INFLOW_SUBSONIC, BC_OUTFLOW_SUBSONIC, BC_INFLOW_SUPERSONIC, BC_OUTFLOW = range(7, 11)
 BC_NAMES = {
     "BCWall": BC_WALL,
     "BCSymmetryPlane": BC_SYMMETRY,
@@ -24,6 +25,10 @@ BC_NAMES = {
     "BCDegeneratePoint": BC_DEGENERATE,
     "BCDegenerateLine": BC_DEGENERATE,
     "BCInflow": BC_INFLOW,
+    "BCInflowSubsonic": BC_INFLOW_SUBSONIC,
+    "BCOutflowSubsonic": BC_OUTFLOW_SUBSONIC,
+    "BCInflowSupersonic": BC_INFLOW_SUPERSONIC,
+    "BCOutflow": BC_OUTFLOW,
 }
 
 

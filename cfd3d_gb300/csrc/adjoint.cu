@@ -210,7 +210,11 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
           push_cell(a, c, n, src, gp, gd);
           break;
         }
-        case G_FARFIELD: {
+        case G_FARFIELD:
+        case G_INFLOW_SUB:
+        case G_OUTFLOW_SUB:
+        case G_INFLOW_SUP: {
+          const int ffm = ghost_ff_mode(op.kind);
           double nx[3];
           face_vec(d, op.fplane, op.fidx, nx);
           for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;
@@ -222,7 +226,7 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
           bpv[0] = c.pref; bpv[1] = c.uref_vec[0]; bpv[2] = c.uref_vec[1]; bpv[3] = c.uref_vec[2];
           bpv[4] = c.tref; bpv[5] = c.y1ref; bpv[6] = c.y2ref; bpv[7] = c.kref; bpv[8] = c.oref;
           for (int v = 0; v < NPVM; ++v) xp[v] = sp[v];
-          farfield_pv<double>(c, nx, dl, pb, rb, c2b, bpv, c.uref * c.uref, xp);
+          farfield_pv<double>(c, nx, dl, pb, rb, c2b, bpv, c.uref * c.uref, xp, ffm);
           // the ghost's dv and tv(1:2) are its EOS; tv(3) (and tv(1:2) without transport
           // properties) is the mirror cell's
           double ge[4];
@@ -240,7 +244,7 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
             for (int v = 0; v < NPVM; ++v) bp[v] = DD(bpv[v]);
             if (c.uref != 0.0 && 15 >= k0 && 15 < k0 + DC)
               for (int e = 0; e < 3; ++e) bp[1 + e].d[15 - k0] = c.uref_vec[e] / c.uref;
-            farfield_pv<DD>(c, nx, dl, pbd, seed(rb, 13, k0), seed(c2b, 14, k0), bp, ur * ur, x);
+            farfield_pv<DD>(c, nx, dl, pbd, seed(rb, 13, k0), seed(c2b, 14, k0), bp, ur * ur, x, ffm);
             for (int qq = 0; qq < DC && k0 + qq < 16; ++qq) {
               double s = 0.0;
               for (int v = 0; v < npv; ++v) s += gp[v] * x[v].d[qq];

@@ -237,7 +237,10 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       store_cell(d, c, op.dst, x);
       return;
     }
-    case G_FARFIELD: {
+    case G_FARFIELD:
+    case G_INFLOW_SUB:
+    case G_OUTFLOW_SUB:
+    case G_INFLOW_SUP: {
       load_cell(d, c, op.src, x);
       double nx[3];
       face_vec(d, op.fplane, op.fidx, nx);
@@ -251,7 +254,7 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       bp[0] = c.pref; bp[1] = c.uref_vec[0]; bp[2] = c.uref_vec[1]; bp[3] = c.uref_vec[2];
       bp[4] = c.tref; bp[5] = c.y1ref; bp[6] = c.y2ref; bp[7] = c.kref; bp[8] = c.oref;
       double* pv = x.pv;
-      farfield_pv<double>(c, nx, dl, pb, rb, c2b, bp, c.uref * c.uref, pv);
+      farfield_pv<double>(c, nx, dl, pb, rb, c2b, bp, c.uref * c.uref, pv, ghost_ff_mode(op.kind));
       deteos(c.fluid, c.with_prop, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
       store_cell(d, c, op.dst, x);
       return;

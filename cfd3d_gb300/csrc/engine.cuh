@@ -31,8 +31,14 @@ enum { GM_CX = 0, GM_EX = 3, GM_TX = 6, GM_GRD = 9 };
 
 enum GhostKind : int {
   G_COPY = 0, G_EXTRAP, G_WALL_VISCOUS, G_WALL_KW, G_SYMMETRY, G_FARFIELD,
-  G_WALLWALL, G_WALLWALL_KW4, G_WALLWALL_KW8, G_NOWALL3, G_NOWALL7
+  G_WALLWALL, G_WALLWALL_KW4, G_WALLWALL_KW8, G_NOWALL3, G_NOWALL7,
+  G_INFLOW_SUB, G_OUTFLOW_SUB, G_INFLOW_SUP   // the farfield treatment with a forced branch
 };
+
+// the farfield_pv branch of a characteristic ghost kind
+__host__ __device__ inline int ghost_ff_mode(int kind) {
+  return kind == G_INFLOW_SUB ? 3 : kind == G_OUTFLOW_SUB ? 1 : kind == G_INFLOW_SUP ? 2 : 0;
+}
 
 // one ghost cell write of the compiled boundary program
 struct GhostOp {

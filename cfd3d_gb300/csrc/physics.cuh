@@ -75,23 +75,33 @@ __device__ __forceinline__ R sndp2_du_of(const Par& c, R snd2, R u2) {
 // and velocity pb[0..3], density rb and sound speed c2b and the free-stream state bp, by the
 // sign and size of the normal Mach number; pv holds the mirror cell's values on entry.  nx
 // is the outward face vector, dl its inverse length.  Templated for the adjoint.
+// The characteristic ghost state of bcfarfield (src/bc_module.f90:2904-3013): by the sign and
+// size of the boundary cell's normal Mach number, the supersonic outflow (mirror), subsonic
+// outflow, supersonic inflow or subsonic inflow treatment.  mode forces one branch, as the
+// dedicated BCs do: FF_OUT_SUB bcoutflowsubsonic (:2699-2869), FF_IN_SUP bcinflowsupersonic
+// (:2642-2678), FF_IN_SUB bcinflowsubsonic (:2464-2640) -- each the same formula as the
+// farfield branch of that name, with bcinfo%pressure = pref.
+enum FarfieldMode { FF_MACH = 0, FF_OUT_SUB = 1, FF_IN_SUP = 2, FF_IN_SUB = 3 };
+
 template <class T>
 __device__ __forceinline__ void farfield_pv(const Par& c, const double* nx, double dl, const T* pb, T rb, T c2b,
-                                            const T* bp, T uref2, T* pv) {
+                                            const T* bp, T uref2, T* pv, int mode = FF_MACH) {
   T vel = (pb[1] * nx[0] + pb[2] * nx[1] + pb[3] * nx[2]) * dl;
-  T mach = vel / sqrt(c2b);
   T a = sqrt(sndp2_u<T>(c, c2b, vel * vel, uref2));
-  if (mach >= 0.0) {
-    if (mach < 1.0) {
-      pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
-      for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (pb[1 + q3] + nx[q3] * (pb[0] + bp[0] - c.pref) / rb / a * dl) - pv[1 + q3];
-    }
-  } else if (mach <= -1.0) {
+  int br = mode;
+  if (mode == FF_MACH) {
+    T mach = vel / sqrt(c2b);
+    br = (mach >= 0.0) ? ((mach < 1.0) ? FF_OUT_SUB : FF_MACH) : ((mach <= -1.0) ? FF_IN_SUP : FF_IN_SUB);
+  }
+  if (br == FF_OUT_SUB) {
+    pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
+    for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (pb[1 + q3] + nx[q3] * (pb[0] + bp[0] - c.pref) / rb / a * dl) - pv[1 + q3];
+  } else if (br == FF_IN_SUP) {
     pv[0] = 2.0 * (c.pref - bp[0]) - pv[0];
     for (int v = 1; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
     pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
     pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
-  } else {
+  } else if (br == FF_IN_SUB) {
     T var = c.pref - bp[0] + pb[0] - rb * a * (nx[0] * (bp[1] - pb[1]) + nx[1] * (bp[2] - pb[2]) + nx[2] * (bp[3] - pb[3])) * dl;
     pv[0] = var - pv[0];
     for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (bp[1 + q3] + nx[q3] * 0.5 * var / rb / a * dl) - pv[1 + q3];

@@ -456,7 +456,10 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
         case CFD3D_BC_SYMMETRY: bi.kind = G_SYMMETRY; break;
         case CFD3D_BC_FARFIELD: bi.kind = G_FARFIELD; bi.farfield_sign = true; break;
         case CFD3D_BC_EXTRAPOLATE: case CFD3D_BC_DEGENERATE: bi.kind = G_EXTRAP; break;
-        case CFD3D_BC_INFLOW: bi.kind = -1; break;
+        case CFD3D_BC_INFLOW_SUBSONIC: bi.kind = G_INFLOW_SUB; bi.farfield_sign = true; break;
+        case CFD3D_BC_OUTFLOW_SUBSONIC: bi.kind = G_OUTFLOW_SUB; bi.farfield_sign = true; break;
+        case CFD3D_BC_INFLOW_SUPERSONIC: bi.kind = G_INFLOW_SUP; bi.farfield_sign = true; break;
+        case CFD3D_BC_INFLOW: case CFD3D_BC_OUTFLOW: bi.kind = -1; break;   // bcinflow / bcoutflow: no-ops
         default: E.err = "unknown bc type"; return false;
       }
       for (int q = 0; q < 6; ++q) for (int r = 0; r < 3; ++r) bi.nb[q][r] = 0;
@@ -485,7 +488,7 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
             op.bnd = op.src;
             for (int q = 0; q < 6; ++q) op.nb[q] = -1;
             op.fidx = op.src; op.fplane = GM_CX; op.fsign = 1.0f;
-            if (bi.kind == G_SYMMETRY || bi.kind == G_FARFIELD || bi.kind == G_WALL_KW) {
+            if (bi.kind == G_SYMMETRY || bi.kind == G_FARFIELD || bi.kind == G_WALL_KW || ghost_ff_mode(bi.kind)) {
               int ii = mi, jj = mj, kk = mk;
               float s = bi.farfield_sign ? -1.0f : 1.0f;
               switch (bi.face) {

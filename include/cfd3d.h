@@ -53,6 +53,10 @@ extern "C" {
 #define CFD3D_BC_EXTRAPOLATE  4   /* BCExtrapolate / BCOutflowSupersonic              */
 #define CFD3D_BC_DEGENERATE   5   /* BCDegeneratePoint / BCDegenerateLine             */
 #define CFD3D_BC_INFLOW       6   /* BCInflow (the reference's routine is a no-op)    */
+#define CFD3D_BC_INFLOW_SUBSONIC    7   /* BCInflowSubsonic: characteristic, free-stream state */
+#define CFD3D_BC_OUTFLOW_SUBSONIC   8   /* BCOutflowSubsonic: characteristic, p = pref        */
+#define CFD3D_BC_INFLOW_SUPERSONIC  9   /* BCInflowSupersonic: free-stream state imposed      */
+#define CFD3D_BC_OUTFLOW           10   /* BCOutflow (the reference's routine is a no-op)     */
 
 /* Solver configuration: the fields of the reference's input.inp
  * (src/config_module.f90:100-119, documented in bin/input_templet.inp:34-66). */

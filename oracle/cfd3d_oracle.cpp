@@ -55,6 +55,7 @@ enum Face { F_IMIN, F_IMAX, F_JMIN, F_JMAX, F_KMIN, F_KMAX, F_KMIN_CAP, F_KMAX_C
 
 enum BcKind {
   K_WALL_INVISCID, K_WALL_VISCOUS, K_WALL_KW, K_FARFIELD, K_EXTRAP, K_SYMMETRY, K_NOOP,
+  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP,
   K_EDGE_WALLWALL, K_EDGE_WALLWALL_KW, K_EDGE_NOWALL, K_CORNER_WALLWALL, K_CORNER_WALLWALL_KW, K_CORNER_NOWALL
 };
 
@@ -394,7 +395,10 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
       case CFD3D_BC_SYMMETRY: bi.kind = K_SYMMETRY; break;
       case CFD3D_BC_FARFIELD: bi.kind = K_FARFIELD; break;
       case CFD3D_BC_EXTRAPOLATE: case CFD3D_BC_DEGENERATE: bi.kind = K_EXTRAP; break;
-      case CFD3D_BC_INFLOW: bi.kind = K_NOOP; break;
+      case CFD3D_BC_INFLOW: case CFD3D_BC_OUTFLOW: bi.kind = K_NOOP; break;   /* bcinflow, bcoutflow */
+      case CFD3D_BC_INFLOW_SUBSONIC: bi.kind = K_INFLOW_SUB; break;    /* bcinflowsubsonic :2464-2640 */
+      case CFD3D_BC_OUTFLOW_SUBSONIC: bi.kind = K_OUTFLOW_SUB; break;  /* bcoutflowsubsonic :2699-2869 */
+      case CFD3D_BC_INFLOW_SUPERSONIC: bi.kind = K_INFLOW_SUP; break;  /* bcinflowsupersonic :2642-2678 */
       default: err = "unknown bc type"; return false;
     }
     bc_reference_state(c, bi);
@@ -753,7 +757,10 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
             put_cell(c, B, i, j, k, pv, dv, tv);
             break;
           }
-          case K_FARFIELD: {
+          case K_FARFIELD:
+          case K_INFLOW_SUB:
+          case K_OUTFLOW_SUB:
+          case K_INFLOW_SUP: {
             int ii = 0, jj = 0, kk = 0;
             face_cell(bi, B, i, j, k, ii, jj, kk, nx, true);
             const double* Pb = B.pv.at(ii, jj, kk);
@@ -765,6 +772,10 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
             double vel = (pvs[1] * nx[0] + pvs[2] * nx[1] + pvs[3] * nx[2]) * dl;
             double mach = vel / std::sqrt(dvs[5]);
             double a = std::sqrt(sndp2_of(c, dvs[5], sq(vel)));
+            /* the dedicated BCs are the farfield branch of their name, whatever the Mach number */
+            if (bi.kind == K_OUTFLOW_SUB) mach = 0.0;
+            else if (bi.kind == K_INFLOW_SUP) mach = -1.0;
+            else if (bi.kind == K_INFLOW_SUB) mach = -0.5;
             if (mach >= 0.0) {
               if (mach < 1.0) {
                 pv[0] = 2.0 * (bi.pressure - bi.pv[0]) - pv[0];

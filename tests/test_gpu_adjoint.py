@@ -55,8 +55,19 @@ def _engine(c, cfg=None):
     return native.Engine(cc, precision=abi.FP64)
 
 
-def _prepared(scale):
+def _with_inout(c):
+    """subsonic inflow at imin and subsonic outflow at imax instead of the far field"""
+    for b in c["blocks"]:
+        im, jm, km = b["imax"], b["jmax"], b["kmax"]
+        repl = {(1, 1, 1, 1, jm, km): abi.BC_INFLOW_SUBSONIC, (im, 1, 1, im, jm, km): abi.BC_OUTFLOW_SUBSONIC}
+        b["bc"] = [(repl.get(tuple(p), k), p) for k, p in b["bc"]]
+    return c
+
+
+def _prepared(scale, inout=False):
     c = _state(scale)
+    if inout:
+        c = _with_inout(c)
     e = _engine(c)
     e.initialize(c["pv0"])
     s = adjoint.StateSetter(e)
@@ -77,6 +88,11 @@ def c4():
 @pytest.fixture(scope="module")
 def c4_small():
     return _prepared(4)
+
+
+@pytest.fixture(scope="module")
+def c4_inout():
+    return _prepared(4, inout=True)
 
 
 def _typical(pv, v):
@@ -210,3 +226,16 @@ def test_vjp_is_linear_in_the_cotangent(c4_small):
     ref = 2.0 * g1[0] - 3.0 * g2[0]
     assert np.abs(g3[0] - ref).max() <= 1e-9 * np.abs(ref).max()
     assert np.allclose(p3, 2.0 * p1 - 3.0 * p2, rtol=1e-9, atol=1e-9 * np.abs(p3).max())
+
+
+def test_vjp_through_subsonic_inflow_and_outflow(c4_inout):
+    """boundary rows next to bcinflowsubsonic / bcoutflowsubsonic ghosts"""
+    d = c4_inout
+    s = d["s"]
+    km, jm, im = d["pv"].shape[:-1]
+    entries = [(k, j, 0 if q % 2 == 0 else im - 1, v)
+               for q, (k, j, _, v) in enumerate(_entries(d["pv"].shape[:-1], d["pv"].shape[-1], 18, 3))]
+    used, errs, rows = _check(lambda p: s.residual([p])[0], d, entries)
+    print(f"in/outflow rows: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
+    assert used >= len(entries) - 2, rows
+    assert errs.max() <= TOL, (errs, rows)

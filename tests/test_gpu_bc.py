@@ -1,0 +1,73 @@
+"""Characteristic inflow / outflow boundaries through the C ABI against the CPU oracle:
+bcinflowsubsonic, bcoutflowsubsonic and bcinflowsupersonic (src/bc_module.f90:2464-2869),
+on single-phase Euler, cavitating laminar and SST cases, in both arithmetic forms."""
+import numpy as np
+import pytest
+
+from cfd3d_gb300 import abi, cases, native
+from tests.helpers import field_err, interior
+
+pytestmark = pytest.mark.gpu
+
+TOL_RES = 1e-9
+TOL_STATE = 1e-9
+TOL_MIXED = 1e-5
+
+BASES = {
+    "plain": ("plain_small", dict(scale=4), {}),
+    "cavitating": ("cavitating", dict(scale=8, fix_cav_clamp=1), {}),
+    "sst": ("large", dict(scale=16), dict(fix_cav_clamp=1, nsteady=0)),
+}
+BCSETS = {
+    "subsonic": {"imin": abi.BC_INFLOW_SUBSONIC, "imax": abi.BC_OUTFLOW_SUBSONIC},
+    "supersonic_in": {"imin": abi.BC_INFLOW_SUPERSONIC, "imax": abi.BC_EXTRAPOLATE},
+    "out_only": {"imin": abi.BC_FARFIELD, "imax": abi.BC_OUTFLOW_SUBSONIC},
+}
+
+
+def make(base, bcset):
+    name, kw, over = BASES[base]
+    c = cases.make(name, **kw)
+    c["cfg"].update(over)
+    for b in c["blocks"]:
+        im, jm, km = b["imax"], b["jmax"], b["kmax"]
+        faces = {"imin": (1, 1, 1, 1, jm, km), "imax": (im, 1, 1, im, jm, km)}
+        bc = []
+        for kind, pnts in b["bc"]:
+            face = next((f for f, p in faces.items() if tuple(p) == tuple(pnts)), None)
+            bc.append((BCSETS[bcset][face], pnts) if face in BCSETS[bcset] else (kind, pnts))
+        b["bc"] = bc
+    return c
+
+
+@pytest.mark.parametrize("bcset", list(BCSETS))
+@pytest.mark.parametrize("base", list(BASES))
+def test_residual_and_iterations_match(oracle, base, bcset):
+    c = make(base, bcset)
+    e = native.Engine(c)
+    o = oracle.Oracle(c)
+    e.initialize(c["pv0"])
+    o.initialize(c["pv0"])
+    for b in range(len(c["blocks"])):
+        assert field_err(e.residual(b)["res"], o.residual(b)["res"]).max() < TOL_RES
+    for it in range(3):
+        _, resg, _ = e.iterate(1, it + 1, 0.0)
+        _, reso, _ = o.iterate(1, it + 1, 0.0)
+        assert np.all(np.isfinite(resg))
+        assert np.allclose(resg, reso, rtol=1e-7, atol=1e-9 * np.abs(reso).max()), (it, resg, reso)
+    for b in range(len(c["blocks"])):
+        sg, so = e.download(b), o.get_state(b)
+        assert field_err(interior(sg["pv"]), interior(so["pv"])).max() < TOL_STATE
+        # the ghost layers the boundary program writes
+        assert field_err(sg["pv"][3:-3, 3:-3, :3], so["pv"][3:-3, 3:-3, :3]).max() < TOL_STATE
+        assert field_err(sg["pv"][3:-3, 3:-3, -3:], so["pv"][3:-3, 3:-3, -3:]).max() < TOL_STATE
+
+
+@pytest.mark.parametrize("bcset", ["subsonic", "supersonic_in"])
+def test_mixed_residual(oracle, bcset):
+    c = make("sst", bcset)
+    e = native.Engine(c, precision=abi.MIXED)
+    o = oracle.Oracle(c)
+    e.initialize(c["pv0"])
+    o.initialize(c["pv0"])
+    assert field_err(e.residual(0)["res"], o.residual(0)["res"]).max() < TOL_MIXED
