@@ -304,7 +304,9 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
 }
 
 // ------------------------------------------------------------------ residual + sources
-template <bool MX>
+// REC = false (the explicit schemes): the residual alone, without the sweep records (a
+// separate instantiation, so that the LU-SGS kernel carries no branch for it)
+template <bool MX, bool REC = true>
 __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
@@ -511,7 +513,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     }
   }
   for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
-  if (c.timemethod != 3) return;   // the explicit schemes need no sweep records
+  if constexpr (!REC) return;   // the explicit schemes need no sweep records
   // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous
   // term), written with its state and residual as the cell's sweep record at pos[g]
   double tvc[3] = {0.0, 0.0, 0.0};
@@ -796,7 +798,7 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
 // (:324-453), pv = a1 rk + a2 pv + a3 getx_ex(res), rk being the state before the
 // iteration (kept in dqs at t by stage 1).  The residual norms measure the change over
 // the whole iteration (they are final after the last stage).
-template <bool MX>
+template <bool MX, bool EX = false>
 __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
   // grid-stride over the interior cells: the grid is a fixed multiple of the SM count,
   // so the per-CTA partials (and the order they are summed in) do not depend on size
@@ -812,7 +814,7 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
     long long g = interior_cell(d.blk[b], t - d.blk[b].int_off, i, j, k);
     const long long n = d.ncell;
     double old[NPVM], p[NPVM];
-    if (stage == 0) {
+    if constexpr (!EX) {
       const long long pq = d.pos[g];   // plane-major position of the sweep's dq
       for (int v = 0; v < npv; ++v) {
         old[v] = d.pv[v * n + g];
@@ -1097,8 +1099,13 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   if (c.mixed) launch_face_flux_mixed(E, s);
   else launch_face_flux(E, s);
   stage(3);
-  if (c.mixed) k_rhs<true><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
-  else k_rhs<false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+  if (c.timemethod != 3) {
+    if (c.mixed) k_rhs<true, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+    else k_rhs<false, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+  } else {
+    if (c.mixed) k_rhs<true><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+    else k_rhs<false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+  }
   stage(4);
   n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
@@ -1112,13 +1119,13 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
           if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
         if (c.mixed) launch_face_flux_mixed(E, s);
         else launch_face_flux(E, s);
-        if (c.mixed) k_rhs<true><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
-        else k_rhs<false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+        if (c.mixed) k_rhs<true, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+        else k_rhs<false, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
         n += c.mixed ? 8 : 4;
       }
       if (m == nstage) { stage(5); stage(6); }
-      if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c, m);
-      else k_update<false><<<E.red_grid, T, 0, s>>>(d, c, m);
+      if (c.mixed) k_update<true, true><<<E.red_grid, T, 0, s>>>(d, c, m);
+      else k_update<false, true><<<E.red_grid, T, 0, s>>>(d, c, m);
       ++n;
       if (m == nstage) stage(7);
       if (c.iturb == 0) {
