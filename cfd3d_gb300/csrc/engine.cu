@@ -518,18 +518,37 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   // term), written with its state and residual as the cell's sweep record at pos[g]
   double tvc[3] = {0.0, 0.0, 0.0};
   for (int q = 0; q < c.ntv; ++q) tvc[q] = d.tv[q * n + g];
+  // face vectors cx1, cx2, ex1, ex2, tx1, tx2: FP64, or (mixed form) their FP32 copies
   double fc[18];
+  float fcf[18];
   for (int q = 0; q < 3; ++q) {
-    fc[q] = d.gm[(GM_CX + q) * n + g - 1]; fc[3 + q] = d.gm[(GM_CX + q) * n + g];
-    fc[6 + q] = d.gm[(GM_EX + q) * n + g - sj]; fc[9 + q] = d.gm[(GM_EX + q) * n + g];
-    fc[12 + q] = d.gm[(GM_TX + q) * n + g - sk]; fc[15 + q] = d.gm[(GM_TX + q) * n + g];
+    const long long o6[6] = {(GM_CX + q) * n + g - 1, (GM_CX + q) * n + g, (GM_EX + q) * n + g - sj,
+                             (GM_EX + q) * n + g, (GM_TX + q) * n + g - sk, (GM_TX + q) * n + g};
+    for (int m = 0; m < 6; ++m) {
+      if (MX) fcf[3 * m + q] = d.gmf[o6[m]];
+      else fc[3 * m + q] = d.gm[o6[m]];
+    }
   }
   double ic[4] = {0, 0, 0, 0}, it4[4] = {0, 0, 0, 0};
   if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
   if (c.iturb == 0) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
   Diag D;
-  const double evis = eigenvis_of(c, dv, tvc);
-  diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D);
+  double evis;
+  float pvf[NPVM], dvf[12];
+  if (MX) {
+    // the spectral radius and the viscous eigenvalue only size the diagonal block: FP32
+    // (the block's closed-form inverse stays FP64)
+    for (int q = 0; q < NPVM; ++q) pvf[q] = (q < npv) ? (float)pv2[q] : 0.0f;
+    for (int q = 0; q < 12; ++q) dvf[q] = (float)dv[q];
+    float tvf[3] = {(float)tvc[0], (float)tvc[1], (float)tvc[2]};
+    float lam_fs[2];
+    diag_spectral_f(c, pvf, dvf[5], fcf, lam_fs);
+    evis = (double)eigenvis_f(c, dvf, tvf);
+    diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D, lam_fs);
+  } else {
+    evis = eigenvis_of(c, dv, tvc);
+    diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D);
+  }
   double o[NREC];
   for (int q = 0; q < NREC; ++q) o[q] = 0.0;
   const int pvi[7] = {1, 2, 3, 5, 6, 7, 8};
@@ -539,21 +558,18 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   diag_to_array(D, o + REC_DIAG);
   if (MX) {
     // the spectral radii only scale the implicit operator: FP32
-    float pvf[NPVM], dvf[6];
-    for (int q = 0; q < NPVM; ++q) pvf[q] = (q < npv) ? (float)pv2[q] : 0.0f;
-    for (int q = 0; q < 6; ++q) dvf[q] = (float)dv[q];
-    for (int q = 0; q < 6; ++q) {
-      const float nf[3] = {(float)fc[3 * q], (float)fc[3 * q + 1], (float)fc[3 * q + 2]};
-      o[REC_SPEC + q] = (double)face_spectral<float>(c, nf, pvf, dvf);
-    }
+    for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = (double)face_spectral<float>(c, fcf + 3 * q, pvf, dvf);
   } else {
     for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = face_spectral<double>(c, fc + 3 * q, pv2, dv);
   }
   // beta = 1/sndp2 - 1/c2 + drho/dp = D.rr - (D.b1 - 1) drho/dp
   o[REC_BETA] = D.rr - (D.b1 - 1.0) * dv[6];
-  o[REC_EVV] = 2.0 * evis / vol;
+  // (the mixed form's sweeps read the face vectors and this viscous term from the FP32
+  // records)
+  o[REC_EVV] = MX ? (double)(2.0f * (float)evis / (float)vol) : 2.0 * evis / vol;
   for (int e = 0; e < 3; ++e) {
-    o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e];
+    if (MX) { o[REC_FACE + e] = fcf[3 + e]; o[REC_FACE + 3 + e] = fcf[9 + e]; o[REC_FACE + 6 + e] = fcf[15 + e]; }
+    else { o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e]; }
   }
   for (int v = 0; v < npv; ++v) o[REC_RES + v] = res[v];
   const long long nint = d.nint, tp = d.pos[g];

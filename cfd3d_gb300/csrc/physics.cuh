@@ -1092,9 +1092,12 @@ struct Diag {
 };
 
 // evis = eigenvis_of(c, dv, tv), which the caller also needs
+// lam_fs (optional): the spectral radius lamda and the face-vector sum fs formed by the
+// caller (the mixed form takes them in FP32: they only size the block)
 __device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, const double* dv, double evis,
                                              const double* fc /* cx1,cx2,ex1,ex2,tx1,tx2 x3 */, double vol,
-                                             double dt, const double* icav, const double* itt, Diag& D) {
+                                             double dt, const double* icav, const double* itt, Diag& D,
+                                             const float* lam_fs = nullptr) {
   // (the reference's repeated quotients are formed once: one reciprocal of c2, of the
   // preconditioned c2 and of the volume; the FP64 pipe is the scarce unit of a GB300)
   double uv2 = pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3];
@@ -1103,7 +1106,8 @@ __device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, con
   const double qr = sndp2 * idv5, qh = 0.5 * (1.0 + qr), qd = sq(1.0 - qr);
   const double cappa = 1.05;
   double lamda = 0.0, fs = 0.0;
-  for (int d = 0; d < 3; ++d) {
+  if (lam_fs) { lamda = (double)lam_fs[0]; fs = (double)lam_fs[1]; }
+  for (int d = 0; d < 3 && !lam_fs; ++d) {
     double ox = 0.5 * (fc[6 * d + 0] + fc[6 * d + 3]);
     double oy = 0.5 * (fc[6 * d + 1] + fc[6 * d + 4]);
     double oz = 0.5 * (fc[6 * d + 2] + fc[6 * d + 5]);
@@ -1138,6 +1142,27 @@ __device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, con
   D.aaa2 = dv[7] * hst + dv[11] * dv[0] - D.cross2 * pv[6];
   D.mm = 1.0 / (D.b1 * dv[0] * (D.ss + D.c[0] * D.cross1) - D.c[1] * D.ssy1 + D.c[2] * D.ss);
   D.tt = 1.0 / (D.t[1] * D.t[2] - (D.t[0] + D.b1 * dv[0]) * (D.t[3] + D.b1 * dv[0]));
+}
+
+// lhs%eigen (src/lhs_module.f90:459-496) in FP32: the spectral radius of the cell and the
+// sum of its squared mean face vectors, from FP32 state and face vectors
+__device__ __forceinline__ void diag_spectral_f(const Par& c, const float* pv, float c2, const float* fc,
+                                                float* lam_fs) {
+  const float uv2 = pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3];
+  const float sndp2 = sndp2_of<float>(c, c2, uv2);
+  const float qr = sndp2 / c2, qh = 0.5f * (1.0f + qr), qd = (1.0f - qr) * (1.0f - qr);
+  float lamda = 0.0f, fs = 0.0f;
+  for (int d = 0; d < 3; ++d) {
+    const float ox = 0.5f * (fc[6 * d + 0] + fc[6 * d + 3]);
+    const float oy = 0.5f * (fc[6 * d + 1] + fc[6 * d + 4]);
+    const float oz = 0.5f * (fc[6 * d + 2] + fc[6 * d + 5]);
+    const float ds = ox * ox + oy * oy + oz * oz;
+    const float u = ox * pv[1] + oy * pv[2] + oz * pv[3];
+    lamda += 1.05f * (fabsf(qh * u) + 0.5f * sqrtf(u * u * qd + 4.0f * sndp2 * ds));
+    fs += ds;
+  }
+  lam_fs[0] = lamda;
+  lam_fs[1] = fs;
 }
 
 // x = D^-1 res (lhs%getx)
