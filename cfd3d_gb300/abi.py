@@ -16,6 +16,7 @@ FP64, MIXED = 0, 1
 
 BC_WALL, BC_SYMMETRY, BC_FARFIELD, BC_EXTRAPOLATE, BC_DEGENERATE, BC_INFLOW = range(1, 7)
 BC_INFLOW_SUBSONIC, BC_OUTFLOW_SUBSONIC, BC_INFLOW_SUPERSONIC, BC_OUTFLOW = range(7, 11)
+BC_WALL_COUNTERROTATING, BC_MASSFLOWRATE_IN, BC_SHIFTED_PERIODIC = 11, 13, 14
 BC_NAMES = {
     "BCWall": BC_WALL,
     "BCSymmetryPlane": BC_SYMMETRY,
@@ -29,6 +30,8 @@ BC_NAMES = {
     "BCOutflowSubsonic": BC_OUTFLOW_SUBSONIC,
     "BCInflowSupersonic": BC_INFLOW_SUPERSONIC,
     "BCOutflow": BC_OUTFLOW,
+    "BCMassflowrateIn": BC_MASSFLOWRATE_IN,
+    "BCShiftedPeriodic": BC_SHIFTED_PERIODIC,
 }
 
 

@@ -195,6 +195,39 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
           push_cell(a, c, n, src, gp, gd);
           break;
         }
+        case G_CRWALL_KW:
+          // u, v, w, k and mu_t reflected, omega and the rest the source cell's
+          gp[1] = -gp[1]; gp[2] = -gp[2]; gp[3] = -gp[3]; gp[7] = -gp[7];
+          gd[GD_MUT] = -gd[GD_MUT];
+          push_cell(a, c, n, src, gp, gd);
+          break;
+        case G_MASSFLOW_IN: {
+          // ghost pv: p = p_src, u = -u_src, T.. = 2 ref - src (y1, y2 clipped); dv and
+          // tv(1:2) its EOS, tv(3) the source cell's
+          double sp[NPVM], xp[NPVM];
+          for (int v = 0; v < NPVM; ++v) sp[v] = (v < npv) ? d.pv[v * n + src] : 0.0;
+          const double bpv[NPVM] = {c.pref, c.uref_vec[0], c.uref_vec[1], c.uref_vec[2], c.tref, c.y1ref, c.y2ref,
+                                    c.kref, c.oref};
+          for (int v = 0; v < NPVM; ++v) xp[v] = sp[v];
+          for (int v = 1; v < 4; ++v) xp[v] = -sp[v];
+          for (int v = 4; v < npv; ++v) xp[v] = 2.0 * bpv[v] - sp[v];
+          const bool c5 = xp[5] > 0.0 && xp[5] < 1.0, c6 = xp[6] > 0.0 && xp[6] < 1.0;
+          xp[5] = fmin(fmax(xp[5], 0.0), 1.0);
+          xp[6] = fmin(fmax(xp[6], 0.0), 1.0);
+          double ge[4];
+          eos_chain(c, xp[0] + bpv[0], xp[4], xp[5], xp[6], gd, ge);
+          gp[0] += ge[0]; gp[4] += ge[1]; gp[5] += ge[2]; gp[6] += ge[3];
+          aadd(&a.gdt[GD_MUT * n + src], gd[GD_MUT]);
+          if (!c.with_prop) { aadd(&a.gdt[GD_VIS * n + src], gd[GD_VIS]); aadd(&a.gdt[GD_CON * n + src], gd[GD_CON]); }
+          // d(ghost pv)/d(source pv): 1 for p, -1 for the rest (0 where a clip is active)
+          aadd(&a.gpv[src], gp[0]);
+          for (int v = 1; v < npv; ++v) {
+            double s = -gp[v];
+            if ((v == 5 && !c5) || (v == 6 && !c6)) s = 0.0;
+            aadd(&a.gpv[v * n + src], s);
+          }
+          break;
+        }
         case G_SYMMETRY: {
           // u_ghost = 2 (u_b - n (u_b . n) / |n|^2) - u_src
           double nx[3];

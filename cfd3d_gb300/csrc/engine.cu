@@ -259,6 +259,31 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       store_cell(d, c, op.dst, x);
       return;
     }
+    case G_CRWALL_KW:
+      // bccounterrotatingwallviscouskw (src/bc_module.f90:3654-3731) with the grid velocity
+      // omega x r = 0 (no rotation): u, v, w, k and mu_t reflected; omega is the mirror's,
+      // the reference's wall value being computed and then discarded
+      load_cell(d, c, op.src, x);
+      x.pv[1] = -x.pv[1]; x.pv[2] = -x.pv[2]; x.pv[3] = -x.pv[3]; x.pv[7] = -x.pv[7];
+      x.tv[2] = -x.tv[2];
+      store_cell(d, c, op.dst, x);
+      return;
+    case G_MASSFLOW_IN: {
+      // bcmassflowratein (:3812-4012) with the rate 0 its construct sets: the inflow speed
+      // m / (rho A) is 0, so the velocity reflects; T, y1, y2, k, omega from the free stream;
+      // the pressure stays the mirror's; EOS of the ghost state
+      load_cell(d, c, op.src, x);
+      const double bp[NPVM] = {c.pref, c.uref_vec[0], c.uref_vec[1], c.uref_vec[2], c.tref, c.y1ref, c.y2ref,
+                               c.kref, c.oref};
+      double* pv = x.pv;
+      for (int q3 = 1; q3 < 4; ++q3) pv[q3] = -pv[q3];
+      for (int v = 4; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
+      pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
+      pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
+      deteos(c.fluid, c.with_prop, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      store_cell(d, c, op.dst, x);
+      return;
+    }
     case G_WALLWALL:
     case G_WALLWALL_KW4:
     case G_WALLWALL_KW8: {

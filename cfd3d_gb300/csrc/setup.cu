@@ -322,7 +322,7 @@ bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
       const cfd3d_block_desc& d = blocks[b];
       HBlock& B = H[b];
       for (int n = 0; n < d.nbc; ++n) {
-        if (d.bc[n].type != CFD3D_BC_WALL) continue;
+        if (d.bc[n].type != CFD3D_BC_WALL && d.bc[n].type != CFD3D_BC_WALL_COUNTERROTATING) continue;
         const int* p = d.bc[n].pnts;
         int ax = -1;
         for (int a = 0; a < 3; ++a) if (p[a] == p[3 + a]) ax = a;
@@ -413,6 +413,7 @@ struct Bc {
   int s[3], e[3], o[3] = {0, 0, 0}, dir[3] = {0, 0, 0};
   int nb[6][3];
   bool farfield_sign = false;
+  bool shifted = false;   // bcshiftedperiodic: copies from 16 cells along i and the face normal
 };
 
 int wall_kind(const Par& c) {
@@ -453,6 +454,11 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
       bi.face = (Face)(2 * ax + (mn ? 0 : 1));
       switch (bi.type) {
         case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
+        // the counter-rotating family without rotation: the laminar and inviscid variants
+        // are the plain wall's and symmetry's formulas, the SST one differs
+        case CFD3D_BC_WALL_COUNTERROTATING: bi.kind = (c.iturb == 0) ? G_CRWALL_KW : wall_kind(c); break;
+        case CFD3D_BC_MASSFLOWRATE_IN: bi.kind = G_MASSFLOW_IN; break;
+        case CFD3D_BC_SHIFTED_PERIODIC: bi.kind = G_COPY; bi.shifted = true; break;
         case CFD3D_BC_SYMMETRY: bi.kind = G_SYMMETRY; break;
         case CFD3D_BC_FARFIELD: bi.kind = G_FARFIELD; bi.farfield_sign = true; break;
         case CFD3D_BC_EXTRAPOLATE: case CFD3D_BC_DEGENERATE: bi.kind = G_EXTRAP; break;
@@ -467,7 +473,7 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
     }
     auto is_surf = [&](const int* pnt, std::initializer_list<int> axes) {
       for (auto& bc : bcs) {
-        if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_SYMMETRY) continue;
+        if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_SYMMETRY) continue;
         bool in = true;
         for (int a : axes) in = in && bc.s[a] <= pnt[a] && bc.e[a] >= pnt[a];
         if (in) return true;
@@ -475,6 +481,7 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
       return false;
     };
     // emits the ghost ops of one descriptor into a phase
+    bool shift_err = false;
     auto emit = [&](const Bc& bi, int phase, int nnb, bool skip_zero_nb) {
       if (bi.kind < 0) return;
       for (int k = bi.s[2]; k <= bi.e[2]; ++k)
@@ -484,6 +491,24 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
             op.kind = bi.kind;
             op.dst = gi(i, j, k);
             int mi = bi.o[0] + bi.dir[0] * i, mj = bi.o[1] + bi.dir[1] * j, mk = bi.o[2] + bi.dir[2] * k;
+            if (bi.shifted) {
+              // bcshiftedperiodic (src/bc_module.f90:3134-3297): on a j or k face the ghost
+              // takes the cell 16 further along i and 16 further into the block; the last
+              // 16 cells along i take their mirror cell.  i faces are left alone.
+              if (bi.face == F_IMIN || bi.face == F_IMAX) continue;
+              const bool lo = (bi.face == F_JMIN || bi.face == F_KMIN);
+              const bool shift = lo ? (i <= bi.e[0] - 16) : (i >= bi.s[0] + 16);
+              if (shift) {
+                const int di = lo ? 16 : -16;
+                mi = i + di; mj = j; mk = k;
+                if (bi.face == F_JMIN || bi.face == F_JMAX) mj = j + di;
+                else mk = k + di;
+                if (mi < -1 || mi > im + 3 || mj < -1 || mj > jm + 3 || mk < -1 || mk > km + 3) {
+                  shift_err = true;
+                  continue;
+                }
+              }
+            }
             op.src = gi(mi, mj, mk);
             op.bnd = op.src;
             for (int q = 0; q < 6; ++q) op.nb[q] = -1;
@@ -512,6 +537,7 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
           }
     };
     for (auto& bi : bcs) emit(bi, 0, 0, false);
+    if (shift_err) { E.err = "shifted periodic patch: the 16-cell source lies outside the block"; return false; }
     // ---- 12 edges (src/bc_module.f90:505-865)
     struct ED { int s[3], e[3], n1[3], n2[3], n3[3], o[3]; };
     const ED EDG[12] = {

@@ -57,6 +57,9 @@ extern "C" {
 #define CFD3D_BC_OUTFLOW_SUBSONIC   8   /* BCOutflowSubsonic: characteristic, p = pref        */
 #define CFD3D_BC_INFLOW_SUPERSONIC  9   /* BCInflowSupersonic: free-stream state imposed      */
 #define CFD3D_BC_OUTFLOW           10   /* BCOutflow (the reference's routine is a no-op)     */
+#define CFD3D_BC_WALL_COUNTERROTATING 11 /* BCWall of family CounterRotating                 */
+#define CFD3D_BC_MASSFLOWRATE_IN   13   /* BCMassflowrateIn (mass-flow rate 0, as constructed) */
+#define CFD3D_BC_SHIFTED_PERIODIC  14   /* BCShiftedPeriodic (the reference's 16-cell shift)   */
 
 /* Solver configuration: the fields of the reference's input.inp
  * (src/config_module.f90:100-119, documented in bin/input_templet.inp:34-66). */

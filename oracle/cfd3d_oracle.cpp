@@ -55,7 +55,7 @@ enum Face { F_IMIN, F_IMAX, F_JMIN, F_JMAX, F_KMIN, F_KMAX, F_KMIN_CAP, F_KMAX_C
 
 enum BcKind {
   K_WALL_INVISCID, K_WALL_VISCOUS, K_WALL_KW, K_FARFIELD, K_EXTRAP, K_SYMMETRY, K_NOOP,
-  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP,
+  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED,
   K_EDGE_WALLWALL, K_EDGE_WALLWALL_KW, K_EDGE_NOWALL, K_CORNER_WALLWALL, K_CORNER_WALLWALL_KW, K_CORNER_NOWALL
 };
 
@@ -290,7 +290,7 @@ static void wall_distance(Oracle& O) {
   for (auto& B : O.b) {
     A4& X = B.x;
     for (auto& bc : B.bcs) {
-      if (bc.type != CFD3D_BC_WALL) continue;
+      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING) continue;
       /* the patch ranges here are the grid module's (cell ranges before ghost extension) */
       int s[3], e[3];
       for (int d = 0; d < 3; ++d) { s[d] = bc.istart[d]; e[d] = bc.iend[d]; }
@@ -392,6 +392,10 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
     bi.face = (Face)(2 * axis + (mn ? 0 : 1));
     switch (p.type) {
       case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
+      /* the CounterRotating family (:3516-3810) with grid velocity 0: the SST variant differs */
+      case CFD3D_BC_WALL_COUNTERROTATING: bi.kind = (c.iturb == 0) ? K_CRWALL_KW : wall_kind(c); break;
+      case CFD3D_BC_MASSFLOWRATE_IN: bi.kind = K_MASSFLOW_IN; break;   /* bcmassflowratein :3812-4012 */
+      case CFD3D_BC_SHIFTED_PERIODIC: bi.kind = K_SHIFTED; break;      /* bcshiftedperiodic :3134-3297 */
       case CFD3D_BC_SYMMETRY: bi.kind = K_SYMMETRY; break;
       case CFD3D_BC_FARFIELD: bi.kind = K_FARFIELD; break;
       case CFD3D_BC_EXTRAPOLATE: case CFD3D_BC_DEGENERATE: bi.kind = K_EXTRAP; break;
@@ -400,6 +404,15 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
       case CFD3D_BC_OUTFLOW_SUBSONIC: bi.kind = K_OUTFLOW_SUB; break;  /* bcoutflowsubsonic :2699-2869 */
       case CFD3D_BC_INFLOW_SUPERSONIC: bi.kind = K_INFLOW_SUP; break;  /* bcinflowsupersonic :2642-2678 */
       default: err = "unknown bc type"; return false;
+    }
+    if (bi.kind == K_SHIFTED && (bi.face == F_JMIN || bi.face == F_JMAX || bi.face == F_KMIN || bi.face == F_KMAX)) {
+      /* the 16-cell sources must lie in the padded block */
+      const int ax = (bi.face == F_JMIN || bi.face == F_JMAX) ? 1 : 2;
+      const int nmx[3] = {B.imax, B.jmax, B.kmax};
+      const bool lo = (bi.face == F_JMIN || bi.face == F_KMIN);
+      const bool ok = lo ? (bi.iend[ax] + 16 <= nmx[ax] + 3 && bi.iend[0] <= B.imax + 3)
+                         : (bi.istart[ax] - 16 >= -1 && bi.istart[0] >= -1);
+      if (!ok) { err = "shifted periodic patch: the 16-cell source lies outside the block"; return false; }
     }
     bc_reference_state(c, bi);
     for (int q = 0; q < 6; ++q) for (int r = 0; r < 3; ++r) bi.nb[q][r] = 0;
@@ -424,7 +437,7 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
   };
   auto is_surf = [&](const int* pnt, int a0, int a1) {
     for (auto& bc : B.bcs) {
-      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_SYMMETRY) continue;
+      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_SYMMETRY) continue;
       if (bc.istart[a0] <= pnt[a0] && bc.iend[a0] >= pnt[a0] && bc.istart[a1] <= pnt[a1] && bc.iend[a1] >= pnt[a1])
         return true;
     }
@@ -487,7 +500,7 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
   const CD C8[8] = {mk(0, 0, 0), mk(1, 0, 0), mk(0, 1, 0), mk(1, 1, 0), mk(0, 0, 1), mk(1, 0, 1), mk(0, 1, 1), mk(1, 1, 1)};
   auto is_surf3 = [&](const int* pnt) {
     for (auto& bc : B.bcs) {
-      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_SYMMETRY) continue;
+      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_SYMMETRY) continue;
       bool in = true;
       for (int q = 0; q < 3; ++q) in = in && bc.istart[q] <= pnt[q] && bc.iend[q] >= pnt[q];
       if (in) return true;
@@ -719,6 +732,40 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
         int mi = bi.origin[0] + bi.dir[0] * i, mj = bi.origin[1] + bi.dir[1] * j, mk = bi.origin[2] + bi.dir[2] * k;
         switch (bi.kind) {
           case K_NOOP: break;
+          case K_CRWALL_KW:
+            /* omega: the mirror's (the routine computes the wall value and discards it) */
+            get_cell(c, B, mi, mj, mk, pv, dv, tv);
+            pv[1] = -pv[1]; pv[2] = -pv[2]; pv[3] = -pv[3]; pv[7] = -pv[7];
+            tv[2] = -tv[2];
+            put_cell(c, B, i, j, k, pv, dv, tv);
+            break;
+          case K_MASSFLOW_IN: {
+            /* massflowrate = 0 (construct): v = 0, the velocity reflects; p stays the mirror's */
+            get_cell(c, B, mi, mj, mk, pv, dv, tv);
+            for (int q = 0; q < 3; ++q) pv[1 + q] = -pv[1 + q];
+            for (int m = 4; m < c.npv; ++m) pv[m] = 2.0 * bi.pv[m] - pv[m];
+            pv[5] = dmin(dmax(pv[5], 0.0), 1.0);
+            pv[6] = dmin(dmax(pv[6], 0.0), 1.0);
+            deteos(c.eos, c.with_prop, pv[0] + bi.pv[0], pv[4], pv[5], pv[6], dv, tv);
+            put_cell(c, B, i, j, k, pv, dv, tv);
+            break;
+          }
+          case K_SHIFTED: {
+            /* j / k faces: from (i +- 16, j +- 16, k) or (i +- 16, j, k +- 16); the last 16
+               cells along i from the mirror; i faces untouched */
+            if (bi.face == F_IMIN || bi.face == F_IMAX) break;
+            const bool lo = (bi.face == F_JMIN || bi.face == F_KMIN);
+            int si = mi, sj = mj, sk = mk;
+            if (lo ? (i <= bi.iend[0] - 16) : (i >= bi.istart[0] + 16)) {
+              const int di = lo ? 16 : -16;
+              si = i + di; sj = j; sk = k;
+              if (bi.face == F_JMIN || bi.face == F_JMAX) sj = j + di;
+              else sk = k + di;
+            }
+            get_cell(c, B, si, sj, sk, pv, dv, tv);
+            put_cell(c, B, i, j, k, pv, dv, tv);
+            break;
+          }
           case K_EXTRAP:
             get_cell(c, B, mi, mj, mk, pv, dv, tv);
             put_cell(c, B, i, j, k, pv, dv, tv);

@@ -64,10 +64,21 @@ def _with_inout(c):
     return c
 
 
-def _prepared(scale, inout=False):
+def _with_massflow_crwall(c):
+    """bcmassflowratein at imin and the counter-rotating SST wall at jmin"""
+    for b in c["blocks"]:
+        im, jm, km = b["imax"], b["jmax"], b["kmax"]
+        repl = {(1, 1, 1, 1, jm, km): abi.BC_MASSFLOWRATE_IN, (1, 1, 1, im, 1, km): abi.BC_WALL_COUNTERROTATING}
+        b["bc"] = [(repl.get(tuple(p), k), p) for k, p in b["bc"]]
+    return c
+
+
+def _prepared(scale, inout=False, massflow=False):
     c = _state(scale)
     if inout:
         c = _with_inout(c)
+    if massflow:
+        c = _with_massflow_crwall(c)
     e = _engine(c)
     e.initialize(c["pv0"])
     s = adjoint.StateSetter(e)
@@ -93,6 +104,11 @@ def c4_small():
 @pytest.fixture(scope="module")
 def c4_inout():
     return _prepared(4, inout=True)
+
+
+@pytest.fixture(scope="module")
+def c4_massflow():
+    return _prepared(4, massflow=True)
 
 
 def _typical(pv, v):
@@ -237,5 +253,18 @@ def test_vjp_through_subsonic_inflow_and_outflow(c4_inout):
                for q, (k, j, _, v) in enumerate(_entries(d["pv"].shape[:-1], d["pv"].shape[-1], 18, 3))]
     used, errs, rows = _check(lambda p: s.residual([p])[0], d, entries)
     print(f"in/outflow rows: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
+    assert used >= len(entries) - 2, rows
+    assert errs.max() <= TOL, (errs, rows)
+
+
+def test_vjp_through_massflow_inlet_and_counterrotating_wall(c4_massflow):
+    """rows next to bcmassflowratein (i = 0) and the counter-rotating SST wall (j = 0)"""
+    d = c4_massflow
+    s = d["s"]
+    km, jm, im = d["pv"].shape[:-1]
+    base = _entries(d["pv"].shape[:-1], d["pv"].shape[-1], 18, 4)
+    entries = [(k, j, 0, v) if q % 2 == 0 else (k, 0, i, v) for q, (k, j, i, v) in enumerate(base)]
+    used, errs, rows = _check(lambda p: s.residual([p])[0], d, entries)
+    print(f"mass-flow / counter-rotating rows: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
     assert used >= len(entries) - 2, rows
     assert errs.max() <= TOL, (errs, rows)

@@ -22,22 +22,33 @@ BCSETS = {
     "subsonic": {"imin": abi.BC_INFLOW_SUBSONIC, "imax": abi.BC_OUTFLOW_SUBSONIC},
     "supersonic_in": {"imin": abi.BC_INFLOW_SUPERSONIC, "imax": abi.BC_EXTRAPOLATE},
     "out_only": {"imin": abi.BC_FARFIELD, "imax": abi.BC_OUTFLOW_SUBSONIC},
+    # bcmassflowratein at the inlet; counter-rotating walls (the SST case's wall, and the
+    # others' j faces); bcshiftedperiodic on the k faces (their 16-cell shift needs 17 cells)
+    "massflow_crwall": {"imin": abi.BC_MASSFLOWRATE_IN, "jmin": abi.BC_WALL_COUNTERROTATING},
 }
+SHIFTED = {"kmin": abi.BC_SHIFTED_PERIODIC, "kmax": abi.BC_SHIFTED_PERIODIC}
+
+
+def replace_faces(c, kinds):
+    """the case with the BC of the named faces of every block replaced"""
+    for b in c["blocks"]:
+        im, jm, km = b["imax"], b["jmax"], b["kmax"]
+        faces = {"imin": (1, 1, 1, 1, jm, km), "imax": (im, 1, 1, im, jm, km),
+                 "jmin": (1, 1, 1, im, 1, km), "jmax": (1, jm, 1, im, jm, km),
+                 "kmin": (1, 1, 1, im, jm, 1), "kmax": (1, 1, km, im, jm, km)}
+        bc = []
+        for kind, pnts in b["bc"]:
+            face = next((f for f, p in faces.items() if tuple(p) == tuple(pnts)), None)
+            bc.append((kinds[face], pnts) if face in kinds else (kind, pnts))
+        b["bc"] = bc
+    return c
 
 
 def make(base, bcset):
     name, kw, over = BASES[base]
     c = cases.make(name, **kw)
     c["cfg"].update(over)
-    for b in c["blocks"]:
-        im, jm, km = b["imax"], b["jmax"], b["kmax"]
-        faces = {"imin": (1, 1, 1, 1, jm, km), "imax": (im, 1, 1, im, jm, km)}
-        bc = []
-        for kind, pnts in b["bc"]:
-            face = next((f for f, p in faces.items() if tuple(p) == tuple(pnts)), None)
-            bc.append((BCSETS[bcset][face], pnts) if face in BCSETS[bcset] else (kind, pnts))
-        b["bc"] = bc
-    return c
+    return replace_faces(c, BCSETS[bcset])
 
 
 @pytest.mark.parametrize("bcset", list(BCSETS))
@@ -71,3 +82,30 @@ def test_mixed_residual(oracle, bcset):
     e.initialize(c["pv0"])
     o.initialize(c["pv0"])
     assert field_err(e.residual(0)["res"], o.residual(0)["res"]).max() < TOL_MIXED
+
+
+@pytest.mark.parametrize("base", ["plain", "sst"])
+def test_shifted_periodic_matches(oracle, base):
+    name, kw, over = BASES[base]
+    c = cases.make(name, scale=kw["scale"] // 2, **{k: v for k, v in kw.items() if k != "scale"})
+    c["cfg"].update(over)
+    c = replace_faces(c, SHIFTED)
+    e = native.Engine(c)
+    o = oracle.Oracle(c)
+    e.initialize(c["pv0"])
+    o.initialize(c["pv0"])
+    assert field_err(e.residual(0)["res"], o.residual(0)["res"]).max() < TOL_RES
+    for it in range(2):
+        e.iterate(1, it + 1, 0.0)
+        o.iterate(1, it + 1, 0.0)
+    sg, so = e.download(0), o.get_state(0)
+    assert field_err(interior(sg["pv"]), interior(so["pv"])).max() < TOL_STATE
+    assert field_err(sg["pv"][:3, 3:-3, 3:-3], so["pv"][:3, 3:-3, 3:-3]).max() < TOL_STATE
+    assert field_err(sg["pv"][-3:, 3:-3, 3:-3], so["pv"][-3:, 3:-3, 3:-3]).max() < TOL_STATE
+
+
+def test_shifted_periodic_rejects_a_short_block():
+    c = replace_faces(cases.make("plain_small", scale=8), SHIFTED)   # 8 x 4 x 4 cells
+    with pytest.raises(native.Cfd3dError) as ei:
+        native.Engine(c)
+    assert ei.value.code == abi.ERR_DESCRIPTOR
