@@ -212,8 +212,8 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
           for (int v = 1; v < 4; ++v) xp[v] = -sp[v];
           for (int v = 4; v < npv; ++v) xp[v] = 2.0 * bpv[v] - sp[v];
           const bool c5 = xp[5] > 0.0 && xp[5] < 1.0, c6 = xp[6] > 0.0 && xp[6] < 1.0;
-          xp[5] = fmin(fmax(xp[5], 0.0), 1.0);
-          xp[6] = fmin(fmax(xp[6], 0.0), 1.0);
+          xp[5] = ::fmin(::fmax(xp[5], 0.0), 1.0);
+          xp[6] = ::fmin(::fmax(xp[6], 0.0), 1.0);
           double ge[4];
           eos_chain(c, xp[0] + bpv[0], xp[4], xp[5], xp[6], gd, ge);
           gp[0] += ge[0]; gp[4] += ge[1]; gp[5] += ge[2]; gp[6] += ge[3];
