@@ -104,8 +104,17 @@ def test_shifted_periodic_matches(oracle, base):
     assert field_err(sg["pv"][-3:, 3:-3, 3:-3], so["pv"][-3:, 3:-3, 3:-3]).max() < TOL_STATE
 
 
-def test_shifted_periodic_rejects_a_short_block():
-    c = replace_faces(cases.make("plain_small", scale=8), SHIFTED)   # 8 x 4 x 4 cells
+def test_shifted_periodic_rejects_a_source_outside_the_block():
+    """24 cells along i (so the shift applies) but 8 along k: the source k + 16 of a kmin
+    ghost lies beyond the padded block"""
+    c = cases.make("plain_small", scale=4)
+    xyz = cases.box_nodes(24, 8, 8, 2.0, 1.0, 1.0, shear=0.02, seed=0)
+    c["blocks"] = [dict(imax=25, jmax=9, kmax=9, xyz=xyz, con=[],
+                        bc=cases.face_patches(25, 9, 9, {"imin": abi.BC_FARFIELD, "imax": abi.BC_FARFIELD,
+                                                         "jmin": abi.BC_SYMMETRY, "jmax": abi.BC_SYMMETRY,
+                                                         "kmin": abi.BC_SHIFTED_PERIODIC,
+                                                         "kmax": abi.BC_SHIFTED_PERIODIC}))]
     with pytest.raises(native.Cfd3dError) as ei:
         native.Engine(c)
     assert ei.value.code == abi.ERR_DESCRIPTOR
+    assert "shifted periodic" in str(ei.value)
