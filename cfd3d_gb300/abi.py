@@ -16,7 +16,7 @@ FP64, MIXED = 0, 1
 
 BC_WALL, BC_SYMMETRY, BC_FARFIELD, BC_EXTRAPOLATE, BC_DEGENERATE, BC_INFLOW = range(1, 7)
 BC_INFLOW_SUBSONIC, BC_OUTFLOW_SUBSONIC, BC_INFLOW_SUPERSONIC, BC_OUTFLOW = range(7, 11)
-BC_WALL_COUNTERROTATING, BC_MASSFLOWRATE_IN, BC_SHIFTED_PERIODIC = 11, 13, 14
+BC_WALL_COUNTERROTATING, BC_WALL_HEATFLUX, BC_MASSFLOWRATE_IN, BC_SHIFTED_PERIODIC = 11, 12, 13, 14
 BC_NAMES = {
     "BCWall": BC_WALL,
     "BCSymmetryPlane": BC_SYMMETRY,
@@ -55,7 +55,8 @@ class Config(C.Structure):
 
 
 class BcPatch(C.Structure):
-    _fields_ = [("type", C.c_int), ("pnts", C.c_int * 6)]
+    _fields_ = [("type", C.c_int), ("pnts", C.c_int * 6), ("ndata", C.c_int),
+                ("tdata", C.POINTER(C.c_double)), ("heatflux", C.POINTER(C.c_double))]
 
 
 class Connection(C.Structure):
@@ -93,10 +94,20 @@ class BlockSet:
             xyz = np.ascontiguousarray(b["xyz"], dtype=np.float64)
             assert xyz.shape == (b["kmax"], b["jmax"], b["imax"], 3)
             bcs = (BcPatch * max(1, len(b["bc"])))()
+            # heat-flux histories: {patch index: (times, fluxes)}
+            tables = b.get("heatflux", {})
             for q, (t, p) in enumerate(b["bc"]):
                 bcs[q].type = t
                 for r in range(6):
                     bcs[q].pnts[r] = p[r]
+                if q in tables:
+                    td = np.ascontiguousarray(tables[q][0], dtype=np.float64)
+                    hf = np.ascontiguousarray(tables[q][1], dtype=np.float64)
+                    assert td.shape == hf.shape and td.ndim == 1
+                    self._keep += [td, hf]
+                    bcs[q].ndata = td.size
+                    bcs[q].tdata = td.ctypes.data_as(C.POINTER(C.c_double))
+                    bcs[q].heatflux = hf.ctypes.data_as(C.POINTER(C.c_double))
             cons = (Connection * max(1, len(b.get("con", []))))()
             for q, cc in enumerate(b.get("con", [])):
                 cons[q].donor = cc["donor"]

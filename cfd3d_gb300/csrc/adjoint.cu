@@ -195,6 +195,25 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
           push_cell(a, c, n, src, gp, gd);
           break;
         }
+        case G_HFWALL_KW: {
+          // T_g = 2 ((q y_b + mu_b |u_b|^2 / 2) / k_b + T_b) - T_src,
+          // omega_g = 1600 mu_b / (rho_b y_b^2) - omega_src; u, v, w, k, mu_t reflected
+          const long long b = op.bnd;
+          const double hf = heatflux_at(d.hft + op.pad, bc_time(d, c));
+          const double yb = d.gm[(GM_GRD + 4) * n + b], mub = d.tv[b], kb = d.tv[n + b], rb = d.dv[b];
+          const double ub[3] = {d.pv[n + b], d.pv[2 * n + b], d.pv[3 * n + b]};
+          const double u2 = ub[0] * ub[0] + ub[1] * ub[1] + ub[2] * ub[2];
+          const double gt = gp[4], go = gp[8];
+          aadd(&a.gpv[4 * n + b], 2.0 * gt);
+          for (int e = 0; e < 3; ++e) aadd(&a.gpv[(1 + e) * n + b], gt * 2.0 * mub * ub[e] / kb);
+          aadd(&a.gdt[GD_VIS * n + b], gt * u2 / kb + go * 1600.0 / (rb * yb * yb));
+          aadd(&a.gdt[GD_CON * n + b], -gt * 2.0 * (hf * yb + 0.5 * mub * u2) / (kb * kb));
+          aadd(&a.gdt[GD_RHO * n + b], -go * 1600.0 * mub / (rb * rb * yb * yb));
+          gp[1] = -gp[1]; gp[2] = -gp[2]; gp[3] = -gp[3]; gp[4] = -gp[4]; gp[7] = -gp[7]; gp[8] = -gp[8];
+          gd[GD_MUT] = -gd[GD_MUT];
+          push_cell(a, c, n, src, gp, gd);
+          break;
+        }
         case G_CRWALL_KW:
           // u, v, w, k and mu_t reflected, omega and the rest the source cell's
           gp[1] = -gp[1]; gp[2] = -gp[2]; gp[3] = -gp[3]; gp[7] = -gp[7];

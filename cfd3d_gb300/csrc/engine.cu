@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstddef>
 #include <cstring>
 #include <fcntl.h>
 #include <mutex>
@@ -268,6 +269,23 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       x.tv[2] = -x.tv[2];
       store_cell(d, c, op.dst, x);
       return;
+    case G_HFWALL_KW: {
+      // bcheatfluxwallviscouskw (src/bc_module.f90:4184-4273): u, v, w, k reflected, the
+      // wall temperature from the heat flux through the boundary cell, the SST omega wall
+      // value.  The routine's EOS call takes the mirror's state, so the ghost keeps the
+      // mirror's dv and tv(1:2); tv(3) reflects.
+      load_cell(d, c, op.src, x);
+      const long long b = op.bnd;
+      const double hf = heatflux_at(d.hft + op.pad, bc_time(d, c));
+      const double yb = d.gm[(GM_GRD + 4) * n + b], mub = d.tv[b], kb = d.tv[n + b];
+      const double ub = d.pv[n + b], vb = d.pv[2 * n + b], wb = d.pv[3 * n + b];
+      x.pv[1] = -x.pv[1]; x.pv[2] = -x.pv[2]; x.pv[3] = -x.pv[3]; x.pv[7] = -x.pv[7];
+      x.pv[4] = 2.0 * ((hf * yb + 0.5 * mub * (ub * ub + vb * vb + wb * wb)) / kb + d.pv[4 * n + b]) - x.pv[4];
+      x.pv[8] = 1600.0 * mub / d.dv[b] / (yb * yb) - x.pv[8];
+      x.tv[2] = -x.tv[2];
+      store_cell(d, c, op.dst, x);
+      return;
+    }
     case G_MASSFLOW_IN: {
       // bcmassflowratein (:3812-4012) with the rate 0 its construct sets: the inflow speed
       // m / (rho A) is 0, so the velocity reflects; T, y1, y2, k, omega from the free stream;
@@ -1559,6 +1577,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_pos);
   cudaFree(E.d_nbf);
   cudaFree(E.d_nbb);
+  cudaFree(E.d_hft);
   cudaFree(E.d.rec);
   cudaFree(E.d.done);
   cudaFree(E.d.tickets);
@@ -1883,12 +1902,22 @@ static int finish_iteration(cfd3d_handle* h, int nt_phy, double timeprev, double
   return CFD3D_OK;
 }
 
+// the time inputs of the boundary program (heat-flux histories) for the next launches
+static int set_bc_time(Engine& E, int nt_phy, double timeprev) {
+  if (!E.d_hft) return CFD3D_OK;
+  struct { double tp; int nt, pad; } v{timeprev, nt_phy, 0};
+  static_assert(sizeof(v) == 16, "timeprev, nt_phy, pad_ of Scalars");
+  CFD_CUDA(cudaMemcpyAsync((char*)E.d.sc + offsetof(Scalars, timeprev), &v, sizeof(v), cudaMemcpyHostToDevice, E.st));
+  return CFD3D_OK;
+}
+
 int cfd3d_iterate(cfd3d_handle* h, int nt_phy, int nt, double timeprev, double* time_out, double* res_l2, int* loc) {
   if (!h) return CFD3D_ERR_ARG;
   Engine& E = h->E;
   (void)nt;
   int rc = build_graph(E);
   if (rc) return rc;
+  if ((rc = set_bc_time(E, nt_phy, timeprev))) return rc;
   CFD_CUDA(cudaGraphLaunch(E.graph, E.st));
   return finish_iteration(h, nt_phy, timeprev, time_out, res_l2, loc);
 }
@@ -1899,6 +1928,7 @@ int cfd3d_iterate_n(cfd3d_handle* h, int niter, int nt_phy, int nt0, double time
   (void)nt0;
   int rc = build_graph(E);
   if (rc) return rc;
+  if ((rc = set_bc_time(E, nt_phy, timeprev))) return rc;
   for (int q = 0; q < niter; ++q) CFD_CUDA(cudaGraphLaunch(E.graph, E.st));
   return finish_iteration(h, nt_phy, timeprev, time_out, res_l2, nullptr);
 }

@@ -33,7 +33,7 @@ enum GhostKind : int {
   G_COPY = 0, G_EXTRAP, G_WALL_VISCOUS, G_WALL_KW, G_SYMMETRY, G_FARFIELD,
   G_WALLWALL, G_WALLWALL_KW4, G_WALLWALL_KW8, G_NOWALL3, G_NOWALL7,
   G_INFLOW_SUB, G_OUTFLOW_SUB, G_INFLOW_SUP,  // the farfield treatment with a forced branch
-  G_CRWALL_KW, G_MASSFLOW_IN
+  G_CRWALL_KW, G_MASSFLOW_IN, G_HFWALL_KW
 };
 
 // the farfield_pv branch of a characteristic ghost kind
@@ -64,6 +64,11 @@ struct Scalars {
   unsigned long long snd2_fallbacks;
   int nonfinite;
   int sweep_stall;   // a dataflow sweep's wait for a neighbour ran out (the sweep went on)
+  // the time the boundary program sees (heat-flux histories): timeprev and nt_phy of the
+  // current cfd3d_iterate call, written by the host before each launch
+  double timeprev;
+  int nt_phy;
+  int pad_;
 };
 
 struct DevPtr {
@@ -73,6 +78,7 @@ struct DevPtr {
   long long ncell;
   long long nint;
   Scalars* sc;
+  const double* hft;   // heat-flux histories: per table n, t[n], q[n] (GhostOp.pad is its offset)
   double* partial;   // per-CTA partial residual sums [gridsize][npv+2]
   // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
   float *pvf, *fi32, *fv32;
@@ -118,6 +124,7 @@ struct Engine {
   // ghost program: phase 0 faces + halos, 1 edges, 2 corners
   GhostOp* d_ops[3] = {nullptr, nullptr, nullptr};
   int nops[3] = {0, 0, 0};
+  double* d_hft = nullptr;   // heat-flux histories (d.hft), null without heat-flux walls
   // LU-SGS plane-major numbering (setup_planes): cells[t], pos[g], lower / upper neighbours
   int* d_planes = nullptr;
   int* d_pos = nullptr;
@@ -156,6 +163,33 @@ __device__ __forceinline__ int find_block_cell(const BlockGeom* B, int nb, long 
   while (b + 1 < nb && g >= B[b + 1].off) ++b;
   return b;
 }
+// The heat flux of a history at time tm (bcheatfluxwall*, src/bc_module.f90:4026-4033):
+// linear between the bracketing entries, the last value from the last time on.  Before the
+// first time the reference leaves it undefined; the first value is taken there.
+__device__ __forceinline__ double heatflux_at(const double* tab, double tm) {
+  const int nd = (int)tab[0];
+  const double* t = tab + 1;
+  const double* q = tab + 1 + nd;
+  double hf = q[0];
+  for (int i = 0; i < nd - 1; ++i)
+    if (tm >= t[i] && tm < t[i + 1]) {
+      hf = q[i] + (q[i + 1] - q[i]) * (tm - t[i]) / (t[i + 1] - t[i]);
+      break;
+    }
+  if (tm >= t[nd - 1]) hf = q[nd - 1];
+  return hf;
+}
+
+// the time bc%setbc receives (bcinfo%time): dt_phy nt_phy when unsteady, else the
+// accumulated pseudo time including this iteration's minimum step (no step taken yet in a
+// residual-only evaluation), plus timeprev
+__device__ __forceinline__ double bc_time(const DevPtr& d, const Par& c) {
+  if (c.nsteady >= 1) return c.dt_phy * (double)d.sc->nt_phy;
+  const unsigned long long bits = d.sc->dtmin_bits;
+  const double dtm = (bits == (unsigned long long)__double_as_longlong(1.0e10)) ? 0.0 : __longlong_as_double((long long)bits);
+  return d.sc->time_acc + dtm + d.sc->timeprev;
+}
+
 __device__ __forceinline__ long long interior_cell(const BlockGeom& B, long long loc, int& i, int& j, int& k) {
   int ni = B.imax - 1, nj = B.jmax - 1;
   i = (int)(loc % ni) + 2;

@@ -322,7 +322,8 @@ bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
       const cfd3d_block_desc& d = blocks[b];
       HBlock& B = H[b];
       for (int n = 0; n < d.nbc; ++n) {
-        if (d.bc[n].type != CFD3D_BC_WALL && d.bc[n].type != CFD3D_BC_WALL_COUNTERROTATING) continue;
+        const int ty = d.bc[n].type;
+        if (ty != CFD3D_BC_WALL && ty != CFD3D_BC_WALL_COUNTERROTATING && ty != CFD3D_BC_WALL_HEATFLUX) continue;
         const int* p = d.bc[n].pnts;
         int ax = -1;
         for (int a = 0; a < 3; ++a) if (p[a] == p[3 + a]) ax = a;
@@ -414,6 +415,7 @@ struct Bc {
   int nb[6][3];
   bool farfield_sign = false;
   bool shifted = false;   // bcshiftedperiodic: copies from 16 cells along i and the face normal
+  int hf_off = 0;         // heat-flux wall: offset of its history in the table
 };
 
 int wall_kind(const Par& c) {
@@ -427,6 +429,7 @@ int wall_kind(const Par& c) {
 bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
   const Par& c = E.par;
   std::vector<GhostOp> ops[3];
+  std::vector<double> hft;   // heat-flux histories
   for (int b = 0; b < nblocks; ++b) {
     const cfd3d_block_desc& d = blocks[b];
     const BlockGeom& G = E.blk[b];
@@ -457,6 +460,22 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
         // the counter-rotating family without rotation: the laminar and inviscid variants
         // are the plain wall's and symmetry's formulas, the SST one differs
         case CFD3D_BC_WALL_COUNTERROTATING: bi.kind = (c.iturb == 0) ? G_CRWALL_KW : wall_kind(c); break;
+        case CFD3D_BC_WALL_HEATFLUX: {
+          // the HeatFlux family (src/bc_module.f90:233-249): the SST variant.  The laminar
+          // one reads the wall distance grd(5), which a laminar run does not have (its grd
+          // holds 4 values), and an Euler run has no routine for the family at all.
+          if (c.iturb != 0) { E.err = "heat-flux walls need the SST model (iturb = 0)"; return false; }
+          const cfd3d_bc_patch& bp = d.bc[n];
+          if (bp.ndata < 1 || !bp.tdata || !bp.heatflux) { E.err = "heat-flux wall without its history"; return false; }
+          for (int m = 1; m < bp.ndata; ++m)
+            if (!(bp.tdata[m] > bp.tdata[m - 1])) { E.err = "heat-flux history times must increase"; return false; }
+          bi.kind = G_HFWALL_KW;
+          bi.hf_off = (int)hft.size();
+          hft.push_back((double)bp.ndata);
+          for (int m = 0; m < bp.ndata; ++m) hft.push_back(bp.tdata[m]);
+          for (int m = 0; m < bp.ndata; ++m) hft.push_back(bp.heatflux[m]);
+          break;
+        }
         case CFD3D_BC_MASSFLOWRATE_IN: bi.kind = G_MASSFLOW_IN; break;
         case CFD3D_BC_SHIFTED_PERIODIC: bi.kind = G_COPY; bi.shifted = true; break;
         case CFD3D_BC_SYMMETRY: bi.kind = G_SYMMETRY; break;
@@ -473,7 +492,8 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
     }
     auto is_surf = [&](const int* pnt, std::initializer_list<int> axes) {
       for (auto& bc : bcs) {
-        if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_SYMMETRY) continue;
+        if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_WALL_HEATFLUX &&
+            bc.type != CFD3D_BC_SYMMETRY) continue;
         bool in = true;
         for (int a : axes) in = in && bc.s[a] <= pnt[a] && bc.e[a] >= pnt[a];
         if (in) return true;
@@ -513,7 +533,9 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
             op.bnd = op.src;
             for (int q = 0; q < 6; ++q) op.nb[q] = -1;
             op.fidx = op.src; op.fplane = GM_CX; op.fsign = 1.0f;
-            if (bi.kind == G_SYMMETRY || bi.kind == G_FARFIELD || bi.kind == G_WALL_KW || ghost_ff_mode(bi.kind)) {
+            op.pad = bi.hf_off;
+            if (bi.kind == G_SYMMETRY || bi.kind == G_FARFIELD || bi.kind == G_WALL_KW || bi.kind == G_HFWALL_KW ||
+                ghost_ff_mode(bi.kind)) {
               int ii = mi, jj = mj, kk = mk;
               float s = bi.farfield_sign ? -1.0f : 1.0f;
               switch (bi.face) {
@@ -676,6 +698,11 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
     if (E.nops[p] == 0) continue;
     if (cudaMalloc(&E.d_ops[p], ops[p].size() * sizeof(GhostOp)) != cudaSuccess) { E.err = "cudaMalloc ghost ops"; return false; }
     cudaMemcpy(E.d_ops[p], ops[p].data(), ops[p].size() * sizeof(GhostOp), cudaMemcpyHostToDevice);
+  }
+  if (!hft.empty()) {
+    if (cudaMalloc(&E.d_hft, hft.size() * sizeof(double)) != cudaSuccess) { E.err = "cudaMalloc heat-flux tables"; return false; }
+    cudaMemcpy(E.d_hft, hft.data(), hft.size() * sizeof(double), cudaMemcpyHostToDevice);
+    E.d.hft = E.d_hft;
   }
   return true;
 }

@@ -58,6 +58,7 @@ extern "C" {
 #define CFD3D_BC_INFLOW_SUPERSONIC  9   /* BCInflowSupersonic: free-stream state imposed      */
 #define CFD3D_BC_OUTFLOW           10   /* BCOutflow (the reference's routine is a no-op)     */
 #define CFD3D_BC_WALL_COUNTERROTATING 11 /* BCWall of family CounterRotating                 */
+#define CFD3D_BC_WALL_HEATFLUX     12   /* BCWall of family HeatFlux*: q(t) from the patch's table */
 #define CFD3D_BC_MASSFLOWRATE_IN   13   /* BCMassflowrateIn (mass-flow rate 0, as constructed) */
 #define CFD3D_BC_SHIFTED_PERIODIC  14   /* BCShiftedPeriodic (the reference's 16-cell shift)   */
 
@@ -84,10 +85,15 @@ typedef struct cfd3d_config {
 } cfd3d_config;
 
 /* A boundary patch: CGNS PointRange in 1-based NODE indices
- * (imin, jmin, kmin, imax, jmax, kmax), one index pair collapsed to a face. */
+ * (imin, jmin, kmin, imax, jmax, kmax), one index pair collapsed to a face.
+ * CFD3D_BC_WALL_HEATFLUX also carries the heat-flux history that the reference reads from
+ * <family>.dat (src/bc_module.f90:233-249): ndata pairs (tdata[m], heatflux[m]), tdata
+ * ascending; the other types leave ndata = 0 and the pointers NULL. */
 typedef struct cfd3d_bc_patch {
   int type;
   int pnts[6];
+  int ndata;
+  const double *tdata, *heatflux;
 } cfd3d_bc_patch;
 
 /* A point-matched 1-to-1 interface, as cg_1to1_read_f returns it: own range,

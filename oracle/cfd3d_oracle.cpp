@@ -55,7 +55,7 @@ enum Face { F_IMIN, F_IMAX, F_JMIN, F_JMAX, F_KMIN, F_KMAX, F_KMIN_CAP, F_KMAX_C
 
 enum BcKind {
   K_WALL_INVISCID, K_WALL_VISCOUS, K_WALL_KW, K_FARFIELD, K_EXTRAP, K_SYMMETRY, K_NOOP,
-  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED,
+  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED, K_HFWALL_KW,
   K_EDGE_WALLWALL, K_EDGE_WALLWALL_KW, K_EDGE_NOWALL, K_CORNER_WALLWALL, K_CORNER_WALLWALL_KW, K_CORNER_NOWALL
 };
 
@@ -67,6 +67,8 @@ struct BcInfo {
   int nb[6][3];
   double pressure = 0;
   double pv[NPV_MAX], dv[NDV], tv[3];
+  std::vector<double> tdata, heatflux;   /* HeatFlux walls: the <family>.dat history */
+  double time = 0.0;                     /* bcinfo%time, set by setbc */
 };
 
 struct Conn {
@@ -290,7 +292,7 @@ static void wall_distance(Oracle& O) {
   for (auto& B : O.b) {
     A4& X = B.x;
     for (auto& bc : B.bcs) {
-      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING) continue;
+      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_WALL_HEATFLUX) continue;
       /* the patch ranges here are the grid module's (cell ranges before ghost extension) */
       int s[3], e[3];
       for (int d = 0; d < 3; ++d) { s[d] = bc.istart[d]; e[d] = bc.iend[d]; }
@@ -394,6 +396,13 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
       case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
       /* the CounterRotating family (:3516-3810) with grid velocity 0: the SST variant differs */
       case CFD3D_BC_WALL_COUNTERROTATING: bi.kind = (c.iturb == 0) ? K_CRWALL_KW : wall_kind(c); break;
+      case CFD3D_BC_WALL_HEATFLUX:   /* the HeatFlux family: bcheatfluxwallviscouskw :4184-4273 */
+        if (c.iturb != 0) { err = "heat-flux walls need the SST model (iturb = 0)"; return false; }
+        if (p.ndata < 1 || !p.tdata || !p.heatflux) { err = "heat-flux wall without its history"; return false; }
+        bi.kind = K_HFWALL_KW;
+        bi.tdata.assign(p.tdata, p.tdata + p.ndata);
+        bi.heatflux.assign(p.heatflux, p.heatflux + p.ndata);
+        break;
       case CFD3D_BC_MASSFLOWRATE_IN: bi.kind = K_MASSFLOW_IN; break;   /* bcmassflowratein :3812-4012 */
       case CFD3D_BC_SHIFTED_PERIODIC: bi.kind = K_SHIFTED; break;      /* bcshiftedperiodic :3134-3297 */
       case CFD3D_BC_SYMMETRY: bi.kind = K_SYMMETRY; break;
@@ -437,7 +446,8 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
   };
   auto is_surf = [&](const int* pnt, int a0, int a1) {
     for (auto& bc : B.bcs) {
-      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_SYMMETRY) continue;
+      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_WALL_HEATFLUX &&
+          bc.type != CFD3D_BC_SYMMETRY) continue;
       if (bc.istart[a0] <= pnt[a0] && bc.iend[a0] >= pnt[a0] && bc.istart[a1] <= pnt[a1] && bc.iend[a1] >= pnt[a1])
         return true;
     }
@@ -500,7 +510,8 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
   const CD C8[8] = {mk(0, 0, 0), mk(1, 0, 0), mk(0, 1, 0), mk(1, 1, 0), mk(0, 0, 1), mk(1, 0, 1), mk(0, 1, 1), mk(1, 1, 1)};
   auto is_surf3 = [&](const int* pnt) {
     for (auto& bc : B.bcs) {
-      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_SYMMETRY) continue;
+      if (bc.type != CFD3D_BC_WALL && bc.type != CFD3D_BC_WALL_COUNTERROTATING && bc.type != CFD3D_BC_WALL_HEATFLUX &&
+          bc.type != CFD3D_BC_SYMMETRY) continue;
       bool in = true;
       for (int q = 0; q < 3; ++q) in = in && bc.istart[q] <= pnt[q] && bc.iend[q] >= pnt[q];
       if (in) return true;
@@ -732,6 +743,31 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
         int mi = bi.origin[0] + bi.dir[0] * i, mj = bi.origin[1] + bi.dir[1] * j, mk = bi.origin[2] + bi.dir[2] * k;
         switch (bi.kind) {
           case K_NOOP: break;
+          case K_HFWALL_KW: {
+            /* heat flux of the history at bcinfo%time (:4196-4203; the first value before
+               the first time, where the routine leaves it undefined) */
+            const int nd = (int)bi.tdata.size();
+            double hf = bi.heatflux[0];
+            for (int m = 0; m < nd - 1; ++m)
+              if (bi.time >= bi.tdata[m] && bi.time < bi.tdata[m + 1]) {
+                hf = bi.heatflux[m] + (bi.heatflux[m + 1] - bi.heatflux[m]) * (bi.time - bi.tdata[m]) / (bi.tdata[m + 1] - bi.tdata[m]);
+                break;
+              }
+            if (bi.time >= bi.tdata[nd - 1]) hf = bi.heatflux[nd - 1];
+            get_cell(c, B, mi, mj, mk, pv, dv, tv);
+            int ii = mi, jj = mj, kk = mk;
+            face_cell(bi, B, i, j, k, ii, jj, kk, nx, false);
+            const double* Pb = B.pv.at(ii, jj, kk);
+            const double yb = B.grd(4, ii, jj, kk), mub = B.tv(0, ii, jj, kk), kb = B.tv(1, ii, jj, kk);
+            const double rb = B.dv(0, ii, jj, kk);
+            /* the routine's EOS call takes the mirror's state: the ghost keeps its dv, tv(1:2) */
+            pv[1] = -pv[1]; pv[2] = -pv[2]; pv[3] = -pv[3]; pv[7] = -pv[7];
+            pv[4] = 2.0 * ((hf * yb + 0.5 * mub * (sq(Pb[1]) + sq(Pb[2]) + sq(Pb[3]))) / kb + Pb[4]) - pv[4];
+            pv[8] = 1600.0 * mub / rb / sq(yb) - pv[8];
+            tv[2] = -tv[2];
+            put_cell(c, B, i, j, k, pv, dv, tv);
+            break;
+          }
           case K_CRWALL_KW:
             /* omega: the mirror's (the routine computes the wall value and discards it) */
             get_cell(c, B, mi, mj, mk, pv, dv, tv);
@@ -928,7 +964,7 @@ static void apply_halos(Oracle& O) {
 }
 
 static void setbc(Oracle& O) {
-  for (auto& B : O.b) for (auto& bc : B.bcs) apply_bc(O.c, B, bc);
+  for (auto& B : O.b) for (auto& bc : B.bcs) { bc.time = O.time_cur; apply_bc(O.c, B, bc); }
   apply_halos(O);
   for (auto& B : O.b) for (int m = 0; m < 12; ++m) apply_bc(O.c, B, B.edge[m]);
   for (auto& B : O.b) for (int m = 0; m < 8; ++m) apply_bc(O.c, B, B.corner[m]);

@@ -73,12 +73,24 @@ def _with_massflow_crwall(c):
     return c
 
 
-def _prepared(scale, inout=False, massflow=False):
+def _with_heatflux(c):
+    """the jmin wall a HeatFlux-family wall with a constant history"""
+    for b in c["blocks"]:
+        im, jm, km = b["imax"], b["jmax"], b["kmax"]
+        b["bc"] = [(abi.BC_WALL_HEATFLUX if tuple(p) == (1, 1, 1, im, 1, km) else k, p) for k, p in b["bc"]]
+        q = next(n for n, (k, _) in enumerate(b["bc"]) if k == abi.BC_WALL_HEATFLUX)
+        b["heatflux"] = {q: (np.array([0.0, 1.0]), np.array([3.0e4, 3.0e4]))}
+    return c
+
+
+def _prepared(scale, inout=False, massflow=False, heatflux=False):
     c = _state(scale)
     if inout:
         c = _with_inout(c)
     if massflow:
         c = _with_massflow_crwall(c)
+    if heatflux:
+        c = _with_heatflux(c)
     e = _engine(c)
     e.initialize(c["pv0"])
     s = adjoint.StateSetter(e)
@@ -109,6 +121,11 @@ def c4_inout():
 @pytest.fixture(scope="module")
 def c4_massflow():
     return _prepared(4, massflow=True)
+
+
+@pytest.fixture(scope="module")
+def c4_heatflux():
+    return _prepared(4, heatflux=True)
 
 
 def _typical(pv, v):
@@ -266,5 +283,17 @@ def test_vjp_through_massflow_inlet_and_counterrotating_wall(c4_massflow):
     entries = [(k, j, 0, v) if q % 2 == 0 else (k, 0, i, v) for q, (k, j, i, v) in enumerate(base)]
     used, errs, rows = _check(lambda p: s.residual([p])[0], d, entries)
     print(f"mass-flow / counter-rotating rows: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
+    assert used >= len(entries) - 2, rows
+    assert errs.max() <= TOL, (errs, rows)
+
+
+def test_vjp_through_heatflux_wall(c4_heatflux):
+    """rows next to the heat-flux wall (j = 0), whose ghost temperature depends on the
+    boundary cell's temperature, velocity and transport properties"""
+    d = c4_heatflux
+    s = d["s"]
+    entries = [(k, 0, i, v) for (k, j, i, v) in _entries(d["pv"].shape[:-1], d["pv"].shape[-1], 18, 5)]
+    used, errs, rows = _check(lambda p: s.residual([p])[0], d, entries)
+    print(f"heat-flux wall rows: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
     assert used >= len(entries) - 2, rows
     assert errs.max() <= TOL, (errs, rows)

@@ -118,3 +118,45 @@ def test_shifted_periodic_rejects_a_source_outside_the_block():
         native.Engine(c)
     assert ei.value.code == abi.ERR_DESCRIPTOR
     assert "shifted periodic" in str(ei.value)
+
+
+def with_heatflux(c, times, fluxes):
+    """the SST case with its jmin wall a HeatFlux-family wall carrying the given history"""
+    c = replace_faces(c, {"jmin": abi.BC_WALL_HEATFLUX})
+    for b in c["blocks"]:
+        q = next(n for n, (kind, _) in enumerate(b["bc"]) if kind == abi.BC_WALL_HEATFLUX)
+        b["heatflux"] = {q: (np.asarray(times, dtype=np.float64), np.asarray(fluxes, dtype=np.float64))}
+    return c
+
+
+@pytest.mark.parametrize("nsteady", [0, 2])
+def test_heatflux_wall_matches(oracle, nsteady):
+    """bcheatfluxwallviscouskw: the history is read at bcinfo%time -- dt_phy nt_phy when
+    unsteady (stepping through its segments), the accumulated pseudo time when steady"""
+    name, kw, over = BASES["sst"]
+    c = cases.make(name, **kw)
+    c["cfg"].update(over)
+    c["cfg"]["nsteady"] = nsteady
+    dtp = c["cfg"]["dt_phy"]
+    c = with_heatflux(c, [0.0, 1.5 * dtp, 3.0 * dtp], [2.0e4, 6.0e4, 1.0e4])
+    e = native.Engine(c)
+    o = oracle.Oracle(c)
+    e.initialize(c["pv0"])
+    o.initialize(c["pv0"])
+    assert field_err(e.residual(0)["res"], o.residual(0)["res"]).max() < TOL_RES
+    for it, nt_phy in enumerate([1, 2, 4]):
+        _, resg, _ = e.iterate(nt_phy, it + 1, 0.0)
+        _, reso, _ = o.iterate(nt_phy, it + 1, 0.0)
+        assert np.allclose(resg, reso, rtol=1e-7, atol=1e-9 * np.abs(reso).max()), (it, resg, reso)
+    sg, so = e.download(0), o.get_state(0)
+    assert field_err(interior(sg["pv"]), interior(so["pv"])).max() < TOL_STATE
+    # the wall's ghost layers (j = -1, 0, 1)
+    assert field_err(sg["pv"][3:-3, :3, 3:-3], so["pv"][3:-3, :3, 3:-3]).max() < TOL_STATE
+
+
+def test_heatflux_wall_needs_sst():
+    c = cases.make("cavitating", scale=8)
+    c = with_heatflux(replace_faces(c, {"jmin": abi.BC_WALL}), [0.0], [1.0e4])
+    with pytest.raises(native.Cfd3dError) as ei:
+        native.Engine(c)
+    assert ei.value.code == abi.ERR_DESCRIPTOR
