@@ -79,7 +79,7 @@ def _with_heatflux(c):
         im, jm, km = b["imax"], b["jmax"], b["kmax"]
         b["bc"] = [(abi.BC_WALL_HEATFLUX if tuple(p) == (1, 1, 1, im, 1, km) else k, p) for k, p in b["bc"]]
         q = next(n for n, (k, _) in enumerate(b["bc"]) if k == abi.BC_WALL_HEATFLUX)
-        b["heatflux"] = {q: (np.array([0.0, 1.0]), np.array([3.0e4, 3.0e4]))}
+        b["heatflux"] = {q: (np.array([0.0, 1.0]), np.array([150.0, 150.0]))}
     return c
 
 

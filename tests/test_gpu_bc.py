@@ -138,7 +138,7 @@ def test_heatflux_wall_matches(oracle, nsteady):
     c["cfg"].update(over)
     c["cfg"]["nsteady"] = nsteady
     dtp = c["cfg"]["dt_phy"]
-    c = with_heatflux(c, [0.0, 1.5 * dtp, 3.0 * dtp], [2.0e4, 6.0e4, 1.0e4])
+    c = with_heatflux(c, [0.0, 1.5 * dtp, 3.0 * dtp], [50.0, 300.0, 100.0])   # a few K at the wall
     e = native.Engine(c)
     o = oracle.Oracle(c)
     e.initialize(c["pv0"])
