@@ -482,8 +482,10 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
           grf[q][e] = (vv[1] * faf[1][e] + vv[3] * faf[3][e] + vv[5] * faf[5][e] -
                        vv[0] * faf[0][e] - vv[2] * faf[2][e] - vv[4] * faf[4][e]) * ivf;
       }
+      double hs[3] = {0.0, 0.0, 0.0};
+      if (c.ides) grid_spacing<float>(faf, vol, hs);
       const SstOut<float> sf = sst_source_f(grf, (float)kk, (float)oo, (float)dv[0], (float)tv[0], (float)tv[2],
-                                            (float)y5, (float)vol);
+                                            (float)y5, (float)vol, c.ides, hs);
       so.r7 = sf.r7; so.r8 = sf.r8; so.prod = sf.prod; so.dest = sf.dest; so.div = sf.div; so.pkw = sf.pkw;
       so.bigf = sf.bigf; so.talpha = sf.talpha; so.tbeta = sf.tbeta; so.strain = sf.strain;
     } else {
@@ -503,7 +505,9 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
         for (int e = 0; e < 3; ++e)
           gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
       }
-      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol);
+      double hs[3] = {0.0, 0.0, 0.0};
+      if (c.ides) grid_spacing<double>(fa, vol, hs);
+      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, c.ides, hs);
     }
     res[7] = res[7] + so.r7;
     res[8] = res[8] + so.r8;
@@ -1275,7 +1279,8 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   else if (in->iturb == -2) { c.npv = 7; c.ntv = 2; }
   else if (in->iturb == 0) { c.npv = 9; c.ntv = 3; }
   else { err = "iturb must be -3, -2 or 0"; return false; }
-  if (in->iturb == 0 && in->ides != 0) { err = "only ides = 0 is supported"; return false; }
+  if (in->iturb == 0 && (in->ides < 0 || in->ides > 4)) { err = "ides must be 0..4"; return false; }
+  c.ides = (in->iturb == 0) ? in->ides : 0;
   if (in->fluid != 1 && in->fluid != 2) { err = "fluid must be 1 (stiffened) or 2 (IAPWS-97)"; return false; }
   if (in->ngas != 1) { err = "ngas must be 1 (ideal gas)"; return false; }
   if (in->nscheme < 1 || in->nscheme > 4 || in->nmuscl < 0 || in->nmuscl > 2 || in->nlim < 0 || in->nlim > 10) {

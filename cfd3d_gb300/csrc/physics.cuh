@@ -29,6 +29,7 @@ struct Par {
   int nsteady, iturb, nscheme, nmuscl, nlim, local, prec, fluid, ncav, fix_cav_clamp, with_prop;
   int mixed;   // 1: the mixed-precision form (IF97 sums in df64)
   int timemethod;   // 1 explicit Euler, 2 third-order Runge-Kutta, 3 LU-SGS
+  int ides;         // SST length scale: 0 RANS, 1 DES, 2 DDES, 3 IDDES, 4 simplified IDDES
   double dt_phy, cfl, c_v, c_c, pref, uref, str, rhoref, l_chord;
   double kref, oref, emutref;
   double uref_vec[3], tref, y1ref, y2ref;   // free-stream state bcinfo%pv (src/bc_module.f90:133-146)
@@ -824,9 +825,56 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
 template <class T>
 struct SstOut { T r7, r8, prod, dest, div, pkw, bigf, talpha, tbeta, strain; };
 
+// the cell's grid spacings vol / (mean face area) per direction, from its six face vectors
+// (the LES length of the DES variants)
+template <class F>
+__device__ __forceinline__ void grid_spacing(const F (*fa)[3], double vol, double* hs) {
+  for (int d = 0; d < 3; ++d) {
+    const double a1 = ::sqrt((double)fa[2 * d][0] * fa[2 * d][0] + (double)fa[2 * d][1] * fa[2 * d][1] +
+                             (double)fa[2 * d][2] * fa[2 * d][2]);
+    const double a2 = ::sqrt((double)fa[2 * d + 1][0] * fa[2 * d + 1][0] + (double)fa[2 * d + 1][1] * fa[2 * d + 1][1] +
+                             (double)fa[2 * d + 1][2] * fa[2 * d + 1][2]);
+    hs[d] = vol / (0.5 * (a1 + a2));
+  }
+}
+
+// calturblength (src/turbsource_module.f90:406-576): the length scale of the k destruction
+// -- no_des (ides 0), sst_des (1), sst_ddes (2), sst_iddes (3), sst_s_iddes (4).  hs: the
+// grid spacings (metrics only); mu, mut the laminar and eddy viscosities.
+template <class T>
+__device__ __forceinline__ T sst_length(int ides, T kk, T oo, T bigf, T strain, T vort, const double* hs, double y5,
+                                        T mu, T mut) {
+  const T tl_rans = sqrt(kk) / T(9.0) / oo * T(100.0);
+  if (ides == 0) return tl_rans;
+  const double hmax = ::fmax(::fmax(hs[0], hs[1]), hs[2]);
+  if (ides == 1) return fmin(tl_rans, T(0.61 * hmax));
+  const T cdes = T(0.78) * bigf + T(0.61) * (T(1.0) - bigf);
+  const T den = T(0.41 * 0.41 * y5 * y5) * sqrt(T(0.5) * (strain + vort));
+  if (ides == 2) {
+    const T x = T(20.0) * ((mu + mut) / den);
+    const T fd = T(1.0) - tanh(x * x * x);
+    return tl_rans - fd * fmax(T(0.0), tl_rans - cdes * T(hmax));
+  }
+  const T tl_les = cdes * T(::fmin(0.15 * ::fmax(y5, hmax), hmax));
+  const double alpha = 0.25 - y5 / hmax;
+  const double fb = ::fmin(2.0 * ::exp(-9.0 * alpha * alpha), 1.0);
+  const T rdt = mut / den, xt = T(20.0) * rdt;
+  const T fdt = T(1.0) - tanh(xt * xt * xt);
+  const T fd = fmax(T(1.0) - fdt, T(fb));
+  if (ides == 4) return fd * tl_rans + (T(1.0) - fd) * tl_les;
+  const T xl = T(25.0) * (mu / den), xl2 = xl * xl, xl4 = xl2 * xl2;
+  const T fl = tanh(xl4 * xl4 * xl2);
+  const T x3 = T(3.4969) * rdt;
+  const T ft = tanh(x3 * x3 * x3);
+  const T fe2 = T(1.0) - fmax(ft, fl);
+  const double fe1 = (alpha >= 0.0) ? 2.0 * ::exp(-11.09 * alpha * alpha) : 2.0 * ::exp(-9.0 * alpha * alpha);
+  const T fe = fe2 * T(::fmax(fe1 - 1.0, 0.0));
+  return fd * (T(1.0) + fe) * tl_rans + (T(1.0) - fd) * tl_les;
+}
+
 template <class T>
 __device__ __forceinline__ SstOut<T> sst_source(const T (*gr)[3], T kk, T oo, T rho, T mu, T mut, double y5,
-                                                double vol) {
+                                                double vol, int ides = 0, const double* hs = nullptr) {
   const double c23 = 2.0 / 3.0, c59 = 5.0 / 9.0;
   SstOut<T> o;
   T dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
@@ -847,6 +895,10 @@ __device__ __forceinline__ SstOut<T> sst_source(const T (*gr)[3], T kk, T oo, T 
   o.talpha = o.bigf * c59 + (1.0 - o.bigf) * 0.44;
   o.tbeta = o.bigf * 0.075 + (1.0 - o.bigf) * 0.0828;
   T tl = sqrt(kk) / 9.0 / oo * 100.0;
+  if (ides != 0) {
+    const T vort = sq(dudy - dvdx) + sq(dudz - dwdx) + sq(dvdz - dwdy);
+    tl = sst_length<T>(ides, kk, oo, o.bigf, o.strain, vort, hs, y5, mu, mut);
+  }
   o.dest = rho * pow(kk, 1.5) / tl;
   o.r7 = (o.prod - o.dest) * vol;
   o.r8 = (o.talpha * rho * (1.0 / mut) * o.prod - o.tbeta * rho * oo * oo + 1.712 * (1.0 - o.bigf) * rho * (1.0 / oo) * o.pkw) * vol;

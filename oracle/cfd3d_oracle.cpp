@@ -118,7 +118,7 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
   else if (c.iturb == -2) { c.npv = 7; c.ntv = 2; }
   else if (c.iturb == 0) { c.npv = 9; c.ntv = 3; }
   else { err = "iturb must be -3, -2 or 0"; return false; }
-  if (c.iturb == 0 && c.ides != 0) { err = "only ides = 0 is supported"; return false; }
+  if (c.iturb == 0 && (c.ides < 0 || c.ides > 4)) { err = "ides must be 0..4"; return false; }
   c.nqq = c.nsteady >= 1 ? 2 : 0;
   c.ngrd = (c.iturb == 0) ? 5 : 4;
   if (c.fluid != 1 && c.fluid != 2) { err = "fluid must be 1 or 2"; return false; }
@@ -1132,7 +1132,7 @@ static void calrhs_block(const Cfg& c, Block& B) {
           double tv[3];
           for (int m = 0; m < 3; ++m) tv[m] = B.tv(m, i, j, k);
           TurbOut to = kwsst_source(x7, B.cx.at(i - 1, j, k), B.cx.at(i, j, k), B.ex.at(i, j - 1, k), B.ex.at(i, j, k),
-                                    B.tx.at(i, j, k - 1), B.tx.at(i, j, k), grd, dv, tv);
+                                    B.tx.at(i, j, k - 1), B.tx.at(i, j, k), grd, dv, tv, c.ides);
           B.omega_cut(0, i, j, k) = to.omega_cut;
           B.res(7, i, j, k) = B.res(7, i, j, k) + to.source[0];
           B.res(8, i, j, k) = B.res(8, i, j, k) + to.source[1];

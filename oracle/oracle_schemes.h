@@ -662,10 +662,52 @@ static inline void cell_grad(const double (*x)[NPV_MAX], const double* cx1, cons
 
 struct TurbOut { double source[2], itt[4], omega_cut; };
 
-/* kwsst source with ides = 0 (src/turbsource_module.f90:269-414) */
+/* x**10 as a Fortran compiler expands it (cube() is x**3) */
+static inline double pow10i(double x) { const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4; return x8 * x2; }
+
+/* calturblength: the turbulent length scale of the k destruction, by ides -- no_des, sst_des,
+ * sst_ddes, sst_iddes, sst_s_iddes (src/turbsource_module.f90:406-576) */
+static inline double turb_length(int ides, double k, double o, double bigf, double strain_sq, double vorticity_sq,
+                                 const double* cx1, const double* cx2, const double* ex1, const double* ex2,
+                                 const double* tx1, const double* tx2, const double* grd, const double* tv) {
+  const double tl_rans = std::sqrt(k) / 9.0 / o * 100.0;
+  if (ides == 0) return tl_rans;
+  const double vol = grd[0];
+  double gs[3];
+  const double* f[3][2] = {{cx1, cx2}, {ex1, ex2}, {tx1, tx2}};
+  for (int d = 0; d < 3; ++d)
+    gs[d] = vol / (0.5 * (std::sqrt(sq(f[d][0][0]) + sq(f[d][0][1]) + sq(f[d][0][2])) +
+                          std::sqrt(sq(f[d][1][0]) + sq(f[d][1][1]) + sq(f[d][1][2]))));
+  const double hmax = dmax3(gs[0], gs[1], gs[2]);
+  if (ides == 1) return dmin(tl_rans, 0.61 * hmax);
+  const double cdes = 0.78 * bigf + 0.61 * (1.0 - bigf);
+  const double den = sq(0.41) * sq(grd[4]) * std::sqrt(0.5 * (strain_sq + vorticity_sq));
+  if (ides == 2) {
+    const double tl_les = cdes * hmax;
+    const double rd = (tv[0] + tv[2]) / den;
+    const double fd = 1.0 - std::tanh(cube(20.0 * rd));
+    return tl_rans - fd * dmax(0.0, tl_rans - tl_les);
+  }
+  const double tl_les = cdes * dmin(0.15 * dmax(grd[4], hmax), hmax);
+  const double alpha = 0.25 - grd[4] / hmax;
+  const double fb = dmin(2.0 * std::exp(-9.0 * sq(alpha)), 1.0);
+  const double rdt = tv[2] / den;
+  const double fdt = 1.0 - std::tanh(cube(20.0 * rdt));
+  const double fd = dmax(1.0 - fdt, fb);
+  if (ides == 4) return fd * tl_rans + (1.0 - fd) * tl_les;
+  const double rdl = tv[0] / den;
+  const double fl = std::tanh(pow10i(25.0 * rdl));
+  const double ft = std::tanh(cube(3.4969 * rdt));
+  const double fe2 = 1.0 - dmax(ft, fl);
+  const double fe1 = (alpha >= 0.0) ? 2.0 * std::exp(-11.09 * sq(alpha)) : 2.0 * std::exp(-9.0 * sq(alpha));
+  const double fe = fe2 * dmax(fe1 - 1.0, 0.0);
+  return fd * (1.0 + fe) * tl_rans + (1.0 - fd) * tl_les;
+}
+
+/* kwsst source (src/turbsource_module.f90:269-383) with the length scale of ides */
 static inline TurbOut kwsst_source(const double (*x)[NPV_MAX], const double* cx1, const double* cx2,
                                    const double* ex1, const double* ex2, const double* tx1, const double* tx2,
-                                   const double* grd, const double* dv, const double* tv) {
+                                   const double* grd, const double* dv, const double* tv, int ides = 0) {
   TurbOut r;
   double gk[3], go[3], gu[3], gv[3], gw[3];
   cell_grad(x, cx1, cx2, ex1, ex2, tx1, tx2, grd[0], 7, gk);
@@ -694,7 +736,8 @@ static inline TurbOut kwsst_source(const double (*x)[NPV_MAX], const double* cx1
   double talpha = bigf * c59 + (1.0 - bigf) * 0.44;
   double tbeta = bigf * 0.075 + (1.0 - bigf) * 0.0828;
   double ki = 1.0 / k, oi = 1.0 / o, ei = 1.0 / tv[2];
-  double tl = std::sqrt(k) / 9.0 / o * 100.0;          /* no_des (:406-414) */
+  const double vorticity_sq = sq(dudy - dvdx) + sq(dudz - dwdx) + sq(dvdz - dwdy);
+  double tl = turb_length(ides, k, o, bigf, strain_sq, vorticity_sq, cx1, cx2, ex1, ex2, tx1, tx2, grd, tv);
   double dest = dv[0] * std::pow(k, 1.5) / tl;
   r.source[0] = (prod - dest) * grd[0];
   r.source[1] = (talpha * dv[0] * ei * prod - tbeta * dv[0] * sq(o) + 1.712 * (1.0 - bigf) * dv[0] * oi * pkw) * grd[0];
