@@ -93,14 +93,13 @@ __global__ void __launch_bounds__(64) k_adj_cell(DevPtr d, Par c, AdjPtr a) {
       const double mu = d.tv[g], mut = d.tv[2 * n + g];
       const double y5 = d.gm[(GM_GRD + 4) * n + g];
       double w[20];
-      double hs[3] = {0.0, 0.0, 0.0};
-      if (c.ides) grid_spacing<double>(fa, vol, hs);
+      const double hmax = c.ides ? grid_hmax<double>(fa, vol) : 0.0;
       for (int k0 = 0; k0 < 20; k0 += DC) {
         DD gr[5][3];
         for (int q = 0; q < 5; ++q)
           for (int e = 0; e < 3; ++e) gr[q][e] = seed(grv[q][e], 3 * q + e, k0);
         const SstOut<DD> so = sst_source<DD>(gr, seed(pv2[7], 15, k0), seed(pv2[8], 16, k0), seed(dv[0], 17, k0),
-                                             seed(mu, 18, k0), seed(mut, 19, k0), y5, vol, c.ides, hs);
+                                             seed(mu, 18, k0), seed(mut, 19, k0), y5, vol, c.ides, hmax);
         for (int q = 0; q < DC && k0 + q < 20; ++q) w[k0 + q] = lam[7] * so.r7.d[q] + lam[8] * so.r8.d[q];
       }
       // the cell gradients are linear in the face averages 0.5 (P[nbr] + P[g])

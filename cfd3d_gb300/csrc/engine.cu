@@ -482,10 +482,9 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
           grf[q][e] = (vv[1] * faf[1][e] + vv[3] * faf[3][e] + vv[5] * faf[5][e] -
                        vv[0] * faf[0][e] - vv[2] * faf[2][e] - vv[4] * faf[4][e]) * ivf;
       }
-      double hs[3] = {0.0, 0.0, 0.0};
-      if (c.ides) grid_spacing<float>(faf, vol, hs);
+      const double hmax = c.ides ? grid_hmax<float>(faf, vol) : 0.0;
       const SstOut<float> sf = sst_source_f(grf, (float)kk, (float)oo, (float)dv[0], (float)tv[0], (float)tv[2],
-                                            (float)y5, (float)vol, c.ides, hs);
+                                            (float)y5, (float)vol, c.ides, hmax);
       so.r7 = sf.r7; so.r8 = sf.r8; so.prod = sf.prod; so.dest = sf.dest; so.div = sf.div; so.pkw = sf.pkw;
       so.bigf = sf.bigf; so.talpha = sf.talpha; so.tbeta = sf.tbeta; so.strain = sf.strain;
     } else {
@@ -505,9 +504,8 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
         for (int e = 0; e < 3; ++e)
           gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
       }
-      double hs[3] = {0.0, 0.0, 0.0};
-      if (c.ides) grid_spacing<double>(fa, vol, hs);
-      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, c.ides, hs);
+      const double hmax = c.ides ? grid_hmax<double>(fa, vol) : 0.0;
+      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, c.ides, hmax);
     }
     res[7] = res[7] + so.r7;
     res[8] = res[8] + so.r8;

@@ -64,7 +64,7 @@ __device__ __forceinline__ float eos_c2_f(int fluid, float p, float t, float y1,
 // about 1e-6 relative.  Same formulas and order.
 __device__ __forceinline__ SstOut<float> sst_source_f(const float (*gr)[3], float kk, float oo, float rho, float mu,
                                                       float mut, float y5, float vol, int ides = 0,
-                                                      const double* hs = nullptr) {
+                                                      double hmax = 0.0) {
   const float c23 = 2.0f / 3.0f, c59 = 5.0f / 9.0f;
   SstOut<float> o;
   float dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
@@ -87,7 +87,7 @@ __device__ __forceinline__ SstOut<float> sst_source_f(const float (*gr)[3], floa
   float tl = sqrtf(kk) / 9.0f / oo * 100.0f;
   if (ides != 0) {
     const float vort = sq(dudy - dvdx) + sq(dudz - dwdx) + sq(dvdz - dwdy);
-    tl = sst_length<float>(ides, kk, oo, o.bigf, o.strain, vort, hs, (double)y5, mu, mut);
+    tl = sst_length_f(ides, kk, oo, o.bigf, o.strain, vort, hmax, (double)y5, mu, mut);
   }
   o.dest = rho * kk * sqrtf(kk) / tl;
   o.r7 = (o.prod - o.dest) * vol;

@@ -15,6 +15,7 @@
 // The split Jacobian is applied matrix-free: its rows are rank-one updates of row 1 plus
 // a diagonal, so A*dq costs O(npv) instead of the reference's O(npv^2).
 #pragma once
+#include <type_traits>
 #include "iapws.cuh"
 #include "df64.cuh"
 
@@ -825,28 +826,29 @@ __device__ inline void inviscid_flux(const Par& c, const double* n, const FaceSt
 template <class T>
 struct SstOut { T r7, r8, prod, dest, div, pkw, bigf, talpha, tbeta, strain; };
 
-// the cell's grid spacings vol / (mean face area) per direction, from its six face vectors
-// (the LES length of the DES variants)
+// the largest of the cell's grid spacings vol / (mean face area) per direction, from its
+// six face vectors (the LES length of the DES variants)
 template <class F>
-__device__ __forceinline__ void grid_spacing(const F (*fa)[3], double vol, double* hs) {
+__device__ __forceinline__ double grid_hmax(const F (*fa)[3], double vol) {
+  double h = 0.0;
   for (int d = 0; d < 3; ++d) {
     const double a1 = ::sqrt((double)fa[2 * d][0] * fa[2 * d][0] + (double)fa[2 * d][1] * fa[2 * d][1] +
                              (double)fa[2 * d][2] * fa[2 * d][2]);
     const double a2 = ::sqrt((double)fa[2 * d + 1][0] * fa[2 * d + 1][0] + (double)fa[2 * d + 1][1] * fa[2 * d + 1][1] +
                              (double)fa[2 * d + 1][2] * fa[2 * d + 1][2]);
-    hs[d] = vol / (0.5 * (a1 + a2));
+    h = ::fmax(h, vol / (0.5 * (a1 + a2)));
   }
+  return h;
 }
 
 // calturblength (src/turbsource_module.f90:406-576): the length scale of the k destruction
-// -- no_des (ides 0), sst_des (1), sst_ddes (2), sst_iddes (3), sst_s_iddes (4).  hs: the
-// grid spacings (metrics only); mu, mut the laminar and eddy viscosities.
+// -- no_des (ides 0), sst_des (1), sst_ddes (2), sst_iddes (3), sst_s_iddes (4).  hmax: the
+// largest grid spacing (metrics only); mu, mut the laminar and eddy viscosities.
 template <class T>
-__device__ __forceinline__ T sst_length(int ides, T kk, T oo, T bigf, T strain, T vort, const double* hs, double y5,
+__device__ __forceinline__ T sst_length(int ides, T kk, T oo, T bigf, T strain, T vort, double hmax, double y5,
                                         T mu, T mut) {
   const T tl_rans = sqrt(kk) / T(9.0) / oo * T(100.0);
   if (ides == 0) return tl_rans;
-  const double hmax = ::fmax(::fmax(hs[0], hs[1]), hs[2]);
   if (ides == 1) return fmin(tl_rans, T(0.61 * hmax));
   const T cdes = T(0.78) * bigf + T(0.61) * (T(1.0) - bigf);
   const T den = T(0.41 * 0.41 * y5 * y5) * sqrt(T(0.5) * (strain + vort));
@@ -872,9 +874,20 @@ __device__ __forceinline__ T sst_length(int ides, T kk, T oo, T bigf, T strain, 
   return fd * (T(1.0) + fe) * tl_rans + (T(1.0) - fd) * tl_les;
 }
 
+// out-of-line copies for the residual kernels: the DES path keeps its code and registers
+// off the RANS path
+__device__ __noinline__ double sst_length_d(int ides, double kk, double oo, double bigf, double strain, double vort,
+                                            double hmax, double y5, double mu, double mut) {
+  return sst_length<double>(ides, kk, oo, bigf, strain, vort, hmax, y5, mu, mut);
+}
+__device__ __noinline__ float sst_length_f(int ides, float kk, float oo, float bigf, float strain, float vort,
+                                           double hmax, double y5, float mu, float mut) {
+  return sst_length<float>(ides, kk, oo, bigf, strain, vort, hmax, y5, mu, mut);
+}
+
 template <class T>
 __device__ __forceinline__ SstOut<T> sst_source(const T (*gr)[3], T kk, T oo, T rho, T mu, T mut, double y5,
-                                                double vol, int ides = 0, const double* hs = nullptr) {
+                                                double vol, int ides = 0, double hmax = 0.0) {
   const double c23 = 2.0 / 3.0, c59 = 5.0 / 9.0;
   SstOut<T> o;
   T dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
@@ -897,7 +910,8 @@ __device__ __forceinline__ SstOut<T> sst_source(const T (*gr)[3], T kk, T oo, T 
   T tl = sqrt(kk) / 9.0 / oo * 100.0;
   if (ides != 0) {
     const T vort = sq(dudy - dvdx) + sq(dudz - dwdx) + sq(dvdz - dwdy);
-    tl = sst_length<T>(ides, kk, oo, o.bigf, o.strain, vort, hs, y5, mu, mut);
+    if constexpr (std::is_same<T, double>::value) tl = sst_length_d(ides, kk, oo, o.bigf, o.strain, vort, hmax, y5, mu, mut);
+    else tl = sst_length<T>(ides, kk, oo, o.bigf, o.strain, vort, hmax, y5, mu, mut);
   }
   o.dest = rho * pow(kk, 1.5) / tl;
   o.r7 = (o.prod - o.dest) * vol;
