@@ -876,11 +876,11 @@ __device__ __forceinline__ T sst_length(int ides, T kk, T oo, T bigf, T strain, 
 
 // out-of-line copies for the residual kernels: the DES path keeps its code and registers
 // off the RANS path
-__device__ __noinline__ double sst_length_d(int ides, double kk, double oo, double bigf, double strain, double vort,
+static __device__ __noinline__ double sst_length_d(int ides, double kk, double oo, double bigf, double strain, double vort,
                                             double hmax, double y5, double mu, double mut) {
   return sst_length<double>(ides, kk, oo, bigf, strain, vort, hmax, y5, mu, mut);
 }
-__device__ __noinline__ float sst_length_f(int ides, float kk, float oo, float bigf, float strain, float vort,
+static __device__ __noinline__ float sst_length_f(int ides, float kk, float oo, float bigf, float strain, float vort,
                                            double hmax, double y5, float mu, float mut) {
   return sst_length<float>(ides, kk, oo, bigf, strain, vort, hmax, y5, mu, mut);
 }
