@@ -349,7 +349,9 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
 // ------------------------------------------------------------------ residual + sources
 // REC = false (the explicit schemes): the residual alone, without the sweep records (a
 // separate instantiation, so that the LU-SGS kernel carries no branch for it)
-template <bool MX, bool REC = true>
+// DES: the SST destruction takes the DES length scale of c.ides (a separate instantiation,
+// so that the RANS kernel carries none of its code)
+template <bool MX, bool REC = true, bool DES = false>
 __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
@@ -482,9 +484,9 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
           grf[q][e] = (vv[1] * faf[1][e] + vv[3] * faf[3][e] + vv[5] * faf[5][e] -
                        vv[0] * faf[0][e] - vv[2] * faf[2][e] - vv[4] * faf[4][e]) * ivf;
       }
-      const double hmax = c.ides ? grid_hmax<float>(faf, vol) : 0.0;
+      const double hmax = DES ? grid_hmax<float>(faf, vol) : 0.0;
       const SstOut<float> sf = sst_source_f(grf, (float)kk, (float)oo, (float)dv[0], (float)tv[0], (float)tv[2],
-                                            (float)y5, (float)vol, c.ides, hmax);
+                                            (float)y5, (float)vol, DES ? c.ides : 0, hmax);
       so.r7 = sf.r7; so.r8 = sf.r8; so.prod = sf.prod; so.dest = sf.dest; so.div = sf.div; so.pkw = sf.pkw;
       so.bigf = sf.bigf; so.talpha = sf.talpha; so.tbeta = sf.tbeta; so.strain = sf.strain;
     } else {
@@ -504,8 +506,8 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
         for (int e = 0; e < 3; ++e)
           gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
       }
-      const double hmax = c.ides ? grid_hmax<double>(fa, vol) : 0.0;
-      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, c.ides, hmax);
+      const double hmax = DES ? grid_hmax<double>(fa, vol) : 0.0;
+      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, DES ? c.ides : 0, hmax);
     }
     res[7] = res[7] + so.r7;
     res[8] = res[8] + so.r8;
@@ -1138,6 +1140,26 @@ int ensure_staging(cfd3d_handle* h, size_t bytes) {
 // polls of a neighbour's done flag before a dataflow sweep gives up (about 0.1-0.5 s)
 constexpr long long SWEEP_SPIN = 1ll << 22;
 
+// k_rhs in the instantiation of the form (mixed / FP64), the time integrator (sweep records
+// for LU-SGS) and the length scale (DES)
+template <bool REC>
+void launch_rhs_rec(const Engine& E, cudaStream_t s, int T) {
+  const Par& c = E.par;
+  const unsigned g = nblk_of(E.nint, T);
+  const bool des = c.iturb == 0 && c.ides != 0;
+  if (c.mixed) {
+    if (des) k_rhs<true, REC, true><<<g, T, 0, s>>>(E.d, c);
+    else k_rhs<true, REC, false><<<g, T, 0, s>>>(E.d, c);
+  } else {
+    if (des) k_rhs<false, REC, true><<<g, T, 0, s>>>(E.d, c);
+    else k_rhs<false, REC, false><<<g, T, 0, s>>>(E.d, c);
+  }
+}
+void launch_rhs(const Engine& E, cudaStream_t s, int T, bool rec) {
+  if (rec) launch_rhs_rec<true>(E, s, T);
+  else launch_rhs_rec<false>(E, s, T);
+}
+
 // the launch sequence of one iteration (captured into the graph); `mark` (optional)
 // records an event after each stage for the stage profile
 void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
@@ -1160,13 +1182,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   if (c.mixed) launch_face_flux_mixed(E, s);
   else launch_face_flux(E, s);
   stage(3);
-  if (c.timemethod != 3) {
-    if (c.mixed) k_rhs<true, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
-    else k_rhs<false, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
-  } else {
-    if (c.mixed) k_rhs<true><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
-    else k_rhs<false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
-  }
+  launch_rhs(E, s, E.tpb_rhs, c.timemethod == 3);
   stage(4);
   n += c.mixed ? 8 : 4;
   if (!full) { E.launches_per_iter = n; return; }
@@ -1180,8 +1196,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
           if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
         if (c.mixed) launch_face_flux_mixed(E, s);
         else launch_face_flux(E, s);
-        if (c.mixed) k_rhs<true, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
-        else k_rhs<false, false><<<nblk_of(E.nint, E.tpb_rhs), E.tpb_rhs, 0, s>>>(d, c);
+        launch_rhs(E, s, E.tpb_rhs, false);
         n += c.mixed ? 8 : 4;
       }
       if (m == nstage) { stage(5); stage(6); }
@@ -2032,8 +2047,7 @@ int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
   tbest = 1e30f;
   for (int T : cands) {
     const float t = time_calls(E, reps, [&] {
-      if (c.mixed) k_rhs<true><<<nblk_of(E.nint, T), T, 0, E.st>>>(d, c);
-      else k_rhs<false><<<nblk_of(E.nint, T), T, 0, E.st>>>(d, c);
+      launch_rhs(E, E.st, T, c.timemethod == 3);
     });
     if (t < tbest) { tbest = t; best = T; }
   }
