@@ -51,6 +51,7 @@ class Config(C.Structure):
         ("l_domain", C.c_double),
         ("fix_cav_clamp", C.c_int), ("precision", C.c_int),
         ("kinf", C.c_double), ("oinf", C.c_double),
+        ("gravity", C.c_int), ("ngravity", C.c_int), ("gravity_data", C.POINTER(C.c_double)),
     ]
 
 
@@ -77,10 +78,19 @@ def config_from_dict(d):
                     nmuscl=1, nlim=1, timemethod=3, local=1, prec=1, cfl=1.0, fluid=2, ngas=1, ncav=0,
                     c_v=0.0, c_c=0.0, pref=101325.0, uref=10.0, aoa=0.0, aos=0.0, tref=300.0,
                     y1ref=0.0, y2ref=1e-7, l_chord=1.0, l_character=1.0, scale=1.0, l_domain=1.0,
-                    fix_cav_clamp=0, precision=FP64, kinf=0.0, oinf=0.0)
+                    fix_cav_clamp=0, precision=FP64, kinf=0.0, oinf=0.0, gravity=0)
     defaults.update(d)
+    table = defaults.pop("gravity_data", None)
     for k, v in defaults.items():
+        if k in ("ngravity",):
+            continue
         setattr(cfg, k, v)
+    if table is not None:
+        # the gravity history (t, gx, gy, gz) rows; kept alive with the struct
+        arr = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 4)
+        cfg._gravity_keep = arr
+        cfg.ngravity = arr.shape[0]
+        cfg.gravity_data = arr.ctypes.data_as(C.POINTER(C.c_double))
     return cfg
 
 

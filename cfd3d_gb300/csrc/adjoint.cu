@@ -134,6 +134,14 @@ __global__ void __launch_bounds__(64) k_adj_cell(DevPtr d, Par c, AdjPtr a) {
       gd[GD_RHO] += grho;
       gd[GD_H] += mu_[4] * r;
     }
+    // ---- gravity: res(2:4) += rho vol a, res(5) += rho vol (a . u)
+    if (c.gravity) {
+      double ga[3];
+      gravity_at(d.grav, bc_time(d, c), ga);
+      const double au = ga[0] * pv2[1] + ga[1] * pv2[2] + ga[2] * pv2[3];
+      gd[GD_RHO] += vol * (lam[1] * ga[0] + lam[2] * ga[1] + lam[3] * ga[2] + lam[4] * au);
+      for (int e = 0; e < 3; ++e) gp[1 + e] += lam[4] * dv[0] * vol * ga[e];
+    }
     for (int v = 0; v < npv; ++v) aadd(&a.gpv[v * n + g], gp[v]);
     for (int m = 0; m < NGD; ++m) aadd(&a.gdt[m * n + g], gd[m]);
   }

@@ -349,9 +349,10 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
 // ------------------------------------------------------------------ residual + sources
 // REC = false (the explicit schemes): the residual alone, without the sweep records (a
 // separate instantiation, so that the LU-SGS kernel carries no branch for it)
-// DES: the SST destruction takes the DES length scale of c.ides (a separate instantiation,
-// so that the RANS kernel carries none of its code)
-template <bool MX, bool REC = true, bool DES = false>
+// XS (extended sources): the SST destruction with the DES length scale of c.ides and the
+// gravity source (a separate instantiation, so that the plain kernel carries none of their
+// code)
+template <bool MX, bool REC = true, bool XS = false>
 __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
@@ -484,9 +485,9 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
           grf[q][e] = (vv[1] * faf[1][e] + vv[3] * faf[3][e] + vv[5] * faf[5][e] -
                        vv[0] * faf[0][e] - vv[2] * faf[2][e] - vv[4] * faf[4][e]) * ivf;
       }
-      const double hmax = DES ? grid_hmax<float>(faf, vol) : 0.0;
+      const double hmax = (XS && c.ides) ? grid_hmax<float>(faf, vol) : 0.0;
       const SstOut<float> sf = sst_source_f(grf, (float)kk, (float)oo, (float)dv[0], (float)tv[0], (float)tv[2],
-                                            (float)y5, (float)vol, DES ? c.ides : 0, hmax);
+                                            (float)y5, (float)vol, XS ? c.ides : 0, hmax);
       so.r7 = sf.r7; so.r8 = sf.r8; so.prod = sf.prod; so.dest = sf.dest; so.div = sf.div; so.pkw = sf.pkw;
       so.bigf = sf.bigf; so.talpha = sf.talpha; so.tbeta = sf.tbeta; so.strain = sf.strain;
     } else {
@@ -506,8 +507,8 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
         for (int e = 0; e < 3; ++e)
           gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
       }
-      const double hmax = DES ? grid_hmax<double>(fa, vol) : 0.0;
-      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, DES ? c.ides : 0, hmax);
+      const double hmax = (XS && c.ides) ? grid_hmax<double>(fa, vol) : 0.0;
+      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, XS ? c.ides : 0, hmax);
     }
     res[7] = res[7] + so.r7;
     res[8] = res[8] + so.r8;
@@ -558,6 +559,14 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
       double s = (double)c.nsteady * (bb * fx[v] - q1) + 0.5 * ((double)c.nsteady - 1.0) * q2;
       res[v] = res[v] - s * vol / c.dt_phy;
     }
+  }
+  if (XS && c.gravity) {
+    // gravity%getgravitysource (src/gravity_module.f90:110-131) at the residual's time
+    double a[3];
+    gravity_at(d.grav, bc_time(d, c), a);
+    const double rv = dv[0] * vol;
+    for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] + rv * a[e];
+    res[4] = res[4] + rv * (a[0] * pv2[1] + a[1] * pv2[2] + a[2] * pv2[3]);
   }
   for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
   if constexpr (!REC) return;   // the explicit schemes need no sweep records
@@ -1141,17 +1150,17 @@ int ensure_staging(cfd3d_handle* h, size_t bytes) {
 constexpr long long SWEEP_SPIN = 1ll << 22;
 
 // k_rhs in the instantiation of the form (mixed / FP64), the time integrator (sweep records
-// for LU-SGS) and the length scale (DES)
+// for LU-SGS) and the extended sources (DES length scale, gravity)
 template <bool REC>
 void launch_rhs_rec(const Engine& E, cudaStream_t s, int T) {
   const Par& c = E.par;
   const unsigned g = nblk_of(E.nint, T);
-  const bool des = c.iturb == 0 && c.ides != 0;
+  const bool xs = (c.iturb == 0 && c.ides != 0) || c.gravity != 0;
   if (c.mixed) {
-    if (des) k_rhs<true, REC, true><<<g, T, 0, s>>>(E.d, c);
+    if (xs) k_rhs<true, REC, true><<<g, T, 0, s>>>(E.d, c);
     else k_rhs<true, REC, false><<<g, T, 0, s>>>(E.d, c);
   } else {
-    if (des) k_rhs<false, REC, true><<<g, T, 0, s>>>(E.d, c);
+    if (xs) k_rhs<false, REC, true><<<g, T, 0, s>>>(E.d, c);
     else k_rhs<false, REC, false><<<g, T, 0, s>>>(E.d, c);
   }
 }
@@ -1294,6 +1303,14 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   else { err = "iturb must be -3, -2 or 0"; return false; }
   if (in->iturb == 0 && (in->ides < 0 || in->ides > 4)) { err = "ides must be 0..4"; return false; }
   c.ides = (in->iturb == 0) ? in->ides : 0;
+  const int gr = in->gravity;
+  if (!(gr == 0 || gr == 4 || (gr >= -3 && gr <= 3))) { err = "gravity must be 0, +-1, +-2, +-3 or 4"; return false; }
+  if (gr == 4) {
+    if (in->ngravity < 1 || !in->gravity_data) { err = "gravity = 4 without its history"; return false; }
+    for (int m = 1; m < in->ngravity; ++m)
+      if (!(in->gravity_data[4 * m] > in->gravity_data[4 * (m - 1)])) { err = "gravity history times must increase"; return false; }
+  }
+  c.gravity = gr;
   if (in->fluid != 1 && in->fluid != 2) { err = "fluid must be 1 (stiffened) or 2 (IAPWS-97)"; return false; }
   if (in->ngas != 1) { err = "ngas must be 1 (ideal gas)"; return false; }
   if (in->nscheme < 1 || in->nscheme > 4 || in->nmuscl < 0 || in->nmuscl > 2 || in->nlim < 0 || in->nlim > 10) {
@@ -1502,6 +1519,24 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   double big = 1.0e10;
   std::memcpy(&s0.dtmin_bits, &big, 8);
   CFD_CUDA(cudaMemcpy(E.d.sc, &s0, sizeof(Scalars), cudaMemcpyHostToDevice));
+  if (E.par.gravity) {
+    // the history as n, t[n], a[3 n]; a constant acceleration (src/gravity_module.f90:45-61)
+    // is one row at t = 0
+    std::vector<double> tab;
+    if (E.par.gravity == 4) {
+      const int nd = cfg->ngravity;
+      tab.push_back((double)nd);
+      for (int m = 0; m < nd; ++m) tab.push_back(cfg->gravity_data[4 * m]);
+      for (int m = 0; m < nd; ++m) for (int e = 0; e < 3; ++e) tab.push_back(cfg->gravity_data[4 * m + 1 + e]);
+    } else {
+      double a[3] = {0.0, 0.0, 0.0};
+      a[std::abs(E.par.gravity) - 1] = (E.par.gravity > 0 ? 1.0 : -1.0) * 9.80665;
+      tab = {1.0, 0.0, a[0], a[1], a[2]};
+    }
+    CFD_CUDA(cudaMalloc(&E.d_grav, tab.size() * sizeof(double)));
+    CFD_CUDA(cudaMemcpy(E.d_grav, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+    E.d.grav = E.d_grav;
+  }
   {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
@@ -1596,6 +1631,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_nbf);
   cudaFree(E.d_nbb);
   cudaFree(E.d_hft);
+  cudaFree(E.d_grav);
   cudaFree(E.d.rec);
   cudaFree(E.d.done);
   cudaFree(E.d.tickets);
@@ -1922,7 +1958,7 @@ static int finish_iteration(cfd3d_handle* h, int nt_phy, double timeprev, double
 
 // the time inputs of the boundary program (heat-flux histories) for the next launches
 static int set_bc_time(Engine& E, int nt_phy, double timeprev) {
-  if (!E.d_hft) return CFD3D_OK;
+  if (!E.d_hft && !E.d_grav) return CFD3D_OK;
   struct { double tp; int nt, pad; } v{timeprev, nt_phy, 0};
   static_assert(sizeof(v) == 16, "timeprev, nt_phy, pad_ of Scalars");
   CFD_CUDA(cudaMemcpyAsync((char*)E.d.sc + offsetof(Scalars, timeprev), &v, sizeof(v), cudaMemcpyHostToDevice, E.st));

@@ -79,6 +79,7 @@ struct DevPtr {
   long long nint;
   Scalars* sc;
   const double* hft;   // heat-flux histories: per table n, t[n], q[n] (GhostOp.pad is its offset)
+  const double* grav;  // gravity history: n, t[n], a[3 n] (a constant acceleration is one row)
   double* partial;   // per-CTA partial residual sums [gridsize][npv+2]
   // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
   float *pvf, *fi32, *fv32;
@@ -125,6 +126,7 @@ struct Engine {
   GhostOp* d_ops[3] = {nullptr, nullptr, nullptr};
   int nops[3] = {0, 0, 0};
   double* d_hft = nullptr;   // heat-flux histories (d.hft), null without heat-flux walls
+  double* d_grav = nullptr;  // gravity history (d.grav), null without gravity
   // LU-SGS plane-major numbering (setup_planes): cells[t], pos[g], lower / upper neighbours
   int* d_planes = nullptr;
   int* d_pos = nullptr;
@@ -178,6 +180,23 @@ __device__ __forceinline__ double heatflux_at(const double* tab, double tm) {
     }
   if (tm >= t[nd - 1]) hf = q[nd - 1];
   return hf;
+}
+
+// the acceleration of the gravity history at tm (gravity%getgravitysource,
+// src/gravity_module.f90:110-125): linear between the bracketing rows, the last row from
+// its time on; before the first time (undefined in the reference) the first row
+__device__ __forceinline__ void gravity_at(const double* tab, double tm, double* a) {
+  const int nd = (int)tab[0];
+  const double* t = tab + 1;
+  const double* g = tab + 1 + nd;
+  for (int e = 0; e < 3; ++e) a[e] = g[e];
+  for (int i = 0; i < nd - 1; ++i)
+    if (tm >= t[i] && tm < t[i + 1]) {
+      for (int e = 0; e < 3; ++e) a[e] = g[3 * i + e] + (g[3 * (i + 1) + e] - g[3 * i + e]) * (tm - t[i]) / (t[i + 1] - t[i]);
+      break;
+    }
+  if (tm >= t[nd - 1])
+    for (int e = 0; e < 3; ++e) a[e] = g[3 * (nd - 1) + e];
 }
 
 // the time bc%setbc receives (bcinfo%time): dt_phy nt_phy when unsteady, else the

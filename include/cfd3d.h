@@ -82,6 +82,11 @@ typedef struct cfd3d_config {
   int    precision;       /* CFD3D_FP64 or CFD3D_MIXED                            */
   double kinf, oinf;      /* >0: replace the SST free-stream k / omega that
                              config%setref derives (src/config_module.f90:186-189) */
+  /* the gravity source rhs%gravity (src/gravity_module.f90:24-133): 0 none; +-1, +-2, +-3 a
+     constant +-9.80665 m/s^2 along x, y, z; 4 the history of gravity.dat, given here as
+     ngravity rows (t, gx, gy, gz) with t ascending */
+  int    gravity, ngravity;
+  const double *gravity_data;
 } cfd3d_config;
 
 /* A boundary patch: CGNS PointRange in 1-based NODE indices

@@ -101,7 +101,7 @@ struct Oracle {
 
 /* ---------------- config (src/config_module.f90:90-199) ---------------- */
 static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
-  std::memset(&c, 0, sizeof(c));
+  c = Cfg();   /* value-initialised: zeros, empty histories */
   c.nsteady = in->nsteady; c.dt_phy = in->dt_phy;
   c.iturb = in->iturb; c.ides = in->ides; c.nscheme = in->nscheme; c.nmuscl = in->nmuscl; c.nlim = in->nlim;
   c.local = in->local; c.prec = in->prec; c.cfl = in->cfl; c.fluid = in->fluid; c.ngas = in->ngas;
@@ -113,6 +113,19 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
   c.aoa = in->aoa * c.pi / 180.0; c.aos = in->aos * c.pi / 180.0;
   c.str = c.l_character / c.pi / c.dt_phy;
   c.timemethod = in->timemethod;
+  /* gravity (src/gravity_module.f90:24-66): a constant axis acceleration or the history */
+  c.gravity = in->gravity;
+  if (c.gravity == 4) {
+    if (in->ngravity < 1 || !in->gravity_data) { err = "gravity = 4 without its history"; return false; }
+    for (int m = 0; m < in->ngravity; ++m) {
+      c.grav_t.push_back(in->gravity_data[4 * m]);
+      for (int e = 0; e < 3; ++e) c.grav_a.push_back(in->gravity_data[4 * m + 1 + e]);
+    }
+  } else if (c.gravity >= -3 && c.gravity <= 3 && c.gravity != 0) {
+    c.grav_t = {0.0};
+    c.grav_a = {0.0, 0.0, 0.0};
+    c.grav_a[std::abs(c.gravity) - 1] = (c.gravity > 0 ? 1.0 : -1.0) * 9.80665;
+  } else if (c.gravity != 0) { err = "gravity must be 0, +-1, +-2, +-3 or 4"; return false; }
   if (c.timemethod < 1 || c.timemethod > 3) { err = "timemethod must be 1 (Euler), 2 (RK3) or 3 (LU-SGS)"; return false; }
   if (c.iturb == -3) { c.npv = 7; c.ntv = 0; }
   else if (c.iturb == -2) { c.npv = 7; c.ntv = 2; }
@@ -1017,7 +1030,7 @@ static void gather_pv(const Cfg& c, Block& B, int i, int j, int k, double* out) 
   for (int m = 0; m < c.npv; ++m) out[m] = P[m];
 }
 
-static void calrhs_block(const Cfg& c, Block& B) {
+static void calrhs_block(const Cfg& c, Block& B, double time) {
   const int im = B.imax, jm = B.jmax, km = B.kmax, npv = c.npv;
   const bool vis = c.iturb != -3;
   std::vector<double> ea((size_t)npv * (std::max(im, std::max(jm, km)) + 2)), eva(ea.size());
@@ -1143,6 +1156,23 @@ static void calrhs_block(const Cfg& c, Block& B) {
           const double* qq = B.qq.at(i, j, k);
           unsteady_source(c, x7[1], dv, qq, qq + npv, grd[0], us);
           for (int n = 0; n < npv; ++n) B.res(n, i, j, k) = B.res(n, i, j, k) - us[n];
+        }
+        if (c.gravity) {
+          /* gravity%getgravitysource (src/gravity_module.f90:110-131) */
+          double a[3];
+          const int nd = (int)c.grav_t.size();
+          for (int e = 0; e < 3; ++e) a[e] = c.grav_a[e];
+          for (int m = 0; m < nd - 1; ++m)
+            if (time >= c.grav_t[m] && time < c.grav_t[m + 1]) {
+              for (int e = 0; e < 3; ++e)
+                a[e] = c.grav_a[3 * m + e] + (c.grav_a[3 * (m + 1) + e] - c.grav_a[3 * m + e]) * (time - c.grav_t[m]) /
+                                                 (c.grav_t[m + 1] - c.grav_t[m]);
+              break;
+            }
+          if (time >= c.grav_t[nd - 1]) for (int e = 0; e < 3; ++e) a[e] = c.grav_a[3 * (nd - 1) + e];
+          for (int e = 0; e < 3; ++e) B.res(1 + e, i, j, k) = B.res(1 + e, i, j, k) + dv[0] * grd[0] * a[e];
+          B.res(4, i, j, k) = B.res(4, i, j, k) +
+                              dv[0] * grd[0] * (a[0] * x7[1][1] + a[1] * x7[1][2] + a[2] * x7[1][3]);
         }
       }
 }
@@ -1442,7 +1472,7 @@ int orc_metrics(void* h, int b, double* cx, double* ex, double* tx, double* grd)
 int orc_residual(void* h, int b, double* res, double* icav, double* itt, double* omega_cut) {
   Oracle* O = (Oracle*)h;
   setbc(*O);
-  for_blocks(*O, [&](int n) { calrhs_block(O->c, O->b[n]); });
+  for_blocks(*O, [&](int n) { calrhs_block(O->c, O->b[n], O->time_cur); });
   Block& B = O->b[b];
   if (res) std::memcpy(res, B.res.d.data(), B.res.d.size() * 8);
   if (icav) std::memcpy(icav, B.icav.d.data(), B.icav.d.size() * 8);
@@ -1467,14 +1497,14 @@ int orc_iterate(void* h, int nt_phy, int nt, double timeprev, double* time_out, 
   O->time_cur = (c.nsteady == 0) ? tstep : c.dt_phy * (double)nt_phy;
   if (c.timemethod == 3) {
     setbc(*O);
-    for_blocks(*O, [&](int n) { calrhs_block(c, O->b[n]); });
+    for_blocks(*O, [&](int n) { calrhs_block(c, O->b[n], O->time_cur); });
     for_blocks(*O, [&](int n) { lusgs_block(c, O->b[n]); });
   } else {
     /* eulerex: one stage; rk3rd: three, the time step taken at the first only */
     const int nstage = (c.timemethod == 2) ? 3 : 1;
     for (int m = 1; m <= nstage; ++m) {
       setbc(*O);
-      for_blocks(*O, [&](int n) { calrhs_block(c, O->b[n]); });
+      for_blocks(*O, [&](int n) { calrhs_block(c, O->b[n], O->time_cur); });
       for_blocks(*O, [&](int n) { explicit_block(c, O->b[n], m); });
     }
   }

@@ -12,6 +12,7 @@
 #ifndef ORACLE_SCHEMES_H
 #define ORACLE_SCHEMES_H
 
+#include <vector>
 #include "oracle_physics.h"
 
 namespace orc {
@@ -27,6 +28,8 @@ struct Cfg {
   double rhoref, visref, kref, oref, emutref;
   int fix_cav_clamp;
   int timemethod;  /* 1 explicit Euler, 2 RK3, 3 LU-SGS */
+  int gravity;     /* 0 none, +-1..+-3 axis, 4 history */
+  std::vector<double> grav_t, grav_a;   /* the history: times, accelerations (3 per row) */
   bool with_prop;  /* t_eos_prop (iturb >= -2) vs t_eosonly (Euler) */
   EosSel eos;
 };
