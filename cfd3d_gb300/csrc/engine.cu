@@ -77,7 +77,7 @@ __global__ void k_init(DevPtr d, Par c, int b) {
   for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
   if (MX) deteos_split(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
   else deteos<false>(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
-  if (c.iturb == 0) tv[2] = c.emutref;
+  if (c.iturb >= -1) tv[2] = c.emutref;
   for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
   for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
   if (c.nqq) {
@@ -260,6 +260,13 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       store_cell(d, c, op.dst, x);
       return;
     }
+    case G_WALL_KE:
+      // bcwallviscouske (src/bc_module.f90:2324-2366): u, v, w, k, eps and mu_t reflected
+      load_cell(d, c, op.src, x);
+      x.pv[1] = -x.pv[1]; x.pv[2] = -x.pv[2]; x.pv[3] = -x.pv[3]; x.pv[7] = -x.pv[7]; x.pv[8] = -x.pv[8];
+      x.tv[2] = -x.tv[2];
+      store_cell(d, c, op.dst, x);
+      return;
     case G_CRWALL_KW:
       // bccounterrotatingwallviscouskw (src/bc_module.f90:3654-3731) with the grid velocity
       // omega x r = 0 (no rotation): u, v, w, k and mu_t reflected; omega is the mirror's,
@@ -547,6 +554,35 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
       d.itt[g] = it0 * f1; d.itt[n + g] = it1 * f1; d.itt[2 * n + g] = it2 * f2; d.itt[3 * n + g] = it3 * f2;
     }
   }
+  if (c.iturb == -1) {
+    // k-epsilon source (FP64 in both forms); no omega bound
+    const long long nbr[6] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk};
+    double fa[6][3];
+    for (int q = 0; q < 3; ++q) {
+      fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
+      fa[2][q] = d.gm[(GM_EX + q) * n + g - sj]; fa[3][q] = d.gm[(GM_EX + q) * n + g];
+      fa[4][q] = d.gm[(GM_TX + q) * n + g - sk]; fa[5][q] = d.gm[(GM_TX + q) * n + g];
+    }
+    const double ivol = 1.0 / vol;
+    double gr[3][3], gsk[3];
+    for (int q = 0; q < 4; ++q) {
+      const double* P = d.pv + (q < 3 ? 1 + q : 7) * n;
+      const double c0 = P[g];
+      double vv[6];
+      for (int m = 0; m < 6; ++m) vv[m] = 0.5 * (P[nbr[m]] + c0);
+      if (q == 3) for (int m = 0; m < 6; ++m) vv[m] = sqrt(vv[m]);
+      double* o = (q < 3) ? gr[q] : gsk;
+      for (int e = 0; e < 3; ++e)
+        o[e] = (vv[1] * fa[1][e] + vv[3] * fa[3][e] + vv[5] * fa[5][e] - vv[0] * fa[0][e] - vv[2] * fa[2][e] -
+                vv[4] * fa[4][e]) * ivol;
+    }
+    double rk[2], itk[4];
+    ke_source<double>(gr, gsk, pv2[7], pv2[8], dv[0], d.tv[g], d.tv[2 * n + g], vol, rk, itk);
+    res[7] = res[7] + rk[0];
+    res[8] = res[8] + rk[1];
+    for (int q = 0; q < 4; ++q) d.itt[q * n + g] = itk[q];
+    d.ocut[g] = 0.0;
+  }
   if (c.nsteady >= 1) {
     double bb = (c.nsteady == 1) ? 1.0 : 0.75;
     double fx[NPVM];
@@ -587,7 +623,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   }
   double ic[4] = {0, 0, 0, 0}, it4[4] = {0, 0, 0, 0};
   if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
-  if (c.iturb == 0) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
+  if (c.iturb >= -1) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
   Diag D;
   double evis;
   float pvf[NPVM], dvf[12];
@@ -912,7 +948,7 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
     p[0] = fmax(-c.pref + 1.0e1, p[0]);
     p[5] = fmin(1.0, fmax(0.0, p[5]));
     p[6] = fmin(1.0, fmax(0.0, p[6]));
-    if (c.iturb == 0) {
+    if (c.iturb >= -1) {
       p[7] = fmax(p[7], 1.0e-16);
       p[8] = fmax(fmax(p[8], 1.0e-16), d.ocut[g]);
     }
@@ -978,6 +1014,10 @@ __global__ void k_eddy(DevPtr d, Par c) {
   const BlockGeom& B = d.blk[b];
   long long g = interior_cell(B, t - B.int_off, i, j, k);
   const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+  if (c.iturb == -1) {
+    d.tv[2 * n + g] = ke_eddy(d.dv[g], d.pv[7 * n + g], d.pv[8 * n + g], d.tv[g], d.gm[(GM_GRD + 4) * n + g]);
+    return;
+  }
   const long long nbr[6] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk};
   double fa[6][3];
   for (int q = 0; q < 3; ++q) {
@@ -1213,7 +1253,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
       else k_update<false, true><<<E.red_grid, T, 0, s>>>(d, c, m);
       ++n;
       if (m == nstage) stage(7);
-      if (c.iturb == 0) {
+      if (c.iturb >= -1) {
         if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
         else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
         ++n;
@@ -1262,7 +1302,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   else k_update<false><<<E.red_grid, T, 0, s>>>(d, c, 0);
   ++n;
   stage(7);
-  if (c.iturb == 0) {
+  if (c.iturb >= -1) {
     if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
     else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
     ++n;
@@ -1299,8 +1339,8 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   c.timemethod = in->timemethod;
   if (in->iturb == -3) { c.npv = 7; c.ntv = 0; }
   else if (in->iturb == -2) { c.npv = 7; c.ntv = 2; }
-  else if (in->iturb == 0) { c.npv = 9; c.ntv = 3; }
-  else { err = "iturb must be -3, -2 or 0"; return false; }
+  else if (in->iturb == 0 || in->iturb == -1) { c.npv = 9; c.ntv = 3; }
+  else { err = "iturb must be -3, -2, -1 or 0"; return false; }
   if (in->iturb == 0 && (in->ides < 0 || in->ides > 4)) { err = "ides must be 0..4"; return false; }
   c.ides = (in->iturb == 0) ? in->ides : 0;
   const int gr = in->gravity;
@@ -1323,7 +1363,7 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   if (in->precision != CFD3D_FP64 && in->precision != CFD3D_MIXED) { err = "precision must be CFD3D_FP64 or CFD3D_MIXED"; return false; }
   c.mixed = (in->precision == CFD3D_MIXED);
   c.nqq = in->nsteady >= 1 ? 2 : 0;
-  c.ngrd = (in->iturb == 0) ? 5 : 4;
+  c.ngrd = (in->iturb >= -1) ? 5 : 4;
   c.nsteady = in->nsteady; c.iturb = in->iturb; c.nscheme = in->nscheme; c.nmuscl = in->nmuscl; c.nlim = in->nlim;
   c.local = in->local; c.prec = in->prec; c.fluid = in->fluid; c.ncav = in->ncav; c.fix_cav_clamp = in->fix_cav_clamp;
   c.with_prop = (in->iturb != -3);
@@ -1555,6 +1595,13 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
       E.par.oref = 10.0 * cfg->uref / cfg->l_domain;
       E.par.emutref = std::pow(10.0, -5) * tvr[0];
       E.par.kref = E.par.emutref / E.par.rhoref * E.par.oref;
+      if (cfg->kinf > 0) E.par.kref = cfg->kinf;
+      if (cfg->oinf > 0) E.par.oref = cfg->oinf;
+    } else if (c.iturb == -1) {
+      // config%setref for k-epsilon (src/config_module.f90:191-194): oref is epsilon's
+      E.par.kref = 1.5 * (0.0001 * cfg->uref) * (0.0001 * cfg->uref);
+      E.par.emutref = std::pow(10.0, -5) * tvr[0];
+      E.par.oref = 0.09 * E.par.rhoref * E.par.kref * E.par.kref / E.par.emutref;
       if (cfg->kinf > 0) E.par.kref = cfg->kinf;
       if (cfg->oinf > 0) E.par.oref = cfg->oinf;
     }
@@ -2025,6 +2072,7 @@ int cfd3d_residual_vjp(cfd3d_handle* h, const double* cot, double* g_state, doub
   for (const BlockGeom& B : E.blk) maxint = std::max(maxint, (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1));
   int rc = ensure_staging(h, (size_t)maxint * c.npv * 8);
   if (rc) return rc;
+  if (E.par.iturb == -1) { E.err = "the adjoint does not cover the k-epsilon model"; return CFD3D_ERR_ARG; }
   if ((rc = adjoint_buffers(E))) return rc;
   // the cotangent, block after block, into the padded interior
   size_t off = 0;

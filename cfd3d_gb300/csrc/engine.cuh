@@ -33,7 +33,7 @@ enum GhostKind : int {
   G_COPY = 0, G_EXTRAP, G_WALL_VISCOUS, G_WALL_KW, G_SYMMETRY, G_FARFIELD,
   G_WALLWALL, G_WALLWALL_KW4, G_WALLWALL_KW8, G_NOWALL3, G_NOWALL7,
   G_INFLOW_SUB, G_OUTFLOW_SUB, G_INFLOW_SUP,  // the farfield treatment with a forced branch
-  G_CRWALL_KW, G_MASSFLOW_IN, G_HFWALL_KW
+  G_CRWALL_KW, G_MASSFLOW_IN, G_HFWALL_KW, G_WALL_KE
 };
 
 // the farfield_pv branch of a characteristic ghost kind

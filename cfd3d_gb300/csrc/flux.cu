@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) k_face_flux(DevPtr d, Par c) {
   for (int v = 0; v < npv; ++v) fi[v * n + g] = fx[v];
   if (c.iturb == -3) return;
   // ---- viscous flux (vsflux_laminar / vsflux_turbulent)
-  const bool turb = (c.iturb == 0);
+  const bool turb = (c.iturb >= -1);
   const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);   // faces normal to t1
   const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);   // faces normal to t2
   double ev[3], tvv[3];

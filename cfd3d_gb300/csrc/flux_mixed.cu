@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
   for (int v = 0; v < npv; ++v) fo[v * n + g] = fx[v];
   if (c.iturb == -3) return;
   // ---- viscous flux in FP32 (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
-  const bool turb = (c.iturb == 0);
+  const bool turb = (c.iturb >= -1);
   const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);
   const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);
   // metrics from their FP32 copy
@@ -205,7 +205,11 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
           nx[2] * (uc * txz + vc * tyz + wc * tzz + kc * gz[3]);
   fv[5] = 0.0f;
   fv[6] = 0.0f;
-  if (turb) {
+  if (turb && c.iturb == -1) {
+    // k-epsilon: F1 = 0, sigma_k = 1, sigma_eps = 1.3
+    fv[7] = (vis + emut) * (gx[4] * nx[0] + gy[4] * nx[1] + gz[4] * nx[2]);
+    fv[8] = (vis + emut * (1.0f / 1.3f)) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
+  } else if (turb) {
     float pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
     float rho = (float)(0.5 * (d.dv[g] + d.dv[gr]));
     float ydns = 0.5f * (GF[(GM_GRD + 4) * n + g] + GF[(GM_GRD + 4) * n + gr]);

@@ -920,6 +920,51 @@ __device__ __forceinline__ SstOut<T> sst_source(const T (*gr)[3], T kk, T oo, T 
   return o;
 }
 
+// k-epsilon source (t_kepsilon kepsilon, src/turbsource_module.f90:170-267): the production
+// limited to 30 rho eps, the low-Re damping fe1, fe2 and the 2 mu |grad sqrt k|^2 terms, and
+// the 2x2 implicit Jacobian itt with the reference's eigen-sign limiting.  gr: gradients
+// of u, v, w; gsk: gradient of sqrt(k) (from the square roots of the face averages).
+template <class T>
+__device__ __forceinline__ void ke_source(const T (*gr)[3], const T* gsk, T kk, T ee, T rho, T mu, T mut, double vol,
+                                          T* r, T* itt) {
+  const double c23 = 2.0 / 3.0;
+  const T dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
+  const T dvdx = gr[1][0], dvdy = gr[1][1], dvdz = gr[1][2];
+  const T dwdx = gr[2][0], dwdy = gr[2][1], dwdz = gr[2][2];
+  const T kkyy = gsk[0] * gsk[0] + gsk[1] * gsk[1] + gsk[2] * gsk[2];
+  const T div = dudx + dvdy + dwdz;
+  T prod = mut * (2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + sq(dudy + dvdx) + sq(dudz + dwdx) + sq(dvdz + dwdy) -
+                  c23 * div * div) - c23 * rho * kk * div;
+  const T re_t = rho * kk * kk / ee / mu;
+  const T fe1 = 1.0 - exp(-sq(re_t / 40.0));
+  const T fe2 = 1.0 - 2.0 / 9.0 * exp(-sq(re_t / 6.0));
+  prod = fmin(prod, 30.0 * rho * ee);
+  const T ki = 1.0 / kk, oi = 1.0 / ee;
+  r[0] = (prod - rho * ee - 2.0 * mu * kkyy) * vol;
+  r[1] = (1.5 * fe1 * prod * ee - 1.9 * fe2 * rho * ee * ee + 2.9556 * mu * ee * kkyy) * ki * vol;
+  const T dpdk = 2.0 * prod * ki + c23 * rho * div;
+  const T dpdo = -((prod + c23 * rho * kk * div) * oi);
+  itt[0] = dpdk;
+  itt[1] = dpdo - rho;
+  itt[2] = (1.9 * fe2 * rho * ee * ee - 2.9556 * mu * ee * kkyy) * (ki * ki);
+  itt[3] = (1.5 * fe1 * dpdo * ee + 1.5 * fe1 * prod - 3.8 * fe2 * rho * ee + 2.9556 * mu * kkyy) * ki;
+  const T tr = itt[0] + itt[3], de = itt[0] * itt[3] - itt[1] * itt[2];
+  const T sd = sqrt(fmax(0.25 * tr * tr - de, T(0.0)));
+  const T l1 = copysign(T(1.0), 0.5 * tr + sd), l2 = copysign(T(1.0), 0.5 * tr - sd);
+  const T f1 = (1.0 - 0.5 * (1.0 - l1)) - 0.5 * (1.0 - l1), f2 = (1.0 - 0.5 * (1.0 - l2)) - 0.5 * (1.0 - l2);
+  itt[0] = itt[0] * f1; itt[1] = itt[1] * f1; itt[2] = itt[2] * f2; itt[3] = itt[3] * f2;
+}
+
+// k-epsilon eddy viscosity with its low-Re damping (t_eddy_ke kepsilon,
+// src/eddy_module.f90: re_t, re_e from the wall distance y)
+__device__ __forceinline__ double ke_eddy(double rho, double kk, double ee, double mu, double y) {
+  const double re_t = rho * kk * kk / ee / mu;
+  const double re_e = rho * ::pow(mu / rho * ee, 0.25) * y / mu;
+  const double f_mu = (1.0 + 3.0 / ::pow(re_t, 3.0 / 4.0)) * (1.0 + 80.0 * ::exp(-re_e)) *
+                      sq(1.0 - ::exp(-re_e / 43.0 - re_e * re_e / 330.0));
+  return 0.09 * rho * kk * kk / ee * f_mu;
+}
+
 // ------------------------------------------------------------------ viscous flux
 // Face viscous flux (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
 // from the face gradients g[x|y|z][q] of (u, v, w, T, k, omega) and their face averages
@@ -928,7 +973,7 @@ __device__ __forceinline__ SstOut<T> sst_source(const T (*gr)[3], T kk, T oo, T 
 template <class T>
 __device__ __forceinline__ void vsflux_core(const Par& c, const double* nx, const T* gx, const T* gy, const T* gz,
                                             const T* cc, T vis, T con, T emut, T tcon, T rho, double ydns, T* fv) {
-  const bool turb = (c.iturb == 0);
+  const bool turb = (c.iturb >= -1);
   const double c23 = 2.0 / 3.0;
   T mu = turb ? (vis + emut) : vis;
   T div = gx[0] + gy[1] + gz[2];
@@ -944,7 +989,11 @@ __device__ __forceinline__ void vsflux_core(const Par& c, const double* nx, cons
           nx[2] * (uc * txz + vc * tyz + wc * tzz + kc * gz[3]);
   fv[5] = T(0.0);
   fv[6] = T(0.0);
-  if (turb) {
+  if (turb && c.iturb == -1) {
+    // k-epsilon: F1 = 0 with sigma_k = 1, sigma_eps = 1.3 (src/vsflux_module.f90:69-75,427-435)
+    fv[7] = (vis + emut * 1.0) * (gx[4] * nx[0] + gy[4] * nx[1] + gz[4] * nx[2]);
+    fv[8] = (vis + emut * (1.0 / 1.3)) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
+  } else if (turb) {
     T pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
     T kf = cc[4], of = cc[5];
     T cdkw = fmax(1.712 * rho / of * pkw, T(1.0e-10));

@@ -420,6 +420,7 @@ struct Bc {
 
 int wall_kind(const Par& c) {
   if (c.iturb == 0) return G_WALL_KW;
+  if (c.iturb == -1) return G_WALL_KE;
   if (c.iturb == -2) return G_WALL_VISCOUS;
   return G_SYMMETRY;  // bcwallinviscid is the symmetry reflection
 }
@@ -459,7 +460,10 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
         case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
         // the counter-rotating family without rotation: the laminar and inviscid variants
         // are the plain wall's and symmetry's formulas, the SST one differs
-        case CFD3D_BC_WALL_COUNTERROTATING: bi.kind = (c.iturb == 0) ? G_CRWALL_KW : wall_kind(c); break;
+        case CFD3D_BC_WALL_COUNTERROTATING:
+          if (c.iturb == -1) { E.err = "counter-rotating walls under k-epsilon are not built"; return false; }
+          bi.kind = (c.iturb == 0) ? G_CRWALL_KW : wall_kind(c);
+          break;
         case CFD3D_BC_WALL_HEATFLUX: {
           // the HeatFlux family (src/bc_module.f90:233-249): the SST variant.  The laminar
           // one reads the wall distance grd(5), which a laminar run does not have (its grd

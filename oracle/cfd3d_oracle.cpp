@@ -55,7 +55,7 @@ enum Face { F_IMIN, F_IMAX, F_JMIN, F_JMAX, F_KMIN, F_KMAX, F_KMIN_CAP, F_KMAX_C
 
 enum BcKind {
   K_WALL_INVISCID, K_WALL_VISCOUS, K_WALL_KW, K_FARFIELD, K_EXTRAP, K_SYMMETRY, K_NOOP,
-  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED, K_HFWALL_KW,
+  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED, K_HFWALL_KW, K_WALL_KE,
   K_EDGE_WALLWALL, K_EDGE_WALLWALL_KW, K_EDGE_NOWALL, K_CORNER_WALLWALL, K_CORNER_WALLWALL_KW, K_CORNER_NOWALL
 };
 
@@ -129,11 +129,11 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
   if (c.timemethod < 1 || c.timemethod > 3) { err = "timemethod must be 1 (Euler), 2 (RK3) or 3 (LU-SGS)"; return false; }
   if (c.iturb == -3) { c.npv = 7; c.ntv = 0; }
   else if (c.iturb == -2) { c.npv = 7; c.ntv = 2; }
-  else if (c.iturb == 0) { c.npv = 9; c.ntv = 3; }
-  else { err = "iturb must be -3, -2 or 0"; return false; }
+  else if (c.iturb == 0 || c.iturb == -1) { c.npv = 9; c.ntv = 3; }
+  else { err = "iturb must be -3, -2, -1 or 0"; return false; }
   if (c.iturb == 0 && (c.ides < 0 || c.ides > 4)) { err = "ides must be 0..4"; return false; }
   c.nqq = c.nsteady >= 1 ? 2 : 0;
-  c.ngrd = (c.iturb == 0) ? 5 : 4;
+  c.ngrd = (c.iturb >= -1) ? 5 : 4;
   if (c.fluid != 1 && c.fluid != 2) { err = "fluid must be 1 or 2"; return false; }
   if (c.ngas != 1) { err = "ngas must be 1"; return false; }
   if (c.nscheme < 1 || c.nscheme > 4 || c.nmuscl < 0 || c.nmuscl > 2 || c.nlim < 0 || c.nlim > 10) {
@@ -147,6 +147,13 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
   deteos(c.eos, c.with_prop, c.pref, c.tref, c.y1ref, c.y2ref, dv, tv);
   c.rhoref = dv[0];
   c.visref = tv[0];
+  if (c.iturb == -1) {   /* config%setref for k-epsilon (src/config_module.f90:191-194) */
+    c.kref = 1.5 * sq(0.0001 * c.uref);
+    c.emutref = std::pow(10.0, -5) * tv[0];
+    c.oref = 0.09 * c.rhoref * sq(c.kref) / c.emutref;
+    if (in->kinf > 0) c.kref = in->kinf;
+    if (in->oinf > 0) c.oref = in->oinf;
+  }
   if (c.iturb == 0) {
     c.oref = 10.0 * c.uref / c.l_domain;
     c.emutref = std::pow(10.0, -5) * tv[0];
@@ -377,6 +384,7 @@ static void bc_reference_state(const Cfg& c, BcInfo& bi) {
 
 static BcKind wall_kind(const Cfg& c) {
   if (c.iturb == 0) return K_WALL_KW;
+  if (c.iturb == -1) return K_WALL_KE;   /* bcwallviscouske :2324-2366 */
   if (c.iturb == -2) return K_WALL_VISCOUS;
   return K_WALL_INVISCID;
 }
@@ -408,7 +416,10 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
     switch (p.type) {
       case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
       /* the CounterRotating family (:3516-3810) with grid velocity 0: the SST variant differs */
-      case CFD3D_BC_WALL_COUNTERROTATING: bi.kind = (c.iturb == 0) ? K_CRWALL_KW : wall_kind(c); break;
+      case CFD3D_BC_WALL_COUNTERROTATING:
+        if (c.iturb == -1) { err = "counter-rotating walls under k-epsilon are not built"; return false; }
+        bi.kind = (c.iturb == 0) ? K_CRWALL_KW : wall_kind(c);
+        break;
       case CFD3D_BC_WALL_HEATFLUX:   /* the HeatFlux family: bcheatfluxwallviscouskw :4184-4273 */
         if (c.iturb != 0) { err = "heat-flux walls need the SST model (iturb = 0)"; return false; }
         if (p.ndata < 1 || !p.tdata || !p.heatflux) { err = "heat-flux wall without its history"; return false; }
@@ -781,6 +792,12 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
             put_cell(c, B, i, j, k, pv, dv, tv);
             break;
           }
+          case K_WALL_KE:
+            get_cell(c, B, mi, mj, mk, pv, dv, tv);
+            pv[1] = -pv[1]; pv[2] = -pv[2]; pv[3] = -pv[3]; pv[7] = -pv[7]; pv[8] = -pv[8];
+            tv[2] = -tv[2];
+            put_cell(c, B, i, j, k, pv, dv, tv);
+            break;
           case K_CRWALL_KW:
             /* omega: the mirror's (the routine computes the wall value and discards it) */
             get_cell(c, B, mi, mj, mk, pv, dv, tv);
@@ -1151,6 +1168,16 @@ static void calrhs_block(const Cfg& c, Block& B, double time) {
           B.res(8, i, j, k) = B.res(8, i, j, k) + to.source[1];
           for (int q = 0; q < 4; ++q) B.itt(q, i, j, k) = to.itt[q];
         }
+        if (c.iturb == -1) {
+          double tv[3];
+          for (int m = 0; m < 3; ++m) tv[m] = B.tv(m, i, j, k);
+          TurbOut to = kepsilon_source(x7, B.cx.at(i - 1, j, k), B.cx.at(i, j, k), B.ex.at(i, j - 1, k), B.ex.at(i, j, k),
+                                       B.tx.at(i, j, k - 1), B.tx.at(i, j, k), grd, dv, tv);
+          B.omega_cut(0, i, j, k) = to.omega_cut;
+          B.res(7, i, j, k) = B.res(7, i, j, k) + to.source[0];
+          B.res(8, i, j, k) = B.res(8, i, j, k) + to.source[1];
+          for (int q = 0; q < 4; ++q) B.itt(q, i, j, k) = to.itt[q];
+        }
         if (c.nsteady >= 1) {
           double us[NPV_MAX];
           const double* qq = B.qq.at(i, j, k);
@@ -1188,7 +1215,7 @@ static void lhs_in(const Cfg& c, Block& B, int i, int j, int k, LhsIn& L, double
   L.tv = tvbuf;
   L.dt = B.dt(0, i, j, k);
   L.c = (c.ncav > 0) ? B.icav.at(i, j, k) : zero4;
-  L.t = (c.iturb == 0) ? B.itt.at(i, j, k) : zero4;
+  L.t = (c.iturb >= -1) ? B.itt.at(i, j, k) : zero4;
 }
 
 static void jac_apply(const Cfg& c, Block& B, const double* nx, int i, int j, int k, int sign, const double* dq,
@@ -1204,6 +1231,15 @@ static void jac_apply(const Cfg& c, Block& B, const double* nx, int i, int j, in
 /* eddy%caleddy over the block after an update (src/update_module.f90:701-732, :300-330) */
 static void eddy_block(const Cfg& c, Block& B) {
   const int im = B.imax, jm = B.jmax, km = B.kmax;
+  if (c.iturb == -1) {
+    for (int k = 2; k <= km; ++k)
+      for (int j = 2; j <= jm; ++j)
+        for (int i = 2; i <= im; ++i) {
+          double tv[3];
+          for (int m = 0; m < 3; ++m) tv[m] = B.tv(m, i, j, k);
+          B.tv(2, i, j, k) = kepsilon_eddy(B.pv.at(i, j, k), B.dv.at(i, j, k), tv, B.grd.at(i, j, k));
+        }
+  }
   if (c.iturb == 0) {
     for (int k = 2; k <= km; ++k)
       for (int j = 2; j <= jm; ++j)
@@ -1261,7 +1297,7 @@ static void lusgs_block(const Cfg& c, Block& B) {
         p[0] = dmax(-c.pref + 1.0e1, p[0]);
         p[5] = dmin(1.0, dmax(0.0, p[5]));
         p[6] = dmin(1.0, dmax(0.0, p[6]));
-        if (c.iturb == 0) {
+        if (c.iturb >= -1) {
           p[7] = dmax(p[7], 1.0e-16);
           p[8] = dmax3(p[8], 1.0e-16, B.omega_cut(0, i, j, k));
         }
@@ -1300,7 +1336,7 @@ static void explicit_block(const Cfg& c, Block& B, int m) {
         p[0] = dmax(-c.pref + 1.0e1, p[0]);
         p[5] = dmin(1.0, dmax(0.0, p[5]));
         p[6] = dmin(1.0, dmax(0.0, p[6]));
-        if (c.iturb == 0) {
+        if (c.iturb >= -1) {
           p[7] = dmax(p[7], 1.0e-16);
           p[8] = dmax3(p[8], 1.0e-16, B.omega_cut(0, i, j, k));
         }
@@ -1415,13 +1451,13 @@ int orc_initialize(void* h, int b, const double* pv_in) {
           pv[2] = c.uref * std::cos(c.aos) * std::sin(c.aoa);
           pv[3] = c.uref * std::sin(c.aos);
           pv[4] = c.tref; pv[5] = c.y1ref; pv[6] = c.y2ref;
-          if (c.iturb == 0) { pv[7] = c.kref; pv[8] = c.oref; }
+          if (c.iturb >= -1) { pv[7] = c.kref; pv[8] = c.oref; }
         }
         ++q;
         double dv[NDV], tv[3] = {0, 0, 0};
         deteos(c.eos, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv);
         std::memcpy(B.dv.at(i, j, k), dv, sizeof(dv));
-        if (c.iturb == 0) tv[2] = c.emutref;
+        if (c.iturb >= -1) tv[2] = c.emutref;
         for (int m = 0; m < c.ntv; ++m) B.tv(m, i, j, k) = tv[m];
         if (c.nsteady >= 1) {
           double qq[NPV_MAX];

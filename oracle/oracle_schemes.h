@@ -488,8 +488,11 @@ static inline void vsflux(const Cfg& c, const VsIn& s, double* fx) {
     double arg2 = dmax(term1, term2);
     double arg1 = dmin(arg2, term3);
     double bigf = std::tanh(sq(sq(arg1)));
+    /* tdk1, tdk2, tdo1, tdo2 of vsflux%construct (:62-90): SST 0.85, 1, 0.5, 0.856; k-epsilon
+       0, 1, 0, 1/1.3 with calbigf = 0 (:427-435) */
     double tdk = bigf * 0.85 + (1.0 - bigf) * 1.0;
     double tdo = bigf * 0.5 + (1.0 - bigf) * 0.856;
+    if (c.iturb == -1) { bigf = 0.0; tdk = bigf * 0.0 + (1.0 - bigf) * 1.0; tdo = bigf * 0.0 + (1.0 - bigf) * (1.0 / 1.3); }
     fx[7] = (vis + emut * tdk) * (dkdx * n[0] + dkdy * n[1] + dkdz * n[2]);
     fx[8] = (vis + emut * tdo) * (dodx * n[0] + dody * n[1] + dodz * n[2]);
   }
@@ -762,6 +765,64 @@ static inline TurbOut kwsst_source(const double (*x)[NPV_MAX], const double* cx1
   r.itt[0] *= f1; r.itt[1] *= f1;
   r.itt[2] *= f2; r.itt[3] *= f2;
   return r;
+}
+
+/* t_kepsilon kepsilon (src/turbsource_module.f90:170-267) */
+static inline TurbOut kepsilon_source(const double (*x)[NPV_MAX], const double* cx1, const double* cx2,
+                                      const double* ex1, const double* ex2, const double* tx1, const double* tx2,
+                                      const double* grd, const double* dv, const double* tv) {
+  TurbOut r;
+  const double c23 = 2.0 / 3.0, phi = 1.0;
+  double gu[3], gv[3], gw[3], gk[3];
+  cell_grad(x, cx1, cx2, ex1, ex2, tx1, tx2, grd[0], 1, gu);
+  cell_grad(x, cx1, cx2, ex1, ex2, tx1, tx2, grd[0], 2, gv);
+  cell_grad(x, cx1, cx2, ex1, ex2, tx1, tx2, grd[0], 3, gw);
+  /* the gradient of sqrt(k) from the square roots of the face averages */
+  const double k1 = 0.5 * (x[0][7] + x[1][7]), k2 = 0.5 * (x[2][7] + x[1][7]), k3 = 0.5 * (x[3][7] + x[1][7]);
+  const double k4 = 0.5 * (x[4][7] + x[1][7]), k5 = 0.5 * (x[5][7] + x[1][7]), k6 = 0.5 * (x[6][7] + x[1][7]);
+  const double vol = 1.0 / grd[0];
+  for (int d = 0; d < 3; ++d)
+    gk[d] = (std::sqrt(k2) * cx2[d] + std::sqrt(k4) * ex2[d] + std::sqrt(k6) * tx2[d] - std::sqrt(k1) * cx1[d] -
+             std::sqrt(k3) * ex1[d] - std::sqrt(k5) * tx1[d]) * vol;
+  const double dudx = gu[0], dudy = gu[1], dudz = gu[2], dvdx = gv[0], dvdy = gv[1], dvdz = gv[2];
+  const double dwdx = gw[0], dwdy = gw[1], dwdz = gw[2];
+  const double k = x[1][7], e = x[1][8];
+  const double kkyy = sq(gk[0]) + sq(gk[1]) + sq(gk[2]);
+  double prod = tv[2] * (2.0 * (sq(dudx) + sq(dvdy) + sq(dwdz)) + sq(dudy + dvdx) + sq(dudz + dwdx) + sq(dvdz + dwdy) -
+                         c23 * sq(dudx + dvdy + dwdz)) - c23 * dv[0] * k * (dudx + dvdy + dwdz);
+  const double re_t = dv[0] * sq(k) / e / tv[0];
+  const double fe1 = 1.0 - std::exp(-sq(re_t / 40.0));
+  const double fe2 = 1.0 - 2.0 / 9.0 * std::exp(-sq(re_t / 6.0));
+  prod = dmin(prod, 30.0 * dv[0] * e);
+  const double ki = 1.0 / k, oi = 1.0 / e;
+  r.omega_cut = 0.0;
+  r.source[0] = (prod - dv[0] * e - 2.0 * tv[0] * kkyy) * grd[0];
+  r.source[1] = (1.5 * fe1 * prod * e - 1.9 * fe2 * dv[0] * sq(e) + 2.9556 * tv[0] * e * kkyy) * ki * grd[0];
+  const double dpdk = 2.0 * prod * ki + c23 * dv[0] * (dudx + dvdy + dwdz);
+  const double dpdo = -((prod + c23 * dv[0] * k * (dudx + dvdy + dwdz)) * oi);
+  r.itt[0] = dpdk;
+  r.itt[1] = dpdo - dv[0];
+  r.itt[2] = (1.9 * fe2 * dv[0] * sq(e) - 2.9556 * tv[0] * e * kkyy) * sq(ki);
+  r.itt[3] = (1.5 * fe1 * dpdo * e + 1.5 * fe1 * prod - 3.8 * fe2 * dv[0] * e + 2.9556 * tv[0] * kkyy) * ki;
+  const double t = r.itt[0] + r.itt[3], dd = r.itt[0] * r.itt[3] - r.itt[1] * r.itt[2];
+  double lam1 = 0.5 * t + std::sqrt(dmax(0.25 * sq(t) - dd, 0.0));
+  double lam2 = 0.5 * t - std::sqrt(dmax(0.25 * sq(t) - dd, 0.0));
+  lam1 = dsign(1.0, lam1);
+  lam2 = dsign(1.0, lam2);
+  const double f1 = phi * (1.0 - 0.5 * (1.0 - lam1)) - 0.5 * (1.0 - lam1);
+  const double f2 = phi * (1.0 - 0.5 * (1.0 - lam2)) - 0.5 * (1.0 - lam2);
+  r.itt[0] *= f1; r.itt[1] *= f1;
+  r.itt[2] *= f2; r.itt[3] *= f2;
+  return r;
+}
+
+/* t_eddy_ke kepsilon (src/eddy_module.f90) */
+static inline double kepsilon_eddy(const double* pv, const double* dv, const double* tv, const double* grd) {
+  const double re_t = dv[0] * sq(pv[7]) / pv[8] / tv[0];
+  const double re_e = dv[0] * std::pow(tv[0] / dv[0] * pv[8], 0.25) * grd[4] / tv[0];
+  const double f_mu = (1.0 + 3.0 / std::pow(re_t, 3.0 / 4.0)) * (1.0 + 80.0 * std::exp(-re_e)) *
+                      sq(1.0 - std::exp(-re_e / 43.0 - sq(re_e) / 330.0));
+  return 0.09 * dv[0] * sq(pv[7]) / pv[8] * f_mu;
 }
 
 /* eddy%caleddy, SST (src/eddy_module.f90:135-187) */
