@@ -67,9 +67,9 @@ def rhs_bytes(cfg, mixed):
 
 
 # DRAM traffic of k_rhs per cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum)
-# on the large case at 1/2 resolution, mixed form: 2.120 GB + 3.296 GB over 1769472 cells
+# on the large case at 1/2 resolution, mixed form: 2.300 GB + 3.389 GB over 1769472 cells
 # (profiles/k_rhs_large_half_mixed.md); it grows with the cell count
-RHS_TRAFFIC_PER_CELL = (2.120215e9 + 3.295658e9) / 1769472
+RHS_TRAFFIC_PER_CELL = (2.300200e9 + 3.388917e9) / 1769472
 
 
 def measured_peaks():
