@@ -17,6 +17,7 @@ FP64, MIXED = 0, 1
 BC_WALL, BC_SYMMETRY, BC_FARFIELD, BC_EXTRAPOLATE, BC_DEGENERATE, BC_INFLOW = range(1, 7)
 BC_INFLOW_SUBSONIC, BC_OUTFLOW_SUBSONIC, BC_INFLOW_SUPERSONIC, BC_OUTFLOW = range(7, 11)
 BC_WALL_COUNTERROTATING, BC_WALL_HEATFLUX, BC_MASSFLOWRATE_IN, BC_SHIFTED_PERIODIC = 11, 12, 13, 14
+BC_TOTALPRESSURE_IN = 15
 BC_NAMES = {
     "BCWall": BC_WALL,
     "BCSymmetryPlane": BC_SYMMETRY,
@@ -32,6 +33,7 @@ BC_NAMES = {
     "BCOutflow": BC_OUTFLOW,
     "BCMassflowrateIn": BC_MASSFLOWRATE_IN,
     "BCShiftedPeriodic": BC_SHIFTED_PERIODIC,
+    "BCTotalPressureIn": BC_TOTALPRESSURE_IN,
 }
 
 

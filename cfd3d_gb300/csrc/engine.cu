@@ -199,6 +199,177 @@ __global__ void k_timestep(DevPtr d, Par c) {
 }
 
 // ------------------------------------------------------------------ boundary program
+// ---- total-pressure inlet (bctotalpressurein, src/bc_module.f90:3299-3514) ------------
+// newt (:4305-4387) for x = (p, T): f1 = p_t - p (T_t / T)^(g / (g - 1)),
+// f2 = h_t - (h(p, T) + |u|^2 / 2) (funcv :4408-4422), with fdjac's forward differences
+// (:4424-4447), the backtracking line search lnsrch (:4449-4526) and ludcmp / lubksb
+// (:4528-4622) on the 2 x 2 system -- as written, including that newt evaluates its fvec
+// once (lnsrch evaluates into a local copy), so its tests and Jacobian reuse that first one.
+struct TpProblem { double pt, tt, ht, y1, y2, uu, gam; int fluid; };
+__device__ void tp_funcv(const TpProblem& P, const double* x, double* f) {
+  double dv[NDV];
+  deteos_simple<false>(P.fluid, x[0], x[1], P.y1, P.y2, dv, nullptr);
+  f[0] = P.pt - x[0] * pow(P.tt / x[1], P.gam / (P.gam - 1.0));
+  f[1] = P.ht - (dv[1] + 0.5 * P.uu);
+}
+__device__ double tp_fmin(const TpProblem& P, const double* x, double* f) {
+  tp_funcv(P, x, f);
+  return 0.5 * (f[0] * f[0] + f[1] * f[1]);
+}
+__device__ void tp_ludcmp(double (*a)[2], int* indx) {
+  double vv[2];
+  for (int i = 0; i < 2; ++i) vv[i] = 1.0 / fmax(fabs(a[i][0]), fabs(a[i][1]));
+  for (int j = 0; j < 2; ++j) {
+    for (int i = 0; i < j; ++i) {
+      double sum = a[i][j];
+      for (int k = 0; k < i; ++k) sum -= a[i][k] * a[k][j];
+      a[i][j] = sum;
+    }
+    double aamax = 0.0;
+    int imax = j;
+    for (int i = j; i < 2; ++i) {
+      double sum = a[i][j];
+      for (int k = 0; k < j; ++k) sum -= a[i][k] * a[k][j];
+      a[i][j] = sum;
+      const double dum = vv[i] * fabs(sum);
+      if (dum >= aamax) { imax = i; aamax = dum; }
+    }
+    if (j != imax) {
+      for (int k = 0; k < 2; ++k) { const double dum = a[imax][k]; a[imax][k] = a[j][k]; a[j][k] = dum; }
+      vv[imax] = vv[j];
+    }
+    indx[j] = imax;
+    if (a[j][j] == 0.0) a[j][j] = 1.0e-20;
+    if (j != 1) {
+      const double dum = 1.0 / a[j][j];
+      for (int i = j + 1; i < 2; ++i) a[i][j] *= dum;
+    }
+  }
+}
+__device__ void tp_lubksb(const double (*a)[2], const int* indx, double* b) {
+  int ii = -1;
+  for (int i = 0; i < 2; ++i) {
+    const int ll = indx[i];
+    double sum = b[ll];
+    b[ll] = b[i];
+    if (ii >= 0) for (int j = ii; j < i; ++j) sum -= a[i][j] * b[j];
+    else if (sum != 0.0) ii = i;
+    b[i] = sum;
+  }
+  for (int i = 1; i >= 0; --i) {
+    double sum = b[i];
+    for (int j = i + 1; j < 2; ++j) sum -= a[i][j] * b[j];
+    b[i] = sum / a[i][i];
+  }
+}
+__device__ void tp_newt(const TpProblem& P, double* x) {
+  const double tolf = 1.0e-4, tolmin = 1.0e-6, tolx = 1.0e-7, stpmx = 100.0, alf = 1.0e-4;
+  double fvec[2], fjac[2][2], g[2], p[2], xold[2], ftmp[2];
+  double f = tp_fmin(P, x, fvec);
+  if (fmax(fabs(fvec[0]), fabs(fvec[1])) < 0.01 * tolf) return;
+  const double stpmax = stpmx * fmax(sqrt(x[0] * x[0] + x[1] * x[1]), 2.0);
+  for (int its = 0; its < 200; ++its) {
+    for (int j = 0; j < 2; ++j) {   // fdjac
+      double tmp[2] = {x[0], x[1]};
+      double h = 1.0e-4 * fabs(tmp[j]);
+      if (h == 0.0) h = 1.0e-4;
+      tmp[j] = tmp[j] + h;
+      h = tmp[j] - x[j];
+      tp_funcv(P, tmp, ftmp);
+      for (int i = 0; i < 2; ++i) fjac[i][j] = (ftmp[i] - fvec[i]) / h;
+    }
+    for (int i = 0; i < 2; ++i) g[i] = fjac[0][i] * fvec[0] + fjac[1][i] * fvec[1];
+    xold[0] = x[0]; xold[1] = x[1];
+    const double fold = f;
+    p[0] = -fvec[0]; p[1] = -fvec[1];
+    int indx[2];
+    tp_ludcmp(fjac, indx);
+    tp_lubksb(fjac, indx, p);
+    // lnsrch
+    bool check = false;
+    {
+      const double sum = sqrt(p[0] * p[0] + p[1] * p[1]);
+      if (sum > stpmax) { p[0] *= stpmax / sum; p[1] *= stpmax / sum; }
+      const double slope = g[0] * p[0] + g[1] * p[1];
+      const double test = fmax(fabs(p[0]) / fmax(fabs(xold[0]), 1.0), fabs(p[1]) / fmax(fabs(xold[1]), 1.0));
+      const double alamin = tolx / test;
+      double alam = 1.0, alam2 = 0.0, f2 = 0.0, fold2 = 0.0, tmplam = 0.0;
+      for (int ls = 0; ls < 1000; ++ls) {   // (bounded: alam falls by 10x per pass at least)
+        x[0] = xold[0] + alam * p[0];
+        x[1] = xold[1] + alam * p[1];
+        double fl[2];
+        f = tp_fmin(P, x, fl);
+        if (alam < alamin) { x[0] = xold[0]; x[1] = xold[1]; check = true; break; }
+        if (f <= fold + alf * alam * slope) break;
+        if (alam == 1.0) {
+          tmplam = -slope / (2.0 * (f - fold - slope));
+        } else {
+          const double rhs1 = f - fold - alam * slope, rhs2 = f2 - fold2 - alam2 * slope;
+          const double a = (rhs1 / (alam * alam) - rhs2 / (alam2 * alam2)) / (alam - alam2);
+          const double b = (-alam2 * rhs1 / (alam * alam) + alam * rhs2 / (alam2 * alam2)) / (alam - alam2);
+          if (a == 0.0) tmplam = -slope / (2.0 * b);
+          else {
+            const double disc = b * b - 3.0 * a * slope;
+            if (disc < 0.0) tmplam = 0.5 * alam;
+            else if (b <= 0.0) tmplam = (-b + sqrt(disc)) / (3.0 * a);
+            else tmplam = -slope / (b + sqrt(disc));
+          }
+          if (tmplam > 0.5 * alam) tmplam = 0.5 * alam;
+        }
+        alam2 = alam;
+        f2 = f;
+        fold2 = fold;
+        alam = fmax(tmplam, 0.1 * alam);
+      }
+    }
+    if (fmax(fabs(fvec[0]), fabs(fvec[1])) < tolf) return;
+    if (check) return;   // (the reference's test here only sets its check flag)
+    const double tx = fmax(fabs(x[0] - xold[0]) / fmax(fabs(x[0]), 1.0), fabs(x[1] - xold[1]) / fmax(fabs(x[1]), 1.0));
+    if (tx < tolx) return;
+  }
+}
+
+// one CTA per total-pressure patch: the area-weighted boundary averages (the patch's
+// reduction), then the Newton solve by thread 0
+__global__ void __launch_bounds__(128) k_totalp(DevPtr d, Par c) {
+  const int pt = blockIdx.x;
+  const long long n = d.ncell;
+  __shared__ double sh[6][128];
+  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int e = d.tp_off[pt] + threadIdx.x; e < d.tp_off[pt + 1]; e += blockDim.x) {
+    const int* E = d.tp_ent + 4 * e;
+    double nx[3];
+    face_vec(d, E[2], E[1], nx);
+    const double dl = sqrt(nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
+    const long long b = E[0];
+    acc[0] += d.pv[b] * dl;
+    for (int q = 0; q < 3; ++q) acc[1 + q] += d.pv[(1 + q) * n + b] * dl;
+    acc[4] += d.pv[4 * n + b] * dl;
+    acc[5] += dl;
+  }
+  for (int q = 0; q < 6; ++q) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = 64; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < 6; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double area = sh[5][0];
+  const double pa = sh[0][0] / area, ua = sh[1][0] / area, va = sh[2][0] / area, wa = sh[3][0] / area;
+  const double ta = sh[4][0] / area;
+  TpProblem P;
+  P.pt = c.tp_pt; P.tt = c.tp_tt; P.ht = c.tp_ht; P.y1 = c.y1ref; P.y2 = c.y2ref;
+  P.uu = ua * ua + va * va + wa * wa;
+  P.gam = (1.0 - c.y2ref) * 1.33 + c.y2ref * 1.4;   // eos%getgamma_f (water), getgamma_g (ideal gas)
+  P.fluid = c.fluid;
+  double x[2] = {pa + c.pref, ta};
+  tp_newt(P, x);
+  d.tp_x[3 * pt] = x[0];
+  d.tp_x[3 * pt + 1] = x[1];
+  d.tp_x[3 * pt + 2] = P.uu;
+}
+
 __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int nops) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nops) return;
@@ -267,6 +438,30 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       x.tv[2] = -x.tv[2];
       store_cell(d, c, op.dst, x);
       return;
+    case G_TOTALP: {
+      // bctotalpressurein's ghost (:3398-3505): p and T from the patch's Newton solve, the
+      // normal inflow speed |u_avg|, y1, k, omega from the free stream -- and y2 reflected
+      // twice, so the mirror's
+      load_cell(d, c, op.src, x);
+      const double* X = d.tp_x + 3 * op.pad;
+      double nx[3];
+      face_vec(d, op.fplane, op.fidx, nx);
+      for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;
+      const double dl = 1.0 / sqrt(nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
+      const double su = sqrt(X[2]);
+      const double bp[NPVM] = {c.pref, 0.0, 0.0, 0.0, c.tp_tt, c.y1ref, c.y2ref, c.kref, c.oref};
+      double* pv = x.pv;
+      pv[0] = 2.0 * (X[0] - c.pref) - pv[0];
+      for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (-su * nx[q3] * dl - 0.0) - pv[1 + q3];
+      pv[4] = 2.0 * X[1] - pv[4];
+      for (int v = 5; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
+      pv[6] = 2.0 * bp[6] - pv[6];
+      pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
+      pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
+      deteos(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      store_cell(d, c, op.dst, x);
+      return;
+    }
     case G_CRWALL_KW:
       // bccounterrotatingwallviscouskw (src/bc_module.f90:3654-3731) with the grid velocity
       // omega x r = 0 (no rotation): u, v, w, k and mu_t reflected; omega is the mirror's,
@@ -1225,6 +1420,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
     ++n;
   }
   stage(1);
+  if (d.ntp) { k_totalp<<<d.ntp, 128, 0, s>>>(d, c); ++n; }
   for (int p = 0; p < 3; ++p)
     if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
   stage(2);
@@ -1241,6 +1437,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
     const int nstage = (c.timemethod == 2) ? 3 : 1;
     for (int m = 1; m <= nstage; ++m) {
       if (m > 1) {
+        if (d.ntp) { k_totalp<<<d.ntp, 128, 0, s>>>(d, c); ++n; }
         for (int p = 0; p < 3; ++p)
           if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
         if (c.mixed) launch_face_flux_mixed(E, s);
@@ -1605,6 +1802,17 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
       if (cfg->kinf > 0) E.par.kref = cfg->kinf;
       if (cfg->oinf > 0) E.par.oref = cfg->oinf;
     }
+    {
+      // the total-pressure inlet's construct values (src/bc_module.f90:318-321): its totals
+      // and the enthalpy eos%deteos gives there
+      E.par.tp_pt = 51551.30907;
+      E.par.tp_tt = 300.0003719;
+      double hp2[4] = {E.par.tp_pt, E.par.tp_tt, cfg->y1ref, cfg->y2ref};
+      double dvt[NDV], tvt[2] = {0.0, 0.0};
+      rc = cfd3d_eos_eval(cfg->fluid, cfg->ngas, c.with_prop, 1, &hp2[0], &hp2[1], &hp2[2], &hp2[3], dvt, tvt);
+      if (rc != CFD3D_OK) { E.err = "total-pressure EOS failed"; return rc; }
+      E.par.tp_ht = dvt[1];
+    }
     // mixed form: free-stream flux tensor (gauge pressure) for the stored flux deviations
     E.par.href = dvr[1];
     const double* U = E.par.uref_vec;
@@ -1679,6 +1887,9 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_nbb);
   cudaFree(E.d_hft);
   cudaFree(E.d_grav);
+  cudaFree(E.d_tp_off);
+  cudaFree(E.d_tp_ent);
+  cudaFree(E.d_tp_x);
   cudaFree(E.d.rec);
   cudaFree(E.d.done);
   cudaFree(E.d.tickets);
@@ -2073,6 +2284,7 @@ int cfd3d_residual_vjp(cfd3d_handle* h, const double* cot, double* g_state, doub
   int rc = ensure_staging(h, (size_t)maxint * c.npv * 8);
   if (rc) return rc;
   if (E.par.iturb == -1) { E.err = "the adjoint does not cover the k-epsilon model"; return CFD3D_ERR_ARG; }
+  if (E.d.ntp) { E.err = "the adjoint does not cover total-pressure inlets"; return CFD3D_ERR_ARG; }
   if ((rc = adjoint_buffers(E))) return rc;
   // the cotangent, block after block, into the padded interior
   size_t off = 0;

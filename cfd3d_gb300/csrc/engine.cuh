@@ -33,7 +33,7 @@ enum GhostKind : int {
   G_COPY = 0, G_EXTRAP, G_WALL_VISCOUS, G_WALL_KW, G_SYMMETRY, G_FARFIELD,
   G_WALLWALL, G_WALLWALL_KW4, G_WALLWALL_KW8, G_NOWALL3, G_NOWALL7,
   G_INFLOW_SUB, G_OUTFLOW_SUB, G_INFLOW_SUP,  // the farfield treatment with a forced branch
-  G_CRWALL_KW, G_MASSFLOW_IN, G_HFWALL_KW, G_WALL_KE
+  G_CRWALL_KW, G_MASSFLOW_IN, G_HFWALL_KW, G_WALL_KE, G_TOTALP
 };
 
 // the farfield_pv branch of a characteristic ghost kind
@@ -80,6 +80,12 @@ struct DevPtr {
   Scalars* sc;
   const double* hft;   // heat-flux histories: per table n, t[n], q[n] (GhostOp.pad is its offset)
   const double* grav;  // gravity history: n, t[n], a[3 n] (a constant acceleration is one row)
+  // total-pressure inlets: per patch [tp_off[p], tp_off[p+1]) face entries (boundary cell,
+  // face-vector cell, plane, sign) and the solved (p, T, |u|^2) in tp_x[3 p..]
+  int ntp;
+  const int* tp_off;
+  const int* tp_ent;     // 4 ints per entry
+  double* tp_x;
   double* partial;   // per-CTA partial residual sums [gridsize][npv+2]
   // mixed form only: FP32 gauge shadow of pv and FP32 face fluxes (fi / fv unused)
   float *pvf, *fi32, *fv32;
@@ -127,6 +133,9 @@ struct Engine {
   int nops[3] = {0, 0, 0};
   double* d_hft = nullptr;   // heat-flux histories (d.hft), null without heat-flux walls
   double* d_grav = nullptr;  // gravity history (d.grav), null without gravity
+  int* d_tp_off = nullptr;
+  int* d_tp_ent = nullptr;
+  double* d_tp_x = nullptr;
   // LU-SGS plane-major numbering (setup_planes): cells[t], pos[g], lower / upper neighbours
   int* d_planes = nullptr;
   int* d_pos = nullptr;

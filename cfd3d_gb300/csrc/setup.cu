@@ -416,6 +416,7 @@ struct Bc {
   bool farfield_sign = false;
   bool shifted = false;   // bcshiftedperiodic: copies from 16 cells along i and the face normal
   int hf_off = 0;         // heat-flux wall: offset of its history in the table
+  int tp_index = 0;       // total-pressure inlet: its patch number
 };
 
 int wall_kind(const Par& c) {
@@ -431,6 +432,7 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
   const Par& c = E.par;
   std::vector<GhostOp> ops[3];
   std::vector<double> hft;   // heat-flux histories
+  std::vector<std::vector<int>> tp_ent;   // total-pressure inlets: per patch 4 ints per face cell
   for (int b = 0; b < nblocks; ++b) {
     const cfd3d_block_desc& d = blocks[b];
     const BlockGeom& G = E.blk[b];
@@ -480,6 +482,11 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
           for (int m = 0; m < bp.ndata; ++m) hft.push_back(bp.heatflux[m]);
           break;
         }
+        case CFD3D_BC_TOTALPRESSURE_IN:
+          bi.kind = G_TOTALP; bi.farfield_sign = true;
+          bi.tp_index = (int)tp_ent.size();
+          tp_ent.emplace_back();
+          break;
         case CFD3D_BC_MASSFLOWRATE_IN: bi.kind = G_MASSFLOW_IN; break;
         case CFD3D_BC_SHIFTED_PERIODIC: bi.kind = G_COPY; bi.shifted = true; break;
         case CFD3D_BC_SYMMETRY: bi.kind = G_SYMMETRY; break;
@@ -537,9 +544,9 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
             op.bnd = op.src;
             for (int q = 0; q < 6; ++q) op.nb[q] = -1;
             op.fidx = op.src; op.fplane = GM_CX; op.fsign = 1.0f;
-            op.pad = bi.hf_off;
+            op.pad = (bi.kind == G_TOTALP) ? bi.tp_index : bi.hf_off;
             if (bi.kind == G_SYMMETRY || bi.kind == G_FARFIELD || bi.kind == G_WALL_KW || bi.kind == G_HFWALL_KW ||
-                ghost_ff_mode(bi.kind)) {
+                bi.kind == G_TOTALP || ghost_ff_mode(bi.kind)) {
               int ii = mi, jj = mj, kk = mk;
               float s = bi.farfield_sign ? -1.0f : 1.0f;
               switch (bi.face) {
@@ -552,6 +559,15 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
                 default: break;  // corner 'Kmin'/'Kmax': the boundary cell stays the mirror cell
               }
               op.bnd = gi(ii, jj, kk);
+              if (bi.kind == G_TOTALP) {
+                // the patch's reduction visits each boundary face once: the outermost layer
+                const int ax = (int)bi.face / 2;
+                const int idx[3] = {i, j, k};
+                if (idx[ax] == (((int)bi.face % 2 == 0) ? bi.s[ax] : bi.e[ax])) {
+                  std::vector<int>& te = tp_ent[bi.tp_index];
+                  te.push_back(op.bnd); te.push_back(op.fidx); te.push_back(op.fplane); te.push_back(0);
+                }
+              }
             }
             int q2 = 0;
             for (int q = 0; q < nnb; ++q) {
@@ -702,6 +718,20 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
     if (E.nops[p] == 0) continue;
     if (cudaMalloc(&E.d_ops[p], ops[p].size() * sizeof(GhostOp)) != cudaSuccess) { E.err = "cudaMalloc ghost ops"; return false; }
     cudaMemcpy(E.d_ops[p], ops[p].data(), ops[p].size() * sizeof(GhostOp), cudaMemcpyHostToDevice);
+  }
+  if (!tp_ent.empty()) {
+    std::vector<int> off(1, 0), ent;
+    for (const auto& te : tp_ent) { ent.insert(ent.end(), te.begin(), te.end()); off.push_back((int)(ent.size() / 4)); }
+    const size_t nt = tp_ent.size();
+    if (cudaMalloc(&E.d_tp_off, off.size() * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&E.d_tp_ent, std::max<size_t>(ent.size(), 1) * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&E.d_tp_x, 3 * nt * sizeof(double)) != cudaSuccess) {
+      E.err = "cudaMalloc total-pressure inlets"; return false;
+    }
+    cudaMemcpy(E.d_tp_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (!ent.empty()) cudaMemcpy(E.d_tp_ent, ent.data(), ent.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemset(E.d_tp_x, 0, 3 * nt * sizeof(double));
+    E.d.ntp = (int)nt; E.d.tp_off = E.d_tp_off; E.d.tp_ent = E.d_tp_ent; E.d.tp_x = E.d_tp_x;
   }
   if (!hft.empty()) {
     if (cudaMalloc(&E.d_hft, hft.size() * sizeof(double)) != cudaSuccess) { E.err = "cudaMalloc heat-flux tables"; return false; }

@@ -61,6 +61,7 @@ extern "C" {
 #define CFD3D_BC_WALL_HEATFLUX     12   /* BCWall of family HeatFlux*: q(t) from the patch's table */
 #define CFD3D_BC_MASSFLOWRATE_IN   13   /* BCMassflowrateIn (mass-flow rate 0, as constructed) */
 #define CFD3D_BC_SHIFTED_PERIODIC  14   /* BCShiftedPeriodic (the reference's 16-cell shift)   */
+#define CFD3D_BC_TOTALPRESSURE_IN  15   /* BCTotalPressureIn (the reference's fixed totals)    */
 
 /* Solver configuration: the fields of the reference's input.inp
  * (src/config_module.f90:100-119, documented in bin/input_templet.inp:34-66). */

@@ -55,7 +55,7 @@ enum Face { F_IMIN, F_IMAX, F_JMIN, F_JMAX, F_KMIN, F_KMAX, F_KMIN_CAP, F_KMAX_C
 
 enum BcKind {
   K_WALL_INVISCID, K_WALL_VISCOUS, K_WALL_KW, K_FARFIELD, K_EXTRAP, K_SYMMETRY, K_NOOP,
-  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED, K_HFWALL_KW, K_WALL_KE,
+  K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED, K_HFWALL_KW, K_WALL_KE, K_TOTALP,
   K_EDGE_WALLWALL, K_EDGE_WALLWALL_KW, K_EDGE_NOWALL, K_CORNER_WALLWALL, K_CORNER_WALLWALL_KW, K_CORNER_NOWALL
 };
 
@@ -146,6 +146,13 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
   double dv[NDV], tv[3] = {0, 0, 0};
   deteos(c.eos, c.with_prop, c.pref, c.tref, c.y1ref, c.y2ref, dv, tv);
   c.rhoref = dv[0];
+  {   /* the total-pressure inlet's construct (src/bc_module.f90:318-321, 336) */
+    c.tp_pt = 51551.30907;
+    c.tp_tt = 300.0003719;
+    double dvt[NDV], tvt[3] = {0, 0, 0};
+    deteos(c.eos, c.with_prop, c.tp_pt, c.tp_tt, c.y1ref, c.y2ref, dvt, tvt);
+    c.tp_ht = dvt[1];
+  }
   c.visref = tv[0];
   if (c.iturb == -1) {   /* config%setref for k-epsilon (src/config_module.f90:191-194) */
     c.kref = 1.5 * sq(0.0001 * c.uref);
@@ -428,6 +435,7 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
         bi.heatflux.assign(p.heatflux, p.heatflux + p.ndata);
         break;
       case CFD3D_BC_MASSFLOWRATE_IN: bi.kind = K_MASSFLOW_IN; break;   /* bcmassflowratein :3812-4012 */
+      case CFD3D_BC_TOTALPRESSURE_IN: bi.kind = K_TOTALP; break;       /* bctotalpressurein :3299-3514 */
       case CFD3D_BC_SHIFTED_PERIODIC: bi.kind = K_SHIFTED; break;      /* bcshiftedperiodic :3134-3297 */
       case CFD3D_BC_SYMMETRY: bi.kind = K_SYMMETRY; break;
       case CFD3D_BC_FARFIELD: bi.kind = K_FARFIELD; break;
@@ -759,8 +767,139 @@ static void face_cell(const BcInfo& bi, Block& B, int i, int j, int k, int& ii, 
   }
 }
 
+/* newt / funcv / fdjac / lnsrch / ludcmp / lubksb (src/bc_module.f90:4305-4622) for the
+   total-pressure inlet, n = 2: as written, newt's fvec is evaluated once at its start */
+struct TpSys { const Cfg* c; double uu, gam; };
+static void tp_funcv(const TpSys& S, const double* x, double* f) {
+  double dv[NDV];
+  deteos_simple(S.c->eos, x[0], x[1], S.c->y1ref, S.c->y2ref, dv);
+  f[0] = S.c->tp_pt - x[0] * std::pow(S.c->tp_tt / x[1], S.gam / (S.gam - 1.0));
+  f[1] = S.c->tp_ht - (dv[1] + 0.5 * S.uu);
+}
+static double tp_fmin(const TpSys& S, const double* x, double* f) {
+  tp_funcv(S, x, f);
+  return 0.5 * (sq(f[0]) + sq(f[1]));
+}
+static void tp_ludcmp(double a[2][2], int* indx) {
+  double vv[2];
+  for (int i = 0; i < 2; ++i) { double aamax = 0.0; for (int j = 0; j < 2; ++j) aamax = dmax(aamax, std::fabs(a[i][j])); vv[i] = 1.0 / aamax; }
+  for (int j = 0; j < 2; ++j) {
+    for (int i = 0; i < j; ++i) { double sum = a[i][j]; for (int k = 0; k < i; ++k) sum -= a[i][k] * a[k][j]; a[i][j] = sum; }
+    double aamax = 0.0; int imax = j;
+    for (int i = j; i < 2; ++i) {
+      double sum = a[i][j];
+      for (int k = 0; k < j; ++k) sum -= a[i][k] * a[k][j];
+      a[i][j] = sum;
+      double dum = vv[i] * std::fabs(sum);
+      if (dum >= aamax) { imax = i; aamax = dum; }
+    }
+    if (j != imax) { for (int k = 0; k < 2; ++k) std::swap(a[imax][k], a[j][k]); vv[imax] = vv[j]; }
+    indx[j] = imax;
+    if (a[j][j] == 0.0) a[j][j] = 1.0e-20;
+    if (j != 1) { double dum = 1.0 / a[j][j]; for (int i = j + 1; i < 2; ++i) a[i][j] *= dum; }
+  }
+}
+static void tp_lubksb(double a[2][2], const int* indx, double* b) {
+  int ii = -1;
+  for (int i = 0; i < 2; ++i) {
+    int ll = indx[i]; double sum = b[ll]; b[ll] = b[i];
+    if (ii >= 0) { for (int j = ii; j < i; ++j) sum -= a[i][j] * b[j]; }
+    else if (sum != 0.0) ii = i;
+    b[i] = sum;
+  }
+  for (int i = 1; i >= 0; --i) { double sum = b[i]; for (int j = i + 1; j < 2; ++j) sum -= a[i][j] * b[j]; b[i] = sum / a[i][i]; }
+}
+static void tp_newt(const TpSys& S, double* x) {
+  const double tolf = 1.0e-4, tolx = 1.0e-7, stpmx = 100.0, alf = 1.0e-4;
+  double fvec[2], fjac[2][2], g[2], p[2], xold[2];
+  double f = tp_fmin(S, x, fvec);
+  if (dmax(std::fabs(fvec[0]), std::fabs(fvec[1])) < 0.01 * tolf) return;
+  double stpmax = stpmx * dmax(std::sqrt(sq(x[0]) + sq(x[1])), 2.0);
+  for (int its = 1; its <= 200; ++its) {
+    for (int j = 0; j < 2; ++j) {
+      double temp[2] = {x[0], x[1]}, fj[2];
+      double h = 1.0e-4 * std::fabs(temp[j]);
+      if (h == 0.0) h = 1.0e-4;
+      temp[j] = temp[j] + h;
+      h = temp[j] - x[j];
+      tp_funcv(S, temp, fj);
+      for (int i = 0; i < 2; ++i) fjac[i][j] = (fj[i] - fvec[i]) / h;
+    }
+    for (int i = 0; i < 2; ++i) { double sum = 0.0; for (int j = 0; j < 2; ++j) sum += fjac[j][i] * fvec[j]; g[i] = sum; }
+    xold[0] = x[0]; xold[1] = x[1];
+    double fold = f;
+    p[0] = -fvec[0]; p[1] = -fvec[1];
+    int indx[2];
+    tp_ludcmp(fjac, indx);
+    tp_lubksb(fjac, indx, p);
+    bool check = false;
+    { /* lnsrch */
+      double sum = std::sqrt(sq(p[0]) + sq(p[1]));
+      if (sum > stpmax) for (int i = 0; i < 2; ++i) p[i] = p[i] * stpmax / sum;
+      double slope = g[0] * p[0] + g[1] * p[1];
+      double test = 0.0;
+      for (int i = 0; i < 2; ++i) { double temp = std::fabs(p[i]) / dmax(std::fabs(xold[i]), 1.0); if (temp > test) test = temp; }
+      double alamin = tolx / test, alam = 1.0, alam2 = 0.0, f2 = 0.0, fold2 = 0.0, tmplam = 0.0;
+      for (;;) {
+        for (int i = 0; i < 2; ++i) x[i] = xold[i] + alam * p[i];
+        double fl[2];
+        f = tp_fmin(S, x, fl);
+        if (alam < alamin) { x[0] = xold[0]; x[1] = xold[1]; check = true; break; }
+        if (f <= fold + alf * alam * slope) break;
+        if (alam == 1.0) tmplam = -slope / (2.0 * (f - fold - slope));
+        else {
+          double rhs1 = f - fold - alam * slope, rhs2 = f2 - fold2 - alam2 * slope;
+          double a = (rhs1 / sq(alam) - rhs2 / sq(alam2)) / (alam - alam2);
+          double b = (-alam2 * rhs1 / sq(alam) + alam * rhs2 / sq(alam2)) / (alam - alam2);
+          if (a == 0.0) tmplam = -slope / (2.0 * b);
+          else {
+            double disc = b * b - 3.0 * a * slope;
+            if (disc < 0.0) tmplam = 0.5 * alam;
+            else if (b <= 0.0) tmplam = (-b + std::sqrt(disc)) / (3.0 * a);
+            else tmplam = -slope / (b + std::sqrt(disc));
+          }
+          if (tmplam > 0.5 * alam) tmplam = 0.5 * alam;
+        }
+        alam2 = alam; f2 = f; fold2 = fold;
+        alam = dmax(tmplam, 0.1 * alam);
+      }
+    }
+    if (dmax(std::fabs(fvec[0]), std::fabs(fvec[1])) < tolf) return;
+    if (check) return;
+    double test = 0.0;
+    for (int i = 0; i < 2; ++i) { double temp = std::fabs(x[i] - xold[i]) / dmax(std::fabs(x[i]), 1.0); if (temp > test) test = temp; }
+    if (test < tolx) return;
+  }
+}
+
 static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
   double pv[NPV_MAX], dv[NDV], tv[3], pvs[NPV_MAX], dvs[NDV], tvs[3], ppv[NPV_MAX], nx[3];
+  double tpx[2] = {0.0, 0.0}, tpuu = 0.0;
+  if (bi.kind == K_TOTALP) {
+    /* the patch's area-weighted averages over its boundary faces (:3320-3409), then newt */
+    double pa[5] = {0, 0, 0, 0, 0}, area = 0.0;
+    const int ax = (int)bi.face / 2;
+    for (int k = bi.istart[2]; k <= bi.iend[2]; ++k)
+      for (int j = bi.istart[1]; j <= bi.iend[1]; ++j)
+        for (int i = bi.istart[0]; i <= bi.iend[0]; ++i) {
+          const int idx[3] = {i, j, k};
+          if (idx[ax] != (((int)bi.face % 2 == 0) ? bi.istart[ax] : bi.iend[ax])) continue;
+          int ii = 0, jj = 0, kk = 0;
+          face_cell(bi, B, i, j, k, ii, jj, kk, nx, true);
+          const double dl = std::sqrt(sq(nx[0]) + sq(nx[1]) + sq(nx[2]));
+          const double* P = B.pv.at(ii, jj, kk);
+          pa[0] += P[0] * dl;
+          pa[4] += P[4] * dl;
+          for (int m = 1; m <= 3; ++m) pa[m] += P[m] * dl;
+          area += dl;
+        }
+    for (int m = 0; m < 5; ++m) pa[m] /= area;
+    TpSys S{&c, sq(pa[1]) + sq(pa[2]) + sq(pa[3]), (1.0 - c.y2ref) * 1.33 + c.y2ref * 1.4};
+    tpx[0] = pa[0] + bi.pv[0];
+    tpx[1] = pa[4];
+    tpuu = S.uu;
+    tp_newt(S, tpx);
+  }
   for (int k = bi.istart[2]; k <= bi.iend[2]; ++k)
     for (int j = bi.istart[1]; j <= bi.iend[1]; ++j)
       for (int i = bi.istart[0]; i <= bi.iend[0]; ++i) {
@@ -798,6 +937,22 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
             tv[2] = -tv[2];
             put_cell(c, B, i, j, k, pv, dv, tv);
             break;
+          case K_TOTALP: {
+            int ii = 0, jj = 0, kk = 0;
+            face_cell(bi, B, i, j, k, ii, jj, kk, nx, true);
+            const double dl = 1.0 / std::sqrt(sq(nx[0]) + sq(nx[1]) + sq(nx[2]));
+            get_cell(c, B, mi, mj, mk, pv, dv, tv);
+            pv[0] = 2.0 * (tpx[0] - bi.pv[0]) - pv[0];
+            for (int q = 0; q < 3; ++q) pv[1 + q] = 2.0 * (-std::sqrt(tpuu) * nx[q] * dl - 0.0) - pv[1 + q];
+            pv[4] = 2.0 * tpx[1] - pv[4];
+            for (int m = 5; m < c.npv; ++m) pv[m] = 2.0 * bi.pv[m] - pv[m];
+            pv[6] = 2.0 * bi.pv[6] - pv[6];
+            pv[5] = dmin(dmax(pv[5], 0.0), 1.0);
+            pv[6] = dmin(dmax(pv[6], 0.0), 1.0);
+            deteos(c.eos, c.with_prop, pv[0] + bi.pv[0], pv[4], pv[5], pv[6], dv, tv);
+            put_cell(c, B, i, j, k, pv, dv, tv);
+            break;
+          }
           case K_CRWALL_KW:
             /* omega: the mirror's (the routine computes the wall value and discards it) */
             get_cell(c, B, mi, mj, mk, pv, dv, tv);

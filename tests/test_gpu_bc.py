@@ -160,3 +160,28 @@ def test_heatflux_wall_needs_sst():
     with pytest.raises(native.Cfd3dError) as ei:
         native.Engine(c)
     assert ei.value.code == abi.ERR_DESCRIPTOR
+
+
+@pytest.mark.parametrize("base", ["plain", "cavitating", "sst"])
+def test_totalpressure_inlet_matches(oracle, base):
+    """bctotalpressurein: the patch's area-weighted averages, the reference's Newton solve for
+    (p, T) at its fixed totals, and the ghost state from them"""
+    name, kw, over = BASES[base]
+    c = cases.make(name, **kw)
+    c["cfg"].update(over)
+    c = replace_faces(c, {"imin": abi.BC_TOTALPRESSURE_IN})
+    e = native.Engine(c)
+    o = oracle.Oracle(c)
+    e.initialize(c["pv0"])
+    o.initialize(c["pv0"])
+    assert field_err(e.residual(0)["res"], o.residual(0)["res"]).max() < TOL_RES
+    for it in range(3):
+        _, resg, _ = e.iterate(1, it + 1, 0.0)
+        _, reso, _ = o.iterate(1, it + 1, 0.0)
+        assert np.all(np.isfinite(resg))
+        assert np.allclose(resg, reso, rtol=1e-7, atol=1e-9 * np.abs(reso).max()), (it, resg, reso)
+    sg, so = e.download(0), o.get_state(0)
+    assert field_err(interior(sg["pv"]), interior(so["pv"])).max() < TOL_STATE
+    assert field_err(sg["pv"][3:-3, 3:-3, :3], so["pv"][3:-3, 3:-3, :3]).max() < TOL_STATE
+    with pytest.raises(native.Cfd3dError):
+        e.residual_vjp([np.zeros(abi.interior_shape(c["blocks"][0], e.npv))])
