@@ -250,7 +250,7 @@ __device__ __forceinline__ long long stencil_cell(int l, long long g, long long 
 
 
 // cells per chunk of the dataflow sweeps (one CTA's work item)
-constexpr int SW_CH = 64;
+constexpr int SW_CH = 32;
 
 // face-flux launchers (flux.cu: FP64 form; flux_mixed.cu: mixed form)
 void launch_face_flux(const Engine& E, cudaStream_t s);
