@@ -265,7 +265,7 @@ def main():
     ap.add_argument("--ref-scale", type=int, default=2,
                     help="the CPU samples run the workload at 1/ref-scale resolution")
     ap.add_argument("--ref-threads", type=int, default=0, help="host threads of the CPU samples (0: all)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     args = ap.parse_args()
@@ -321,15 +321,20 @@ def main():
         bufs.append(keep)
     d2h += 8 * eng.npv
     import torch
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s in range(args.e2e_steps):
+
+    def e2e_step(s):
         for n, keep in enumerate(bufs):
             eng.upload(n, pv=keep["pv"][1], dv=keep["dv"][1], tv=keep["tv"][1] if "tv" in keep else None,
                        qq=keep["qq"][1] if "qq" in keep else None)
         eng.iterate(1, args.warmup + s + 1, 0.0)
         for n, keep in enumerate(bufs):
             eng.download_arrays(n, pv=keep["pv"][1], dv=keep["dv"][1], tv=keep["tv"][1] if "tv" in keep else None)
+
+    e2e_step(0)                                   # untimed: first touch of the pinned pages
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(args.e2e_steps):
+        e2e_step(s + 1)
     e2e_ms, e2e_value = combine_ranks((time.perf_counter() - t0) / args.e2e_steps * 1e3, ncell, dist)
     if rank != 0:
         dist.barrier()

@@ -1364,6 +1364,10 @@ struct cfd3d_handle {
   Engine E;
   double* staging = nullptr;
   size_t staging_bytes = 0;
+  // the copy stream of upload_state / download_state and one event per staged array:
+  // the layout kernel of one array overlaps the host copy of the next
+  cudaStream_t cp = nullptr;
+  cudaEvent_t ev[6] = {};
 };
 
 namespace {
@@ -1378,6 +1382,14 @@ int ensure_staging(cfd3d_handle* h, size_t bytes) {
   h->staging_bytes = 0;
   CFD_CUDA(cudaMalloc(&h->staging, bytes));
   h->staging_bytes = bytes;
+  return CFD3D_OK;
+}
+
+int ensure_copy_stream(cfd3d_handle* h) {
+  Engine& E = h->E;
+  if (h->cp) return CFD3D_OK;
+  for (auto& e : h->ev) CFD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  CFD_CUDA(cudaStreamCreateWithFlags(&h->cp, cudaStreamNonBlocking));
   return CFD3D_OK;
 }
 
@@ -1898,6 +1910,8 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d.recf);
   cudaFree(E.d.dqsf);
   adjoint_free(E);
+  if (h->cp) cudaStreamDestroy(h->cp);
+  for (auto e : h->ev) if (e) cudaEventDestroy(e);
   if (E.st) cudaStreamDestroy(E.st);
   delete h;
 }
@@ -1956,19 +1970,33 @@ int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const doubl
   const Par& c = E.par;
   long long ncb = (long long)B.ni * B.nj * B.nk;
   long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
-  int rc = ensure_staging(h, (size_t)ncb * NDV * 8);
+  // each array has its own staging region; the copies run back to back on the copy
+  // stream and the layout kernel of each waits only for its own copy
+  int rc = ensure_staging(h, (size_t)(ncb * (c.npv + NDV + c.ntv) + nint * 2 * c.npv) * 8);
+  if (!rc) rc = ensure_copy_stream(h);
   if (rc) return rc;
+  CFD_CUDA(cudaEventRecord(h->ev[5], E.st));          // staging no longer read by earlier work
+  CFD_CUDA(cudaStreamWaitEvent(h->cp, h->ev[5], 0));
   struct { const double* a; int nv; double* dst; } items[3] = {{pv, c.npv, E.d.pv}, {dv, NDV, E.d.dv}, {tv, c.ntv, E.d.tv}};
+  double* stg = h->staging;
+  int q = 0;
   for (auto& it : items) {
     if (!it.a || it.nv == 0) continue;
-    CFD_CUDA(cudaMemcpyAsync(h->staging, it.a, (size_t)ncb * it.nv * 8, cudaMemcpyHostToDevice, E.st));
-    k_aos_to_soa<<<nblk_of(ncb, 256), 256, 0, E.st>>>(h->staging, it.nv, ncb, it.dst, E.ncell, B.off);
+    CFD_CUDA(cudaMemcpyAsync(stg, it.a, (size_t)ncb * it.nv * 8, cudaMemcpyHostToDevice, h->cp));
+    CFD_CUDA(cudaEventRecord(h->ev[q], h->cp));
+    CFD_CUDA(cudaStreamWaitEvent(E.st, h->ev[q], 0));
+    k_aos_to_soa<<<nblk_of(ncb, 256), 256, 0, E.st>>>(stg, it.nv, ncb, it.dst, E.ncell, B.off);
+    stg += ncb * it.nv;
+    ++q;
   }
   if (qq && c.nqq) {
-    CFD_CUDA(cudaMemcpyAsync(h->staging, qq, (size_t)nint * 2 * c.npv * 8, cudaMemcpyHostToDevice, E.st));
-    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, 2 * c.npv, B, E.d.qq, E.ncell, 1);
+    CFD_CUDA(cudaMemcpyAsync(stg, qq, (size_t)nint * 2 * c.npv * 8, cudaMemcpyHostToDevice, h->cp));
+    CFD_CUDA(cudaEventRecord(h->ev[q], h->cp));
+    CFD_CUDA(cudaStreamWaitEvent(E.st, h->ev[q], 0));
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(stg, 2 * c.npv, B, E.d.qq, E.ncell, 1);
   }
-  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaStreamSynchronize(E.st));               // waited for every copy too
+  CFD_CUDA(cudaGetLastError());
   return CFD3D_OK;
 }
 
@@ -1980,25 +2008,39 @@ int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, dou
   const Par& c = E.par;
   long long ncb = (long long)B.ni * B.nj * B.nk;
   long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
-  int rc = ensure_staging(h, (size_t)ncb * NDV * 8);
+  // the layout kernels run back to back on the engine's stream; the copy of each array
+  // leaves on the copy stream as soon as its own kernel is done
+  int rc = ensure_staging(h, (size_t)(ncb * (c.npv + NDV + c.ntv) + nint * (2 * c.npv + 2)) * 8);
+  if (!rc) rc = ensure_copy_stream(h);
   if (rc) return rc;
   struct { double* a; int nv; double* src; } items[3] = {{pv, c.npv, E.d.pv}, {dv, NDV, E.d.dv}, {tv, c.ntv, E.d.tv}};
+  double* stg = h->staging;
+  int q = 0;
+  auto send = [&](double* host, size_t bytes) -> int {
+    CFD_CUDA(cudaEventRecord(h->ev[q], E.st));
+    CFD_CUDA(cudaStreamWaitEvent(h->cp, h->ev[q], 0));
+    CFD_CUDA(cudaMemcpyAsync(host, stg, bytes, cudaMemcpyDeviceToHost, h->cp));
+    ++q;
+    return CFD3D_OK;
+  };
   for (auto& it : items) {
     if (!it.a || it.nv == 0) continue;
-    k_soa_to_aos<<<nblk_of(ncb, 256), 256, 0, E.st>>>(it.src, it.nv, ncb, h->staging, E.ncell, B.off);
-    CFD_CUDA(cudaMemcpyAsync(it.a, h->staging, (size_t)ncb * it.nv * 8, cudaMemcpyDeviceToHost, E.st));
-    CFD_CUDA(cudaStreamSynchronize(E.st));
+    k_soa_to_aos<<<nblk_of(ncb, 256), 256, 0, E.st>>>(it.src, it.nv, ncb, stg, E.ncell, B.off);
+    if ((rc = send(it.a, (size_t)ncb * it.nv * 8))) return rc;
+    stg += ncb * it.nv;
   }
   if (qq && c.nqq) {
-    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, 2 * c.npv, B, E.d.qq, E.ncell, 0);
-    CFD_CUDA(cudaMemcpyAsync(qq, h->staging, (size_t)nint * 2 * c.npv * 8, cudaMemcpyDeviceToHost, E.st));
-    CFD_CUDA(cudaStreamSynchronize(E.st));
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(stg, 2 * c.npv, B, E.d.qq, E.ncell, 0);
+    if ((rc = send(qq, (size_t)nint * 2 * c.npv * 8))) return rc;
+    stg += nint * 2 * c.npv;
   }
   if (rcav) {
-    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, 2, B, E.d.rcav, E.ncell, 0);
-    CFD_CUDA(cudaMemcpyAsync(rcav, h->staging, (size_t)nint * 2 * 8, cudaMemcpyDeviceToHost, E.st));
-    CFD_CUDA(cudaStreamSynchronize(E.st));
+    k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(stg, 2, B, E.d.rcav, E.ncell, 0);
+    if ((rc = send(rcav, (size_t)nint * 2 * 8))) return rc;
   }
+  CFD_CUDA(cudaStreamSynchronize(h->cp));             // every copy waited for its kernel
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
   return CFD3D_OK;
 }
 
