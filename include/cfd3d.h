@@ -142,6 +142,10 @@ int  cfd3d_initialize(cfd3d_handle *h, int block, const double *pv_interior);
 
 /* Copy a full padded state in/out: pv(npv,-1:imax+3,..), dv(ndv,..), tv(ntv,..),
  * qq(npv,nqq,2:imax,..) and (out only) rcav(2,2:imax,..).  Any pointer may be NULL.
+ * Pinned (page-locked) host arrays move at the link's full rate. The handle keeps one
+ * device staging region per array, (npv+ndv+ntv) padded + (2 npv+2) interior doubles
+ * per cell of the largest block, so that the layout change of one array overlaps the copy
+ * of the next. Both calls return after every copy has finished.
  * Replaces the accessors t_variable%getpv/setpv.. (src/variable_module.f90:22-39). */
 int  cfd3d_upload_state(cfd3d_handle *h, int block, const double *pv, const double *dv,
                         const double *tv, const double *qq);
