@@ -8,7 +8,7 @@
  * src/initial_module.f90:678-771).  Storage follows the reference: AoS arrays with the
  * variable index fastest and the padded index ranges of src/variable_module.f90:69-77.
  *
- * Used only by tests/ and by bench.py's CPU-baseline arm, as the checker.  The product
+ * Used only by tests/ (to verify the GPU path) and by bench.py's CPU-baseline arm (timed).  The product
  * library never links or calls it.
  *
  * parity unpinned: the reference cannot be compiled here (Fortran + MPI + CGNS) and has

@@ -3,7 +3,7 @@
 The file out_########.dat written by `variable%export_variable`
 (src/variable_module.f90:116-182) and read by `t_ini_restart%restart`
 (src/initial_module.f90:245-389; the steadyini variant :103-242).  Imported only by
-tests/, as the checker of the engine's cfd3d_checkpoint_write / cfd3d_checkpoint_read.
+tests/, to verify the engine's cfd3d_checkpoint_write / cfd3d_checkpoint_read.
 
 Each MPI rank r owns block r and writes its record at a displacement equal to the sizes
 of the records of ranks 0..r-1 (src/variable_module.f90:80-91, with intsize = 4 and

@@ -3,12 +3,12 @@
  *
  * Pointwise physics of the CPU oracle: a line-by-line FP64 restatement of the
  * reference's EOS, reconstruction, flux, viscous, source, Jacobian and diagonal
- * operators (kwonhwi1/3dcode, src/*.f90).  Nothing in the product includes this
- * file; the tests and the CPU baseline arm of bench.py use it as the checker.
+ * operators (kwonhwi1/3dcode, the src/ Fortran files).  Nothing in the product includes this
+ * file; the tests use it to verify the GPU path and bench.py's CPU baseline arm times it.
  *
  * parity unpinned: the reference is Fortran + MPI + CGNS and cannot be built in this
  * environment, and it ships no tests or golden vectors; this restatement is the
- * checker, validated by self-consistency properties (tests/test_oracle.py).
+ * parity reference, validated by self-consistency properties (tests/test_oracle.py).
  *
  * Evaluation order follows the Fortran source (left-to-right products, no fused
  * multiply-add: build with -ffp-contract=off).  Integer powers with a variable

@@ -2,7 +2,8 @@
 
 Loads oracle/_build/liboracle.so (built by `make -C oracle`) and exposes the restated
 reference path on the same descriptors the product takes.  Imported only by tests/,
-by __graft_entry__.smoke() and by bench.py's CPU-baseline arm, always as the checker.
+by __graft_entry__.smoke() (to verify the GPU path) and by bench.py's CPU-baseline arm (timed
+as the CPU baseline); never by the product path.
 
 parity unpinned: the reference (Fortran + MPI + CGNS) cannot be built here and has no
 tests or golden vectors; see oracle_physics.h.
