@@ -1,0 +1,76 @@
+"""cfd3d_upload_state / cfd3d_download_state (the t_variable accessors getpv/setpv..,
+src/variable_module.f90:22-39): a seeded state goes in and comes back bit for bit, from
+pinned and from pageable host memory, array by array, without touching the other block."""
+import numpy as np
+import pytest
+import torch
+
+from cfd3d_gb300 import abi, cases, native
+
+pytestmark = pytest.mark.gpu
+
+
+def _case():
+    c = cases.split_i(cases.make("large", scale=16), 2)     # SST, cavitation, BDF2: nqq = 2
+    return c
+
+
+def _random_state(e, b, rng):
+    blk = e.case["blocks"][b]
+    return dict(pv=rng.normal(size=abi.padded_shape(blk, e.npv)),
+                dv=rng.normal(size=abi.padded_shape(blk, 18)),
+                tv=rng.normal(size=abi.padded_shape(blk, e.ntv)),
+                qq=rng.normal(size=abi.interior_shape(blk, 2 * e.npv)))
+
+
+def _pinned(a):
+    t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+    v = t.numpy().reshape(a.shape)
+    v[...] = a
+    return t, v
+
+
+@pytest.mark.parametrize("memory", ["pinned", "pageable"])
+def test_round_trip_is_bit_exact(memory):
+    c = _case()
+    e = native.Engine(c)
+    e.initialize(c["pv0"])
+    assert e.nqq and e.ntv == 3 and len(c["blocks"]) == 2
+    rng = np.random.default_rng(21)
+    before = e.download(0)
+    st = _random_state(e, 1, rng)
+    keep = {k: _pinned(v) for k, v in st.items()} if memory == "pinned" else None
+    src = {k: keep[k][1] for k in st} if keep else st
+    e.upload(1, **src)
+    got = e.download(1)
+    for k in ("pv", "dv", "tv", "qq"):
+        assert np.array_equal(got[k], st[k]), k
+    # the other block is untouched
+    after = e.download(0)
+    for k in ("pv", "dv", "tv", "qq"):
+        assert np.array_equal(after[k], before[k]), k
+    # download into caller-owned pinned arrays, every field in one call
+    out = {k: _pinned(np.zeros_like(v)) for k, v in st.items()}
+    rcav = np.zeros(abi.interior_shape(c["blocks"][1], 2))
+    e.download_arrays(1, pv=out["pv"][1], dv=out["dv"][1], tv=out["tv"][1], qq=out["qq"][1], rcav=rcav)
+    for k in ("pv", "dv", "tv", "qq"):
+        assert np.array_equal(out[k][1], st[k]), k
+    assert np.array_equal(rcav, got["rcav"])
+
+
+def test_partial_upload_leaves_the_rest():
+    c = _case()
+    e = native.Engine(c)
+    e.initialize(c["pv0"])
+    rng = np.random.default_rng(22)
+    before = e.download(0)
+    st = _random_state(e, 0, rng)
+    e.upload(0, dv=st["dv"])
+    got = e.download(0)
+    assert np.array_equal(got["dv"], st["dv"])
+    for k in ("pv", "tv", "qq"):
+        assert np.array_equal(got[k], before[k]), k
+    e.upload(0, tv=st["tv"], qq=st["qq"])
+    got = e.download(0)
+    assert np.array_equal(got["tv"], st["tv"]) and np.array_equal(got["qq"], st["qq"])
+    assert np.array_equal(got["pv"], before["pv"])
