@@ -51,24 +51,25 @@ __global__ void __launch_bounds__(64) k_adj_cell(DevPtr d, Par c, AdjPtr a) {
     double gp[NPVM], gd[NGD];
     for (int v = 0; v < NPVM; ++v) gp[v] = 0.0;
     for (int m = 0; m < NGD; ++m) gd[m] = 0.0;
-    // ---- cavitation: res(6) += r_v - r_c; seeds p, T, y1, y2, rho, rho_l, rho_v, uref, c_v, c_c
+    // ---- cavitation: res(6) += r_v - r_c; seeds p, T, y1, y2, rho, rho_l, rho_v, rho_g (Kunz's
+    // gas volume fraction), uref, c_v, c_c
     if (c.ncav && lam[5] != 0.0) {
       const int pvs[4] = {0, 4, 5, 6};
-      const int dvs[3] = {0, 2, 3};
-      double w[10];
-      for (int k0 = 0; k0 < 10; k0 += DC) {
+      const int dvs[4] = {0, 2, 3, 4};
+      double w[11];
+      for (int k0 = 0; k0 < 11; k0 += DC) {
         DD p2[NPVM], dd[NDV];
         for (int v = 0; v < NPVM; ++v) p2[v] = DD(pv2[v]);
         for (int q = 0; q < NDV; ++q) dd[q] = DD(dv[q]);
         for (int m = 0; m < 4; ++m) p2[pvs[m]] = seed(pv2[pvs[m]], m, k0);
-        for (int m = 0; m < 3; ++m) dd[dvs[m]] = seed(dv[dvs[m]], 4 + m, k0);
-        const CavOutT<DD> o = cavsource_t<DD>(c, p2, dd, vol, seed(c.uref, 7, k0), seed(c.c_v, 8, k0),
-                                              seed(c.c_c, 9, k0));
-        for (int q = 0; q < DC && k0 + q < 10; ++q) w[k0 + q] = lam[5] * (o.r_v.d[q] - o.r_c.d[q]);
+        for (int m = 0; m < 4; ++m) dd[dvs[m]] = seed(dv[dvs[m]], 4 + m, k0);
+        const CavOutT<DD> o = cavsource_t<DD>(c, p2, dd, vol, seed(c.uref, 8, k0), seed(c.c_v, 9, k0),
+                                              seed(c.c_c, 10, k0));
+        for (int q = 0; q < DC && k0 + q < 11; ++q) w[k0 + q] = lam[5] * (o.r_v.d[q] - o.r_c.d[q]);
       }
       for (int m = 0; m < 4; ++m) gp[pvs[m]] += w[m];
-      gd[GD_RHO] += w[4]; gd[GD_RL] += w[5]; gd[GD_RV] += w[6];
-      wp[0] += w[7]; wp[1] += w[8]; wp[2] += w[9];
+      gd[GD_RHO] += w[4]; gd[GD_RL] += w[5]; gd[GD_RV] += w[6]; gd[GD_RG] += w[7];
+      wp[0] += w[8]; wp[1] += w[9]; wp[2] += w[10];
     }
     // ---- SST: res(8) += r7, res(9) += r8; seeds the 15 cell gradients, k, omega, rho, mu, mu_t
     if (c.iturb == 0 && (lam[7] != 0.0 || lam[8] != 0.0)) {

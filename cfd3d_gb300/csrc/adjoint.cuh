@@ -8,10 +8,11 @@
 
 namespace cfd {
 
-// gdt planes: dv(1), dv(2), dv(6), dv(12), dv(3), dv(4), tv(1), tv(2), tv(3) in the
+// gdt planes: dv(1), dv(2), dv(6), dv(12), dv(3), dv(4), dv(5), tv(1), tv(2), tv(3) in the
 // reference's 1-based numbering
-enum { GD_RHO = 0, GD_H, GD_C2, GD_CP, GD_RL, GD_RV, GD_VIS, GD_CON, GD_MUT, NGD };
-static __constant__ int kGdDv[6] = {0, 1, 5, 11, 2, 3};   // dv slot of the first six planes
+enum { GD_RHO = 0, GD_H, GD_C2, GD_CP, GD_RL, GD_RV, GD_RG, GD_VIS, GD_CON, GD_MUT, NGD };
+constexpr int NGD_DV = 7;   // the planes that are dv entries
+static __constant__ int kGdDv[NGD_DV] = {0, 1, 5, 11, 2, 3, 4};   // their dv slots
 
 struct AdjPtr {
   const double* lam;   // padded cotangent (npv x ncell), zero outside the interior
@@ -44,7 +45,7 @@ static __device__ __noinline__ void eos_chain(const Par& c, double p, double t, 
   deteos_t<D4>(c.fluid, c.with_prop, D4::seed(p, 0), D4::seed(t, 1), D4::seed(y1, 2), D4::seed(y2, 3), dv, tv);
   for (int m = 0; m < 4; ++m) {
     double s = 0.0;
-    for (int q = 0; q < 6; ++q) s += gd[q] * dv[kGdDv[q]].d[m];
+    for (int q = 0; q < NGD_DV; ++q) s += gd[q] * dv[kGdDv[q]].d[m];
     if (c.with_prop) s += gd[GD_VIS] * tv[0].d[m] + gd[GD_CON] * tv[1].d[m];
     ge[m] = s;
   }

@@ -22,11 +22,13 @@
 #include <cstdlib>
 #include <cstddef>
 #include <cstring>
+#include <cuda.h>
 #include <fcntl.h>
 #include <mutex>
 #include <new>
 #include <type_traits>
 #include <unistd.h>
+#include <vector>
 #include "engine.cuh"
 #include "mixed.cuh"
 
@@ -329,8 +331,9 @@ __device__ void tp_newt(const TpProblem& P, double* x) {
   }
 }
 
-// one CTA per total-pressure patch: the area-weighted boundary averages (the patch's
-// reduction), then the Newton solve by thread 0
+// one CTA per pool of total-pressure patches (the n-th inlet of every block): the
+// area-weighted boundary averages over the pool (the reference's reduction over its
+// communicator), then the Newton solve by thread 0
 __global__ void __launch_bounds__(128) k_totalp(DevPtr d, Par c) {
   const int pt = blockIdx.x;
   const long long n = d.ncell;
@@ -1648,9 +1651,36 @@ struct EosScratch {
   double dv[NDV * CFD3D_EOS_NOALLOC_MAX], tv[2 * CFD3D_EOS_NOALLOC_MAX];
   unsigned long long fallbacks;   // must start at zero: the kernel counts into it
 };
-constexpr int EOS_SCRATCH_DEVICES = 64;
+// The buffer's device address per CUDA context.  A context has its own copy of every
+// module's globals, and a context that ends (cudaDeviceReset, a primary context released
+// and made again) takes the copy with it, so the cache is keyed on the context's unique id
+// (cuCtxGetId; ids are never reused within a process), not on the device index.
+struct ScratchSlot { unsigned long long ctx; EosScratch* ptr; };
 std::mutex g_eos_scratch_mu;
-EosScratch* g_eos_scratch_ptr[EOS_SCRATCH_DEVICES] = {};
+std::vector<ScratchSlot> g_eos_scratch_slots;
+
+// the current context's id, through the runtime's driver entry points (no link against
+// the driver library); 0 when no context is current
+using FnCtxGetCurrent = CUresult (*)(CUcontext*);
+using FnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+bool current_ctx_id(unsigned long long& id) {
+  static FnCtxGetCurrent get_cur = nullptr;
+  static FnCtxGetId get_id = nullptr;
+  if (!get_cur || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, nullptr) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, nullptr) != cudaSuccess ||
+        !f1 || !f2)
+      return false;
+    get_cur = reinterpret_cast<FnCtxGetCurrent>(f1);
+    get_id = reinterpret_cast<FnCtxGetId>(f2);
+  }
+  CUcontext ctx = nullptr;
+  if (get_cur(&ctx) != CUDA_SUCCESS) return false;
+  id = 0;
+  return !ctx || get_id(ctx, &id) == CUDA_SUCCESS;
+}
 }  // namespace
 static __device__ __align__(256) EosScratch g_eos_scratch;
 
@@ -1659,19 +1689,24 @@ int cfd3d_eos_eval_noalloc(int fluid, int ngas, int with_prop, int64_t n, const 
   if (n <= 0 || n > CFD3D_EOS_NOALLOC_MAX || !p || !t || !y1 || !y2 || !dv || (fluid != 1 && fluid != 2) ||
       ngas != 1)
     return CFD3D_ERR_ARG;
-  int ndev = 0, dev = 0;
+  int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CFD3D_ERR_NODEVICE;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= EOS_SCRATCH_DEVICES) return CFD3D_ERR_CUDA;
   EosScratch* S = nullptr;
   {
-    // per-device set-up on the first call: the buffer's device address
+    // set-up on the first call in a context: the buffer's device address there
     std::lock_guard<std::mutex> lock(g_eos_scratch_mu);
-    if (!g_eos_scratch_ptr[dev]) {
+    unsigned long long ctx = 0;
+    if (!current_ctx_id(ctx)) return CFD3D_ERR_CUDA;
+    for (const ScratchSlot& sl : g_eos_scratch_slots)
+      if (ctx && sl.ctx == ctx) S = sl.ptr;
+    if (!S) {
+      // (with no context current yet, the lookup makes the device's primary context current)
       void* ptr = nullptr;
       if (cudaGetSymbolAddress(&ptr, g_eos_scratch) != cudaSuccess || !ptr) return CFD3D_ERR_CUDA;
-      g_eos_scratch_ptr[dev] = static_cast<EosScratch*>(ptr);
+      if (!ctx && (!current_ctx_id(ctx) || !ctx)) return CFD3D_ERR_CUDA;
+      S = static_cast<EosScratch*>(ptr);
+      g_eos_scratch_slots.push_back({ctx, S});
     }
-    S = g_eos_scratch_ptr[dev];
   }
   const size_t b = (size_t)n * 8;
   if (cudaMemcpy(S->p, p, b, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1698,8 +1733,13 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   if (!cfg || nblocks < 1 || nblocks > MAXBLK || !blocks) { E.err = "bad arguments"; return CFD3D_ERR_ARG; }
   E.cfg = *cfg;
   if (!make_par(cfg, E.par, E.err)) return CFD3D_ERR_ARG;
+  // descriptor checks that need no device: they fail the same way on a CPU-only host
   for (int b = 0; b < nblocks; ++b) {
     const cfd3d_block_desc& d = blocks[b];
+    if (d.imax < 4 || d.jmax < 4 || d.kmax < 4 || !d.xyz) { E.err = "block too small or no coordinates"; return CFD3D_ERR_DESCRIPTOR; }
+    if (d.nbc < 0 || (d.nbc > 0 && !d.bc) || d.ncon < 0 || (d.ncon > 0 && !d.con)) {
+      E.err = "bad bc or connection list"; return CFD3D_ERR_DESCRIPTOR;
+    }
     for (int q = 0; q < d.nbc; ++q) {
       const int* p = d.bc[q].pnts;
       int nmax[3] = {d.imax, d.jmax, d.kmax}, faces = 0;
@@ -1962,8 +2002,21 @@ int cfd3d_initialize(cfd3d_handle* h, int block, const double* pv_interior) {
   return CFD3D_OK;
 }
 
-int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const double* dv, const double* tv, const double* qq) {
-  if (!h) return CFD3D_ERR_ARG;
+}  // extern "C"
+
+namespace {
+// An upload or download that fails part-way has copies queued that read or write the
+// caller's host arrays: wait for them before returning, so that no copy touches those
+// arrays after the call has returned.
+int drain_on_error(cfd3d_handle* h, int rc) {
+  if (rc != CFD3D_OK) {
+    if (h->cp) cudaStreamSynchronize(h->cp);
+    cudaStreamSynchronize(h->E.st);
+  }
+  return rc;
+}
+
+int upload_state(cfd3d_handle* h, int block, const double* pv, const double* dv, const double* tv, const double* qq) {
   Engine& E = h->E;
   if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
   const BlockGeom& B = E.blk[block];
@@ -2000,8 +2053,7 @@ int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const doubl
   return CFD3D_OK;
 }
 
-int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, double* tv, double* qq, double* rcav) {
-  if (!h) return CFD3D_ERR_ARG;
+int download_state(cfd3d_handle* h, int block, double* pv, double* dv, double* tv, double* qq, double* rcav) {
   Engine& E = h->E;
   if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
   const BlockGeom& B = E.blk[block];
@@ -2042,6 +2094,19 @@ int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, dou
   CFD_CUDA(cudaStreamSynchronize(E.st));
   CFD_CUDA(cudaGetLastError());
   return CFD3D_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const double* dv, const double* tv, const double* qq) {
+  if (!h) return CFD3D_ERR_ARG;
+  return drain_on_error(h, upload_state(h, block, pv, dv, tv, qq));
+}
+
+int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, double* tv, double* qq, double* rcav) {
+  if (!h) return CFD3D_ERR_ARG;
+  return drain_on_error(h, download_state(h, block, pv, dv, tv, qq, rcav));
 }
 
 // ---- checkpoints ----------------------------------------------------------------------

@@ -80,8 +80,9 @@ struct DevPtr {
   Scalars* sc;
   const double* hft;   // heat-flux histories: per table n, t[n], q[n] (GhostOp.pad is its offset)
   const double* grav;  // gravity history: n, t[n], a[3 n] (a constant acceleration is one row)
-  // total-pressure inlets: per patch [tp_off[p], tp_off[p+1]) face entries (boundary cell,
-  // face-vector cell, plane, sign) and the solved (p, T, |u|^2) in tp_x[3 p..]
+  // total-pressure inlets: per pool p (the p-th inlet of every block) [tp_off[p], tp_off[p+1])
+  // face entries (boundary cell, face-vector cell, plane, sign) and the solved (p, T, |u|^2)
+  // in tp_x[3 p..]
   int ntp;
   const int* tp_off;
   const int* tp_ent;     // 4 ints per entry

@@ -416,7 +416,7 @@ struct Bc {
   bool farfield_sign = false;
   bool shifted = false;   // bcshiftedperiodic: copies from 16 cells along i and the face normal
   int hf_off = 0;         // heat-flux wall: offset of its history in the table
-  int tp_index = 0;       // total-pressure inlet: its patch number
+  int tp_index = 0;       // total-pressure inlet: its pool (the patch's number among its block's inlets)
 };
 
 int wall_kind(const Par& c) {
@@ -432,9 +432,15 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
   const Par& c = E.par;
   std::vector<GhostOp> ops[3];
   std::vector<double> hft;   // heat-flux histories
-  std::vector<std::vector<int>> tp_ent;   // total-pressure inlets: per patch 4 ints per face cell
+  // total-pressure inlets: per pool 4 ints per face cell.  The reference reduces each inlet's
+  // averages over the communicator of every rank carrying one (bc_comm_world, icolor 12,
+  // src/bc_module.f90:321,349,3411-3416), and the n-th inlet of each rank meets the others'
+  // n-th in the collective: pool n gathers the n-th total-pressure patch of every block, and
+  // all of its patches take the pool's Newton solution.
+  std::vector<std::vector<int>> tp_ent;
   for (int b = 0; b < nblocks; ++b) {
     const cfd3d_block_desc& d = blocks[b];
+    int tp_ord = 0;
     const BlockGeom& G = E.blk[b];
     const int im = d.imax, jm = d.jmax, km = d.kmax;
     auto gi = [&](int i, int j, int k) -> int {
@@ -484,8 +490,8 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
         }
         case CFD3D_BC_TOTALPRESSURE_IN:
           bi.kind = G_TOTALP; bi.farfield_sign = true;
-          bi.tp_index = (int)tp_ent.size();
-          tp_ent.emplace_back();
+          bi.tp_index = tp_ord++;
+          if ((int)tp_ent.size() <= bi.tp_index) tp_ent.emplace_back();
           break;
         case CFD3D_BC_MASSFLOWRATE_IN: bi.kind = G_MASSFLOW_IN; break;
         case CFD3D_BC_SHIFTED_PERIODIC: bi.kind = G_COPY; bi.shifted = true; break;

@@ -237,16 +237,19 @@ int  cfd3d_eos_eval(int fluid, int ngas, int with_prop, int64_t n, const double 
                     double *tv);
 
 /* cfd3d_eos_eval without any device allocation: the points pass through one static
- * device buffer of CFD3D_EOS_NOALLOC_MAX points (about 0.8 MB, reserved when the library
- * is loaded) instead of cudaMalloc'd arrays.  No counterpart in the reference.  It serves
+ * device buffer of CFD3D_EOS_NOALLOC_MAX points (about 0.8 MB of each context that loads
+ * the library's device code, held until the context ends) instead of cudaMalloc'd arrays.  No counterpart in the reference.  It serves
  * callers that cannot allocate device memory: a caller evaluating a few points while the
  * engine's iterations run on their own stream (cudaFree synchronises the whole device,
  * so cfd3d_eos_eval would wait for them), and a caller whose device memory is taken by
  * a large case or by another allocator's pool (cudaMalloc would fail).  Same arguments
  * and results as cfd3d_eos_eval.  n > CFD3D_EOS_NOALLOC_MAX returns CFD3D_ERR_ARG before
- * any device work.  The first call on a device looks up the buffer's device address, so
- * make it before any stream capture on that device.  All calls on one device share the
- * buffer: calls must not overlap (serialise them across host threads). */
+ * any device work.  The first call in a context (a device's primary context, or a new
+ * one after cudaDeviceReset) looks up the buffer's device address, so make it before any
+ * stream capture there.  Under lazy module loading (the CUDA default) that first call is
+ * also when the buffer is reserved: make it while device memory is still free, or load
+ * modules eagerly (CUDA_MODULE_LOADING=EAGER).  All calls on one device share the buffer:
+ * calls must not overlap (serialise them across host threads). */
 #define CFD3D_EOS_NOALLOC_MAX 4096
 int  cfd3d_eos_eval_noalloc(int fluid, int ngas, int with_prop, int64_t n, const double *p,
                             const double *t, const double *y1, const double *y2, double *dv,

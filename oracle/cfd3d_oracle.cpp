@@ -69,6 +69,8 @@ struct BcInfo {
   double pv[NPV_MAX], dv[NDV], tv[3];
   std::vector<double> tdata, heatflux;   /* HeatFlux walls: the <family>.dat history */
   double time = 0.0;                     /* bcinfo%time, set by setbc */
+  /* total-pressure inlets: the pooled Newton solution (p, T) and |u_avg|^2, set by setbc */
+  double tpx[2] = {0.0, 0.0}, tpuu = 0.0;
 };
 
 struct Conn {
@@ -872,34 +874,38 @@ static void tp_newt(const TpSys& S, double* x) {
   }
 }
 
+/* one total-pressure patch's area-weighted sums over its boundary faces (:3320-3409):
+   pa[0..4] += pv(1..5) dl, pa[5] += dl */
+static void tp_patch_sums(const Block& B, const BcInfo& bi, double* pa) {
+  double nx[3];
+  const int ax = (int)bi.face / 2;
+  for (int k = bi.istart[2]; k <= bi.iend[2]; ++k)
+    for (int j = bi.istart[1]; j <= bi.iend[1]; ++j)
+      for (int i = bi.istart[0]; i <= bi.iend[0]; ++i) {
+        const int idx[3] = {i, j, k};
+        if (idx[ax] != (((int)bi.face % 2 == 0) ? bi.istart[ax] : bi.iend[ax])) continue;
+        int ii = 0, jj = 0, kk = 0;
+        face_cell(bi, const_cast<Block&>(B), i, j, k, ii, jj, kk, nx, true);
+        const double dl = std::sqrt(sq(nx[0]) + sq(nx[1]) + sq(nx[2]));
+        const double* P = const_cast<Block&>(B).pv.at(ii, jj, kk);
+        pa[0] += P[0] * dl;
+        pa[4] += P[4] * dl;
+        for (int m = 1; m <= 3; ++m) pa[m] += P[m] * dl;
+        pa[5] += dl;
+      }
+}
+
+/* The reference reduces the sums over bc_comm_world (mpi_reduce + mpi_bcast, :3411-3416),
+   the communicator of every rank that carries a total-pressure inlet (icolor 12, :321,349),
+   and each rank's n-th inlet meets the others' n-th in the collective.  So pool n holds the
+   n-th total-pressure patch of every block; its averages feed one newt, whose solution all
+   of the pool's patches take. */
+static void tp_solve_pools(Oracle& O);
+
 static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
   double pv[NPV_MAX], dv[NDV], tv[3], pvs[NPV_MAX], dvs[NDV], tvs[3], ppv[NPV_MAX], nx[3];
-  double tpx[2] = {0.0, 0.0}, tpuu = 0.0;
-  if (bi.kind == K_TOTALP) {
-    /* the patch's area-weighted averages over its boundary faces (:3320-3409), then newt */
-    double pa[5] = {0, 0, 0, 0, 0}, area = 0.0;
-    const int ax = (int)bi.face / 2;
-    for (int k = bi.istart[2]; k <= bi.iend[2]; ++k)
-      for (int j = bi.istart[1]; j <= bi.iend[1]; ++j)
-        for (int i = bi.istart[0]; i <= bi.iend[0]; ++i) {
-          const int idx[3] = {i, j, k};
-          if (idx[ax] != (((int)bi.face % 2 == 0) ? bi.istart[ax] : bi.iend[ax])) continue;
-          int ii = 0, jj = 0, kk = 0;
-          face_cell(bi, B, i, j, k, ii, jj, kk, nx, true);
-          const double dl = std::sqrt(sq(nx[0]) + sq(nx[1]) + sq(nx[2]));
-          const double* P = B.pv.at(ii, jj, kk);
-          pa[0] += P[0] * dl;
-          pa[4] += P[4] * dl;
-          for (int m = 1; m <= 3; ++m) pa[m] += P[m] * dl;
-          area += dl;
-        }
-    for (int m = 0; m < 5; ++m) pa[m] /= area;
-    TpSys S{&c, sq(pa[1]) + sq(pa[2]) + sq(pa[3]), (1.0 - c.y2ref) * 1.33 + c.y2ref * 1.4};
-    tpx[0] = pa[0] + bi.pv[0];
-    tpx[1] = pa[4];
-    tpuu = S.uu;
-    tp_newt(S, tpx);
-  }
+  const double* tpx = bi.tpx;
+  const double tpuu = bi.tpuu;
   for (int k = bi.istart[2]; k <= bi.iend[2]; ++k)
     for (int j = bi.istart[1]; j <= bi.iend[1]; ++j)
       for (int i = bi.istart[0]; i <= bi.iend[0]; ++i) {
@@ -1148,7 +1154,39 @@ static void apply_halos(Oracle& O) {
   }
 }
 
+static void tp_solve_pools(Oracle& O) {
+  std::vector<std::vector<double>> sums;
+  for (auto& B : O.b) {
+    size_t n = 0;
+    for (auto& bc : B.bcs) {
+      if (bc.kind != K_TOTALP) continue;
+      if (sums.size() <= n) sums.emplace_back(6, 0.0);
+      tp_patch_sums(B, bc, sums[n].data());
+      ++n;
+    }
+  }
+  std::vector<double> x(2 * sums.size()), uu(sums.size());
+  for (size_t n = 0; n < sums.size(); ++n) {
+    double pa[5];
+    for (int m = 0; m < 5; ++m) pa[m] = sums[n][m] / sums[n][5];
+    TpSys S{&O.c, sq(pa[1]) + sq(pa[2]) + sq(pa[3]), (1.0 - O.c.y2ref) * 1.33 + O.c.y2ref * 1.4};
+    x[2 * n] = pa[0] + O.c.pref;
+    x[2 * n + 1] = pa[4];
+    uu[n] = S.uu;
+    tp_newt(S, &x[2 * n]);
+  }
+  for (auto& B : O.b) {
+    size_t n = 0;
+    for (auto& bc : B.bcs) {
+      if (bc.kind != K_TOTALP) continue;
+      bc.tpx[0] = x[2 * n]; bc.tpx[1] = x[2 * n + 1]; bc.tpuu = uu[n];
+      ++n;
+    }
+  }
+}
+
 static void setbc(Oracle& O) {
+  tp_solve_pools(O);
   for (auto& B : O.b) for (auto& bc : B.bcs) { bc.time = O.time_cur; apply_bc(O.c, B, bc); }
   apply_halos(O);
   for (auto& B : O.b) for (int m = 0; m < 12; ++m) apply_bc(O.c, B, B.edge[m]);

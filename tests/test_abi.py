@@ -56,8 +56,17 @@ def test_create_rejects_bad_config_without_gpu():
 
 
 def test_create_rejects_bad_descriptor_without_gpu():
+    """descriptor validation runs before device selection, so it reports the bad descriptor
+    on a host without a GPU as well"""
     c = cases.make("plain_small", scale=8)
     c["blocks"][0]["bc"].append((abi.BC_WALL, (2, 1, 1, 3, 5, 5)))  # not on a face
     with pytest.raises(native.Cfd3dError) as e:
         native.Engine(c)
-    assert e.value.code in (abi.ERR_DESCRIPTOR, abi.ERR_NODEVICE)
+    assert e.value.code == abi.ERR_DESCRIPTOR
+    c = cases.make("plain_small", scale=8)
+    b = c["blocks"][0]
+    b["xyz"] = b["xyz"][:, :, :3].copy()   # 2 cells along i: fewer than the stencil needs
+    b["imax"] = 3
+    with pytest.raises(native.Cfd3dError) as e:
+        native.Engine(c)
+    assert e.value.code == abi.ERR_DESCRIPTOR

@@ -83,8 +83,10 @@ def _with_heatflux(c):
     return c
 
 
-def _prepared(scale, inout=False, massflow=False, heatflux=False):
+def _prepared(scale, inout=False, massflow=False, heatflux=False, ncav=None):
     c = _state(scale)
+    if ncav is not None:
+        c["cfg"]["ncav"] = ncav
     if inout:
         c = _with_inout(c)
     if massflow:
@@ -126,6 +128,11 @@ def c4_massflow():
 @pytest.fixture(scope="module")
 def c4_heatflux():
     return _prepared(4, heatflux=True)
+
+
+@pytest.fixture(scope="module", params=[2, 3, 4, 5], ids=["kunz", "singhal", "schnerr_sauer", "lee"])
+def c4_model(request):
+    return _prepared(4, ncav=request.param)
 
 
 def _typical(pv, v):
@@ -297,3 +304,37 @@ def test_vjp_through_heatflux_wall(c4_heatflux):
     print(f"heat-flux wall rows: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
     assert used >= len(entries) - 2, rows
     assert errs.max() <= TOL, (errs, rows)
+
+
+def test_vjp_cavitation_models(c4_model):
+    """Kunz, Singhal, Schnerr-Sauer and Lee (src/cav_module.f90:173-357): rows of p, T, y1
+    and y2 in the two bands next to the vapour pressure, where vaporisation and condensation
+    are active, against finite differences of the GPU residual; and the gradients with
+    respect to c_v and c_c against engines built with the perturbed coefficient"""
+    d = c4_model
+    s = d["s"]
+    km, jm, im = d["pv"].shape[:-1]
+    w = max(im // 8, 2)
+    rng = np.random.default_rng(6)
+    entries = [(int(rng.integers(0, km)), int(rng.integers(0, jm)), int(rng.integers(0, 2 * w)), v)
+               for v in (0, 4, 5, 6) for _ in range(4)]
+    used, errs, rows = _check(lambda p: s.residual([p])[0], d, entries)
+    print(f"ncav {d['case']['cfg']['ncav']}: {used}/{len(entries)} entries, max relative error {errs.max():.2e}")
+    assert used >= len(entries) - 2, rows
+    assert errs.max() <= TOL, (errs, rows)
+    c, lam = d["case"], d["lam"]
+    base = d["s"].base[0]
+    for q, name in ((1, "c_v"), (2, "c_c")):
+        x0 = float(c["cfg"][name])
+        h = 1e-6 * abs(x0)
+        r = []
+        for sgn in (1.0, -1.0):
+            cfg = dict(c["cfg"])
+            cfg[name] = x0 + sgn * h
+            e2 = _engine(c, cfg)
+            e2.upload(0, pv=base["pv"], dv=base["dv"], tv=base["tv"], qq=base["qq"] if e2.nqq else None)
+            r.append(e2.residual(0)["res"])
+            e2.close()
+        fd = float(np.sum(lam * (r[0] - r[1])) / (2.0 * h))
+        ga = d["gpar"][q]
+        assert abs(fd - ga) <= TOL * max(abs(fd), abs(ga), 1e-12 * np.abs(d["g"]).max()), (name, fd, ga)

@@ -185,3 +185,28 @@ def test_totalpressure_inlet_matches(oracle, base):
     assert field_err(sg["pv"][3:-3, 3:-3, :3], so["pv"][3:-3, 3:-3, :3]).max() < TOL_STATE
     with pytest.raises(native.Cfd3dError):
         e.residual_vjp([np.zeros(abi.interior_shape(c["blocks"][0], e.npv))])
+
+
+def test_totalpressure_inlet_pooled_over_blocks(oracle):
+    """a total-pressure inlet on the k face of the SST case split in two along i: one pooled
+    reduction and Newton solve for both blocks' patches (the reference's communicator of
+    every rank carrying the inlet)"""
+    name, kw, over = BASES["sst"]
+    c = cases.make(name, **kw)
+    c["cfg"].update(over)
+    c = replace_faces(cases.split_i(c, 2), {"kmin": abi.BC_TOTALPRESSURE_IN})
+    e = native.Engine(c)
+    o = oracle.Oracle(c)
+    e.initialize(c["pv0"])
+    o.initialize(c["pv0"])
+    for b in range(2):
+        assert field_err(e.residual(b)["res"], o.residual(b)["res"]).max() < TOL_RES
+    for it in range(3):
+        _, resg, _ = e.iterate(1, it + 1, 0.0)
+        _, reso, _ = o.iterate(1, it + 1, 0.0)
+        assert np.all(np.isfinite(resg))
+        assert np.allclose(resg, reso, rtol=1e-7, atol=1e-9 * np.abs(reso).max()), (it, resg, reso)
+    for b in range(2):
+        sg, so = e.download(b), o.get_state(b)
+        assert field_err(interior(sg["pv"]), interior(so["pv"])).max() < TOL_STATE
+        assert field_err(sg["pv"][:3, 3:-3, 3:-3], so["pv"][:3, 3:-3, 3:-3]).max() < TOL_STATE

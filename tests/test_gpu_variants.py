@@ -1,0 +1,232 @@
+"""GPU parity of the scheme variants against the CPU oracle, through the C ABI.
+
+Covers the variants that the main parity cases do not select:
+  * the five cavitation models (ncav 1-5: Merkle, Kunz, Singhal, Schnerr-Sauer, Lee;
+    src/cav_module.f90:136-357), whose Singhal and Lee forms evaluate the surface tension
+    and the saturation temperature on the device (src/eos_module.f90:2340-2354,2430-2439);
+  * all eleven limiters (nlim 0-10, src/muscl_module.f90:292-413) under TVD and MLP
+    reconstruction;
+  * the three preconditioning speeds (prec 0, 1, 2; src/flux_module.f90:643-671), prec 2
+    with str = L / pi / dt_phy above the reference speed so that its branch is taken;
+  * the BDF1 and BDF2 history shift over three physical steps (src/solve_module.f90:155-183);
+  * full iterations with the stiffened-water EOS (fluid = 1);
+  * the plain configuration at its stated 64x32x32 for its stated 100 iterations, and the
+    cavitating configuration at its stated 128x64x64.
+Tolerances are those of the main parity tests (the FP64 engine contracts multiply-adds and
+re-associates the IF97 sums, so it is not bit-identical to the oracle), normalised by each
+field's maximum.
+"""
+import numpy as np
+import pytest
+
+from cfd3d_gb300 import cases, native
+from tests.helpers import field_err, interior
+
+pytestmark = pytest.mark.gpu
+
+TOL_RES = 1e-9
+TOL_STATE = 1e-9
+# the plain configuration after its 100 iterations: the per-cell bound of the CPU
+# restatement's parity target
+TOL_STATE_C1 = 1e-10
+
+
+def _make(base, kw, over):
+    c = cases.make(base, **kw)
+    c["cfg"].update(over)
+    return c
+
+
+def _pair(c):
+    e = native.Engine(c)
+    from oracle import oracle_py
+    o = oracle_py.Oracle(c)
+    e.initialize(c["pv0"])
+    o.initialize(c["pv0"])
+    return e, o
+
+
+def _residual_parity(e, o, c):
+    for b in range(len(c["blocks"])):
+        rg, ro = e.residual(b), o.residual(b)
+        assert np.all(np.isfinite(ro["res"]))
+        err = field_err(rg["res"], ro["res"]).max()
+        assert err < TOL_RES, err
+        if c["cfg"].get("ncav", 0):
+            assert field_err(rg["icav"], ro["icav"]).max() < TOL_RES
+        if c["cfg"].get("iturb", -3) == 0:
+            assert field_err(rg["itt"], ro["itt"]).max() < TOL_RES
+
+
+def _state_err(e, o, c, fields=("pv", "dv", "tv", "rcav")):
+    worst = 0.0
+    for b in range(len(c["blocks"])):
+        sg, so = e.download(b), o.get_state(b)
+        for f in fields:
+            if f == "tv" and not e.ntv:
+                continue
+            if f == "rcav":
+                if not c["cfg"].get("ncav", 0):
+                    continue
+                worst = max(worst, field_err(sg[f], so[f]).max())
+                continue
+            worst = max(worst, field_err(interior(sg[f]), interior(so[f])).max())
+    return worst
+
+
+def _iterate_parity(e, o, c, nit=3, nt_phy=1, tol=TOL_STATE):
+    for it in range(nit):
+        tg, resg, _ = e.iterate(nt_phy, it + 1, 0.0)
+        to, reso, _ = o.iterate(nt_phy, it + 1, 0.0)
+        assert np.all(np.isfinite(reso)), (it, reso)
+        assert abs(tg - to) <= 1e-9 * abs(to)
+        assert np.allclose(resg, reso, rtol=1e-7, atol=1e-9 * np.abs(reso).max()), (it, resg, reso)
+    err = _state_err(e, o, c)
+    assert err < tol, err
+    return err
+
+
+# ---------------------------------------------------------------- cavitation models
+@pytest.mark.parametrize("ncav", [1, 2, 3, 4, 5])
+def test_cavitation_model_residual(ncav):
+    """the reference's clamp (indexed by temperature): residual, icav"""
+    c = _make("cavitating", dict(scale=8), dict(ncav=ncav))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+
+
+@pytest.mark.parametrize("ncav", [1, 2, 3, 4, 5])
+def test_cavitation_model_iterations(ncav):
+    """three iterations with the intended clamp (the reference's drives Singhal and Lee to
+    NaN within two iterations from this start, in the oracle as on the GPU): state and
+    the phase-change rates rcav"""
+    c = _make("cavitating", dict(scale=8, fix_cav_clamp=1), dict(ncav=ncav))
+    e, o = _pair(c)
+    _iterate_parity(e, o, c)
+
+
+@pytest.mark.parametrize("ncav", [2, 4])
+def test_cavitation_model_iterations_reference_clamp(ncav):
+    """Kunz and Schnerr-Sauer stay finite under the reference's own clamp"""
+    c = _make("cavitating", dict(scale=8), dict(ncav=ncav))
+    e, o = _pair(c)
+    _iterate_parity(e, o, c)
+
+
+@pytest.mark.parametrize("ncav", [2, 3, 4, 5])
+def test_cavitation_model_sst_bdf2(ncav):
+    """each model inside the SST + BDF2 configuration of the large case"""
+    c = _make("large", dict(scale=16), dict(fix_cav_clamp=1, ncav=ncav))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+# ---------------------------------------------------------------- limiters
+@pytest.mark.parametrize("nlim", list(range(11)))
+def test_limiter_tvd(nlim):
+    c = _make("plain_small", dict(scale=4), dict(nmuscl=1, nlim=nlim))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+@pytest.mark.parametrize("nlim", list(range(11)))
+def test_limiter_mlp(nlim):
+    """MLP on the cavitating state (vapour-fraction and pressure jumps at the bubble)"""
+    c = _make("cavitating", dict(scale=8, fix_cav_clamp=1), dict(nmuscl=2, nlim=nlim))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+# ---------------------------------------------------------------- preconditioning
+def test_prec0_no_preconditioning():
+    """no_prec: sndp2 = c^2.  At M ~ 0.01 the unpreconditioned system only tolerates a
+    small CFL; three iterations at CFL 0.5 stay finite."""
+    c = _make("plain_small", dict(scale=4), dict(prec=0, cfl=0.5))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+def test_prec2_unsteady_bdf1():
+    """unsteady_prec with BDF1: dt_phy = 5 ms gives str = L / pi / dt_phy = 127 m/s, above
+    uref = 10 m/s, so sndp2 = min(c^2, str^2) in most cells"""
+    c = _make("plain_small", dict(scale=4), dict(prec=2, nsteady=1, dt_phy=5e-3))
+    e, o = _pair(c)
+    assert o.refs()["str"] > 10.0 * c["cfg"]["uref"]
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+def test_prec2_unsteady_large_bdf2():
+    """unsteady_prec in the large case's SST + cavitation + BDF2 configuration"""
+    c = _make("large", dict(scale=16), dict(fix_cav_clamp=1, prec=2))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+# ---------------------------------------------------------------- BDF history shift
+@pytest.mark.parametrize("nsteady", [1, 2])
+def test_bdf_shift_over_physical_steps(nsteady):
+    """three physical steps of three pseudo-iterations, the history shifted after each
+    (k_unsteady_shift against the oracle's unsteadyupdate): state and qq after each step"""
+    c = _make("large", dict(scale=16), dict(fix_cav_clamp=1, nsteady=nsteady))
+    e, o = _pair(c)
+    for step in range(1, 4):
+        for it in range(3):
+            tg, resg, _ = e.iterate(step, it + 1, 0.0)
+            to, reso, _ = o.iterate(step, it + 1, 0.0)
+            assert np.allclose(resg, reso, rtol=1e-7, atol=1e-9 * np.abs(reso).max()), (step, it, resg, reso)
+        e.unsteady_shift()
+        o.unsteady_shift()
+        sg, so = e.download(0), o.get_state(0)
+        assert field_err(interior(sg["pv"]), interior(so["pv"])).max() < TOL_STATE
+        qg, qo = sg["qq"], so["qq"]
+        assert qg.shape == qo.shape
+        assert np.any(qo != 0.0)
+        assert field_err(qg, qo).max() < TOL_STATE, (step, field_err(qg, qo))
+
+
+# ---------------------------------------------------------------- stiffened water
+def test_stiffened_water_iterations():
+    c = _make("plain_small", dict(scale=4), dict(fluid=1))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+def test_stiffened_water_cavitating_iterations():
+    c = _make("cavitating", dict(scale=8, fix_cav_clamp=1), dict(fluid=1))
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    _iterate_parity(e, o, c)
+
+
+# ---------------------------------------------------------------- stated sizes
+def test_plain_stated_size_100_iterations():
+    """the plain configuration as stated: 64x32x32 cells, Roe, TVD minmod, 100 LU-SGS
+    iterations; the per-cell state error after the last one"""
+    c = cases.make("plain_small")
+    assert c["iterations"] == 100
+    e, o = _pair(c)
+    for it in range(c["iterations"]):
+        e.iterate(1, it + 1, 0.0)
+        o.iterate(1, it + 1, 0.0)
+    err = _state_err(e, o, c)
+    print(f"plain 64x32x32, 100 iterations: max per-cell state error {err:.3e}")
+    assert err < TOL_STATE_C1, err
+
+
+def test_cavitating_stated_size():
+    """the cavitating configuration as stated, 128x64x64 cells: the residual with the
+    reference's clamp, then three iterations with the intended clamp"""
+    c = cases.make("cavitating")
+    e, o = _pair(c)
+    _residual_parity(e, o, c)
+    c2 = cases.make("cavitating", fix_cav_clamp=1)
+    e2, o2 = _pair(c2)
+    err = _iterate_parity(e2, o2, c2)
+    print(f"cavitating 128x64x64, 3 iterations: max per-cell state error {err:.3e}")

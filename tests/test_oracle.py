@@ -120,6 +120,34 @@ def test_multiblock_split_matches_single_block_residual(oracle):
     assert err.max() < 1e-12, err
 
 
+def test_totalpressure_inlet_pooled_across_blocks(oracle):
+    """A total-pressure inlet on a k face split over two blocks: the reference reduces its
+    averages over every rank carrying the inlet (one communicator), so the split case
+    reproduces the single block's residual next to the inlet, not per-block averages."""
+    from cfd3d_gb300.abi import BC_TOTALPRESSURE_IN
+    single = cases.make("large", scale=16)
+    single["cfg"].update(fix_cav_clamp=1, nsteady=0)
+    for b in single["blocks"]:
+        im, jm, km = b["imax"], b["jmax"], b["kmax"]
+        b["bc"] = [(BC_TOTALPRESSURE_IN if tuple(p) == (1, 1, 1, im, jm, 1) else k, p) for k, p in b["bc"]]
+    split = cases.split_i(single, 2)
+    assert sum(k == BC_TOTALPRESSURE_IN for b in split["blocks"] for k, _ in b["bc"]) == 2
+    o1 = oracle.Oracle(single)
+    o1.initialize(single["pv0"])
+    o2 = oracle.Oracle(split)
+    o2.initialize(split["pv0"])
+    r1 = o1.residual(0)["res"]
+    r2 = np.concatenate([o2.residual(0)["res"], o2.residual(1)["res"]], axis=2)
+    # away from the split's own halo seam: cells next to the inlet (k = 0) included
+    ia = split["blocks"][0]["imax"] - 1
+    core = np.ones(r1.shape[2], dtype=bool)
+    core[ia - 2:ia + 2] = False
+    core[:2] = core[-2:] = False
+    scale = np.maximum(np.abs(r1).max(axis=(0, 1, 2)), 1e-300)
+    err = np.abs(r1[:-2, 2:-2, core] - r2[:-2, 2:-2, core]).max(axis=(0, 1, 2)) / scale
+    assert err.max() < 1e-10, err
+
+
 def test_golden_fixtures(oracle):
     """The oracle reproduces its committed golden vectors (regression pin)."""
     g = np.load(os.path.join(GOLDEN, "eos_points.npz"))
