@@ -2,33 +2,39 @@
 
 A step is one pseudo-iteration (update%timeinteg + resi%residual of kwonhwi1/3dcode,
 src/solve_module.f90:134-136) over the whole synthetic workload.  The default workload is
-the large turbulent cavitating case: 384x192x192 cells (14.16 M), stretched wall grid,
-k-omega SST, IAPWS water/vapour with Merkle cavitation, BDF2 dual time.
+the large turbulent cavitating case as stated: 384x192x192 cells (14.16 M), stretched wall
+grid, k-omega SST, IAPWS water/vapour with Merkle cavitation, BDF2 dual time with the
+unsteady preconditioning speed (prec = 2), decomposed along i into 16 blocks -- the
+reference's MPI decomposition with one block per rank (src/grid_module.f90:95-116), which
+the CPU arm runs with one block per host thread.  Both arms run the same blocks, so the
+same block-Jacobi LU-SGS operator.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
-                  [--case large] [--impl gb300|reference]
+                  [--case large] [--blocks 16] [--impl gb300|reference]
 
 value      device-resident throughput: K graph replays timed with CUDA events on the
            engine's stream; the working set (~20 GB) is far larger than L2, so no flush.
-e2e        the same metric through the C ABI as a Fortran caller that owns its arrays would
-           use it: each step uploads pv/dv/tv/qq from pinned host buffers, iterates, and
-           downloads pv/dv/tv (host<->device copies inside the timed region).
-roofline   algorithmic bytes per cell-iteration (persisted pv/dv/tv, metrics, LU-SGS
-           intermediates, BDF history, rcav; 1040 B for this case) x cells / time, against
-           the measured HBM copy bandwidth; per-stage times come from an event-instrumented
-           iteration.
-cpu_baseline  the CPU oracle (C++ FP64 restatement of the reference) on a bounded sample
-           of the same workload (the case at 1/2 resolution), cut into one block per host
-           thread -- the reference's MPI decomposition, one rank per core.
+e2e        the same metric through the C ABI as a Fortran caller that keeps the state on
+           the host would use it: each step uploads pv and the BDF history qq from pinned
+           host buffers (dv and tv follow on the device from the EOS and the eddy
+           viscosity, cfd3d_upload_primitives), iterates, and downloads pv, dv and tv
+           (host<->device copies inside the timed region).
+roofline   the whole pseudo-iteration: algorithmic bytes per cell-iteration (persisted
+           pv/dv/tv, metrics, LU-SGS intermediates, BDF history, rcav; 1040 B for this
+           case) x cells / time, against the measured HBM copy bandwidth; beside it the
+           residual kernel k_rhs alone and the measured FP64 peak (cfd3d_fp64_peak).
+cpu_baseline  the CPU oracle (C++ FP64 restatement of the reference, its speed build) on a
+           bounded sample of the same workload: the same 16 blocks, two iterations, one
+           block per host thread.
 N > 1      replicas: one independent engine per GPU (the case does not shard without
            changing the block-Jacobi operator); barrier + max over ranks; value is the sum.
 """
 import argparse
+import concurrent.futures as cf
 import json
 import os
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
@@ -38,6 +44,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mcell-iter/s per GB300, mixed vs FP64 form at stated error; % HBM peak"
 UNIT = "Mcell-iter/s"
+
+# The large case's unsteady preconditioning (prec = 2, str = L / pi / dt_phy = 477 m/s)
+# diverges at CFL 2 within a few pseudo-iterations from this synthetic start, in the CPU
+# restatement as on the GPU, from the cells next to the far-field inflow; CFL 0.05 keeps it
+# stable and converging.
+LARGE_CFL = 0.05
+
+# DRAM bytes per cell of one k_rhs launch, dram__bytes_read.sum + dram__bytes_write.sum
+# of an ncu capture of the mixed form on the large case at 1/2 resolution (1769472 cells),
+# divided by the cells; the capture grows in proportion to the cells
+RHS_TRAFFIC_PER_CELL = (2.300200e9 + 3.388917e9) / 1769472
 
 
 def algorithmic_bytes(cfg):
@@ -64,12 +81,6 @@ def rhs_bytes(cfg, mixed):
         rd += 4 * 5 + 4 * (9 + 2)
     wr = 8 * npv + 8 * 66 + (4 * 34 if mixed else 0) + 8 * (4 + 4 + 1 + 2)
     return rd + wr
-
-
-# DRAM traffic of k_rhs per cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum)
-# on the large case at 1/2 resolution, mixed form: 2.300 GB + 3.389 GB over 1769472 cells
-# (profiles/k_rhs_large_half_mixed.md); it grows with the cell count
-RHS_TRAFFIC_PER_CELL = (2.300200e9 + 3.388917e9) / 1769472
 
 
 def measured_peaks():
@@ -145,91 +156,115 @@ def host_threads():
         return os.cpu_count() or 1
 
 
-def reference_sample(case_name, scale, threads):
-    """The CPU oracle on the workload at 1/scale resolution, cut into `threads` blocks
-    along i and run one block per thread: the reference's MPI decomposition, one rank per
-    host core."""
+def workload(name, scale=1, blocks=1, cfl=None):
+    """The benchmark case: the named configuration (the intended cavitation clamp; the
+    reference's temperature-indexed one diverges from a cavitating start), the large case
+    with its stated unsteady preconditioning, cut along i into `blocks` blocks."""
     from cfd3d_gb300 import cases
-    from oracle import oracle_py
-    c = cases.make(case_name, scale=scale)
+    c = cases.make(name, scale=scale)
     c["cfg"]["fix_cav_clamp"] = 1
-    if threads > 1 and len(c["blocks"]) == 1:
-        c = cases.split_i(c, threads)
+    if name == "large":
+        c["cfg"]["prec"] = 2
+        c["cfg"]["cfl"] = LARGE_CFL
+    if cfl is not None:
+        c["cfg"]["cfl"] = cfl
+    if blocks > 1 and len(c["blocks"]) == 1:
+        c = cases.split_i(c, blocks)
+    return c
+
+
+def describe(c, ncell):
+    cfg = c["cfg"]
+    return (f"{c['name']}: {ncell} cells in {len(c['blocks'])} blocks, prec={cfg.get('prec')}, cfl={cfg.get('cfl')}, "
+            f"nsteady={cfg.get('nsteady', 0)}, iturb={cfg.get('iturb')}, ncav={cfg.get('ncav', 0)}")
+
+
+def oracle_sample(c, threads):
+    """The CPU oracle's speed build on the case, one block per host thread (the reference's
+    MPI ranks); the blocks are initialised in parallel (ctypes releases the interpreter)."""
+    from oracle import oracle_py
     nb = len(c["blocks"])
-    o = oracle_py.Oracle(c, threads=min(threads, nb))
-    o.initialize(c["pv0"])
-    return o, cases.total_cells(c), nb
+    o = oracle_py.Oracle(c, threads=min(threads, nb), fast=True)
+
+    def init(n):
+        o._L.orc_initialize(o.h, n, oracle_py._p(np.ascontiguousarray(c["pv0"][n], dtype=np.float64)))
+
+    with cf.ThreadPoolExecutor(max(1, min(threads, nb))) as ex:
+        list(ex.map(init, range(nb)))
+    return o
 
 
-def cpu_baseline(case_name, scale, threads, iters=2):
-    """Oracle throughput on a bounded sample of the same workload."""
-    o, ncell, nb = reference_sample(case_name, scale, threads)
+def cpu_baseline(c, ncell, threads, iters=2):
+    """Oracle throughput on a bounded sample of the same workload: the same blocks, a few
+    pseudo-iterations."""
+    o = oracle_sample(c, threads)
     o.iterate(1, 1, 0.0)
     t0 = time.perf_counter()
     for it in range(iters):
         o.iterate(1, it + 2, 0.0)
     dt = time.perf_counter() - t0
+    nb = len(c["blocks"])
     return {"value": ncell * iters / dt / 1e6, "unit": UNIT, "cores": min(threads, nb), "kind": "port",
-            "sample": f"{case_name} at 1/{scale} resolution ({ncell} cells) in {nb} blocks, {iters} "
-                      f"pseudo-iterations, CPU oracle (C++ FP64 restatement of the reference), one block "
-                      f"per thread, {dt:.2f} s"}
+            "sample": f"{describe(c, ncell)}; {iters} pseudo-iterations after 1 untimed, CPU oracle (C++ FP64 "
+                      f"restatement of the reference, -O3 build), one block per thread, {dt:.2f} s"}
 
 
 def run_reference(args):
-    """--impl reference: the reference's algorithm on the host cores (CPU oracle), the
-    workload at 1/ref_scale resolution decomposed over all host threads."""
+    """--impl reference: the reference's algorithm on the host cores (the CPU oracle's
+    speed build) on the GPU arm's workload, one block per host thread; one untimed
+    iteration warms the caches (the GPU arm's warm-up iterations build graphs and tune
+    launch shapes, which the CPU has no counterpart of)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
+    from cfd3d_gb300 import cases
     threads = args.ref_threads or host_threads()
-    o, ncell, nb = reference_sample(args.case, args.ref_scale, threads)
-    for w in range(args.warmup):
+    c = workload(args.case, args.scale, args.blocks, args.cfl)
+    ncell = cases.total_cells(c)
+    o = oracle_sample(c, threads)
+    for w in range(min(args.warmup, 1)):
         o.iterate(1, w + 1, 0.0)
     t0 = time.perf_counter()
     for s in range(args.steps):
-        o.iterate(1, args.warmup + s + 1, 0.0)
+        o.iterate(1, s + 2, 0.0)
     dt = time.perf_counter() - t0
     value = ncell * args.steps / dt / 1e6
-    cores = min(threads, nb)
+    cores = min(threads, len(c["blocks"]))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.case} at 1/{args.ref_scale} resolution ({ncell} cells) in {nb} blocks",
-                   "cells": ncell},
+        "config": {"workload": describe(c, ncell), "cells": ncell, "blocks": len(c["blocks"])},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.case} at 1/{args.ref_scale} resolution, {nb} blocks along i, "
-                                   f"{args.steps} pseudo-iterations per run, CPU oracle (C++ FP64 restatement), "
-                                   f"one block per thread = one reference MPI rank per core"},
+                         "sample": f"the whole workload every step ({args.steps} pseudo-iterations after "
+                                   f"{min(args.warmup, 1)} untimed), CPU oracle (C++ FP64 restatement, -O3 "
+                                   f"build), one block per thread = one reference MPI rank per core"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
-def fp64_form(case, res_mixed, steps, ncell, ws):
-    """The plain all-FP64 form on the same workload: its throughput, and the error of the
-    mixed form's residual on the initial state, max over cells of |R_mixed - R_fp64|
-    divided by the largest |R_fp64| of the same variable and block."""
-    from cfd3d_gb300 import abi, native
-    e64 = native.Engine(case, precision=abi.FP64)
-    e64.initialize(case["pv0"])
-    err = 0.0
-    per_var = None
-    for n, rm in enumerate(res_mixed):
-        r64 = e64.residual(n)["res"]
-        sc = np.maximum(np.abs(r64).max(axis=(0, 1, 2)), 1e-300)
-        ev = (np.abs(rm - r64) / sc).max(axis=(0, 1, 2))
-        per_var = ev if per_var is None else np.maximum(per_var, ev)
-    err = float(per_var.max())
-    for w in range(2):
-        e64.iterate(1, w + 1, 0.0)
-    ms = e64.time_iterate(steps) / steps
-    e64.close()
-    return {"fp64_form": {"value": ws * ncell / ms / 1e3, "ms_per_step": ms, "steps": steps},
-            "mixed_residual_error": {"max": err, "per_variable": [float(x) for x in per_var],
-                                     "definition": "max over cells of |R_mixed - R_fp64| / max |R_fp64|, "
-                                                   "per variable and block, initial state"}}
+def residual_error(res_a, res_b):
+    """max over cells of |R_a - R_b| / max |R_b|, per variable (max over blocks)"""
+    per = None
+    for ra, rb in zip(res_a, res_b):
+        sc = np.maximum(np.abs(rb).max(axis=(0, 1, 2)), 1e-300)
+        ev = (np.abs(ra - rb) / sc).max(axis=(0, 1, 2))
+        per = ev if per is None else np.maximum(per, ev)
+    return per
+
+
+def field_error(emx, e64, nblocks):
+    """max over interior cells of |pv_mixed - pv_fp64| / max |pv_fp64|, per variable"""
+    per = None
+    for n in range(nblocks):
+        a = emx.download(n)["pv"][3:-3, 3:-3, 3:-3]
+        b = e64.download(n)["pv"][3:-3, 3:-3, 3:-3]
+        sc = np.maximum(np.abs(b).max(axis=(0, 1, 2)), 1e-300)
+        ev = (np.abs(a - b) / sc).max(axis=(0, 1, 2))
+        per = ev if per is None else np.maximum(per, ev)
+    return per
 
 
 def combine_ranks(ms_step, ncell, dist=None):
@@ -251,6 +286,72 @@ def pinned(shape):
     return t, t.numpy().reshape(shape)
 
 
+def run_e2e(eng, case, steps, it0):
+    """The drop-in mode: per step, pv and qq up from pinned host memory (dv, tv derived on
+    the device), one iteration, pv, dv, tv down.  Returns (ms per step, H2D, D2H bytes)."""
+    import torch
+    bufs = []
+    h2d = d2h = 0
+    for n in range(len(case["blocks"])):
+        st = eng.download(n)
+        keep = {}
+        for k in ("pv", "dv", "tv", "qq"):
+            if (k == "qq" and not eng.nqq) or (k == "tv" and eng.ntv == 0):
+                continue
+            t, a = pinned(np.ascontiguousarray(st[k]).shape)
+            a[...] = st[k]
+            keep[k] = (t, a)
+            if k in ("pv", "qq"):
+                h2d += a.nbytes
+            if k != "qq":
+                d2h += a.nbytes
+        bufs.append(keep)
+    d2h += 8 * eng.npv   # the residual norms
+
+    def step(s):
+        for n, keep in enumerate(bufs):
+            eng.upload_primitives(n, keep["pv"][1], keep["qq"][1] if "qq" in keep else None)
+        eng.iterate(1, it0 + s, 0.0)
+        for n, keep in enumerate(bufs):
+            eng.download_arrays(n, pv=keep["pv"][1], dv=keep["dv"][1], tv=keep["tv"][1] if "tv" in keep else None)
+
+    step(0)                                   # untimed: first touch of the pinned pages
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(steps):
+        step(s + 1)
+    return (time.perf_counter() - t0) / steps * 1e3, h2d, d2h
+
+
+def batched_leg(args):
+    """The 24 uneven blocks (~12 M cells) of the batched configuration in one launch per
+    stage: mixed form, its per-iteration roofline, and the plain FP64 form beside it."""
+    from cfd3d_gb300 import abi, cases, native
+    c = workload("batched")
+    ncell = cases.total_cells(c)
+    eng = native.Engine(c, precision=abi.MIXED)
+    eng.initialize(c["pv0"])
+    for w in range(3):
+        eng.iterate(1, w + 1, 0.0)
+    shapes = eng.autotune(3) if not args.no_autotune else None
+    ms = eng.time_iterate(args.batched_steps) / args.batched_steps
+    eng.close()
+    e64 = native.Engine(c, precision=abi.FP64)
+    e64.initialize(c["pv0"])
+    for w in range(2):
+        e64.iterate(1, w + 1, 0.0)
+    ms64 = e64.time_iterate(3) / 3
+    e64.close()
+    peak, _ = measured_peaks()
+    bpc = algorithmic_bytes(c["cfg"])
+    gbs = ncell * bpc / (ms * 1e-3) / 1e9
+    return {"workload": describe(c, ncell), "cells": ncell, "blocks": len(c["blocks"]),
+            "value": ncell / ms / 1e3, "ms_per_step": ms, "steps": args.batched_steps,
+            "roofline": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "bytes_per_cell": bpc},
+            "fp64_form": {"value": ncell / ms64 / 1e3, "ms_per_step": ms64, "steps": 3},
+            "launch_shapes": None if shapes is None else list(shapes)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -258,14 +359,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--case", default="large")
     ap.add_argument("--scale", type=int, default=1)
+    ap.add_argument("--blocks", type=int, default=16,
+                    help="blocks along i (the reference's MPI decomposition); both arms run them")
+    ap.add_argument("--cfl", type=float, default=None)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--fp64-steps", type=int, default=5,
+    ap.add_argument("--fp64-steps", type=int, default=3,
                     help="iterations of the plain FP64 form timed beside the mixed form (0 skips)")
+    ap.add_argument("--field-iters", type=int, default=20,
+                    help="iterations after which the mixed form's state is compared with the FP64 form's (0 skips)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ref-scale", type=int, default=2,
-                    help="the CPU samples run the workload at 1/ref-scale resolution")
     ap.add_argument("--ref-threads", type=int, default=0, help="host threads of the CPU samples (0: all)")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--batched-steps", type=int, default=10, help="timed iterations of the 24-block leg (0 skips)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     args = ap.parse_args()
@@ -281,14 +386,14 @@ def main():
         dist.init_process_group("gloo")
     from cfd3d_gb300 import abi, cases, native
     native.set_device(local)
-    case = cases.make(args.case, scale=args.scale)
-    case["cfg"]["fix_cav_clamp"] = 1
+    case = workload(args.case, args.scale, args.blocks, args.cfl)
     cfg = case["cfg"]
+    nb = len(case["blocks"])
     prec = abi.MIXED if args.precision == "mixed" else abi.FP64
     eng = native.Engine(case, precision=prec)
     eng.initialize(case["pv0"])
     ncell = cases.total_cells(case)
-    res0 = [eng.residual(n)["res"] for n in range(len(case["blocks"]))] if prec == abi.MIXED else None
+    res0 = [eng.residual(n)["res"] for n in range(nb)] if prec == abi.MIXED else None
     for w in range(args.warmup):
         eng.iterate(1, w + 1, 0.0)
     shapes = eng.autotune(3) if not args.no_autotune else None
@@ -299,83 +404,79 @@ def main():
     ms_step, value = combine_ranks(ms / args.steps, ncell, dist)
     stats = eng.stats()
     prof = eng.profile_iterate()
-    # ---- end to end through the C ABI with pinned host buffers
-    blocks = case["blocks"]
-    bufs = []
-    h2d = d2h = 0
-    for n, b in enumerate(blocks):
-        st = eng.download(n)
-        keep = {}
-        for k in ("pv", "dv", "tv", "qq"):
-            if k == "qq" and not eng.nqq:
-                continue
-            arr = st[k] if k != "tv" else st["tv"]
-            if k == "tv" and eng.ntv == 0:
-                continue
-            t, a = pinned(np.ascontiguousarray(arr).shape)
-            a[...] = arr
-            keep[k] = (t, a)
-            h2d += a.nbytes
-            if k != "qq":
-                d2h += a.nbytes
-        bufs.append(keep)
-    d2h += 8 * eng.npv
-    import torch
-
-    def e2e_step(s):
-        for n, keep in enumerate(bufs):
-            eng.upload(n, pv=keep["pv"][1], dv=keep["dv"][1], tv=keep["tv"][1] if "tv" in keep else None,
-                       qq=keep["qq"][1] if "qq" in keep else None)
-        eng.iterate(1, args.warmup + s + 1, 0.0)
-        for n, keep in enumerate(bufs):
-            eng.download_arrays(n, pv=keep["pv"][1], dv=keep["dv"][1], tv=keep["tv"][1] if "tv" in keep else None)
-
-    e2e_step(0)                                   # untimed: first touch of the pinned pages
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s in range(args.e2e_steps):
-        e2e_step(s + 1)
-    e2e_ms, e2e_value = combine_ranks((time.perf_counter() - t0) / args.e2e_steps * 1e3, ncell, dist)
+    it_next = args.warmup + args.steps + 2
+    e2e = None
+    if args.e2e_steps > 0:
+        e2e_ms, h2d, d2h = run_e2e(eng, case, args.e2e_steps, it_next)
+        e2e_ms, e2e_value = combine_ranks(e2e_ms, ncell, dist)
+        e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": e2e_ms, "steps": args.e2e_steps}
     if rank != 0:
         dist.barrier()
         return 0
+    fp64_tflops = native.fp64_peak(1.0)
     peak, peak_kind = measured_peaks()
     bpc = algorithmic_bytes(cfg)
     achieved_it = ncell * bpc / (ms_step * 1e-3) / 1e9
-    # the dominant kernel: k_rhs (the 'residual' stage is that one launch), timed with CUDA
+    # the residual kernel k_rhs (the 'residual' stage is that one launch), timed with CUDA
     # events on the engine's stream by profile_iterate
     rb = rhs_bytes(cfg, prec == abi.MIXED)
     rhs_ms = prof["residual"]
-    achieved = ncell * rb / (rhs_ms * 1e-3) / 1e9
+    achieved_rhs = ncell * rb / (rhs_ms * 1e-3) / 1e9
     total_stage = sum(prof.values())
     dominant = max(prof, key=prof.get)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == abi.FP64 else "f32+f64", "data": "synthetic",
-        "config": {"workload": f"{args.case}: {ncell} cells, SST + IAPWS + Merkle, BDF2, LU-SGS",
-                   "cells": ncell, "precision": args.precision, "blocks": len(blocks),
+        "config": {"workload": describe(case, ncell), "cells": ncell, "precision": args.precision, "blocks": nb,
                    "l2": "working set >> 129 MB L2 (no flush needed)", "parallelism": "replicas" if ws > 1 else "1 GPU",
                    "launch_shapes": None if shapes is None else {"face_threads": shapes[0], "rhs_threads": shapes[1],
                                                                  "sweep_ctas_per_sm": shapes[2]}},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind,
-                     "traffic": RHS_TRAFFIC_PER_CELL * ncell if prec == abi.MIXED else None,
-                     "kernel": "k_rhs (residual, sources, sweep records)", "kernel_ms": rhs_ms,
-                     "algorithmic_bytes_per_cell": rb,
-                     "note": "FP64-pipe bound, not HBM bound: see the ncu summaries",
-                     "iteration": {"achieved": achieved_it, "frac": achieved_it / peak,
-                                   "bytes_per_cell": bpc, "dominant_stage": dominant,
-                                   "dominant_share": prof[dominant] / total_stage, "stage_ms": prof}},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved_it, "peak": peak, "unit": "GB/s", "frac": achieved_it / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "scope": "whole pseudo-iteration: algorithmic bytes per cell-iteration x cells / ms_per_step",
+                     "bytes_per_cell": bpc, "dominant_stage": dominant,
+                     "dominant_share": prof[dominant] / total_stage, "stage_ms": prof,
+                     "kernel": {"name": "k_rhs (residual, sources, sweep records)", "achieved": achieved_rhs,
+                                "frac": achieved_rhs / peak, "kernel_ms": rhs_ms, "algorithmic_bytes_per_cell": rb,
+                                "traffic": RHS_TRAFFIC_PER_CELL * ncell if prec == abi.MIXED else None},
+                     "fp64": {"peak_tflops": fp64_tflops,
+                              "peak_kind": "measured: cfd3d_fp64_peak, independent DFMA chains, 1 s"}},
+        "e2e": e2e,
         "gpu_launches": stats["launches_per_iter"] * args.steps,
         "clocks": clk.summary(),
     }
-    if prec == abi.MIXED and args.fp64_steps > 0:
-        line.update(fp64_form(case, res0, args.fp64_steps, ncell, ws))
-        line["speedup_vs_fp64"] = value / line["fp64_form"]["value"]
+    if prec == abi.MIXED and (args.fp64_steps > 0 or args.field_iters > 0):
+        e64 = native.Engine(case, precision=abi.FP64)
+        e64.initialize(case["pv0"])
+        err = residual_error(res0, [e64.residual(n)["res"] for n in range(nb)])
+        line["mixed_residual_error"] = {
+            "max": float(err.max()), "per_variable": [float(x) for x in err],
+            "definition": "max over cells of |R_mixed - R_fp64| / max |R_fp64|, per variable and block, initial state"}
+        if args.fp64_steps > 0:
+            for w in range(2):
+                e64.iterate(1, w + 1, 0.0)
+            ms64 = e64.time_iterate(args.fp64_steps) / args.fp64_steps
+            line["fp64_form"] = {"value": ws * ncell / ms64 / 1e3, "ms_per_step": ms64, "steps": args.fp64_steps}
+            line["speedup_vs_fp64"] = value / line["fp64_form"]["value"]
+        if args.field_iters > 0:
+            eng.initialize(case["pv0"])
+            e64.initialize(case["pv0"])
+            for it in range(args.field_iters):
+                eng.iterate(1, it + 1, 0.0)
+                e64.iterate(1, it + 1, 0.0)
+            ferr = field_error(eng, e64, nb)
+            line["mixed_field_error"] = {
+                "max": float(ferr.max()), "per_variable": [float(x) for x in ferr], "iterations": args.field_iters,
+                "definition": "max over interior cells of |pv_mixed - pv_fp64| / max |pv_fp64|, per variable, "
+                              "after the stated pseudo-iterations from the same initial state"}
+        e64.close()
+    eng.close()
+    if args.batched_steps > 0 and args.case == "large" and args.scale == 1:
+        line["batched"] = batched_leg(args)
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.case, args.ref_scale, args.ref_threads or host_threads())
+        line["cpu_baseline"] = cpu_baseline(case, ncell, args.ref_threads or host_threads())
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

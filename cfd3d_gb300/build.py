@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcfd3d_gb300.so")
-UNITS = ["adjoint_face.cu", "adjoint.cu", "engine.cu", "setup.cu", "flux.cu", "flux_mixed.cu"]
+UNITS = ["adjoint_face.cu", "adjoint.cu", "engine.cu", "setup.cu", "flux.cu", "flux_mixed.cu", "peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include")]

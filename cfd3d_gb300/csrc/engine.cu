@@ -68,7 +68,9 @@ __global__ void k_eos_points(int fluid, int with_prop, long long n, const double
 // ------------------------------------------------------------------ initial state
 // set_others (src/initial_module.f90:707-771) on the uploaded interior pv
 template <bool MX>
-__global__ void k_init(DevPtr d, Par c, int b) {
+// fresh = 0 (cfd3d_upload_primitives): dv and tv(1:2) only; the eddy viscosity follows
+// from k_eddy and the history and rates are the caller's
+__global__ void k_init(DevPtr d, Par c, int b, int fresh) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const BlockGeom& B = d.blk[b];
   if (t >= (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1)) return;
@@ -79,8 +81,12 @@ __global__ void k_init(DevPtr d, Par c, int b) {
   for (int v = 0; v < c.npv; ++v) pv[v] = d.pv[v * n + g];
   if (MX) deteos_split(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
   else deteos<false>(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
-  if (c.iturb >= -1) tv[2] = c.emutref;
   for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
+  if (!fresh) {
+    for (int v = 0; v < c.ntv && v < 2; ++v) d.tv[v * n + g] = tv[v];
+    return;
+  }
+  if (c.iturb >= -1) tv[2] = c.emutref;
   for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
   if (c.nqq) {
     double q[NPVM];
@@ -913,33 +919,67 @@ __device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long 
   }
 }
 
+// Mixed form: since D^-1 is linear, a sweep's dq splits into the cell's own part, in FP64,
+// and D^-1 applied to the neighbours' FP32 products, in FP32:
+//   forward   dq* = D^-1 (res + sum A+ dq*)   = x0 + D^-1 (sum A+ dq*),   x0 = D^-1 res
+//   backward  dq  = D^-1 (dcv - sum A- dq)    = dq* + D^-1 (- sum A- dq)   (D^-1 dcv = dq*)
+// The own part does not wait for the neighbours, so only FP32 work stays on the sweep's
+// dependency chain; the FP64 form applies D^-1 to the full right-hand side as lhs%getx does.
+template <bool FWD>
+__device__ __forceinline__ void mx_own(const DevPtr& d, const Par& c, long long t, const double* o, const double* pv,
+                                       const double* dv, double* x0) {
+  const long long nint = d.nint;
+  const int npv = c.npv;
+  for (int v = 0; v < NPVM; ++v) x0[v] = 0.0;
+  if (FWD) {
+    double res[NPVM];
+    for (int v = 0; v < NPVM; ++v) res[v] = (v < npv) ? d.rec[(REC_RES + v) * nint + t] : 0.0;
+    Diag D;
+    diag_from_array(o, D);
+    diag_solve(c, D, pv, dv, res, x0);
+  } else {
+    for (int v = 0; v < npv; ++v) x0[v] = d.dqs[v * nint + t];   // the forward sweep's dq*
+  }
+}
+__device__ __forceinline__ void mx_corr(const Par& c, const double* o, const double* pv, const double* dv,
+                                        const float* an, float* y) {
+  DiagT<float> D;
+  diag_from_array(o, D);
+  float pf[NPVM], df[14];
+  for (int v = 0; v < NPVM; ++v) { pf[v] = (float)pv[v]; y[v] = 0.0f; }
+  for (int v = 0; v < 14; ++v) df[v] = (float)dv[v];
+  diag_solve_t<float>(c, D, pf, df, an, y);
+}
+
 // one cell of a sweep: its three neighbours' products, the closed-form D^-1, dq
 template <bool FWD, bool MX, bool CG>
 __device__ __forceinline__ void sweep_cell(const DevPtr& d, const Par& c, long long t) {
   const long long nint = d.nint;
   const double* R = d.rec;
   const int npv = c.npv;
-  double acc[NPVM];
-  for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
-  if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
-  else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
-  if (MX) {
-    float an[NPVM];
-    for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
-    sweep_neighbours<FWD, float, CG>(d, npv, t, d.recf, d.dqsf, an);
-    for (int v = 0; v < npv; ++v) acc[v] += (double)an[v];
-  } else {
-    sweep_neighbours<FWD, double, CG>(d, npv, t, R, d.dqs, acc);
-  }
-  if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
   double pv[NPVM], dv[14], o[PREP_DIAG];
   rec_state<double>(R, nint, t, pv, dv);
   for (int q = 0; q < PREP_DIAG; ++q) o[q] = R[(REC_DIAG + q) * nint + t];
-  Diag D;
-  diag_from_array(o, D);
   double x[NPVM];
   for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
-  diag_solve(c, D, pv, dv, acc, x);
+  if (MX) {
+    mx_own<FWD>(d, c, t, o, pv, dv, x);
+    float an[NPVM], y[NPVM];
+    for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
+    sweep_neighbours<FWD, float, CG>(d, npv, t, d.recf, d.dqsf, an);
+    mx_corr(c, o, pv, dv, an, y);
+    for (int v = 0; v < npv; ++v) x[v] += (double)y[v];
+  } else {
+    double acc[NPVM];
+    for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
+    if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
+    else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
+    sweep_neighbours<FWD, double, CG>(d, npv, t, R, d.dqs, acc);
+    if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
+    Diag D;
+    diag_from_array(o, D);
+    diag_solve(c, D, pv, dv, acc, x);
+  }
   for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
   if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
 }
@@ -1036,17 +1076,22 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
     const int ch = FWD ? q : d.nchunk - 1 - q;
     const long long t = d.chunk_t0[ch] + threadIdx.x;
     const bool live = t < d.chunk_t0[ch + 1];
-    // ---- loads that do not wait: own record, neighbour records, the needed chunks
+    // ---- work that does not wait: own record (and in the mixed form the cell's own part
+    // of dq), neighbour records, the needed chunks
     SweepNb<T> nbs[3];
     double acc[NPVM], pv[NPVM], dv[14], o[PREP_DIAG];
     int lo = 0x7fffffff, hi = -1;
     if (live) {
       const double* R = d.rec;
-      for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
-      if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
-      else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
       rec_state<double>(R, nint, t, pv, dv);
       for (int k = 0; k < PREP_DIAG; ++k) o[k] = R[(REC_DIAG + k) * nint + t];
+      if constexpr (MX) {
+        mx_own<FWD>(d, c, t, o, pv, dv, acc);
+      } else {
+        for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
+        if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
+        else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
+      }
       for (int k = 0; k < 3; ++k) {
         sweep_nb_load<FWD, T>(d, t, k, RN, nbs[k]);
         if (nbs[k].nb >= 0) {
@@ -1076,20 +1121,22 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
     }
     __syncthreads();
     if (live) {
+      double x[NPVM];
       if constexpr (MX) {
-        float an[NPVM];
+        // acc holds the own part; the neighbours' FP32 contribution through an FP32 D^-1
+        float an[NPVM], y[NPVM];
         for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
         for (int k = 0; k < 3; ++k) sweep_nb_apply<FWD, float>(d, npv, nbs[k], DQ, an);
-        for (int v = 0; v < npv; ++v) acc[v] += (double)an[v];
+        mx_corr(c, o, pv, dv, an, y);
+        for (int v = 0; v < NPVM; ++v) x[v] = acc[v] + (double)y[v];
       } else {
         for (int k = 0; k < 3; ++k) sweep_nb_apply<FWD, double>(d, npv, nbs[k], DQ, acc);
+        if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
+        Diag D;
+        diag_from_array(o, D);
+        for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
+        diag_solve(c, D, pv, dv, acc, x);
       }
-      if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
-      Diag D;
-      diag_from_array(o, D);
-      double x[NPVM];
-      for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
-      diag_solve(c, D, pv, dv, acc, x);
       for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
       if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
     }
@@ -1205,9 +1252,9 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
 
 // MX: FP32, with the velocity gradients formed from u - U (exact differences)
 template <bool MX>
-__global__ void k_eddy(DevPtr d, Par c) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= d.nint) return;
+__global__ void k_eddy(DevPtr d, Par c, long long t0, long long t1) {
+  long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= t1) return;
   int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
   const BlockGeom& B = d.blk[b];
   long long g = interior_cell(B, t - B.int_off, i, j, k);
@@ -1466,8 +1513,8 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
       ++n;
       if (m == nstage) stage(7);
       if (c.iturb >= -1) {
-        if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
-        else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+        if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c, 0, E.nint);
+        else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c, 0, E.nint);
         ++n;
       }
     }
@@ -1515,8 +1562,8 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   ++n;
   stage(7);
   if (c.iturb >= -1) {
-    if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
-    else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c);
+    if (c.mixed) k_eddy<true><<<nblk_of(E.nint, T), T, 0, s>>>(d, c, 0, E.nint);
+    else k_eddy<false><<<nblk_of(E.nint, T), T, 0, s>>>(d, c, 0, E.nint);
     ++n;
   }
   k_finish<<<1, FIN_T, 0, s>>>(d, c, E.red_grid);
@@ -1791,7 +1838,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   };
   if (c.mixed)
     ok = ok && allocf(E.d.pvf, c.npv) && allocf(E.d.fi32, 3 * c.npv) && allocf(E.d.fv32, (c.iturb == -3) ? 1 : 3 * c.npv) &&
-         allocf(E.d.frec, 2 * 12);
+         allocf(E.d.frec, 2 * 12) && alloc(E.d.lqd, 2) && allocf(E.d.lqf, 6);
   else
     ok = ok && alloc(E.d.fi, 3 * c.npv) && alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
   if (!ok) { E.err = "device allocation failed"; return CFD3D_ERR_NOMEM; }
@@ -1926,9 +1973,9 @@ void cfd3d_destroy(cfd3d_handle* h) {
   Engine& E = h->E;
   if (E.graph) cudaGraphExecDestroy(E.graph);
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
-                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
+                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging, E.d.lqd};
   for (double* p : bufs) cudaFree(p);
-  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf, E.d.gmlo};
+  float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf, E.d.gmlo, E.d.lqf};
   for (float* p : fbufs) cudaFree(p);
   cudaFree((void*)E.d.blk);
   cudaFree(E.d.sc);
@@ -1990,8 +2037,8 @@ int cfd3d_initialize(cfd3d_handle* h, int block, const double* pv_interior) {
   if (rc) return rc;
   CFD_CUDA(cudaMemcpyAsync(h->staging, src, (size_t)nint * c.npv * 8, cudaMemcpyHostToDevice, E.st));
   k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, c.npv, B, E.d.pv, E.ncell, 1);
-  if (c.mixed) k_init<true><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block);
-  else k_init<false><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block);
+  if (c.mixed) k_init<true><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block, 1);
+  else k_init<false><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block, 1);
   CFD_CUDA(cudaStreamSynchronize(E.st));
   CFD_CUDA(cudaGetLastError());
   // reset the solution-time accumulator of the local time step
@@ -2107,6 +2154,28 @@ int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const doubl
 int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, double* tv, double* qq, double* rcav) {
   if (!h) return CFD3D_ERR_ARG;
   return drain_on_error(h, download_state(h, block, pv, dv, tv, qq, rcav));
+}
+
+int cfd3d_upload_primitives(cfd3d_handle* h, int block, const double* pv, const double* qq) {
+  if (!h) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (!pv) { E.err = "pv is required"; return CFD3D_ERR_ARG; }
+  int rc = drain_on_error(h, upload_state(h, block, pv, nullptr, nullptr, qq));
+  if (rc) return rc;
+  // dv, tv(1:2) by the EOS of the update, then tv(3) by its eddy viscosity (which reads
+  // the block's ghost pv as uploaded: those of the boundary program before the update)
+  const BlockGeom& B = E.blk[block];
+  const Par& c = E.par;
+  const long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  if (c.mixed) k_init<true><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block, 0);
+  else k_init<false><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, block, 0);
+  if (c.iturb >= -1 && c.ntv >= 3) {
+    if (c.mixed) k_eddy<true><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, B.int_off, B.int_off + nint);
+    else k_eddy<false><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, B.int_off, B.int_off + nint);
+  }
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  return CFD3D_OK;
 }
 
 // ---- checkpoints ----------------------------------------------------------------------

@@ -93,6 +93,12 @@ struct DevPtr {
   float* gmf;        // mixed form: FP32 copy of gm (metrics of the FP32 viscous and SST terms)
   float* gmlo;       // mixed form: low parts of the face vectors, gm = gmf + gmlo (df64 terms)
   float* frec;       // mixed form: reconstructed face states of one direction (2 x 12 planes)
+  // mixed form: per padded cell, the liquid phase of its EOS state, the base of the face
+  // states' first-order expansion (k_shadow): lqd = (1/rho_l, h_l) in FP64 (1/rho_l = 0:
+  // the cell carries vapour, no base); lqf = d(1/rho_l)/dp, d(1/rho_l)/dT, dh_l/dp,
+  // dh_l/dT and the rounding of the FP32 shadow's p and T (exact - shadow)
+  double* lqd;
+  float* lqf;
   // LU-SGS sweep records in plane-major order t (REC_* planes of nint entries); dqs and
   // dcv are plane-major too
   double* rec;

@@ -1,8 +1,11 @@
 // flux_mixed.cu -- face fluxes of the mixed-precision form (CFD3D_MIXED).
 //
-//   k_shadow          FP32 gauge shadow pvf of every padded cell, after the boundary program
-//   k_recon_mx<DIR>   per face: MUSCL / MLP on pvf, clips, face-state rho and h (df64 IF97
-//                     sums, FP64 mixture), written to the face record frec
+//   k_shadow          FP32 gauge shadow pvf of every padded cell, after the boundary program,
+//                     and the liquid base of the cell's EOS state (lqd / lqf)
+//   k_recon_mx<DIR>   per face: MUSCL / MLP on pvf, clips, face-state rho and h (FP64
+//                     mixture of phases from df64 IF97 sums, or for a vapour-free state
+//                     near its cell the liquid by first-order expansion), written to the
+//                     face record frec
 //   k_flux_mx<DIR>    per face: FP32 Roe-average sound speed, inviscid flux with FP64
 //                     leading-order terms, FP32 viscous flux; stores F - Phi.n dl in FP32
 // Splitting reconstruction + EOS from the flux keeps each kernel's code within the
@@ -14,21 +17,71 @@
 
 namespace cfd {
 
+// Per padded cell: the FP32 gauge shadow, and the liquid base of the cell's EOS state for
+// the face states' expansion.  With y1 = 0 the mixture holds only liquid and gas, so the
+// liquid's 1/rho and h follow from dv: 1/rho_l = 1/dv(3), h_l = h - y2 (h_g - h_l), and its
+// derivatives d(1/rho_l)/d(p, T) = -drho_l/d(p, T) / rho_l^2, dh_l/dp = dh/dp / (1 - y2)
+// (the gas's h does not depend on p) and dh_l/dT = (dh/dT - y2 cp_g) / (1 - y2).
 __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c) {
   const long long n = d.ncell;
-  const long long total = n * c.npv;
   const long long stride = (long long)gridDim.x * blockDim.x;
+  const int npv = c.npv;
   const double off[NPVM] = {0.0, c.uref_vec[0], c.uref_vec[1], c.uref_vec[2], c.tref, 0.0, 0.0, 0.0, 0.0};
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += stride) {
-    const int v = (int)(q / n);
-    d.pvf[q] = (float)(d.pv[q] - off[v]);
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += stride) {
+    float sh[NPVM];
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      if (v < npv) {
+        sh[v] = (float)(d.pv[v * n + g] - off[v]);
+        d.pvf[v * n + g] = sh[v];
+      }
+    }
+    double il = 0.0, hl = 0.0;
+    float q[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const double y1 = d.pv[5 * n + g], rl = d.dv[2 * n + g];
+    if (c.fluid == 2 && y1 == 0.0 && rl > 0.0) {
+      const double y2 = d.pv[6 * n + g];
+      il = 1.0 / rl;
+      hl = d.dv[n + g] - y2 * d.dv[13 * n + g];
+      const float ilf = (float)il, iyl = 1.0f / (1.0f - (float)y2);
+      q[0] = -(float)d.dv[16 * n + g] * ilf * ilf;
+      q[1] = -(float)d.dv[17 * n + g] * ilf * ilf;
+      q[2] = (float)d.dv[10 * n + g] * iyl;
+      q[3] = ((float)d.dv[11 * n + g] - (float)y2 * 1004.64f) * iyl;
+      q[4] = (float)(d.pv[g] - (double)sh[0]);
+      q[5] = (float)((d.pv[4 * n + g] - c.tref) - (double)sh[4]);
+    }
+    d.lqd[g] = il;
+    d.lqd[n + g] = hl;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) d.lqf[m * n + g] = q[m];
   }
 }
 
-// face of direction DIR for thread t: left cell g and the stencil strides
+// The liquid's 1/rho and h at a face state (gauge shadow x) by first-order expansion about
+// its base cell b (shadow xb).  The expansion's error stays below the FP32 storage of the
+// face's rho - rhoref and h - href when |dp| <= 2e4 Pa and |dT| <= 0.02 K (the second
+// derivatives of IF97 region 1 near 300 K: d2rho/dp2 ~ rho kappa^2, d2rho/dT2 ~ -0.01
+// kg/m^3/K^2, d2h/dp2 ~ -v kappa, dcp/dT ~ -0.3 J/kg/K^2).  Returns false -- the caller
+// evaluates the IF97 sums -- when the base carries vapour or the state is farther away.
+__device__ __forceinline__ bool liquid_expand(const DevPtr& d, long long b, const float* x, const float* xb, double& il,
+                                              double& hl) {
+  const long long n = d.ncell;
+  const double il0 = d.lqd[b];
+  if (il0 == 0.0) return false;
+  const float dp = (x[0] - xb[0]) - d.lqf[4 * n + b];
+  const float dt = (x[4] - xb[4]) - d.lqf[5 * n + b];
+  if (!(fabsf(dp) <= 2.0e4f && fabsf(dt) <= 0.02f)) return false;
+  il = il0 + (double)(d.lqf[b] * dp + d.lqf[n + b] * dt);
+  hl = d.lqd[n + b] + (double)(d.lqf[2 * n + b] * dp + d.lqf[3 * n + b] * dt);
+  return true;
+}
+
+// face of direction DIR for thread t: left cell g, the stencil strides, and whether the
+// left and right cells are interior cells
 struct FaceIdx {
   long long g, sn, s1, s2;
-  bool ok;
+  bool ok, lin, rin;
 };
 template <int DIR>
 __device__ __forceinline__ FaceIdx face_of(const DevPtr& d, long long t) {
@@ -49,6 +102,9 @@ __device__ __forceinline__ FaceIdx face_of(const DevPtr& d, long long t) {
   int k = (int)(r / fj) + (DIR == 2 ? 1 : 2);
   const long long si = 1, sj = B.ni, sk = (long long)B.ni * B.nj;
   f.g = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
+  const int fn = (DIR == 0) ? i : (DIR == 1 ? j : k), nmax = (DIR == 0) ? B.imax : (DIR == 1 ? B.jmax : B.kmax);
+  f.lin = fn >= 2;
+  f.rin = fn + 1 <= nmax;
   if (DIR == 0) { f.sn = si; f.s1 = sj; f.s2 = sk; }
   else if (DIR == 1) { f.sn = sj; f.s1 = sk; f.s2 = si; }
   else { f.sn = sk; f.s1 = si; f.s2 = sj; }
@@ -77,8 +133,16 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
     muscl_clip_mx(c, c9, c10, gl, gR);
     const double pl = c.pref + (double)gl[0], tl = c.tref + (double)gl[4];
     const double pr = c.pref + (double)gR[0], tr = c.tref + (double)gR[4];
-    eos_rho_h<true>(c.fluid, pl, tl, gl[5], gl[6], rl, hl);
-    eos_rho_h<true>(c.fluid, pr, tr, gR[5], gR[6], rr, hr);
+    // a vapour-free face state next to its interior base cell: the liquid by expansion
+    double il, hll;
+    if (f.lin && gl[5] == 0.0f && liquid_expand(d, g, gl, c9, il, hll))
+      mix_face_mx(pl, tl, 0.0, gl[6], il, hll, 0.0, 0.0, rl, hl);
+    else
+      eos_rho_h<true>(c.fluid, pl, tl, gl[5], gl[6], rl, hl);
+    if (f.rin && gR[5] == 0.0f && liquid_expand(d, gr, gR, c10, il, hll))
+      mix_face_mx(pr, tr, 0.0, gR[6], il, hll, 0.0, 0.0, rr, hr);
+    else
+      eos_rho_h<true>(c.fluid, pr, tr, gR[5], gR[6], rr, hr);
     if (c.nscheme == 2 || c.nscheme == 3) {
       cl = eos_c2_f(c.fluid, (float)pl, (float)tl, gl[5], gl[6], &d.sc->snd2_fallbacks);
       cr = eos_c2_f(c.fluid, (float)pr, (float)tr, gR[5], gR[6], &d.sc->snd2_fallbacks);

@@ -402,19 +402,25 @@ __device__ __forceinline__ void deteos_simple(int fluid, double p, double t, dou
 
 // mixture density and static enthalpy only: all that the Roe and AUSM+-up fluxes read of
 // the reconstructed face states; the same operations as the rho, h of deteos_simple
+// the mixed form's face mixture from the phases' 1/rho and h: the gas's reciprocal as
+// t / (p r1) in df64, the mixture sums and its one reciprocal in FP64
+__device__ __forceinline__ void mix_face_mx(double p, double t, double y1, double y2, double il, double hl, double iv,
+                                            double hv, double& rho, double& h) {
+  const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
+  const double yl = 1.0 - y1 - y2;
+  rho = 1.0 / (yl * il + y1 * iv + y2 * ig);
+  h = yl * hl + y1 * hv + y2 * (1004.64 * t);
+}
+
 template <bool MX = false>
 __device__ __forceinline__ void eos_rho_h(int fluid, double p, double t, double y1, double y2, double& rho, double& h) {
   if constexpr (MX) {
     if (fluid != 1) {
-      // phase reciprocals in df64 (the gas's as t / (p r1)); the mixture sums and its one
-      // reciprocal in FP64
+      // phase reciprocals in df64
       double il, hl, iv = 0.0, hv = 0.0;
       if (y1 != 0.0) iapws_inv_df64<true>(p, t, p > h2o_pww(t), &il, &hl, &iv, &hv);
       else iapws_inv_df64<false>(p, t, false, &il, &hl, &iv, &hv);
-      const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
-      const double yl = 1.0 - y1 - y2;
-      rho = 1.0 / (yl * il + y1 * iv + y2 * ig);
-      h = yl * hl + y1 * hv + y2 * (1004.64 * t);
+      mix_face_mx(p, t, y1, y2, il, hl, iv, hv, rho, h);
       return;
     }
   }
@@ -505,6 +511,13 @@ __device__ __forceinline__ double nsub(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ float nmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float nadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float nsub(float a, float b) { return __fsub_rn(a, b); }
+// quotients of the reconstruction: IEEE division in FP64 (the reference's arithmetic), the
+// hardware's fast reciprocal-based quotient (2 ulp) in the mixed form's FP32 (a correctly
+// rounded FP32 division is a long instruction sequence, and the reconstruction's several
+// per variable swell the face kernel beyond the instruction cache)
+template <class R>
+__device__ __forceinline__ R rdiv(R a, R b) { return a / b; }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
 
 template <class R>
 __device__ __forceinline__ R limiter(int nlim, R r, R r1, R r2, R alp) {
@@ -513,16 +526,16 @@ __device__ __forceinline__ R limiter(int nlim, R r, R r1, R r2, R alp) {
     case 0: return R(1);
     case 1: return fmax(R(0), fmin(R(1), r));
     case 2: return fmax(fmax(R(0), fmin(R(1), alp * r)), fmin(alp, r));
-    case 3: c = (r + fabs(r)) / (R(1) + fabs(r)); return fmax(R(0), fmin(fmin(alp, alp * r), c));
-    case 4: c = (R(1) + r) / R(2); return fmax(R(0), fmin(fmin(alp, alp * r), c));
-    case 5: c = nadd(nmul(r, r), r) / nadd(R(1), nmul(r, r)); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
+    case 3: c = rdiv(r + fabs(r), R(1) + fabs(r)); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 4: c = rdiv(R(1) + r, R(2)); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 5: c = rdiv(nadd(nmul(r, r), r), nadd(R(1), nmul(r, r))); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
     case 6: c = fmin(R(1.5), alp); return fmax(fmax(R(0), fmin(c * r, R(1))), fmin(r, c));
-    case 7: c = nadd(R(1), nmul(R(2), r)) / R(3); return fmax(R(0), fmin(fmin(alp, alp * r), c));
+    case 7: c = rdiv(nadd(R(1), nmul(R(2), r)), R(3)); return fmax(R(0), fmin(fmin(alp, alp * r), c));
     case 8:
-      c = nsub(nadd(nadd(nmul(R(-2), r1), R(11)), nmul(R(24), r)), nmul(R(3), r2)) / R(30);
+      c = rdiv(nsub(nadd(nadd(nmul(R(-2), r1), R(11)), nmul(R(24), r)), nmul(R(3), r2)), R(30));
       return fmax(R(0), fmin(fmin(alp, alp * r), c));
-    case 9: return nadd(R(1), nmul(R(2), r)) / R(3);
-    default: return nsub(nadd(nadd(nmul(R(-2), r1), R(11)), nmul(R(24), r)), nmul(R(3), r2)) / R(30);
+    case 9: return rdiv(nadd(R(1), nmul(R(2), r)), R(3));
+    default: return rdiv(nsub(nadd(nadd(nmul(R(-2), r1), R(11)), nmul(R(24), r)), nmul(R(3), r2)), R(30));
   }
 }
 
@@ -534,16 +547,16 @@ __device__ __forceinline__ void muscl_var(const Par& c, const R* x, R& xl, R& xr
   R dqm1 = x[22] - x[36];
   R dqp = x[31] - x[9];
   R dqp1 = x[37] - x[31];
-  R dqmm = R(1) / (dqm + eps);
+  R dqmm = rdiv(R(1), dqm + eps);
   R r0 = dq * dqmm, r10 = dqm1 * dqmm, r20 = dqp * dqmm;
-  R dqpp = R(1) / (dqp + eps);
+  R dqpp = rdiv(R(1), dqp + eps);
   R r1 = dq * dqpp, r11 = dqp1 * dqpp, r21 = dqm * dqpp;
   R alp0 = R(2), alp1 = R(2);
   if (c.nmuscl == 2) {
-    R rxy_l = fabs((x[10] - x[6]) / (x[9] - x[22] + eps));
-    R rxz_l = fabs((x[14] - x[2]) / (x[9] - x[22] + eps));
-    R rxy_r = fabs((x[11] - x[7]) / (x[31] - x[8] + eps));
-    R rxz_r = fabs((x[15] - x[3]) / (x[31] - x[8] + eps));
+    R rxy_l = fabs(rdiv(x[10] - x[6], x[9] - x[22] + eps));
+    R rxz_l = fabs(rdiv(x[14] - x[2], x[9] - x[22] + eps));
+    R rxy_r = fabs(rdiv(x[11] - x[7], x[31] - x[8] + eps));
+    R rxz_r = fabs(rdiv(x[15] - x[3], x[31] - x[8] + eps));
     // min/max over the 3x3 planes: A = cells 0..17 (both face sides), L = i-1 plane (18..26),
     // R = i+2 plane (27..35); "even" = the 9 cells of the left side (0,2,..,16), "odd" right side
     R mA = x[0], MA = x[0], mE = x[0], ME = x[0], mO = x[1], MO = x[1];
@@ -567,9 +580,9 @@ __device__ __forceinline__ void muscl_var(const Par& c, const R* x, R& xl, R& xr
     else if (x[31] - x[8] > R(0)) { qmax = fmax(MO, MR); qmin = mA; }
     else { qmin = fmin(mO, mR); qmax = MA; }
     R qmr = fmin(fabs(qmax - x[9]), fabs(qmin - x[9]));
-    alp0 = R(2) * fmax(R(1), r0) / (fabs(dq) + eps) / (R(1) + rxy_l + rxz_l) * qml;
-    if (fabs(dq) <= eps) alp1 = R(2) * fmax(R(1), dqp / eps) * fabs(dqpp) / (R(1) + rxy_r + rxz_r) * qmr;
-    else alp1 = R(2) * fmax(R(1), R(1) / r1) * fabs(dqpp) / (R(1) + rxy_r + rxz_r) * qmr;
+    alp0 = rdiv(rdiv(R(2) * fmax(R(1), r0), fabs(dq) + eps), R(1) + rxy_l + rxz_l) * qml;
+    if (fabs(dq) <= eps) alp1 = rdiv(R(2) * fmax(R(1), rdiv(dqp, eps)) * fabs(dqpp), R(1) + rxy_r + rxz_r) * qmr;
+    else alp1 = rdiv(R(2) * fmax(R(1), rdiv(R(1), r1)) * fabs(dqpp), R(1) + rxy_r + rxz_r) * qmr;
     alp0 = fmax(R(1), fmin(R(2), alp0));
     alp1 = fmax(R(1), fmin(R(2), alp1));
   }
@@ -1203,10 +1216,13 @@ __device__ __forceinline__ void getx_explicit(const Par& c, const double* pv, co
   for (int v = 0; v < c.npv; ++v) x[v] *= a;
 }
 
-// everything of lhs%getx that does not depend on the right-hand side
-struct Diag {
-  double a, b1, i_b1, ss, rr, cross, cross1, cross2, ssy1, ssy2, ssh, aaa1, aaa2, mm, c[4], tt, t[4];
+// everything of lhs%getx that does not depend on the right-hand side (R = float: the mixed
+// form's sweeps apply it to the neighbours' FP32 contribution)
+template <class R>
+struct DiagT {
+  R a, b1, i_b1, ss, rr, cross, cross1, cross2, ssy1, ssy2, ssh, aaa1, aaa2, mm, c[4], tt, t[4];
 };
+using Diag = DiagT<double>;
 
 // evis = eigenvis_of(c, dv, tv), which the caller also needs
 // lam_fs (optional): the spectral radius lamda and the face-vector sum fs formed by the
@@ -1283,14 +1299,15 @@ __device__ __forceinline__ void diag_spectral_f(const Par& c, const float* pv, f
 }
 
 // x = D^-1 res (lhs%getx)
-__device__ __forceinline__ void diag_solve(const Par& c, const Diag& D, const double* pv, const double* dv,
-                                           const double* res, double* x) {
-  const double* C4 = D.c;
-  double uuu = res[1] * pv[1] + res[2] * pv[2] + res[3] * pv[3] - res[4];
-  double coeff1 = res[0] * D.aaa1 + dv[8] * uuu + D.cross * res[6];
-  double coeff2 = res[0] * D.aaa2 + dv[7] * uuu + D.cross2 * res[6];
-  double coeff3 = res[0] * (D.ssh - D.ssy2 * pv[6]) + dv[0] * D.rr * uuu + res[6] * D.ssy2;
-  double r6 = res[6] - res[0] * pv[6];
+template <class R>
+__device__ __forceinline__ void diag_solve_t(const Par& c, const DiagT<R>& D, const R* pv, const R* dv, const R* res,
+                                             R* x) {
+  const R* C4 = D.c;
+  R uuu = res[1] * pv[1] + res[2] * pv[2] + res[3] * pv[3] - res[4];
+  R coeff1 = res[0] * D.aaa1 + dv[8] * uuu + D.cross * res[6];
+  R coeff2 = res[0] * D.aaa2 + dv[7] * uuu + D.cross2 * res[6];
+  R coeff3 = res[0] * (D.ssh - D.ssy2 * pv[6]) + dv[0] * D.rr * uuu + res[6] * D.ssy2;
+  R r6 = res[6] - res[0] * pv[6];
   x[0] = (C4[3] * D.cross1 * (res[0] * pv[6] - res[6]) - C4[1] * coeff1 + C4[2] * coeff2 +
           dv[0] * D.b1 * (coeff2 + D.cross1 * res[5] - D.cross1 * pv[5] * res[0])) * D.mm;
   x[1] = (res[1] - res[0] * pv[1]) * D.i_b1;
@@ -1301,12 +1318,16 @@ __device__ __forceinline__ void diag_solve(const Par& c, const Diag& D, const do
   x[5] = (D.ss * (res[5] - res[0] * pv[5]) - C4[3] * D.ss * D.i_b1 * r6 - C4[0] * coeff2 + C4[1] * D.i_b1 * coeff3) * D.mm;
   x[6] = r6 * D.i_b1;
   if (c.npv > 7) {
-    double bd = D.b1 * dv[0];
-    double r7 = res[7] - res[0] * pv[7], r8 = res[8] - res[0] * pv[8];
+    R bd = D.b1 * dv[0];
+    R r7 = res[7] - res[0] * pv[7], r8 = res[8] - res[0] * pv[8];
     x[7] = (r8 * D.t[1] - (bd + D.t[3]) * r7) * D.tt;
     x[8] = (r7 * D.t[2] - (bd + D.t[0]) * r8) * D.tt;
   }
   for (int n = 0; n < c.npv; ++n) x[n] *= D.a;
+}
+__device__ __forceinline__ void diag_solve(const Par& c, const Diag& D, const double* pv, const double* dv,
+                                           const double* res, double* x) {
+  diag_solve_t<double>(c, D, pv, dv, res, x);
 }
 
 // the Diag fields as an array (the sweep record's diagonal part)
@@ -1318,11 +1339,13 @@ __device__ __forceinline__ void diag_to_array(const Diag& D, double* o) {
   for (int q = 0; q < 4; ++q) { o[14 + q] = D.c[q]; o[19 + q] = D.t[q]; }
   o[18] = D.tt;
 }
-__device__ __forceinline__ void diag_from_array(const double* o, Diag& D) {
-  D.a = o[0]; D.b1 = o[1]; D.i_b1 = o[2]; D.ss = o[3]; D.rr = o[4]; D.cross = o[5]; D.cross1 = o[6];
-  D.cross2 = o[7]; D.ssy1 = o[8]; D.ssy2 = o[9]; D.ssh = o[10]; D.aaa1 = o[11]; D.aaa2 = o[12]; D.mm = o[13];
-  for (int q = 0; q < 4; ++q) { D.c[q] = o[14 + q]; D.t[q] = o[19 + q]; }
-  D.tt = o[18];
+template <class R>
+__device__ __forceinline__ void diag_from_array(const double* o, DiagT<R>& D) {
+  D.a = (R)o[0]; D.b1 = (R)o[1]; D.i_b1 = (R)o[2]; D.ss = (R)o[3]; D.rr = (R)o[4]; D.cross = (R)o[5];
+  D.cross1 = (R)o[6]; D.cross2 = (R)o[7]; D.ssy1 = (R)o[8]; D.ssy2 = (R)o[9]; D.ssh = (R)o[10]; D.aaa1 = (R)o[11];
+  D.aaa2 = (R)o[12]; D.mm = (R)o[13];
+  for (int q = 0; q < 4; ++q) { D.c[q] = (R)o[14 + q]; D.t[q] = (R)o[19 + q]; }
+  D.tt = (R)o[18];
 }
 
 // spectral radius of the split Jacobian for one face: 1.05 (|u'| + d)

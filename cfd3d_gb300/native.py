@@ -46,6 +46,7 @@ def lib():
     L.cfd3d_initialize.argtypes = [H, C.c_int, dp]
     L.cfd3d_upload_state.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_download_state.argtypes = [H, C.c_int, dp, dp, dp, dp, dp]
+    L.cfd3d_upload_primitives.argtypes = [H, C.c_int, dp, dp]
     L.cfd3d_checkpoint_write.argtypes = [H, C.c_char_p, C.c_int, C.c_int, C.c_double]
     L.cfd3d_checkpoint_read.argtypes = [H, C.c_char_p, C.c_int, ip, ip, dp]
     L.cfd3d_iterate.argtypes = [H, C.c_int, C.c_int, C.c_double, dp, dp, ip]
@@ -62,15 +63,16 @@ def lib():
     L.cfd3d_time_iterate.argtypes = [H, C.c_int, dp]
     L.cfd3d_profile_iterate.argtypes = [H, dp]
     L.cfd3d_set_device.argtypes = [C.c_int]
+    L.cfd3d_fp64_peak.argtypes = [C.c_double, dp]
     _lib = L
     return L
 
 
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
-           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
+           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_upload_primitives", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
            "cfd3d_iterate", "cfd3d_iterate_n",
            "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
-           "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device"]
+           "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device", "cfd3d_fp64_peak"]
 STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
 
 
@@ -83,6 +85,15 @@ def set_device(dev):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def fp64_peak(seconds=1.0):
+    """cfd3d_fp64_peak: the current device's FP64 FMA throughput in TFLOP/s"""
+    out = C.c_double(0.0)
+    rc = lib().cfd3d_fp64_peak(float(seconds), C.byref(out))
+    if rc:
+        raise Cfd3dError(rc, "cfd3d_fp64_peak failed")
+    return out.value
 
 
 def eos_eval(p, t, y1, y2, fluid=2, prop=False):
@@ -154,6 +165,12 @@ class Engine:
     def upload(self, n, pv=None, dv=None, tv=None, qq=None):
         args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (pv, dv, tv, qq)]
         self._check(lib().cfd3d_upload_state(self.h, n, *[_p(a) for a in args]))
+
+    def upload_primitives(self, n, pv, qq=None):
+        """cfd3d_upload_primitives: padded pv (and the history qq); dv and tv follow on the
+        device from the EOS and the eddy viscosity."""
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (pv, qq)]
+        self._check(lib().cfd3d_upload_primitives(self.h, n, *[_p(a) for a in args]))
 
     def download(self, n, out=None):
         b = self.case["blocks"][n]

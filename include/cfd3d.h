@@ -152,6 +152,17 @@ int  cfd3d_upload_state(cfd3d_handle *h, int block, const double *pv, const doub
 int  cfd3d_download_state(cfd3d_handle *h, int block, double *pv, double *dv, double *tv,
                           double *qq, double *rcav);
 
+/* Set a block's state from its primitives alone: pv(npv,-1:imax+3,..) padded as
+ * cfd3d_upload_state takes it, and qq(npv,nqq,2:imax,..) (NULL keeps the history on the
+ * device).  dv and tv of the interior follow from pv as the update sets them: the mixture
+ * EOS with transport properties (eos%deteos, src/update_module.f90:689) and the eddy
+ * viscosity (src/update_module.f90:701-732, reading the uploaded ghost pv), so the result
+ * equals a cfd3d_upload_state of pv, dv, tv that an iteration produced.  A caller that
+ * keeps the state on the host moves pv and qq instead of pv, dv, tv and qq.  Ghost cells
+ * are set by the next iteration's boundary program.  No counterpart in the reference (its
+ * state never leaves the host); it serves the drop-in mode's per-step upload. */
+int  cfd3d_upload_primitives(cfd3d_handle *h, int block, const double *pv, const double *qq);
+
 /* Checkpoint file out_########.dat in the layout of variable%export_variable
  * (src/variable_module.f90:116-182), native byte order: one record per block, in block
  * order (rank r of the reference owns block r), each record
@@ -274,6 +285,12 @@ int  cfd3d_time_iterate(cfd3d_handle *h, int niter, double *ms);
  * No reference counterpart (measurement only). */
 #define CFD3D_NSTAGES 8
 int  cfd3d_profile_iterate(cfd3d_handle *h, double *stage_ms);
+
+/* FP64 throughput of the current device in TFLOP/s: every thread of a full grid runs
+ * independent fused multiply-add chains on doubles for about `seconds` (at most 60),
+ * timed with CUDA events.  The denominator of the FP64 compute roofline of this path's
+ * kernels.  No reference counterpart (measurement only). */
+int  cfd3d_fp64_peak(double seconds, double *tflops);
 
 #ifdef __cplusplus
 }

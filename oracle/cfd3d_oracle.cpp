@@ -355,6 +355,48 @@ static void wall_distance(Oracle& O) {
       }
     }
   }
+  /* The reference scans every wall-face centre for every cell.  The same minimum comes
+     from a uniform grid of bins over the centres: bins are visited in shells of growing
+     Chebyshev radius around the cell's bin until the nearest centre found is closer than
+     any unvisited bin can be.  The distance of each candidate is the same expression, so
+     the minimum is the scan's (the scan's 1e6 start value only matters with no wall). */
+  const size_t nw = wx.size();
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (size_t m = 0; m < nw; ++m) {
+    const double w3[3] = {wx[m], wy[m], wz[m]};
+    for (int d = 0; d < 3; ++d) { lo[d] = std::min(lo[d], w3[d]); hi[d] = std::max(hi[d], w3[d]); }
+  }
+  int nb[3] = {1, 1, 1};
+  double hb[3] = {1.0, 1.0, 1.0};
+  std::vector<int> first, items;
+  if (nw > 0) {
+    double ext[3], vol = 1.0;
+    int nd = 0;
+    for (int d = 0; d < 3; ++d) { ext[d] = hi[d] - lo[d]; if (ext[d] > 0.0) { vol *= ext[d]; ++nd; } }
+    const double side = (nd > 0) ? std::pow(vol / (double)nw, 1.0 / nd) : 1.0;   /* about one centre per bin */
+    for (int d = 0; d < 3; ++d) {
+      nb[d] = (ext[d] > 0.0) ? (int)std::min(512.0, std::max(1.0, std::ceil(ext[d] / side))) : 1;
+      hb[d] = (ext[d] > 0.0) ? ext[d] / nb[d] : 1.0;
+    }
+  }
+  auto bin_of = [&](const double* q, int* b) {
+    for (int d = 0; d < 3; ++d) b[d] = std::min(nb[d] - 1, std::max(0, (int)std::floor((q[d] - lo[d]) / hb[d])));
+  };
+  if (nw > 0) {
+    first.assign((size_t)nb[0] * nb[1] * nb[2] + 1, 0);
+    std::vector<int> bi(nw);
+    for (size_t m = 0; m < nw; ++m) {
+      const double w3[3] = {wx[m], wy[m], wz[m]};
+      int b[3];
+      bin_of(w3, b);
+      bi[m] = (b[2] * nb[1] + b[1]) * nb[0] + b[0];
+      ++first[bi[m] + 1];
+    }
+    for (size_t q = 1; q < first.size(); ++q) first[q] += first[q - 1];
+    items.resize(nw);
+    std::vector<int> fill(first.begin(), first.end() - 1);
+    for (size_t m = 0; m < nw; ++m) items[fill[bi[m]]++] = (int)m;
+  }
   for (auto& B : O.b) {
     A4& X = B.x; A4& G = B.grd;
     const int im = B.imax, jm = B.jmax, km = B.kmax;
@@ -366,9 +408,33 @@ static void wall_distance(Oracle& O) {
             c3[v] = 0.125 * (X(v, i, j, k) + X(v, i + 1, j, k) + X(v, i, j + 1, k) + X(v, i, j, k + 1) + X(v, i + 1, j + 1, k) +
                              X(v, i, j + 1, k + 1) + X(v, i + 1, j, k + 1) + X(v, i + 1, j + 1, k + 1));
           double ymin = 1.0e6;
-          for (size_t m = 0; m < wx.size(); ++m) {
-            double yt = std::sqrt(sq(c3[0] - wx[m]) + sq(c3[1] - wy[m]) + sq(c3[2] - wz[m]));
-            if (yt < ymin) ymin = yt;
+          if (nw > 0) {
+            int b[3];
+            bin_of(c3, b);
+            const int rmax = std::max(nb[0], std::max(nb[1], nb[2]));
+            for (int r = 0; r <= rmax; ++r) {
+              const int z0 = std::max(0, b[2] - r), z1 = std::min(nb[2] - 1, b[2] + r);
+              const int y0 = std::max(0, b[1] - r), y1 = std::min(nb[1] - 1, b[1] + r);
+              const int x0 = std::max(0, b[0] - r), x1 = std::min(nb[0] - 1, b[0] + r);
+              for (int z = z0; z <= z1; ++z)
+                for (int y = y0; y <= y1; ++y)
+                  for (int x = x0; x <= x1; ++x) {
+                    if (std::max(std::abs(z - b[2]), std::max(std::abs(y - b[1]), std::abs(x - b[0]))) != r) continue;
+                    const int q = (z * nb[1] + y) * nb[0] + x;
+                    for (int it = first[q]; it < first[q + 1]; ++it) {
+                      const int m = items[it];
+                      double yt = std::sqrt(sq(c3[0] - wx[m]) + sq(c3[1] - wy[m]) + sq(c3[2] - wz[m]));
+                      if (yt < ymin) ymin = yt;
+                    }
+                  }
+              /* the nearest any unvisited bin can be, less a margin far above rounding */
+              double bound = 1e300;
+              for (int d = 0; d < 3; ++d) {
+                if (b[d] - r > 0) bound = std::min(bound, c3[d] - (lo[d] + (b[d] - r) * hb[d]));
+                if (b[d] + r < nb[d] - 1) bound = std::min(bound, lo[d] + (b[d] + r + 1) * hb[d] - c3[d]);
+              }
+              if (bound >= 1e299 || ymin < bound - 1e-9 * (hb[0] + hb[1] + hb[2])) break;
+            }
           }
           G(4, i, j, k) = ymin;
         }

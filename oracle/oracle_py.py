@@ -18,19 +18,22 @@ from cfd3d_gb300 import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
-_lib = None
+# the same source built for speed (-O3, multiply-add contraction): times the CPU baseline
+# only, never a parity check
+LIB_FAST = os.path.join(HERE, "_build", "liboracle_fast.so")
+_libs = {}
 
 
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def lib(fast=False):
+    path = LIB_FAST if fast else LIB
+    if path not in _libs:
+        if not os.path.exists(path):
             build()
-        L = C.CDLL(LIB)
+        L = C.CDLL(path)
         dp = C.POINTER(C.c_double)
         L.orc_create.restype = C.c_void_p
         L.orc_create.argtypes = [C.POINTER(abi.Config), C.c_int, C.POINTER(abi.BlockDesc), C.c_char_p, C.c_int]
@@ -50,8 +53,8 @@ def lib():
         L.orc_tww.restype = C.c_double
         L.orc_tww.argtypes = [C.c_double]
         L.orc_snd2_fallbacks.restype = C.c_long
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def _p(a):
@@ -70,21 +73,23 @@ def eos(p, t, y1, y2, fluid=2, prop=False):
 class Oracle:
     """One oracle instance over a case (see cfd3d_gb300.cases)."""
 
-    def __init__(self, case, threads=1):
+    def __init__(self, case, threads=1, fast=False):
+        """fast: the speed build (CPU-baseline timing only)"""
         self.case = case
+        self._L = lib(fast)
         self.cfgd = dict(case["cfg"])
         self.npv, self.ntv, self.nqq, self.ngrd = abi.sizes(self.cfgd)
         self._cfg = abi.config_from_dict(self.cfgd)
         self._bs = abi.BlockSet(case["blocks"])
         err = C.create_string_buffer(512)
-        self.h = lib().orc_create(C.byref(self._cfg), self._bs.n, self._bs.arr, err, 512)
+        self.h = self._L.orc_create(C.byref(self._cfg), self._bs.n, self._bs.arr, err, 512)
         if not self.h:
             raise RuntimeError("oracle create failed: " + err.value.decode())
-        lib().orc_set_threads(self.h, threads)
+        self._L.orc_set_threads(self.h, threads)
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().orc_destroy(self.h)
+            self._L.orc_destroy(self.h)
             self.h = None
 
     def blocks(self):
@@ -93,11 +98,11 @@ class Oracle:
     def initialize(self, pv0=None):
         for n in range(len(self.case["blocks"])):
             a = None if pv0 is None else np.ascontiguousarray(pv0[n], dtype=np.float64)
-            lib().orc_initialize(self.h, n, _p(a))
+            self._L.orc_initialize(self.h, n, _p(a))
 
     def refs(self):
         out = np.zeros(6)
-        lib().orc_refs(self.h, _p(out))
+        self._L.orc_refs(self.h, _p(out))
         return dict(zip(["rhoref", "visref", "kref", "oref", "emutref", "str"], out))
 
     def get_state(self, n):
@@ -107,7 +112,7 @@ class Oracle:
         tv = np.zeros(abi.padded_shape(b, max(self.ntv, 1)))
         qq = np.zeros(abi.interior_shape(b, max(self.npv * self.nqq, 1)))
         rc = np.zeros(abi.interior_shape(b, 2))
-        lib().orc_get_state(self.h, n, _p(pv), _p(dv), _p(tv), _p(qq), _p(rc))
+        self._L.orc_get_state(self.h, n, _p(pv), _p(dv), _p(tv), _p(qq), _p(rc))
         return dict(pv=pv, dv=dv, tv=tv[..., :self.ntv], qq=qq, rcav=rc)
 
     def set_state(self, n, pv=None, dv=None, tv=None, qq=None):
@@ -115,7 +120,7 @@ class Oracle:
         if tv is not None and self.ntv:
             tv = np.ascontiguousarray(tv, dtype=np.float64)
         args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (pv, dv, tv, qq)]
-        lib().orc_set_state(self.h, n, *[_p(a) for a in args])
+        self._L.orc_set_state(self.h, n, *[_p(a) for a in args])
         del b
 
     def metrics(self, n):
@@ -125,7 +130,7 @@ class Oracle:
         ex = np.zeros((km + 1, jm, im + 1, 3))
         tx = np.zeros((km, jm + 1, im + 1, 3))
         grd = np.zeros((km + 1, jm + 1, im + 1, self.ngrd))
-        lib().orc_metrics(self.h, n, _p(cx), _p(ex), _p(tx), _p(grd))
+        self._L.orc_metrics(self.h, n, _p(cx), _p(ex), _p(tx), _p(grd))
         return cx, ex, tx, grd
 
     def residual(self, n=0):
@@ -134,15 +139,15 @@ class Oracle:
         icav = np.zeros(abi.interior_shape(b, 4))
         itt = np.zeros(abi.interior_shape(b, 4))
         oc = np.zeros(abi.interior_shape(b, 1))
-        lib().orc_residual(self.h, n, _p(res), _p(icav), _p(itt), _p(oc))
+        self._L.orc_residual(self.h, n, _p(res), _p(icav), _p(itt), _p(oc))
         return dict(res=res, icav=icav, itt=itt, omega_cut=oc[..., 0])
 
     def iterate(self, nt_phy=1, nt=1, timeprev=0.0):
         t = C.c_double(0.0)
         res = np.zeros(self.npv)
         loc = (C.c_int * 4)()
-        lib().orc_iterate(self.h, nt_phy, nt, timeprev, C.byref(t), _p(res), loc)
+        self._L.orc_iterate(self.h, nt_phy, nt, timeprev, C.byref(t), _p(res), loc)
         return t.value, res, tuple(loc)
 
     def unsteady_shift(self):
-        lib().orc_unsteady_shift(self.h)
+        self._L.orc_unsteady_shift(self.h)

@@ -125,3 +125,20 @@ def test_split_i_decomposition():
         assert len(b["con"]) == (1 if q in (0, 3) else 2)
     for a, b in zip(s["blocks"][:-1], s["blocks"][1:]):
         assert np.array_equal(a["xyz"][:, :, -1, :], b["xyz"][:, :, 0, :])
+
+
+def test_reference_arm_runs_the_gpu_arms_workload():
+    """--impl reference times the CPU oracle on the GPU arm's workload: the same case, cut
+    into the same blocks (one per host thread), with the same preconditioning and CFL"""
+    import json
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--scale", "16",
+                        "--blocks", "4", "--steps", "1", "--warmup", "1", "--ref-threads", "4"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    c = bench.workload("large", 16, 4)
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["config"]["blocks"] == 4 and line["config"]["cells"] == cases.total_cells(c)
+    assert line["config"]["workload"] == bench.describe(c, cases.total_cells(c))
+    assert c["cfg"]["prec"] == 2 and c["cfg"]["cfl"] == bench.LARGE_CFL
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
