@@ -3,8 +3,8 @@
 A step is one pseudo-iteration (update%timeinteg + resi%residual of kwonhwi1/3dcode,
 src/solve_module.f90:134-136) over the whole synthetic workload.  The default workload is
 the large turbulent cavitating case as stated: 384x192x192 cells (14.16 M), stretched wall
-grid, k-omega SST, IAPWS water/vapour with Merkle cavitation, BDF2 dual time with the
-unsteady preconditioning speed (prec = 2), decomposed along i into 16 blocks -- the
+grid, k-omega SST, IAPWS water/vapour with Merkle cavitation, BDF2 dual time, decomposed
+along i into 16 blocks -- the
 reference's MPI decomposition with one block per rank (src/grid_module.f90:95-116), which
 the CPU arm runs with one block per host thread.  Both arms run the same blocks, so the
 same block-Jacobi LU-SGS operator.
@@ -45,11 +45,6 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell-iter/s per GB300, mixed vs FP64 form at stated error; % HBM peak"
 UNIT = "Mcell-iter/s"
 
-# The large case's unsteady preconditioning (prec = 2, str = L / pi / dt_phy = 477 m/s)
-# diverges at CFL 2 within a few pseudo-iterations from this synthetic start, in the CPU
-# restatement as on the GPU, from the cells next to the far-field inflow; CFL 0.05 keeps it
-# stable and converging.
-LARGE_CFL = 0.05
 
 # DRAM bytes per cell of one k_rhs launch, dram__bytes_read.sum + dram__bytes_write.sum
 # of an ncu capture of the mixed form on the large case at 1/2 resolution (1769472 cells),
@@ -156,18 +151,17 @@ def host_threads():
         return os.cpu_count() or 1
 
 
-def workload(name, scale=1, blocks=1, cfl=None):
+def workload(name, scale=1, blocks=1, cfl=None, prec=None):
     """The benchmark case: the named configuration (the intended cavitation clamp; the
-    reference's temperature-indexed one diverges from a cavitating start), the large case
-    with its stated unsteady preconditioning, cut along i into `blocks` blocks."""
+    reference's temperature-indexed one diverges from a cavitating start), cut along i
+    into `blocks` blocks."""
     from cfd3d_gb300 import cases
     c = cases.make(name, scale=scale)
     c["cfg"]["fix_cav_clamp"] = 1
-    if name == "large":
-        c["cfg"]["prec"] = 2
-        c["cfg"]["cfl"] = LARGE_CFL
     if cfl is not None:
         c["cfg"]["cfl"] = cfl
+    if prec is not None:
+        c["cfg"]["prec"] = prec
     if blocks > 1 and len(c["blocks"]) == 1:
         c = cases.split_i(c, blocks)
     return c
@@ -219,7 +213,7 @@ def run_reference(args):
         return 0
     from cfd3d_gb300 import cases
     threads = args.ref_threads or host_threads()
-    c = workload(args.case, args.scale, args.blocks, args.cfl)
+    c = workload(args.case, args.scale, args.blocks, args.cfl, args.prec)
     ncell = cases.total_cells(c)
     o = oracle_sample(c, threads)
     for w in range(min(args.warmup, 1)):
@@ -362,6 +356,7 @@ def main():
     ap.add_argument("--blocks", type=int, default=16,
                     help="blocks along i (the reference's MPI decomposition); both arms run them")
     ap.add_argument("--cfl", type=float, default=None)
+    ap.add_argument("--prec", type=int, default=None, help="preconditioning speed (the case's own by default)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--fp64-steps", type=int, default=3,
                     help="iterations of the plain FP64 form timed beside the mixed form (0 skips)")
@@ -386,7 +381,7 @@ def main():
         dist.init_process_group("gloo")
     from cfd3d_gb300 import abi, cases, native
     native.set_device(local)
-    case = workload(args.case, args.scale, args.blocks, args.cfl)
+    case = workload(args.case, args.scale, args.blocks, args.cfl, args.prec)
     cfg = case["cfg"]
     nb = len(case["blocks"])
     prec = abi.MIXED if args.precision == "mixed" else abi.FP64

@@ -736,9 +736,11 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
       const float it0 = dpdk - df_ * ki, it1 = dpdo - df_ * oi, it2 = 0.0f;
       const float it3 = taf * rho * ei * dpdo + taf * rho * ei * pf * oi - 2.0f * tbf * rho * of -
                         1.712f * (1.0f - bf) * rho * oi * oi * pkf;
-      const float tr = it0 + it3, de = it0 * it3 - it1 * it2;
-      const float sd = sqrtf(fmaxf(0.25f * tr * tr - de, 0.0f));
-      const float l1 = copysignf(1.0f, 0.5f * tr + sd), l2 = copysignf(1.0f, 0.5f * tr - sd);
+      // the signs of the block's eigenvalues 0.5 tr +- sqrt(0.25 tr^2 - det): with it2 = 0
+      // these are max(it0, it3) and min(it0, it3).  Taken from those directly: in FP32 the
+      // difference 0.5 tr - sqrt(..) cancels catastrophically next to walls, where omega
+      // makes it3 ~ 1e12 against it0 ~ 1e4, and its sign comes out at random.
+      const float l1 = copysignf(1.0f, fmaxf(it0, it3)), l2 = copysignf(1.0f, fminf(it0, it3));
       const float f1 = (1.0f - 0.5f * (1.0f - l1)) - 0.5f * (1.0f - l1);
       const float f2 = (1.0f - 0.5f * (1.0f - l2)) - 0.5f * (1.0f - l2);
       d.itt[g] = it0 * f1; d.itt[n + g] = it1 * f1; d.itt[2 * n + g] = it2 * f2; d.itt[3 * n + g] = it3 * f2;
@@ -867,20 +869,42 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     if (MX) { o[REC_FACE + e] = fcf[3 + e]; o[REC_FACE + 3 + e] = fcf[9 + e]; o[REC_FACE + 6 + e] = fcf[15 + e]; }
     else { o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e]; }
   }
-  for (int v = 0; v < npv; ++v) o[REC_RES + v] = res[v];
-  const long long nint = d.nint, tp = d.pos[g];
-  for (int q = 0; q < NREC; ++q) d.rec[q * nint + tp] = o[q];
-  if (MX) for (int q = 0; q < REC_DIAG; ++q) d.recf[q * nint + tp] = (float)o[q];
+  if constexpr (MX) {
+    // the cell's tile record (FP32) and the forward sweep's own part x0 = D^-1 res (FP64),
+    // at its tile slot: consecutive i are consecutive slots
+    const long long sl = d.pos[g];
+    double x0[NPVM];
+    for (int v = 0; v < NPVM; ++v) x0[v] = 0.0;
+    diag_solve(c, D, pv2, dv, res, x0);
+    for (int v = 0; v < npv; ++v) d.tq[tq_at(sl, v)] = x0[v];
+    float* R = d.trf + trf_at(sl, 0);
+    for (int q = 0; q < 7; ++q) R[(TR_PV + q) * TILE_SLOTS] = (float)o[REC_PV + q];
+    for (int q = 0; q < 10; ++q) R[(TR_DV + q) * TILE_SLOTS] = (float)o[REC_DV + q];
+    R[TR_BETA * TILE_SLOTS] = (float)o[REC_BETA];
+    R[TR_EVV * TILE_SLOTS] = (float)o[REC_EVV];
+    for (int q = 0; q < PREP_DIAG; ++q) R[(TR_DIAG + q) * TILE_SLOTS] = (float)o[REC_DIAG + q];
+    for (int dir = 0; dir < 3; ++dir) {
+      for (int e = 0; e < 3; ++e) {
+        R[(TR_FACEP + 3 * dir + e) * TILE_SLOTS] = fcf[6 * dir + 3 + e];   // cx2, ex2, tx2
+        R[(TR_FACEM + 3 * dir + e) * TILE_SLOTS] = fcf[6 * dir + e];       // cx1, ex1, tx1
+      }
+      R[(TR_SPECP + dir) * TILE_SLOTS] = (float)o[REC_SPEC + 2 * dir + 1];
+      R[(TR_SPECM + dir) * TILE_SLOTS] = (float)o[REC_SPEC + 2 * dir];
+    }
+  } else {
+    for (int v = 0; v < npv; ++v) o[REC_RES + v] = res[v];
+    const long long nint = d.nint, tp = d.pos[g];
+    for (int q = 0; q < NREC; ++q) d.rec[q * nint + tp] = o[q];
+  }
 }
 
 // ------------------------------------------------------------------ LU-SGS sweeps
-// The sweeps work in the plane-major numbering t (setup_planes).  k_rhs writes what they
-// read of each cell -- as itself (diagonal block, residual) and as a neighbour (state,
-// split-Jacobian coefficients, + face vectors) -- as the cell's sweep record at t; each
-// hyperplane launch then reads its own records and those of the previous (next) plane
+// FP64 form: the sweeps work in the plane-major numbering t (setup_planes).  k_rhs writes
+// what they read of each cell -- as itself (diagonal block, residual) and as a neighbour
+// (state, split-Jacobian coefficients, + face vectors) -- as the cell's sweep record at t;
+// each hyperplane launch then reads its own records and those of the previous (next) plane
 // with coalesced loads.  dcv and dqs live at t as well; k_update reads dqs through pos[g].
-// The mixed form reads the neighbour part of the records, and the neighbours' dq, in FP32
-// (recf, dqsf): they only enter the off-diagonal products of the implicit operator.
+// The mixed form sweeps by tiles (k_sweep_tile, below).
 
 // a cell's pv / dv as the Jacobian and diagonal routines index them, from its record
 template <class T>
@@ -896,10 +920,10 @@ __device__ __forceinline__ void rec_state(const T* R, long long nint, long long 
 }
 
 // the three lower (forward) or upper (backward) neighbours' products, added to acc
-template <bool FWD, class T, bool CG = false>
-__device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long long t, const T* R, const T* dqs,
-                                                 T* acc) {
+template <bool FWD, bool CG = false>
+__device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long long t, double* acc) {
   const long long nint = d.nint;
+  const double* R = d.rec;
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     // forward: lower neighbour through its + face; backward: upper neighbour through this
@@ -907,106 +931,49 @@ __device__ __forceinline__ void sweep_neighbours(const DevPtr& d, int npv, long 
     const int nb = FWD ? d.nbf[q * nint + t] : d.nbb[q * nint + t];
     if (nb < 0) continue;
     const long long fr = FWD ? nb : t;
-    T nx[3], pv[NPVM], dv[14], dq[NPVM];
+    double nx[3], pv[NPVM], dv[14], dq[NPVM];
     for (int e = 0; e < 3; ++e) nx[e] = R[(REC_FACE + 3 * q + e) * nint + fr];
-    rec_state<T>(R, nint, nb, pv, dv);
+    rec_state<double>(R, nint, nb, pv, dv);
     // the dataflow sweep reads dq written during this launch by other CTAs: from L2 (CG)
-    for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? (CG ? __ldcg(dqs + v * nint + nb) : dqs[v * nint + nb]) : T(0);
-    const T spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + nb];
-    const T beta = R[REC_BETA * nint + nb];
-    const T evv = R[REC_EVV * nint + nb];
-    jac_apply_pre<T>(npv, nx, pv, dv, spec, beta, evv, FWD ? T(1) : T(-1), dq, acc);
+    for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? (CG ? __ldcg(d.dqs + v * nint + nb) : d.dqs[v * nint + nb]) : 0.0;
+    const double spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + nb];
+    const double beta = R[REC_BETA * nint + nb];
+    const double evv = R[REC_EVV * nint + nb];
+    jac_apply_pre<double>(npv, nx, pv, dv, spec, beta, evv, FWD ? 1.0 : -1.0, dq, acc);
   }
-}
-
-// Mixed form: since D^-1 is linear, a sweep's dq splits into the cell's own part, in FP64,
-// and D^-1 applied to the neighbours' FP32 products, in FP32:
-//   forward   dq* = D^-1 (res + sum A+ dq*)   = x0 + D^-1 (sum A+ dq*),   x0 = D^-1 res
-//   backward  dq  = D^-1 (dcv - sum A- dq)    = dq* + D^-1 (- sum A- dq)   (D^-1 dcv = dq*)
-// The own part does not wait for the neighbours, so only FP32 work stays on the sweep's
-// dependency chain; the FP64 form applies D^-1 to the full right-hand side as lhs%getx does.
-template <bool FWD>
-__device__ __forceinline__ void mx_own(const DevPtr& d, const Par& c, long long t, const double* o, const double* pv,
-                                       const double* dv, double* x0) {
-  const long long nint = d.nint;
-  const int npv = c.npv;
-  for (int v = 0; v < NPVM; ++v) x0[v] = 0.0;
-  if (FWD) {
-    double res[NPVM];
-    for (int v = 0; v < NPVM; ++v) res[v] = (v < npv) ? d.rec[(REC_RES + v) * nint + t] : 0.0;
-    Diag D;
-    diag_from_array(o, D);
-    diag_solve(c, D, pv, dv, res, x0);
-  } else {
-    for (int v = 0; v < npv; ++v) x0[v] = d.dqs[v * nint + t];   // the forward sweep's dq*
-  }
-}
-__device__ __forceinline__ void mx_corr(const Par& c, const double* o, const double* pv, const double* dv,
-                                        const float* an, float* y) {
-  DiagT<float> D;
-  diag_from_array(o, D);
-  float pf[NPVM], df[14];
-  for (int v = 0; v < NPVM; ++v) { pf[v] = (float)pv[v]; y[v] = 0.0f; }
-  for (int v = 0; v < 14; ++v) df[v] = (float)dv[v];
-  diag_solve_t<float>(c, D, pf, df, an, y);
 }
 
 // one cell of a sweep: its three neighbours' products, the closed-form D^-1, dq
-template <bool FWD, bool MX, bool CG>
+template <bool FWD, bool CG>
 __device__ __forceinline__ void sweep_cell(const DevPtr& d, const Par& c, long long t) {
   const long long nint = d.nint;
   const double* R = d.rec;
   const int npv = c.npv;
-  double pv[NPVM], dv[14], o[PREP_DIAG];
+  double pv[NPVM], dv[14], o[PREP_DIAG], acc[NPVM], x[NPVM];
   rec_state<double>(R, nint, t, pv, dv);
   for (int q = 0; q < PREP_DIAG; ++q) o[q] = R[(REC_DIAG + q) * nint + t];
-  double x[NPVM];
-  for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
-  if (MX) {
-    mx_own<FWD>(d, c, t, o, pv, dv, x);
-    float an[NPVM], y[NPVM];
-    for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
-    sweep_neighbours<FWD, float, CG>(d, npv, t, d.recf, d.dqsf, an);
-    mx_corr(c, o, pv, dv, an, y);
-    for (int v = 0; v < npv; ++v) x[v] += (double)y[v];
-  } else {
-    double acc[NPVM];
-    for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
-    if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
-    else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
-    sweep_neighbours<FWD, double, CG>(d, npv, t, R, d.dqs, acc);
-    if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
-    Diag D;
-    diag_from_array(o, D);
-    diag_solve(c, D, pv, dv, acc, x);
-  }
+  for (int v = 0; v < NPVM; ++v) { acc[v] = 0.0; x[v] = 0.0; }
+  if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
+  else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
+  sweep_neighbours<FWD, CG>(d, npv, t, acc);
+  if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
+  Diag D;
+  diag_from_array(o, D);
+  diag_solve(c, D, pv, dv, acc, x);
   for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
-  if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
 }
 
 // one launch per hyperplane
-template <bool FWD, bool MX>
+template <bool FWD>
 __global__ void __launch_bounds__(64) k_sweep(DevPtr d, Par c, long long p0, long long p1) {
   const long long t = p0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= p1) return;
-  sweep_cell<FWD, MX, false>(d, c, t);
+  sweep_cell<FWD, false>(d, c, t);
 }
 
-// Dataflow sweep: one persistent launch per sweep.  CTAs take chunks (runs of at most
-// SW_CH cells of one plane) in plane order -- reversed for the backward sweep -- from a
-// ticket counter.  A chunk's cells need the dq of their lower (upper) neighbours, which lie
-// in a few chunks of the previous (next) plane; the CTA's first thread waits for those
-// chunks' done flags, the CTA runs the hyperplane kernel's arithmetic on its cells, and the
-// first thread raises the chunk's flag.  The needed chunks always hold earlier tickets, so
-// the earliest unfinished chunk never waits and its CTA is running: the waits end.  Each
-// wait is still bounded by `spin` polls; a wait that runs out records sweep_stall, which
-// also ends every other wait, so the launch completes and the host reports
-// CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose flag is never raised (the stall
-// test).
-// the dataflow sweeps' done flags: a release store by the CTA's first thread after a
-// barrier publishes the whole CTA's dq (release is cumulative over what the barrier
-// ordered before it), an acquire load followed by a barrier makes them visible to all
-// threads of the consuming CTA
+// the dataflow sweeps' done flags: a release store by one thread after a barrier publishes
+// what the barrier ordered before it (release is cumulative), an acquire load followed by a
+// barrier makes it visible to the threads that passed the barrier
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
   asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -1016,58 +983,66 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
 
+// a bounded wait for a done flag: gives up (recording sweep_stall, which ends every other
+// wait too) after `spin` polls
+__device__ __forceinline__ void wait_flag(const DevPtr& d, const int* flag, long long spin) {
+  long long it = 0;
+  while (ld_acquire(flag) == 0) {
+    ++it;
+    if ((it & 63) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
+    if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
+    if (it > 8) __nanosleep(32);
+  }
+}
+
 // what a dataflow sweep cell reads of one neighbour before its dq is known
-template <class T>
 struct SweepNb {
   int nb;
-  T nx[3], pv[NPVM], dv[14], spec, beta, evv;
+  double nx[3], pv[NPVM], dv[14], spec, beta, evv;
 };
 
-template <bool FWD, class T>
-__device__ __forceinline__ void sweep_nb_load(const DevPtr& d, long long t, int q, const T* R, SweepNb<T>& s) {
+template <bool FWD>
+__device__ __forceinline__ void sweep_nb_load(const DevPtr& d, long long t, int q, SweepNb& s) {
   const long long nint = d.nint;
+  const double* R = d.rec;
   s.nb = FWD ? d.nbf[q * nint + t] : d.nbb[q * nint + t];
   if (s.nb < 0) return;
   const long long fr = FWD ? s.nb : t;
   for (int e = 0; e < 3; ++e) s.nx[e] = R[(REC_FACE + 3 * q + e) * nint + fr];
-  rec_state<T>(R, nint, s.nb, s.pv, s.dv);
+  rec_state<double>(R, nint, s.nb, s.pv, s.dv);
   s.spec = R[(REC_SPEC + 2 * q + (FWD ? 1 : 0)) * nint + s.nb];
   s.beta = R[REC_BETA * nint + s.nb];
   s.evv = R[REC_EVV * nint + s.nb];
 }
 
-template <bool FWD, class T>
-__device__ __forceinline__ void sweep_nb_apply(const DevPtr& d, int npv, const SweepNb<T>& s, const T* dqs, T* acc) {
+template <bool FWD>
+__device__ __forceinline__ void sweep_nb_apply(const DevPtr& d, int npv, const SweepNb& s, double* acc) {
   if (s.nb < 0) return;
   const long long nint = d.nint;
-  T dq[NPVM];
-  for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? __ldcg(dqs + v * nint + s.nb) : T(0);
-  jac_apply_pre<T>(npv, s.nx, s.pv, s.dv, s.spec, s.beta, s.evv, FWD ? T(1) : T(-1), dq, acc);
+  double dq[NPVM];
+  for (int v = 0; v < NPVM; ++v) dq[v] = (v < npv) ? __ldcg(d.dqs + v * nint + s.nb) : 0.0;
+  jac_apply_pre<double>(npv, s.nx, s.pv, s.dv, s.spec, s.beta, s.evv, FWD ? 1.0 : -1.0, dq, acc);
 }
 
-// Dataflow sweep: one persistent launch per sweep.  CTAs take chunks (runs of at most
-// SW_CH cells of one plane) in plane order -- reversed for the backward sweep -- from a
-// ticket counter.  A chunk's cells need the dq of their lower (upper) neighbours, which lie
-// in a few chunks of the previous (next) plane.  Each cell first loads everything that
-// does not depend on those dq (its own record, the neighbours' records); then the CTA waits
-// for the needed chunks' done flags (one polling thread per flag), runs the hyperplane
-// kernel's arithmetic and raises its own chunk's flag.  The needed chunks always hold
-// earlier tickets, so the earliest unfinished chunk never waits and its CTA is running:
-// the waits end.  Each wait is still bounded by `spin` polls; a wait that runs out records
-// sweep_stall, which also ends every other wait, so the launch completes and the host
-// reports CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose flag is never raised (the
-// stall test).
-template <bool FWD, bool MX>
+// Dataflow sweep of the FP64 form: one persistent launch per sweep.  CTAs take chunks
+// (runs of at most SW_CH cells of one plane) in plane order -- reversed for the backward
+// sweep -- from a ticket counter.  A chunk's cells need the dq of their lower (upper)
+// neighbours, which lie in a few chunks of the previous (next) plane.  Each cell first
+// loads everything that does not depend on those dq (its own record, the neighbours'
+// records); then the CTA waits for the needed chunks' done flags (one polling thread per
+// flag), runs the hyperplane kernel's arithmetic and raises its own chunk's flag.  The
+// needed chunks always hold earlier tickets, so the earliest unfinished chunk never waits
+// and its CTA is running: the waits end.  Each wait is still bounded by `spin` polls; a
+// wait that runs out records sweep_stall, which also ends every other wait, so the launch
+// completes and the host reports CFD3D_ERR_TIMEOUT.  `withhold` >= 0 names a chunk whose
+// flag is never raised (the stall test).
+template <bool FWD>
 __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long spin, int withhold) {
-  using T = typename std::conditional<MX, float, double>::type;
   __shared__ int s_q, s_lo[SW_CH / 32], s_hi[SW_CH / 32];
   const long long nint = d.nint;
   const int npv = c.npv;
   unsigned* ticket = d.tickets + (FWD ? 0 : 1);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const T* RN;
-  const T* DQ;
-  if constexpr (MX) { RN = d.recf; DQ = d.dqsf; } else { RN = d.rec; DQ = d.dqs; }
   for (;;) {
     if (threadIdx.x == 0) s_q = (int)atomicAdd(ticket, 1u);
     __syncthreads();
@@ -1076,24 +1051,19 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
     const int ch = FWD ? q : d.nchunk - 1 - q;
     const long long t = d.chunk_t0[ch] + threadIdx.x;
     const bool live = t < d.chunk_t0[ch + 1];
-    // ---- work that does not wait: own record (and in the mixed form the cell's own part
-    // of dq), neighbour records, the needed chunks
-    SweepNb<T> nbs[3];
+    // ---- work that does not wait: own record, neighbour records, the needed chunks
+    SweepNb nbs[3];
     double acc[NPVM], pv[NPVM], dv[14], o[PREP_DIAG];
     int lo = 0x7fffffff, hi = -1;
     if (live) {
       const double* R = d.rec;
       rec_state<double>(R, nint, t, pv, dv);
       for (int k = 0; k < PREP_DIAG; ++k) o[k] = R[(REC_DIAG + k) * nint + t];
-      if constexpr (MX) {
-        mx_own<FWD>(d, c, t, o, pv, dv, acc);
-      } else {
-        for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
-        if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
-        else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
-      }
+      for (int v = 0; v < NPVM; ++v) acc[v] = 0.0;
+      if (FWD) for (int v = 0; v < npv; ++v) acc[v] = R[(REC_RES + v) * nint + t];
+      else for (int v = 0; v < npv; ++v) acc[v] = d.dcv[v * nint + t];
       for (int k = 0; k < 3; ++k) {
-        sweep_nb_load<FWD, T>(d, t, k, RN, nbs[k]);
+        sweep_nb_load<FWD>(d, t, k, nbs[k]);
         if (nbs[k].nb >= 0) {
           const int cn = d.chunk_of[nbs[k].nb];
           lo = min(lo, cn);
@@ -1110,38 +1080,224 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
     for (int w = 0; w < SW_CH / 32; ++w) { lo = min(lo, s_lo[w]); hi = max(hi, s_hi[w]); }
     // ---- wait: thread k polls chunks lo + k, lo + k + SW_CH, ... (none when no cell of
     // the chunk has a neighbour: then hi = -1 and lo is not a chunk index)
-    for (int cn = (hi >= 0) ? lo + (int)threadIdx.x : 0; hi >= 0 && cn <= hi; cn += SW_CH) {
-      long long it = 0;
-      while (ld_acquire(d.done + cn) == 0) {
-        ++it;
-        if ((it & 63) == 0 && *(volatile int*)&d.sc->sweep_stall) break;
-        if (it > spin) { atomicExch(&d.sc->sweep_stall, 1); break; }
-        if (it > 8) __nanosleep(32);
-      }
-    }
+    for (int cn = (hi >= 0) ? lo + (int)threadIdx.x : 0; hi >= 0 && cn <= hi; cn += SW_CH) wait_flag(d, d.done + cn, spin);
     __syncthreads();
     if (live) {
       double x[NPVM];
-      if constexpr (MX) {
-        // acc holds the own part; the neighbours' FP32 contribution through an FP32 D^-1
-        float an[NPVM], y[NPVM];
-        for (int v = 0; v < NPVM; ++v) an[v] = 0.0f;
-        for (int k = 0; k < 3; ++k) sweep_nb_apply<FWD, float>(d, npv, nbs[k], DQ, an);
-        mx_corr(c, o, pv, dv, an, y);
-        for (int v = 0; v < NPVM; ++v) x[v] = acc[v] + (double)y[v];
-      } else {
-        for (int k = 0; k < 3; ++k) sweep_nb_apply<FWD, double>(d, npv, nbs[k], DQ, acc);
-        if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
-        Diag D;
-        diag_from_array(o, D);
-        for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
-        diag_solve(c, D, pv, dv, acc, x);
-      }
+      for (int k = 0; k < 3; ++k) sweep_nb_apply<FWD>(d, npv, nbs[k], acc);
+      if (FWD) for (int v = 0; v < npv; ++v) d.dcv[v * nint + t] = acc[v];
+      Diag D;
+      diag_from_array(o, D);
+      for (int v = 0; v < NPVM; ++v) x[v] = 0.0;
+      diag_solve(c, D, pv, dv, acc, x);
       for (int v = 0; v < npv; ++v) d.dqs[v * nint + t] = x[v];
-      if (MX) for (int v = 0; v < npv; ++v) d.dqsf[v * nint + t] = (float)x[v];
     }
     __syncthreads();
     if (threadIdx.x == 0 && ch != withhold) st_release(d.done + ch, 1);
+  }
+}
+
+// ---- the mixed form's tile sweeps -----------------------------------------------------
+// Since D^-1 is linear, a sweep's dq splits into the cell's own part, in FP64, and D^-1
+// applied to the neighbours' FP32 products, in FP32:
+//   forward   dq* = D^-1 (res + sum A+ dq*)  = x0 + D^-1 (sum A+ dq*),   x0 = D^-1 res
+//   backward  dq  = D^-1 (dcv - sum A- dq)   = dq* + D^-1 (- sum A- dq)   (D^-1 dcv = dq*)
+// k_rhs writes x0 (FP64) and the cell's FP32 tile record.  One warp sweeps one tile at a
+// time (tiles from a ticket counter in tile-hyperplane order, reversed for the backward
+// sweep): it stages the tile's records in shared memory with one bulk copy per array
+// (cp.async.bulk, completion on an mbarrier), waits for the done flags of the (at most
+// three) tiles it depends on, reads the contributions they left at its faces, and then
+// walks the tile's hyperplanes: lane (lj, lk) holds cell (s - lj - lk, lj, lk) at step s.
+// Each cell forms its products A.dq for its three downstream neighbours (its outgoing
+// contributions) once its dq is known: the +i one stays in the lane for its next cell, the
+// +j and +k ones move to lanes +1 and +TILE_J by shuffles, and those leaving the tile go to
+// the downstream tile's entry block (tin).  So only FP32 arithmetic, shuffles and the done
+// flags between tiles lie on the sweep's dependency chain.  The waits are bounded as in the
+// FP64 form's dataflow sweep; `withhold` >= 0 names a tile whose flag is never raised (the
+// stall test).
+constexpr unsigned TILE_B64 = NPVM * TILE_SLOTS * 8;        // FP64 block of one tile
+constexpr unsigned TILE_B32 = TS_FIELDS * TILE_SLOTS * 4;   // the FP32 fields one sweep reads
+constexpr unsigned TILE_BIN = NPVM * TILE_IN * 4;           // the entering contributions
+constexpr unsigned TILE_SMEM = TILE_B64 + TILE_B32 + TILE_BIN + 16;
+static_assert(TILE_B64 % 16 == 0 && TILE_B32 % 16 == 0 && (TR_COMMON * TILE_SLOTS * 4) % 16 == 0,
+              "bulk copies move multiples of 16 bytes");
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" : : : "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned long long* bar, unsigned bytes) {
+  asm volatile("{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }"
+               : : "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+               : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               : : "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+template <bool FWD>
+__global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long spin, int withhold) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  double* S64 = reinterpret_cast<double*>(smem);
+  float* S32 = reinterpret_cast<float*>(smem + TILE_B64);
+  float* SIN = reinterpret_cast<float*>(smem + TILE_B64 + TILE_B32);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + TILE_B64 + TILE_B32 + TILE_BIN);
+  const int lane = threadIdx.x, npv = c.npv;
+  const int lj = lane % TILE_J, lk = lane / TILE_J;
+  const float sgn = FWD ? 1.0f : -1.0f;
+  unsigned* ticket = d.tickets + (FWD ? 0 : 1);
+  if (lane == 0) mbar_init(bar);
+  __syncwarp();
+  unsigned parity = 0;
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = (int)atomicAdd(ticket, 1u);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= d.ntile) break;
+    const int tile = FWD ? q : d.ntile - 1 - q;
+    const TileDesc T = d.tiles[tile];
+    // ---- stage the tile's records (written by earlier launches): the FP64 block, the
+    // common FP32 fields and this sweep's faces and spectral radii
+    if (lane == 0) {
+      // the previous tile's shared-memory reads (generic proxy) before the bulk writes
+      asm volatile("fence.proxy.async.shared::cta;" : : : "memory");
+      mbar_expect(bar, TILE_B64 + TILE_B32);
+      const float* rf = d.trf + (long long)tile * NTR * TILE_SLOTS;
+      bulk_load(S64, d.tq + (long long)tile * NPVM * TILE_SLOTS, TILE_B64, bar);
+      bulk_load(S32, rf, TR_COMMON * TILE_SLOTS * 4, bar);
+      bulk_load(S32 + TR_COMMON * TILE_SLOTS, rf + (FWD ? TR_FACEP : TR_FACEM) * TILE_SLOTS, 12 * TILE_SLOTS * 4, bar);
+    }
+    // ---- the tiles this one depends on, then the contributions they left at its faces
+    const int* dep = FWD ? T.lo : T.hi;
+    if (lane < 3 && dep[lane] >= 0) wait_flag(d, d.done + dep[lane], spin);
+    __syncwarp();
+    {
+      const float* in = d.tin + (long long)tile * NPVM * TILE_IN;
+      for (int e = lane; e < NPVM * TILE_IN; e += 32) SIN[e] = __ldcg(in + e);
+    }
+    // ---- the staged records (the copy completes by itself: the wait is bounded only as a
+    // guard, and on a timeout the tile's cells are skipped)
+    bool staged = false;
+    for (long long it = 0; it < (1ll << 26); ++it)
+      if (mbar_test(bar, parity)) { staged = true; break; }
+    parity ^= 1u;
+    __syncwarp();
+    if (!staged) atomicExch(&d.sc->sweep_stall, 1);
+    // ---- the tile's hyperplanes
+    const int ni = T.ni, nj = T.nj, nk = T.nk;
+    const bool col = lj < nj && lk < nk && staged;
+    // faces with a tile beyond them: the others (block faces) bring no contribution
+    const bool hi_ = dep[0] >= 0, hj_ = dep[1] >= 0, hk_ = dep[2] >= 0;
+    // lane's sweep-local column coordinates (reversed in the backward sweep)
+    const int pj = FWD ? lj : nj - 1 - lj, pk = FWD ? lk : nk - 1 - lk;
+    float ci[NPVM], cj[NPVM], ck[NPVM];
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) ci[v] = cj[v] = ck[v] = 0.0f;
+    const int nsteps = ni + nj + nk - 2;
+    for (int s = 0; s < nsteps; ++s) {
+      // the +j / +k contributions of the previous step from the neighbouring columns
+      float rj[NPVM], rk[NPVM];
+#pragma unroll
+      for (int v = 0; v < NPVM; ++v) {
+        rj[v] = FWD ? __shfl_up_sync(0xffffffffu, cj[v], 1) : __shfl_down_sync(0xffffffffu, cj[v], 1);
+        rk[v] = FWD ? __shfl_up_sync(0xffffffffu, ck[v], TILE_J) : __shfl_down_sync(0xffffffffu, ck[v], TILE_J);
+      }
+      const int pi = s - pj - pk;   // sweep-local i of the lane's cell
+      if (col && pi >= 0 && pi < ni) {
+        const int li = FWD ? pi : ni - 1 - pi;
+        const int sl = lane * TILE_LS + li;
+        // entering contributions: from the tile's face, or from this tile's cells
+        float acc[NPVM];
+        const bool fi = pi == 0, fj = pj == 0, fk = pk == 0;
+#pragma unroll
+        for (int v = 0; v < NPVM; ++v) {
+          const float a0 = fi ? (hi_ ? SIN[v * TILE_IN + lj + TILE_J * lk] : 0.0f) : ci[v];
+          const float a1 = fj ? (hj_ ? SIN[v * TILE_IN + 32 + TILE_I * lk + li] : 0.0f) : rj[v];
+          const float a2 = fk ? (hk_ ? SIN[v * TILE_IN + 64 + TILE_I * lj + li] : 0.0f) : rk[v];
+          acc[v] = (a0 + a1) + a2;
+        }
+        // the cell's state and diagonal block (FP32), D^-1 acc, dq = own part + it
+        float pv[NPVM], dv[14], od[PREP_DIAG];
+        pv[0] = 0.0f; pv[4] = 0.0f;
+        pv[1] = S32[(TR_PV + 0) * TILE_SLOTS + sl]; pv[2] = S32[(TR_PV + 1) * TILE_SLOTS + sl];
+        pv[3] = S32[(TR_PV + 2) * TILE_SLOTS + sl]; pv[5] = S32[(TR_PV + 3) * TILE_SLOTS + sl];
+        pv[6] = S32[(TR_PV + 4) * TILE_SLOTS + sl]; pv[7] = S32[(TR_PV + 5) * TILE_SLOTS + sl];
+        pv[8] = S32[(TR_PV + 6) * TILE_SLOTS + sl];
+        dv[0] = S32[(TR_DV + 0) * TILE_SLOTS + sl]; dv[1] = S32[(TR_DV + 1) * TILE_SLOTS + sl];
+        dv[2] = dv[3] = dv[4] = dv[5] = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) dv[6 + m] = S32[(TR_DV + 2 + m) * TILE_SLOTS + sl];
+#pragma unroll
+        for (int m = 0; m < PREP_DIAG; ++m) od[m] = S32[(TR_DIAG + m) * TILE_SLOTS + sl];
+        DiagT<float> D;
+        D.a = od[0]; D.b1 = od[1]; D.i_b1 = od[2]; D.ss = od[3]; D.rr = od[4]; D.cross = od[5];
+        D.cross1 = od[6]; D.cross2 = od[7]; D.ssy1 = od[8]; D.ssy2 = od[9]; D.ssh = od[10];
+        D.aaa1 = od[11]; D.aaa2 = od[12]; D.mm = od[13];
+        for (int m = 0; m < 4; ++m) { D.c[m] = od[14 + m]; D.t[m] = od[19 + m]; }
+        D.tt = od[18];
+        float y[NPVM];
+#pragma unroll
+        for (int v = 0; v < NPVM; ++v) y[v] = 0.0f;
+        diag_solve_t<float>(c, D, pv, dv, acc, y);
+        float dqf[NPVM];
+        const long long gq = (long long)tile * NPVM * TILE_SLOTS + sl;
+#pragma unroll
+        for (int v = 0; v < NPVM; ++v) {
+          if (v < npv) {
+            const double x = S64[v * TILE_SLOTS + sl] + (double)y[v];
+            d.tq[gq + (long long)v * TILE_SLOTS] = x;
+            dqf[v] = (float)x;
+          } else {
+            dqf[v] = 0.0f;
+          }
+        }
+        // outgoing contributions: A+ dq through the cell's + faces (forward), -A- dq through
+        // its - faces (backward), each from zero so that the receiver adds them in order
+        const float beta = S32[TR_BETA * TILE_SLOTS + sl], evv = S32[TR_EVV * TILE_SLOTS + sl];
+        auto contribution = [&](int dir, float* o) {
+          float nx[3];
+#pragma unroll
+          for (int e = 0; e < 3; ++e) nx[e] = S32[(TR_COMMON + 3 * dir + e) * TILE_SLOTS + sl];
+          const float spec = S32[(TR_COMMON + 9 + dir) * TILE_SLOTS + sl];
+#pragma unroll
+          for (int v = 0; v < NPVM; ++v) o[v] = 0.0f;
+          jac_apply_pre<float>(npv, nx, pv, dv, spec, beta, evv, sgn, dqf, o);
+        };
+        contribution(0, ci);
+        contribution(1, cj);
+        contribution(2, ck);
+        // contributions that leave the tile: into the entry block of the tile beyond
+        const int* nxt = FWD ? T.hi : T.lo;
+        if (pi == ni - 1 && nxt[0] >= 0) {
+          float* dst = d.tin + (long long)nxt[0] * NPVM * TILE_IN + lj + TILE_J * lk;
+          for (int v = 0; v < NPVM; ++v) dst[v * TILE_IN] = ci[v];
+        }
+        if (pj == nj - 1 && nxt[1] >= 0) {
+          float* dst = d.tin + (long long)nxt[1] * NPVM * TILE_IN + 32 + TILE_I * lk + li;
+          for (int v = 0; v < NPVM; ++v) dst[v * TILE_IN] = cj[v];
+        }
+        if (pk == nk - 1 && nxt[2] >= 0) {
+          float* dst = d.tin + (long long)nxt[2] * NPVM * TILE_IN + 64 + TILE_I * lj + li;
+          for (int v = 0; v < NPVM; ++v) dst[v * TILE_IN] = ck[v];
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < NPVM; ++v) cj[v] = ck[v] = 0.0f;
+      }
+    }
+    // ---- publish the tile's contributions and dq
+    __syncwarp();
+    if (lane == 0 && tile != withhold) {
+      __threadfence();
+      st_release(d.done + tile, 1);
+    }
   }
 }
 
@@ -1168,10 +1324,11 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
     const long long n = d.ncell;
     double old[NPVM], p[NPVM];
     if constexpr (!EX) {
-      const long long pq = d.pos[g];   // plane-major position of the sweep's dq
+      // the sweep's dq: at the cell's tile slot (mixed form) or plane-major position
+      const long long pq = d.pos[g];
       for (int v = 0; v < npv; ++v) {
         old[v] = d.pv[v * n + g];
-        p[v] = old[v] + d.dqs[v * d.nint + pq];
+        p[v] = old[v] + (MX ? d.tq[tq_at(pq, v)] : d.dqs[v * d.nint + pq]);
       }
     } else {
       double cur[NPVM], dvc[NDV], r[NPVM], x[NPVM];
@@ -1524,37 +1681,36 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
     E.launches_per_iter = n;
     return;
   }
-  if (!E.sweep_planes) {
+  if (c.mixed) {
+    // tile sweeps: flags and tickets cleared, one persistent launch per sweep
+    cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), s);
+    cudaMemsetAsync(d.done, 0, (size_t)d.ntile * sizeof(int), s);
+    k_sweep_tile<true><<<E.sweep_grid, 32, TILE_SMEM, s>>>(d, c, SWEEP_SPIN, -1);
+    stage(5);
+    cudaMemsetAsync(d.done, 0, (size_t)d.ntile * sizeof(int), s);
+    k_sweep_tile<false><<<E.sweep_grid, 32, TILE_SMEM, s>>>(d, c, SWEEP_SPIN, -1);
+    n += 2;
+  } else if (!E.sweep_planes) {
     // dataflow sweeps: flags and tickets cleared, one persistent launch per sweep
     cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), s);
     cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), s);
-    if (c.mixed) k_sweep_df<true, true><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
-    else k_sweep_df<true, false><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
+    k_sweep_df<true><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
     stage(5);
     cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), s);
-    if (c.mixed) k_sweep_df<false, true><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
-    else k_sweep_df<false, false><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
+    k_sweep_df<false><<<E.sweep_grid, SW_CH, 0, s>>>(d, c, SWEEP_SPIN, -1);
     n += 2;
   } else {
-  const int np = (int)E.plane_off.size() - 1;
-  const int TS = 64;
-  for (int q = 0; q < np; ++q) {
-    long long a = E.plane_off[q], b = E.plane_off[q + 1];
-    if (b > a) {
-      if (c.mixed) k_sweep<true, true><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
-      else k_sweep<true, false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
-      ++n;
+    const int np = (int)E.plane_off.size() - 1;
+    const int TS = 64;
+    for (int q = 0; q < np; ++q) {
+      long long a = E.plane_off[q], b = E.plane_off[q + 1];
+      if (b > a) { k_sweep<true><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b); ++n; }
     }
-  }
-  stage(5);
-  for (int q = np - 1; q >= 0; --q) {
-    long long a = E.plane_off[q], b = E.plane_off[q + 1];
-    if (b > a) {
-      if (c.mixed) k_sweep<false, true><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
-      else k_sweep<false, false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b);
-      ++n;
+    stage(5);
+    for (int q = np - 1; q >= 0; --q) {
+      long long a = E.plane_off[q], b = E.plane_off[q + 1];
+      if (b > a) { k_sweep<false><<<nblk_of(b - a, TS), TS, 0, s>>>(d, c, a, b); ++n; }
     }
-  }
   }
   stage(6);
   if (c.mixed) k_update<true><<<E.red_grid, T, 0, s>>>(d, c, 0);
@@ -1940,6 +2096,19 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     CFD_CUDA(cudaStreamSynchronize(E.st));
   }
   if (!setup_ghost_program(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
+  if (c.mixed) {
+    // the mixed form sweeps by tiles (its records are tile records)
+    if (!setup_tiles(E)) return CFD3D_ERR_NOMEM;
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    CFD_CUDA(cudaFuncSetAttribute(k_sweep_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM));
+    CFD_CUDA(cudaFuncSetAttribute(k_sweep_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_tile<true>, 32, TILE_SMEM);
+    E.sweep_grid = std::max(1, std::min(std::max(per, 1) * nsm, E.d.ntile));
+    CFD_CUDA(cudaDeviceSynchronize());
+    return CFD3D_OK;
+  }
   setup_planes(E);
   E.d.cells = E.d_planes; E.d.pos = E.d_pos; E.d.nbf = E.d_nbf; E.d.nbb = E.d_nbb;
   if (!E.d_planes || !E.d_pos || !E.d_nbf || !E.d_nbb) { E.err = "device allocation failed (sweep maps)"; return CFD3D_ERR_NOMEM; }
@@ -1955,14 +2124,8 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, true>, SW_CH, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, false>, SW_CH, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true>, SW_CH, 0);
     E.sweep_grid = std::max(1, std::min(std::min(per, 8) * nsm, E.d.nchunk));
-  }
-  if (c.mixed && (cudaMalloc(&E.d.recf, (size_t)REC_DIAG * E.nint * 4) != cudaSuccess ||
-                  cudaMalloc(&E.d.dqsf, (size_t)c.npv * E.nint * 4) != cudaSuccess)) {
-    E.err = "device allocation failed (sweep records)";
-    return CFD3D_ERR_NOMEM;
   }
   CFD_CUDA(cudaDeviceSynchronize());
   return CFD3D_OK;
@@ -1996,6 +2159,10 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_chunk_of);
   cudaFree(E.d.recf);
   cudaFree(E.d.dqsf);
+  cudaFree(E.d_tiles);
+  cudaFree(E.d.trf);
+  cudaFree(E.d.tq);
+  cudaFree(E.d.tin);
   adjoint_free(E);
   if (h->cp) cudaStreamDestroy(h->cp);
   for (auto e : h->ev) if (e) cudaEventDestroy(e);
@@ -2528,21 +2695,24 @@ int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, true>, SW_CH, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true, false>, SW_CH, 0);
+  if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_tile<true>, 32, TILE_SMEM);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true>, SW_CH, 0);
+  const int nwork = c.mixed ? d.ntile : d.nchunk;
   int bestg = E.sweep_grid;
   tbest = 1e30f;
   for (int m = 1; c.timemethod == 3 && m <= std::max(per, 1); ++m) {   // (no sweeps in the explicit schemes)
     if (m > 2 && m % 2) continue;   // 1, 2, 4, 6, ...
-    const int grid = std::max(1, std::min(m * nsm, d.nchunk));
+    const int grid = std::max(1, std::min(m * nsm, nwork));
+    // (the timed sweeps run on the records of the iteration launched above; the forward one
+    // rewrites the right-hand side it reads, which changes the values but not the work)
     const float t = time_calls(E, reps, [&] {
       cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), E.st);
-      cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), E.st);
-      if (c.mixed) k_sweep_df<true, true><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
-      else k_sweep_df<true, false><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
-      cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), E.st);
-      if (c.mixed) k_sweep_df<false, true><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
-      else k_sweep_df<false, false><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
+      cudaMemsetAsync(d.done, 0, (size_t)nwork * sizeof(int), E.st);
+      if (c.mixed) k_sweep_tile<true><<<grid, 32, TILE_SMEM, E.st>>>(d, c, SWEEP_SPIN, -1);
+      else k_sweep_df<true><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
+      cudaMemsetAsync(d.done, 0, (size_t)nwork * sizeof(int), E.st);
+      if (c.mixed) k_sweep_tile<false><<<grid, 32, TILE_SMEM, E.st>>>(d, c, SWEEP_SPIN, -1);
+      else k_sweep_df<false><<<grid, SW_CH, 0, E.st>>>(d, c, SWEEP_SPIN, -1);
     });
     if (t < tbest) { tbest = t; bestg = grid; }
   }
@@ -2574,9 +2744,9 @@ int cfd3d_sweep_stall_test(cfd3d_handle* h) {
   // raises its flags, with a short poll limit
   launch_iteration(E, false);
   CFD_CUDA(cudaMemsetAsync(d.tickets, 0, 2 * sizeof(unsigned), E.st));
-  CFD_CUDA(cudaMemsetAsync(d.done, 0, (size_t)d.nchunk * sizeof(int), E.st));
-  if (c.mixed) k_sweep_df<true, true><<<E.sweep_grid, SW_CH, 0, E.st>>>(d, c, 1 << 12, 0);
-  else k_sweep_df<true, false><<<E.sweep_grid, SW_CH, 0, E.st>>>(d, c, 1 << 12, 0);
+  CFD_CUDA(cudaMemsetAsync(d.done, 0, (size_t)(c.mixed ? d.ntile : d.nchunk) * sizeof(int), E.st));
+  if (c.mixed) k_sweep_tile<true><<<E.sweep_grid, 32, TILE_SMEM, E.st>>>(d, c, 1 << 12, 0);
+  else k_sweep_df<true><<<E.sweep_grid, SW_CH, 0, E.st>>>(d, c, 1 << 12, 0);
   CFD_CUDA(cudaStreamSynchronize(E.st));
   CFD_CUDA(cudaGetLastError());
   Scalars sc;

@@ -71,6 +71,50 @@ struct Scalars {
   int pad_;
 };
 
+// ---- the mixed form's tile sweeps ------------------------------------------------------
+// A tile is a box of at most TILE_I x TILE_J x TILE_K interior cells of one block.  One warp
+// sweeps it: lane (lj, lk) = lj + TILE_J lk walks the column of cells (li, lj, lk), li
+// ascending (descending in the backward sweep), so that at step s the lanes hold the
+// tile's hyperplane li + lj + lk = s; a cell's lower (upper) neighbours within the tile are
+// the lane's own previous cell and the previous cells of lanes -1 and -TILE_J (+1, +TILE_J).
+constexpr int TILE_I = 8, TILE_J = 8, TILE_K = 4;
+static_assert(TILE_J * TILE_K == 32, "one lane per (j, k) column of a tile");
+constexpr int TILE_LS = TILE_I + 1;          // slots per lane: odd, so lanes hit distinct banks
+constexpr int TILE_SLOTS = 32 * TILE_LS;     // slots per tile
+constexpr int TILE_IN = 128;                 // contributions entering a tile: 32 + 32 + 64 face cells
+// FP32 tile-record fields of a cell: state, beta, viscous term, diagonal block (both sweeps),
+// then its + face vectors and + face spectral radii (the forward sweep's) and its - ones
+// (the backward sweep's)
+enum {
+  TR_PV = 0,       // pv 1, 2, 3, 5, 6, 7, 8
+  TR_DV = 7,       // dv 0, 1, 6 .. 13
+  TR_BETA = 17,
+  TR_EVV = 18,
+  TR_DIAG = 19,    // 23 values of the closed-form diagonal block
+  TR_COMMON = 42,
+  TR_FACEP = 42,   // + face vectors cx, ex, tx
+  TR_SPECP = 51,   // + face spectral radii of the three directions
+  TR_FACEM = 54,   // - face vectors
+  TR_SPECM = 63,   // - face spectral radii
+  NTR = 66
+};
+constexpr int TS_FIELDS = TR_COMMON + 12;    // the FP32 fields one sweep reads
+struct TileDesc {
+  int blk, i0, j0, k0;     // block and first interior cell (the reference's 2-based indices)
+  int ni, nj, nk;          // extents, at most TILE_I, TILE_J, TILE_K
+  int lo[3], hi[3];        // the tiles before (-i, -j, -k) and after (+i, +j, +k); -1: none
+};
+// slot s = tile * TILE_SLOTS + lane * TILE_LS + li; per-tile blocks of NTR (FP32 record),
+// NPVM (FP64 right-hand side / dq) and NPVM x TILE_IN (entering contributions) planes
+__host__ __device__ __forceinline__ long long trf_at(long long s, int f) {
+  const long long tile = s / TILE_SLOTS;
+  return (tile * NTR + f) * TILE_SLOTS + (s - tile * TILE_SLOTS);
+}
+__host__ __device__ __forceinline__ long long tq_at(long long s, int v) {
+  const long long tile = s / TILE_SLOTS;
+  return (tile * NPVM + v) * TILE_SLOTS + (s - tile * TILE_SLOTS);
+}
+
 struct DevPtr {
   double *pv, *dv, *tv, *gm, *res, *icav, *itt, *ocut, *dt, *rcav, *qq, *dqs, *dcv, *qold, *fi, *fv;
   const BlockGeom* blk;
@@ -114,6 +158,16 @@ struct DevPtr {
   // mixed form: FP32 copy of the neighbour part of the records (the first REC_DIAG
   // planes) and FP32 dq
   float *recf, *dqsf;
+  // mixed form: the tile sweeps (setup_tiles).  tiles in forward ticket order; trf the FP32
+  // tile records; tq the FP64 right-hand side per slot (k_rhs writes D^-1 res, the forward
+  // sweep overwrites it with dq*, the backward one with dq); tin the contributions entering
+  // each tile (written by the neighbouring tiles during a sweep); done flags per tile
+  int ntile;
+  long long nslot;
+  const TileDesc* tiles;
+  float* trf;
+  double* tq;
+  float* tin;
 };
 
 // sweep record planes: what the sweeps read of a cell, as itself and as a neighbour
@@ -151,6 +205,7 @@ struct Engine {
   std::vector<long long> plane_off;
   int* d_chunk_t0 = nullptr;   // dataflow sweep chunks (setup_planes)
   int* d_chunk_of = nullptr;
+  TileDesc* d_tiles = nullptr;  // the mixed form's tiles (setup_tiles)
   int sweep_grid = 0;          // persistent CTAs of the dataflow sweep
   int sweep_planes = 0;        // 1: one launch per hyperplane instead (CFD3D_SWEEP=planes)
   // launch shapes chosen by cfd3d_autotune: threads per CTA of the face kernels and of the
@@ -272,6 +327,7 @@ void adjoint_free(Engine& E);
 bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks);
 bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks);
 void setup_planes(Engine& E);
+bool setup_tiles(Engine& E);
 
 #define CFD_CUDA(call)                                                                 \
   do {                                                                                 \

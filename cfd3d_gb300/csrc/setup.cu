@@ -12,6 +12,7 @@
 //  * the LU-SGS hyperplane schedule: interior cells of all blocks grouped by
 //    i + j + k, so each sweep stage is one launch over independent cells.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include "engine.cuh"
@@ -814,6 +815,95 @@ void setup_planes(Engine& E) {
   cudaMemcpy(E.d_nbf, nbf.data(), 3 * nint * sizeof(int), cudaMemcpyHostToDevice);
   cudaMalloc(&E.d_nbb, 3 * nint * sizeof(int));
   cudaMemcpy(E.d_nbb, nbb.data(), 3 * nint * sizeof(int), cudaMemcpyHostToDevice);
+}
+
+}  // namespace cfd
+
+namespace cfd {
+
+// The mixed form's tiles: every block's interior cut into boxes of TILE_I x TILE_J x
+// TILE_K cells (smaller at the block's far faces), numbered in forward ticket order: by
+// tile hyperplane a + b + c, then block, then c, b, a.  A tile's tiles below (-i, -j, -k)
+// lie on the previous tile hyperplane, so they always hold earlier tickets.  pos[g] is the
+// cell's slot: tile * TILE_SLOTS + lane * TILE_LS + li, lane = lj + TILE_J lk.
+bool setup_tiles(Engine& E) {
+  struct Raw { int blk, a, b, c; };
+  std::vector<Raw> raw;
+  std::vector<std::array<int, 3>> nt(E.blk.size());
+  for (size_t bi = 0; bi < E.blk.size(); ++bi) {
+    const BlockGeom& B = E.blk[bi];
+    const int n3[3] = {(B.imax - 1 + TILE_I - 1) / TILE_I, (B.jmax - 1 + TILE_J - 1) / TILE_J,
+                       (B.kmax - 1 + TILE_K - 1) / TILE_K};
+    nt[bi] = {n3[0], n3[1], n3[2]};
+    for (int c = 0; c < n3[2]; ++c)
+      for (int b = 0; b < n3[1]; ++b)
+        for (int a = 0; a < n3[0]; ++a) raw.push_back({(int)bi, a, b, c});
+  }
+  std::stable_sort(raw.begin(), raw.end(), [](const Raw& x, const Raw& y) {
+    const int sx = x.a + x.b + x.c, sy = y.a + y.b + y.c;
+    if (sx != sy) return sx < sy;
+    if (x.blk != y.blk) return x.blk < y.blk;
+    if (x.c != y.c) return x.c < y.c;
+    if (x.b != y.b) return x.b < y.b;
+    return x.a < y.a;
+  });
+  const long long ntile = (long long)raw.size();
+  if (ntile * TILE_SLOTS >= (1ll << 31)) { E.err = "case too large for 32-bit tile slots"; return false; }
+  // tile index of (block, a, b, c)
+  std::vector<std::vector<int>> idx(E.blk.size());
+  for (size_t bi = 0; bi < E.blk.size(); ++bi) idx[bi].assign((size_t)nt[bi][0] * nt[bi][1] * nt[bi][2], -1);
+  for (long long t = 0; t < ntile; ++t) {
+    const Raw& r = raw[t];
+    idx[r.blk][((size_t)r.c * nt[r.blk][1] + r.b) * nt[r.blk][0] + r.a] = (int)t;
+  }
+  std::vector<TileDesc> tiles(ntile);
+  std::vector<int> pos(E.ncell, -1);
+  for (long long t = 0; t < ntile; ++t) {
+    const Raw& r = raw[t];
+    const BlockGeom& B = E.blk[r.blk];
+    const auto& n3 = nt[r.blk];
+    TileDesc& T = tiles[t];
+    T.blk = r.blk;
+    T.i0 = 2 + r.a * TILE_I; T.j0 = 2 + r.b * TILE_J; T.k0 = 2 + r.c * TILE_K;
+    T.ni = std::min(TILE_I, B.imax + 1 - T.i0);
+    T.nj = std::min(TILE_J, B.jmax + 1 - T.j0);
+    T.nk = std::min(TILE_K, B.kmax + 1 - T.k0);
+    auto at = [&](int a, int b, int c) -> int {
+      if (a < 0 || b < 0 || c < 0 || a >= n3[0] || b >= n3[1] || c >= n3[2]) return -1;
+      return idx[r.blk][((size_t)c * n3[1] + b) * n3[0] + a];
+    };
+    T.lo[0] = at(r.a - 1, r.b, r.c); T.lo[1] = at(r.a, r.b - 1, r.c); T.lo[2] = at(r.a, r.b, r.c - 1);
+    T.hi[0] = at(r.a + 1, r.b, r.c); T.hi[1] = at(r.a, r.b + 1, r.c); T.hi[2] = at(r.a, r.b, r.c + 1);
+    for (int lk = 0; lk < T.nk; ++lk)
+      for (int lj = 0; lj < T.nj; ++lj)
+        for (int li = 0; li < T.ni; ++li) {
+          const int i = T.i0 + li, j = T.j0 + lj, k = T.k0 + lk;
+          const long long g = B.off + (i + 1) + (long long)B.ni * ((j + 1) + (long long)B.nj * (k + 1));
+          pos[g] = (int)(t * TILE_SLOTS + (lj + TILE_J * lk) * TILE_LS + li);
+        }
+  }
+  E.d.ntile = (int)ntile;
+  E.d.nslot = ntile * TILE_SLOTS;
+  if (cudaMalloc(&E.d_tiles, ntile * sizeof(TileDesc)) != cudaSuccess ||
+      cudaMalloc(&E.d_pos, E.ncell * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&E.d.trf, (size_t)ntile * NTR * TILE_SLOTS * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&E.d.tq, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&E.d.tin, (size_t)ntile * NPVM * TILE_IN * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&E.d.done, (size_t)ntile * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&E.d.tickets, 2 * sizeof(unsigned)) != cudaSuccess) {
+    E.err = "device allocation failed (tile sweeps)";
+    return false;
+  }
+  cudaMemcpy(E.d_tiles, tiles.data(), ntile * sizeof(TileDesc), cudaMemcpyHostToDevice);
+  cudaMemcpy(E.d_pos, pos.data(), E.ncell * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemset(E.d.tq, 0, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(double));
+  cudaMemset(E.d.trf, 0, (size_t)ntile * NTR * TILE_SLOTS * sizeof(float));
+  cudaMemset(E.d.tin, 0, (size_t)ntile * NPVM * TILE_IN * sizeof(float));
+  cudaMemset(E.d.done, 0, (size_t)ntile * sizeof(int));
+  cudaMemset(E.d.tickets, 0, 2 * sizeof(unsigned));
+  E.d.tiles = E.d_tiles;
+  E.d.pos = E.d_pos;
+  return true;
 }
 
 }  // namespace cfd

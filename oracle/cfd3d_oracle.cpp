@@ -376,11 +376,12 @@ static void wall_distance(Oracle& O) {
     const double side = (nd > 0) ? std::pow(vol / (double)nw, 1.0 / nd) : 1.0;   /* about one centre per bin */
     for (int d = 0; d < 3; ++d) {
       nb[d] = (ext[d] > 0.0) ? (int)std::min(512.0, std::max(1.0, std::ceil(ext[d] / side))) : 1;
-      hb[d] = (ext[d] > 0.0) ? ext[d] / nb[d] : 1.0;
+      hb[d] = (ext[d] > 0.0) ? ext[d] / nb[d] : 0.0;   /* zero width: every centre in one plane */
     }
   }
   auto bin_of = [&](const double* q, int* b) {
-    for (int d = 0; d < 3; ++d) b[d] = std::min(nb[d] - 1, std::max(0, (int)std::floor((q[d] - lo[d]) / hb[d])));
+    for (int d = 0; d < 3; ++d)
+      b[d] = (hb[d] > 0.0) ? std::min(nb[d] - 1, std::max(0, (int)std::floor((q[d] - lo[d]) / hb[d]))) : 0;
   };
   if (nw > 0) {
     first.assign((size_t)nb[0] * nb[1] * nb[2] + 1, 0);
@@ -427,11 +428,19 @@ static void wall_distance(Oracle& O) {
                       if (yt < ymin) ymin = yt;
                     }
                   }
-              /* the nearest any unvisited bin can be, less a margin far above rounding */
+              /* the nearest any unvisited bin can be: past the visited slab along one
+                 axis, and within the bins' extent along the other two; less a margin far
+                 above rounding */
+              double out[3];
+              for (int d = 0; d < 3; ++d) {
+                const double top = lo[d] + nb[d] * hb[d];
+                out[d] = std::max(0.0, std::max(lo[d] - c3[d], c3[d] - top));
+              }
               double bound = 1e300;
               for (int d = 0; d < 3; ++d) {
-                if (b[d] - r > 0) bound = std::min(bound, c3[d] - (lo[d] + (b[d] - r) * hb[d]));
-                if (b[d] + r < nb[d] - 1) bound = std::min(bound, lo[d] + (b[d] + r + 1) * hb[d] - c3[d]);
+                const double rest = sq(out[(d + 1) % 3]) + sq(out[(d + 2) % 3]);
+                if (b[d] - r > 0) bound = std::min(bound, std::sqrt(sq(std::max(0.0, c3[d] - (lo[d] + (b[d] - r) * hb[d]))) + rest));
+                if (b[d] + r < nb[d] - 1) bound = std::min(bound, std::sqrt(sq(std::max(0.0, lo[d] + (b[d] + r + 1) * hb[d] - c3[d])) + rest));
               }
               if (bound >= 1e299 || ymin < bound - 1e-9 * (hb[0] + hb[1] + hb[2])) break;
             }

@@ -64,3 +64,45 @@ def test_mixed_iterations_follow_fp64(oracle, name):
         assert np.all(np.isfinite(resg))
         big = reso > 1e-6 * reso.max()
         assert np.allclose(resg[big], reso[big], rtol=2e-2), (it, resg, reso)
+
+
+# mixed against FP64 form, one iteration from the same state: per-cell state difference,
+# normalised by each variable's largest value.  The FP32 neighbour products and FP32 diagonal
+# correction of the sweeps, the FP32 fluxes and the FP32 time step move dq by a small
+# fraction of itself; a missing or misplaced neighbour contribution moves it by its whole
+# size (~1e-2 of the state's scale), which this bound catches.
+TOL_FIELD_ONE_ITERATION = 2e-3
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_state_follows_fp64(name):
+    c = make(name)
+    e64 = native.Engine(c, precision=abi.FP64)
+    emx = native.Engine(c, precision=abi.MIXED)
+    e64.initialize(c["pv0"])
+    emx.initialize(c["pv0"])
+    e64.iterate(1, 1, 0.0)
+    emx.iterate(1, 1, 0.0)
+    worst = 0.0
+    for b in range(len(c["blocks"])):
+        a = emx.download(b)["pv"][3:-3, 3:-3, 3:-3]
+        r = e64.download(b)["pv"][3:-3, 3:-3, 3:-3]
+        worst = max(worst, field_err(a, r).max())
+    print(f"{name}: mixed vs FP64 state after one iteration {worst:.2e}")
+    assert worst < TOL_FIELD_ONE_ITERATION, worst
+
+
+def test_mixed_iterations_are_deterministic():
+    """two engines, same state, same iterations: the same state bit for bit (the tile
+    sweeps' result does not depend on which warp took which tile when)"""
+    c = make("batched_multiblock")
+    out = []
+    for _ in range(2):
+        e = native.Engine(c, precision=abi.MIXED)
+        e.initialize(c["pv0"])
+        for it in range(3):
+            e.iterate(1, it + 1, 0.0)
+        out.append([e.download(b)["pv"] for b in range(len(c["blocks"]))])
+        e.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)

@@ -129,7 +129,7 @@ def test_split_i_decomposition():
 
 def test_reference_arm_runs_the_gpu_arms_workload():
     """--impl reference times the CPU oracle on the GPU arm's workload: the same case, cut
-    into the same blocks (one per host thread), with the same preconditioning and CFL"""
+    into the same blocks (one per host thread)"""
     import json
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--scale", "16",
                         "--blocks", "4", "--steps", "1", "--warmup", "1", "--ref-threads", "4"],
@@ -140,5 +140,4 @@ def test_reference_arm_runs_the_gpu_arms_workload():
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["config"]["blocks"] == 4 and line["config"]["cells"] == cases.total_cells(c)
     assert line["config"]["workload"] == bench.describe(c, cases.total_cells(c))
-    assert c["cfg"]["prec"] == 2 and c["cfg"]["cfl"] == bench.LARGE_CFL
     assert line["e2e"]["h2d_bytes_per_step"] == 0
