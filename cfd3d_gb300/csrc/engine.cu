@@ -878,6 +878,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     diag_solve(c, D, pv2, dv, res, x0);
     for (int v = 0; v < npv; ++v) d.tq[tq_at(sl, v)] = x0[v];
     float* R = d.trf + trf_at(sl, 0);
+    for (int v = 0; v < npv; ++v) R[(TR_X + v) * TILE_SLOTS] = (float)x0[v];
     for (int q = 0; q < 7; ++q) R[(TR_PV + q) * TILE_SLOTS] = (float)o[REC_PV + q];
     for (int q = 0; q < 10; ++q) R[(TR_DV + q) * TILE_SLOTS] = (float)o[REC_DV + q];
     R[TR_BETA * TILE_SLOTS] = (float)o[REC_BETA];
@@ -1098,11 +1099,14 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
 }
 
 // ---- the mixed form's tile sweeps -----------------------------------------------------
-// Since D^-1 is linear, a sweep's dq splits into the cell's own part, in FP64, and D^-1
-// applied to the neighbours' FP32 products, in FP32:
-//   forward   dq* = D^-1 (res + sum A+ dq*)  = x0 + D^-1 (sum A+ dq*),   x0 = D^-1 res
-//   backward  dq  = D^-1 (dcv - sum A- dq)   = dq* + D^-1 (- sum A- dq)   (D^-1 dcv = dq*)
-// k_rhs writes x0 (FP64) and the cell's FP32 tile record.  One warp sweeps one tile at a
+// Since D^-1 is linear, a sweep's dq splits into the cell's own part and D^-1 applied to
+// the neighbours' FP32 products:
+//   forward   dq* = D^-1 (res + sum A+ dq*)  = x0 + y_f,   y_f = D^-1 (sum A+ dq*),   x0 = D^-1 res
+//   backward  dq  = D^-1 (dcv - sum A- dq)   = dq* + y_b,  y_b = D^-1 (- sum A- dq)   (D^-1 dcv = dq*)
+// k_rhs writes x0 in FP64 (tq) and in FP32 within the cell's tile record; the sweeps work
+// in FP32 alone -- the products take dq in FP32 -- and store their corrections y_f, y_b;
+// the update forms dq = x0 + y_f + y_b in FP64.  (On a GB300 each FP64 instruction holds a
+// warp for tens of cycles: none stays on the sweeps' dependency chain.)  One warp sweeps one tile at a
 // time (tiles from a ticket counter in tile-hyperplane order, reversed for the backward
 // sweep): it stages the tile's records in shared memory with one bulk copy per array
 // (cp.async.bulk, completion on an mbarrier), waits for the done flags of the (at most
@@ -1115,12 +1119,10 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
 // flags between tiles lie on the sweep's dependency chain.  The waits are bounded as in the
 // FP64 form's dataflow sweep; `withhold` >= 0 names a tile whose flag is never raised (the
 // stall test).
-constexpr unsigned TILE_B64 = NPVM * TILE_SLOTS * 8;        // FP64 block of one tile
 constexpr unsigned TILE_B32 = TS_FIELDS * TILE_SLOTS * 4;   // the FP32 fields one sweep reads
 constexpr unsigned TILE_BIN = NPVM * TILE_IN * 4;           // the entering contributions
-constexpr unsigned TILE_SMEM = TILE_B64 + TILE_B32 + TILE_BIN + 16;
-static_assert(TILE_B64 % 16 == 0 && TILE_B32 % 16 == 0 && (TR_COMMON * TILE_SLOTS * 4) % 16 == 0,
-              "bulk copies move multiples of 16 bytes");
+constexpr unsigned TILE_SMEM = TILE_B32 + TILE_BIN + 16;
+static_assert(TILE_B32 % 16 == 0 && (TR_COMMON * TILE_SLOTS * 4) % 16 == 0, "bulk copies move multiples of 16 bytes");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(unsigned long long* bar) {
@@ -1145,10 +1147,9 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 template <bool FWD>
 __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long spin, int withhold) {
   extern __shared__ __align__(128) unsigned char smem[];
-  double* S64 = reinterpret_cast<double*>(smem);
-  float* S32 = reinterpret_cast<float*>(smem + TILE_B64);
-  float* SIN = reinterpret_cast<float*>(smem + TILE_B64 + TILE_B32);
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + TILE_B64 + TILE_B32 + TILE_BIN);
+  float* S32 = reinterpret_cast<float*>(smem);
+  float* SIN = reinterpret_cast<float*>(smem + TILE_B32);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + TILE_B32 + TILE_BIN);
   const int lane = threadIdx.x, npv = c.npv;
   const int lj = lane % TILE_J, lk = lane / TILE_J;
   const float sgn = FWD ? 1.0f : -1.0f;
@@ -1163,14 +1164,13 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
     if (q >= d.ntile) break;
     const int tile = FWD ? q : d.ntile - 1 - q;
     const TileDesc T = d.tiles[tile];
-    // ---- stage the tile's records (written by earlier launches): the FP64 block, the
-    // common FP32 fields and this sweep's faces and spectral radii
+    // ---- stage the tile's records (written by earlier launches): the common fields and
+    // this sweep's faces and spectral radii
     if (lane == 0) {
       // the previous tile's shared-memory reads (generic proxy) before the bulk writes
       asm volatile("fence.proxy.async.shared::cta;" : : : "memory");
-      mbar_expect(bar, TILE_B64 + TILE_B32);
+      mbar_expect(bar, TILE_B32);
       const float* rf = d.trf + (long long)tile * NTR * TILE_SLOTS;
-      bulk_load(S64, d.tq + (long long)tile * NPVM * TILE_SLOTS, TILE_B64, bar);
       bulk_load(S32, rf, TR_COMMON * TILE_SLOTS * 4, bar);
       bulk_load(S32 + TR_COMMON * TILE_SLOTS, rf + (FWD ? TR_FACEP : TR_FACEM) * TILE_SLOTS, 12 * TILE_SLOTS * 4, bar);
     }
@@ -1246,14 +1246,18 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
 #pragma unroll
         for (int v = 0; v < NPVM; ++v) y[v] = 0.0f;
         diag_solve_t<float>(c, D, pv, dv, acc, y);
+        // dq in FP32 for the products: own part + correction; the correction kept for the
+        // update, and (forward) dq* as the backward sweep's own part
         float dqf[NPVM];
         const long long gq = (long long)tile * NPVM * TILE_SLOTS + sl;
+        float* ty = FWD ? d.tyf : d.tyb;
+        float* own = d.trf + ((long long)tile * NTR + TR_X) * TILE_SLOTS + sl;
 #pragma unroll
         for (int v = 0; v < NPVM; ++v) {
           if (v < npv) {
-            const double x = S64[v * TILE_SLOTS + sl] + (double)y[v];
-            d.tq[gq + (long long)v * TILE_SLOTS] = x;
-            dqf[v] = (float)x;
+            dqf[v] = S32[(TR_X + v) * TILE_SLOTS + sl] + y[v];
+            ty[gq + (long long)v * TILE_SLOTS] = y[v];
+            if (FWD) own[v * TILE_SLOTS] = dqf[v];
           } else {
             dqf[v] = 0.0f;
           }
@@ -1328,7 +1332,8 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
       const long long pq = d.pos[g];
       for (int v = 0; v < npv; ++v) {
         old[v] = d.pv[v * n + g];
-        p[v] = old[v] + (MX ? d.tq[tq_at(pq, v)] : d.dqs[v * d.nint + pq]);
+        p[v] = old[v] + (MX ? d.tq[tq_at(pq, v)] + (double)d.tyf[tq_at(pq, v)] + (double)d.tyb[tq_at(pq, v)]
+                            : d.dqs[v * d.nint + pq]);
       }
     } else {
       double cur[NPVM], dvc[NDV], r[NPVM], x[NPVM];
@@ -2162,6 +2167,8 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_tiles);
   cudaFree(E.d.trf);
   cudaFree(E.d.tq);
+  cudaFree(E.d.tyf);
+  cudaFree(E.d.tyb);
   cudaFree(E.d.tin);
   adjoint_free(E);
   if (h->cp) cudaStreamDestroy(h->cp);

@@ -82,7 +82,8 @@ static_assert(TILE_J * TILE_K == 32, "one lane per (j, k) column of a tile");
 constexpr int TILE_LS = TILE_I + 1;          // slots per lane: odd, so lanes hit distinct banks
 constexpr int TILE_SLOTS = 32 * TILE_LS;     // slots per tile
 constexpr int TILE_IN = 128;                 // contributions entering a tile: 32 + 32 + 64 face cells
-// FP32 tile-record fields of a cell: state, beta, viscous term, diagonal block (both sweeps),
+// FP32 tile-record fields of a cell: state, beta, viscous term, diagonal block, the cell's
+// own part of dq (both sweeps: D^-1 res from k_rhs, replaced by dq* in the forward sweep),
 // then its + face vectors and + face spectral radii (the forward sweep's) and its - ones
 // (the backward sweep's)
 enum {
@@ -91,12 +92,13 @@ enum {
   TR_BETA = 17,
   TR_EVV = 18,
   TR_DIAG = 19,    // 23 values of the closed-form diagonal block
-  TR_COMMON = 42,
-  TR_FACEP = 42,   // + face vectors cx, ex, tx
-  TR_SPECP = 51,   // + face spectral radii of the three directions
-  TR_FACEM = 54,   // - face vectors
-  TR_SPECM = 63,   // - face spectral radii
-  NTR = 66
+  TR_X = 42,       // the own part of dq (npv)
+  TR_COMMON = 51,
+  TR_FACEP = 51,   // + face vectors cx, ex, tx
+  TR_SPECP = 60,   // + face spectral radii of the three directions
+  TR_FACEM = 63,   // - face vectors
+  TR_SPECM = 72,   // - face spectral radii
+  NTR = 75
 };
 constexpr int TS_FIELDS = TR_COMMON + 12;    // the FP32 fields one sweep reads
 struct TileDesc {
@@ -105,7 +107,8 @@ struct TileDesc {
   int lo[3], hi[3];        // the tiles before (-i, -j, -k) and after (+i, +j, +k); -1: none
 };
 // slot s = tile * TILE_SLOTS + lane * TILE_LS + li; per-tile blocks of NTR (FP32 record),
-// NPVM (FP64 right-hand side / dq) and NPVM x TILE_IN (entering contributions) planes
+// NPVM (FP64 own part, FP32 sweep corrections) and NPVM x TILE_IN (entering contributions)
+// planes
 __host__ __device__ __forceinline__ long long trf_at(long long s, int f) {
   const long long tile = s / TILE_SLOTS;
   return (tile * NTR + f) * TILE_SLOTS + (s - tile * TILE_SLOTS);
@@ -159,14 +162,16 @@ struct DevPtr {
   // planes) and FP32 dq
   float *recf, *dqsf;
   // mixed form: the tile sweeps (setup_tiles).  tiles in forward ticket order; trf the FP32
-  // tile records; tq the FP64 right-hand side per slot (k_rhs writes D^-1 res, the forward
-  // sweep overwrites it with dq*, the backward one with dq); tin the contributions entering
-  // each tile (written by the neighbouring tiles during a sweep); done flags per tile
+  // tile records; tq the FP64 own part D^-1 res per slot (k_rhs); tyf / tyb the FP32
+  // corrections of the forward / backward sweep, so that dq = tq + tyf + tyb (k_update);
+  // tin the contributions entering each tile (written by the neighbouring tiles during a
+  // sweep); done flags per tile
   int ntile;
   long long nslot;
   const TileDesc* tiles;
   float* trf;
   double* tq;
+  float *tyf, *tyb;
   float* tin;
 };
 
