@@ -1175,8 +1175,13 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
       bulk_load(S32 + TR_COMMON * TILE_SLOTS, rf + (FWD ? TR_FACEP : TR_FACEM) * TILE_SLOTS, 12 * TILE_SLOTS * 4, bar);
     }
     // ---- the tiles this one depends on, then the contributions they left at its faces
-    const int* dep = FWD ? T.lo : T.hi;
-    if (lane < 3 && dep[lane] >= 0) wait_flag(d, d.done + dep[lane], spin);
+    // (the tiles before and after, as scalars: no indexing into the descriptor)
+    const int dep0 = FWD ? T.lo[0] : T.hi[0], dep1 = FWD ? T.lo[1] : T.hi[1], dep2 = FWD ? T.lo[2] : T.hi[2];
+    const int nxt0 = FWD ? T.hi[0] : T.lo[0], nxt1 = FWD ? T.hi[1] : T.lo[1], nxt2 = FWD ? T.hi[2] : T.lo[2];
+    {
+      const int mine = (lane == 0) ? dep0 : (lane == 1) ? dep1 : (lane == 2) ? dep2 : -1;
+      if (mine >= 0) wait_flag(d, d.done + mine, spin);
+    }
     __syncwarp();
     {
       const float* in = d.tin + (long long)tile * NPVM * TILE_IN;
@@ -1194,7 +1199,7 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
     const int ni = T.ni, nj = T.nj, nk = T.nk;
     const bool col = lj < nj && lk < nk && staged;
     // faces with a tile beyond them: the others (block faces) bring no contribution
-    const bool hi_ = dep[0] >= 0, hj_ = dep[1] >= 0, hk_ = dep[2] >= 0;
+    const bool hi_ = dep0 >= 0, hj_ = dep1 >= 0, hk_ = dep2 >= 0;
     // lane's sweep-local column coordinates (reversed in the backward sweep)
     const int pj = FWD ? lj : nj - 1 - lj, pk = FWD ? lk : nk - 1 - lk;
     float ci[NPVM], cj[NPVM], ck[NPVM];
@@ -1219,8 +1224,8 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
 #pragma unroll
         for (int v = 0; v < NPVM; ++v) {
           const float a0 = fi ? (hi_ ? SIN[v * TILE_IN + lj + TILE_J * lk] : 0.0f) : ci[v];
-          const float a1 = fj ? (hj_ ? SIN[v * TILE_IN + 32 + TILE_I * lk + li] : 0.0f) : rj[v];
-          const float a2 = fk ? (hk_ ? SIN[v * TILE_IN + 64 + TILE_I * lj + li] : 0.0f) : rk[v];
+          const float a1 = fj ? (hj_ ? SIN[v * TILE_IN + TILE_IN_J + TILE_I * lk + li] : 0.0f) : rj[v];
+          const float a2 = fk ? (hk_ ? SIN[v * TILE_IN + TILE_IN_K + TILE_I * lj + li] : 0.0f) : rk[v];
           acc[v] = (a0 + a1) + a2;
         }
         // the cell's state and diagonal block (FP32), D^-1 acc, dq = own part + it
@@ -1278,17 +1283,16 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
         contribution(1, cj);
         contribution(2, ck);
         // contributions that leave the tile: into the entry block of the tile beyond
-        const int* nxt = FWD ? T.hi : T.lo;
-        if (pi == ni - 1 && nxt[0] >= 0) {
-          float* dst = d.tin + (long long)nxt[0] * NPVM * TILE_IN + lj + TILE_J * lk;
+        if (pi == ni - 1 && nxt0 >= 0) {
+          float* dst = d.tin + (long long)nxt0 * NPVM * TILE_IN + lj + TILE_J * lk;
           for (int v = 0; v < NPVM; ++v) dst[v * TILE_IN] = ci[v];
         }
-        if (pj == nj - 1 && nxt[1] >= 0) {
-          float* dst = d.tin + (long long)nxt[1] * NPVM * TILE_IN + 32 + TILE_I * lk + li;
+        if (pj == nj - 1 && nxt1 >= 0) {
+          float* dst = d.tin + (long long)nxt1 * NPVM * TILE_IN + TILE_IN_J + TILE_I * lk + li;
           for (int v = 0; v < NPVM; ++v) dst[v * TILE_IN] = cj[v];
         }
-        if (pk == nk - 1 && nxt[2] >= 0) {
-          float* dst = d.tin + (long long)nxt[2] * NPVM * TILE_IN + 64 + TILE_I * lj + li;
+        if (pk == nk - 1 && nxt2 >= 0) {
+          float* dst = d.tin + (long long)nxt2 * NPVM * TILE_IN + TILE_IN_K + TILE_I * lj + li;
           for (int v = 0; v < NPVM; ++v) dst[v * TILE_IN] = ck[v];
         }
       } else {
@@ -1999,7 +2003,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   };
   if (c.mixed)
     ok = ok && allocf(E.d.pvf, c.npv) && allocf(E.d.fi32, 3 * c.npv) && allocf(E.d.fv32, (c.iturb == -3) ? 1 : 3 * c.npv) &&
-         allocf(E.d.frec, 2 * 12) && alloc(E.d.lqd, 2) && allocf(E.d.lqf, 6);
+         allocf(E.d.frec, 2 * 12) && allocf(E.d.lqf, NLQ);
   else
     ok = ok && alloc(E.d.fi, 3 * c.npv) && alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
   if (!ok) { E.err = "device allocation failed"; return CFD3D_ERR_NOMEM; }
@@ -2141,7 +2145,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   Engine& E = h->E;
   if (E.graph) cudaGraphExecDestroy(E.graph);
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
-                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging, E.d.lqd};
+                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
   for (double* p : bufs) cudaFree(p);
   float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf, E.d.gmlo, E.d.lqf};
   for (float* p : fbufs) cudaFree(p);

@@ -71,17 +71,24 @@ struct Scalars {
   int pad_;
 };
 
+// the base state of a face state's expansion (k_shadow): d(1/rho_l)/dp, d(1/rho_l)/dT,
+// dh_l/dp, dh_l/dT, the rounding of the FP32 shadow's p and T (exact - shadow), the mixture's
+// rho - rhoref and h - href, rho, 1/rho_l, h_l - h_g
+enum { LQ_VP = 0, LQ_VT, LQ_HP, LQ_HT, LQ_RP, LQ_RT, LQ_RDEV, LQ_HDEV, LQ_RHO, LQ_VL, LQ_HLG, NLQ };
+
 // ---- the mixed form's tile sweeps ------------------------------------------------------
 // A tile is a box of at most TILE_I x TILE_J x TILE_K interior cells of one block.  One warp
 // sweeps it: lane (lj, lk) = lj + TILE_J lk walks the column of cells (li, lj, lk), li
 // ascending (descending in the backward sweep), so that at step s the lanes hold the
 // tile's hyperplane li + lj + lk = s; a cell's lower (upper) neighbours within the tile are
 // the lane's own previous cell and the previous cells of lanes -1 and -TILE_J (+1, +TILE_J).
-constexpr int TILE_I = 8, TILE_J = 8, TILE_K = 4;
+constexpr int TILE_I = 4, TILE_J = 8, TILE_K = 4;
 static_assert(TILE_J * TILE_K == 32, "one lane per (j, k) column of a tile");
 constexpr int TILE_LS = TILE_I + 1;          // slots per lane: odd, so lanes hit distinct banks
 constexpr int TILE_SLOTS = 32 * TILE_LS;     // slots per tile
-constexpr int TILE_IN = 128;                 // contributions entering a tile: 32 + 32 + 64 face cells
+// contributions entering a tile, by face cell: the i face (one per lane), then the j face
+// (TILE_K x TILE_I cells) from TILE_IN_J, then the k face (TILE_J x TILE_I) from TILE_IN_K
+constexpr int TILE_IN_J = 32, TILE_IN_K = TILE_IN_J + TILE_K * TILE_I, TILE_IN = TILE_IN_K + TILE_J * TILE_I;
 // FP32 tile-record fields of a cell: state, beta, viscous term, diagonal block, the cell's
 // own part of dq (both sweeps: D^-1 res from k_rhs, replaced by dq* in the forward sweep),
 // then its + face vectors and + face spectral radii (the forward sweep's) and its - ones
@@ -140,11 +147,8 @@ struct DevPtr {
   float* gmf;        // mixed form: FP32 copy of gm (metrics of the FP32 viscous and SST terms)
   float* gmlo;       // mixed form: low parts of the face vectors, gm = gmf + gmlo (df64 terms)
   float* frec;       // mixed form: reconstructed face states of one direction (2 x 12 planes)
-  // mixed form: per padded cell, the liquid phase of its EOS state, the base of the face
-  // states' first-order expansion (k_shadow): lqd = (1/rho_l, h_l) in FP64 (1/rho_l = 0:
-  // the cell carries vapour, no base); lqf = d(1/rho_l)/dp, d(1/rho_l)/dT, dh_l/dp,
-  // dh_l/dT and the rounding of the FP32 shadow's p and T (exact - shadow)
-  double* lqd;
+  // mixed form: per padded cell, its EOS state as the base of the face states' first-order
+  // expansion (k_shadow), NLQ FP32 planes (LQ_*); rho = 0 marks a cell that carries vapour
   float* lqf;
   // LU-SGS sweep records in plane-major order t (REC_* planes of nint entries); dqs and
   // dcv are plane-major too

@@ -1,7 +1,7 @@
 // flux_mixed.cu -- face fluxes of the mixed-precision form (CFD3D_MIXED).
 //
 //   k_shadow          FP32 gauge shadow pvf of every padded cell, after the boundary program,
-//                     and the liquid base of the cell's EOS state (lqd / lqf)
+//                     and the cell's EOS state as the base of face-state expansions (lqf)
 //   k_recon_mx<DIR>   per face: MUSCL / MLP on pvf, clips, face-state rho and h (FP64
 //                     mixture of phases from df64 IF97 sums, or for a vapour-free state
 //                     near its cell the liquid by first-order expansion), written to the
@@ -17,11 +17,12 @@
 
 namespace cfd {
 
-// Per padded cell: the FP32 gauge shadow, and the liquid base of the cell's EOS state for
-// the face states' expansion.  With y1 = 0 the mixture holds only liquid and gas, so the
-// liquid's 1/rho and h follow from dv: 1/rho_l = 1/dv(3), h_l = h - y2 (h_g - h_l), and its
-// derivatives d(1/rho_l)/d(p, T) = -drho_l/d(p, T) / rho_l^2, dh_l/dp = dh/dp / (1 - y2)
-// (the gas's h does not depend on p) and dh_l/dT = (dh/dT - y2 cp_g) / (1 - y2).
+// Per padded cell: the FP32 gauge shadow, and its EOS state as the base of the face states'
+// expansion.  With y1 = 0 the mixture holds only liquid and gas, so the liquid's 1/rho and h
+// follow from dv: 1/rho_l = 1/dv(3), h_l = h - y2 (h_g - h_l), and its derivatives
+// d(1/rho_l)/d(p, T) = -drho_l/d(p, T) / rho_l^2, dh_l/dp = dh/dp / (1 - y2) (the gas's h
+// does not depend on p) and dh_l/dT = (dh/dT - y2 cp_g) / (1 - y2).  The mixture's rho -
+// rhoref and h - href are formed in FP64 and stored in FP32, as the face records keep them.
 __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c) {
   const long long n = d.ncell;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -36,44 +37,63 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c) {
         d.pvf[v * n + g] = sh[v];
       }
     }
-    double il = 0.0, hl = 0.0;
-    float q[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    float q[NLQ];
+#pragma unroll
+    for (int m = 0; m < NLQ; ++m) q[m] = 0.0f;
     const double y1 = d.pv[5 * n + g], rl = d.dv[2 * n + g];
     if (c.fluid == 2 && y1 == 0.0 && rl > 0.0) {
-      const double y2 = d.pv[6 * n + g];
-      il = 1.0 / rl;
-      hl = d.dv[n + g] - y2 * d.dv[13 * n + g];
-      const float ilf = (float)il, iyl = 1.0f / (1.0f - (float)y2);
-      q[0] = -(float)d.dv[16 * n + g] * ilf * ilf;
-      q[1] = -(float)d.dv[17 * n + g] * ilf * ilf;
-      q[2] = (float)d.dv[10 * n + g] * iyl;
-      q[3] = ((float)d.dv[11 * n + g] - (float)y2 * 1004.64f) * iyl;
-      q[4] = (float)(d.pv[g] - (double)sh[0]);
-      q[5] = (float)((d.pv[4 * n + g] - c.tref) - (double)sh[4]);
+      const double y2 = d.pv[6 * n + g], rho = d.dv[g], h = d.dv[n + g];
+      const float ilf = (float)(1.0 / rl), iyl = 1.0f / (1.0f - (float)y2);
+      q[LQ_VP] = -(float)d.dv[16 * n + g] * ilf * ilf;
+      q[LQ_VT] = -(float)d.dv[17 * n + g] * ilf * ilf;
+      q[LQ_HP] = (float)d.dv[10 * n + g] * iyl;
+      q[LQ_HT] = ((float)d.dv[11 * n + g] - (float)y2 * 1004.64f) * iyl;
+      q[LQ_RP] = (float)(d.pv[g] - (double)sh[0]);
+      q[LQ_RT] = (float)((d.pv[4 * n + g] - c.tref) - (double)sh[4]);
+      q[LQ_RDEV] = (float)(rho - c.rhoref);
+      q[LQ_HDEV] = (float)(h - c.href);
+      q[LQ_RHO] = (float)rho;
+      q[LQ_VL] = ilf;
+      q[LQ_HLG] = -(float)d.dv[13 * n + g];   // h_l - h_g = -(dh/dy2)
     }
-    d.lqd[g] = il;
-    d.lqd[n + g] = hl;
 #pragma unroll
-    for (int m = 0; m < 6; ++m) d.lqf[m * n + g] = q[m];
+    for (int m = 0; m < NLQ; ++m) d.lqf[m * n + g] = q[m];
   }
 }
 
-// The liquid's 1/rho and h at a face state (gauge shadow x) by first-order expansion about
-// its base cell b (shadow xb).  The expansion's error stays below the FP32 storage of the
-// face's rho - rhoref and h - href when |dp| <= 2e4 Pa and |dT| <= 0.02 K (the second
-// derivatives of IF97 region 1 near 300 K: d2rho/dp2 ~ rho kappa^2, d2rho/dT2 ~ -0.01
-// kg/m^3/K^2, d2h/dp2 ~ -v kappa, dcp/dT ~ -0.3 J/kg/K^2).  Returns false -- the caller
-// evaluates the IF97 sums -- when the base carries vapour or the state is farther away.
-__device__ __forceinline__ bool liquid_expand(const DevPtr& d, long long b, const float* x, const float* xb, double& il,
-                                              double& hl) {
+// A vapour-free face state (gauge shadow x: y1 = 0) by first-order expansion about its base
+// cell b (shadow xb), in FP32 throughout: the liquid's 1/rho and h are expanded in (p, T),
+// the gas's are exact (ideal gas), and the mixture's change from the base,
+//   dv = (1 - y2) dv_l + dy2 (v_g - v_l) + y2_b dv_g,   drho = -rho^2 dv / (1 + rho dv),
+//   dh = (1 - y2) dh_l + dy2 (h_g - h_l) + y2_b cp_g dT,
+// is added to the base's rho - rhoref and h - href, which is what the face record keeps.
+// The expansion's error stays below that record's FP32 rounding when |dp| <= 2e4 Pa and
+// |dT| <= 0.02 K (the second derivatives of IF97 region 1 near 300 K: d2rho/dp2 ~ rho kappa^2,
+// d2rho/dT2 ~ -0.01 kg/m^3/K^2, d2h/dp2 ~ -v kappa, dcp/dT ~ -0.3 J/kg/K^2).  Returns false
+// -- the caller evaluates the IF97 sums -- when the base carries vapour or the state is
+// farther away.
+__device__ __forceinline__ bool liquid_expand(const DevPtr& d, const Par& c, long long b, const float* x,
+                                              const float* xb, float& rdev, float& hdev) {
   const long long n = d.ncell;
-  const double il0 = d.lqd[b];
-  if (il0 == 0.0) return false;
-  const float dp = (x[0] - xb[0]) - d.lqf[4 * n + b];
-  const float dt = (x[4] - xb[4]) - d.lqf[5 * n + b];
+  const float rho = d.lqf[LQ_RHO * n + b];
+  if (rho == 0.0f) return false;
+  const float dp = (x[0] - xb[0]) - d.lqf[LQ_RP * n + b];
+  const float dt = (x[4] - xb[4]) - d.lqf[LQ_RT * n + b];
   if (!(fabsf(dp) <= 2.0e4f && fabsf(dt) <= 0.02f)) return false;
-  il = il0 + (double)(d.lqf[b] * dp + d.lqf[n + b] * dt);
-  hl = d.lqd[n + b] + (double)(d.lqf[2 * n + b] * dp + d.lqf[3 * n + b] * dt);
+  const float dvl = d.lqf[LQ_VP * n + b] * dp + d.lqf[LQ_VT * n + b] * dt;
+  const float dhl = d.lqf[LQ_HP * n + b] * dp + d.lqf[LQ_HT * n + b] * dt;
+  // the gas: 1/rho_g = T / (p r1), h_g = cp_g T; base state from its shadow and roundings
+  const float r1 = 0.00348383500557f, cpg = 1004.64f;
+  const float pb = (float)c.pref + xb[0] + d.lqf[LQ_RP * n + b];
+  const float tb = (float)c.tref + xb[4] + d.lqf[LQ_RT * n + b];
+  const float pf = pb + dp, tf = tb + dt;
+  const float vgf = tf / (pf * r1);
+  const float dvg = (dt * pb - tb * dp) / (pf * pb * r1);
+  const float y2b = xb[6], y2f = x[6], dy2 = y2f - y2b;
+  const float dv = (1.0f - y2f) * dvl + dy2 * (vgf - d.lqf[LQ_VL * n + b]) + y2b * dvg;
+  rdev = d.lqf[LQ_RDEV * n + b] - rho * rho * dv / (1.0f + rho * dv);
+  const float hgl = -d.lqf[LQ_HLG * n + b] + cpg * dt;   // h_g(face) - h_l(base)
+  hdev = d.lqf[LQ_HDEV * n + b] + ((1.0f - y2f) * dhl + dy2 * hgl + y2b * cpg * dt);
   return true;
 }
 
@@ -119,7 +139,7 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
   const int npv = c.npv;
   const float* P = d.pvf;
   float gl[NPVM], gR[NPVM];
-  double rl, hl, rr, hr;
+  float rdl, hdl, rdr, hdr;   // face rho - rhoref, h - href
   float cl = 0.0f, cr = 0.0f;
   if (c.nmuscl > 0) {
     float c9[NPVM], c10[NPVM];
@@ -131,34 +151,36 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
       c9[v] = x[8]; c10[v] = x[9];
     }
     muscl_clip_mx(c, c9, c10, gl, gR);
-    const double pl = c.pref + (double)gl[0], tl = c.tref + (double)gl[4];
-    const double pr = c.pref + (double)gR[0], tr = c.tref + (double)gR[4];
-    // a vapour-free face state next to its interior base cell: the liquid by expansion
-    double il, hll;
-    if (f.lin && gl[5] == 0.0f && liquid_expand(d, g, gl, c9, il, hll))
-      mix_face_mx(pl, tl, 0.0, gl[6], il, hll, 0.0, 0.0, rl, hl);
-    else
-      eos_rho_h<true>(c.fluid, pl, tl, gl[5], gl[6], rl, hl);
-    if (f.rin && gR[5] == 0.0f && liquid_expand(d, gr, gR, c10, il, hll))
-      mix_face_mx(pr, tr, 0.0, gR[6], il, hll, 0.0, 0.0, rr, hr);
-    else
-      eos_rho_h<true>(c.fluid, pr, tr, gR[5], gR[6], rr, hr);
+    // a vapour-free face state next to its interior base cell by expansion; any other by
+    // the IF97 sums (FP64 mixture)
+    if (!(f.lin && gl[5] == 0.0f && liquid_expand(d, c, g, gl, c9, rdl, hdl))) {
+      double rho, h;
+      eos_rho_h<true>(c.fluid, c.pref + (double)gl[0], c.tref + (double)gl[4], gl[5], gl[6], rho, h);
+      rdl = (float)(rho - c.rhoref);
+      hdl = (float)(h - c.href);
+    }
+    if (!(f.rin && gR[5] == 0.0f && liquid_expand(d, c, gr, gR, c10, rdr, hdr))) {
+      double rho, h;
+      eos_rho_h<true>(c.fluid, c.pref + (double)gR[0], c.tref + (double)gR[4], gR[5], gR[6], rho, h);
+      rdr = (float)(rho - c.rhoref);
+      hdr = (float)(h - c.href);
+    }
     if (c.nscheme == 2 || c.nscheme == 3) {
-      cl = eos_c2_f(c.fluid, (float)pl, (float)tl, gl[5], gl[6], &d.sc->snd2_fallbacks);
-      cr = eos_c2_f(c.fluid, (float)pr, (float)tr, gR[5], gR[6], &d.sc->snd2_fallbacks);
+      cl = eos_c2_f(c.fluid, (float)c.pref + gl[0], (float)c.tref + gl[4], gl[5], gl[6], &d.sc->snd2_fallbacks);
+      cr = eos_c2_f(c.fluid, (float)c.pref + gR[0], (float)c.tref + gR[4], gR[5], gR[6], &d.sc->snd2_fallbacks);
     }
   } else {
     for (int v = 0; v < npv; ++v) { gl[v] = P[v * n + g]; gR[v] = P[v * n + gr]; }
-    rl = d.dv[g]; hl = d.dv[n + g]; cl = (float)d.dv[5 * n + g];
-    rr = d.dv[gr]; hr = d.dv[n + gr]; cr = (float)d.dv[5 * n + gr];
+    rdl = (float)(d.dv[g] - c.rhoref); hdl = (float)(d.dv[n + g] - c.href); cl = (float)d.dv[5 * n + g];
+    rdr = (float)(d.dv[gr] - c.rhoref); hdr = (float)(d.dv[n + gr] - c.href); cr = (float)d.dv[5 * n + gr];
   }
   float* F = d.frec;
   for (int v = 0; v < npv; ++v) { F[v * n + g] = gl[v]; F[(FREC_SIDE + v) * n + g] = gR[v]; }
-  F[NPVM * n + g] = (float)(rl - c.rhoref);
-  F[(NPVM + 1) * n + g] = (float)(hl - c.href);
+  F[NPVM * n + g] = rdl;
+  F[(NPVM + 1) * n + g] = hdl;
   F[(NPVM + 2) * n + g] = cl;
-  F[(FREC_SIDE + NPVM) * n + g] = (float)(rr - c.rhoref);
-  F[(FREC_SIDE + NPVM + 1) * n + g] = (float)(hr - c.href);
+  F[(FREC_SIDE + NPVM) * n + g] = rdr;
+  F[(FREC_SIDE + NPVM + 1) * n + g] = hdr;
   F[(FREC_SIDE + NPVM + 2) * n + g] = cr;
 }
 
