@@ -557,6 +557,32 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
   }
 }
 
+// the mixed form's free-stream closure of every interior cell, (Phi + pref I).sum(n dl)
+// over its six faces, for k_rhs (the metrics do not change, so this runs once)
+__global__ void k_closure(DevPtr d, Par c) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= d.nint) return;
+  int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
+  const BlockGeom& B = d.blk[b];
+  const long long g = interior_cell(B, t - B.int_off, i, j, k);
+  const long long n = d.ncell, st[3] = {1, B.ni, (long long)B.ni * B.nj};
+  const int planes[3] = {GM_CX, GM_EX, GM_TX};
+  double sn[3];
+  for (int e = 0; e < 3; ++e) {
+    double s = 0.0;
+    for (int q = 0; q < 3; ++q) {
+      const double* G = d.gm + (planes[q] + e) * n;
+      s += G[g] - G[g - st[q]];
+    }
+    sn[e] = s;
+  }
+  for (int v = 0; v < c.npv; ++v) {
+    double r = c.phi[v][0] * sn[0] + c.phi[v][1] * sn[1] + c.phi[v][2] * sn[2];
+    if (v >= 1 && v <= 3) r += c.pref * sn[v - 1];
+    d.clo[v * n + g] = r;
+  }
+}
+
 // ------------------------------------------------------------------ residual + sources
 // REC = false (the explicit schemes): the residual alone, without the sweep records (a
 // separate instantiation, so that the LU-SGS kernel carries no branch for it)
@@ -622,21 +648,10 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     res[v] = r;
   }
   if (MX) {
-    // the stored mixed-form fluxes are F - (Phi + pref I).n dl; add the free-stream part
-    // back through the cell's face-vector sum (zero up to the metrics' closure error).
-    // (In FP64: the same sum from the face vectors' df64 float pairs measured slower.)
-    const int planes[3] = {GM_CX, GM_EX, GM_TX};
-    double sn[3];
-    for (int e = 0; e < 3; ++e) {
-      double s = 0.0;
-      for (int q = 0; q < 3; ++q) {
-        const double* G = d.gm + (planes[q] + e) * n;
-        s += G[g] - G[g - st[q]];
-      }
-      sn[e] = s;
-    }
-    for (int v = 0; v < npv; ++v) res[v] -= c.phi[v][0] * sn[0] + c.phi[v][1] * sn[1] + c.phi[v][2] * sn[2];
-    for (int e = 0; e < 3; ++e) res[1 + e] -= c.pref * sn[e];
+    // the stored mixed-form fluxes are F - (Phi + pref I).n dl: the free-stream part comes
+    // back through the cell's face-vector sum (zero up to the metrics' closure error),
+    // formed once by k_closure
+    for (int v = 0; v < npv; ++v) res[v] -= d.clo[v * n + g];
   }
   double pv2[NPVM], dv[NDV];
   for (int v = 0; v < npv; ++v) pv2[v] = d.pv[v * n + g];
@@ -2102,6 +2117,8 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     const long long m9 = (long long)GM_GRD * E.ncell;
     if (cudaMalloc(&E.d.gmlo, (size_t)m9 * 4) != cudaSuccess) { E.err = "device allocation failed (gmlo)"; return CFD3D_ERR_NOMEM; }
     k_lo_f32<<<nblk_of(m9, 256), 256, 0, E.st>>>(E.d.gm, E.d.gmf, E.d.gmlo, m9);
+    if (cudaMalloc(&E.d.clo, (size_t)c.npv * E.ncell * 8) != cudaSuccess) { E.err = "device allocation failed (closure)"; return CFD3D_ERR_NOMEM; }
+    k_closure<<<nblk_of(E.nint, 256), 256, 0, E.st>>>(E.d, E.par);
     CFD_CUDA(cudaStreamSynchronize(E.st));
   }
   if (!setup_ghost_program(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
@@ -2145,7 +2162,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   Engine& E = h->E;
   if (E.graph) cudaGraphExecDestroy(E.graph);
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
-                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging};
+                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging, E.d.clo};
   for (double* p : bufs) cudaFree(p);
   float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf, E.d.gmlo, E.d.lqf};
   for (float* p : fbufs) cudaFree(p);

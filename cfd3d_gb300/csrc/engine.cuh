@@ -82,7 +82,7 @@ enum { LQ_VP = 0, LQ_VT, LQ_HP, LQ_HT, LQ_RP, LQ_RT, LQ_RDEV, LQ_HDEV, LQ_RHO, L
 // ascending (descending in the backward sweep), so that at step s the lanes hold the
 // tile's hyperplane li + lj + lk = s; a cell's lower (upper) neighbours within the tile are
 // the lane's own previous cell and the previous cells of lanes -1 and -TILE_J (+1, +TILE_J).
-constexpr int TILE_I = 4, TILE_J = 8, TILE_K = 4;
+constexpr int TILE_I = 8, TILE_J = 8, TILE_K = 4;
 static_assert(TILE_J * TILE_K == 32, "one lane per (j, k) column of a tile");
 constexpr int TILE_LS = TILE_I + 1;          // slots per lane: odd, so lanes hit distinct banks
 constexpr int TILE_SLOTS = 32 * TILE_LS;     // slots per tile
@@ -147,6 +147,9 @@ struct DevPtr {
   float* gmf;        // mixed form: FP32 copy of gm (metrics of the FP32 viscous and SST terms)
   float* gmlo;       // mixed form: low parts of the face vectors, gm = gmf + gmlo (df64 terms)
   float* frec;       // mixed form: reconstructed face states of one direction (2 x 12 planes)
+  // mixed form: per interior cell the free-stream part of its stored flux deviations,
+  // (Phi + pref I).sum(n dl) over its faces, which depends on the metrics alone (npv planes)
+  double* clo;
   // mixed form: per padded cell, its EOS state as the base of the face states' first-order
   // expansion (k_shadow), NLQ FP32 planes (LQ_*); rho = 0 marks a cell that carries vapour
   float* lqf;
