@@ -16,9 +16,10 @@ value      device-resident throughput: K graph replays timed with CUDA events on
            engine's stream; the working set (~20 GB) is far larger than L2, so no flush.
 e2e        the same metric through the C ABI as a Fortran caller that keeps the state on
            the host would use it: each step uploads pv and the BDF history qq from pinned
-           host buffers (dv and tv follow on the device from the EOS and the eddy
-           viscosity, cfd3d_upload_primitives), iterates, and downloads pv, dv and tv
-           (host<->device copies inside the timed region).
+           host buffers for all blocks in one call (dv and tv follow on the device from
+           the EOS and the eddy viscosity, cfd3d_upload_primitives_all), iterates, and
+           downloads pv, dv and tv of all blocks (cfd3d_download_state_all); the
+           host<->device copies are inside the timed region.
 roofline   the whole pseudo-iteration: algorithmic bytes per cell-iteration (persisted
            pv/dv/tv, metrics, LU-SGS intermediates, BDF history, rcav; 1040 B for this
            case) x cells / time, against the measured HBM copy bandwidth; beside it the
@@ -302,12 +303,15 @@ def run_e2e(eng, case, steps, it0):
         bufs.append(keep)
     d2h += 8 * eng.npv   # the residual norms
 
+    pv_l = [keep["pv"][1] for keep in bufs]
+    qq_l = [keep["qq"][1] for keep in bufs] if eng.nqq else None
+    dv_l = [keep["dv"][1] for keep in bufs]
+    tv_l = [keep["tv"][1] for keep in bufs] if eng.ntv else None
+
     def step(s):
-        for n, keep in enumerate(bufs):
-            eng.upload_primitives(n, keep["pv"][1], keep["qq"][1] if "qq" in keep else None)
+        eng.upload_primitives_all(pv_l, qq_l)
         eng.iterate(1, it0 + s, 0.0)
-        for n, keep in enumerate(bufs):
-            eng.download_arrays(n, pv=keep["pv"][1], dv=keep["dv"][1], tv=keep["tv"][1] if "tv" in keep else None)
+        eng.download_state_all(pv_l, dv_l, tv_l)
 
     step(0)                                   # untimed: first touch of the pinned pages
     torch.cuda.synchronize()

@@ -1595,6 +1595,7 @@ struct cfd3d_handle {
   Engine E;
   double* staging = nullptr;
   size_t staging_bytes = 0;
+  std::vector<cudaEvent_t> bev;   // one per block: the whole-case transfers' per-block stages
   // the copy stream of upload_state / download_state and one event per staged array:
   // the layout kernel of one array overlaps the host copy of the next
   cudaStream_t cp = nullptr;
@@ -2192,6 +2193,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d.tyb);
   cudaFree(E.d.tin);
   adjoint_free(E);
+  for (auto e : h->bev) cudaEventDestroy(e);
   if (h->cp) cudaStreamDestroy(h->cp);
   for (auto e : h->ev) if (e) cudaEventDestroy(e);
   if (E.st) cudaStreamDestroy(E.st);
@@ -2349,6 +2351,122 @@ int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const doubl
 int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, double* tv, double* qq, double* rcav) {
   if (!h) return CFD3D_ERR_ARG;
   return drain_on_error(h, download_state(h, block, pv, dv, tv, qq, rcav));
+}
+
+// ---- the whole case in one call: every block's copy leaves as soon as it can, and each
+// block's layout kernel overlaps the copies of the blocks after it
+namespace {
+int block_events(cfd3d_handle* h) {
+  Engine& E = h->E;
+  while (h->bev.size() < E.blk.size()) {
+    cudaEvent_t e;
+    CFD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->bev.push_back(e);
+  }
+  return CFD3D_OK;
+}
+
+int upload_primitives_all(cfd3d_handle* h, const double* const* pv, const double* const* qq) {
+  Engine& E = h->E;
+  const Par& c = E.par;
+  const int nb = (int)E.blk.size();
+  const bool hist = qq && c.nqq;
+  size_t total = 0;
+  for (int b = 0; b < nb; ++b) {
+    if (!pv[b]) { E.err = "pv is required for every block"; return CFD3D_ERR_ARG; }
+    const BlockGeom& B = E.blk[b];
+    total += (size_t)B.ni * B.nj * B.nk * c.npv;
+    if (hist && qq[b]) total += (size_t)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1) * 2 * c.npv;
+  }
+  int rc = ensure_staging(h, total * 8);
+  if (!rc) rc = ensure_copy_stream(h);
+  if (!rc) rc = block_events(h);
+  if (rc) return rc;
+  CFD_CUDA(cudaEventRecord(h->ev[5], E.st));          // staging no longer read by earlier work
+  CFD_CUDA(cudaStreamWaitEvent(h->cp, h->ev[5], 0));
+  std::vector<double*> spv(nb), sqq(nb, nullptr);
+  double* stg = h->staging;
+  for (int b = 0; b < nb; ++b) {
+    const BlockGeom& B = E.blk[b];
+    const size_t ncb = (size_t)B.ni * B.nj * B.nk, nint = (size_t)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+    spv[b] = stg;
+    CFD_CUDA(cudaMemcpyAsync(stg, pv[b], ncb * c.npv * 8, cudaMemcpyHostToDevice, h->cp));
+    stg += ncb * c.npv;
+    if (hist && qq[b]) {
+      sqq[b] = stg;
+      CFD_CUDA(cudaMemcpyAsync(stg, qq[b], nint * 2 * c.npv * 8, cudaMemcpyHostToDevice, h->cp));
+      stg += nint * 2 * c.npv;
+    }
+    CFD_CUDA(cudaEventRecord(h->bev[b], h->cp));
+  }
+  for (int b = 0; b < nb; ++b) {
+    const BlockGeom& B = E.blk[b];
+    const long long ncb = (long long)B.ni * B.nj * B.nk, nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+    CFD_CUDA(cudaStreamWaitEvent(E.st, h->bev[b], 0));
+    k_aos_to_soa<<<nblk_of(ncb, 256), 256, 0, E.st>>>(spv[b], c.npv, ncb, E.d.pv, E.ncell, B.off);
+    if (sqq[b]) k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(sqq[b], 2 * c.npv, B, E.d.qq, E.ncell, 1);
+    if (c.mixed) k_init<true><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, b, 0);
+    else k_init<false><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, b, 0);
+  }
+  if (c.iturb >= -1 && c.ntv >= 3) {
+    if (c.mixed) k_eddy<true><<<nblk_of(E.nint, 128), 128, 0, E.st>>>(E.d, c, 0, E.nint);
+    else k_eddy<false><<<nblk_of(E.nint, 128), 128, 0, E.st>>>(E.d, c, 0, E.nint);
+  }
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  return CFD3D_OK;
+}
+
+int download_state_all(cfd3d_handle* h, double* const* pv, double* const* dv, double* const* tv) {
+  Engine& E = h->E;
+  const Par& c = E.par;
+  const int nb = (int)E.blk.size();
+  size_t total = 0;
+  for (int b = 0; b < nb; ++b) {
+    const BlockGeom& B = E.blk[b];
+    const size_t ncb = (size_t)B.ni * B.nj * B.nk;
+    total += ncb * ((pv && pv[b] ? c.npv : 0) + (dv && dv[b] ? NDV : 0) + (tv && tv[b] ? c.ntv : 0));
+  }
+  int rc = ensure_staging(h, std::max<size_t>(total, 1) * 8);
+  if (!rc) rc = ensure_copy_stream(h);
+  if (!rc) rc = block_events(h);
+  if (rc) return rc;
+  double* stg = h->staging;
+  for (int b = 0; b < nb; ++b) {
+    const BlockGeom& B = E.blk[b];
+    const long long ncb = (long long)B.ni * B.nj * B.nk;
+    struct { double* a; int nv; const double* src; } items[3] = {
+        {pv ? pv[b] : nullptr, c.npv, E.d.pv}, {dv ? dv[b] : nullptr, NDV, E.d.dv}, {tv ? tv[b] : nullptr, c.ntv, E.d.tv}};
+    double* first = stg;
+    for (auto& it : items) {
+      if (!it.a || it.nv == 0) continue;
+      k_soa_to_aos<<<nblk_of(ncb, 256), 256, 0, E.st>>>(it.src, it.nv, ncb, stg, E.ncell, B.off);
+      stg += ncb * it.nv;
+    }
+    CFD_CUDA(cudaEventRecord(h->bev[b], E.st));
+    CFD_CUDA(cudaStreamWaitEvent(h->cp, h->bev[b], 0));
+    double* s2 = first;
+    for (auto& it : items) {
+      if (!it.a || it.nv == 0) continue;
+      CFD_CUDA(cudaMemcpyAsync(it.a, s2, (size_t)ncb * it.nv * 8, cudaMemcpyDeviceToHost, h->cp));
+      s2 += ncb * it.nv;
+    }
+  }
+  CFD_CUDA(cudaStreamSynchronize(h->cp));
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  return CFD3D_OK;
+}
+}  // namespace
+
+int cfd3d_upload_primitives_all(cfd3d_handle* h, const double* const* pv, const double* const* qq) {
+  if (!h || !pv) return CFD3D_ERR_ARG;
+  return drain_on_error(h, upload_primitives_all(h, pv, qq));
+}
+
+int cfd3d_download_state_all(cfd3d_handle* h, double* const* pv, double* const* dv, double* const* tv) {
+  if (!h) return CFD3D_ERR_ARG;
+  return drain_on_error(h, download_state_all(h, pv, dv, tv));
 }
 
 int cfd3d_upload_primitives(cfd3d_handle* h, int block, const double* pv, const double* qq) {

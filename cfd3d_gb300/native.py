@@ -47,6 +47,9 @@ def lib():
     L.cfd3d_upload_state.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_download_state.argtypes = [H, C.c_int, dp, dp, dp, dp, dp]
     L.cfd3d_upload_primitives.argtypes = [H, C.c_int, dp, dp]
+    pp = C.POINTER(dp)
+    L.cfd3d_upload_primitives_all.argtypes = [H, pp, pp]
+    L.cfd3d_download_state_all.argtypes = [H, pp, pp, pp]
     L.cfd3d_checkpoint_write.argtypes = [H, C.c_char_p, C.c_int, C.c_int, C.c_double]
     L.cfd3d_checkpoint_read.argtypes = [H, C.c_char_p, C.c_int, ip, ip, dp]
     L.cfd3d_iterate.argtypes = [H, C.c_int, C.c_int, C.c_double, dp, dp, ip]
@@ -69,7 +72,7 @@ def lib():
 
 
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
-           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_upload_primitives", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
+           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_upload_primitives", "cfd3d_upload_primitives_all", "cfd3d_download_state_all", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
            "cfd3d_iterate", "cfd3d_iterate_n",
            "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device", "cfd3d_fp64_peak"]
@@ -171,6 +174,26 @@ class Engine:
         device from the EOS and the eddy viscosity."""
         args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (pv, qq)]
         self._check(lib().cfd3d_upload_primitives(self.h, n, *[_p(a) for a in args]))
+
+    def _ptrs(self, arrays, writable=False):
+        """an array of per-block pointers (NULL for None entries, or None for no list)"""
+        if arrays is None:
+            return None
+        arr = (C.POINTER(C.c_double) * len(arrays))()
+        for q, a in enumerate(arrays):
+            if a is not None:
+                assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"] and (a.flags["WRITEABLE"] or not writable)
+                arr[q] = _p(a)
+        return arr
+
+    def upload_primitives_all(self, pv, qq=None):
+        """cfd3d_upload_primitives_all: per-block padded pv (and qq) lists, contiguous float64"""
+        self._check(lib().cfd3d_upload_primitives_all(self.h, self._ptrs(pv), self._ptrs(qq)))
+
+    def download_state_all(self, pv=None, dv=None, tv=None):
+        """cfd3d_download_state_all into caller-owned per-block arrays (None skips)"""
+        self._check(lib().cfd3d_download_state_all(self.h, self._ptrs(pv, True), self._ptrs(dv, True),
+                                                   self._ptrs(tv, True) if self.ntv else None))
 
     def download(self, n, out=None):
         b = self.case["blocks"][n]

@@ -163,6 +163,16 @@ int  cfd3d_download_state(cfd3d_handle *h, int block, double *pv, double *dv, do
  * state never leaves the host); it serves the drop-in mode's per-step upload. */
 int  cfd3d_upload_primitives(cfd3d_handle *h, int block, const double *pv, const double *qq);
 
+/* The two transfers of the drop-in mode for every block in one call: pv[b] (and qq[b],
+ * either array or any entry may be NULL) for block b = 0..nblocks-1 as cfd3d_upload_primitives
+ * takes them, and pv / dv / tv of every block as cfd3d_download_state gives them (NULL arrays
+ * or entries are skipped).  The copies of all blocks leave back to back at the link's rate
+ * and each block's layout kernel overlaps the copies of the blocks after it; the results
+ * equal the per-block calls'.  The handle's staging region grows to the case's whole state.
+ * No counterpart in the reference (its state never leaves the host). */
+int  cfd3d_upload_primitives_all(cfd3d_handle *h, const double *const *pv, const double *const *qq);
+int  cfd3d_download_state_all(cfd3d_handle *h, double *const *pv, double *const *dv, double *const *tv);
+
 /* Checkpoint file out_########.dat in the layout of variable%export_variable
  * (src/variable_module.f90:116-182), native byte order: one record per block, in block
  * order (rank r of the reference owns block r), each record

@@ -103,3 +103,30 @@ def test_upload_primitives_reproduces_the_iterated_state(precision):
         s1, s2 = e1.download(b), e2.download(b)
         for k in ("pv", "dv", "tv"):
             assert np.array_equal(s2[k][3:-3, 3:-3, 3:-3], s1[k][3:-3, 3:-3, 3:-3]), (b, k)
+
+
+def test_whole_case_transfers_equal_the_per_block_calls():
+    """cfd3d_upload_primitives_all / cfd3d_download_state_all over every block give what
+    the per-block calls give, bit for bit"""
+    c = _case()
+    c["cfg"]["fix_cav_clamp"] = 1
+    e1 = native.Engine(c, precision=abi.MIXED)
+    e1.initialize(c["pv0"])
+    for it in range(2):
+        e1.iterate(1, it + 1, 0.0)
+    st = [e1.download(b) for b in range(2)]
+    ea = native.Engine(c, precision=abi.MIXED)
+    eb = native.Engine(c, precision=abi.MIXED)
+    for e in (ea, eb):
+        e.initialize(c["pv0"])
+    ea.upload_primitives_all([np.ascontiguousarray(s["pv"]) for s in st], [np.ascontiguousarray(s["qq"]) for s in st])
+    for b in range(2):
+        eb.upload_primitives(b, st[b]["pv"], st[b]["qq"])
+    for e in (ea, eb):
+        e.iterate(1, 3, 0.0)
+    outs = [dict(pv=np.zeros_like(s["pv"]), dv=np.zeros_like(s["dv"]), tv=np.zeros_like(s["tv"])) for s in st]
+    ea.download_state_all([o["pv"] for o in outs], [o["dv"] for o in outs], [o["tv"] for o in outs])
+    for b in range(2):
+        ref = eb.download(b)
+        for k in ("pv", "dv", "tv"):
+            assert np.array_equal(outs[b][k], ref[k]), (b, k)
