@@ -389,8 +389,11 @@ def main():
     cfg = case["cfg"]
     nb = len(case["blocks"])
     prec = abi.MIXED if args.precision == "mixed" else abi.FP64
+    t_setup = time.perf_counter()
     eng = native.Engine(case, precision=prec)
+    t_create = time.perf_counter()
     eng.initialize(case["pv0"])
+    t_init = time.perf_counter()
     ncell = cases.total_cells(case)
     res0 = [eng.residual(n)["res"] for n in range(nb)] if prec == abi.MIXED else None
     for w in range(args.warmup):
@@ -444,6 +447,9 @@ def main():
                               "peak_kind": "measured: cfd3d_fp64_peak, independent DFMA chains, 1 s"}},
         "e2e": e2e,
         "gpu_launches": stats["launches_per_iter"] * args.steps,
+        "setup_s": {"create": t_create - t_setup, "initialize": t_init - t_create,
+                    "what": "cfd3d_create (metrics, wall distance, boundary program, tiles, device buffers) "
+                            "and cfd3d_initialize (state upload and EOS) of the mixed engine"},
         "clocks": clk.summary(),
     }
     if prec == abi.MIXED and (args.fp64_steps > 0 or args.field_iters > 0):
