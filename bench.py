@@ -389,9 +389,12 @@ def main():
     cfg = case["cfg"]
     nb = len(case["blocks"])
     prec = abi.MIXED if args.precision == "mixed" else abi.FP64
+    import torch
+    free0 = torch.cuda.mem_get_info(local)[0]
     t_setup = time.perf_counter()
     eng = native.Engine(case, precision=prec)
     t_create = time.perf_counter()
+    device_gb = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
     eng.initialize(case["pv0"])
     t_init = time.perf_counter()
     ncell = cases.total_cells(case)
@@ -449,7 +452,8 @@ def main():
         "gpu_launches": stats["launches_per_iter"] * args.steps,
         "setup_s": {"create": t_create - t_setup, "initialize": t_init - t_create,
                     "what": "cfd3d_create (metrics, wall distance, boundary program, tiles, device buffers) "
-                            "and cfd3d_initialize (state upload and EOS) of the mixed engine"},
+                            "and cfd3d_initialize (state upload and EOS) of the mixed engine",
+                    "device_gb": device_gb},
         "clocks": clk.summary(),
     }
     if prec == abi.MIXED and (args.fp64_steps > 0 or args.field_iters > 0):

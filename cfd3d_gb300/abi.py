@@ -54,6 +54,7 @@ class Config(C.Structure):
         ("fix_cav_clamp", C.c_int), ("precision", C.c_int),
         ("kinf", C.c_double), ("oinf", C.c_double),
         ("gravity", C.c_int), ("ngravity", C.c_int), ("gravity_data", C.POINTER(C.c_double)),
+        ("csf", C.c_int), ("rotation", C.c_int), ("rpm", C.c_double),
     ]
 
 
@@ -80,7 +81,8 @@ def config_from_dict(d):
                     nmuscl=1, nlim=1, timemethod=3, local=1, prec=1, cfl=1.0, fluid=2, ngas=1, ncav=0,
                     c_v=0.0, c_c=0.0, pref=101325.0, uref=10.0, aoa=0.0, aos=0.0, tref=300.0,
                     y1ref=0.0, y2ref=1e-7, l_chord=1.0, l_character=1.0, scale=1.0, l_domain=1.0,
-                    fix_cav_clamp=0, precision=FP64, kinf=0.0, oinf=0.0, gravity=0)
+                    fix_cav_clamp=0, precision=FP64, kinf=0.0, oinf=0.0, gravity=0, csf=0, rotation=0,
+                    rpm=0.0)
     defaults.update(d)
     table = defaults.pop("gravity_data", None)
     for k, v in defaults.items():

@@ -8,9 +8,9 @@ label line followed by a value line, read list-directed in this order
   gravity csf | rotation rpm | pref uref aoa aos tref y1ref y2ref |
   l_chord l_character scale l_domain
 
-and returns the dict `cfd3d_gb300.abi.config_from_dict` accepts.  Options the engine
-does not implement (gravity, csf, rotation, restart) are returned so a caller can reject
-them.
+and returns the dict `cfd3d_gb300.abi.config_from_dict` accepts.  A restart request
+(iread), which the caller serves through `Solver.solve(restart=...)`, is returned as an
+option the engine itself does not take.
 """
 
 FIELDS = [
@@ -30,7 +30,7 @@ FIELDS = [
 ]
 REALS = {"dt_phy", "cfl", "c_v", "c_c", "rpm", "pref", "uref", "aoa", "aos", "tref", "y1ref", "y2ref",
          "l_chord", "l_character", "scale", "l_domain"}
-UNSUPPORTED = {"gravity": 0, "csf": 0, "rotation": 0, "iread": 0}
+UNSUPPORTED = {"iread": 0}
 
 
 def _num(tok, real):

@@ -583,11 +583,113 @@ __global__ void k_closure(DevPtr d, Par c) {
   }
 }
 
+// ------------------------------------------------------------------ surface tension
+// Products that are summed are rounded first (no multiply-add contraction), as the
+// reference's evaluation order gives them, so that the interface threshold |vfg| = 0.04 and
+// the curvature see the same values as the CPU restatement.
+__device__ __forceinline__ double mr(double a, double b) { return __dmul_rn(a, b); }
+
+// (block, i, j, k) of padded cell g
+__device__ __forceinline__ int padded_ijk(const DevPtr& d, long long g, int& i, int& j, int& k) {
+  const int b = find_block_cell(d.blk, d.nblk, g);
+  const BlockGeom& B = d.blk[b];
+  const long long r = g - B.off;
+  i = (int)(r % B.ni) - 1;
+  const long long r2 = r / B.ni;
+  j = (int)(r2 % B.nj) - 1;
+  k = (int)(r2 / B.nj) - 1;
+  return b;
+}
+
+// calvfg (src/variable_module.f90:304-318): vf = rho (y1 / rho_v + y2 / rho_g), the volume
+// fraction of vapour and gas, over the cells 0..imax+2 of each block
+__global__ void k_vf(DevPtr d) {
+  const long long n = d.ncell;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const BlockGeom& B = d.blk[padded_ijk(d, g, i, j, k)];
+    if (i < 0 || j < 0 || k < 0 || i > B.imax + 2 || j > B.jmax + 2 || k > B.kmax + 2) continue;
+    d.vf[g] = d.dv[g] * (d.pv[5 * n + g] / d.dv[3 * n + g] + d.pv[6 * n + g] / d.dv[4 * n + g]);
+  }
+}
+
+// calvfg / calgrad_gg (:320-377): the Green-Gauss gradient of vf over the cells 1..imax+1,
+// the interior and the first ghost layer.  For the ghost layer the reference reads face
+// vectors past the ends of its arrays (cx(0), cx(imax+1), ex(., 0, .), ex(., jmax+1, .),
+// tx(., ., 0), tx(., ., kmax+1)), which hold no defined values; here such a face takes the
+// vector of the nearest face of its row.
+__global__ void k_vfg(DevPtr d) {
+  const long long n = d.ncell;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const BlockGeom& B = d.blk[padded_ijk(d, g, i, j, k)];
+    if (i < 1 || j < 1 || k < 1 || i > B.imax + 1 || j > B.jmax + 1 || k > B.kmax + 1) continue;
+    const long long sj = B.ni, sk = (long long)B.ni * B.nj;
+    const double x[7] = {d.vf[g - 1], d.vf[g + 1], d.vf[g - sj], d.vf[g + sj], d.vf[g - sk], d.vf[g + sk], d.vf[g]};
+    const long long f[6] = {g + (max(i - 1, 1) - i), g + (min(i, B.imax) - i), g + (max(j - 1, 1) - j) * sj,
+                            g + (min(j, B.jmax) - j) * sj, g + (max(k - 1, 1) - k) * sk, g + (min(k, B.kmax) - k) * sk};
+    const int pl[6] = {GM_CX, GM_CX, GM_EX, GM_EX, GM_TX, GM_TX};
+    double gr[3] = {0.0, 0.0, 0.0};
+    for (int l = 0; l < 6; ++l) {
+      const double xm = 0.5 * (x[6] + x[l]);
+      const double sg = (l % 2 == 0) ? -1.0 : 1.0;
+      for (int e = 0; e < 3; ++e) gr[e] = gr[e] + mr(xm, sg * d.gm[(pl[l] + e) * n + f[l]]);
+    }
+    const double vol = d.gm[GM_GRD * n + g];
+    for (int e = 0; e < 3; ++e) d.vfg[e * n + g] = gr[e] / vol;
+  }
+}
+
+// setbc_vfg (src/bc_module.f90:1398-1804): across each 1-to-1 interface the donor's first
+// ghost layer takes the block's first interior layer
+__global__ void k_vfg_halo(DevPtr d) {
+  const long long n = d.ncell;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= d.nvfg_halo) return;
+  const long long src = d.vfg_halo[2 * q], dst = d.vfg_halo[2 * q + 1];
+  for (int e = 0; e < 3; ++e) d.vfg[e * n + dst] = d.vfg[e * n + src];
+}
+
+// csfsource (src/csf_module.f90:97-175) of interior cell g as calrhs calls it
+// (src/rhs_module.f90:607-635): vfg of the cell and its six neighbours, the outward face
+// vectors -cx(i-1), cx(i), -ex(j-1), ex(j), -tx(k-1), tx(k).  Below |vfg| = 0.04 there is no
+// interface and the source is zero.  The surface tension is the reference's constant
+// 0.071684196047 N/m in every cell, so its tangential (Marangoni) part, made of its
+// differences, is zero.  out: the five flow components of the source, times the volume.
+__device__ void csf_cell(const DevPtr& d, long long g, long long sj, long long sk, double vol, const double* pvc,
+                         double* out) {
+  const long long n = d.ncell;
+  for (int q = 0; q < 5; ++q) out[q] = 0.0;
+  const long long nb[7] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk, g};
+  double v[7][3];
+  for (int l = 0; l < 7; ++l)
+    for (int e = 0; e < 3; ++e) v[l][e] = d.vfg[e * n + nb[l]];
+  const double delta = sqrt(mr(v[6][0], v[6][0]) + mr(v[6][1], v[6][1]) + mr(v[6][2], v[6][2]));
+  if (delta <= 0.04) return;
+  const double sigma = 0.071684196047;
+  double nv[7][3];
+  for (int l = 0; l < 7; ++l) {
+    const double dl = mr(v[l][0], v[l][0]) + mr(v[l][1], v[l][1]) + mr(v[l][2], v[l][2]);
+    for (int e = 0; e < 3; ++e) nv[l][e] = (dl > 0.0) ? v[l][e] / sqrt(dl) : 0.0;
+  }
+  const long long f[6] = {g - 1, g, g - sj, g, g - sk, g};
+  const int pl[6] = {GM_CX, GM_CX, GM_EX, GM_EX, GM_TX, GM_TX};
+  double kappa = 0.0;
+  for (int m = 0; m < 6; ++m) {
+    const double sg = (m % 2 == 0) ? -1.0 : 1.0;
+    for (int e = 0; e < 3; ++e) kappa = kappa + mr(0.5 * (nv[6][e] + nv[m][e]), sg * d.gm[(pl[m] + e) * n + f[m]]);
+  }
+  kappa = -kappa / vol;
+  for (int e = 0; e < 3; ++e) out[1 + e] = sigma * kappa * v[6][e];
+  out[4] = mr(out[1], pvc[1]) + mr(out[2], pvc[2]) + mr(out[3], pvc[3]);
+  for (int q = 0; q < 5; ++q) out[q] = out[q] * vol;
+}
+
 // ------------------------------------------------------------------ residual + sources
 // REC = false (the explicit schemes): the residual alone, without the sweep records (a
 // separate instantiation, so that the LU-SGS kernel carries no branch for it)
-// XS (extended sources): the SST destruction with the DES length scale of c.ides and the
-// gravity source (a separate instantiation, so that the plain kernel carries none of their
+// XS (extended sources): the SST destruction with the DES length scale of c.ides, the
+// gravity and the surface-tension sources (a separate instantiation, so that the plain kernel carries none of their
 // code)
 template <bool MX, bool REC = true, bool XS = false>
 __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
@@ -824,6 +926,12 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     const double rv = dv[0] * vol;
     for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] + rv * a[e];
     res[4] = res[4] + rv * (a[0] * pv2[1] + a[1] * pv2[2] + a[2] * pv2[3]);
+  }
+  if (XS && c.csf) {
+    double cs[5];
+    csf_cell(d, g, sj, sk, vol, pv2, cs);
+    for (int q = 0; q < 5; ++q) res[q] = res[q] + cs[q];
+    for (int e = 0; e < 3; ++e) d.csf[e * n + g] = cs[1 + e];
   }
   for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
   if constexpr (!REC) return;   // the explicit schemes need no sweep records
@@ -1634,7 +1742,7 @@ template <bool REC>
 void launch_rhs_rec(const Engine& E, cudaStream_t s, int T) {
   const Par& c = E.par;
   const unsigned g = nblk_of(E.nint, T);
-  const bool xs = (c.iturb == 0 && c.ides != 0) || c.gravity != 0;
+  const bool xs = (c.iturb == 0 && c.ides != 0) || c.gravity != 0 || c.csf != 0;
   if (c.mixed) {
     if (xs) k_rhs<true, REC, true><<<g, T, 0, s>>>(E.d, c);
     else k_rhs<true, REC, false><<<g, T, 0, s>>>(E.d, c);
@@ -1646,6 +1754,25 @@ void launch_rhs_rec(const Engine& E, cudaStream_t s, int T) {
 void launch_rhs(const Engine& E, cudaStream_t s, int T, bool rec) {
   if (rec) launch_rhs_rec<true>(E, s, T);
   else launch_rhs_rec<false>(E, s, T);
+}
+
+// The boundary program -- the total-pressure pools, then faces + halos, edges, corners -- and,
+// with the surface-tension source, calvfg and setbc_vfg after it, as timeinteg calls them
+// (src/update_module.f90:240-243, 359-362, 479-482).  Returns the number of launches.
+int launch_boundary(const Engine& E, cudaStream_t s) {
+  const DevPtr& d = E.d;
+  const Par& c = E.par;
+  int n = 0;
+  if (d.ntp) { k_totalp<<<d.ntp, 128, 0, s>>>(d, c); ++n; }
+  for (int p = 0; p < 3; ++p)
+    if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
+  if (c.csf) {
+    k_vf<<<nblk_of(E.ncell, 256), 256, 0, s>>>(d);
+    k_vfg<<<nblk_of(E.ncell, 256), 256, 0, s>>>(d);
+    n += 2;
+    if (d.nvfg_halo) { k_vfg_halo<<<nblk_of(d.nvfg_halo, 256), 256, 0, s>>>(d); ++n; }
+  }
+  return n;
 }
 
 // the launch sequence of one iteration (captured into the graph); `mark` (optional)
@@ -1664,9 +1791,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
     ++n;
   }
   stage(1);
-  if (d.ntp) { k_totalp<<<d.ntp, 128, 0, s>>>(d, c); ++n; }
-  for (int p = 0; p < 3; ++p)
-    if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
+  n += launch_boundary(E, s);
   stage(2);
   if (c.mixed) launch_face_flux_mixed(E, s);
   else launch_face_flux(E, s);
@@ -1681,9 +1806,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
     const int nstage = (c.timemethod == 2) ? 3 : 1;
     for (int m = 1; m <= nstage; ++m) {
       if (m > 1) {
-        if (d.ntp) { k_totalp<<<d.ntp, 128, 0, s>>>(d, c); ++n; }
-        for (int p = 0; p < 3; ++p)
-          if (E.nops[p]) { k_ghost<<<nblk_of(E.nops[p], 128), 128, 0, s>>>(d, c, E.d_ops[p], E.nops[p]); ++n; }
+        n += launch_boundary(E, s);
         if (c.mixed) launch_face_flux_mixed(E, s);
         else launch_face_flux(E, s);
         launch_rhs(E, s, E.tpb_rhs, false);
@@ -1799,6 +1922,9 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   if (in->ncav < 0 || in->ncav > 5) { err = "ncav out of range"; return false; }
   if (in->local < -1 || in->local > 1) { err = "local out of range"; return false; }
   if (in->prec < 0 || in->prec > 2) { err = "prec out of range"; return false; }
+  if (in->csf != 0 && in->csf != 1) { err = "csf must be 0 or 1"; return false; }
+  c.csf = in->csf;
+  if (in->rotation != 0) { err = "rotation is not supported"; return false; }
   if (in->nsteady >= 1 && !(in->dt_phy > 0.0)) { err = "dual time stepping needs dt_phy > 0"; return false; }
   if (in->precision != CFD3D_FP64 && in->precision != CFD3D_MIXED) { err = "precision must be CFD3D_FP64 or CFD3D_MIXED"; return false; }
   c.mixed = (in->precision == CFD3D_MIXED);
@@ -2022,6 +2148,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
          allocf(E.d.frec, 2 * 12) && allocf(E.d.lqf, NLQ);
   else
     ok = ok && alloc(E.d.fi, 3 * c.npv) && alloc(E.d.fv, (c.iturb == -3) ? 1 : 3 * c.npv);
+  if (c.csf) ok = ok && alloc(E.d.vf, 1) && alloc(E.d.vfg, 3) && alloc(E.d.csf, 3);
   if (!ok) { E.err = "device allocation failed"; return CFD3D_ERR_NOMEM; }
   E.d.ncell = n;
   E.d.nint = E.nint;
@@ -2110,6 +2237,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     for (int v = 0; v < NPVM; ++v) split((v >= 1 && v <= 3) ? U[v - 1] : sc[v], E.par.sc2[v]);
   }
   if (!setup_geometry(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
+  if (c.csf && !setup_vfg_halo(E, blocks, nblocks)) return CFD3D_ERR_DESCRIPTOR;
   if (c.mixed) {
     const long long m = (long long)(GM_GRD + c.ngrd) * E.ncell;
     if (cudaMalloc(&E.d.gmf, (size_t)m * 4) != cudaSuccess) { E.err = "device allocation failed (gmf)"; return CFD3D_ERR_NOMEM; }
@@ -2163,7 +2291,8 @@ void cfd3d_destroy(cfd3d_handle* h) {
   Engine& E = h->E;
   if (E.graph) cudaGraphExecDestroy(E.graph);
   double* bufs[] = {E.d.pv, E.d.dv, E.d.tv, E.d.gm, E.d.res, E.d.icav, E.d.itt, E.d.ocut, E.d.dt, E.d.rcav,
-                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging, E.d.clo};
+                    E.d.qq, E.d.dqs, E.d.dcv, E.d.fi, E.d.fv, E.d.partial, h->staging, E.d.clo,
+                    E.d.vf, E.d.vfg, E.d.csf};
   for (double* p : bufs) cudaFree(p);
   float* fbufs[] = {E.d.pvf, E.d.fi32, E.d.fv32, E.d.frec, E.d.gmf, E.d.gmlo, E.d.lqf};
   for (float* p : fbufs) cudaFree(p);
@@ -2176,6 +2305,7 @@ void cfd3d_destroy(cfd3d_handle* h) {
   cudaFree(E.d_nbb);
   cudaFree(E.d_hft);
   cudaFree(E.d_grav);
+  cudaFree((void*)E.d.vfg_halo);
   cudaFree(E.d_tp_off);
   cudaFree(E.d_tp_ent);
   cudaFree(E.d_tp_x);
@@ -2348,6 +2478,22 @@ int cfd3d_upload_state(cfd3d_handle* h, int block, const double* pv, const doubl
   return drain_on_error(h, upload_state(h, block, pv, dv, tv, qq));
 }
 
+int cfd3d_download_csf(cfd3d_handle* h, int block, double* csf) {
+  if (!h || !csf) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  if (!E.par.csf) { E.err = "the case has no surface-tension source"; return CFD3D_ERR_ARG; }
+  if (block < 0 || block >= (int)E.blk.size()) { E.err = "bad block"; return CFD3D_ERR_ARG; }
+  const BlockGeom& B = E.blk[block];
+  const long long nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
+  int rc = ensure_staging(h, (size_t)nint * 3 * 8);
+  if (rc) return rc;
+  k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(h->staging, 3, B, E.d.csf, E.ncell, 0);
+  CFD_CUDA(cudaMemcpyAsync(csf, h->staging, (size_t)nint * 3 * 8, cudaMemcpyDeviceToHost, E.st));
+  CFD_CUDA(cudaStreamSynchronize(E.st));
+  CFD_CUDA(cudaGetLastError());
+  return CFD3D_OK;
+}
+
 int cfd3d_download_state(cfd3d_handle* h, int block, double* pv, double* dv, double* tv, double* qq, double* rcav) {
   if (!h) return CFD3D_ERR_ARG;
   return drain_on_error(h, download_state(h, block, pv, dv, tv, qq, rcav));
@@ -2500,8 +2646,8 @@ namespace {
 
 struct CkptRecord {
   long long npad, nint;                     // padded and interior cells of the block
-  bool turb, cav;                           // l_turb (iturb >= -1), l_cav (ncav != 0)
-  long long pv_off, emut_off, qq_off, rcav_off, bytes;   // byte offsets within the record
+  bool turb, cav, csf;                      // l_turb (iturb >= -1), l_cav (ncav != 0), l_csf
+  long long pv_off, emut_off, qq_off, rcav_off, csf_off, bytes;   // byte offsets within the record
 };
 
 CkptRecord ckpt_record(const Par& c, const BlockGeom& B, bool with_qq) {
@@ -2510,11 +2656,13 @@ CkptRecord ckpt_record(const Par& c, const BlockGeom& B, bool with_qq) {
   r.nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
   r.turb = c.iturb >= -1;
   r.cav = c.ncav != 0;
+  r.csf = c.csf != 0;
   r.pv_off = 4 + 4 + 8;                      // nt_phy, nt (default integers), time
   r.emut_off = r.pv_off + 8ll * c.npv * r.npad;
   r.qq_off = r.emut_off + (r.turb ? 8ll * r.npad : 0);
   r.rcav_off = r.qq_off + (with_qq ? 8ll * c.nqq * c.npv * r.nint : 0);
-  r.bytes = r.rcav_off + (r.cav ? 16ll * r.nint : 0);
+  r.csf_off = r.rcav_off + (r.cav ? 16ll * r.nint : 0);
+  r.bytes = r.csf_off + (r.csf ? 24ll * r.nint : 0);
   return r;
 }
 
@@ -2552,7 +2700,7 @@ int cfd3d_checkpoint_write(cfd3d_handle* h, const char* path, int nt_phy, int nt
   if (fd < 0) { E.err = std::string("cannot open checkpoint for writing: ") + path; return CFD3D_ERR_IO; }
   long long disp = 0;
   int rc = CFD3D_OK;
-  std::vector<double> pv, tv, qq, rcav, emut;
+  std::vector<double> pv, tv, qq, rcav, emut, csf;
   for (int b = 0; b < (int)E.blk.size() && rc == CFD3D_OK; ++b) {
     const BlockGeom& B = E.blk[b];
     const CkptRecord r = ckpt_record(c, B, true);
@@ -2563,6 +2711,10 @@ int cfd3d_checkpoint_write(cfd3d_handle* h, const char* path, int nt_phy, int nt
     rc = cfd3d_download_state(h, b, pv.data(), nullptr, c.ntv ? tv.data() : nullptr, c.nqq ? qq.data() : nullptr,
                               rcav.data());
     if (rc) break;
+    if (r.csf) {
+      csf.assign((size_t)(3 * r.nint), 0.0);
+      if ((rc = cfd3d_download_csf(h, b, csf.data()))) break;
+    }
     char head[16];
     const int32_t i2[2] = {(int32_t)nt_phy, (int32_t)nt};
     memcpy(head, i2, 8);
@@ -2577,6 +2729,7 @@ int cfd3d_checkpoint_write(cfd3d_handle* h, const char* path, int nt_phy, int nt
     }
     if (ok && c.nqq) ok = pio(fd, qq.data(), 8ll * c.nqq * c.npv * r.nint, disp + r.qq_off, true);
     if (ok && r.cav) ok = pio(fd, rcav.data(), 16ll * r.nint, disp + r.rcav_off, true);
+    if (ok && r.csf) ok = pio(fd, csf.data(), 24ll * r.nint, disp + r.csf_off, true);
     if (!ok) { E.err = std::string("checkpoint write failed: ") + path; rc = CFD3D_ERR_IO; }
     disp += r.bytes;
   }
@@ -2621,12 +2774,13 @@ int cfd3d_checkpoint_read(cfd3d_handle* h, const char* path, int steady_start, i
       for (long long q = 0; q < r.nint; ++q) interior[(size_t)(q * c.npv + v)] = buf[(size_t)q];
     }
     if ((rc = cfd3d_initialize(h, b, interior.data()))) break;
-    // tv(3) = emut, qq and rcav from the file, interior cells only
+    // tv(3) = emut, qq, rcav and the surface-tension source from the file, interior cells only
     struct Part { bool on; long long off; int nv; bool padded; double* dst; };
-    const Part parts[3] = {
+    const Part parts[4] = {
         {r.turb && c.ntv >= 3, r.emut_off, 1, true, E.d.tv + 2 * E.ncell},
         {with_qq && c.nqq > 0, r.qq_off, c.nqq * c.npv, false, E.d.qq},
-        {r.cav, r.rcav_off, 2, false, E.d.rcav}};
+        {r.cav, r.rcav_off, 2, false, E.d.rcav},
+        {r.csf, r.csf_off, 3, false, E.d.csf}};
     for (const Part& p : parts) {
       if (!p.on) continue;
       const long long cnt = p.nv * (p.padded ? r.npad : r.nint);
@@ -2774,6 +2928,7 @@ int cfd3d_residual_vjp(cfd3d_handle* h, const double* cot, double* g_state, doub
   if (rc) return rc;
   if (E.par.iturb == -1) { E.err = "the adjoint does not cover the k-epsilon model"; return CFD3D_ERR_ARG; }
   if (E.d.ntp) { E.err = "the adjoint does not cover total-pressure inlets"; return CFD3D_ERR_ARG; }
+  if (E.par.csf) { E.err = "the adjoint does not cover the surface-tension source"; return CFD3D_ERR_ARG; }
   if ((rc = adjoint_buffers(E))) return rc;
   // the cotangent, block after block, into the padded interior
   size_t off = 0;

@@ -134,6 +134,12 @@ struct DevPtr {
   Scalars* sc;
   const double* hft;   // heat-flux histories: per table n, t[n], q[n] (GhostOp.pad is its offset)
   const double* grav;  // gravity history: n, t[n], a[3 n] (a constant acceleration is one row)
+  // surface tension (csf = 1): per padded cell the vapour + gas volume fraction vf, its
+  // gradient vfg (3 planes, cells 1..imax+1 of each block) and the source of the last
+  // residual (3 planes, interior cells); the vfg halo as (source, target) cell pairs
+  double *vf, *vfg, *csf;
+  const int* vfg_halo;
+  int nvfg_halo;
   // total-pressure inlets: per pool p (the p-th inlet of every block) [tp_off[p], tp_off[p+1])
   // face entries (boundary cell, face-vector cell, plane, sign) and the solved (p, T, |u|^2)
   // in tp_x[3 p..]
@@ -339,6 +345,7 @@ void adjoint_free(Engine& E);
 bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks);
 bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks);
 void setup_planes(Engine& E);
+bool setup_vfg_halo(Engine& E, const cfd3d_block_desc* blocks, int nblocks);
 bool setup_tiles(Engine& E);
 
 #define CFD_CUDA(call)                                                                 \

@@ -151,15 +151,17 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
       c9[v] = x[8]; c10[v] = x[9];
     }
     muscl_clip_mx(c, c9, c10, gl, gR);
-    // a vapour-free face state next to its interior base cell by expansion; any other by
-    // the IF97 sums (FP64 mixture)
-    if (!(f.lin && gl[5] == 0.0f && liquid_expand(d, c, g, gl, c9, rdl, hdl))) {
+    // a vapour-free face state by expansion about an interior cell -- its own side's, or at
+    // a block face, where that cell is a ghost, the cell across the face; any other state by
+    // the IF97 sums (FP64 mixture).  (Without the second base, the boundary faces of the i
+    // direction, two in every warp's row of faces, would send their warps through the sums.)
+    if (!(gl[5] == 0.0f && liquid_expand(d, c, f.lin ? g : gr, gl, f.lin ? c9 : c10, rdl, hdl))) {
       double rho, h;
       eos_rho_h<true>(c.fluid, c.pref + (double)gl[0], c.tref + (double)gl[4], gl[5], gl[6], rho, h);
       rdl = (float)(rho - c.rhoref);
       hdl = (float)(h - c.href);
     }
-    if (!(f.rin && gR[5] == 0.0f && liquid_expand(d, c, gr, gR, c10, rdr, hdr))) {
+    if (!(gR[5] == 0.0f && liquid_expand(d, c, f.rin ? gr : g, gR, f.rin ? c10 : c9, rdr, hdr))) {
       double rho, h;
       eos_rho_h<true>(c.fluid, c.pref + (double)gR[0], c.tref + (double)gR[4], gR[5], gR[6], rho, h);
       rdr = (float)(rho - c.rhoref);

@@ -32,6 +32,7 @@ struct Par {
   int timemethod;   // 1 explicit Euler, 2 third-order Runge-Kutta, 3 LU-SGS
   int ides;         // SST length scale: 0 RANS, 1 DES, 2 DDES, 3 IDDES, 4 simplified IDDES
   int gravity;      // gravity source: 0 none, else the device history d.grav
+  int csf;          // 1: the surface-tension source (d.vfg, d.csf)
   double tp_pt, tp_tt, tp_ht;   // total-pressure inlet: p_total, T_total, h(p_total, T_total)
   double dt_phy, cfl, c_v, c_c, pref, uref, str, rhoref, l_chord;
   double kref, oref, emutref;

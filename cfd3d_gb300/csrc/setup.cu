@@ -1,8 +1,8 @@
 // setup.cu -- build-time work of the engine (runs once per cfd3d_create).
 //
-//  * grid metrics: face area vectors, volumes, centroids (calnormal / calvolume,
-//    src/grid_module.f90:609-1241) computed on the host per block, with the reference's
-//    metric halos across 1-to-1 interfaces (:725-940, :1115-1212);
+//  * grid metrics on the device: face area vectors, volumes, centroids (calnormal /
+//    calvolume, src/grid_module.f90:609-1241), their ghost rows and the reference's metric
+//    halos across 1-to-1 interfaces (:725-940, :1115-1212), from the node coordinates;
 //  * wall distance (calydns, :350-607) as a two-pass brute-force GPU kernel: an FP32
 //    pass finds each cell's nearest wall-face distance, an FP64 pass re-evaluates only
 //    the faces within a relative margin of it, so the result equals the FP64 minimum;
@@ -21,155 +21,153 @@ namespace cfd {
 
 namespace {
 
-struct HBlock {
-  int im, jm, km;
-  std::vector<double> x;   // x(3, 2:im+1, 2:jm+1, 2:km+1)
-  std::vector<double> cx, ex, tx, grd;  // Fortran ranges as in the reference
-  int ngrd;
-  double& X(int v, int i, int j, int k) { return x[v + 3 * ((i - 2) + (size_t)im * ((j - 2) + (size_t)jm * (k - 2)))]; }
-  double& CX(int v, int i, int j, int k) { return cx[v + 3 * ((i - 1) + (size_t)im * ((j - 1) + (size_t)(jm + 1) * (k - 1)))]; }
-  double& EX(int v, int i, int j, int k) { return ex[v + 3 * ((i - 1) + (size_t)(im + 1) * ((j - 1) + (size_t)jm * (k - 1)))]; }
-  double& TX(int v, int i, int j, int k) { return tx[v + 3 * ((i - 1) + (size_t)(im + 1) * ((j - 1) + (size_t)(jm + 1) * (k - 1)))]; }
-  double& G(int v, int i, int j, int k) { return grd[v + ngrd * ((i - 1) + (size_t)(im + 1) * ((j - 1) + (size_t)(jm + 1) * (k - 1)))]; }
-};
-
 struct Con {
   int donor;
   int s[3], e[3], sd[3], ed[3];
   int tm[3][3];
 };
 
-double pyramid(const double* pa, const double* pb, const double* pc, const double* pd, const double* cen) {
+// ---- grid metrics on the device --------------------------------------------------------
+// One block's node coordinates x(3, 2:imax+1, 2:jmax+1, 2:kmax+1), the reference's node
+// range, as the block descriptor holds them.
+struct NodeBlock {
+  const double* x;
+  int im, jm;
+  __device__ double operator()(int v, int i, int j, int k) const {
+    return x[v + 3 * ((i - 2) + (long long)im * ((j - 2) + (long long)jm * (k - 2)))];
+  }
+};
+__device__ __forceinline__ long long gidx(const BlockGeom& G, int i, int j, int k) {
+  return G.off + (i + 1) + (long long)G.ni * ((j + 1) + (long long)G.nj * (k + 1));
+}
+// (i, j, k) inside the block's padded box -1..imax+3 (a connection's mapped index must be)
+__device__ __forceinline__ bool in_box(const BlockGeom& G, int i, int j, int k) {
+  return i >= -1 && i < G.ni - 1 && j >= -1 && j < G.nj - 1 && k >= -1 && k < G.nk - 1;
+}
+// Products are rounded before they are summed (no multiply-add contraction), as the
+// reference's evaluation order gives them; the metrics then equal the CPU restatement's.
+__device__ __forceinline__ double mulr(double a, double b) { return __dmul_rn(a, b); }
+
+__device__ double pyramid(const double* pa, const double* pb, const double* pc, const double* pd, const double* cen) {
   double cs[3], va[3], vb[3];
   for (int v = 0; v < 3; ++v) {
     cs[v] = 0.25 * (pa[v] + pb[v] + pc[v] + pd[v]);
     va[v] = pc[v] - pa[v];
     vb[v] = pd[v] - pb[v];
   }
-  double px = (cen[0] - cs[0]) * (va[1] * vb[2] - va[2] * vb[1]);
-  double py = (cen[1] - cs[1]) * (va[2] * vb[0] - va[0] * vb[2]);
-  double pz = (cen[2] - cs[2]) * (va[0] * vb[1] - va[1] * vb[0]);
-  return std::fabs(px + py + pz);
+  const double px = mulr(cen[0] - cs[0], mulr(va[1], vb[2]) - mulr(va[2], vb[1]));
+  const double py = mulr(cen[1] - cs[1], mulr(va[2], vb[0]) - mulr(va[0], vb[2]));
+  const double pz = mulr(cen[2] - cs[2], mulr(va[0], vb[1]) - mulr(va[1], vb[0]));
+  return fabs(px + py + pz);
 }
 
-void face_vectors(HBlock& B, const cfd3d_block_desc& d) {
-  const int im = B.im, jm = B.jm, km = B.km;
-  B.cx.assign(3 * (size_t)im * (jm + 1) * (km + 1), 0.0);
-  B.ex.assign(3 * (size_t)(im + 1) * jm * (km + 1), 0.0);
-  B.tx.assign(3 * (size_t)(im + 1) * (jm + 1) * km, 0.0);
-  auto cross_half = [](const double* a, const double* b, double* out) {
-    out[0] = 0.5 * (a[1] * b[2] - b[1] * a[2]);
-    out[1] = 0.5 * (b[0] * a[2] - a[0] * b[2]);
-    out[2] = 0.5 * (a[0] * b[1] - b[0] * a[1]);
-  };
-  for (int k = 2; k <= km; ++k)
-    for (int j = 2; j <= jm; ++j)
-      for (int i = 1; i <= im; ++i) {
-        double e[3], s[3], o[3];
-        for (int v = 0; v < 3; ++v) {
-          e[v] = B.X(v, i + 1, j + 1, k) - B.X(v, i + 1, j, k + 1);
-          s[v] = B.X(v, i + 1, j + 1, k + 1) - B.X(v, i + 1, j, k);
-        }
-        cross_half(e, s, o);
-        for (int v = 0; v < 3; ++v) B.CX(v, i, j, k) = o[v];
-      }
-  for (int i = 2; i <= im; ++i)
-    for (int k = 2; k <= km; ++k)
-      for (int j = 1; j <= jm; ++j) {
-        double c[3], s[3], o[3];
-        for (int v = 0; v < 3; ++v) {
-          c[v] = B.X(v, i, j + 1, k) - B.X(v, i + 1, j + 1, k + 1);
-          s[v] = B.X(v, i, j + 1, k + 1) - B.X(v, i + 1, j + 1, k);
-        }
-        cross_half(c, s, o);
-        for (int v = 0; v < 3; ++v) B.EX(v, i, j, k) = o[v];
-      }
-  for (int j = 2; j <= jm; ++j)
-    for (int i = 2; i <= im; ++i)
-      for (int k = 1; k <= km; ++k) {
-        double c[3], e[3], o[3];
-        for (int v = 0; v < 3; ++v) {
-          c[v] = B.X(v, i + 1, j, k + 1) - B.X(v, i, j + 1, k + 1);
-          e[v] = B.X(v, i + 1, j + 1, k + 1) - B.X(v, i, j, k + 1);
-        }
-        cross_half(c, e, o);
-        for (int v = 0; v < 3; ++v) B.TX(v, i, j, k) = o[v];
-      }
-  // degenerate patches zero the boundary face vectors (src/grid_module.f90:672-708)
-  for (int n = 0; n < d.nbc; ++n) {
-    if (d.bc[n].type != CFD3D_BC_DEGENERATE) continue;
-    const int* p = d.bc[n].pnts;
-    for (int ax = 0; ax < 3; ++ax) {
-      if (p[ax] != p[3 + ax]) continue;
-      bool mn = (p[ax] == 1);
-      if (ax == 0) { int ii = mn ? 1 : im; for (int k = 1; k <= km + 1; ++k) for (int j = 1; j <= jm + 1; ++j) for (int v = 0; v < 3; ++v) B.CX(v, ii, j, k) = 0.0; }
-      if (ax == 1) { int jj = mn ? 1 : jm; for (int k = 1; k <= km + 1; ++k) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) B.EX(v, i, jj, k) = 0.0; }
-      if (ax == 2) { int kk = mn ? 1 : km; for (int j = 1; j <= jm + 1; ++j) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) B.TX(v, i, j, kk) = 0.0; }
-      break;
+// Face area vectors of direction DIR (calnormal, src/grid_module.f90:609-724): half the
+// cross product of the face's diagonals, for the face array's whole range -- cx over
+// (1..im, 1..jm+1, 1..km+1), ex over (1..im+1, 1..jm, 1..km+1), tx over (1..im+1, 1..jm+1,
+// 1..km).  The reference computes the faces of the interior rows and then copies them to
+// the ghost rows along each transverse direction in turn; clamping the transverse index to
+// the computed rows gives the same values.  A degenerate patch zeroes the whole plane of
+// its face (:672-708), edges included, before those copies (zlo, zhi: first, last plane).
+template <int DIR>
+__global__ void k_geo_faces(BlockGeom G, NodeBlock X, double* __restrict__ gm, long long nc, int zlo, int zhi) {
+  const int im = G.imax, jm = G.jmax, km = G.kmax;
+  const int n0 = DIR == 0 ? im : im + 1, n1 = DIR == 1 ? jm : jm + 1, n2 = DIR == 2 ? km : km + 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)n0 * n1 * n2) return;
+  const int i = (int)(t % n0) + 1;
+  const long long r = t / n0;
+  const int j = (int)(r % n1) + 1, k = (int)(r / n1) + 1;
+  const int a = DIR == 0 ? i : min(max(i, 2), im);
+  const int b = DIR == 1 ? j : min(max(j, 2), jm);
+  const int c = DIR == 2 ? k : min(max(k, 2), km);
+  double p[3], q[3];
+  for (int v = 0; v < 3; ++v) {
+    if (DIR == 0) { p[v] = X(v, a + 1, b + 1, c) - X(v, a + 1, b, c + 1); q[v] = X(v, a + 1, b + 1, c + 1) - X(v, a + 1, b, c); }
+    else if (DIR == 1) { p[v] = X(v, a, b + 1, c) - X(v, a + 1, b + 1, c + 1); q[v] = X(v, a, b + 1, c + 1) - X(v, a + 1, b + 1, c); }
+    else { p[v] = X(v, a + 1, b, c + 1) - X(v, a, b + 1, c + 1); q[v] = X(v, a + 1, b + 1, c + 1) - X(v, a, b, c + 1); }
+  }
+  const int fn = DIR == 0 ? i : (DIR == 1 ? j : k), fmax = DIR == 0 ? im : (DIR == 1 ? jm : km);
+  const bool zero = (fn == 1 && zlo) || (fn == fmax && zhi);
+  const long long g = gidx(G, i, j, k);
+  const int plane = DIR == 0 ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
+  gm[(plane + 0) * nc + g] = zero ? 0.0 : 0.5 * (mulr(p[1], q[2]) - mulr(q[1], p[2]));
+  gm[(plane + 1) * nc + g] = zero ? 0.0 : 0.5 * (mulr(q[0], p[2]) - mulr(p[0], q[2]));
+  gm[(plane + 2) * nc + g] = zero ? 0.0 : 0.5 * (mulr(p[0], q[1]) - mulr(q[0], p[1]));
+}
+
+// Centroid and volume of every interior cell (calvolume, src/grid_module.f90:942-1080):
+// the mean of the eight nodes, and the six pyramids from the centroid to the faces.
+__global__ void k_geo_cells(BlockGeom G, NodeBlock X, double* __restrict__ gm, long long nc) {
+  const int ni = G.imax - 1, nj = G.jmax - 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)ni * nj * (G.kmax - 1)) return;
+  const int i = (int)(t % ni) + 2;
+  const long long r = t / ni;
+  const int j = (int)(r % nj) + 2, k = (int)(r / nj) + 2;
+  double cen[3];
+  for (int v = 0; v < 3; ++v)
+    cen[v] = 0.125 * (X(v, i, j, k) + X(v, i + 1, j, k) + X(v, i, j + 1, k) + X(v, i, j, k + 1) + X(v, i + 1, j + 1, k) +
+                      X(v, i, j + 1, k + 1) + X(v, i + 1, j, k + 1) + X(v, i + 1, j + 1, k + 1));
+  auto P = [&](int a, int b, int c, double* o) { for (int v = 0; v < 3; ++v) o[v] = X(v, a, b, c); };
+  double pa[3], pb[3], pc[3], pd[3], s = 0.0;
+  P(i, j, k, pa); P(i + 1, j, k, pb); P(i + 1, j + 1, k, pc); P(i, j + 1, k, pd); s += pyramid(pa, pb, pc, pd, cen);
+  P(i, j, k + 1, pa); P(i + 1, j, k + 1, pb); P(i + 1, j + 1, k + 1, pc); P(i, j + 1, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+  P(i, j, k, pa); P(i + 1, j, k, pb); P(i + 1, j, k + 1, pc); P(i, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+  P(i, j + 1, k, pa); P(i + 1, j + 1, k, pb); P(i + 1, j + 1, k + 1, pc); P(i, j + 1, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+  P(i, j, k, pa); P(i, j + 1, k, pb); P(i, j + 1, k + 1, pc); P(i, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+  P(i + 1, j, k, pa); P(i + 1, j + 1, k, pb); P(i + 1, j + 1, k + 1, pc); P(i + 1, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
+  const long long g = gidx(G, i, j, k);
+  gm[GM_GRD * nc + g] = s / 6.0;
+  for (int v = 0; v < 3; ++v) gm[(GM_GRD + 1 + v) * nc + g] = cen[v];
+}
+
+// Ghost cells of the cell geometry (src/grid_module.f90:1082-1113 and the wall distance's
+// :560-590), in the reference's three passes: step 0 the j ghosts of the interior rows,
+// step 1 the i ghosts of every j, step 2 the k ghosts of every i and j.  The volume and the
+// wall distance are copied; the centroid is extrapolated linearly, at k = 1 from the fixed
+// cell (3, j, 3) as the reference does.  what: 0 volume and centroid, 1 wall distance.
+__global__ void k_geo_ghosts(BlockGeom G, double* __restrict__ gm, long long nc, int step, int what) {
+  const int im = G.imax, jm = G.jmax, km = G.kmax;
+  const int na = step == 0 ? im - 1 : (step == 1 ? jm + 1 : im + 1);
+  const int nb = step == 2 ? jm + 1 : km - 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nb) return;
+  const int ta = (int)(t % na), tb = (int)(t / na);
+  for (int side = 0; side < 2; ++side) {
+    int i, j, k, i1, j1, k1, i2, j2, k2;   // ghost, nearest interior row, next row
+    if (step == 0) {
+      i = i1 = i2 = ta + 2; k = k1 = k2 = tb + 2;
+      j = side ? jm + 1 : 1; j1 = side ? jm : 2; j2 = side ? jm - 1 : 3;
+    } else if (step == 1) {
+      j = j1 = j2 = ta + 1; k = k1 = k2 = tb + 2;
+      i = side ? im + 1 : 1; i1 = side ? im : 2; i2 = side ? im - 1 : 3;
+    } else {
+      i = i1 = ta + 1; j = j1 = j2 = tb + 1;
+      k = side ? km + 1 : 1; k1 = side ? km : 2;
+      i2 = side ? i : 3; k2 = side ? km - 1 : 3;
+    }
+    const long long g = gidx(G, i, j, k), g1 = gidx(G, i1, j1, k1), g2 = gidx(G, i2, j2, k2);
+    if (what == 1) {
+      gm[(GM_GRD + 4) * nc + g] = gm[(GM_GRD + 4) * nc + g1];
+    } else {
+      gm[GM_GRD * nc + g] = gm[GM_GRD * nc + g1];
+      for (int v = 1; v <= 3; ++v) gm[(GM_GRD + v) * nc + g] = 2.0 * gm[(GM_GRD + v) * nc + g1] - gm[(GM_GRD + v) * nc + g2];
     }
   }
-  // copy to the ghost edges of the face arrays
-  for (int k = 1; k <= km + 1; ++k) for (int i = 1; i <= im; ++i) for (int v = 0; v < 3; ++v) { B.CX(v, i, 1, k) = B.CX(v, i, 2, k); B.CX(v, i, jm + 1, k) = B.CX(v, i, jm, k); }
-  for (int j = 1; j <= jm + 1; ++j) for (int i = 1; i <= im; ++i) for (int v = 0; v < 3; ++v) { B.CX(v, i, j, 1) = B.CX(v, i, j, 2); B.CX(v, i, j, km + 1) = B.CX(v, i, j, km); }
-  for (int k = 1; k <= km + 1; ++k) for (int j = 1; j <= jm; ++j) for (int v = 0; v < 3; ++v) { B.EX(v, 1, j, k) = B.EX(v, 2, j, k); B.EX(v, im + 1, j, k) = B.EX(v, im, j, k); }
-  for (int j = 1; j <= jm; ++j) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) { B.EX(v, i, j, 1) = B.EX(v, i, j, 2); B.EX(v, i, j, km + 1) = B.EX(v, i, j, km); }
-  for (int k = 1; k <= km; ++k) for (int j = 1; j <= jm + 1; ++j) for (int v = 0; v < 3; ++v) { B.TX(v, 1, j, k) = B.TX(v, 2, j, k); B.TX(v, im + 1, j, k) = B.TX(v, im, j, k); }
-  for (int k = 1; k <= km; ++k) for (int i = 1; i <= im + 1; ++i) for (int v = 0; v < 3; ++v) { B.TX(v, i, 1, k) = B.TX(v, i, 2, k); B.TX(v, i, jm + 1, k) = B.TX(v, i, jm, k); }
 }
 
-void volumes(HBlock& B) {
-  const int im = B.im, jm = B.jm, km = B.km;
-  B.grd.assign((size_t)B.ngrd * (im + 1) * (jm + 1) * (km + 1), 0.0);
-  for (int k = 2; k <= km; ++k)
-    for (int j = 2; j <= jm; ++j)
-      for (int i = 2; i <= im; ++i) {
-        double cen[3];
-        for (int v = 0; v < 3; ++v)
-          cen[v] = 0.125 * (B.X(v, i, j, k) + B.X(v, i + 1, j, k) + B.X(v, i, j + 1, k) + B.X(v, i, j, k + 1) +
-                            B.X(v, i + 1, j + 1, k) + B.X(v, i, j + 1, k + 1) + B.X(v, i + 1, j, k + 1) +
-                            B.X(v, i + 1, j + 1, k + 1));
-        for (int v = 0; v < 3; ++v) B.G(1 + v, i, j, k) = cen[v];
-        auto P = [&](int a, int b, int c, double* o) { for (int v = 0; v < 3; ++v) o[v] = B.X(v, a, b, c); };
-        double pa[3], pb[3], pc[3], pd[3], s = 0.0;
-        P(i, j, k, pa); P(i + 1, j, k, pb); P(i + 1, j + 1, k, pc); P(i, j + 1, k, pd); s += pyramid(pa, pb, pc, pd, cen);
-        P(i, j, k + 1, pa); P(i + 1, j, k + 1, pb); P(i + 1, j + 1, k + 1, pc); P(i, j + 1, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
-        P(i, j, k, pa); P(i + 1, j, k, pb); P(i + 1, j, k + 1, pc); P(i, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
-        P(i, j + 1, k, pa); P(i + 1, j + 1, k, pb); P(i + 1, j + 1, k + 1, pc); P(i, j + 1, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
-        P(i, j, k, pa); P(i, j + 1, k, pb); P(i, j + 1, k + 1, pc); P(i, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
-        P(i + 1, j, k, pa); P(i + 1, j + 1, k, pb); P(i + 1, j + 1, k + 1, pc); P(i + 1, j, k + 1, pd); s += pyramid(pa, pb, pc, pd, cen);
-        B.G(0, i, j, k) = s / 6.0;
-      }
-  for (int k = 2; k <= km; ++k)
-    for (int i = 2; i <= im; ++i) {
-      B.G(0, i, 1, k) = B.G(0, i, 2, k);
-      B.G(0, i, jm + 1, k) = B.G(0, i, jm, k);
-      for (int v = 1; v <= 3; ++v) {
-        B.G(v, i, 1, k) = 2.0 * B.G(v, i, 2, k) - B.G(v, i, 3, k);
-        B.G(v, i, jm + 1, k) = 2.0 * B.G(v, i, jm, k) - B.G(v, i, jm - 1, k);
-      }
-    }
-  for (int k = 2; k <= km; ++k)
-    for (int j = 1; j <= jm + 1; ++j) {
-      B.G(0, 1, j, k) = B.G(0, 2, j, k);
-      B.G(0, im + 1, j, k) = B.G(0, im, j, k);
-      for (int v = 1; v <= 3; ++v) {
-        B.G(v, 1, j, k) = 2.0 * B.G(v, 2, j, k) - B.G(v, 3, j, k);
-        B.G(v, im + 1, j, k) = 2.0 * B.G(v, im, j, k) - B.G(v, im - 1, j, k);
-      }
-    }
-  for (int j = 1; j <= jm + 1; ++j)
-    for (int i = 1; i <= im + 1; ++i) {
-      B.G(0, i, j, 1) = B.G(0, i, j, 2);
-      B.G(0, i, j, km + 1) = B.G(0, i, j, km);
-      for (int v = 1; v <= 3; ++v) {
-        // the reference extrapolates the k=1 centroids from the fixed cell (3, j, 3)
-        B.G(v, i, j, 1) = 2.0 * B.G(v, i, j, 2) - B.G(v, 3, j, 3);
-        B.G(v, i, j, km + 1) = 2.0 * B.G(v, i, j, km) - B.G(v, i, j, km - 1);
-      }
-    }
+// any interior volume that is not positive
+__global__ void k_geo_check(BlockGeom G, const double* __restrict__ gm, long long nc, int* bad) {
+  const int ni = G.imax - 1, nj = G.jmax - 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)ni * nj * (G.kmax - 1)) return;
+  const int i = (int)(t % ni) + 2;
+  const long long r = t / ni;
+  const int j = (int)(r % nj) + 2, k = (int)(r / nj) + 2;
+  if (!(gm[GM_GRD * nc + gidx(G, i, j, k)] > 0.0)) atomicExch(bad, 1);
 }
 
-inline void cmap(const Con& g, int i, int j, int k, int& ii, int& jj, int& kk) {
+__host__ __device__ inline void cmap(const Con& g, int i, int j, int k, int& ii, int& jj, int& kk) {
   ii = g.tm[0][0] * (i - g.s[0]) + g.tm[0][1] * (j - g.s[1]) + g.tm[0][2] * (k - g.s[2]) + g.sd[0];
   jj = g.tm[1][0] * (i - g.s[0]) + g.tm[1][1] * (j - g.s[1]) + g.tm[1][2] * (k - g.s[2]) + g.sd[1];
   kk = g.tm[2][0] * (i - g.s[0]) + g.tm[2][1] * (j - g.s[1]) + g.tm[2][2] * (k - g.s[2]) + g.sd[2];
@@ -207,24 +205,74 @@ bool read_cons(const cfd3d_block_desc& d, int nblocks, std::vector<Con>& out, st
   return true;
 }
 
+// Face-vector halo of one 1-to-1 connection (src/grid_module.f90:725-918), on the node-based
+// ranges: the two face arrays tangential to the interface, from the block's own faces to
+// the donor's ghost row, with the orientation signs s1, s2.
+__global__ void k_geo_face_halo(Con g, BlockGeom S, BlockGeom D, int s1, int s2, double* __restrict__ gm, long long nc) {
+  const int n0 = g.e[0] - g.s[0] + 1, n1 = g.e[1] - g.s[1] + 1, n2 = g.e[2] - g.s[2] + 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)n0 * n1 * n2) return;
+  const int i = g.s[0] + (int)(t % n0);
+  const long long r = t / n0;
+  const int j = g.s[1] + (int)(r % n1), k = g.s[2] + (int)(r / n1);
+  int ii, jj, kk;
+  cmap(g, i, j, k, ii, jj, kk);
+  if (!in_box(S, i, j, k) || !in_box(D, ii, jj, kk)) return;
+  const long long gs = gidx(S, i, j, k), gd = gidx(D, ii, jj, kk);
+  const int pa = (g.s[0] == g.e[0]) ? GM_EX : (g.s[1] == g.e[1]) ? GM_TX : GM_CX;
+  const int pc = (g.s[0] == g.e[0]) ? GM_TX : (g.s[1] == g.e[1]) ? GM_CX : GM_EX;
+  const int qa = (g.sd[0] == g.ed[0]) ? GM_EX : (g.sd[1] == g.ed[1]) ? GM_TX : GM_CX;
+  const int qc = (g.sd[0] == g.ed[0]) ? GM_TX : (g.sd[1] == g.ed[1]) ? GM_CX : GM_EX;
+  for (int m = 0; m < 3; ++m) {
+    const double a = gm[(pa + m) * nc + gs], c = gm[(pc + m) * nc + gs];
+    gm[(qa + m) * nc + gd] = s1 * a;
+    gm[(qc + m) * nc + gd] = s2 * c;
+  }
+}
+
+// Halo of one cell-geometry variable across one connection (cell ranges): the donor's
+// ghost cell takes the block's interior value (src/grid_module.f90:1115-1212, 592-607).
+__global__ void k_geo_exchange(Con g, BlockGeom S, BlockGeom D, int var, double* __restrict__ gm, long long nc) {
+  const int n0 = g.e[0] - g.s[0] + 1, n1 = g.e[1] - g.s[1] + 1, n2 = g.e[2] - g.s[2] + 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)n0 * n1 * n2) return;
+  const int i = g.s[0] + (int)(t % n0);
+  const long long r = t / n0;
+  const int j = g.s[1] + (int)(r % n1), k = g.s[2] + (int)(r / n1);
+  int ii, jj, kk;
+  cmap(g, i, j, k, ii, jj, kk);
+  if (!in_box(S, i, j, k) || !in_box(D, ii, jj, kk)) return;
+  gm[(GM_GRD + var) * nc + gidx(D, ii, jj, kk)] = gm[(GM_GRD + var) * nc + gidx(S, i, j, k)];
+}
+
 // ---- wall distance ------------------------------------------------------------------
-__global__ void k_wall_distance(const double* __restrict__ cen, long long ncen, const double* __restrict__ wall,
-                                int nwall, double* __restrict__ out) {
+// calydns (src/grid_module.f90:350-607): each interior cell's distance to the nearest
+// wall-face centre, by brute force over all of them.  An FP32 pass finds the nearest
+// squared distance; an FP64 pass re-evaluates only the faces within a relative margin of it,
+// so the result is the FP64 minimum.  The cell centre is the centroid in gm.
+__global__ void k_wall_distance(const BlockGeom* __restrict__ blk, int nblk, long long nint, double* __restrict__ gm,
+                                long long nc, const double* __restrict__ wall, int nwall) {
   extern __shared__ float sw[];
-  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   double cx = 0, cy = 0, cz = 0;
-  if (c < ncen) { cx = cen[3 * c]; cy = cen[3 * c + 1]; cz = cen[3 * c + 2]; }
+  long long g = -1;
+  if (t < nint) {
+    const int b = find_block_interior(blk, nblk, t);
+    int i, j, k;
+    g = interior_cell(blk[b], t - blk[b].int_off, i, j, k);
+    cx = gm[(GM_GRD + 1) * nc + g]; cy = gm[(GM_GRD + 2) * nc + g]; cz = gm[(GM_GRD + 3) * nc + g];
+  }
   float fx = (float)cx, fy = (float)cy, fz = (float)cz;
   float best = 3.0e38f;
   // pass 1: FP32 minimum of the squared distance
   for (int t0 = 0; t0 < nwall; t0 += blockDim.x) {
     __syncthreads();
-    int t = t0 + threadIdx.x;
-    if (t < nwall) { sw[3 * threadIdx.x] = (float)wall[3 * t]; sw[3 * threadIdx.x + 1] = (float)wall[3 * t + 1]; sw[3 * threadIdx.x + 2] = (float)wall[3 * t + 2]; }
+    int q = t0 + threadIdx.x;
+    if (q < nwall) { sw[3 * threadIdx.x] = (float)wall[3 * q]; sw[3 * threadIdx.x + 1] = (float)wall[3 * q + 1]; sw[3 * threadIdx.x + 2] = (float)wall[3 * q + 2]; }
     __syncthreads();
     int nt = min((int)blockDim.x, nwall - t0);
-    for (int q = 0; q < nt; ++q) {
-      float dx = fx - sw[3 * q], dy = fy - sw[3 * q + 1], dz = fz - sw[3 * q + 2];
+    for (int q2 = 0; q2 < nt; ++q2) {
+      float dx = fx - sw[3 * q2], dy = fy - sw[3 * q2 + 1], dz = fz - sw[3 * q2 + 2];
       best = fminf(best, dx * dx + dy * dy + dz * dz);
     }
   }
@@ -233,62 +281,96 @@ __global__ void k_wall_distance(const double* __restrict__ cen, long long ncen, 
   double ymin = 1.0e6;
   for (int t0 = 0; t0 < nwall; t0 += blockDim.x) {
     __syncthreads();
-    int t = t0 + threadIdx.x;
-    if (t < nwall) { sw[3 * threadIdx.x] = (float)wall[3 * t]; sw[3 * threadIdx.x + 1] = (float)wall[3 * t + 1]; sw[3 * threadIdx.x + 2] = (float)wall[3 * t + 2]; }
+    int q = t0 + threadIdx.x;
+    if (q < nwall) { sw[3 * threadIdx.x] = (float)wall[3 * q]; sw[3 * threadIdx.x + 1] = (float)wall[3 * q + 1]; sw[3 * threadIdx.x + 2] = (float)wall[3 * q + 2]; }
     __syncthreads();
     int nt = min((int)blockDim.x, nwall - t0);
-    for (int q = 0; q < nt; ++q) {
-      float dx = fx - sw[3 * q], dy = fy - sw[3 * q + 1], dz = fz - sw[3 * q + 2];
+    for (int q2 = 0; q2 < nt; ++q2) {
+      float dx = fx - sw[3 * q2], dy = fy - sw[3 * q2 + 1], dz = fz - sw[3 * q2 + 2];
       if (dx * dx + dy * dy + dz * dz <= thr) {
-        const double* w = wall + 3 * (size_t)(t0 + q);
-        double yt = sqrt((cx - w[0]) * (cx - w[0]) + (cy - w[1]) * (cy - w[1]) + (cz - w[2]) * (cz - w[2]));
+        const double* w = wall + 3 * (size_t)(t0 + q2);
+        const double ex = cx - w[0], ey = cy - w[1], ez = cz - w[2];
+        double yt = sqrt(mulr(ex, ex) + mulr(ey, ey) + mulr(ez, ez));
         if (yt < ymin) ymin = yt;
       }
     }
   }
-  if (c < ncen) out[c] = ymin;
+  if (g >= 0) gm[(GM_GRD + 4) * nc + g] = ymin;
+}
+
+__global__ void k_scale(double* __restrict__ x, long long n, double s) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) x[t] = x[t] * s;
 }
 
 }  // namespace
 
 // ---------------------------------------------------------------------------------------
+// The grid's metrics, computed on the device in the order of grid%construct: face vectors
+// and their halo, the reordering of the connection ranges, volumes and centroids with
+// their ghosts and halo, then the wall distance with its ghosts and halo.  The host holds
+// only the node coordinates (uploaded once) and the wall-face centres.
 bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
   const int ngrd = E.par.ngrd;
-  std::vector<HBlock> H(nblocks);
+  const long long nc = E.ncell;
+  double* gm = E.d.gm;
+  const double scale = E.cfg.scale;
   std::vector<std::vector<Con>> cons(nblocks);
+  std::vector<long long> xoff(nblocks + 1, 0);
+  for (int b = 0; b < nblocks; ++b) {
+    if (!read_cons(blocks[b], nblocks, cons[b], E.err)) return false;
+    xoff[b + 1] = xoff[b] + 3ll * blocks[b].imax * blocks[b].jmax * blocks[b].kmax;
+  }
+  double* dx = nullptr;
+  int* dbad = nullptr;
+  if (cudaMalloc(&dx, (size_t)xoff[nblocks] * 8) != cudaSuccess || cudaMalloc(&dbad, sizeof(int)) != cudaSuccess) {
+    cudaFree(dx);
+    E.err = "device allocation failed (grid nodes)";
+    return false;
+  }
+  auto fail = [&](const char* what) {
+    cudaFree(dx); cudaFree(dbad);
+    E.err = std::string(what) + ": " + cudaGetErrorString(cudaGetLastError());
+    return false;
+  };
+  const int T = 256;
+  auto nblk_of = [T](long long n) { return (unsigned)((n + T - 1) / T); };
+  for (int b = 0; b < nblocks; ++b)
+    if (cudaMemcpy(dx + xoff[b], blocks[b].xyz, (size_t)(xoff[b + 1] - xoff[b]) * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail("grid node upload");
+  k_scale<<<nblk_of(xoff[nblocks]), T>>>(dx, xoff[nblocks], scale);
+  cudaMemset(dbad, 0, sizeof(int));
+  // face vectors (degenerate patches zero their face's plane)
   for (int b = 0; b < nblocks; ++b) {
     const cfd3d_block_desc& d = blocks[b];
-    HBlock& B = H[b];
-    B.im = d.imax; B.jm = d.jmax; B.km = d.kmax; B.ngrd = ngrd;
-    B.x.resize(3 * (size_t)d.imax * d.jmax * d.kmax);
-    for (size_t q = 0; q < B.x.size(); ++q) B.x[q] = d.xyz[q] * E.cfg.scale;
-    face_vectors(B, d);
-    if (!read_cons(d, nblocks, cons[b], E.err)) return false;
+    const BlockGeom& G = E.blk[b];
+    int zl[3] = {0, 0, 0}, zh[3] = {0, 0, 0};
+    const int nmax[3] = {d.imax, d.jmax, d.kmax};
+    for (int n = 0; n < d.nbc; ++n) {
+      if (d.bc[n].type != CFD3D_BC_DEGENERATE) continue;
+      const int* p = d.bc[n].pnts;
+      for (int ax = 0; ax < 3; ++ax) {
+        if (p[ax] != p[3 + ax]) continue;
+        if (p[ax] == 1) zl[ax] = 1;
+        else if (p[ax] == nmax[ax]) zh[ax] = 1;
+        break;
+      }
+    }
+    NodeBlock X{dx + xoff[b], d.imax, d.jmax};
+    const int im = d.imax, jm = d.jmax, km = d.kmax;
+    k_geo_faces<0><<<nblk_of((long long)im * (jm + 1) * (km + 1)), T>>>(G, X, gm, nc, zl[0], zh[0]);
+    k_geo_faces<1><<<nblk_of((long long)(im + 1) * jm * (km + 1)), T>>>(G, X, gm, nc, zl[1], zh[1]);
+    k_geo_faces<2><<<nblk_of((long long)(im + 1) * (jm + 1) * km), T>>>(G, X, gm, nc, zl[2], zh[2]);
   }
-  // face-vector halo on the node-based ranges, with orientation signs
+  // face-vector halo, one connection after the other (a later one overwrites an earlier)
   for (int b = 0; b < nblocks; ++b)
     for (auto& g : cons[b]) {
-      HBlock& S = H[b];
-      HBlock& D = H[g.donor];
       int s1 = 1, s2 = 1;
       if (g.sd[0] == g.ed[0]) { if (g.sd[1] > g.ed[1]) s1 = -1; if (g.sd[2] > g.ed[2]) s2 = -1; }
       else if (g.sd[1] == g.ed[1]) { if (g.sd[2] > g.ed[2]) s1 = -1; if (g.sd[0] > g.ed[0]) s2 = -1; }
       else { if (g.sd[0] > g.ed[0]) s1 = -1; if (g.sd[1] > g.ed[1]) s2 = -1; }
-      for (int k = g.s[2]; k <= g.e[2]; ++k)
-        for (int j = g.s[1]; j <= g.e[1]; ++j)
-          for (int i = g.s[0]; i <= g.e[0]; ++i) {
-            int ii, jj, kk;
-            cmap(g, i, j, k, ii, jj, kk);
-            for (int m = 0; m < 3; ++m) {
-              double a, c;
-              if (g.s[0] == g.e[0]) { a = S.EX(m, i, j, k); c = S.TX(m, i, j, k); }
-              else if (g.s[1] == g.e[1]) { a = S.TX(m, i, j, k); c = S.CX(m, i, j, k); }
-              else { a = S.CX(m, i, j, k); c = S.EX(m, i, j, k); }
-              if (g.sd[0] == g.ed[0]) { D.EX(m, ii, jj, kk) = s1 * a; D.TX(m, ii, jj, kk) = s2 * c; }
-              else if (g.sd[1] == g.ed[1]) { D.TX(m, ii, jj, kk) = s1 * a; D.CX(m, ii, jj, kk) = s2 * c; }
-              else { D.CX(m, ii, jj, kk) = s1 * a; D.EX(m, ii, jj, kk) = s2 * c; }
-            }
-          }
+      const long long n = (long long)(g.e[0] - g.s[0] + 1) * (g.e[1] - g.s[1] + 1) * (g.e[2] - g.s[2] + 1);
+      k_geo_face_halo<<<nblk_of(n), T>>>(g, E.blk[b], E.blk[g.donor], s1, s2, gm, nc);
     }
   // node ranges become cell ranges ("reodering", src/grid_module.f90:926-940)
   for (auto& cl : cons)
@@ -300,35 +382,45 @@ bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
           else g.ed[m] += 1;
         }
       }
-  for (auto& B : H) volumes(B);
-  for (auto& B : H)
-    for (int k = 2; k <= B.km; ++k) for (int j = 2; j <= B.jm; ++j) for (int i = 2; i <= B.im; ++i)
-      if (!(B.G(0, i, j, k) > 0.0)) { E.err = "zero/negative cell volume"; return false; }
   auto exchange = [&](int var) {
     for (int b = 0; b < nblocks; ++b)
-      for (auto& g : cons[b])
-        for (int k = g.s[2]; k <= g.e[2]; ++k)
-          for (int j = g.s[1]; j <= g.e[1]; ++j)
-            for (int i = g.s[0]; i <= g.e[0]; ++i) {
-              int ii, jj, kk;
-              cmap(g, i, j, k, ii, jj, kk);
-              H[g.donor].G(var, ii, jj, kk) = H[b].G(var, i, j, k);
-            }
+      for (auto& g : cons[b]) {
+        const long long n = (long long)(g.e[0] - g.s[0] + 1) * (g.e[1] - g.s[1] + 1) * (g.e[2] - g.s[2] + 1);
+        k_geo_exchange<<<nblk_of(n), T>>>(g, E.blk[b], E.blk[g.donor], var, gm, nc);
+      }
   };
+  // volumes and centroids, their ghosts, the volume check and halo
+  for (int b = 0; b < nblocks; ++b) {
+    const cfd3d_block_desc& d = blocks[b];
+    const BlockGeom& G = E.blk[b];
+    NodeBlock X{dx + xoff[b], d.imax, d.jmax};
+    const long long nin = (long long)(d.imax - 1) * (d.jmax - 1) * (d.kmax - 1);
+    k_geo_cells<<<nblk_of(nin), T>>>(G, X, gm, nc);
+    k_geo_ghosts<<<nblk_of((long long)(d.imax - 1) * (d.kmax - 1)), T>>>(G, gm, nc, 0, 0);
+    k_geo_ghosts<<<nblk_of((long long)(d.jmax + 1) * (d.kmax - 1)), T>>>(G, gm, nc, 1, 0);
+    k_geo_ghosts<<<nblk_of((long long)(d.imax + 1) * (d.jmax + 1)), T>>>(G, gm, nc, 2, 0);
+    k_geo_check<<<nblk_of(nin), T>>>(G, gm, nc, dbad);
+  }
+  int bad = 0;
+  if (cudaMemcpy(&bad, dbad, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return fail("grid metrics");
+  if (bad) { cudaFree(dx); cudaFree(dbad); E.err = "zero/negative cell volume"; return false; }
   exchange(0);
   if (ngrd == 5) {
-    // wall-face centres of every block (BCWall patches), then the GPU brute force
-    std::vector<double> wall, cen;
+    // wall-face centres of every block's wall patches (from the scaled nodes, as the
+    // device has them), then the brute force over all interior cells
+    std::vector<double> wall;
     for (int b = 0; b < nblocks; ++b) {
       const cfd3d_block_desc& d = blocks[b];
-      HBlock& B = H[b];
+      auto XN = [&](int v, int i, int j, int k) {
+        return d.xyz[v + 3 * ((i - 2) + (size_t)d.imax * ((j - 2) + (size_t)d.jmax * (k - 2)))] * scale;
+      };
       for (int n = 0; n < d.nbc; ++n) {
         const int ty = d.bc[n].type;
         if (ty != CFD3D_BC_WALL && ty != CFD3D_BC_WALL_COUNTERROTATING && ty != CFD3D_BC_WALL_HEATFLUX) continue;
         const int* p = d.bc[n].pnts;
         int ax = -1;
         for (int a = 0; a < 3; ++a) if (p[a] == p[3 + a]) ax = a;
-        int nmax[3] = {B.im, B.jm, B.km};
+        int nmax[3] = {d.imax, d.jmax, d.kmax};
         int lo[3], hi[3];
         for (int a = 0; a < 3; ++a) { lo[a] = p[a] + 1; hi[a] = p[3 + a]; }
         int plane = (p[ax] == 1) ? 2 : nmax[ax] + 1;
@@ -343,62 +435,74 @@ bool setup_geometry(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
             q2[t1] = a2; q2[t2] = b2 + 1;
             q3[t1] = a2 + 1; q3[t2] = b2 + 1;
             for (int v = 0; v < 3; ++v)
-              wall.push_back(0.25 * (B.X(v, q0[0], q0[1], q0[2]) + B.X(v, q1[0], q1[1], q1[2]) +
-                                     B.X(v, q2[0], q2[1], q2[2]) + B.X(v, q3[0], q3[1], q3[2])));
+              wall.push_back(0.25 * (XN(v, q0[0], q0[1], q0[2]) + XN(v, q1[0], q1[1], q1[2]) +
+                                     XN(v, q2[0], q2[1], q2[2]) + XN(v, q3[0], q3[1], q3[2])));
           }
       }
-      for (int k = 2; k <= B.km; ++k) for (int j = 2; j <= B.jm; ++j) for (int i = 2; i <= B.im; ++i)
-        for (int v = 0; v < 3; ++v)
-          cen.push_back(0.125 * (B.X(v, i, j, k) + B.X(v, i + 1, j, k) + B.X(v, i, j + 1, k) + B.X(v, i, j, k + 1) +
-                                 B.X(v, i + 1, j + 1, k) + B.X(v, i, j + 1, k + 1) + B.X(v, i + 1, j, k + 1) +
-                                 B.X(v, i + 1, j + 1, k + 1)));
     }
-    long long ncen = (long long)cen.size() / 3;
-    std::vector<double> yd(ncen, 1.0e6);
-    int nwall = (int)(wall.size() / 3);
+    const int nwall = (int)(wall.size() / 3);
+    double* dwall = nullptr;
     if (nwall > 0) {
-      double *dcen = nullptr, *dwall = nullptr, *dy = nullptr;
-      if (cudaMalloc(&dcen, cen.size() * 8) != cudaSuccess || cudaMalloc(&dwall, wall.size() * 8) != cudaSuccess ||
-          cudaMalloc(&dy, ncen * 8) != cudaSuccess) {
-        E.err = "cudaMalloc failed in wall distance"; cudaFree(dcen); cudaFree(dwall); return false;
-      }
-      cudaMemcpy(dcen, cen.data(), cen.size() * 8, cudaMemcpyHostToDevice);
+      if (cudaMalloc(&dwall, wall.size() * 8) != cudaSuccess) return fail("device allocation failed (wall faces)");
       cudaMemcpy(dwall, wall.data(), wall.size() * 8, cudaMemcpyHostToDevice);
-      const int T = 256;
-      k_wall_distance<<<(unsigned)((ncen + T - 1) / T), T, 3 * T * sizeof(float)>>>(dcen, ncen, dwall, nwall, dy);
-      cudaError_t e = cudaMemcpy(yd.data(), dy, ncen * 8, cudaMemcpyDeviceToHost);
-      cudaFree(dcen); cudaFree(dwall); cudaFree(dy);
-      if (e != cudaSuccess) { E.err = std::string("wall distance: ") + cudaGetErrorString(e); return false; }
     }
-    long long q = 0;
-    for (auto& B : H) {
-      for (int k = 2; k <= B.km; ++k) for (int j = 2; j <= B.jm; ++j) for (int i = 2; i <= B.im; ++i) B.G(4, i, j, k) = yd[q++];
-      for (int k = 2; k <= B.km; ++k) for (int i = 2; i <= B.im; ++i) { B.G(4, i, 1, k) = B.G(4, i, 2, k); B.G(4, i, B.jm + 1, k) = B.G(4, i, B.jm, k); }
-      for (int k = 2; k <= B.km; ++k) for (int j = 1; j <= B.jm + 1; ++j) { B.G(4, 1, j, k) = B.G(4, 2, j, k); B.G(4, B.im + 1, j, k) = B.G(4, B.im, j, k); }
-      for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im + 1; ++i) { B.G(4, i, j, 1) = B.G(4, i, j, 2); B.G(4, i, j, B.km + 1) = B.G(4, i, j, B.km); }
+    k_wall_distance<<<nblk_of(E.nint), T, 3 * T * sizeof(float)>>>(E.d.blk, nblocks, E.nint, gm, nc, dwall, nwall);
+    for (int b = 0; b < nblocks; ++b) {
+      const cfd3d_block_desc& d = blocks[b];
+      const BlockGeom& G = E.blk[b];
+      k_geo_ghosts<<<nblk_of((long long)(d.imax - 1) * (d.kmax - 1)), T>>>(G, gm, nc, 0, 1);
+      k_geo_ghosts<<<nblk_of((long long)(d.jmax + 1) * (d.kmax - 1)), T>>>(G, gm, nc, 1, 1);
+      k_geo_ghosts<<<nblk_of((long long)(d.imax + 1) * (d.jmax + 1)), T>>>(G, gm, nc, 2, 1);
     }
     exchange(4);
+    const cudaError_t e = cudaDeviceSynchronize();
+    cudaFree(dwall);
+    if (e != cudaSuccess) return fail("wall distance");
   }
-  // scatter into the SoA metric planes
-  const long long nc = E.ncell;
-  const int ngm = GM_GRD + ngrd;
-  std::vector<double> gm((size_t)ngm * nc, 0.0);
+  const cudaError_t e = cudaDeviceSynchronize();
+  cudaFree(dx); cudaFree(dbad);
+  if (e != cudaSuccess) { E.err = std::string("grid metrics: ") + cudaGetErrorString(e); return false; }
+  return true;
+}
+
+// The halo of the volume-fraction gradient (setbc_vfg, src/bc_module.f90:1398-1804): for
+// each 1-to-1 interface, the block's first interior layer into the donor's first ghost
+// layer, as (source, target) padded-cell pairs.
+bool setup_vfg_halo(Engine& E, const cfd3d_block_desc* blocks, int nblocks) {
+  std::vector<int> pairs;
   for (int b = 0; b < nblocks; ++b) {
-    HBlock& B = H[b];
-    const BlockGeom& G = E.blk[b];
-    auto gi = [&](int i, int j, int k) { return G.off + (i + 1) + (long long)G.ni * ((j + 1) + (long long)G.nj * (k + 1)); };
-    for (int k = 1; k <= B.km + 1; ++k) for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im; ++i)
-      for (int v = 0; v < 3; ++v) gm[(size_t)(GM_CX + v) * nc + gi(i, j, k)] = B.CX(v, i, j, k);
-    for (int k = 1; k <= B.km + 1; ++k) for (int j = 1; j <= B.jm; ++j) for (int i = 1; i <= B.im + 1; ++i)
-      for (int v = 0; v < 3; ++v) gm[(size_t)(GM_EX + v) * nc + gi(i, j, k)] = B.EX(v, i, j, k);
-    for (int k = 1; k <= B.km; ++k) for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im + 1; ++i)
-      for (int v = 0; v < 3; ++v) gm[(size_t)(GM_TX + v) * nc + gi(i, j, k)] = B.TX(v, i, j, k);
-    for (int k = 1; k <= B.km + 1; ++k) for (int j = 1; j <= B.jm + 1; ++j) for (int i = 1; i <= B.im + 1; ++i)
-      for (int v = 0; v < ngrd; ++v) gm[(size_t)(GM_GRD + v) * nc + gi(i, j, k)] = B.G(v, i, j, k);
+    std::vector<Con> cons;
+    if (!read_cons(blocks[b], nblocks, cons, E.err)) return false;
+    const BlockGeom& S = E.blk[b];
+    for (auto g : cons) {
+      for (int m = 0; m < 3; ++m) {
+        if (g.s[m] != g.e[m]) g.s[m] += 1;
+        if (g.sd[m] != g.ed[m]) { if (g.sd[m] < g.ed[m]) g.sd[m] += 1; else g.ed[m] += 1; }
+      }
+      const BlockGeom& D = E.blk[g.donor];
+      for (int k = g.s[2]; k <= g.e[2]; ++k)
+        for (int j = g.s[1]; j <= g.e[1]; ++j)
+          for (int i = g.s[0]; i <= g.e[0]; ++i) {
+            int ii, jj, kk;
+            cmap(g, i, j, k, ii, jj, kk);
+            if (ii < 1 || ii > D.imax + 1 || jj < 1 || jj > D.jmax + 1 || kk < 1 || kk > D.kmax + 1) {
+              E.err = "volume-fraction halo target outside the donor block"; return false;
+            }
+            pairs.push_back((int)(S.off + (i + 1) + (long long)S.ni * ((j + 1) + (long long)S.nj * (k + 1))));
+            pairs.push_back((int)(D.off + (ii + 1) + (long long)D.ni * ((jj + 1) + (long long)D.nj * (kk + 1))));
+          }
+    }
   }
-  if (cudaMemcpy(E.d.gm, gm.data(), gm.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
-    E.err = "metric upload failed"; return false;
+  E.d.nvfg_halo = (int)(pairs.size() / 2);
+  if (pairs.empty()) return true;
+  int* dp = nullptr;
+  if (cudaMalloc(&dp, pairs.size() * sizeof(int)) != cudaSuccess ||
+      cudaMemcpy(dp, pairs.data(), pairs.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(dp);
+    E.err = "device allocation failed (volume-fraction halo)";
+    return false;
   }
+  E.d.vfg_halo = dp;
   return true;
 }
 

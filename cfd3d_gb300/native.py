@@ -46,6 +46,7 @@ def lib():
     L.cfd3d_initialize.argtypes = [H, C.c_int, dp]
     L.cfd3d_upload_state.argtypes = [H, C.c_int, dp, dp, dp, dp]
     L.cfd3d_download_state.argtypes = [H, C.c_int, dp, dp, dp, dp, dp]
+    L.cfd3d_download_csf.argtypes = [H, C.c_int, dp]
     L.cfd3d_upload_primitives.argtypes = [H, C.c_int, dp, dp]
     pp = C.POINTER(dp)
     L.cfd3d_upload_primitives_all.argtypes = [H, pp, pp]
@@ -72,7 +73,7 @@ def lib():
 
 
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
-           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_upload_primitives", "cfd3d_upload_primitives_all", "cfd3d_download_state_all", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
+           "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_upload_primitives", "cfd3d_upload_primitives_all", "cfd3d_download_state_all", "cfd3d_download_csf", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
            "cfd3d_iterate", "cfd3d_iterate_n",
            "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device", "cfd3d_fp64_peak"]
@@ -194,6 +195,12 @@ class Engine:
         """cfd3d_download_state_all into caller-owned per-block arrays (None skips)"""
         self._check(lib().cfd3d_download_state_all(self.h, self._ptrs(pv, True), self._ptrs(dv, True),
                                                    self._ptrs(tv, True) if self.ntv else None))
+
+    def download_csf(self, n):
+        """The surface-tension source csf(3, interior) of block n from the last residual."""
+        out = np.zeros(abi.interior_shape(self.case["blocks"][n], 3))
+        self._check(lib().cfd3d_download_csf(self.h, n, _p(out)))
+        return out
 
     def download(self, n, out=None):
         b = self.case["blocks"][n]

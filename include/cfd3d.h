@@ -88,6 +88,12 @@ typedef struct cfd3d_config {
      ngravity rows (t, gx, gy, gz) with t ascending */
   int    gravity, ngravity;
   const double *gravity_data;
+  /* the surface-tension source rhs%csf (src/csf_module.f90:97-175): 0 none, 1 on */
+  int    csf;
+  /* the rotating frame (src/rotation_module.f90, src/config_module.f90:126-141): rotation
+     0 none, +-1, +-2, +-3 about +-x, +-y, +-z at rpm revolutions per minute */
+  int    rotation;
+  double rpm;
 } cfd3d_config;
 
 /* A boundary patch: CGNS PointRange in 1-based NODE indices
@@ -172,6 +178,12 @@ int  cfd3d_upload_primitives(cfd3d_handle *h, int block, const double *pv, const
  * No counterpart in the reference (its state never leaves the host). */
 int  cfd3d_upload_primitives_all(cfd3d_handle *h, const double *const *pv, const double *const *qq);
 int  cfd3d_download_state_all(cfd3d_handle *h, double *const *pv, double *const *dv, double *const *tv);
+
+/* With the surface-tension source (csf = 1): csf(3, 2:imax, 2:jmax, 2:kmax) of one block, the
+ * momentum source of the last residual (its volume included), as calrhs stores it in
+ * variable%csf (src/rhs_module.f90:632-634) for export_variable.  CFD3D_ERR_ARG without csf.
+ * Replaces t_variable%getcsf-style access to variable%csf (src/variable_module.f90:21). */
+int  cfd3d_download_csf(cfd3d_handle *h, int block, double *csf);
 
 /* Checkpoint file out_########.dat in the layout of variable%export_variable
  * (src/variable_module.f90:116-182), native byte order: one record per block, in block

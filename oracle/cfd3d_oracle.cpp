@@ -86,6 +86,7 @@ struct Block {
   A4 pv, dv, tv, qq, rcav;
   A4 res, icav, itt, omega_cut, dt;
   A4 dqs, dcv, qres;
+  A4 vfg, csf;                  /* csf = 1: volume-fraction gradient, surface-tension source */
   std::vector<BcInfo> bcs;
   BcInfo edge[12], corner[8];
   std::vector<Conn> cons;       /* state halo (3 layers) */
@@ -128,6 +129,8 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
     c.grav_a = {0.0, 0.0, 0.0};
     c.grav_a[std::abs(c.gravity) - 1] = (c.gravity > 0 ? 1.0 : -1.0) * 9.80665;
   } else if (c.gravity != 0) { err = "gravity must be 0, +-1, +-2, +-3 or 4"; return false; }
+  c.csf = in->csf;
+  if (c.csf != 0 && c.csf != 1) { err = "csf must be 0 or 1"; return false; }
   if (c.timemethod < 1 || c.timemethod > 3) { err = "timemethod must be 1 (Euler), 2 (RK3) or 3 (LU-SGS)"; return false; }
   if (c.iturb == -3) { c.npv = 7; c.ntv = 0; }
   else if (c.iturb == -2) { c.npv = 7; c.ntv = 2; }
@@ -314,7 +317,7 @@ static void volumes(const Cfg& c, Block& B) {
     }
 }
 
-/* wall distance: brute force over all wall-face centres of all blocks (src/grid_module.f90:350-607) */
+/* wall distance: the nearest wall-face centre over all blocks (src/grid_module.f90:350-607) */
 static void wall_distance(Oracle& O) {
   if (O.c.ngrd < 5) return;
   std::vector<double> wx, wy, wz;
@@ -976,6 +979,8 @@ static void tp_patch_sums(const Block& B, const BcInfo& bi, double* pa) {
    n-th total-pressure patch of every block; its averages feed one newt, whose solution all
    of the pool's patches take. */
 static void tp_solve_pools(Oracle& O);
+static void calvfg_block(Block& B);
+static void exchange_vfg(Oracle& O);
 
 static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
   double pv[NPV_MAX], dv[NDV], tv[3], pvs[NPV_MAX], dvs[NDV], tvs[3], ppv[NPV_MAX], nx[3];
@@ -1266,6 +1271,12 @@ static void setbc(Oracle& O) {
   apply_halos(O);
   for (auto& B : O.b) for (int m = 0; m < 12; ++m) apply_bc(O.c, B, B.edge[m]);
   for (auto& B : O.b) for (int m = 0; m < 8; ++m) apply_bc(O.c, B, B.corner[m]);
+  /* with the surface-tension source every setbc is followed by calvfg and setbc_vfg
+     (src/update_module.f90:240-243, 359-362, 479-482) */
+  if (O.c.csf) {
+    for (auto& B : O.b) calvfg_block(B);
+    exchange_vfg(O);
+  }
 }
 
 /* ---------------- local time step (src/timestep_module.f90:127-316) ---------------- */
@@ -1313,6 +1324,88 @@ static double timestep_block(const Cfg& c, Block& B) {
 static void gather_pv(const Cfg& c, Block& B, int i, int j, int k, double* out) {
   const double* P = B.pv.at(i, j, k);
   for (int m = 0; m < c.npv; ++m) out[m] = P[m];
+}
+
+/* ---------------- surface tension (csf = 1) ---------------- */
+/* calvfg (src/variable_module.f90:304-351): vf = rho (y1 / rho_v + y2 / rho_g), the volume
+   fraction of vapour and gas, over 0..imax+2, and its Green-Gauss gradient calgrad_gg
+   (:353-377) over the cells 1..imax+1, the interior and the first ghost layer.  For the
+   ghost layer the reference reads face vectors past the ends of its arrays (cx(0),
+   cx(imax+1), ex(.,0,.), ex(.,jmax+1,.), tx(.,.,0), tx(.,.,kmax+1)), which hold no defined
+   values; here such a face takes the vector of the nearest face of its row. */
+static void calvfg_block(Block& B) {
+  const int im = B.imax, jm = B.jmax, km = B.kmax;
+  A4 vf;
+  vf.init(1, 0, im + 2, 0, jm + 2, 0, km + 2);
+  for (int k = 0; k <= km + 2; ++k)
+    for (int j = 0; j <= jm + 2; ++j)
+      for (int i = 0; i <= im + 2; ++i)
+        vf(0, i, j, k) = B.dv(0, i, j, k) * (B.pv(5, i, j, k) / B.dv(3, i, j, k) + B.pv(6, i, j, k) / B.dv(4, i, j, k));
+  auto clampi = [](int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); };
+  for (int k = 1; k <= km + 1; ++k)
+    for (int j = 1; j <= jm + 1; ++j)
+      for (int i = 1; i <= im + 1; ++i) {
+        const double x[7] = {vf(0, i - 1, j, k), vf(0, i + 1, j, k), vf(0, i, j - 1, k), vf(0, i, j + 1, k),
+                             vf(0, i, j, k - 1), vf(0, i, j, k + 1), vf(0, i, j, k)};
+        const double* n6[6] = {B.cx.at(clampi(i - 1, 1, im), j, k), B.cx.at(clampi(i, 1, im), j, k),
+                               B.ex.at(i, clampi(j - 1, 1, jm), k), B.ex.at(i, clampi(j, 1, jm), k),
+                               B.tx.at(i, j, clampi(k - 1, 1, km)), B.tx.at(i, j, clampi(k, 1, km))};
+        const double sg[6] = {-1.0, 1.0, -1.0, 1.0, -1.0, 1.0};
+        double g[3] = {0.0, 0.0, 0.0};
+        for (int l = 0; l < 6; ++l) {
+          const double xm = 0.5 * (x[6] + x[l]);
+          for (int e = 0; e < 3; ++e) g[e] = g[e] + xm * (sg[l] * n6[l][e]);
+        }
+        for (int e = 0; e < 3; ++e) B.vfg(e, i, j, k) = g[e] / B.grd(0, i, j, k);
+      }
+}
+
+/* setbc_vfg (src/bc_module.f90:1398-1804): across each 1-to-1 interface the donor's first
+   ghost layer takes the block's first interior layer of vfg */
+static void exchange_vfg(Oracle& O) {
+  for (size_t bi = 0; bi < O.b.size(); ++bi) {
+    Block& S = O.b[bi];
+    for (auto& g : S.gcons) {
+      Block& D = O.b[g.donor];
+      for (int k = g.istart[2]; k <= g.iend[2]; ++k)
+        for (int j = g.istart[1]; j <= g.iend[1]; ++j)
+          for (int i = g.istart[0]; i <= g.iend[0]; ++i) {
+            int ii, jj, kk;
+            conn_map(g, i, j, k, ii, jj, kk);
+            for (int e = 0; e < 3; ++e) D.vfg(e, ii, jj, kk) = S.vfg(e, i, j, k);
+          }
+    }
+  }
+}
+
+/* csfsource (src/csf_module.f90:97-175) for cell (i, j, k), as calrhs calls it
+   (src/rhs_module.f90:607-635): the cell (7) and its six neighbours' vfg, the outward face
+   vectors -cx(i-1), cx(i), -ex(j-1), ex(j), -tx(k-1), tx(k).  Below |vfg| = 0.04 there is no
+   interface and the source is zero.  The surface tension is the reference's constant
+   0.071684196047 N/m in every cell, so its tangential (Marangoni) part, which is made of
+   its differences, is zero. */
+static void csf_source(Block& B, int i, int j, int k, const double* grd, const double* pv7, double* out) {
+  for (int n = 0; n < 5; ++n) out[n] = 0.0;
+  const double* v[7] = {B.vfg.at(i - 1, j, k), B.vfg.at(i + 1, j, k), B.vfg.at(i, j - 1, k), B.vfg.at(i, j + 1, k),
+                        B.vfg.at(i, j, k - 1), B.vfg.at(i, j, k + 1), B.vfg.at(i, j, k)};
+  const double delta = std::sqrt(v[6][0] * v[6][0] + v[6][1] * v[6][1] + v[6][2] * v[6][2]);
+  if (delta <= 0.04) return;
+  const double sigma = 0.071684196047;
+  double nv[7][3];
+  for (int l = 0; l < 7; ++l) {
+    const double dl = v[l][0] * v[l][0] + v[l][1] * v[l][1] + v[l][2] * v[l][2];
+    for (int e = 0; e < 3; ++e) nv[l][e] = (dl > 0.0) ? v[l][e] / std::sqrt(dl) : 0.0;
+  }
+  const double* n6[6] = {B.cx.at(i - 1, j, k), B.cx.at(i, j, k), B.ex.at(i, j - 1, k),
+                         B.ex.at(i, j, k), B.tx.at(i, j, k - 1), B.tx.at(i, j, k)};
+  const double sg[6] = {-1.0, 1.0, -1.0, 1.0, -1.0, 1.0};
+  double kappa = 0.0;
+  for (int m = 0; m < 6; ++m)
+    for (int e = 0; e < 3; ++e) kappa = kappa + 0.5 * (nv[6][e] + nv[m][e]) * (sg[m] * n6[m][e]);
+  kappa = -kappa / grd[0];
+  for (int e = 0; e < 3; ++e) out[1 + e] = sigma * kappa * v[6][e];
+  out[4] = out[1] * pv7[1] + out[2] * pv7[2] + out[3] * pv7[3];
+  for (int n = 0; n < 5; ++n) out[n] = out[n] * grd[0];
 }
 
 static void calrhs_block(const Cfg& c, Block& B, double time) {
@@ -1468,6 +1561,12 @@ static void calrhs_block(const Cfg& c, Block& B, double time) {
           for (int e = 0; e < 3; ++e) B.res(1 + e, i, j, k) = B.res(1 + e, i, j, k) + dv[0] * grd[0] * a[e];
           B.res(4, i, j, k) = B.res(4, i, j, k) +
                               dv[0] * grd[0] * (a[0] * x7[1][1] + a[1] * x7[1][2] + a[2] * x7[1][3]);
+        }
+        if (c.csf) {
+          double cs[5];
+          csf_source(B, i, j, k, grd, B.pv.at(i, j, k), cs);
+          for (int n = 0; n < 5; ++n) B.res(n, i, j, k) = B.res(n, i, j, k) + cs[n];
+          for (int e = 0; e < 3; ++e) B.csf(e, i, j, k) = cs[1 + e];
         }
       }
 }
@@ -1642,6 +1741,10 @@ static void alloc_block(const Cfg& c, Block& B) {
   B.dqs.init(c.npv, 1, im + 1, 1, jm + 1, 1, km + 1);
   B.dcv.init(c.npv, 1, im + 1, 1, jm + 1, 1, km + 1);
   B.qres.init(c.npv, 2, im, 2, jm, 2, km);
+  if (c.csf) {
+    B.vfg.init(3, 1, im + 1, 1, jm + 1, 1, km + 1);
+    B.csf.init(3, 2, im, 2, jm, 2, km);
+  }
 }
 
 }  // namespace
@@ -1759,6 +1862,16 @@ int orc_get_state(void* h, int b, double* pv, double* dv, double* tv, double* qq
   if (tv && O->c.ntv) std::memcpy(tv, B.tv.d.data(), B.tv.d.size() * 8);
   if (qq && O->c.nqq) std::memcpy(qq, B.qq.d.data(), B.qq.d.size() * 8);
   if (rcav) std::memcpy(rcav, B.rcav.d.data(), B.rcav.d.size() * 8);
+  return 0;
+}
+
+/* csf = 1: vfg(3, 1:imax+1, 1:jmax+1, 1:kmax+1) and csf(3, 2:imax, 2:jmax, 2:kmax) of block b */
+int orc_get_csf(void* h, int b, double* vfg, double* csf) {
+  Oracle* O = (Oracle*)h;
+  if (!O->c.csf) return 1;
+  Block& B = O->b[b];
+  if (vfg) std::memcpy(vfg, B.vfg.d.data(), B.vfg.d.size() * 8);
+  if (csf) std::memcpy(csf, B.csf.d.data(), B.csf.d.size() * 8);
   return 0;
 }
 

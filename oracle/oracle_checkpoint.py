@@ -14,7 +14,7 @@ realsize = 8 from mpi_type_size).  A record is, in native byte order:
     emut(-1:imax+3, ..) = tv(3, ..)          if iturb >= -1        :144-158
     qq(npv, nqq, 2:imax, 2:jmax, 2:kmax)                          :160-163
     rcav(2, 2:imax, ..)                      if ncav != 0          :165-170
-    csf(3, 2:imax, ..)                       if csf != 0 (not carried by the engine)
+    csf(3, 2:imax, ..)                       if csf != 0           :172-177
 
 Arrays here use the engine's host shapes: a padded array is (kmax+5, jmax+5, imax+5, nv)
 in C order, an interior one (kmax-1, jmax-1, imax-1, nv): the same bytes as the Fortran
@@ -32,7 +32,12 @@ def flags(cfg):
     return cfg.get("iturb", -3) >= -1, cfg.get("ncav", 0) != 0
 
 
-def record_size(npv, nqq, imax, jmax, kmax, turb, cav, with_qq=True):
+def csf_flag(cfg):
+    """l_csf of t_variable%construct (src/variable_module.f90:67)."""
+    return cfg.get("csf", 0) != 0
+
+
+def record_size(npv, nqq, imax, jmax, kmax, turb, cav, with_qq=True, csf=False):
     """Bytes of one block's record: the summand of the displacement loop
     (src/variable_module.f90:84-89; without the qq term for steadyini, initial_module :130-136)."""
     npad = (imax + 5) * (jmax + 5) * (kmax + 5)
@@ -44,6 +49,8 @@ def record_size(npv, nqq, imax, jmax, kmax, turb, cav, with_qq=True):
         s += REALSIZE * npad
     if cav:
         s += REALSIZE * 2 * nint
+    if csf:
+        s += REALSIZE * 3 * nint
     return s
 
 
@@ -53,11 +60,11 @@ def displacements(cfg, blocks, npv, nqq, with_qq=True):
     out, d = [], 0
     for b in blocks:
         out.append(d)
-        d += record_size(npv, nqq, b["imax"], b["jmax"], b["kmax"], turb, cav, with_qq)
+        d += record_size(npv, nqq, b["imax"], b["jmax"], b["kmax"], turb, cav, with_qq, csf_flag(cfg))
     return out, d
 
 
-def encode_record(cfg, b, npv, nqq, nt_phy, nt, time, pv, tv=None, qq=None, rcav=None, with_qq=True):
+def encode_record(cfg, b, npv, nqq, nt_phy, nt, time, pv, tv=None, qq=None, rcav=None, with_qq=True, csf=None):
     """The bytes of one record, in export_variable's order."""
     turb, cav = flags(cfg)
     pad = (b["kmax"] + 5, b["jmax"] + 5, b["imax"] + 5)
@@ -78,13 +85,17 @@ def encode_record(cfg, b, npv, nqq, nt_phy, nt, time, pv, tv=None, qq=None, rcav
         rcav = np.asarray(rcav, dtype="<f8")
         assert rcav.shape == inner + (2,)
         parts.append(rcav.tobytes())
+    if csf_flag(cfg):
+        csf = np.asarray(csf, dtype="<f8")
+        assert csf.shape == inner + (3,)
+        parts.append(csf.tobytes())
     return b"".join(parts)
 
 
 def write_checkpoint(path, cfg, blocks, npv, nqq, nt_phy, nt, time, states):
-    """export_variable for every rank: `states[r]` holds pv, tv, qq, rcav of block r."""
+    """export_variable for every rank: `states[r]` holds pv, tv, qq, rcav (and csf) of block r."""
     data = b"".join(encode_record(cfg, b, npv, nqq, nt_phy, nt, time, s["pv"], s.get("tv"), s.get("qq"),
-                                  s.get("rcav")) for b, s in zip(blocks, states))
+                                  s.get("rcav"), csf=s.get("csf")) for b, s in zip(blocks, states))
     with open(path, "wb") as f:
         f.write(data)
     return data
@@ -115,6 +126,7 @@ def read_checkpoint(path, cfg, blocks, npv, nqq, with_qq=True):
         rec["emut"] = take(int(np.prod(pad)), "<f8").reshape(pad) if turb else None
         rec["qq"] = take(int(np.prod(inner)) * nqq * npv, "<f8").reshape(inner + (nqq * npv,)) if (with_qq and nqq) else None
         rec["rcav"] = take(int(np.prod(inner)) * 2, "<f8").reshape(inner + (2,)) if cav else None
+        rec["csf"] = take(int(np.prod(inner)) * 3, "<f8").reshape(inner + (3,)) if csf_flag(cfg) else None
         out.append(rec)
     return out
 

@@ -42,6 +42,7 @@ def lib(fast=False):
         L.orc_initialize.argtypes = [C.c_void_p, C.c_int, dp]
         L.orc_set_state.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
         L.orc_get_state.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp]
+        L.orc_get_csf.argtypes = [C.c_void_p, C.c_int, dp, dp]
         L.orc_metrics.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
         L.orc_residual.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
         L.orc_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, dp, dp, C.POINTER(C.c_int)]
@@ -114,6 +115,16 @@ class Oracle:
         rc = np.zeros(abi.interior_shape(b, 2))
         self._L.orc_get_state(self.h, n, _p(pv), _p(dv), _p(tv), _p(qq), _p(rc))
         return dict(pv=pv, dv=dv, tv=tv[..., :self.ntv], qq=qq, rcav=rc)
+
+    def get_csf(self, n):
+        """csf = 1: the volume-fraction gradient vfg (k, j, i, 3) over the cells 1..imax+1
+        and the surface-tension source csf (interior, 3) of the last residual."""
+        b = self.case["blocks"][n]
+        vfg = np.zeros((b["kmax"] + 1, b["jmax"] + 1, b["imax"] + 1, 3))
+        csf = np.zeros(abi.interior_shape(b, 3))
+        if self._L.orc_get_csf(self.h, n, _p(vfg), _p(csf)) != 0:
+            raise ValueError("the case has no surface-tension source")
+        return dict(vfg=vfg, csf=csf)
 
     def set_state(self, n, pv=None, dv=None, tv=None, qq=None):
         b = self.case["blocks"][n]

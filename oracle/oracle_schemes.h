@@ -30,6 +30,7 @@ struct Cfg {
   int timemethod;  /* 1 explicit Euler, 2 RK3, 3 LU-SGS */
   int gravity;     /* 0 none, +-1..+-3 axis, 4 history */
   std::vector<double> grav_t, grav_a;   /* the history: times, accelerations (3 per row) */
+  int csf;         /* 1: the surface-tension source rhs%csf */
   double tp_pt, tp_tt, tp_ht;   /* total-pressure inlet: its totals and h(p_t, T_t) */
   bool with_prop;  /* t_eos_prop (iturb >= -2) vs t_eosonly (Euler) */
   EosSel eos;

@@ -14,7 +14,7 @@ def _blocks(dims):
     return [dict(imax=i, jmax=j, kmax=k) for i, j, k in dims]
 
 
-def _reference_disp(rank, dims, npv, nqq, turb, cav, with_qq=True):
+def _reference_disp(rank, dims, npv, nqq, turb, cav, with_qq=True, csf=False):
     """The displacement loop of t_variable%construct (src/variable_module.f90:80-91),
     term by term, with intsize = 4 and realsize = 8."""
     intsize, realsize = 4, 8
@@ -28,10 +28,12 @@ def _reference_disp(rank, dims, npv, nqq, turb, cav, with_qq=True):
             disp += realsize * (im + 5) * (jm + 5) * (km + 5)
         if cav:
             disp += realsize * 2 * (im - 1) * (jm - 1) * (km - 1)
+        if csf:
+            disp += realsize * 3 * (im - 1) * (jm - 1) * (km - 1)
     return disp
 
 
-CFGS = [dict(iturb=-3, ncav=0, nsteady=0), dict(iturb=-2, ncav=1, nsteady=0),
+CFGS = [dict(iturb=-3, ncav=0, nsteady=0), dict(iturb=-2, ncav=1, nsteady=0), dict(iturb=-2, ncav=1, nsteady=0, csf=1),
         dict(iturb=0, ncav=1, nsteady=2), dict(iturb=0, ncav=0, nsteady=1)]
 
 
@@ -41,10 +43,11 @@ def test_displacements_follow_the_reference_formula(cfg, with_qq):
     npv = 9 if cfg["iturb"] == 0 else 7
     nqq = 2 if cfg["nsteady"] else 0
     turb, cav = ock.flags(cfg)
+    csf = ock.csf_flag(cfg)
     disp, total = ock.displacements(cfg, _blocks(DIMS), npv, nqq, with_qq)
     for r in range(len(DIMS)):
-        assert disp[r] == _reference_disp(r, DIMS, npv, nqq, turb, cav, with_qq)
-    assert total == _reference_disp(len(DIMS), DIMS, npv, nqq, turb, cav, with_qq)
+        assert disp[r] == _reference_disp(r, DIMS, npv, nqq, turb, cav, with_qq, csf)
+    assert total == _reference_disp(len(DIMS), DIMS, npv, nqq, turb, cav, with_qq, csf)
 
 
 def _random_states(cfg, blocks, npv, nqq, rng):
@@ -54,7 +57,7 @@ def _random_states(cfg, blocks, npv, nqq, rng):
         inner = (b["kmax"] - 1, b["jmax"] - 1, b["imax"] - 1)
         states.append(dict(pv=rng.standard_normal(pad + (npv,)), tv=rng.standard_normal(pad + (3,)),
                            qq=rng.standard_normal(inner + (max(nqq, 1) * npv,))[..., :nqq * npv],
-                           rcav=rng.standard_normal(inner + (2,))))
+                           rcav=rng.standard_normal(inner + (2,)), csf=rng.standard_normal(inner + (3,))))
     return states
 
 
@@ -81,6 +84,9 @@ def test_oracle_write_read_round_trip(cfg, tmp_path):
         assert (rec["rcav"] is not None) == cav
         if cav:
             assert np.array_equal(rec["rcav"], s["rcav"])
+        assert (rec["csf"] is not None) == ock.csf_flag(cfg)
+        if ock.csf_flag(cfg):
+            assert np.array_equal(rec["csf"], s["csf"])
     with open(path, "r+b") as f:
         f.truncate(len(data) - 8)
     with pytest.raises(ValueError):

@@ -1,5 +1,6 @@
-"""Error paths of the C ABI on a GPU, made on the host: a non-finite uploaded state, and
-out-of-range arguments.  Nothing here faults the device; the handle stays usable."""
+"""Error paths of the C ABI on a GPU, made on the host: a non-finite uploaded state,
+out-of-range arguments, a grid with a collapsed cell.  Nothing here faults the device; the
+handle stays usable."""
 import numpy as np
 import pytest
 
@@ -71,3 +72,16 @@ def test_dataflow_sweeps_equal_hyperplane_sweeps(monkeypatch):
         scale = np.abs(a).reshape(-1, a.shape[-1]).max(axis=0)
         assert (np.abs(a - b).reshape(-1, a.shape[-1]).max(axis=0) <= 1e-12 * scale).all()
         assert np.array_equal(b, b2)
+
+
+def test_collapsed_cell_is_rejected_at_create():
+    """The device metrics find a cell of zero volume (two node planes made to coincide) and
+    create fails with a descriptor error, as the host check did; a good grid still builds."""
+    c = cases.make("plain_small", scale=8)
+    xyz = c["blocks"][0]["xyz"]
+    xyz[3] = xyz[2]          # node planes k = 3 and k = 4 (Fortran numbering) coincide
+    with pytest.raises(Cfd3dError) as ei:
+        native.Engine(c)
+    assert ei.value.code == abi.ERR_DESCRIPTOR
+    assert "volume" in str(ei.value)
+    native.Engine(cases.make("plain_small", scale=8))

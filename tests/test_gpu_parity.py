@@ -31,6 +31,8 @@ CASES = {
     "adjoint_sst": ("adjoint", dict(scale=8), dict(fix_cav_clamp=1)),
     "large_sst_bdf2": ("large", dict(scale=16), dict(fix_cav_clamp=1)),
     "batched_multiblock": ("batched", dict(scale=4, nblocks=6), dict(fix_cav_clamp=1)),
+    # the batched workload's 24 uneven blocks in four chains, at 1/8 of its extents
+    "batched_24": ("batched", dict(scale=8, nblocks=24), dict(fix_cav_clamp=1)),
 }
 
 

@@ -20,15 +20,12 @@ import numpy as np
 import pytest
 
 from cfd3d_gb300 import cases, native
-from tests.helpers import field_err, interior, rel_err
+from tests.helpers import dv_eos_err, field_err, interior
 
 pytestmark = pytest.mark.gpu
 
 TOL_RES = 1e-9
 TOL_STATE = 1e-9
-# the update's EOS against the oracle's at the same state (as the pointwise EOS test)
-TOL_EOS = 1e-11
-TOL_EOS_STIFFENED = 2e-9
 # the plain configuration after its 100 iterations: the per-cell bound of the CPU
 # restatement's parity target
 TOL_STATE_C1 = 1e-10
@@ -77,9 +74,7 @@ def _state_err(e, o, c):
     the same p, T, y1, y2): the mixture sound speed of a cell holding a trace of vapour
     (y1 ~ 1e-11) moves with y1 far more than y1 itself does, so the two trajectories'
     dv may differ by more than their pv while each is the EOS of its state."""
-    from oracle import oracle_py
     worst = 0.0
-    pref = float(c["cfg"]["pref"])
     for b in range(len(c["blocks"])):
         sg, so = e.download(b), o.get_state(b)
         worst = max(worst, field_err(interior(sg["pv"]), interior(so["pv"])).max())
@@ -87,12 +82,8 @@ def _state_err(e, o, c):
             worst = max(worst, field_err(interior(sg["tv"]), interior(so["tv"])).max())
         if c["cfg"].get("ncav", 0):
             worst = max(worst, field_err(sg["rcav"], so["rcav"]).max())
-        pv = interior(sg["pv"]).reshape(-1, e.npv)
-        dv_eos, _ = oracle_py.eos(pv[:, 0] + pref, pv[:, 4], pv[:, 5], pv[:, 6], fluid=int(c["cfg"]["fluid"]),
-                                  prop=int(c["cfg"]["iturb"]) != -3)
-        dv = interior(sg["dv"]).reshape(-1, 18)
-        tol = TOL_EOS_STIFFENED if int(c["cfg"]["fluid"]) == 1 else TOL_EOS
-        assert np.all(rel_err(dv, dv_eos, floor=1e-30) < tol), np.max(rel_err(dv, dv_eos, floor=1e-30))
+        err, tol = dv_eos_err(interior(sg["pv"]), interior(sg["dv"]), c["cfg"])
+        assert err < tol, err
     return worst
 
 

@@ -28,10 +28,14 @@ def test_input_roundtrip():
 def test_input_flags_unsupported_options():
     cfg = dict(cases.make("plain_small", scale=16)["cfg"])
     text = write_input(cfg).splitlines()
-    # gravity / csf value line is the 20th line (10th label/value pair)
-    text[19] = "1 0"
+    # gravity / csf value line is the 20th line (10th label/value pair): both are engine options
+    text[19] = "1 1"
+    back, bad = read_input("\n".join(text) + "\n")
+    assert bad == [] and back["gravity"] == 1 and back["csf"] == 1
+    # iread / rstnum (2nd pair): a restart, which the solve loop takes, not the engine
+    text[3] = "1 5"
     _, bad = read_input("\n".join(text) + "\n")
-    assert bad == ["gravity"]
+    assert bad == ["iread"]
 
 
 def test_fortran_real_literals():

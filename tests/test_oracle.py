@@ -120,6 +120,56 @@ def test_multiblock_split_matches_single_block_residual(oracle):
     assert err.max() < 1e-12, err
 
 
+def _split_i(single, kinds_a, kinds_b):
+    """The single block of `single` cut into two point-matched blocks along i."""
+    xyz = single["blocks"][0]["xyz"]
+    nk, nj, ni, _ = xyz.shape
+    h = (ni - 1) // 2
+    a, b = xyz[:, :, : h + 1], xyz[:, :, h:]
+    J, K = nj, nk
+    Ia, Ib = a.shape[2], b.shape[2]
+    ba = {"imax": Ia, "jmax": J, "kmax": K, "xyz": a, "bc": cases.face_patches(Ia, J, K, kinds_a),
+          "con": [{"donor": 1, "pnts": (Ia, 1, 1, Ia, J, K), "pnts_donor": (1, 1, 1, 1, J, K), "transform": (1, 2, 3)}]}
+    bb = {"imax": Ib, "jmax": J, "kmax": K, "xyz": b, "bc": cases.face_patches(Ib, J, K, kinds_b),
+          "con": [{"donor": 0, "pnts": (1, 1, 1, 1, J, K), "pnts_donor": (Ia, 1, 1, Ia, J, K), "transform": (1, 2, 3)}]}
+    pv = single["pv0"][0]
+    return {"cfg": dict(single["cfg"]), "blocks": [ba, bb], "pv0": [pv[:, :, : Ia - 1], pv[:, :, Ia - 1:]]}
+
+
+def test_surface_tension_split_matches_single_block(oracle):
+    """The surface-tension source (csf = 1) on the cavitating start, whose vapour sphere
+    straddles the cut: two point-matched blocks reproduce the single block's residual and
+    source, which needs the volume-fraction gradient's halo (setbc_vfg) at the cut.  The
+    source is not zero, and uniform flow (no interface) gets none."""
+    from cfd3d_gb300.abi import BC_FARFIELD, BC_SYMMETRY
+    single = cases.make("cavitating", scale=8, fix_cav_clamp=1)
+    single["cfg"]["csf"] = 1
+    sym = {"jmin": BC_SYMMETRY, "jmax": BC_SYMMETRY, "kmin": BC_SYMMETRY, "kmax": BC_SYMMETRY}
+    split = _split_i(single, dict(sym, imin=BC_FARFIELD), dict(sym, imax=BC_FARFIELD))
+    o1 = oracle.Oracle(single)
+    o1.initialize(single["pv0"])
+    o2 = oracle.Oracle(split)
+    o2.initialize(split["pv0"])
+    r1 = o1.residual(0)["res"]
+    c1 = o1.get_csf(0)["csf"]
+    r2 = np.concatenate([o2.residual(0)["res"], o2.residual(1)["res"]], axis=2)
+    c2 = np.concatenate([o2.get_csf(0)["csf"], o2.get_csf(1)["csf"]], axis=2)
+    assert np.abs(c1).max() > 0.0
+    core = (slice(2, -2), slice(2, -2), slice(None))
+    scale = np.maximum(np.abs(r1).max(axis=(0, 1, 2)), 1e-300)
+    assert (np.abs(r1[core] - r2[core]).max(axis=(0, 1, 2)) / scale).max() < 1e-12
+    assert np.abs(c1[core] - c2[core]).max() <= 1e-12 * np.abs(c1).max()
+    uni = cases.make("cavitating", scale=8, fix_cav_clamp=1)
+    uni["cfg"]["csf"] = 1
+    ou = oracle.Oracle(uni)
+    pv = uni["pv0"][0].copy()
+    pv[..., :] = pv[0, 0, 0, :]
+    pv[..., 5] = 0.0
+    ou.initialize([pv])
+    ou.residual(0)
+    assert np.abs(ou.get_csf(0)["csf"]).max() == 0.0
+
+
 def test_totalpressure_inlet_pooled_across_blocks(oracle):
     """A total-pressure inlet on a k face split over two blocks: the reference reduces its
     averages over every rank carrying the inlet (one communicator), so the split case
