@@ -191,6 +191,7 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
           push_cell(a, c, n, src, gp, gd);
           break;
         case G_WALL_VISCOUS:
+        case G_CRWALL:   // (the grid velocity is no function of the state)
           gp[1] = -gp[1]; gp[2] = -gp[2]; gp[3] = -gp[3];
           push_cell(a, c, n, src, gp, gd);
           break;
@@ -257,8 +258,9 @@ __global__ void k_adj_ghost(DevPtr d, Par c, AdjPtr a, const GhostOp* __restrict
           }
           break;
         }
-        case G_SYMMETRY: {
-          // u_ghost = 2 (u_b - n (u_b . n) / |n|^2) - u_src
+        case G_SYMMETRY:
+        case G_CRWALL_INV: {
+          // u_ghost = 2 (u_b - n (u_b . n) / |n|^2 [- gridvel]) - u_src
           double nx[3];
           face_vec(d, op.fplane, op.fidx, nx);
           for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;

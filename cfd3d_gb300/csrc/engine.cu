@@ -337,6 +337,15 @@ __device__ void tp_newt(const TpProblem& P, double* x) {
   }
 }
 
+// the grid velocity omega x r of a boundary face: r the mean of the centroids of the
+// boundary cell b and the ghost cell across the face (gridvel, e.g. src/bc_module.f90:3539-3559)
+__device__ __forceinline__ void face_gridvel(const DevPtr& d, const Par& c, long long b, long long gc, double* gv) {
+  const long long n = d.ncell;
+  double r[3];
+  for (int e = 0; e < 3; ++e) r[e] = 0.5 * (d.gm[(GM_GRD + 1 + e) * n + b] + d.gm[(GM_GRD + 1 + e) * n + gc]);
+  grid_vel(c, r, gv);
+}
+
 // one CTA per pool of total-pressure patches (the n-th inlet of every block): the
 // area-weighted boundary averages over the pool (the reference's reduction over its
 // communicator), then the Newton solve by thread 0
@@ -351,8 +360,10 @@ __global__ void __launch_bounds__(128) k_totalp(DevPtr d, Par c) {
     face_vec(d, E[2], E[1], nx);
     const double dl = sqrt(nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
     const long long b = E[0];
+    double gv[3] = {0.0, 0.0, 0.0};
+    if (c.rot) face_gridvel(d, c, b, E[3], gv);
     acc[0] += d.pv[b] * dl;
-    for (int q = 0; q < 3; ++q) acc[1 + q] += d.pv[(1 + q) * n + b] * dl;
+    for (int q = 0; q < 3; ++q) acc[1 + q] += (d.pv[(1 + q) * n + b] + gv[q]) * dl;
     acc[4] += d.pv[4 * n + b] * dl;
     acc[5] += dl;
   }
@@ -459,9 +470,11 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       const double dl = 1.0 / sqrt(nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
       const double su = sqrt(X[2]);
       const double bp[NPVM] = {c.pref, 0.0, 0.0, 0.0, c.tp_tt, c.y1ref, c.y2ref, c.kref, c.oref};
+      double gv[3] = {0.0, 0.0, 0.0};
+      if (c.rot) face_gridvel(d, c, op.bnd, op.gcell, gv);
       double* pv = x.pv;
       pv[0] = 2.0 * (X[0] - c.pref) - pv[0];
-      for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (-su * nx[q3] * dl - 0.0) - pv[1 + q3];
+      for (int q3 = 0; q3 < 3; ++q3) pv[1 + q3] = 2.0 * (-su * nx[q3] * dl - gv[q3]) - pv[1 + q3];
       pv[4] = 2.0 * X[1] - pv[4];
       for (int v = 5; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
       pv[6] = 2.0 * bp[6] - pv[6];
@@ -471,15 +484,36 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       store_cell(d, c, op.dst, x);
       return;
     }
-    case G_CRWALL_KW:
-      // bccounterrotatingwallviscouskw (src/bc_module.f90:3654-3731) with the grid velocity
-      // omega x r = 0 (no rotation): u, v, w, k and mu_t reflected; omega is the mirror's,
-      // the reference's wall value being computed and then discarded
+    case G_CRWALL:
+    case G_CRWALL_KW: {
+      // bccounterrotatingwallviscous (src/bc_module.f90:3516-3580) and its k-omega variant
+      // (:3654-3731): u = -u_mirror - 2 gridvel; k-omega: k and mu_t reflected, omega the
+      // mirror's, the reference's wall value being computed and then discarded
       load_cell(d, c, op.src, x);
-      x.pv[1] = -x.pv[1]; x.pv[2] = -x.pv[2]; x.pv[3] = -x.pv[3]; x.pv[7] = -x.pv[7];
-      x.tv[2] = -x.tv[2];
+      double gv[3] = {0.0, 0.0, 0.0};
+      if (c.rot) face_gridvel(d, c, op.bnd, op.gcell, gv);
+      for (int q3 = 0; q3 < 3; ++q3) x.pv[1 + q3] = -x.pv[1 + q3] - 2.0 * gv[q3];
+      if (op.kind == G_CRWALL_KW) { x.pv[7] = -x.pv[7]; x.tv[2] = -x.tv[2]; }
       store_cell(d, c, op.dst, x);
       return;
+    }
+    case G_CRWALL_INV: {
+      // bccounterrotatingwallinviscid (:3733-3810): the symmetry reflection of the boundary
+      // cell's velocity less the face's grid velocity
+      load_cell(d, c, op.src, x);
+      double nx[3];
+      face_vec(d, op.fplane, op.fidx, nx);
+      for (int v = 0; v < 3; ++v) nx[v] *= (double)op.fsign;
+      double gv[3] = {0.0, 0.0, 0.0};
+      if (c.rot) face_gridvel(d, c, op.bnd, op.gcell, gv);
+      const double us = d.pv[n + op.bnd], vs = d.pv[2 * n + op.bnd], ws = d.pv[3 * n + op.bnd];
+      const double un = (us * nx[0] + vs * nx[1] + ws * nx[2]) / (nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2]);
+      x.pv[1] = 2.0 * (us - nx[0] * un - gv[0]) - x.pv[1];
+      x.pv[2] = 2.0 * (vs - nx[1] * un - gv[1]) - x.pv[2];
+      x.pv[3] = 2.0 * (ws - nx[2] * un - gv[2]) - x.pv[3];
+      store_cell(d, c, op.dst, x);
+      return;
+    }
     case G_HFWALL_KW: {
       // bcheatfluxwallviscouskw (src/bc_module.f90:4184-4273): u, v, w, k reflected, the
       // wall temperature from the heat flux through the boundary cell, the SST omega wall
@@ -499,13 +533,15 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
     }
     case G_MASSFLOW_IN: {
       // bcmassflowratein (:3812-4012) with the rate 0 its construct sets: the inflow speed
-      // m / (rho A) is 0, so the velocity reflects; T, y1, y2, k, omega from the free stream;
-      // the pressure stays the mirror's; EOS of the ghost state
+      // m / (rho A) is 0, so u = 2 (0 - gridvel) - u_mirror; T, y1, y2, k, omega from the
+      // free stream; the pressure stays the mirror's; EOS of the ghost state
       load_cell(d, c, op.src, x);
       const double bp[NPVM] = {c.pref, c.uref_vec[0], c.uref_vec[1], c.uref_vec[2], c.tref, c.y1ref, c.y2ref,
                                c.kref, c.oref};
+      double gv[3] = {0.0, 0.0, 0.0};
+      if (c.rot) face_gridvel(d, c, op.bnd, op.gcell, gv);
       double* pv = x.pv;
-      for (int q3 = 1; q3 < 4; ++q3) pv[q3] = -pv[q3];
+      for (int q3 = 1; q3 < 4; ++q3) pv[q3] = 2.0 * (0.0 - gv[q3 - 1]) - pv[q3];
       for (int v = 4; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
       pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
       pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
@@ -927,6 +963,19 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] + rv * a[e];
     res[4] = res[4] + rv * (a[0] * pv2[1] + a[1] * pv2[2] + a[2] * pv2[3]);
   }
+  if (XS && c.rot) {
+    // rotation%getrotationsource (src/rotation_module.f90:75-97), subtracted
+    // (src/rhs_module.f90:600-605): rho vol (2 omega x u + omega x (omega x r))
+    const double* w = c.omega;
+    double r[3];
+    for (int e = 0; e < 3; ++e) r[e] = d.gm[(GM_GRD + 1 + e) * n + g];
+    const double cor[3] = {2.0 * (w[1] * pv2[3] - w[2] * pv2[2]), 2.0 * (w[2] * pv2[1] - w[0] * pv2[3]),
+                           2.0 * (w[0] * pv2[2] - w[1] * pv2[1])};
+    const double cen[3] = {w[0] * (w[1] * r[1] + w[2] * r[2]) - r[0] * (w[1] * w[1] + w[2] * w[2]),
+                           w[1] * (w[0] * r[0] + w[2] * r[2]) - r[1] * (w[0] * w[0] + w[2] * w[2]),
+                           w[2] * (w[0] * r[0] + w[1] * r[1]) - r[2] * (w[0] * w[0] + w[1] * w[1])};
+    for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] - dv[0] * vol * (cor[e] + cen[e]);
+  }
   if (XS && c.csf) {
     double cs[5];
     csf_cell(d, g, sj, sk, vol, pv2, cs);
@@ -935,6 +984,13 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   }
   for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
   if constexpr (!REC) return;   // the explicit schemes need no sweep records
+  if (c.rot) {
+    // the implicit operator's enthalpy is the rothalpy (lhs%getenthalpy, jac%getenthalpy):
+    // the diagonal block below and the neighbours' products read it from the record's dv(2)
+    double r[3];
+    for (int e = 0; e < 3; ++e) r[e] = d.gm[(GM_GRD + 1 + e) * n + g];
+    dv[1] = dv[1] - rot_q(c, r);
+  }
   // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous
   // term), written with its state and residual as the cell's sweep record at pos[g]
   double tvc[3] = {0.0, 0.0, 0.0};
@@ -1466,6 +1522,12 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
       double cur[NPVM], dvc[NDV], r[NPVM], x[NPVM];
       for (int v = 0; v < npv; ++v) { cur[v] = d.pv[v * n + g]; r[v] = d.res[v * n + g]; }
       for (int v = 0; v < NDV; ++v) dvc[v] = d.dv[v * n + g];
+      if (c.rot) {
+        // the explicit diagonal's enthalpy is the rothalpy (lhs%getenthalpy)
+        double rc[3];
+        for (int e = 0; e < 3; ++e) rc[e] = d.gm[(GM_GRD + 1 + e) * n + g];
+        dvc[1] = dvc[1] - rot_q(c, rc);
+      }
       getx_explicit(c, cur, dvc, r, d.dt[g], d.gm[GM_GRD * n + g], x);
       const double a1[3] = {0.0, 0.75, 1.0 / 3.0}, a2[3] = {1.0, 0.25, 2.0 / 3.0};
       const bool rk3 = c.timemethod == 2;
@@ -1742,7 +1804,7 @@ template <bool REC>
 void launch_rhs_rec(const Engine& E, cudaStream_t s, int T) {
   const Par& c = E.par;
   const unsigned g = nblk_of(E.nint, T);
-  const bool xs = (c.iturb == 0 && c.ides != 0) || c.gravity != 0 || c.csf != 0;
+  const bool xs = (c.iturb == 0 && c.ides != 0) || c.gravity != 0 || c.csf != 0 || c.rot != 0;
   if (c.mixed) {
     if (xs) k_rhs<true, REC, true><<<g, T, 0, s>>>(E.d, c);
     else k_rhs<true, REC, false><<<g, T, 0, s>>>(E.d, c);
@@ -1924,7 +1986,12 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
   if (in->prec < 0 || in->prec > 2) { err = "prec out of range"; return false; }
   if (in->csf != 0 && in->csf != 1) { err = "csf must be 0 or 1"; return false; }
   c.csf = in->csf;
-  if (in->rotation != 0) { err = "rotation is not supported"; return false; }
+  // rotation, rpm: omega along +-x, +-y, +-z (src/config_module.f90:126-141)
+  if (in->rotation < -3 || in->rotation > 3) { err = "rotation must be 0, +-1, +-2 or +-3"; return false; }
+  if (in->rotation != 0 && in->precision == CFD3D_MIXED) { err = "the rotating frame runs in the FP64 form"; return false; }
+  c.rot = in->rotation != 0;
+  if (c.rot)
+    c.omega[std::abs(in->rotation) - 1] = (in->rotation > 0 ? 1.0 : -1.0) * in->rpm * 2.0 * (std::atan(1.0) * 4.0) / 60.0;
   if (in->nsteady >= 1 && !(in->dt_phy > 0.0)) { err = "dual time stepping needs dt_phy > 0"; return false; }
   if (in->precision != CFD3D_FP64 && in->precision != CFD3D_MIXED) { err = "precision must be CFD3D_FP64 or CFD3D_MIXED"; return false; }
   c.mixed = (in->precision == CFD3D_MIXED);
@@ -2929,6 +2996,7 @@ int cfd3d_residual_vjp(cfd3d_handle* h, const double* cot, double* g_state, doub
   if (E.par.iturb == -1) { E.err = "the adjoint does not cover the k-epsilon model"; return CFD3D_ERR_ARG; }
   if (E.d.ntp) { E.err = "the adjoint does not cover total-pressure inlets"; return CFD3D_ERR_ARG; }
   if (E.par.csf) { E.err = "the adjoint does not cover the surface-tension source"; return CFD3D_ERR_ARG; }
+  if (E.par.rot) { E.err = "the adjoint does not cover the rotating frame"; return CFD3D_ERR_ARG; }
   if ((rc = adjoint_buffers(E))) return rc;
   // the cotangent, block after block, into the padded interior
   size_t off = 0;

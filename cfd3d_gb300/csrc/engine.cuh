@@ -33,7 +33,7 @@ enum GhostKind : int {
   G_COPY = 0, G_EXTRAP, G_WALL_VISCOUS, G_WALL_KW, G_SYMMETRY, G_FARFIELD,
   G_WALLWALL, G_WALLWALL_KW4, G_WALLWALL_KW8, G_NOWALL3, G_NOWALL7,
   G_INFLOW_SUB, G_OUTFLOW_SUB, G_INFLOW_SUP,  // the farfield treatment with a forced branch
-  G_CRWALL_KW, G_MASSFLOW_IN, G_HFWALL_KW, G_WALL_KE, G_TOTALP
+  G_CRWALL_KW, G_MASSFLOW_IN, G_HFWALL_KW, G_WALL_KE, G_TOTALP, G_CRWALL, G_CRWALL_INV
 };
 
 // the farfield_pv branch of a characteristic ghost kind
@@ -52,6 +52,7 @@ struct GhostOp {
   int fplane;     // GM_CX / GM_EX / GM_TX
   float fsign;    // +1 / -1
   int pad;
+  int gcell;      // the ghost cell across the boundary face from bnd (the face's grid velocity)
 };
 
 // device scalars of one iteration

@@ -68,6 +68,15 @@ __global__ void __launch_bounds__(256) k_face_flux(DevPtr d, Par c) {
     L.rho = d.dv[g]; L.h = d.dv[n + g]; L.c2 = d.dv[5 * n + g];
     R.rho = d.dv[gr]; R.h = d.dv[n + gr]; R.c2 = d.dv[5 * n + gr];
   }
+  if (c.rot) {
+    // rothalpy_l / rothalpy_r (src/flux_module.f90:697-721): the face states' total enthalpy
+    // less 0.5 |omega x r|^2 at the left and right cells' centroids; h enters the fluxes
+    // only through it
+    double rl[3], rr[3];
+    for (int e = 0; e < 3; ++e) { rl[e] = d.gm[(GM_GRD + 1 + e) * n + g]; rr[e] = d.gm[(GM_GRD + 1 + e) * n + gr]; }
+    L.h = L.h - rot_q(c, rl);
+    R.h = R.h - rot_q(c, rr);
+  }
   double sdst[18];
   if (c.nscheme == 2 || c.nscheme == 3) {
 #pragma unroll

@@ -33,6 +33,8 @@ struct Par {
   int ides;         // SST length scale: 0 RANS, 1 DES, 2 DDES, 3 IDDES, 4 simplified IDDES
   int gravity;      // gravity source: 0 none, else the device history d.grav
   int csf;          // 1: the surface-tension source (d.vfg, d.csf)
+  int rot;          // 1: a rotating frame of angular velocity omega (FP64 form)
+  double omega[3];
   double tp_pt, tp_tt, tp_ht;   // total-pressure inlet: p_total, T_total, h(p_total, T_total)
   double dt_phy, cfl, c_v, c_c, pref, uref, str, rhoref, l_chord;
   double kref, oref, emutref;
@@ -48,6 +50,24 @@ struct Par {
 
 template <class T>
 __device__ __forceinline__ T sq(const T& x) { return x * x; }
+
+// The rotating frame (src/rotation_module.f90, src/config_module.f90:126-141): the grid
+// velocity omega x r of the boundary routines (gridvel, e.g. src/bc_module.f90:3557-3559),
+// and 0.5 |omega x r|^2, the term that turns the total enthalpy into the rothalpy, written
+// as rothalpy_l / rothalpy_r / the lhs's and jacobian's rothalpy write it
+// (src/flux_module.f90:697-721, src/lhs_module.f90:573-584, src/jacobian_module.f90:486-495),
+// r the cell centroid.
+__device__ __forceinline__ void grid_vel(const Par& c, const double* r, double* gv) {
+  gv[0] = c.omega[1] * r[2] - c.omega[2] * r[1];
+  gv[1] = c.omega[2] * r[0] - c.omega[0] * r[2];
+  gv[2] = c.omega[0] * r[1] - c.omega[1] * r[0];
+}
+__device__ __forceinline__ double rot_q(const Par& c, const double* r) {
+  const double* w = c.omega;
+  return 0.5 * (w[0] * w[0] * (r[1] * r[1] + r[2] * r[2]) + w[1] * w[1] * (r[0] * r[0] + r[2] * r[2]) +
+                w[2] * w[2] * (r[0] * r[0] + r[1] * r[1]) -
+                2.0 * (w[0] * w[1] * r[0] * r[1] + w[1] * w[2] * r[1] * r[2] + w[2] * w[0] * r[2] * r[0]));
+}
 
 // the preconditioning speed with the squared reference speed uref2 given, for the
 // adjoint's derivative with respect to the free-stream speed

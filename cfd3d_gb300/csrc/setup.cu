@@ -571,11 +571,11 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
       bi.face = (Face)(2 * ax + (mn ? 0 : 1));
       switch (bi.type) {
         case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
-        // the counter-rotating family without rotation: the laminar and inviscid variants
-        // are the plain wall's and symmetry's formulas, the SST one differs
+        // the counter-rotating family (src/bc_module.f90:3516-3810): the wall at rest while
+        // the grid turns, so the ghost velocity takes twice the face's grid velocity off
         case CFD3D_BC_WALL_COUNTERROTATING:
           if (c.iturb == -1) { E.err = "counter-rotating walls under k-epsilon are not built"; return false; }
-          bi.kind = (c.iturb == 0) ? G_CRWALL_KW : wall_kind(c);
+          bi.kind = (c.iturb == 0) ? G_CRWALL_KW : (c.iturb == -2 ? G_CRWALL : G_CRWALL_INV);
           break;
         case CFD3D_BC_WALL_HEATFLUX: {
           // the HeatFlux family (src/bc_module.f90:233-249): the SST variant.  The laminar
@@ -656,8 +656,10 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
             for (int q = 0; q < 6; ++q) op.nb[q] = -1;
             op.fidx = op.src; op.fplane = GM_CX; op.fsign = 1.0f;
             op.pad = (bi.kind == G_TOTALP) ? bi.tp_index : bi.hf_off;
+            op.gcell = op.src;
             if (bi.kind == G_SYMMETRY || bi.kind == G_FARFIELD || bi.kind == G_WALL_KW || bi.kind == G_HFWALL_KW ||
-                bi.kind == G_TOTALP || ghost_ff_mode(bi.kind)) {
+                bi.kind == G_TOTALP || bi.kind == G_CRWALL || bi.kind == G_CRWALL_INV || bi.kind == G_CRWALL_KW ||
+                bi.kind == G_MASSFLOW_IN || ghost_ff_mode(bi.kind)) {
               int ii = mi, jj = mj, kk = mk;
               float s = bi.farfield_sign ? -1.0f : 1.0f;
               switch (bi.face) {
@@ -670,13 +672,22 @@ bool setup_ghost_program(Engine& E, const cfd3d_block_desc* blocks, int nblocks)
                 default: break;  // corner 'Kmin'/'Kmax': the boundary cell stays the mirror cell
               }
               op.bnd = gi(ii, jj, kk);
+              switch (bi.face) {
+                case F_IMIN: op.gcell = gi(ii - 1, jj, kk); break;
+                case F_IMAX: op.gcell = gi(ii + 1, jj, kk); break;
+                case F_JMIN: op.gcell = gi(ii, jj - 1, kk); break;
+                case F_JMAX: op.gcell = gi(ii, jj + 1, kk); break;
+                case F_KMIN: op.gcell = gi(ii, jj, kk - 1); break;
+                case F_KMAX: op.gcell = gi(ii, jj, kk + 1); break;
+                default: op.gcell = op.bnd; break;
+              }
               if (bi.kind == G_TOTALP) {
                 // the patch's reduction visits each boundary face once: the outermost layer
                 const int ax = (int)bi.face / 2;
                 const int idx[3] = {i, j, k};
                 if (idx[ax] == (((int)bi.face % 2 == 0) ? bi.s[ax] : bi.e[ax])) {
                   std::vector<int>& te = tp_ent[bi.tp_index];
-                  te.push_back(op.bnd); te.push_back(op.fidx); te.push_back(op.fplane); te.push_back(0);
+                  te.push_back(op.bnd); te.push_back(op.fidx); te.push_back(op.fplane); te.push_back(op.gcell);
                 }
               }
             }

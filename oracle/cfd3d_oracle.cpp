@@ -56,6 +56,7 @@ enum Face { F_IMIN, F_IMAX, F_JMIN, F_JMAX, F_KMIN, F_KMAX, F_KMIN_CAP, F_KMAX_C
 enum BcKind {
   K_WALL_INVISCID, K_WALL_VISCOUS, K_WALL_KW, K_FARFIELD, K_EXTRAP, K_SYMMETRY, K_NOOP,
   K_INFLOW_SUB, K_OUTFLOW_SUB, K_INFLOW_SUP, K_CRWALL_KW, K_MASSFLOW_IN, K_SHIFTED, K_HFWALL_KW, K_WALL_KE, K_TOTALP,
+  K_CRWALL, K_CRWALL_INV,
   K_EDGE_WALLWALL, K_EDGE_WALLWALL_KW, K_EDGE_NOWALL, K_CORNER_WALLWALL, K_CORNER_WALLWALL_KW, K_CORNER_NOWALL
 };
 
@@ -131,6 +132,12 @@ static bool make_cfg(const cfd3d_config* in, Cfg& c, std::string& err) {
   } else if (c.gravity != 0) { err = "gravity must be 0, +-1, +-2, +-3 or 4"; return false; }
   c.csf = in->csf;
   if (c.csf != 0 && c.csf != 1) { err = "csf must be 0 or 1"; return false; }
+  /* rotation, rpm: omega along +-x, +-y, +-z (src/config_module.f90:126-141) */
+  c.rotation = in->rotation;
+  if (c.rotation < -3 || c.rotation > 3) { err = "rotation must be 0, +-1, +-2 or +-3"; return false; }
+  for (int e = 0; e < 3; ++e) c.omega[e] = 0.0;
+  if (c.rotation != 0)
+    c.omega[std::abs(c.rotation) - 1] = (c.rotation > 0 ? 1.0 : -1.0) * in->rpm * 2.0 * c.pi / 60.0;
   if (c.timemethod < 1 || c.timemethod > 3) { err = "timemethod must be 1 (Euler), 2 (RK3) or 3 (LU-SGS)"; return false; }
   if (c.iturb == -3) { c.npv = 7; c.ntv = 0; }
   else if (c.iturb == -2) { c.npv = 7; c.ntv = 2; }
@@ -502,10 +509,10 @@ static bool build_bcs(const Cfg& c, Block& B, const cfd3d_block_desc& d, std::st
     bi.face = (Face)(2 * axis + (mn ? 0 : 1));
     switch (p.type) {
       case CFD3D_BC_WALL: bi.kind = wall_kind(c); break;
-      /* the CounterRotating family (:3516-3810) with grid velocity 0: the SST variant differs */
+      /* the CounterRotating family (:3516-3810): the wall at rest while the grid turns */
       case CFD3D_BC_WALL_COUNTERROTATING:
         if (c.iturb == -1) { err = "counter-rotating walls under k-epsilon are not built"; return false; }
-        bi.kind = (c.iturb == 0) ? K_CRWALL_KW : wall_kind(c);
+        bi.kind = (c.iturb == 0) ? K_CRWALL_KW : (c.iturb == -2 ? K_CRWALL : K_CRWALL_INV);
         break;
       case CFD3D_BC_WALL_HEATFLUX:   /* the HeatFlux family: bcheatfluxwallviscouskw :4184-4273 */
         if (c.iturb != 0) { err = "heat-flux walls need the SST model (iturb = 0)"; return false; }
@@ -847,6 +854,25 @@ static void face_cell(const BcInfo& bi, Block& B, int i, int j, int k, int& ii, 
   }
 }
 
+/* The grid velocity of a boundary face (gridvel of the counter-rotating walls, the
+   mass-flow and total-pressure inlets): omega x r at the mean of the centroids of the
+   boundary cell (ii, jj, kk) and the ghost cell across the face (e.g. :3539-3559). */
+static void face_gridvel(const Cfg& c, Block& B, const BcInfo& bi, int ii, int jj, int kk, double* gv) {
+  int gi = ii, gj = jj, gk = kk;
+  switch (bi.face) {
+    case F_IMIN: gi = ii - 1; break;
+    case F_IMAX: gi = ii + 1; break;
+    case F_JMIN: gj = jj - 1; break;
+    case F_JMAX: gj = jj + 1; break;
+    case F_KMIN: gk = kk - 1; break;
+    case F_KMAX: gk = kk + 1; break;
+    default: break;
+  }
+  double r[3];
+  for (int e = 0; e < 3; ++e) r[e] = 0.5 * (B.grd(1 + e, ii, jj, kk) + B.grd(1 + e, gi, gj, gk));
+  grid_vel(c, r, gv);
+}
+
 /* newt / funcv / fdjac / lnsrch / ludcmp / lubksb (src/bc_module.f90:4305-4622) for the
    total-pressure inlet, n = 2: as written, newt's fvec is evaluated once at its start */
 struct TpSys { const Cfg* c; double uu, gam; };
@@ -953,8 +979,8 @@ static void tp_newt(const TpSys& S, double* x) {
 }
 
 /* one total-pressure patch's area-weighted sums over its boundary faces (:3320-3409):
-   pa[0..4] += pv(1..5) dl, pa[5] += dl */
-static void tp_patch_sums(const Block& B, const BcInfo& bi, double* pa) {
+   pa[0..4] += pv(1..5) dl, the velocities with the grid velocity added, pa[5] += dl */
+static void tp_patch_sums(const Cfg& c, const Block& B, const BcInfo& bi, double* pa) {
   double nx[3];
   const int ax = (int)bi.face / 2;
   for (int k = bi.istart[2]; k <= bi.iend[2]; ++k)
@@ -966,9 +992,11 @@ static void tp_patch_sums(const Block& B, const BcInfo& bi, double* pa) {
         face_cell(bi, const_cast<Block&>(B), i, j, k, ii, jj, kk, nx, true);
         const double dl = std::sqrt(sq(nx[0]) + sq(nx[1]) + sq(nx[2]));
         const double* P = const_cast<Block&>(B).pv.at(ii, jj, kk);
+        double gv[3];
+        face_gridvel(c, const_cast<Block&>(B), bi, ii, jj, kk, gv);
         pa[0] += P[0] * dl;
         pa[4] += P[4] * dl;
-        for (int m = 1; m <= 3; ++m) pa[m] += P[m] * dl;
+        for (int m = 1; m <= 3; ++m) pa[m] += (P[m] + gv[m - 1]) * dl;
         pa[5] += dl;
       }
 }
@@ -1028,8 +1056,10 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
             face_cell(bi, B, i, j, k, ii, jj, kk, nx, true);
             const double dl = 1.0 / std::sqrt(sq(nx[0]) + sq(nx[1]) + sq(nx[2]));
             get_cell(c, B, mi, mj, mk, pv, dv, tv);
+            double gv[3];
+            face_gridvel(c, B, bi, ii, jj, kk, gv);
             pv[0] = 2.0 * (tpx[0] - bi.pv[0]) - pv[0];
-            for (int q = 0; q < 3; ++q) pv[1 + q] = 2.0 * (-std::sqrt(tpuu) * nx[q] * dl - 0.0) - pv[1 + q];
+            for (int q = 0; q < 3; ++q) pv[1 + q] = 2.0 * (-std::sqrt(tpuu) * nx[q] * dl - gv[q]) - pv[1 + q];
             pv[4] = 2.0 * tpx[1] - pv[4];
             for (int m = 5; m < c.npv; ++m) pv[m] = 2.0 * bi.pv[m] - pv[m];
             pv[6] = 2.0 * bi.pv[6] - pv[6];
@@ -1039,17 +1069,48 @@ static void apply_bc(const Cfg& c, Block& B, const BcInfo& bi) {
             put_cell(c, B, i, j, k, pv, dv, tv);
             break;
           }
-          case K_CRWALL_KW:
-            /* omega: the mirror's (the routine computes the wall value and discards it) */
+          case K_CRWALL:
+          case K_CRWALL_KW: {
+            /* bccounterrotatingwallviscous (:3516-3580) and its k-omega variant (:3654-3731):
+               u = -u_mirror - 2 gridvel; k-omega: k and mu_t reflected, omega the mirror's
+               (the routine computes the wall value and discards it) */
             get_cell(c, B, mi, mj, mk, pv, dv, tv);
-            pv[1] = -pv[1]; pv[2] = -pv[2]; pv[3] = -pv[3]; pv[7] = -pv[7];
-            tv[2] = -tv[2];
+            int ii = mi, jj = mj, kk = mk;
+            face_cell(bi, B, i, j, k, ii, jj, kk, nx, false);
+            double gv[3];
+            face_gridvel(c, B, bi, ii, jj, kk, gv);
+            for (int q = 0; q < 3; ++q) pv[1 + q] = -pv[1 + q] - 2.0 * gv[q];
+            if (bi.kind == K_CRWALL_KW) { pv[7] = -pv[7]; tv[2] = -tv[2]; }
             put_cell(c, B, i, j, k, pv, dv, tv);
             break;
-          case K_MASSFLOW_IN: {
-            /* massflowrate = 0 (construct): v = 0, the velocity reflects; p stays the mirror's */
+          }
+          case K_CRWALL_INV: {
+            /* bccounterrotatingwallinviscid (:3733-3810): the symmetry reflection of the
+               boundary cell's velocity less the grid velocity */
+            int ii = 0, jj = 0, kk = 0;
+            face_cell(bi, B, i, j, k, ii, jj, kk, nx, false);
+            const double* P = B.pv.at(ii, jj, kk);
+            for (int m = 0; m < c.npv; ++m) pvs[m] = P[m];
+            double gv[3];
+            face_gridvel(c, B, bi, ii, jj, kk, gv);
             get_cell(c, B, mi, mj, mk, pv, dv, tv);
-            for (int q = 0; q < 3; ++q) pv[1 + q] = -pv[1 + q];
+            double v3[3];
+            for (int q = 0; q < 3; ++q)
+              v3[q] = 2.0 * (pvs[1 + q] - nx[q] * (pvs[1] * nx[0] + pvs[2] * nx[1] + pvs[3] * nx[2]) /
+                                              (sq(nx[0]) + sq(nx[1]) + sq(nx[2])) - gv[q]) - pv[1 + q];
+            pv[1] = v3[0]; pv[2] = v3[1]; pv[3] = v3[2];
+            put_cell(c, B, i, j, k, pv, dv, tv);
+            break;
+          }
+          case K_MASSFLOW_IN: {
+            /* massflowrate = 0 (construct): v = 0, so u = 2 (0 - gridvel) - u_mirror; p stays
+               the mirror's */
+            get_cell(c, B, mi, mj, mk, pv, dv, tv);
+            int ii = mi, jj = mj, kk = mk;
+            face_cell(bi, B, i, j, k, ii, jj, kk, nx, false);
+            double gv[3];
+            face_gridvel(c, B, bi, ii, jj, kk, gv);
+            for (int q = 0; q < 3; ++q) pv[1 + q] = 2.0 * (0.0 - gv[q]) - pv[1 + q];
             for (int m = 4; m < c.npv; ++m) pv[m] = 2.0 * bi.pv[m] - pv[m];
             pv[5] = dmin(dmax(pv[5], 0.0), 1.0);
             pv[6] = dmin(dmax(pv[6], 0.0), 1.0);
@@ -1241,7 +1302,7 @@ static void tp_solve_pools(Oracle& O) {
     for (auto& bc : B.bcs) {
       if (bc.kind != K_TOTALP) continue;
       if (sums.size() <= n) sums.emplace_back(6, 0.0);
-      tp_patch_sums(B, bc, sums[n].data());
+      tp_patch_sums(O.c, B, bc, sums[n].data());
       ++n;
     }
   }
@@ -1448,7 +1509,8 @@ static void calrhs_block(const Cfg& c, Block& B, double time) {
     const double* nx = (dir == 0) ? B.cx.at(i, j, k) : (dir == 1 ? B.ex.at(i, j, k) : B.tx.at(i, j, k));
     double sdst[18];
     for (int l = 0; l < 18; ++l) sdst[l] = x[l][0];
-    FaceIn f{nx, pvl, pvr, dvl, dvr, sdst};
+    FaceIn f{nx, pvl, pvr, dvl, dvr, sdst, rot_q(c, B.grd.at(ci[0], ci[1], ci[2]) + 1),
+             rot_q(c, B.grd.at(cr[0], cr[1], cr[2]) + 1)};
     calflux(c, f, fi);
     if (vis) {
       const double *e1, *e2, *e3, *e4, *t1, *t2, *t3, *t4;
@@ -1561,6 +1623,19 @@ static void calrhs_block(const Cfg& c, Block& B, double time) {
           for (int e = 0; e < 3; ++e) B.res(1 + e, i, j, k) = B.res(1 + e, i, j, k) + dv[0] * grd[0] * a[e];
           B.res(4, i, j, k) = B.res(4, i, j, k) +
                               dv[0] * grd[0] * (a[0] * x7[1][1] + a[1] * x7[1][2] + a[2] * x7[1][3]);
+        }
+        if (c.rotation) {
+          /* rotation%getrotationsource (src/rotation_module.f90:75-97), subtracted
+             (src/rhs_module.f90:600-605): rho vol (2 omega x u + omega x (omega x r)) */
+          const double* w = c.omega;
+          const double* u = x7[1];
+          const double* r = grd + 1;
+          const double cor[3] = {2.0 * (w[1] * u[3] - w[2] * u[2]), 2.0 * (w[2] * u[1] - w[0] * u[3]),
+                                 2.0 * (w[0] * u[2] - w[1] * u[1])};
+          const double cen[3] = {w[0] * (w[1] * r[1] + w[2] * r[2]) - r[0] * (w[1] * w[1] + w[2] * w[2]),
+                                 w[1] * (w[0] * r[0] + w[2] * r[2]) - r[1] * (w[0] * w[0] + w[2] * w[2]),
+                                 w[2] * (w[0] * r[0] + w[1] * r[1]) - r[2] * (w[0] * w[0] + w[1] * w[1])};
+          for (int e = 0; e < 3; ++e) B.res(1 + e, i, j, k) = B.res(1 + e, i, j, k) - dv[0] * grd[0] * (cor[e] + cen[e]);
         }
         if (c.csf) {
           double cs[5];

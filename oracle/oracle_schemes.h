@@ -31,10 +31,30 @@ struct Cfg {
   int gravity;     /* 0 none, +-1..+-3 axis, 4 history */
   std::vector<double> grav_t, grav_a;   /* the history: times, accelerations (3 per row) */
   int csf;         /* 1: the surface-tension source rhs%csf */
+  int rotation;    /* 0 none, +-1..+-3: the rotating frame about +-x, +-y, +-z */
+  double omega[3]; /* its angular velocity (src/config_module.f90:126-141) */
   double tp_pt, tp_tt, tp_ht;   /* total-pressure inlet: its totals and h(p_t, T_t) */
   bool with_prop;  /* t_eos_prop (iturb >= -2) vs t_eosonly (Euler) */
   EosSel eos;
 };
+
+/* The rotating frame.  The grid velocity omega x r of the boundary routines (gridvel,
+   src/bc_module.f90:2496-2498 and the others), and the term that turns the total enthalpy
+   into the rothalpy, 0.5 |omega x r|^2 written as rothalpy_l / rothalpy_r / the lhs's and the
+   jacobian's rothalpy do (src/flux_module.f90:697-721, lhs_module.f90:573-584,
+   jacobian_module.f90:486-495), r the cell centroid grd(2:4).  Zero without rotation. */
+static inline void grid_vel(const Cfg& c, const double* r, double* gv) {
+  gv[0] = c.omega[1] * r[2] - c.omega[2] * r[1];
+  gv[1] = c.omega[2] * r[0] - c.omega[0] * r[2];
+  gv[2] = c.omega[0] * r[1] - c.omega[1] * r[0];
+}
+static inline double rot_q(const Cfg& c, const double* r) {
+  if (!c.rotation) return 0.0;
+  const double* w = c.omega;
+  return 0.5 * (w[0] * w[0] * (r[1] * r[1] + r[2] * r[2]) + w[1] * w[1] * (r[0] * r[0] + r[2] * r[2]) +
+                w[2] * w[2] * (r[0] * r[0] + r[1] * r[1]) -
+                2.0 * (w[0] * w[1] * r[0] * r[1] + w[1] * w[2] * r[1] * r[2] + w[2] * w[0] * r[2] * r[0]));
+}
 
 /* preconditioning speed (flux/lhs/jacobian/timestep/bc all share the same forms) */
 static inline double sndp2_of(const Cfg& c, double snd2, double u2) {
@@ -164,10 +184,12 @@ struct FaceIn {
   const double* nx;              /* unnormalised face area vector */
   const double *pvl, *pvr, *dvl, *dvr;
   const double* sdst;            /* pressure of stencil cells 1..18 */
+  double rotl, rotr;             /* rot_q of the left and right cells (0 without rotation) */
 };
 
-static inline double enth_l(const FaceIn& f) { return f.dvl[1] + 0.5 * (sq(f.pvl[1]) + sq(f.pvl[2]) + sq(f.pvl[3])); }
-static inline double enth_r(const FaceIn& f) { return f.dvr[1] + 0.5 * (sq(f.pvr[1]) + sq(f.pvr[2]) + sq(f.pvr[3])); }
+/* enthalpy_l / enthalpy_r, or rothalpy_l / rothalpy_r in a rotating frame */
+static inline double enth_l(const FaceIn& f) { return f.dvl[1] + 0.5 * (sq(f.pvl[1]) + sq(f.pvl[2]) + sq(f.pvl[3])) - f.rotl; }
+static inline double enth_r(const FaceIn& f) { return f.dvr[1] + 0.5 * (sq(f.pvr[1]) + sq(f.pvr[2]) + sq(f.pvr[3])) - f.rotr; }
 
 static inline double sdst_ratio_min(const double* s) {
   /* min over the 18 pressure ratios of the AUSMPW+ / Roe-M shock sensor */
@@ -919,7 +941,7 @@ static inline void lhs_getx(const Cfg& cf, const LhsIn& L, const double* res, do
   double sndp2 = sndp2_of(cf, dv[5], uv2);
   double ss = dv[0] * dv[11] * (1.0 / sndp2 + b / dv[5]);
   double rr = 1.0 / sndp2 - 1.0 / dv[5] + b1 * dv[6];
-  double hst = dv[1] + 0.5 * (sq(pv[1]) + sq(pv[2]) + sq(pv[3])) - uv2;
+  double hst = dv[1] + 0.5 * (sq(pv[1]) + sq(pv[2]) + sq(pv[3])) - rot_q(cf, L.grd + 1) - uv2;
   double cross = dv[13] * dv[8] - dv[12] * dv[9];
   double cross1 = dv[12] * dv[7] - dv[11] * dv[8];
   double cross2 = dv[13] * dv[7] - dv[11] * dv[9];
@@ -966,7 +988,7 @@ static inline void lhs_getx_ex(const Cfg& cf, const LhsIn& L, const double* res,
   double uv2 = sq(pv[1]) + sq(pv[2]) + sq(pv[3]);
   double ss = dv[0] * dv[11] * (1.0 / sndp2_of(cf, dv[5], uv2) + b / dv[5]);
   double rr = 1.0 / sndp2_of(cf, dv[5], uv2) - 1.0 / dv[5] + b1 * dv[6];
-  double hst = dv[1] + 0.5 * (sq(pv[1]) + sq(pv[2]) + sq(pv[3])) - uv2;
+  double hst = dv[1] + 0.5 * (sq(pv[1]) + sq(pv[2]) + sq(pv[3])) - rot_q(cf, L.grd + 1) - uv2;
   double cross = dv[13] * dv[8] - dv[12] * dv[9];
   double cross1 = dv[12] * dv[7] - dv[11] * dv[8];
   double cross2 = dv[13] * dv[7] - dv[11] * dv[9];
@@ -1015,7 +1037,7 @@ static inline void caljac(const Cfg& cf, const double* nx, const double* grd, co
     a[r][0] = pv[r] * a[0][0] + nx[r - 1];
     a[r][r] = pv[r] * a[0][r] + dv[0] * uuu;
   }
-  double h = dv[1] + 0.5 * (sq(pv[1]) + sq(pv[2]) + sq(pv[3]));
+  double h = dv[1] + 0.5 * (sq(pv[1]) + sq(pv[2]) + sq(pv[3])) - rot_q(cf, grd + 1);
   a[4][0] = dv[0] * uuu * dv[10] + h * a[0][0] - lamda - vis;
   a[4][1] = dv[0] * uuu * pv[1] + h * a[0][1];
   a[4][2] = dv[0] * uuu * pv[2] + h * a[0][2];
