@@ -1818,6 +1818,11 @@ void launch_rhs(const Engine& E, cudaStream_t s, int T, bool rec) {
   else launch_rhs_rec<false>(E, s, T);
 }
 
+// launches of the face fluxes and the residual: the FP64 form's three face kernels, or the
+// mixed form's shadow, its reconstruction and flux kernels of each direction (with the j and
+// k faces' column reconstruction under MUSCL), and k_rhs
+int face_rhs_launches(const Par& c) { return c.mixed ? (8 + (c.nmuscl > 0 ? 2 : 0)) : 4; }
+
 // The boundary program -- the total-pressure pools, then faces + halos, edges, corners -- and,
 // with the surface-tension source, calvfg and setbc_vfg after it, as timeinteg calls them
 // (src/update_module.f90:240-243, 359-362, 479-482).  Returns the number of launches.
@@ -1860,7 +1865,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   stage(3);
   launch_rhs(E, s, E.tpb_rhs, c.timemethod == 3);
   stage(4);
-  n += c.mixed ? 8 : 4;
+  n += face_rhs_launches(c);
   if (!full) { E.launches_per_iter = n; return; }
   if (c.timemethod != 3) {
     // explicit Euler (one stage) or RK3 (three; the time step is taken at the first only):
@@ -1872,7 +1877,7 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
         if (c.mixed) launch_face_flux_mixed(E, s);
         else launch_face_flux(E, s);
         launch_rhs(E, s, E.tpb_rhs, false);
-        n += c.mixed ? 8 : 4;
+        n += face_rhs_launches(c);
       }
       if (m == nstage) { stage(5); stage(6); }
       if (c.mixed) k_update<true, true><<<E.red_grid, T, 0, s>>>(d, c, m);
@@ -2172,7 +2177,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { E.err = "no CUDA device"; return CFD3D_ERR_NODEVICE; }
   // block layout
-  long long off = 0, ioff = 0, foff[3] = {0, 0, 0};
+  long long off = 0, ioff = 0, foff[3] = {0, 0, 0}, coff[3] = {0, 0, 0};
   for (int b = 0; b < nblocks; ++b) {
     const cfd3d_block_desc& d = blocks[b];
     if (d.imax < 4 || d.jmax < 4 || d.kmax < 4 || !d.xyz) { E.err = "block too small or no coordinates"; return CFD3D_ERR_DESCRIPTOR; }
@@ -2180,7 +2185,9 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     G.imax = d.imax; G.jmax = d.jmax; G.kmax = d.kmax;
     G.ni = d.imax + 5; G.nj = d.jmax + 5; G.nk = d.kmax + 5;
     G.off = off; G.int_off = ioff;
-    for (int q = 0; q < 3; ++q) G.face_off[q] = foff[q];
+    for (int q = 0; q < 3; ++q) { G.face_off[q] = foff[q]; G.col_off[q] = coff[q]; }
+    coff[1] += (long long)(d.imax - 1) * (d.kmax - 1);
+    coff[2] += (long long)(d.imax - 1) * (d.jmax - 1);
     off += (long long)G.ni * G.nj * G.nk;
     ioff += (long long)(d.imax - 1) * (d.jmax - 1) * (d.kmax - 1);
     foff[0] += (long long)d.imax * (d.jmax - 1) * (d.kmax - 1);
@@ -2190,7 +2197,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   }
   if (off >= (1ll << 31)) { E.err = "case too large for 32-bit cell indices"; return CFD3D_ERR_ARG; }
   E.ncell = off; E.nint = ioff;
-  for (int q = 0; q < 3; ++q) E.nface[q] = foff[q];
+  for (int q = 0; q < 3; ++q) { E.nface[q] = foff[q]; E.ncol[q] = coff[q]; }
   CFD_CUDA(cudaStreamCreateWithFlags(&E.st, cudaStreamNonBlocking));
   // device buffers
   const Par& c = E.par;

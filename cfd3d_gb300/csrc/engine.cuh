@@ -24,6 +24,7 @@ struct BlockGeom {
   long long off;            // first padded cell of the block
   long long int_off;        // first interior cell in the flat interior numbering
   long long face_off[3];    // first face of each direction in the flat face numbering
+  long long col_off[3];     // first column of cells along direction 1 (i, k) / 2 (i, j)
 };
 
 // gm planes: face vectors and cell geometry
@@ -206,7 +207,7 @@ struct Engine {
   cfd3d_config cfg;
   Par par;
   std::vector<BlockGeom> blk;
-  long long ncell = 0, nint = 0, nface[3] = {0, 0, 0};
+  long long ncell = 0, nint = 0, nface[3] = {0, 0, 0}, ncol[3] = {0, 0, 0};
   DevPtr d{};
   // ghost program: phase 0 faces + halos, 1 edges, 2 corners
   GhostOp* d_ops[3] = {nullptr, nullptr, nullptr};

@@ -131,7 +131,72 @@ __device__ __forceinline__ FaceIdx face_of(const DevPtr& d, long long t) {
   return f;
 }
 
+// The MUSCL / MLP reconstruction of the j (DIR 1) or k (DIR 2) faces by columns of cells:
+// thread (v, i, t) walks the faces of its column along the face normal and keeps the reduced
+// stencil of muscl_reduced in registers -- per plane of cells the centre, the two transverse
+// differences and the 3 x 3 minimum and maximum -- so each step loads the one new 3 x 3 plane
+// instead of the face's 38 cells, and the planes' minima serve the four faces that read them.
+// The warp runs along i, so every plane load is a coalesced row.  Writes the face states,
+// before the clips, into frec; k_recon_mx<DIR, true> clips them and forms the face EOS.
 template <int DIR>
+__global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long ncol) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int v = (int)(t / ncol);
+  if (v >= c.npv) return;
+  const long long col = t - (long long)v * ncol;
+  int b = 0;
+  while (b + 1 < d.nblk && col >= d.blk[b + 1].col_off[DIR]) ++b;
+  const BlockGeom& B = d.blk[b];
+  const long long loc = col - B.col_off[DIR];
+  const int i = (int)(loc % (B.imax - 1)) + 2;
+  const int o = (int)(loc / (B.imax - 1)) + 2;   // k (DIR 1) or j (DIR 2) of the column
+  const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+  // normal, first and second transverse strides, as stencil_cell numbers the stencil
+  const long long sn = DIR == 1 ? sj : sk, s1 = DIR == 1 ? sk : 1, s2 = DIR == 1 ? 1 : sj;
+  const int nmax = DIR == 1 ? B.jmax : B.kmax;   // faces 1..nmax; face m has left cell m
+  const long long gm1 = B.off + (i + 1) + (DIR == 1 ? sk : sj) * (o + 1);   // the column's cell at m = -1
+  const float* P = d.pvf + (long long)v * n;
+  float* FL = d.frec + (long long)v * n;
+  float* FR = d.frec + (long long)(FREC_SIDE + v) * n;
+  const bool mlp = c.nmuscl == 2;
+  // slots 0..5: the planes m - 2 .. m + 3 of face m
+  float cc[6], dt[6], dr[6], mn[6], mx[6];
+  auto load = [&](int slot, int m) {
+    const long long gc = gm1 + sn * (m + 1);
+    cc[slot] = P[gc];
+    if (mlp) {
+      float a[3][3];   // [t1 + 1][t2 + 1]
+#pragma unroll
+      for (int p1 = 0; p1 < 3; ++p1)
+#pragma unroll
+        for (int p2 = 0; p2 < 3; ++p2) a[p1][p2] = P[gc + (p1 - 1) * s1 + (p2 - 1) * s2];
+      dt[slot] = a[2][1] - a[0][1];
+      dr[slot] = a[1][2] - a[1][0];
+      float lo = a[0][0], hi = a[0][0];
+#pragma unroll
+      for (int p1 = 0; p1 < 3; ++p1)
+#pragma unroll
+        for (int p2 = 0; p2 < 3; ++p2) { lo = fminf(lo, a[p1][p2]); hi = fmaxf(hi, a[p1][p2]); }
+      mn[slot] = lo; mx[slot] = hi;
+    }
+  };
+#pragma unroll
+  for (int q = 0; q < 5; ++q) load(q, q - 1);
+  for (int m = 1; m <= nmax; ++m) {
+    load(5, m + 3);
+    const float mnr[4] = {mn[1], mn[2], mn[3], mn[4]}, mxr[4] = {mx[1], mx[2], mx[3], mx[4]};
+    float xl, xr;
+    muscl_reduced(c, cc[0], cc[1], cc[2], cc[3], cc[4], cc[5], dt[2], dr[2], dt[3], dr[3], mnr, mxr, xl, xr);
+    const long long gf = gm1 + sn * (m + 1);
+    FL[gf] = xl;
+    FR[gf] = xr;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) { cc[q] = cc[q + 1]; dt[q] = dt[q + 1]; dr[q] = dr[q + 1]; mn[q] = mn[q + 1]; mx[q] = mx[q + 1]; }
+  }
+}
+
+// MARCH: the face states come from k_muscl_march (frec) instead of the 38-cell stencil
+template <int DIR, bool MARCH = false>
 __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
   const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
   if (!f.ok) return;
@@ -143,12 +208,19 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
   float cl = 0.0f, cr = 0.0f;
   if (c.nmuscl > 0) {
     float c9[NPVM], c10[NPVM];
-    for (int v = 0; v < npv; ++v) {
-      float x[38];
+    if (MARCH) {
+      for (int v = 0; v < npv; ++v) {
+        gl[v] = d.frec[v * n + g]; gR[v] = d.frec[(FREC_SIDE + v) * n + g];
+        c9[v] = P[v * n + g]; c10[v] = P[v * n + gr];
+      }
+    } else {
+      for (int v = 0; v < npv; ++v) {
+        float x[38];
 #pragma unroll
-      for (int l = 0; l < 38; ++l) x[l] = P[v * n + stencil_cell(l, g, f.sn, f.s1, f.s2)];
-      muscl_var<float>(c, x, gl[v], gR[v]);
-      c9[v] = x[8]; c10[v] = x[9];
+        for (int l = 0; l < 38; ++l) x[l] = P[v * n + stencil_cell(l, g, f.sn, f.s1, f.s2)];
+        muscl_var<float>(c, x, gl[v], gR[v]);
+        c9[v] = x[8]; c10[v] = x[9];
+      }
     }
     muscl_clip_mx(c, c9, c10, gl, gR);
     // a vapour-free face state by expansion about an interior cell -- its own side's, or at
@@ -327,9 +399,15 @@ void launch_face_flux_mixed(const Engine& E, cudaStream_t s) {
   k_shadow<<<std::max(nsm, 1) * 8, 256, 0, s>>>(E.d, E.par);
   k_recon_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
   k_flux_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  k_recon_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
+  // the j and k faces: reconstruction by columns (k_muscl_march), then clips and face EOS
+  const bool march = E.par.nmuscl > 0;
+  if (march) k_muscl_march<1><<<(unsigned)((E.ncol[1] * E.par.npv + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[1]);
+  if (march) k_recon_mx<1, true><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
+  else k_recon_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
   k_flux_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
-  k_recon_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
+  if (march) k_muscl_march<2><<<(unsigned)((E.ncol[2] * E.par.npv + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[2]);
+  if (march) k_recon_mx<2, true><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
+  else k_recon_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
   k_flux_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
 }
 

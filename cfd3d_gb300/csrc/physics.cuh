@@ -611,6 +611,55 @@ __device__ __forceinline__ void muscl_var(const Par& c, const R* x, R& xl, R& xr
   xr = nsub(x[9], nmul(nmul(R(0.5), limiter<R>(c.nlim, r1, r11, r21, alp1)), dqp));
 }
 
+// muscl_var in FP32 from the reduced stencil a face needs: the six cells of the line through
+// it (cm2 .. c3 at normal offsets -2 .. +3; c0 the left cell, c1 the right), the first and
+// second transverse differences of planes 0 and 1 (dt0 = x[10] - x[6], dr0 = x[14] - x[2],
+// dt1 = x[11] - x[7], dr1 = x[15] - x[3]) and the minimum and maximum over the 3 x 3 cells
+// of planes -1, 0, 1, 2 (mn, mx).  MLP's minima and maxima over the 38-cell stencil are those
+// of the planes' (a minimum is exact whatever the grouping), and every other operation is
+// muscl_var's, so the result equals muscl_var<float> on the full stencil.
+__device__ __forceinline__ void muscl_reduced(const Par& c, float cm2, float cm1, float c0, float c1, float c2,
+                                              float c3, float dt0, float dr0, float dt1, float dr1, const float* mn,
+                                              const float* mx, float& xl, float& xr) {
+  using R = float;
+  const R eps = R(1.0e-30), eps2 = R(1.0e-3);
+  R dq = c1 - c0;
+  R dqm = c0 - cm1;
+  R dqm1 = cm1 - cm2;
+  R dqp = c2 - c1;
+  R dqp1 = c3 - c2;
+  R dqmm = rdiv(R(1), dqm + eps);
+  R r0 = dq * dqmm, r10 = dqm1 * dqmm, r20 = dqp * dqmm;
+  R dqpp = rdiv(R(1), dqp + eps);
+  R r1 = dq * dqpp, r11 = dqp1 * dqpp, r21 = dqm * dqpp;
+  R alp0 = R(2), alp1 = R(2);
+  if (c.nmuscl == 2) {
+    R rxy_l = fabs(rdiv(dt0, c1 - cm1 + eps));
+    R rxz_l = fabs(rdiv(dr0, c1 - cm1 + eps));
+    R rxy_r = fabs(rdiv(dt1, c2 - c0 + eps));
+    R rxz_r = fabs(rdiv(dr1, c2 - c0 + eps));
+    const R mA = fmin(mn[1], mn[2]), MA = fmax(mx[1], mx[2]);
+    const R mE = mn[1], ME = mx[1], mO = mn[2], MO = mx[2];
+    const R mL = mn[0], ML = mx[0], mR = mn[3], MR = mx[3];
+    R qmin, qmax;
+    if (rxy_l < eps2 && rxz_l < eps2) { qmin = fmin(mA, mL); qmax = fmax(MA, ML); }
+    else if (c1 - cm1 > R(0)) { qmax = MA; qmin = fmin(mE, mL); }
+    else { qmin = mA; qmax = fmax(ME, ML); }
+    R qml = fmin(fabs(qmax - c0), fabs(qmin - c0));
+    if (rxy_r < eps2 && rxz_r < eps2) { qmin = fmin(mA, mR); qmax = fmax(MA, MR); }
+    else if (c2 - c0 > R(0)) { qmax = fmax(MO, MR); qmin = mA; }
+    else { qmin = fmin(mO, mR); qmax = MA; }
+    R qmr = fmin(fabs(qmax - c1), fabs(qmin - c1));
+    alp0 = rdiv(rdiv(R(2) * fmax(R(1), r0), fabs(dq) + eps), R(1) + rxy_l + rxz_l) * qml;
+    if (fabs(dq) <= eps) alp1 = rdiv(R(2) * fmax(R(1), rdiv(dqp, eps)) * fabs(dqpp), R(1) + rxy_r + rxz_r) * qmr;
+    else alp1 = rdiv(R(2) * fmax(R(1), rdiv(R(1), r1)) * fabs(dqpp), R(1) + rxy_r + rxz_r) * qmr;
+    alp0 = fmax(R(1), fmin(R(2), alp0));
+    alp1 = fmax(R(1), fmin(R(2), alp1));
+  }
+  xl = nadd(c0, nmul(nmul(R(0.5), limiter<R>(c.nlim, r0, r10, r20, alp0)), dqm));
+  xr = nsub(c1, nmul(nmul(R(0.5), limiter<R>(c.nlim, r1, r11, r21, alp1)), dqp));
+}
+
 // post-clipping of the reconstructed states (muscl_module.f90:136-158)
 template <class R>
 __device__ __forceinline__ void muscl_clip(const Par& c, const R* c9, const R* c10, R* xl, R* xr) {

@@ -67,10 +67,13 @@ def test_rotating_frame_totalpressure_inlet(oracle):
     _parity(oracle, make("sst", 3, {"imin": abi.BC_TOTALPRESSURE_IN, "jmin": abi.BC_WALL_COUNTERROTATING}))
 
 
+@pytest.mark.parametrize("base", ["plain", "sst"])
 @pytest.mark.parametrize("timemethod", [1, 2])
-def test_rotating_frame_explicit(oracle, timemethod):
-    """the explicit schemes' diagonal solve takes the rothalpy too"""
-    _parity(oracle, make("cavitating", 3, WALL_INLET, timemethod=timemethod))
+def test_rotating_frame_explicit(oracle, timemethod, base):
+    """the explicit schemes' diagonal solve takes the rothalpy too.  (On the cavitating
+    start with the reflecting mass-flow inlet, RK3 reaches NaN at its third iteration in
+    the oracle as on the GPU, so the explicit cases are the Euler and SST ones.)"""
+    _parity(oracle, make(base, 3, WALL_INLET, timemethod=timemethod))
 
 
 def test_rotation_changes_the_residual_and_is_refused_where_not_built():
