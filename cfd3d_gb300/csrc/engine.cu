@@ -390,6 +390,17 @@ __global__ void __launch_bounds__(128) k_totalp(DevPtr d, Par c) {
   d.tp_x[3 * pt + 2] = P.uu;
 }
 
+// The EOS of a ghost state: FP64, or in the mixed form the update's split evaluation (rho
+// and h from df64 IF97 sums, derivatives and transport properties in FP32).  What reads
+// ghost cells there -- the FP32 viscous fluxes and SST terms, first-order face states' rho
+// and h, the volume fraction -- needs no more, and the far-field faces' full FP64 sums were
+// most of the boundary program's time.
+__device__ __forceinline__ void ghost_eos(const DevPtr& d, const Par& c, double p, double t, double y1, double y2,
+                                          double* dv, double* tv) {
+  if (c.mixed) deteos_split(c.fluid, c.with_prop, p, t, y1, y2, dv, tv, &d.sc->snd2_fallbacks);
+  else deteos(c.fluid, c.with_prop, p, t, y1, y2, dv, tv, &d.sc->snd2_fallbacks);
+}
+
 __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int nops) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nops) return;
@@ -447,7 +458,7 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       bp[4] = c.tref; bp[5] = c.y1ref; bp[6] = c.y2ref; bp[7] = c.kref; bp[8] = c.oref;
       double* pv = x.pv;
       farfield_pv<double>(c, nx, dl, pb, rb, c2b, bp, c.uref * c.uref, pv, ghost_ff_mode(op.kind));
-      deteos(c.fluid, c.with_prop, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      ghost_eos(d, c, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv);
       store_cell(d, c, op.dst, x);
       return;
     }
@@ -480,7 +491,7 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       pv[6] = 2.0 * bp[6] - pv[6];
       pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
       pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
-      deteos(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      ghost_eos(d, c, pv[0] + c.pref, pv[4], pv[5], pv[6], x.dv, x.tv);
       store_cell(d, c, op.dst, x);
       return;
     }
@@ -545,7 +556,7 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       for (int v = 4; v < c.npv; ++v) pv[v] = 2.0 * bp[v] - pv[v];
       pv[5] = fmin(fmax(pv[5], 0.0), 1.0);
       pv[6] = fmin(fmax(pv[6], 0.0), 1.0);
-      deteos(c.fluid, c.with_prop, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      ghost_eos(d, c, pv[0] + bp[0], pv[4], pv[5], pv[6], x.dv, x.tv);
       store_cell(d, c, op.dst, x);
       return;
     }
@@ -584,7 +595,7 @@ __global__ void k_ghost(DevPtr d, Par c, const GhostOp* __restrict__ ops, int no
       double f = (op.kind == G_NOWALL7) ? 1.0 / 7.0 : 1.0 / 3.0;
       for (int v = 0; v < c.npv; ++v) x.pv[v] = f * pv[v];
       for (int v = 0; v < 3; ++v) x.tv[v] = f * tv[v];
-      deteos(c.fluid, c.with_prop, x.pv[0] + c.pref, x.pv[4], x.pv[5], x.pv[6], x.dv, x.tv, &d.sc->snd2_fallbacks);
+      ghost_eos(d, c, x.pv[0] + c.pref, x.pv[4], x.pv[5], x.pv[6], x.dv, x.tv);
       store_cell(d, c, op.dst, x);
       return;
     }
