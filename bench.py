@@ -63,19 +63,24 @@ def algorithmic_bytes(cfg):
 
 
 def rhs_bytes(cfg, mixed):
-    """Algorithmic bytes per cell of the residual kernel k_rhs (each datum once per cell):
-    reads -- the cell's + face fluxes (inviscid and viscous), pv (and the FP32 shadow of
-    the SST gradients), dv, tv, its + face vectors, volume and wall distance (and their FP32
-    copy), the BDF history, dt; writes -- residual, the sweep record (66 FP64 values, and 34
-    FP32 in the mixed form), icav, itt, the omega bound, rcav."""
+    """Algorithmic bytes per cell of the residual kernel k_rhs (each datum once per cell).
+    Reads: the cell's + face fluxes (inviscid and viscous), pv, dv, tv, its + face vectors,
+    volume and wall distance, the BDF history, dt; the mixed form reads the fluxes in FP32
+    and adds the free-stream closure, the FP32 shadow of the SST gradients and the FP32
+    metric copy.  Writes: the residual, icav, itt, the omega bound, rcav, and the LU-SGS
+    record -- 66 FP64 values in the FP64 form; in the mixed form the 75-value FP32 tile
+    record and the own part x0 of dq in FP64."""
     from cfd3d_gb300.abi import sizes
     npv, ntv, nqq, ngrd = sizes(cfg)
     vis = cfg.get("iturb", 0) != -3
     fw = 4 if mixed else 8
     rd = 3 * (2 if vis else 1) * npv * fw + 8 * npv + 8 * 18 + 8 * ntv + 8 * (9 + 2) + 8 * nqq * npv + 8
+    wr = 8 * npv + 8 * (4 + 4 + 1 + 2)
     if mixed:
-        rd += 4 * 5 + 4 * (9 + 2)
-    wr = 8 * npv + 8 * 66 + (4 * 34 if mixed else 0) + 8 * (4 + 4 + 1 + 2)
+        rd += 8 * npv + 4 * 5 + 4 * (9 + 2)
+        wr += 4 * 75 + 8 * npv
+    else:
+        wr += 8 * 66
     return rd + wr
 
 

@@ -251,8 +251,9 @@ def adjoint(scale=1, seed=3):
 def large(scale=1, seed=4, nt_phy=20, ntmax=30):
     """384x192x192 stretched (wall spacing 1e-5 L, ratio 1.1) SST cavitating block with
     BDF2 dual time stepping; Re = 1e6 via L = 1 m.  Steady-form preconditioning (prec = 1):
-    from this synthetic start the unsteady form (prec = 2, str = L / pi / dt_phy) diverges
-    within ten pseudo-iterations in both the CPU restatement and the GPU engine."""
+    the unsteady form (prec = 2) floors the preconditioning speed at str = L / pi / dt_phy =
+    477 m/s here, and from this synthetic start it diverges at CFL >= 0.5 (stable at CFL 0.1
+    and below, or with dt_phy ten times larger), in the CPU restatement as in the engine."""
     ni, nj, nk = 384 // scale, 192 // scale, 192 // scale
     xyz = box_nodes(ni, nj, nk, 2.0, 1.0, 1.0, shear=0.0, seed=seed, ystretch=(1e-5 * scale, 1.1))
     bc = face_patches(ni + 1, nj + 1, nk + 1, {"imin": BC_FARFIELD, "imax": BC_FARFIELD, "jmin": BC_WALL,

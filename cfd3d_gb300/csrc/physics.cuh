@@ -373,6 +373,50 @@ __device__ __forceinline__ void mixture(const Phase<T>& l, const Phase<T>& v, co
   dv[14] = v.drdp; dv[15] = v.drdt; dv[16] = l.drdp; dv[17] = l.drdt;
 }
 
+// mixture() for the mixed form's update and ghost states: the mixture and phase densities and
+// the enthalpy in FP64 -- they reach the residual through the dual-time source, the
+// first-order face states and the face-state expansions -- and the derivatives, the
+// enthalpy differences and the sound speed in FP32 from the phases' FP32 derivatives (lf,
+// vf, gf): they shape the implicit operator, the preconditioning speed and the FP32 flux
+// and viscous terms only.  Same formulas and order as mixture().
+__device__ __forceinline__ void mixture_split(const Phase<double>& l, const Phase<double>& v, const Phase<double>& g,
+                                              const Phase<float>& lf, const Phase<float>& vf, const Phase<float>& gf,
+                                              double y1, double y2, double* dv, unsigned long long* fallbacks,
+                                              double* irh) {
+  dv[2] = l.rho; dv[3] = v.rho; dv[4] = g.rho;
+  const double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
+  irh[0] = irhol; irh[1] = irhov; irh[2] = irhog;
+  const double yl = 1.0 - y1 - y2;
+  const double irho = yl * irhol + y1 * irhov + y2 * irhog;
+  dv[0] = 1.0 / irho;
+  dv[1] = yl * l.h + y1 * v.h + y2 * g.h;
+  const float r0 = (float)dv[0], fyl = (float)yl, fy1 = (float)y1, fy2 = (float)y2;
+  const float fil = (float)irhol, fiv = (float)irhov, fig = (float)irhog;
+  const float r2 = r0 * r0;
+  const float il2 = fil * fil, iv2 = fiv * fiv, ig2 = fig * fig;
+  const float d6 = r2 * (fyl * il2 * lf.drdp + fy1 * iv2 * vf.drdp + fy2 * ig2 * gf.drdp);
+  const float d7 = r2 * (fyl * il2 * lf.drdt + fy1 * iv2 * vf.drdt + fy2 * ig2 * gf.drdt);
+  const float d10 = fyl * lf.dhdp + fy1 * vf.dhdp + fy2 * gf.dhdp;
+  const float d11 = fyl * lf.dhdt + fy1 * vf.dhdt + fy2 * gf.dhdt;
+  dv[6] = d6; dv[7] = d7;
+  dv[8] = r2 * (fil - fiv);
+  dv[9] = r2 * (fil - fig);
+  dv[10] = d10; dv[11] = d11;
+  dv[12] = (float)(v.h - l.h);
+  dv[13] = (float)(g.h - l.h);
+  float c2 = r0 * d11 / (r0 * d6 * d11 + d7 * (1.0f - r0 * d10));
+  if (c2 <= 0.0f) {  // the reference's "alternative calculation for snd2"
+    if (fallbacks) atomicAdd(fallbacks, 1ull);
+    const float rl = (float)dv[2], rv = (float)dv[3], rg = (float)dv[4];
+    const float ic2l = (rl * lf.drdp * lf.dhdt + lf.drdt * (1.0f - rl * lf.dhdp)) / (rl * lf.dhdt);
+    const float ic2v = (rv * vf.drdp * vf.dhdt + vf.drdt * (1.0f - rv * vf.dhdp)) / (rv * vf.dhdt);
+    const float ic2g = (rg * gf.drdp * gf.dhdt + gf.drdt * (1.0f - rg * gf.dhdp)) / (rg * gf.dhdt);
+    c2 = 1.0f / (r2 * (fyl * ic2l * il2 + fy1 * ic2v * iv2 + fy2 * ic2g * ig2));
+  }
+  dv[5] = c2;
+  dv[14] = vf.drdp; dv[15] = vf.drdt; dv[16] = lf.drdp; dv[17] = lf.drdt;
+}
+
 // Phase properties and the mixture EOS in a generic scalar (the adjoint's dual numbers);
 // the metastable branch is chosen on the values, as in the FP64 form.
 template <class T>
@@ -488,22 +532,23 @@ __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, doubl
 __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p, double t, double y1, double y2,
                                              double* dv, double* tv, unsigned long long* fb) {
   Phase<double> l, v, g;
+  Phase<float> lf, vf, gf;
   const float pf = (float)p, tf = (float)t;
   if (fluid == 1) {
     stiffened(p, t, l);
     ideal_gas(p, t, v);
+    lf.drdp = (float)l.drdp; lf.drdt = (float)l.drdt; lf.dhdp = (float)l.dhdp; lf.dhdt = (float)l.dhdt;
+    vf.drdp = (float)v.drdp; vf.drdt = (float)v.drdt; vf.dhdp = (float)v.dhdp; vf.dhdt = (float)v.dhdt;
   } else {
     const bool meta = p > h2o_pww(t);
     iapws_pair_df64<false>(p, t, meta, l, v);
-    Phase<float> lf, vf;
     iapws_l<float, true>(pf, tf, lf);
     iapws_v_meta<float, true>(pf, tf, meta, vf);
-    l.drdp = lf.drdp; l.drdt = lf.drdt; l.dhdp = lf.dhdp; l.dhdt = lf.dhdt;
-    v.drdp = vf.drdp; v.drdt = vf.drdt; v.dhdp = vf.dhdp; v.dhdt = vf.dhdt;
   }
   ideal_gas(p, t, g);
+  ideal_gas<float>(pf, tf, gf);
   double irh[3];
-  mixture(l, v, g, y1, y2, dv, fb, irh);
+  mixture_split(l, v, g, lf, vf, gf, y1, y2, dv, fb, irh);
   if (with_prop) {
     float lv, lc, vv, vc;
     if (fluid == 1) {
