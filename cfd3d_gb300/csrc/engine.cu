@@ -67,6 +67,34 @@ __global__ void k_eos_points(int fluid, int with_prop, long long n, const double
 
 // ------------------------------------------------------------------ initial state
 // set_others (src/initial_module.f90:707-771) on the uploaded interior pv
+// One block's uploaded primitives (AoS staging a, every padded cell) into pv, for the cells
+// whose values differ from the device's: dv and tv(1:2) of such an interior cell follow by
+// the update's EOS, as k_init(fresh = 0) forms them, and pv_changed records the change for
+// the eddy viscosity.  A cell whose uploaded pv equals the device's bit for bit keeps the dv
+// and tv that are already the EOS of that pv.
+template <bool MX>
+__global__ void k_take_pv(const double* __restrict__ a, BlockGeom B, DevPtr d, Par c) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= (long long)B.ni * B.nj * B.nk) return;
+  const long long n = d.ncell, g = B.off + q;
+  double pv[NPVM];
+  bool same = true;
+  for (int v = 0; v < c.npv; ++v) {
+    pv[v] = a[q * c.npv + v];
+    same = same && (__double_as_longlong(pv[v]) == __double_as_longlong(d.pv[v * n + g]));
+  }
+  if (same) return;
+  for (int v = 0; v < c.npv; ++v) d.pv[v * n + g] = pv[v];
+  d.sc->pv_changed = 1;
+  const int i = (int)(q % B.ni) - 1, j = (int)((q / B.ni) % B.nj) - 1, k = (int)(q / ((long long)B.ni * B.nj)) - 1;
+  if (i < 2 || j < 2 || k < 2 || i > B.imax || j > B.jmax || k > B.kmax) return;
+  double dv[NDV], tv[3] = {0.0, 0.0, 0.0};
+  if (MX) deteos_split(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
+  else deteos<false>(c.fluid, c.with_prop, pv[0] + c.pref, pv[4], pv[5], pv[6], dv, tv, &d.sc->snd2_fallbacks);
+  for (int v = 0; v < NDV; ++v) d.dv[v * n + g] = dv[v];
+  for (int v = 0; v < c.ntv && v < 2; ++v) d.tv[v * n + g] = tv[v];
+}
+
 template <bool MX>
 // fresh = 0 (cfd3d_upload_primitives): dv and tv(1:2) only; the eddy viscosity follows
 // from k_eddy and the history and rates are the caller's
@@ -1614,7 +1642,10 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
 
 // MX: FP32, with the velocity gradients formed from u - U (exact differences)
 template <bool MX>
-__global__ void k_eddy(DevPtr d, Par c, long long t0, long long t1) {
+// if_changed: only when an upload changed some pv (the eddy viscosity is a function of the
+// cell's and its neighbours' pv)
+__global__ void k_eddy(DevPtr d, Par c, long long t0, long long t1, int if_changed = 0) {
+  if (if_changed && !*(volatile int*)&d.sc->pv_changed) return;
   long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= t1) return;
   int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
@@ -2613,6 +2644,7 @@ int upload_primitives_all(cfd3d_handle* h, const double* const* pv, const double
   if (!rc) rc = ensure_copy_stream(h);
   if (!rc) rc = block_events(h);
   if (rc) return rc;
+  CFD_CUDA(cudaMemsetAsync(&E.d.sc->pv_changed, 0, sizeof(int), E.st));
   CFD_CUDA(cudaEventRecord(h->ev[5], E.st));          // staging no longer read by earlier work
   CFD_CUDA(cudaStreamWaitEvent(h->cp, h->ev[5], 0));
   std::vector<double*> spv(nb), sqq(nb, nullptr);
@@ -2634,14 +2666,13 @@ int upload_primitives_all(cfd3d_handle* h, const double* const* pv, const double
     const BlockGeom& B = E.blk[b];
     const long long ncb = (long long)B.ni * B.nj * B.nk, nint = (long long)(B.imax - 1) * (B.jmax - 1) * (B.kmax - 1);
     CFD_CUDA(cudaStreamWaitEvent(E.st, h->bev[b], 0));
-    k_aos_to_soa<<<nblk_of(ncb, 256), 256, 0, E.st>>>(spv[b], c.npv, ncb, E.d.pv, E.ncell, B.off);
+    if (c.mixed) k_take_pv<true><<<nblk_of(ncb, 128), 128, 0, E.st>>>(spv[b], B, E.d, c);
+    else k_take_pv<false><<<nblk_of(ncb, 128), 128, 0, E.st>>>(spv[b], B, E.d, c);
     if (sqq[b]) k_interior_io<<<nblk_of(nint, 256), 256, 0, E.st>>>(sqq[b], 2 * c.npv, B, E.d.qq, E.ncell, 1);
-    if (c.mixed) k_init<true><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, b, 0);
-    else k_init<false><<<nblk_of(nint, 128), 128, 0, E.st>>>(E.d, c, b, 0);
   }
   if (c.iturb >= -1 && c.ntv >= 3) {
-    if (c.mixed) k_eddy<true><<<nblk_of(E.nint, 128), 128, 0, E.st>>>(E.d, c, 0, E.nint);
-    else k_eddy<false><<<nblk_of(E.nint, 128), 128, 0, E.st>>>(E.d, c, 0, E.nint);
+    if (c.mixed) k_eddy<true><<<nblk_of(E.nint, 128), 128, 0, E.st>>>(E.d, c, 0, E.nint, 1);
+    else k_eddy<false><<<nblk_of(E.nint, 128), 128, 0, E.st>>>(E.d, c, 0, E.nint, 1);
   }
   CFD_CUDA(cudaStreamSynchronize(E.st));
   CFD_CUDA(cudaGetLastError());
@@ -2945,9 +2976,9 @@ static int finish_iteration(cfd3d_handle* h, int nt_phy, double timeprev, double
 // the time inputs of the boundary program (heat-flux histories) for the next launches
 static int set_bc_time(Engine& E, int nt_phy, double timeprev) {
   if (!E.d_hft && !E.d_grav) return CFD3D_OK;
-  struct { double tp; int nt, pad; } v{timeprev, nt_phy, 0};
-  static_assert(sizeof(v) == 16, "timeprev, nt_phy, pad_ of Scalars");
-  CFD_CUDA(cudaMemcpyAsync((char*)E.d.sc + offsetof(Scalars, timeprev), &v, sizeof(v), cudaMemcpyHostToDevice, E.st));
+  struct { double tp; int nt; } v{timeprev, nt_phy};
+  static_assert(offsetof(Scalars, nt_phy) == offsetof(Scalars, timeprev) + 8, "timeprev, nt_phy of Scalars");
+  CFD_CUDA(cudaMemcpyAsync((char*)E.d.sc + offsetof(Scalars, timeprev), &v, 12, cudaMemcpyHostToDevice, E.st));
   return CFD3D_OK;
 }
 

@@ -70,7 +70,7 @@ struct Scalars {
   // current cfd3d_iterate call, written by the host before each launch
   double timeprev;
   int nt_phy;
-  int pad_;
+  int pv_changed;   // cfd3d_upload_primitives_all: some uploaded pv differed from the device's
 };
 
 // the base state of a face state's expansion (k_shadow): d(1/rho_l)/dp, d(1/rho_l)/dT,

@@ -174,8 +174,11 @@ int  cfd3d_upload_primitives(cfd3d_handle *h, int block, const double *pv, const
  * takes them, and pv / dv / tv of every block as cfd3d_download_state gives them (NULL arrays
  * or entries are skipped).  The copies of all blocks leave back to back at the link's rate
  * and each block's layout kernel overlaps the copies of the blocks after it; the results
- * equal the per-block calls'.  The handle's staging region grows to the case's whole state.
- * No counterpart in the reference (its state never leaves the host). */
+ * equal the per-block calls'.  The upload runs the EOS only for the cells whose uploaded pv
+ * differs from the device's (an unchanged cell's dv and tv already are the EOS of its pv),
+ * and the eddy viscosity only when some pv changed.  The handle's staging region grows to
+ * the case's whole state.  No counterpart in the reference (its state never leaves the
+ * host). */
 int  cfd3d_upload_primitives_all(cfd3d_handle *h, const double *const *pv, const double *const *qq);
 int  cfd3d_download_state_all(cfd3d_handle *h, double *const *pv, double *const *dv, double *const *tv);
 

@@ -130,3 +130,41 @@ def test_whole_case_transfers_equal_the_per_block_calls():
         ref = eb.download(b)
         for k in ("pv", "dv", "tv"):
             assert np.array_equal(outs[b][k], ref[k]), (b, k)
+
+
+def test_whole_case_upload_takes_only_changed_cells():
+    """cfd3d_upload_primitives_all of the engine's own state changes nothing (the cells whose
+    pv is unchanged keep their dv and tv, which are the EOS of that pv); a cell whose pv the
+    host changed gets the update's EOS, as the per-block call gives it; the next iteration
+    matches an engine that took the same state through the per-block calls"""
+    c = _case()
+    c["cfg"]["fix_cav_clamp"] = 1
+    e1 = native.Engine(c, precision=abi.MIXED)
+    e1.initialize(c["pv0"])
+    for it in range(2):
+        e1.iterate(1, it + 1, 0.0)
+    st = [e1.download(b) for b in range(2)]
+    e1.upload_primitives_all([np.ascontiguousarray(s["pv"]) for s in st], [np.ascontiguousarray(s["qq"]) for s in st])
+    for b in range(2):
+        after = e1.download(b)
+        for k in ("pv", "dv", "tv", "qq"):
+            assert np.array_equal(after[k], st[b][k]), (b, k)
+    # one interior cell of block 1 changed on the host
+    pv = [np.ascontiguousarray(s["pv"]).copy() for s in st]
+    pv[1][5, 5, 5, 0] += 250.0
+    pv[1][5, 5, 5, 4] += 0.01
+    e1.upload_primitives_all(pv, [np.ascontiguousarray(s["qq"]) for s in st])
+    e2 = native.Engine(c, precision=abi.MIXED)
+    e2.initialize(c["pv0"])
+    for b in range(2):
+        e2.upload_primitives(b, pv[b], st[b]["qq"])
+    for b in range(2):
+        a, r = e1.download(b), e2.download(b)
+        for k in ("pv", "dv", "tv"):
+            assert np.array_equal(a[k][3:-3, 3:-3, 3:-3], r[k][3:-3, 3:-3, 3:-3]), (b, k)
+    e1.iterate(1, 3, 0.0)
+    e2.iterate(1, 3, 0.0)
+    for b in range(2):
+        a, r = e1.download(b), e2.download(b)
+        for k in ("pv", "dv", "tv"):
+            assert np.array_equal(a[k][3:-3, 3:-3, 3:-3], r[k][3:-3, 3:-3, 3:-3]), (b, k)
