@@ -50,7 +50,7 @@ UNIT = "Mcell-iter/s"
 # DRAM bytes per cell of one k_rhs launch, dram__bytes_read.sum + dram__bytes_write.sum
 # of an ncu capture of the mixed form on the large case at 1/2 resolution (1769472 cells),
 # divided by the cells; the capture grows in proportion to the cells
-RHS_TRAFFIC_PER_CELL = (2.300200e9 + 3.388917e9) / 1769472
+RHS_TRAFFIC_PER_CELL = (3.174136e9 + 1.794411e9) / 1769472
 
 
 def algorithmic_bytes(cfg):
