@@ -373,25 +373,25 @@ __device__ __forceinline__ void mixture(const Phase<T>& l, const Phase<T>& v, co
   dv[14] = v.drdp; dv[15] = v.drdt; dv[16] = l.drdp; dv[17] = l.drdt;
 }
 
-// mixture() for the mixed form's update and ghost states: the mixture and phase densities and
-// the enthalpy in FP64 -- they reach the residual through the dual-time source, the
-// first-order face states and the face-state expansions -- and the derivatives, the
-// enthalpy differences and the sound speed in FP32 from the phases' FP32 derivatives (lf,
-// vf, gf): they shape the implicit operator, the preconditioning speed and the FP32 flux
-// and viscous terms only.  Same formulas and order as mixture().
-__device__ __forceinline__ void mixture_split(const Phase<double>& l, const Phase<double>& v, const Phase<double>& g,
+// mixture() for the mixed form's update and ghost states, from the phases' specific
+// volumes il, iv, ig and enthalpies hl, hv, hg (FP64 values of df64 sums: no FP64 division
+// but the mixture density's) and their FP32 derivatives lf, vf, gf.  The mixture density
+// and enthalpy are FP64 -- they reach the residual through the dual-time source, the
+// first-order face states and the face-state expansions; the phase densities, the
+// derivatives, the enthalpy differences and the sound speed are FP32 -- they shape the
+// implicit operator, the preconditioning speed and the FP32 flux and viscous terms only.
+// Same formulas and order as mixture().
+__device__ __forceinline__ void mixture_split(double il, double hl, double iv, double hv, double ig, double hg,
                                               const Phase<float>& lf, const Phase<float>& vf, const Phase<float>& gf,
-                                              double y1, double y2, double* dv, unsigned long long* fallbacks,
-                                              double* irh) {
-  dv[2] = l.rho; dv[3] = v.rho; dv[4] = g.rho;
-  const double irhol = 1.0 / dv[2], irhov = 1.0 / dv[3], irhog = 1.0 / dv[4];
-  irh[0] = irhol; irh[1] = irhov; irh[2] = irhog;
+                                              double y1, double y2, double* dv, unsigned long long* fallbacks) {
   const double yl = 1.0 - y1 - y2;
-  const double irho = yl * irhol + y1 * irhov + y2 * irhog;
+  const double irho = yl * il + y1 * iv + y2 * ig;
   dv[0] = 1.0 / irho;
-  dv[1] = yl * l.h + y1 * v.h + y2 * g.h;
+  dv[1] = yl * hl + y1 * hv + y2 * hg;
+  const float fil = (float)il, fiv = (float)iv, fig = (float)ig;
+  const float rl = 1.0f / fil, rv = 1.0f / fiv, rg = 1.0f / fig;
+  dv[2] = rl; dv[3] = rv; dv[4] = rg;
   const float r0 = (float)dv[0], fyl = (float)yl, fy1 = (float)y1, fy2 = (float)y2;
-  const float fil = (float)irhol, fiv = (float)irhov, fig = (float)irhog;
   const float r2 = r0 * r0;
   const float il2 = fil * fil, iv2 = fiv * fiv, ig2 = fig * fig;
   const float d6 = r2 * (fyl * il2 * lf.drdp + fy1 * iv2 * vf.drdp + fy2 * ig2 * gf.drdp);
@@ -402,12 +402,11 @@ __device__ __forceinline__ void mixture_split(const Phase<double>& l, const Phas
   dv[8] = r2 * (fil - fiv);
   dv[9] = r2 * (fil - fig);
   dv[10] = d10; dv[11] = d11;
-  dv[12] = (float)(v.h - l.h);
-  dv[13] = (float)(g.h - l.h);
+  dv[12] = (float)(hv - hl);
+  dv[13] = (float)(hg - hl);
   float c2 = r0 * d11 / (r0 * d6 * d11 + d7 * (1.0f - r0 * d10));
   if (c2 <= 0.0f) {  // the reference's "alternative calculation for snd2"
     if (fallbacks) atomicAdd(fallbacks, 1ull);
-    const float rl = (float)dv[2], rv = (float)dv[3], rg = (float)dv[4];
     const float ic2l = (rl * lf.drdp * lf.dhdt + lf.drdt * (1.0f - rl * lf.dhdp)) / (rl * lf.dhdt);
     const float ic2v = (rv * vf.drdp * vf.dhdt + vf.drdt * (1.0f - rv * vf.dhdp)) / (rv * vf.dhdt);
     const float ic2g = (rg * gf.drdp * gf.dhdt + gf.drdt * (1.0f - rg * gf.dhdp)) / (rg * gf.dhdt);
@@ -531,38 +530,43 @@ __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, doubl
 // operator, the preconditioning speed and the FP32 viscous fluxes); mixture in FP64.
 __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p, double t, double y1, double y2,
                                              double* dv, double* tv, unsigned long long* fb) {
-  Phase<double> l, v, g;
+  double il, hl, iv, hv;
   Phase<float> lf, vf, gf;
   const float pf = (float)p, tf = (float)t;
   if (fluid == 1) {
+    Phase<double> l, v;
     stiffened(p, t, l);
     ideal_gas(p, t, v);
+    il = 1.0 / l.rho; hl = l.h; iv = 1.0 / v.rho; hv = v.h;
     lf.drdp = (float)l.drdp; lf.drdt = (float)l.drdt; lf.dhdp = (float)l.dhdp; lf.dhdt = (float)l.dhdt;
     vf.drdp = (float)v.drdp; vf.drdt = (float)v.drdt; vf.dhdp = (float)v.dhdp; vf.dhdt = (float)v.dhdt;
   } else {
     const bool meta = p > h2o_pww(t);
-    iapws_pair_df64<false>(p, t, meta, l, v);
+    iapws_inv_df64<true>(p, t, meta, &il, &hl, &iv, &hv);
     iapws_l<float, true>(pf, tf, lf);
     iapws_v_meta<float, true>(pf, tf, meta, vf);
   }
-  ideal_gas(p, t, g);
   ideal_gas<float>(pf, tf, gf);
-  double irh[3];
-  mixture_split(l, v, g, lf, vf, gf, y1, y2, dv, fb, irh);
+  // the gas: 1/rho = T / (p r1) in df64, h = cp T
+  const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
+  const double hg = 1004.64 * t;
+  mixture_split(il, hl, iv, hv, ig, hg, lf, vf, gf, y1, y2, dv, fb);
   if (with_prop) {
+    // the transport properties in FP32: they feed the FP32 viscous fluxes, the SST terms
+    // and the operator's viscous eigenvalue
     float lv, lc, vv, vc;
     if (fluid == 1) {
       lv = stiffened_vis<float>(tf); lc = 4598.0f * lv;
       vv = ideal_vis<float>(tf); vc = 1395.333333f * vv;
     } else {
-      iapws_transport<float>(tf, (float)l.rho, lv, lc);
-      iapws_transport<float>(tf, (float)v.rho, vv, vc);
+      iapws_transport<float>(tf, (float)dv[2], lv, lc);
+      iapws_transport<float>(tf, (float)dv[3], vv, vc);
     }
     float gv = ideal_vis<float>(tf), gc = 1395.333333f * gv;
-    double yl = 1.0 - y1 - y2;
-    const double irhol = irh[0], irhov = irh[1], irhog = irh[2];
-    tv[0] = dv[0] * ((double)lv * yl * irhol + (double)vv * y1 * irhov + (double)gv * y2 * irhog);
-    tv[1] = dv[0] * ((double)lc * yl * irhol + (double)vc * y1 * irhov + (double)gc * y2 * irhog);
+    const float r0 = (float)dv[0], fyl = (float)(1.0 - y1 - y2), fy1 = (float)y1, fy2 = (float)y2;
+    const float fil = (float)il, fiv = (float)iv, fig = (float)ig;
+    tv[0] = r0 * (lv * fyl * fil + vv * fy1 * fiv + gv * fy2 * fig);
+    tv[1] = r0 * (lc * fyl * fil + vc * fy1 * fiv + gc * fy2 * fig);
   }
 }
 
