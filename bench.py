@@ -51,6 +51,9 @@ UNIT = "Mcell-iter/s"
 # of an ncu capture of the mixed form on the large case at 1/2 resolution (1769472 cells),
 # divided by the cells; the capture grows in proportion to the cells
 RHS_TRAFFIC_PER_CELL = (3.174136e9 + 1.794411e9) / 1769472
+# the same for one whole pseudo-iteration of that workload: dram read + write summed over
+# the 19 launches of its third iteration, divided by the cells
+ITER_TRAFFIC_PER_CELL = (11.845088e9 + 5.483316e9) / 1769472
 
 
 def algorithmic_bytes(cfg):
@@ -444,13 +447,14 @@ def main():
                    "launch_shapes": None if shapes is None else {"face_threads": shapes[0], "rhs_threads": shapes[1],
                                                                  "sweep_ctas_per_sm": shapes[2]}},
         "roofline": {"bound": "hbm", "achieved": achieved_it, "peak": peak, "unit": "GB/s", "frac": achieved_it / peak,
-                     "peak_kind": peak_kind, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "traffic": ITER_TRAFFIC_PER_CELL * ncell if (prec == abi.MIXED and args.case == "large") else None,
                      "scope": "whole pseudo-iteration: algorithmic bytes per cell-iteration x cells / ms_per_step",
                      "bytes_per_cell": bpc, "dominant_stage": dominant,
                      "dominant_share": prof[dominant] / total_stage, "stage_ms": prof,
                      "kernel": {"name": "k_rhs (residual, sources, sweep records)", "achieved": achieved_rhs,
                                 "frac": achieved_rhs / peak, "kernel_ms": rhs_ms, "algorithmic_bytes_per_cell": rb,
-                                "traffic": RHS_TRAFFIC_PER_CELL * ncell if prec == abi.MIXED else None},
+                                "traffic": RHS_TRAFFIC_PER_CELL * ncell if (prec == abi.MIXED and args.case == "large") else None},
                      "fp64": {"peak_tflops": fp64_tflops,
                               "peak_kind": "measured: cfd3d_fp64_peak, independent DFMA chains, 1 s"}},
         "e2e": e2e,
