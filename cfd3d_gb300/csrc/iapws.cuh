@@ -159,6 +159,16 @@ __device__ __forceinline__ T h2o_pww(T t) {
   return T(1.0e6) * (q2 * q2);
 }
 
+// p > p_sat(T) -- the metastable-branch test of the vapour phase -- decided as the FP64
+// comparison decides it: the FP32 saturation pressure first (its relative error stays
+// below 7e-6 over 273-647 K), the FP64 one only where p lies within 1e-4 of it.  (An FP64
+// saturation pressure is a division, a square root and a quotient on the FP64 pipe.)
+__device__ __forceinline__ bool above_psat(double p, double t) {
+  const float psf = h2o_pww<float>((float)t), pf = (float)p;
+  if (fabsf(pf - psf) > 1.0e-4f * psf) return pf > psf;
+  return p > h2o_pww<double>(t);
+}
+
 template <class T>
 __device__ __forceinline__ T h2o_tww(T p) {
   T beta = pow(p / T(1.0e6), T(0.25));

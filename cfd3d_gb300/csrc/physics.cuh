@@ -331,7 +331,7 @@ __device__ __forceinline__ void phases(int fluid, double p, double t, Phase<doub
     v.rho = 1.0; v.h = 0.0; v.drdp = 0.0; v.drdt = 0.0; v.dhdp = 0.0; v.dhdt = 1.0;
     return;
   }
-  const bool meta = p > h2o_pww(t);
+  const bool meta = above_psat(p, t);
   if constexpr (MX) {
     iapws_pair_df64<FULL>(p, t, meta, l, v);
   } else {
@@ -425,7 +425,7 @@ __device__ __forceinline__ void phases_t(int fluid, T p, T t, Phase<T>& l, Phase
     ideal_gas<T>(p, t, v);
     return;
   }
-  const bool meta = (double)p > h2o_pww((double)t);
+  const bool meta = above_psat((double)p, (double)t);
   iapws_l<T, true>(p, t, l);
   iapws_v_meta<T, true>(p, t, meta, v);
 }
@@ -482,7 +482,7 @@ __device__ __forceinline__ void eos_rho_h(int fluid, double p, double t, double 
     if (fluid != 1) {
       // phase reciprocals in df64
       double il, hl, iv = 0.0, hv = 0.0;
-      if (y1 != 0.0) iapws_inv_df64<true>(p, t, p > h2o_pww(t), &il, &hl, &iv, &hv);
+      if (y1 != 0.0) iapws_inv_df64<true>(p, t, above_psat(p, t), &il, &hl, &iv, &hv);
       else iapws_inv_df64<false>(p, t, false, &il, &hl, &iv, &hv);
       mix_face_mx(p, t, y1, y2, il, hl, iv, hv, rho, h);
       return;
@@ -541,7 +541,7 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
     lf.drdp = (float)l.drdp; lf.drdt = (float)l.drdt; lf.dhdp = (float)l.dhdp; lf.dhdt = (float)l.dhdt;
     vf.drdp = (float)v.drdp; vf.drdt = (float)v.drdt; vf.dhdp = (float)v.dhdp; vf.dhdt = (float)v.dhdt;
   } else {
-    const bool meta = p > h2o_pww(t);
+    const bool meta = above_psat(p, t);
     iapws_inv_df64<true>(p, t, meta, &il, &hl, &iv, &hv);
     iapws_l<float, true>(pf, tf, lf);
     iapws_v_meta<float, true>(pf, tf, meta, vf);
