@@ -1049,18 +1049,22 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
   if (c.iturb >= -1) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
   Diag D;
+  DiagT<float> Df;
   double evis;
-  float pvf[NPVM], dvf[12];
+  float pvf[NPVM], dvf[NDV];
   if (MX) {
-    // the spectral radius and the viscous eigenvalue only size the diagonal block: FP32
-    // (the block's closed-form inverse stays FP64)
+    // the diagonal block in FP32: it shapes the implicit operator only (the sweeps' FP32
+    // corrections use it as well), and its closed-form inverse gives x0 below
     for (int q = 0; q < NPVM; ++q) pvf[q] = (q < npv) ? (float)pv2[q] : 0.0f;
-    for (int q = 0; q < 12; ++q) dvf[q] = (float)dv[q];
+    for (int q = 0; q < NDV; ++q) dvf[q] = (float)dv[q];
     float tvf[3] = {(float)tvc[0], (float)tvc[1], (float)tvc[2]};
     float lam_fs[2];
     diag_spectral_f(c, pvf, dvf[5], fcf, lam_fs);
-    evis = (double)eigenvis_f(c, dvf, tvf);
-    diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D, lam_fs);
+    const float evf = eigenvis_f(c, dvf, tvf);
+    evis = (double)evf;
+    float icf[4], itf[4];
+    for (int q = 0; q < 4; ++q) { icf[q] = (float)ic[q]; itf[q] = (float)it4[q]; }
+    diag_prepare_t<float>(c, pvf, dvf, evf, fcf, (float)vol, (float)d.dt[g], icf, itf, Df, lam_fs);
   } else {
     evis = eigenvis_of(c, dv, tvc);
     diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D);
@@ -1071,7 +1075,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   const int dvi[10] = {0, 1, 6, 7, 8, 9, 10, 11, 12, 13};
   for (int q = 0; q < 7; ++q) o[REC_PV + q] = (pvi[q] < npv) ? pv2[pvi[q]] : 0.0;
   for (int q = 0; q < 10; ++q) o[REC_DV + q] = dv[dvi[q]];
-  diag_to_array(D, o + REC_DIAG);
+  if (!MX) diag_to_array(D, o + REC_DIAG);
   if (MX) {
     // the spectral radii only scale the implicit operator: FP32
     for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = (double)face_spectral<float>(c, fcf + 3 * q, pvf, dvf);
@@ -1079,7 +1083,8 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = face_spectral<double>(c, fc + 3 * q, pv2, dv);
   }
   // beta = 1/sndp2 - 1/c2 + drho/dp = D.rr - (D.b1 - 1) drho/dp
-  o[REC_BETA] = D.rr - (D.b1 - 1.0) * dv[6];
+  if (MX) o[REC_BETA] = (double)(Df.rr - (Df.b1 - 1.0f) * dvf[6]);
+  else o[REC_BETA] = D.rr - (D.b1 - 1.0) * dv[6];
   // (the mixed form's sweeps read the face vectors and this viscous term from the FP32
   // records)
   o[REC_EVV] = MX ? (double)(2.0f * (float)evis / (float)vol) : 2.0 * evis / vol;
@@ -1088,20 +1093,30 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     else { o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e]; }
   }
   if constexpr (MX) {
-    // the cell's tile record (FP32) and the forward sweep's own part x0 = D^-1 res (FP64),
-    // at its tile slot: consecutive i are consecutive slots
+    // the cell's tile record (FP32) and the forward sweep's own part x0 = D^-1 res, at its
+    // tile slot: consecutive i are consecutive slots.  x0 is an FP32 solve of the FP64
+    // residual (rounded once): an inexact step of the iteration, not of its fixed point.
     const long long sl = d.pos[g];
-    double x0[NPVM];
-    for (int v = 0; v < NPVM; ++v) x0[v] = 0.0;
-    diag_solve(c, D, pv2, dv, res, x0);
-    for (int v = 0; v < npv; ++v) d.tq[tq_at(sl, v)] = x0[v];
+    float rf[NPVM], xf[NPVM];
+    for (int v = 0; v < NPVM; ++v) { rf[v] = (v < npv) ? (float)res[v] : 0.0f; xf[v] = 0.0f; }
+    diag_solve_t<float>(c, Df, pvf, dvf, rf, xf);
+    for (int v = 0; v < npv; ++v) d.tq[tq_at(sl, v)] = (double)xf[v];
     float* R = d.trf + trf_at(sl, 0);
-    for (int v = 0; v < npv; ++v) R[(TR_X + v) * TILE_SLOTS] = (float)x0[v];
+    for (int v = 0; v < npv; ++v) R[(TR_X + v) * TILE_SLOTS] = xf[v];
     for (int q = 0; q < 7; ++q) R[(TR_PV + q) * TILE_SLOTS] = (float)o[REC_PV + q];
     for (int q = 0; q < 10; ++q) R[(TR_DV + q) * TILE_SLOTS] = (float)o[REC_DV + q];
     R[TR_BETA * TILE_SLOTS] = (float)o[REC_BETA];
     R[TR_EVV * TILE_SLOTS] = (float)o[REC_EVV];
-    for (int q = 0; q < PREP_DIAG; ++q) R[(TR_DIAG + q) * TILE_SLOTS] = (float)o[REC_DIAG + q];
+    {
+      double od[PREP_DIAG];
+      Diag Dd;
+      Dd.a = Df.a; Dd.b1 = Df.b1; Dd.i_b1 = Df.i_b1; Dd.ss = Df.ss; Dd.rr = Df.rr; Dd.cross = Df.cross;
+      Dd.cross1 = Df.cross1; Dd.cross2 = Df.cross2; Dd.ssy1 = Df.ssy1; Dd.ssy2 = Df.ssy2; Dd.ssh = Df.ssh;
+      Dd.aaa1 = Df.aaa1; Dd.aaa2 = Df.aaa2; Dd.mm = Df.mm; Dd.tt = Df.tt;
+      for (int q = 0; q < 4; ++q) { Dd.c[q] = Df.c[q]; Dd.t[q] = Df.t[q]; }
+      diag_to_array(Dd, od);
+      for (int q = 0; q < PREP_DIAG; ++q) R[(TR_DIAG + q) * TILE_SLOTS] = (float)od[q];
+    }
     for (int dir = 0; dir < 3; ++dir) {
       for (int e = 0; e < 3; ++e) {
         R[(TR_FACEP + 3 * dir + e) * TILE_SLOTS] = fcf[6 * dir + 3 + e];   // cx2, ex2, tx2

@@ -1346,54 +1346,60 @@ using Diag = DiagT<double>;
 // evis = eigenvis_of(c, dv, tv), which the caller also needs
 // lam_fs (optional): the spectral radius lamda and the face-vector sum fs formed by the
 // caller (the mixed form takes them in FP32: they only size the block)
-__device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, const double* dv, double evis,
-                                             const double* fc /* cx1,cx2,ex1,ex2,tx1,tx2 x3 */, double vol,
-                                             double dt, const double* icav, const double* itt, Diag& D,
-                                             const float* lam_fs = nullptr) {
+template <class R>
+__device__ __forceinline__ void diag_prepare_t(const Par& c, const R* pv, const R* dv, R evis,
+                                               const R* fc /* cx1,cx2,ex1,ex2,tx1,tx2 x3 */, R vol, R dt,
+                                               const R* icav, const R* itt, DiagT<R>& D,
+                                               const float* lam_fs = nullptr) {
   // (the reference's repeated quotients are formed once: one reciprocal of c2, of the
   // preconditioned c2 and of the volume; the FP64 pipe is the scarce unit of a GB300)
-  double uv2 = pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3];
-  double sndp2 = sndp2_of<double>(c, dv[5], uv2);
-  const double idv5 = 1.0 / dv[5], isnd = 1.0 / sndp2;
-  const double qr = sndp2 * idv5, qh = 0.5 * (1.0 + qr), qd = sq(1.0 - qr);
-  const double cappa = 1.05;
-  double lamda = 0.0, fs = 0.0;
-  if (lam_fs) { lamda = (double)lam_fs[0]; fs = (double)lam_fs[1]; }
+  R uv2 = pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3];
+  R sndp2 = sndp2_of<R>(c, dv[5], uv2);
+  const R idv5 = R(1) / dv[5], isnd = R(1) / sndp2;
+  const R qr = sndp2 * idv5, qh = R(0.5) * (R(1) + qr), qd = sq(R(1) - qr);
+  const R cappa = R(1.05);
+  R lamda = R(0), fs = R(0);
+  if (lam_fs) { lamda = (R)lam_fs[0]; fs = (R)lam_fs[1]; }
   for (int d = 0; d < 3 && !lam_fs; ++d) {
-    double ox = 0.5 * (fc[6 * d + 0] + fc[6 * d + 3]);
-    double oy = 0.5 * (fc[6 * d + 1] + fc[6 * d + 4]);
-    double oz = 0.5 * (fc[6 * d + 2] + fc[6 * d + 5]);
-    double ds = ox * ox + oy * oy + oz * oz;
-    double u = ox * pv[1] + oy * pv[2] + oz * pv[3];
-    double up = qh * u;
-    double dd = 0.5 * sqrt(u * u * qd + 4.0 * sndp2 * ds);
+    R ox = R(0.5) * (fc[6 * d + 0] + fc[6 * d + 3]);
+    R oy = R(0.5) * (fc[6 * d + 1] + fc[6 * d + 4]);
+    R oz = R(0.5) * (fc[6 * d + 2] + fc[6 * d + 5]);
+    R ds = ox * ox + oy * oy + oz * oz;
+    R u = ox * pv[1] + oy * pv[2] + oz * pv[3];
+    R up = qh * u;
+    R dd = R(0.5) * sqrt(u * u * qd + R(4) * sndp2 * ds);
     lamda += cappa * (fabs(up) + dd);
     fs += ds;  // 0.25*(f1+f2)^2 summed over the components
   }
-  const double ivol = 1.0 / vol;
-  double ev = evis * fs;
-  double bb = (c.nsteady == 1) ? 1.0 : 0.75;
-  double a = 1.0 / (vol / dt + lamda);
-  double unst = (c.nsteady >= 1) ? (double)c.nsteady * bb * vol / c.dt_phy : 0.0;
-  double b = (unst + 2.0 * ev * ivol) * a;
+  const R ivol = R(1) / vol;
+  R ev = evis * fs;
+  R bb = (c.nsteady == 1) ? R(1) : R(0.75);
+  R a = R(1) / (vol / dt + lamda);
+  R unst = (c.nsteady >= 1) ? (R)c.nsteady * bb * vol / (R)c.dt_phy : R(0);
+  R b = (unst + R(2) * ev * ivol) * a;
   for (int q = 0; q < 4; ++q) { D.c[q] = icav[q] * vol * a; D.t[q] = itt[q] * vol * a; }
   D.a = a;
-  D.b1 = 1.0 + b;
-  D.i_b1 = 1.0 / (D.b1 * dv[0]);
+  D.b1 = R(1) + b;
+  D.i_b1 = R(1) / (D.b1 * dv[0]);
   D.ss = dv[0] * dv[11] * (isnd + b * idv5);
   D.rr = isnd - idv5 + D.b1 * dv[6];
-  double hst = dv[1] + 0.5 * uv2 - uv2;
+  R hst = dv[1] + R(0.5) * uv2 - uv2;
   D.cross = dv[13] * dv[8] - dv[12] * dv[9];
   D.cross1 = dv[12] * dv[7] - dv[11] * dv[8];
   D.cross2 = dv[13] * dv[7] - dv[11] * dv[9];
-  double dhdp1 = 1.0 - dv[10] * dv[0];
+  R dhdp1 = R(1) - dv[10] * dv[0];
   D.ssy1 = dv[12] * dv[0] * D.rr + D.b1 * dv[8] * dhdp1;
   D.ssy2 = dv[13] * dv[0] * D.rr + D.b1 * dv[9] * dhdp1;
   D.ssh = dv[0] * D.rr * hst - D.b1 * dhdp1 * dv[0];
   D.aaa1 = dv[8] * hst + dv[12] * dv[0] - D.cross * pv[6];
   D.aaa2 = dv[7] * hst + dv[11] * dv[0] - D.cross2 * pv[6];
-  D.mm = 1.0 / (D.b1 * dv[0] * (D.ss + D.c[0] * D.cross1) - D.c[1] * D.ssy1 + D.c[2] * D.ss);
-  D.tt = 1.0 / (D.t[1] * D.t[2] - (D.t[0] + D.b1 * dv[0]) * (D.t[3] + D.b1 * dv[0]));
+  D.mm = R(1) / (D.b1 * dv[0] * (D.ss + D.c[0] * D.cross1) - D.c[1] * D.ssy1 + D.c[2] * D.ss);
+  D.tt = R(1) / (D.t[1] * D.t[2] - (D.t[0] + D.b1 * dv[0]) * (D.t[3] + D.b1 * dv[0]));
+}
+__device__ __forceinline__ void diag_prepare(const Par& c, const double* pv, const double* dv, double evis,
+                                             const double* fc, double vol, double dt, const double* icav,
+                                             const double* itt, Diag& D, const float* lam_fs = nullptr) {
+  diag_prepare_t<double>(c, pv, dv, evis, fc, vol, dt, icav, itt, D, lam_fs);
 }
 
 // lhs%eigen (src/lhs_module.f90:459-496) in FP32: the spectral radius of the cell and the
