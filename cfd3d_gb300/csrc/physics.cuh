@@ -291,6 +291,20 @@ __device__ __noinline__ void iapws_liq_df64(double p, double t, Phase<double>& l
   }
 }
 
+// h2o_pww (src/eos_module.f90:2266-2279) in df64 on the FP32 pipes (~1e-14 relative): the
+// mixed form's cavitation source takes p - p_sat from it
+__device__ __forceinline__ double h2o_pww_df64(double t) {
+  const df64 tt(fmin(fmax(t, 273.15), 647.096));
+  const df64 theta = tt - df64(0.23855557567849) / (tt - df64(0.65017534844798e3));
+  const df64 th2 = theta * theta;
+  const df64 a = th2 + df64(0.11670521452767e4) * theta - df64(0.72421316703206e6);
+  const df64 b = -(df64(0.17073846940092e2) * th2) + df64(0.12020824702470e5) * theta - df64(0.32325550322333e7);
+  const df64 c = df64(0.14915108613530e2) * th2 - df64(0.48232657361591e4) * theta + df64(0.40511340542057e6);
+  const df64 q = df64(2.0) * c / (-b + dsqrt(b * b - df64(4.0) * a * c));
+  const df64 q2 = q * q;
+  return (double)(df64(1.0e6) * (q2 * q2));
+}
+
 // The mixed form's face-state EOS: 1/rho and h of the liquid (and of the vapour when VAP)
 // from the df64 sums, the reciprocal also taken in df64 (on the FP32 pipes: an FP64
 // division costs a GB300 far more)
@@ -542,9 +556,19 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
     vf.drdp = (float)v.drdp; vf.drdt = (float)v.drdt; vf.dhdp = (float)v.dhdp; vf.dhdt = (float)v.dhdt;
   } else {
     const bool meta = above_psat(p, t);
-    iapws_inv_df64<true>(p, t, meta, &il, &hl, &iv, &hv);
     iapws_l<float, true>(pf, tf, lf);
     iapws_v_meta<float, true>(pf, tf, meta, vf);
+    if (y1 != 0.0) {
+      iapws_inv_df64<true>(p, t, meta, &il, &hl, &iv, &hv);
+    } else {
+      // without vapour the vapour's 1/rho and h enter the mixture with the factor y1 = 0:
+      // its df64 sums are skipped, and the phase's FP32 values serve the vapour density,
+      // enthalpy difference and derivatives the implicit operator and the cavitation
+      // source read
+      iapws_inv_df64<false>(p, t, meta, &il, &hl, &iv, &hv);
+      iv = (double)(1.0f / vf.rho);
+      hv = (double)vf.h;
+    }
   }
   ideal_gas<float>(pf, tf, gf);
   // the gas: 1/rho = T / (p r1) in df64, h = cp T
