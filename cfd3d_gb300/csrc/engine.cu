@@ -1876,9 +1876,9 @@ void launch_rhs(const Engine& E, cudaStream_t s, int T, bool rec) {
 }
 
 // launches of the face fluxes and the residual: the FP64 form's three face kernels, or the
-// mixed form's shadow, its reconstruction and flux kernels of each direction (with the j and
-// k faces' column reconstruction under MUSCL), and k_rhs
-int face_rhs_launches(const Par& c) { return c.mixed ? (8 + (c.nmuscl > 0 ? 2 : 0)) : 4; }
+// mixed form's shadow, its reconstruction and flux kernels of each direction (with the
+// chunk and column reconstructions under MUSCL), and k_rhs
+int face_rhs_launches(const Par& c) { return c.mixed ? (8 + (c.nmuscl > 0 ? 3 : 0)) : 4; }
 
 // The boundary program -- the total-pressure pools, then faces + halos, edges, corners -- and,
 // with the surface-tension source, calvfg and setbc_vfg after it, as timeinteg calls them
@@ -2243,6 +2243,7 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     G.ni = d.imax + 5; G.nj = d.jmax + 5; G.nk = d.kmax + 5;
     G.off = off; G.int_off = ioff;
     for (int q = 0; q < 3; ++q) { G.face_off[q] = foff[q]; G.col_off[q] = coff[q]; }
+    coff[0] += (long long)(d.jmax - 1) * (d.kmax - 1) * ((d.imax + I_CHUNK - 1) / I_CHUNK);
     coff[1] += (long long)(d.imax - 1) * (d.kmax - 1);
     coff[2] += (long long)(d.imax - 1) * (d.jmax - 1);
     off += (long long)G.ni * G.nj * G.nk;

@@ -195,6 +195,71 @@ __global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long 
   }
 }
 
+// The MUSCL / MLP reconstruction of the i faces, warp-cooperatively: a warp takes a chunk of
+// up to I_CHUNK consecutive i faces of one (j, k) line and one variable; lane l forms the
+// reduced stencil's plane data (centre, transverse differences, 3 x 3 minimum and maximum)
+// of the line's cell f0 - 2 + l, and each face lane gathers the planes of its six cells
+// from its neighbours by shuffles.  One 3 x 3 plane load per lane instead of 38 cells per
+// face, all of them coalesced rows along i.  Writes the face states, before the clips, into
+// frec; k_recon_mx<0, true> clips them and forms the face EOS.
+__global__ void __launch_bounds__(128) k_muscl_chunk_i(DevPtr d, Par c, long long nwork) {
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nwork * c.npv) return;   // whole warps leave together
+  const int v = (int)(w / nwork);
+  const long long rem = w - (long long)v * nwork;
+  int b = 0;
+  while (b + 1 < d.nblk && rem >= d.blk[b + 1].col_off[0]) ++b;
+  const BlockGeom& B = d.blk[b];
+  const long long loc = rem - B.col_off[0];
+  const int nch = (B.imax + I_CHUNK - 1) / I_CHUNK;
+  const int chunk = (int)(loc % nch);
+  const long long line = loc / nch;
+  const int j = (int)(line % (B.jmax - 1)) + 2, k = (int)(line / (B.jmax - 1)) + 2;
+  const int f0 = 1 + chunk * I_CHUNK, nf = min(I_CHUNK, B.imax - f0 + 1);
+  const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
+  const float* P = d.pvf + (long long)v * n;
+  const bool mlp = c.nmuscl == 2;
+  // this lane's cell of the line, i = f0 - 2 + lane (f0 - 2 >= -1, and the chunk's last
+  // face's stencil ends at imax + 3)
+  const int i = f0 - 2 + lane;
+  const bool has = lane < nf + 5;
+  const long long gc = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
+  float cc = 0.0f, dt = 0.0f, dr = 0.0f, mn = 0.0f, mx = 0.0f;
+  if (has) {
+    cc = P[gc];
+    if (mlp) {
+      // first transverse direction j (stride sj), second k (stride sk), as stencil_cell
+      float a[3][3];
+#pragma unroll
+      for (int p1 = 0; p1 < 3; ++p1)
+#pragma unroll
+        for (int p2 = 0; p2 < 3; ++p2) a[p1][p2] = P[gc + (p1 - 1) * sj + (p2 - 1) * sk];
+      dt = a[2][1] - a[0][1];
+      dr = a[1][2] - a[1][0];
+      mn = a[0][0]; mx = a[0][0];
+#pragma unroll
+      for (int p1 = 0; p1 < 3; ++p1)
+#pragma unroll
+        for (int p2 = 0; p2 < 3; ++p2) { mn = fminf(mn, a[p1][p2]); mx = fmaxf(mx, a[p1][p2]); }
+    }
+  }
+  // face lane l: face f0 + l, left cell at plane l + 2; its cells are planes l .. l + 5
+  const unsigned full = 0xffffffffu;
+  auto at = [&](float x, int q) { return __shfl_sync(full, x, (lane + q) & 31); };
+  const float cm2 = at(cc, 0), cm1 = at(cc, 1), c0 = at(cc, 2), c1 = at(cc, 3), c2 = at(cc, 4), c3 = at(cc, 5);
+  const float dt0 = at(dt, 2), dr0 = at(dr, 2), dt1 = at(dt, 3), dr1 = at(dr, 3);
+  const float mnr[4] = {at(mn, 1), at(mn, 2), at(mn, 3), at(mn, 4)};
+  const float mxr[4] = {at(mx, 1), at(mx, 2), at(mx, 3), at(mx, 4)};
+  if (lane < nf) {
+    float xl, xr;
+    muscl_reduced(c, cm2, cm1, c0, c1, c2, c3, dt0, dr0, dt1, dr1, mnr, mxr, xl, xr);
+    const long long gf = B.off + (f0 + lane + 1) + sj * (j + 1) + sk * (k + 1);
+    d.frec[(long long)v * n + gf] = xl;
+    d.frec[(long long)(FREC_SIDE + v) * n + gf] = xr;
+  }
+}
+
 // MARCH: the face states come from k_muscl_march (frec) instead of the 38-cell stencil
 template <int DIR, bool MARCH = false>
 __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
@@ -397,10 +462,16 @@ void launch_face_flux_mixed(const Engine& E, cudaStream_t s) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   k_shadow<<<std::max(nsm, 1) * 8, 256, 0, s>>>(E.d, E.par);
-  k_recon_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  k_flux_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  // the j and k faces: reconstruction by columns (k_muscl_march), then clips and face EOS
+  // the i faces: reconstruction by warp-wide chunks of a line (k_muscl_chunk_i), the j and
+  // k faces by columns (k_muscl_march); then the clips and the face EOS
   const bool march = E.par.nmuscl > 0;
+  if (march) {
+    k_muscl_chunk_i<<<(unsigned)((E.ncol[0] * E.par.npv * 32 + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[0]);
+    k_recon_mx<0, true><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
+  } else {
+    k_recon_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
+  }
+  k_flux_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
   if (march) k_muscl_march<1><<<(unsigned)((E.ncol[1] * E.par.npv + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[1]);
   if (march) k_recon_mx<1, true><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
   else k_recon_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
