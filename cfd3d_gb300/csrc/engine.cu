@@ -1105,7 +1105,6 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     for (int v = 0; v < npv; ++v) R[(TR_X + v) * TILE_SLOTS] = xf[v];
     for (int q = 0; q < 7; ++q) R[(TR_PV + q) * TILE_SLOTS] = (float)o[REC_PV + q];
     for (int q = 0; q < 10; ++q) R[(TR_DV + q) * TILE_SLOTS] = (float)o[REC_DV + q];
-    R[TR_BETA * TILE_SLOTS] = (float)o[REC_BETA];
     R[TR_EVV * TILE_SLOTS] = (float)o[REC_EVV];
     {
       double od[PREP_DIAG];
@@ -1502,7 +1501,7 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
         }
         // outgoing contributions: A+ dq through the cell's + faces (forward), -A- dq through
         // its - faces (backward), each from zero so that the receiver adds them in order
-        const float beta = S32[TR_BETA * TILE_SLOTS + sl], evv = S32[TR_EVV * TILE_SLOTS + sl];
+        const float beta = D.rr - (D.b1 - 1.0f) * dv[6], evv = S32[TR_EVV * TILE_SLOTS + sl];
         auto contribution = [&](int dir, float* o) {
           float nx[3];
 #pragma unroll
@@ -2391,6 +2390,9 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     CFD_CUDA(cudaFuncSetAttribute(k_sweep_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM));
     CFD_CUDA(cudaFuncSetAttribute(k_sweep_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM));
+    // the largest shared-memory carveout: three tiles' records per SM
+    CFD_CUDA(cudaFuncSetAttribute(k_sweep_tile<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    CFD_CUDA(cudaFuncSetAttribute(k_sweep_tile<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_tile<true>, 32, TILE_SMEM);
     E.sweep_grid = std::max(1, std::min(std::max(per, 1) * nsm, E.d.ntile));
     CFD_CUDA(cudaDeviceSynchronize());

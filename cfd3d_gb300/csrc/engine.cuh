@@ -102,16 +102,15 @@ constexpr int TILE_IN_J = 32, TILE_IN_K = TILE_IN_J + TILE_K * TILE_I, TILE_IN =
 enum {
   TR_PV = 0,       // pv 1, 2, 3, 5, 6, 7, 8
   TR_DV = 7,       // dv 0, 1, 6 .. 13
-  TR_BETA = 17,
-  TR_EVV = 18,
-  TR_DIAG = 19,    // 23 values of the closed-form diagonal block
-  TR_X = 42,       // the own part of dq (npv)
-  TR_COMMON = 51,
-  TR_FACEP = 51,   // + face vectors cx, ex, tx
-  TR_SPECP = 60,   // + face spectral radii of the three directions
-  TR_FACEM = 63,   // - face vectors
-  TR_SPECM = 72,   // - face spectral radii
-  NTR = 75
+  TR_EVV = 17,     // (beta follows from the block: rr - (b1 - 1) drho/dp)
+  TR_DIAG = 18,    // 23 values of the closed-form diagonal block
+  TR_X = 41,       // the own part of dq (npv)
+  TR_COMMON = 50,
+  TR_FACEP = 50,   // + face vectors cx, ex, tx
+  TR_SPECP = 59,   // + face spectral radii of the three directions
+  TR_FACEM = 62,   // - face vectors
+  TR_SPECM = 71,   // - face spectral radii
+  NTR = 74
 };
 constexpr int TS_FIELDS = TR_COMMON + 12;    // the FP32 fields one sweep reads
 struct TileDesc {
