@@ -62,11 +62,5 @@ __device__ __forceinline__ df64 operator/(df64 a, df64 b) {
   return q + df64(q3, 0.0f);
 }
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { a = a + b; return a; }
-// square root: the FP32 root and one Newton correction from the exact remainder a - s^2
-__device__ __forceinline__ df64 dsqrt(df64 a) {
-  const float s = sqrtf(a.hi);
-  const df64 r = a - df64(s, 0.0f) * df64(s, 0.0f);
-  return fast_two_sum(s, __fdiv_rn(r.hi, 2.0f * s));
-}
 
 }  // namespace cfd

@@ -837,11 +837,12 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   if (c.ncav) {
     if (MX) {
       // FP32 source (its rates reach the residual to ~1e-7 of their size) with the
-      // saturation pressure in df64 / the saturation temperature in FP64
+      // saturation pressure / temperature in FP64 (a df64 saturation pressure measured
+      // slower here: its quotients and root cost more FP32 issue than the FP64 pipe frees)
       double sat[2] = {0.0, 0.0};
       if (pv2[4] < 647.096) {
         if (c.ncav == 5) sat[1] = h2o_tww(pv2[0] + c.pref);
-        else sat[0] = h2o_pww_df64(pv2[4]);
+        else sat[0] = h2o_pww(pv2[4]);
       }
       float p2f[NPVM], dvf[NDV];
       for (int q = 0; q < NPVM; ++q) p2f[q] = (float)pv2[q];

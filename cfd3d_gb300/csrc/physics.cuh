@@ -291,20 +291,6 @@ __device__ __noinline__ void iapws_liq_df64(double p, double t, Phase<double>& l
   }
 }
 
-// h2o_pww (src/eos_module.f90:2266-2279) in df64 on the FP32 pipes (~1e-14 relative): the
-// mixed form's cavitation source takes p - p_sat from it
-__device__ __forceinline__ double h2o_pww_df64(double t) {
-  const df64 tt(fmin(fmax(t, 273.15), 647.096));
-  const df64 theta = tt - df64(0.23855557567849) / (tt - df64(0.65017534844798e3));
-  const df64 th2 = theta * theta;
-  const df64 a = th2 + df64(0.11670521452767e4) * theta - df64(0.72421316703206e6);
-  const df64 b = -(df64(0.17073846940092e2) * th2) + df64(0.12020824702470e5) * theta - df64(0.32325550322333e7);
-  const df64 c = df64(0.14915108613530e2) * th2 - df64(0.48232657361591e4) * theta + df64(0.40511340542057e6);
-  const df64 q = df64(2.0) * c / (-b + dsqrt(b * b - df64(4.0) * a * c));
-  const df64 q2 = q * q;
-  return (double)(df64(1.0e6) * (q2 * q2));
-}
-
 // The mixed form's face-state EOS: 1/rho and h of the liquid (and of the vapour when VAP)
 // from the df64 sums, the reciprocal also taken in df64 (on the FP32 pipes: an FP64
 // division costs a GB300 far more)
