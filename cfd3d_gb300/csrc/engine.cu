@@ -767,7 +767,7 @@ __device__ void csf_cell(const DevPtr& d, long long g, long long sj, long long s
 // gravity and the surface-tension sources (a separate instantiation, so that the plain kernel carries none of their
 // code)
 template <bool MX, bool REC = true, bool XS = false>
-__global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
   int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
@@ -782,7 +782,10 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     // the stored FP32 fluxes are deviations from the free-stream flux: their differences
     // and sums in FP32 carry rounding of the order of the storage's own (one conversion to
     // FP64 per variable instead of one per stored value)
-    for (int v = 0; v < npv; ++v) {
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      res[v] = 0.0;
+      if (v >= npv) continue;
       float r = 0.0f;
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
@@ -828,10 +831,13 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     // the stored mixed-form fluxes are F - (Phi + pref I).n dl: the free-stream part comes
     // back through the cell's face-vector sum (zero up to the metrics' closure error),
     // formed once by k_closure
-    for (int v = 0; v < npv; ++v) res[v] -= d.clo[v * n + g];
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v)
+      if (v < npv) res[v] -= d.clo[v * n + g];
   }
   double pv2[NPVM], dv[NDV];
-  for (int v = 0; v < npv; ++v) pv2[v] = d.pv[v * n + g];
+#pragma unroll
+  for (int v = 0; v < NPVM; ++v) pv2[v] = (v < npv) ? d.pv[v * n + g] : 0.0;
   for (int v = 0; v < NDV; ++v) dv[v] = d.dv[v * n + g];
   const double vol = d.gm[GM_GRD * n + g];
   if (c.ncav) {
@@ -988,8 +994,11 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     fx[0] = dv[0];
     fx[1] = dv[0] * pv2[1]; fx[2] = dv[0] * pv2[2]; fx[3] = dv[0] * pv2[3];
     fx[4] = dv[0] * (dv[1] + 0.5 * (pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3])) - (pv2[0] + c.pref);
-    for (int v = 5; v < npv; ++v) fx[v] = dv[0] * pv2[v];
-    for (int v = 0; v < npv; ++v) {
+#pragma unroll
+    for (int v = 5; v < NPVM; ++v) fx[v] = dv[0] * pv2[v];
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      if (v >= npv) continue;
       double q1 = d.qq[v * n + g], q2 = d.qq[(npv + v) * n + g];
       double s = (double)c.nsteady * (bb * fx[v] - q1) + 0.5 * ((double)c.nsteady - 1.0) * q2;
       res[v] = res[v] - s * vol / c.dt_phy;
@@ -1022,7 +1031,9 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     for (int q = 0; q < 5; ++q) res[q] = res[q] + cs[q];
     for (int e = 0; e < 3; ++e) d.csf[e * n + g] = cs[1 + e];
   }
-  for (int v = 0; v < npv; ++v) d.res[v * n + g] = res[v];
+#pragma unroll
+  for (int v = 0; v < NPVM; ++v)
+    if (v < npv) d.res[v * n + g] = res[v];
   if constexpr (!REC) return;   // the explicit schemes need no sweep records
   if (c.rot) {
     // the implicit operator's enthalpy is the rothalpy (lhs%getenthalpy, jac%getenthalpy):
@@ -1034,7 +1045,9 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous
   // term), written with its state and residual as the cell's sweep record at pos[g]
   double tvc[3] = {0.0, 0.0, 0.0};
-  for (int q = 0; q < c.ntv; ++q) tvc[q] = d.tv[q * n + g];
+#pragma unroll
+  for (int q = 0; q < 3; ++q)
+    if (q < c.ntv) tvc[q] = d.tv[q * n + g];
   // face vectors cx1, cx2, ex1, ex2, tx1, tx2: FP64, or (mixed form) their FP32 copies
   double fc[18];
   float fcf[18];
@@ -1101,9 +1114,10 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     float rf[NPVM], xf[NPVM];
     for (int v = 0; v < NPVM; ++v) { rf[v] = (v < npv) ? (float)res[v] : 0.0f; xf[v] = 0.0f; }
     diag_solve_t<float>(c, Df, pvf, dvf, rf, xf);
-    for (int v = 0; v < npv; ++v) d.tq[tq_at(sl, v)] = (double)xf[v];
     float* R = d.trf + trf_at(sl, 0);
-    for (int v = 0; v < npv; ++v) R[(TR_X + v) * TILE_SLOTS] = xf[v];
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v)
+      if (v < npv) { d.tq[tq_at(sl, v)] = (double)xf[v]; R[(TR_X + v) * TILE_SLOTS] = xf[v]; }
     for (int q = 0; q < 7; ++q) R[(TR_PV + q) * TILE_SLOTS] = (float)o[REC_PV + q];
     for (int q = 0; q < 10; ++q) R[(TR_DV + q) * TILE_SLOTS] = (float)o[REC_DV + q];
     R[TR_EVV * TILE_SLOTS] = (float)o[REC_EVV];
@@ -1549,7 +1563,7 @@ __global__ void __launch_bounds__(32) k_sweep_tile(DevPtr d, Par c, long long sp
 // iteration (kept in dqs at t by stage 1).  The residual norms measure the change over
 // the whole iteration (they are final after the last stage).
 template <bool MX, bool EX = false>
-__global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
+__global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
   // grid-stride over the interior cells: the grid is a fixed multiple of the SM count,
   // so the per-CTA partials (and the order they are summed in) do not depend on size
   const int npv = c.npv;
@@ -1567,7 +1581,10 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
     if constexpr (!EX) {
       // the sweep's dq: at the cell's tile slot (mixed form) or plane-major position
       const long long pq = d.pos[g];
-      for (int v = 0; v < npv; ++v) {
+#pragma unroll
+      for (int v = 0; v < NPVM; ++v) {
+        old[v] = p[v] = 0.0;
+        if (v >= npv) continue;
         old[v] = d.pv[v * n + g];
         p[v] = old[v] + (MX ? d.tq[tq_at(pq, v)] + (double)d.tyf[tq_at(pq, v)] + (double)d.tyb[tq_at(pq, v)]
                             : d.dqs[v * d.nint + pq]);
@@ -1593,8 +1610,9 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
         p[v] = c1 * old[v] + c2 * cur[v] + c2 * x[v];   // a3 = a2 in both schemes
       }
     }
-    for (int v = 0; v < npv; ++v)
-      if (!isfinite(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v)
+      if (v < npv && !isfinite(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
     p[0] = fmax(-c.pref + 1.0e1, p[0]);
     p[5] = fmin(1.0, fmax(0.0, p[5]));
     p[6] = fmin(1.0, fmax(0.0, p[6]));
@@ -1603,10 +1621,14 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
       p[8] = fmax(fmax(p[8], 1.0e-16), d.ocut[g]);
     }
     double dv[NDV], tv[3] = {0.0, 0.0, 0.0};
-    for (int v = 0; v < c.ntv; ++v) tv[v] = d.tv[v * n + g];
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+      if (v < c.ntv) tv[v] = d.tv[v * n + g];
     if (MX) deteos_split(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
     else deteos<false>(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
-    for (int v = 0; v < npv; ++v) {
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      if (v >= npv) continue;
       d.pv[v * n + g] = p[v];
       double df = fabs(old[v] - p[v]);
       sq_[v] += df * df;
@@ -1616,7 +1638,9 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
       d.dv[v * n + g] = dv[v];
       if (!isfinite(dv[v])) bad = 1;
     }
-    for (int v = 0; v < c.ntv; ++v) d.tv[v * n + g] = tv[v];
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+      if (v < c.ntv) d.tv[v * n + g] = tv[v];
     double dp = fabs(old[0] - p[0]);
     if (dp > dpmax) { dpmax = dp; dpidx = t; }   // t increases: ties keep the first cell
   }
@@ -1624,7 +1648,9 @@ __global__ void __launch_bounds__(128) k_update(DevPtr d, Par c, int stage) {
   // per-CTA partial sums (deterministic order: warp shuffles then warps in order)
   __shared__ double sh[4][NPVM + 2];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int v = 0; v < npv; ++v) {
+#pragma unroll
+  for (int v = 0; v < NPVM; ++v) {
+    if (v >= npv) continue;
     double s = sq_[v];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) sh[w][v] = s;
@@ -1876,9 +1902,9 @@ void launch_rhs(const Engine& E, cudaStream_t s, int T, bool rec) {
 }
 
 // launches of the face fluxes and the residual: the FP64 form's three face kernels, or the
-// mixed form's shadow, its reconstruction and flux kernels of each direction (with the
-// chunk and column reconstructions under MUSCL), and k_rhs
-int face_rhs_launches(const Par& c) { return c.mixed ? (8 + (c.nmuscl > 0 ? 3 : 0)) : 4; }
+// mixed form's shadow, its reconstruction and flux kernels of each direction (with the j and
+// k faces' column reconstruction under MUSCL), and k_rhs
+int face_rhs_launches(const Par& c) { return c.mixed ? (8 + (c.nmuscl > 0 ? 2 : 0)) : 4; }
 
 // The boundary program -- the total-pressure pools, then faces + halos, edges, corners -- and,
 // with the surface-tension source, calvfg and setbc_vfg after it, as timeinteg calls them
@@ -2243,7 +2269,6 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     G.ni = d.imax + 5; G.nj = d.jmax + 5; G.nk = d.kmax + 5;
     G.off = off; G.int_off = ioff;
     for (int q = 0; q < 3; ++q) { G.face_off[q] = foff[q]; G.col_off[q] = coff[q]; }
-    coff[0] += (long long)(d.jmax - 1) * (d.kmax - 1) * ((d.imax + I_CHUNK - 1) / I_CHUNK);
     coff[1] += (long long)(d.imax - 1) * (d.kmax - 1);
     coff[2] += (long long)(d.imax - 1) * (d.jmax - 1);
     off += (long long)G.ni * G.nj * G.nk;
@@ -3138,7 +3163,7 @@ int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
   int bestg = E.sweep_grid;
   tbest = 1e30f;
   for (int m = 1; c.timemethod == 3 && m <= std::max(per, 1); ++m) {   // (no sweeps in the explicit schemes)
-    if (m > 2 && m % 2) continue;   // 1, 2, 4, 6, ...
+    if (m > 4 && m % 2) continue;   // 1, 2, 3, 4, 6, 8, ...
     const int grid = std::max(1, std::min(m * nsm, nwork));
     // (the timed sweeps run on the records of the iteration launched above; the forward one
     // rewrites the right-hand side it reads, which changes the values but not the work)

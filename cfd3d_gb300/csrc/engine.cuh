@@ -24,12 +24,8 @@ struct BlockGeom {
   long long off;            // first padded cell of the block
   long long int_off;        // first interior cell in the flat interior numbering
   long long face_off[3];    // first face of each direction in the flat face numbering
-  long long col_off[3];     // first column of cells along direction 1 (i, k) / 2 (i, j); direction 0:
-                            // first chunk of I_CHUNK i-faces of its (j, k) lines
+  long long col_off[3];     // first column of cells along direction 1 (i, k) / 2 (i, j)
 };
-// i faces of one line that one warp reconstructs together (its 32 lanes hold the planes of
-// the chunk's cells and the two before and three after it)
-constexpr int I_CHUNK = 27;
 
 // gm planes: face vectors and cell geometry
 enum { GM_CX = 0, GM_EX = 3, GM_TX = 6, GM_GRD = 9 };

@@ -73,23 +73,23 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c) {
 // -- the caller evaluates the IF97 sums -- when the base carries vapour or the state is
 // farther away.
 __device__ __forceinline__ bool liquid_expand(const DevPtr& d, const Par& c, long long b, const float* x,
-                                              const float* xb, float& rdev, float& hdev) {
+                                              float xb0, float xb4, float xb6, float& rdev, float& hdev) {
   const long long n = d.ncell;
   const float rho = d.lqf[LQ_RHO * n + b];
   if (rho == 0.0f) return false;
-  const float dp = (x[0] - xb[0]) - d.lqf[LQ_RP * n + b];
-  const float dt = (x[4] - xb[4]) - d.lqf[LQ_RT * n + b];
+  const float dp = (x[0] - xb0) - d.lqf[LQ_RP * n + b];
+  const float dt = (x[4] - xb4) - d.lqf[LQ_RT * n + b];
   if (!(fabsf(dp) <= 2.0e4f && fabsf(dt) <= 0.02f)) return false;
   const float dvl = d.lqf[LQ_VP * n + b] * dp + d.lqf[LQ_VT * n + b] * dt;
   const float dhl = d.lqf[LQ_HP * n + b] * dp + d.lqf[LQ_HT * n + b] * dt;
   // the gas: 1/rho_g = T / (p r1), h_g = cp_g T; base state from its shadow and roundings
   const float r1 = 0.00348383500557f, cpg = 1004.64f;
-  const float pb = (float)c.pref + xb[0] + d.lqf[LQ_RP * n + b];
-  const float tb = (float)c.tref + xb[4] + d.lqf[LQ_RT * n + b];
+  const float pb = (float)c.pref + xb0 + d.lqf[LQ_RP * n + b];
+  const float tb = (float)c.tref + xb4 + d.lqf[LQ_RT * n + b];
   const float pf = pb + dp, tf = tb + dt;
   const float vgf = tf / (pf * r1);
   const float dvg = (dt * pb - tb * dp) / (pf * pb * r1);
-  const float y2b = xb[6], y2f = x[6], dy2 = y2f - y2b;
+  const float y2b = xb6, y2f = x[6], dy2 = y2f - y2b;
   const float dv = (1.0f - y2f) * dvl + dy2 * (vgf - d.lqf[LQ_VL * n + b]) + y2b * dvg;
   rdev = d.lqf[LQ_RDEV * n + b] - rho * rho * dv / (1.0f + rho * dv);
   const float hgl = -d.lqf[LQ_HLG * n + b] + cpg * dt;   // h_g(face) - h_l(base)
@@ -195,72 +195,10 @@ __global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long 
   }
 }
 
-// The MUSCL / MLP reconstruction of the i faces, warp-cooperatively: a warp takes a chunk of
-// up to I_CHUNK consecutive i faces of one (j, k) line and one variable; lane l forms the
-// reduced stencil's plane data (centre, transverse differences, 3 x 3 minimum and maximum)
-// of the line's cell f0 - 2 + l, and each face lane gathers the planes of its six cells
-// from its neighbours by shuffles.  One 3 x 3 plane load per lane instead of 38 cells per
-// face, all of them coalesced rows along i.  Writes the face states, before the clips, into
-// frec; k_recon_mx<0, true> clips them and forms the face EOS.
-__global__ void __launch_bounds__(128) k_muscl_chunk_i(DevPtr d, Par c, long long nwork) {
-  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (w >= nwork * c.npv) return;   // whole warps leave together
-  const int v = (int)(w / nwork);
-  const long long rem = w - (long long)v * nwork;
-  int b = 0;
-  while (b + 1 < d.nblk && rem >= d.blk[b + 1].col_off[0]) ++b;
-  const BlockGeom& B = d.blk[b];
-  const long long loc = rem - B.col_off[0];
-  const int nch = (B.imax + I_CHUNK - 1) / I_CHUNK;
-  const int chunk = (int)(loc % nch);
-  const long long line = loc / nch;
-  const int j = (int)(line % (B.jmax - 1)) + 2, k = (int)(line / (B.jmax - 1)) + 2;
-  const int f0 = 1 + chunk * I_CHUNK, nf = min(I_CHUNK, B.imax - f0 + 1);
-  const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
-  const float* P = d.pvf + (long long)v * n;
-  const bool mlp = c.nmuscl == 2;
-  // this lane's cell of the line, i = f0 - 2 + lane (f0 - 2 >= -1, and the chunk's last
-  // face's stencil ends at imax + 3)
-  const int i = f0 - 2 + lane;
-  const bool has = lane < nf + 5;
-  const long long gc = B.off + (i + 1) + sj * (j + 1) + sk * (k + 1);
-  float cc = 0.0f, dt = 0.0f, dr = 0.0f, mn = 0.0f, mx = 0.0f;
-  if (has) {
-    cc = P[gc];
-    if (mlp) {
-      // first transverse direction j (stride sj), second k (stride sk), as stencil_cell
-      float a[3][3];
-#pragma unroll
-      for (int p1 = 0; p1 < 3; ++p1)
-#pragma unroll
-        for (int p2 = 0; p2 < 3; ++p2) a[p1][p2] = P[gc + (p1 - 1) * sj + (p2 - 1) * sk];
-      dt = a[2][1] - a[0][1];
-      dr = a[1][2] - a[1][0];
-      mn = a[0][0]; mx = a[0][0];
-#pragma unroll
-      for (int p1 = 0; p1 < 3; ++p1)
-#pragma unroll
-        for (int p2 = 0; p2 < 3; ++p2) { mn = fminf(mn, a[p1][p2]); mx = fmaxf(mx, a[p1][p2]); }
-    }
-  }
-  // face lane l: face f0 + l, left cell at plane l + 2; its cells are planes l .. l + 5
-  const unsigned full = 0xffffffffu;
-  auto at = [&](float x, int q) { return __shfl_sync(full, x, (lane + q) & 31); };
-  const float cm2 = at(cc, 0), cm1 = at(cc, 1), c0 = at(cc, 2), c1 = at(cc, 3), c2 = at(cc, 4), c3 = at(cc, 5);
-  const float dt0 = at(dt, 2), dr0 = at(dr, 2), dt1 = at(dt, 3), dr1 = at(dr, 3);
-  const float mnr[4] = {at(mn, 1), at(mn, 2), at(mn, 3), at(mn, 4)};
-  const float mxr[4] = {at(mx, 1), at(mx, 2), at(mx, 3), at(mx, 4)};
-  if (lane < nf) {
-    float xl, xr;
-    muscl_reduced(c, cm2, cm1, c0, c1, c2, c3, dt0, dr0, dt1, dr1, mnr, mxr, xl, xr);
-    const long long gf = B.off + (f0 + lane + 1) + sj * (j + 1) + sk * (k + 1);
-    d.frec[(long long)v * n + gf] = xl;
-    d.frec[(long long)(FREC_SIDE + v) * n + gf] = xr;
-  }
-}
-
-// MARCH: the face states come from k_muscl_march (frec) instead of the 38-cell stencil
+// Second order (nmuscl > 0): with MARCH the face states come from k_muscl_march (frec,
+// before the clips), otherwise from the face's 38-cell stencil; first order: the face states
+// are the cells' own.  (The per-variable loops run over the compile-time bound, guarded by
+// npv, so that the arrays stay in registers.)
 template <int DIR, bool MARCH = false>
 __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
   const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
@@ -273,13 +211,14 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
   float cl = 0.0f, cr = 0.0f;
   if (c.nmuscl > 0) {
     float c9[NPVM], c10[NPVM];
-    if (MARCH) {
-      for (int v = 0; v < npv; ++v) {
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      gl[v] = gR[v] = c9[v] = c10[v] = 0.0f;
+      if (v >= npv) continue;
+      if (MARCH) {
         gl[v] = d.frec[v * n + g]; gR[v] = d.frec[(FREC_SIDE + v) * n + g];
         c9[v] = P[v * n + g]; c10[v] = P[v * n + gr];
-      }
-    } else {
-      for (int v = 0; v < npv; ++v) {
+      } else {
         float x[38];
 #pragma unroll
         for (int l = 0; l < 38; ++l) x[l] = P[v * n + stencil_cell(l, g, f.sn, f.s1, f.s2)];
@@ -292,13 +231,15 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
     // a block face, where that cell is a ghost, the cell across the face; any other state by
     // the IF97 sums (FP64 mixture).  (Without the second base, the boundary faces of the i
     // direction, two in every warp's row of faces, would send their warps through the sums.)
-    if (!(gl[5] == 0.0f && liquid_expand(d, c, f.lin ? g : gr, gl, f.lin ? c9 : c10, rdl, hdl))) {
+    const float bl0 = f.lin ? c9[0] : c10[0], bl4 = f.lin ? c9[4] : c10[4], bl6 = f.lin ? c9[6] : c10[6];
+    const float br0 = f.rin ? c10[0] : c9[0], br4 = f.rin ? c10[4] : c9[4], br6 = f.rin ? c10[6] : c9[6];
+    if (!(gl[5] == 0.0f && liquid_expand(d, c, f.lin ? g : gr, gl, bl0, bl4, bl6, rdl, hdl))) {
       double rho, h;
       eos_rho_h<true>(c.fluid, c.pref + (double)gl[0], c.tref + (double)gl[4], gl[5], gl[6], rho, h);
       rdl = (float)(rho - c.rhoref);
       hdl = (float)(h - c.href);
     }
-    if (!(gR[5] == 0.0f && liquid_expand(d, c, f.rin ? gr : g, gR, f.rin ? c10 : c9, rdr, hdr))) {
+    if (!(gR[5] == 0.0f && liquid_expand(d, c, f.rin ? gr : g, gR, br0, br4, br6, rdr, hdr))) {
       double rho, h;
       eos_rho_h<true>(c.fluid, c.pref + (double)gR[0], c.tref + (double)gR[4], gR[5], gR[6], rho, h);
       rdr = (float)(rho - c.rhoref);
@@ -309,12 +250,18 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
       cr = eos_c2_f(c.fluid, (float)c.pref + gR[0], (float)c.tref + gR[4], gR[5], gR[6], &d.sc->snd2_fallbacks);
     }
   } else {
-    for (int v = 0; v < npv; ++v) { gl[v] = P[v * n + g]; gR[v] = P[v * n + gr]; }
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      gl[v] = gR[v] = 0.0f;
+      if (v < npv) { gl[v] = P[v * n + g]; gR[v] = P[v * n + gr]; }
+    }
     rdl = (float)(d.dv[g] - c.rhoref); hdl = (float)(d.dv[n + g] - c.href); cl = (float)d.dv[5 * n + g];
     rdr = (float)(d.dv[gr] - c.rhoref); hdr = (float)(d.dv[n + gr] - c.href); cr = (float)d.dv[5 * n + gr];
   }
   float* F = d.frec;
-  for (int v = 0; v < npv; ++v) { F[v * n + g] = gl[v]; F[(FREC_SIDE + v) * n + g] = gR[v]; }
+#pragma unroll
+  for (int v = 0; v < NPVM; ++v)
+    if (v < npv) { F[v * n + g] = gl[v]; F[(FREC_SIDE + v) * n + g] = gR[v]; }
   F[NPVM * n + g] = rdl;
   F[(NPVM + 1) * n + g] = hdl;
   F[(NPVM + 2) * n + g] = cl;
@@ -324,7 +271,7 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256, 2) k_flux_mx(DevPtr d, Par c) {
   const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
   if (!f.ok) return;
   const long long n = d.ncell, g = f.g, gr = g + f.sn;
@@ -337,7 +284,11 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
   FaceMx L, R;
   {
     const float* F = d.frec;
-    for (int v = 0; v < npv; ++v) { L.g[v] = F[v * n + g]; R.g[v] = F[(FREC_SIDE + v) * n + g]; }
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      L.g[v] = R.g[v] = 0.0f;
+      if (v < npv) { L.g[v] = F[v * n + g]; R.g[v] = F[(FREC_SIDE + v) * n + g]; }
+    }
     const df64 rref = dfp(c.rhoref2), href = dfp(c.href2);
     L.rho = rref + dff(F[NPVM * n + g]);
     L.h = href + dff(F[(NPVM + 1) * n + g]);
@@ -355,7 +306,9 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
     float rd = 1.0f / (srl + srr);
     for (int q = 0; q < 3; ++q) ravg_u[q] = c.U2[q][0] + (srl * L.g[1 + q] + srr * R.g[1 + q]) * rd;
     for (int q = 0; q < NPVM; ++q) ravg_s[q] = 0.0f;
-    for (int q = 5; q < npv; ++q) ravg_s[q] = (srl * L.g[q] + srr * R.g[q]) * rd;
+#pragma unroll
+    for (int q = 5; q < NPVM; ++q)
+      if (q < npv) ravg_s[q] = (srl * L.g[q] + srr * R.g[q]) * rd;
     if (nv[0].hi != 0.0f || nv[1].hi != 0.0f || nv[2].hi != 0.0f) {
       // the FP32 sound speed of the Roe average: FP32 state
       const float pa = (float)c.pref + 0.5f * (L.g[0] + R.g[0]);
@@ -371,7 +324,9 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
   float fx[NPVM];
   inviscid_flux_mx(c, nv, L, R, sdst, rc2, ravg_u, ravg_s, fx);
   float* fo = d.fi32 + (long long)DIR * npv * n;
-  for (int v = 0; v < npv; ++v) fo[v * n + g] = fx[v];
+#pragma unroll
+  for (int v = 0; v < NPVM; ++v)
+    if (v < npv) fo[v * n + g] = fx[v];
   if (c.iturb == -3) return;
   // ---- viscous flux in FP32 (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
   const bool turb = (c.iturb >= -1);
@@ -389,7 +344,9 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
   }
   float vol = 2.0f / (GF[GM_GRD * n + g] + GF[GM_GRD * n + gr]);
   float tvl[3] = {0, 0, 0}, tvr[3] = {0, 0, 0};
-  for (int q = 0; q < c.ntv; ++q) { tvl[q] = (float)d.tv[q * n + g]; tvr[q] = (float)d.tv[q * n + gr]; }
+#pragma unroll
+  for (int q = 0; q < 3; ++q)
+    if (q < c.ntv) { tvl[q] = (float)d.tv[q * n + g]; tvr[q] = (float)d.tv[q * n + gr]; }
   float vis = 0.5f * (tvl[0] + tvr[0]);
   float con = 0.5f * (tvl[1] + tvr[1]);
   float emut = 0.0f, tcon = 0.0f;
@@ -400,7 +357,10 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
   const int vars[6] = {1, 2, 3, 4, 7, 8};
   float gx[6], gy[6], gz[6], cc[6];
   const int nvv = turb ? 6 : 4;
-  for (int q = 0; q < nvv; ++q) {
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    gx[q] = gy[q] = gz[q] = cc[q] = 0.0f;
+    if (q >= nvv) continue;
     const float* X = P + vars[q] * n;
     float x[18];
 #pragma unroll
@@ -452,7 +412,9 @@ __global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c) {
     fv[8] = (vis + emut * tdo) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
   }
   float* fvo = d.fv32 + (long long)DIR * npv * n;
-  for (int v = 0; v < npv; ++v) fvo[v * n + g] = fv[v];
+#pragma unroll
+  for (int v = 0; v < NPVM; ++v)
+    if (v < npv) fvo[v * n + g] = fv[v];
 }
 
 void launch_face_flux_mixed(const Engine& E, cudaStream_t s) {
@@ -462,15 +424,10 @@ void launch_face_flux_mixed(const Engine& E, cudaStream_t s) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   k_shadow<<<std::max(nsm, 1) * 8, 256, 0, s>>>(E.d, E.par);
-  // the i faces: reconstruction by warp-wide chunks of a line (k_muscl_chunk_i), the j and
-  // k faces by columns (k_muscl_march); then the clips and the face EOS
+  // the i faces from their 38-cell stencils, the j and k faces by columns (k_muscl_march)
+  // under MUSCL; then the clips and the face EOS
   const bool march = E.par.nmuscl > 0;
-  if (march) {
-    k_muscl_chunk_i<<<(unsigned)((E.ncol[0] * E.par.npv * 32 + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[0]);
-    k_recon_mx<0, true><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  } else {
-    k_recon_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  }
+  k_recon_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
   k_flux_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
   if (march) k_muscl_march<1><<<(unsigned)((E.ncol[1] * E.par.npv + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[1]);
   if (march) k_recon_mx<1, true><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);

@@ -159,7 +159,8 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const df64* nv, c
   const float nvf[3] = {nv[0].hi, nv[1].hi, nv[2].hi};
   const float dlf = sqrtf(nvf[0] * nvf[0] + nvf[1] * nvf[1] + nvf[2] * nvf[2]);
   if (dlf == 0.0f) {
-    for (int k = 0; k < npv; ++k) fx[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NPVM; ++k) if (k < npv) fx[k] = 0.0f;
     return;
   }
   df64 fd[NPVM];
@@ -215,11 +216,13 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const df64* nv, c
       }
       float df4 = au * (rr * dH + drho * hlf - dp) + du * rrho * ravg_ht + dpp * uuu;
       fd[4] = half * (mL * HL + mR * HR - dff(dlf * df4));
-      for (int k = 5; k < npv; ++k) {
+#pragma unroll
+      for (int k = 5; k < NPVM; ++k) if (k < npv) {
         float df = au * (rr * (pr[k] - pl[k]) + drho * pl[k]) + du * rrho * ravg_s[k];
         fd[k] = half * (mL * dff(pl[k]) + mR * dff(pr[k]) - dff(dlf * df));
       }
-      for (int k = 0; k < npv; ++k) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
+#pragma unroll
+      for (int k = 0; k < NPVM; ++k) if (k < npv) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
       return;
     }
     // Roe-M
@@ -247,11 +250,13 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const df64* nv, c
     dq[0] = drho;
     for (int k = 1; k <= 3; ++k) dq[k] = rr * du3[k - 1] + drho * ulf[k - 1];
     dq[4] = rr * dH + drho * hlf;
-    for (int k = 5; k < npv; ++k) dq[k] = rr * (pr[k] - pl[k]) + drho * pl[k];
+#pragma unroll
+    for (int k = 5; k < NPVM; ++k) if (k < npv) dq[k] = rr * (pr[k] - pl[k]) + drho * pl[k];
     bdq[0] = dq[0] - ff * dp / rc2 / fmid;
     for (int k = 1; k <= 3; ++k) bdq[k] = bdq[0] * ravg_u[k - 1] + rrho * du3[k - 1];
     bdq[4] = bdq[0] * ravg_ht + rrho * dH;
-    for (int k = 5; k < npv; ++k) bdq[k] = bdq[0] * ravg_s[k] + rrho * (pr[k] - pl[k]);
+#pragma unroll
+    for (int k = 5; k < NPVM; ++k) if (k < npv) bdq[k] = bdq[0] * ravg_s[k] + rrho * (pr[k] - pl[k]);
     // central part (b1 F_L - b2 F_R) / (b1 - b2) in FP64
     // the weights b1 / (b1 - b2), b2 / (b1 - b2) in df64 from FP32 wave speeds (their
     // difference is exact in df64); fluxes times dl
@@ -265,13 +270,16 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const df64* nv, c
       fr[1 + q3] = mR * R.u[q3] + nv[q3] * dff(pr[0]);
     }
     fl[4] = mL * HL; fr[4] = mR * HR;
-    for (int k = 5; k < npv; ++k) { fl[k] = mL * dff(pl[k]); fr[k] = mR * dff(pr[k]); }
+#pragma unroll
+    for (int k = 5; k < NPVM; ++k) if (k < npv) { fl[k] = mL * dff(pl[k]); fr[k] = mR * dff(pr[k]); }
     const float wdiss = dlf * b1 * b2 / (b1 - b2);
-    for (int k = 0; k < npv; ++k)
-      fd[k] = w1 * fl[k] - w2 * fr[k] + dff(wdiss * (dq[k] - gg * bdq[k] / add));
+#pragma unroll
+    for (int k = 0; k < NPVM; ++k)
+      if (k < npv) fd[k] = w1 * fl[k] - w2 * fr[k] + dff(wdiss * (dq[k] - gg * bdq[k] / add));
     for (int q3 = 0; q3 < 3; ++q3)
       fd[1 + q3] += dff(dlf * gg * b1_du * b2_du * rrho * dun * nf[q3] / aaa / (b1_du - b2_du));
-    for (int k = 0; k < npv; ++k) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
+#pragma unroll
+    for (int k = 0; k < NPVM; ++k) if (k < npv) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
     return;
   }
   // AUSM family: the interface velocity amid * M_1/2 = (u_L + u_R)/2 + small terms is
@@ -368,8 +376,10 @@ __device__ __forceinline__ void inviscid_flux_mx(const Par& c, const df64* nv, c
   fd[0] = ml + mr;
   for (int q3 = 0; q3 < 3; ++q3) fd[1 + q3] = ml * L.u[q3] + mr * R.u[q3] + dff(pmid) * nv[q3];
   fd[4] = ml * HL + mr * HR;
-  for (int k = 5; k < npv; ++k) fd[k] = ml * dff(pl[k]) + mr * dff(pr[k]);
-  for (int k = 0; k < npv; ++k) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
+#pragma unroll
+  for (int k = 5; k < NPVM; ++k) if (k < npv) fd[k] = ml * dff(pl[k]) + mr * dff(pr[k]);
+#pragma unroll
+  for (int k = 0; k < NPVM; ++k) if (k < npv) fx[k] = tof(fd[k] - mn * dfp(c.sc2[k]));
 }
 
 }  // namespace cfd
