@@ -767,7 +767,7 @@ __device__ void csf_cell(const DevPtr& d, long long g, long long sj, long long s
 // gravity and the surface-tension sources (a separate instantiation, so that the plain kernel carries none of their
 // code)
 template <bool MX, bool REC = true, bool XS = false>
-__global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= d.nint) return;
   int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
@@ -840,6 +840,67 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
   for (int v = 0; v < NPVM; ++v) pv2[v] = (v < npv) ? d.pv[v * n + g] : 0.0;
   for (int v = 0; v < NDV; ++v) dv[v] = d.dv[v * n + g];
   const double vol = d.gm[GM_GRD * n + g];
+  // the FP64 sources first (the dual-time source, the extended sources): after them the
+  // mixed form needs only the FP32 copies of the state
+  if (c.nsteady >= 1) {
+    double bb = (c.nsteady == 1) ? 1.0 : 0.75;
+    const double vdt = vol / c.dt_phy;
+    double fx[NPVM];
+    fx[0] = dv[0];
+    fx[1] = dv[0] * pv2[1]; fx[2] = dv[0] * pv2[2]; fx[3] = dv[0] * pv2[3];
+    fx[4] = dv[0] * (dv[1] + 0.5 * (pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3])) - (pv2[0] + c.pref);
+#pragma unroll
+    for (int v = 5; v < NPVM; ++v) fx[v] = dv[0] * pv2[v];
+#pragma unroll
+    for (int v = 0; v < NPVM; ++v) {
+      if (v >= npv) continue;
+      double q1 = d.qq[v * n + g], q2 = d.qq[(npv + v) * n + g];
+      double s = (double)c.nsteady * (bb * fx[v] - q1) + 0.5 * ((double)c.nsteady - 1.0) * q2;
+      res[v] = res[v] - s * vdt;
+    }
+  }
+  if (XS && c.gravity) {
+    // gravity%getgravitysource (src/gravity_module.f90:110-131) at the residual's time
+    double a[3];
+    gravity_at(d.grav, bc_time(d, c), a);
+    const double rv = dv[0] * vol;
+    for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] + rv * a[e];
+    res[4] = res[4] + rv * (a[0] * pv2[1] + a[1] * pv2[2] + a[2] * pv2[3]);
+  }
+  if (XS && c.rot) {
+    // rotation%getrotationsource (src/rotation_module.f90:75-97), subtracted
+    // (src/rhs_module.f90:600-605): rho vol (2 omega x u + omega x (omega x r))
+    const double* w = c.omega;
+    double r[3];
+    for (int e = 0; e < 3; ++e) r[e] = d.gm[(GM_GRD + 1 + e) * n + g];
+    const double cor[3] = {2.0 * (w[1] * pv2[3] - w[2] * pv2[2]), 2.0 * (w[2] * pv2[1] - w[0] * pv2[3]),
+                           2.0 * (w[0] * pv2[2] - w[1] * pv2[1])};
+    const double cen[3] = {w[0] * (w[1] * r[1] + w[2] * r[2]) - r[0] * (w[1] * w[1] + w[2] * w[2]),
+                           w[1] * (w[0] * r[0] + w[2] * r[2]) - r[1] * (w[0] * w[0] + w[2] * w[2]),
+                           w[2] * (w[0] * r[0] + w[1] * r[1]) - r[2] * (w[0] * w[0] + w[1] * w[1])};
+    for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] - dv[0] * vol * (cor[e] + cen[e]);
+  }
+  if (XS && c.csf) {
+    double cs[5];
+    csf_cell(d, g, sj, sk, vol, pv2, cs);
+    for (int q = 0; q < 5; ++q) res[q] = res[q] + cs[q];
+    for (int e = 0; e < 3; ++e) d.csf[e * n + g] = cs[1 + e];
+  }
+  // the mixed form's FP32 copies of the state, made once (its cavitation source, diagonal
+  // block and tile record read them), and its sources' FP32 implicit coefficients, kept in
+  // registers for the diagonal block
+  float p2f[NPVM], dvf[NDV], tvf[3] = {0.0f, 0.0f, 0.0f};
+  float icf[4] = {0.0f, 0.0f, 0.0f, 0.0f}, itf[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  if (MX) {
+#pragma unroll
+    for (int q = 0; q < NPVM; ++q) p2f[q] = (float)pv2[q];
+#pragma unroll
+    for (int q = 0; q < NDV; ++q) dvf[q] = (float)dv[q];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      if (q < c.ntv) tvf[q] = (float)d.tv[q * n + g];
+  }
+  const float volf = MX ? d.gmf[GM_GRD * n + g] : 0.0f;
   if (c.ncav) {
     if (MX) {
       // FP32 source (its rates reach the residual to ~1e-7 of their size) with the
@@ -850,12 +911,9 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
         if (c.ncav == 5) sat[1] = h2o_tww(pv2[0] + c.pref);
         else sat[0] = h2o_pww(pv2[4]);
       }
-      float p2f[NPVM], dvf[NDV];
-      for (int q = 0; q < NPVM; ++q) p2f[q] = (float)pv2[q];
-      for (int q = 0; q < NDV; ++q) dvf[q] = (float)dv[q];
       const CavOutT<float> o = cavsource_t<float>(c, p2f, dvf, vol, (float)c.uref, (float)c.c_v, (float)c.c_c, sat);
       res[5] = res[5] + (double)o.r_v - (double)o.r_c;
-      for (int q = 0; q < 4; ++q) d.icav[q * n + g] = o.icav[q];
+      for (int q = 0; q < 4; ++q) { d.icav[q * n + g] = o.icav[q]; icf[q] = o.icav[q]; }
       d.rcav[g] = o.r_c;
       d.rcav[n + g] = o.r_v;
     } else {
@@ -870,12 +928,7 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
     // cell-centred gradients of u, v, w, k, omega (turbsource kwsst, :269-383)
     const long long nbr[6] = {g - 1, g + 1, g - sj, g + sj, g - sk, g + sk};
     const int gv[5] = {1, 2, 3, 7, 8};
-    double tv[3];
-    for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
     const double c23 = 2.0 / 3.0;
-    const double kk = pv2[7], oo = pv2[8];
-    const double y5 = d.gm[(GM_GRD + 4) * n + g];
-    SstOut<double> so;
     if (MX) {
       // FP32 on the gauge shadow: differences of u - U are exact where u's are not
       float faf[6][3];
@@ -885,7 +938,7 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
         faf[4][q] = d.gmf[(GM_TX + q) * n + g - sk]; faf[5][q] = d.gmf[(GM_TX + q) * n + g];
       }
       float grf[5][3];
-      const float ivf = 1.0f / d.gmf[GM_GRD * n + g];
+      const float ivf = 1.0f / volf;
       for (int q = 0; q < 5; ++q) {
         const float* P = d.pvf + gv[q] * n;
         const float c0 = P[g];
@@ -896,11 +949,35 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
                        vv[0] * faf[0][e] - vv[2] * faf[2][e] - vv[4] * faf[4][e]) * ivf;
       }
       const double hmax = (XS && c.ides) ? grid_hmax<float>(faf, vol) : 0.0;
-      const SstOut<float> sf = sst_source_f(grf, (float)kk, (float)oo, (float)dv[0], (float)tv[0], (float)tv[2],
-                                            (float)y5, (float)vol, XS ? c.ides : 0, hmax);
-      so.r7 = sf.r7; so.r8 = sf.r8; so.prod = sf.prod; so.dest = sf.dest; so.div = sf.div; so.pkw = sf.pkw;
-      so.bigf = sf.bigf; so.talpha = sf.talpha; so.tbeta = sf.tbeta; so.strain = sf.strain;
+      const float kf = p2f[7], of = p2f[8], rho = dvf[0];
+      const SstOut<float> sf = sst_source_f(grf, kf, of, rho, tvf[0], tvf[2], d.gmf[(GM_GRD + 4) * n + g], volf,
+                                            XS ? c.ides : 0, hmax);
+      res[7] = res[7] + (double)sf.r7;
+      res[8] = res[8] + (double)sf.r8;
+      // the implicit coefficients and the omega bound of the update: FP32
+      const float pf = sf.prod, df_ = sf.dest, dvf_ = sf.div, pkf = sf.pkw, bf = sf.bigf;
+      const float taf = sf.talpha, tbf = sf.tbeta;
+      d.ocut[g] = (double)sqrtf(sf.strain - (2.0f / 3.0f) * dvf_ * dvf_);
+      const float ki = 1.0f / kf, oi = 1.0f / of, ei = 1.0f / tvf[2];
+      const float dpdk = pf * ki;
+      const float dpdo = -((pf + (2.0f / 3.0f) * rho * kf * dvf_) * oi);
+      const float it0 = dpdk - df_ * ki, it1 = dpdo - df_ * oi, it2 = 0.0f;
+      const float it3 = taf * rho * ei * dpdo + taf * rho * ei * pf * oi - 2.0f * tbf * rho * of -
+                        1.712f * (1.0f - bf) * rho * oi * oi * pkf;
+      // the signs of the block's eigenvalues 0.5 tr +- sqrt(0.25 tr^2 - det): with it2 = 0
+      // these are max(it0, it3) and min(it0, it3).  Taken from those directly: in FP32 the
+      // difference 0.5 tr - sqrt(..) cancels catastrophically next to walls, where omega
+      // makes it3 ~ 1e12 against it0 ~ 1e4, and its sign comes out at random.
+      const float l1 = copysignf(1.0f, fmaxf(it0, it3)), l2 = copysignf(1.0f, fminf(it0, it3));
+      const float f1 = (1.0f - 0.5f * (1.0f - l1)) - 0.5f * (1.0f - l1);
+      const float f2 = (1.0f - 0.5f * (1.0f - l2)) - 0.5f * (1.0f - l2);
+      itf[0] = it0 * f1; itf[1] = it1 * f1; itf[2] = it2 * f2; itf[3] = it3 * f2;
+      for (int q = 0; q < 4; ++q) d.itt[q * n + g] = itf[q];
     } else {
+      double tv[3];
+      for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
+      const double kk = pv2[7], oo = pv2[8];
+      const double y5 = d.gm[(GM_GRD + 4) * n + g];
       double fa[6][3];
       for (int q = 0; q < 3; ++q) {
         fa[0][q] = d.gm[(GM_CX + q) * n + g - 1]; fa[1][q] = d.gm[(GM_CX + q) * n + g];
@@ -918,32 +995,11 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
           gr[q][e] = (v2 * fa[1][e] + v4 * fa[3][e] + v6 * fa[5][e] - v1 * fa[0][e] - v3 * fa[2][e] - v5 * fa[4][e]) * ivol;
       }
       const double hmax = (XS && c.ides) ? grid_hmax<double>(fa, vol) : 0.0;
-      so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, XS ? c.ides : 0, hmax);
-    }
-    res[7] = res[7] + so.r7;
-    res[8] = res[8] + so.r8;
-    const double prod = so.prod, dest = so.dest, div = so.div, pkw = so.pkw, bigf = so.bigf;
-    const double talpha = so.talpha, tbeta = so.tbeta;
-    if (MX) {
-      // the implicit coefficients and the omega bound of the update: FP32
-      const float pf = (float)prod, df_ = (float)dest, dvf = (float)div, pkf = (float)pkw, bf = (float)bigf;
-      const float taf = (float)talpha, tbf = (float)tbeta, rho = (float)dv[0], kf = (float)kk, of = (float)oo;
-      d.ocut[g] = (double)sqrtf((float)so.strain - (2.0f / 3.0f) * dvf * dvf);
-      const float ki = 1.0f / kf, oi = 1.0f / of, ei = 1.0f / (float)tv[2];
-      const float dpdk = pf * ki;
-      const float dpdo = -((pf + (2.0f / 3.0f) * rho * kf * dvf) * oi);
-      const float it0 = dpdk - df_ * ki, it1 = dpdo - df_ * oi, it2 = 0.0f;
-      const float it3 = taf * rho * ei * dpdo + taf * rho * ei * pf * oi - 2.0f * tbf * rho * of -
-                        1.712f * (1.0f - bf) * rho * oi * oi * pkf;
-      // the signs of the block's eigenvalues 0.5 tr +- sqrt(0.25 tr^2 - det): with it2 = 0
-      // these are max(it0, it3) and min(it0, it3).  Taken from those directly: in FP32 the
-      // difference 0.5 tr - sqrt(..) cancels catastrophically next to walls, where omega
-      // makes it3 ~ 1e12 against it0 ~ 1e4, and its sign comes out at random.
-      const float l1 = copysignf(1.0f, fmaxf(it0, it3)), l2 = copysignf(1.0f, fminf(it0, it3));
-      const float f1 = (1.0f - 0.5f * (1.0f - l1)) - 0.5f * (1.0f - l1);
-      const float f2 = (1.0f - 0.5f * (1.0f - l2)) - 0.5f * (1.0f - l2);
-      d.itt[g] = it0 * f1; d.itt[n + g] = it1 * f1; d.itt[2 * n + g] = it2 * f2; d.itt[3 * n + g] = it3 * f2;
-    } else {
+      const SstOut<double> so = sst_source<double>(gr, kk, oo, dv[0], tv[0], tv[2], y5, vol, XS ? c.ides : 0, hmax);
+      res[7] = res[7] + so.r7;
+      res[8] = res[8] + so.r8;
+      const double prod = so.prod, dest = so.dest, div = so.div, pkw = so.pkw, bigf = so.bigf;
+      const double talpha = so.talpha, tbeta = so.tbeta;
       d.ocut[g] = sqrt(so.strain - c23 * so.div * so.div);
       const double ki = 1.0 / kk, oi = 1.0 / oo, ei = 1.0 / tv[2];
       double dpdk = prod * ki;
@@ -985,51 +1041,8 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
     ke_source<double>(gr, gsk, pv2[7], pv2[8], dv[0], d.tv[g], d.tv[2 * n + g], vol, rk, itk);
     res[7] = res[7] + rk[0];
     res[8] = res[8] + rk[1];
-    for (int q = 0; q < 4; ++q) d.itt[q * n + g] = itk[q];
+    for (int q = 0; q < 4; ++q) { d.itt[q * n + g] = itk[q]; itf[q] = (float)itk[q]; }
     d.ocut[g] = 0.0;
-  }
-  if (c.nsteady >= 1) {
-    double bb = (c.nsteady == 1) ? 1.0 : 0.75;
-    double fx[NPVM];
-    fx[0] = dv[0];
-    fx[1] = dv[0] * pv2[1]; fx[2] = dv[0] * pv2[2]; fx[3] = dv[0] * pv2[3];
-    fx[4] = dv[0] * (dv[1] + 0.5 * (pv2[1] * pv2[1] + pv2[2] * pv2[2] + pv2[3] * pv2[3])) - (pv2[0] + c.pref);
-#pragma unroll
-    for (int v = 5; v < NPVM; ++v) fx[v] = dv[0] * pv2[v];
-#pragma unroll
-    for (int v = 0; v < NPVM; ++v) {
-      if (v >= npv) continue;
-      double q1 = d.qq[v * n + g], q2 = d.qq[(npv + v) * n + g];
-      double s = (double)c.nsteady * (bb * fx[v] - q1) + 0.5 * ((double)c.nsteady - 1.0) * q2;
-      res[v] = res[v] - s * vol / c.dt_phy;
-    }
-  }
-  if (XS && c.gravity) {
-    // gravity%getgravitysource (src/gravity_module.f90:110-131) at the residual's time
-    double a[3];
-    gravity_at(d.grav, bc_time(d, c), a);
-    const double rv = dv[0] * vol;
-    for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] + rv * a[e];
-    res[4] = res[4] + rv * (a[0] * pv2[1] + a[1] * pv2[2] + a[2] * pv2[3]);
-  }
-  if (XS && c.rot) {
-    // rotation%getrotationsource (src/rotation_module.f90:75-97), subtracted
-    // (src/rhs_module.f90:600-605): rho vol (2 omega x u + omega x (omega x r))
-    const double* w = c.omega;
-    double r[3];
-    for (int e = 0; e < 3; ++e) r[e] = d.gm[(GM_GRD + 1 + e) * n + g];
-    const double cor[3] = {2.0 * (w[1] * pv2[3] - w[2] * pv2[2]), 2.0 * (w[2] * pv2[1] - w[0] * pv2[3]),
-                           2.0 * (w[0] * pv2[2] - w[1] * pv2[1])};
-    const double cen[3] = {w[0] * (w[1] * r[1] + w[2] * r[2]) - r[0] * (w[1] * w[1] + w[2] * w[2]),
-                           w[1] * (w[0] * r[0] + w[2] * r[2]) - r[1] * (w[0] * w[0] + w[2] * w[2]),
-                           w[2] * (w[0] * r[0] + w[1] * r[1]) - r[2] * (w[0] * w[0] + w[1] * w[1])};
-    for (int e = 0; e < 3; ++e) res[1 + e] = res[1 + e] - dv[0] * vol * (cor[e] + cen[e]);
-  }
-  if (XS && c.csf) {
-    double cs[5];
-    csf_cell(d, g, sj, sk, vol, pv2, cs);
-    for (int q = 0; q < 5; ++q) res[q] = res[q] + cs[q];
-    for (int e = 0; e < 3; ++e) d.csf[e * n + g] = cs[1 + e];
   }
 #pragma unroll
   for (int v = 0; v < NPVM; ++v)
@@ -1041,13 +1054,10 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
     double r[3];
     for (int e = 0; e < 3; ++e) r[e] = d.gm[(GM_GRD + 1 + e) * n + g];
     dv[1] = dv[1] - rot_q(c, r);
+    if (MX) dvf[1] = (float)dv[1];
   }
   // ---- LU-SGS coefficients of this cell (diagonal block, spectral radii, beta, viscous
-  // term), written with its state and residual as the cell's sweep record at pos[g]
-  double tvc[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-  for (int q = 0; q < 3; ++q)
-    if (q < c.ntv) tvc[q] = d.tv[q * n + g];
+  // term), written with its state and residual as the cell's sweep record
   // face vectors cx1, cx2, ex1, ex2, tx1, tx2: FP64, or (mixed form) their FP32 copies
   double fc[18];
   float fcf[18];
@@ -1059,87 +1069,69 @@ __global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c) {
       else fc[3 * m + q] = d.gm[o6[m]];
     }
   }
-  double ic[4] = {0, 0, 0, 0}, it4[4] = {0, 0, 0, 0};
-  if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
-  if (c.iturb >= -1) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
-  Diag D;
-  DiagT<float> Df;
-  double evis;
-  float pvf[NPVM], dvf[NDV];
-  if (MX) {
-    // the diagonal block in FP32: it shapes the implicit operator only (the sweeps' FP32
-    // corrections use it as well), and its closed-form inverse gives x0 below
-    for (int q = 0; q < NPVM; ++q) pvf[q] = (q < npv) ? (float)pv2[q] : 0.0f;
-    for (int q = 0; q < NDV; ++q) dvf[q] = (float)dv[q];
-    float tvf[3] = {(float)tvc[0], (float)tvc[1], (float)tvc[2]};
-    float lam_fs[2];
-    diag_spectral_f(c, pvf, dvf[5], fcf, lam_fs);
-    const float evf = eigenvis_f(c, dvf, tvf);
-    evis = (double)evf;
-    float icf[4], itf[4];
-    for (int q = 0; q < 4; ++q) { icf[q] = (float)ic[q]; itf[q] = (float)it4[q]; }
-    diag_prepare_t<float>(c, pvf, dvf, evf, fcf, (float)vol, (float)d.dt[g], icf, itf, Df, lam_fs);
-  } else {
-    evis = eigenvis_of(c, dv, tvc);
-    diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D);
-  }
-  double o[NREC];
-  for (int q = 0; q < NREC; ++q) o[q] = 0.0;
   const int pvi[7] = {1, 2, 3, 5, 6, 7, 8};
   const int dvi[10] = {0, 1, 6, 7, 8, 9, 10, 11, 12, 13};
-  for (int q = 0; q < 7; ++q) o[REC_PV + q] = (pvi[q] < npv) ? pv2[pvi[q]] : 0.0;
-  for (int q = 0; q < 10; ++q) o[REC_DV + q] = dv[dvi[q]];
-  if (!MX) diag_to_array(D, o + REC_DIAG);
-  if (MX) {
-    // the spectral radii only scale the implicit operator: FP32
-    for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = (double)face_spectral<float>(c, fcf + 3 * q, pvf, dvf);
-  } else {
-    for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = face_spectral<double>(c, fc + 3 * q, pv2, dv);
-  }
-  // beta = 1/sndp2 - 1/c2 + drho/dp = D.rr - (D.b1 - 1) drho/dp
-  if (MX) o[REC_BETA] = (double)(Df.rr - (Df.b1 - 1.0f) * dvf[6]);
-  else o[REC_BETA] = D.rr - (D.b1 - 1.0) * dv[6];
-  // (the mixed form's sweeps read the face vectors and this viscous term from the FP32
-  // records)
-  o[REC_EVV] = MX ? (double)(2.0f * (float)evis / (float)vol) : 2.0 * evis / vol;
-  for (int e = 0; e < 3; ++e) {
-    if (MX) { o[REC_FACE + e] = fcf[3 + e]; o[REC_FACE + 3 + e] = fcf[9 + e]; o[REC_FACE + 6 + e] = fcf[15 + e]; }
-    else { o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e]; }
-  }
   if constexpr (MX) {
+    // the diagonal block in FP32: it shapes the implicit operator only (the sweeps' FP32
+    // corrections use it as well), and its closed-form inverse gives x0 below
+    DiagT<float> Df;
+    float lam_fs[2];
+    diag_spectral_f(c, p2f, dvf[5], fcf, lam_fs);
+    const float evf = eigenvis_f(c, dvf, tvf);
+    diag_prepare_t<float>(c, p2f, dvf, evf, fcf, volf, (float)d.dt[g], icf, itf, Df, lam_fs);
     // the cell's tile record (FP32) and the forward sweep's own part x0 = D^-1 res, at its
     // tile slot: consecutive i are consecutive slots.  x0 is an FP32 solve of the FP64
     // residual (rounded once): an inexact step of the iteration, not of its fixed point.
     const long long sl = d.pos[g];
     float rf[NPVM], xf[NPVM];
+#pragma unroll
     for (int v = 0; v < NPVM; ++v) { rf[v] = (v < npv) ? (float)res[v] : 0.0f; xf[v] = 0.0f; }
-    diag_solve_t<float>(c, Df, pvf, dvf, rf, xf);
+    diag_solve_t<float>(c, Df, p2f, dvf, rf, xf);
     float* R = d.trf + trf_at(sl, 0);
 #pragma unroll
     for (int v = 0; v < NPVM; ++v)
-      if (v < npv) { d.tq[tq_at(sl, v)] = (double)xf[v]; R[(TR_X + v) * TILE_SLOTS] = xf[v]; }
-    for (int q = 0; q < 7; ++q) R[(TR_PV + q) * TILE_SLOTS] = (float)o[REC_PV + q];
-    for (int q = 0; q < 10; ++q) R[(TR_DV + q) * TILE_SLOTS] = (float)o[REC_DV + q];
-    R[TR_EVV * TILE_SLOTS] = (float)o[REC_EVV];
+      if (v < npv) { d.tq[tq_at(sl, v)] = xf[v]; R[(TR_X + v) * TILE_SLOTS] = xf[v]; }
+#pragma unroll
+    for (int q = 0; q < 7; ++q) R[(TR_PV + q) * TILE_SLOTS] = (pvi[q] < npv) ? p2f[pvi[q]] : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 10; ++q) R[(TR_DV + q) * TILE_SLOTS] = dvf[dvi[q]];
+    // (the sweeps form beta = rr - (b1 - 1) drho/dp from the block)
+    R[TR_EVV * TILE_SLOTS] = 2.0f * evf / volf;
     {
-      double od[PREP_DIAG];
-      Diag Dd;
-      Dd.a = Df.a; Dd.b1 = Df.b1; Dd.i_b1 = Df.i_b1; Dd.ss = Df.ss; Dd.rr = Df.rr; Dd.cross = Df.cross;
-      Dd.cross1 = Df.cross1; Dd.cross2 = Df.cross2; Dd.ssy1 = Df.ssy1; Dd.ssy2 = Df.ssy2; Dd.ssh = Df.ssh;
-      Dd.aaa1 = Df.aaa1; Dd.aaa2 = Df.aaa2; Dd.mm = Df.mm; Dd.tt = Df.tt;
-      for (int q = 0; q < 4; ++q) { Dd.c[q] = Df.c[q]; Dd.t[q] = Df.t[q]; }
-      diag_to_array(Dd, od);
-      for (int q = 0; q < PREP_DIAG; ++q) R[(TR_DIAG + q) * TILE_SLOTS] = (float)od[q];
+      float od[PREP_DIAG];
+      diag_to_array(Df, od);
+#pragma unroll
+      for (int q = 0; q < PREP_DIAG; ++q) R[(TR_DIAG + q) * TILE_SLOTS] = od[q];
     }
+    // the spectral radii only scale the implicit operator: FP32
     for (int dir = 0; dir < 3; ++dir) {
       for (int e = 0; e < 3; ++e) {
         R[(TR_FACEP + 3 * dir + e) * TILE_SLOTS] = fcf[6 * dir + 3 + e];   // cx2, ex2, tx2
         R[(TR_FACEM + 3 * dir + e) * TILE_SLOTS] = fcf[6 * dir + e];       // cx1, ex1, tx1
       }
-      R[(TR_SPECP + dir) * TILE_SLOTS] = (float)o[REC_SPEC + 2 * dir + 1];
-      R[(TR_SPECM + dir) * TILE_SLOTS] = (float)o[REC_SPEC + 2 * dir];
+      R[(TR_SPECP + dir) * TILE_SLOTS] = face_spectral<float>(c, fcf + 3 * (2 * dir + 1), p2f, dvf);
+      R[(TR_SPECM + dir) * TILE_SLOTS] = face_spectral<float>(c, fcf + 3 * (2 * dir), p2f, dvf);
     }
   } else {
+    double tvc[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < 3; ++q)
+      if (q < c.ntv) tvc[q] = d.tv[q * n + g];
+    double ic[4] = {0, 0, 0, 0}, it4[4] = {0, 0, 0, 0};
+    if (c.ncav) for (int q = 0; q < 4; ++q) ic[q] = d.icav[q * n + g];
+    if (c.iturb >= -1) for (int q = 0; q < 4; ++q) it4[q] = d.itt[q * n + g];
+    Diag D;
+    const double evis = eigenvis_of(c, dv, tvc);
+    diag_prepare(c, pv2, dv, evis, fc, vol, d.dt[g], ic, it4, D);
+    double o[NREC];
+    for (int q = 0; q < NREC; ++q) o[q] = 0.0;
+    for (int q = 0; q < 7; ++q) o[REC_PV + q] = (pvi[q] < npv) ? pv2[pvi[q]] : 0.0;
+    for (int q = 0; q < 10; ++q) o[REC_DV + q] = dv[dvi[q]];
+    diag_to_array(D, o + REC_DIAG);
+    for (int q = 0; q < 6; ++q) o[REC_SPEC + q] = face_spectral<double>(c, fc + 3 * q, pv2, dv);
+    // beta = 1/sndp2 - 1/c2 + drho/dp = D.rr - (D.b1 - 1) drho/dp
+    o[REC_BETA] = D.rr - (D.b1 - 1.0) * dv[6];
+    o[REC_EVV] = 2.0 * evis / vol;
+    for (int e = 0; e < 3; ++e) { o[REC_FACE + e] = fc[3 + e]; o[REC_FACE + 3 + e] = fc[9 + e]; o[REC_FACE + 6 + e] = fc[15 + e]; }
     for (int v = 0; v < npv; ++v) o[REC_RES + v] = res[v];
     const long long nint = d.nint, tp = d.pos[g];
     for (int q = 0; q < NREC; ++q) d.rec[q * nint + tp] = o[q];
@@ -1586,7 +1578,7 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
         old[v] = p[v] = 0.0;
         if (v >= npv) continue;
         old[v] = d.pv[v * n + g];
-        p[v] = old[v] + (MX ? d.tq[tq_at(pq, v)] + (double)d.tyf[tq_at(pq, v)] + (double)d.tyb[tq_at(pq, v)]
+        p[v] = old[v] + (MX ? (double)d.tq[tq_at(pq, v)] + (double)d.tyf[tq_at(pq, v)] + (double)d.tyb[tq_at(pq, v)]
                             : d.dqs[v * d.nint + pq]);
       }
     } else {
@@ -1620,12 +1612,8 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
       p[7] = fmax(p[7], 1.0e-16);
       p[8] = fmax(fmax(p[8], 1.0e-16), d.ocut[g]);
     }
-    double dv[NDV], tv[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-    for (int v = 0; v < 3; ++v)
-      if (v < c.ntv) tv[v] = d.tv[v * n + g];
-    if (MX) deteos_split(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
-    else deteos<false>(c.fluid, c.with_prop, p[0] + c.pref, p[4], p[5], p[6], dv, tv, &d.sc->snd2_fallbacks);
+    // the state, its change norms and the largest |dp| before the EOS, so that only the EOS's
+    // inputs stay live across it
 #pragma unroll
     for (int v = 0; v < NPVM; ++v) {
       if (v >= npv) continue;
@@ -1634,6 +1622,15 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
       sq_[v] += df * df;
       if (!isfinite(p[v])) bad = 1;
     }
+    double dp = fabs(old[0] - p[0]);
+    if (dp > dpmax) { dpmax = dp; dpidx = t; }   // t increases: ties keep the first cell
+    const double pe = p[0] + c.pref, te = p[4], y1 = p[5], y2 = p[6];
+    double dv[NDV], tv[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+      if (v < c.ntv) tv[v] = d.tv[v * n + g];
+    if (MX) deteos_split(c.fluid, c.with_prop, pe, te, y1, y2, dv, tv, &d.sc->snd2_fallbacks);
+    else deteos<false>(c.fluid, c.with_prop, pe, te, y1, y2, dv, tv, &d.sc->snd2_fallbacks);
     for (int v = 0; v < NDV; ++v) {
       d.dv[v * n + g] = dv[v];
       if (!isfinite(dv[v])) bad = 1;
@@ -1641,8 +1638,6 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
 #pragma unroll
     for (int v = 0; v < 3; ++v)
       if (v < c.ntv) d.tv[v * n + g] = tv[v];
-    double dp = fabs(old[0] - p[0]);
-    if (dp > dpmax) { dpmax = dp; dpidx = t; }   // t increases: ties keep the first cell
   }
   if (bad) atomicExch(&d.sc->nonfinite, 1);
   // per-CTA partial sums (deterministic order: warp shuffles then warps in order)
@@ -2342,7 +2337,13 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    E.red_grid = (int)std::min<long long>(nblk_of(E.nint, 128), (long long)std::max(nsm, 1) * 8);
+    // the update's CTAs all resident at once (its grid-stride loop leaves no partial last
+    // wave), at most 8 per SM
+    int per = 0;
+    if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_update<true>, 128, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_update<false>, 128, 0);
+    per = std::min(std::max(per, 1), 8);
+    E.red_grid = (int)std::min<long long>(nblk_of(E.nint, 128), (long long)std::max(nsm, 1) * per);
   }
   CFD_CUDA(cudaMalloc(&E.d.partial, (size_t)E.red_grid * (NPVM + 2) * 8));
   // reference state: deteos at (pref, tref, y1ref, y2ref), then config%setref

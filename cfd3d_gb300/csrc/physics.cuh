@@ -1468,7 +1468,8 @@ __device__ __forceinline__ void diag_solve(const Par& c, const Diag& D, const do
 // the Diag fields as an array (the sweep record's diagonal part)
 constexpr int PREP_DIAG = 23;
 
-__device__ __forceinline__ void diag_to_array(const Diag& D, double* o) {
+template <class R>
+__device__ __forceinline__ void diag_to_array(const DiagT<R>& D, R* o) {
   o[0] = D.a; o[1] = D.b1; o[2] = D.i_b1; o[3] = D.ss; o[4] = D.rr; o[5] = D.cross; o[6] = D.cross1;
   o[7] = D.cross2; o[8] = D.ssy1; o[9] = D.ssy2; o[10] = D.ssh; o[11] = D.aaa1; o[12] = D.aaa2; o[13] = D.mm;
   for (int q = 0; q < 4; ++q) { o[14 + q] = D.c[q]; o[19 + q] = D.t[q]; }

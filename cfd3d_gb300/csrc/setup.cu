@@ -1002,7 +1002,7 @@ bool setup_tiles(Engine& E) {
   if (cudaMalloc(&E.d_tiles, ntile * sizeof(TileDesc)) != cudaSuccess ||
       cudaMalloc(&E.d_pos, E.ncell * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&E.d.trf, (size_t)ntile * NTR * TILE_SLOTS * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&E.d.tq, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&E.d.tq, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&E.d.tyf, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&E.d.tyb, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&E.d.tin, (size_t)ntile * NPVM * TILE_IN * sizeof(float)) != cudaSuccess ||
@@ -1013,7 +1013,7 @@ bool setup_tiles(Engine& E) {
   }
   cudaMemcpy(E.d_tiles, tiles.data(), ntile * sizeof(TileDesc), cudaMemcpyHostToDevice);
   cudaMemcpy(E.d_pos, pos.data(), E.ncell * sizeof(int), cudaMemcpyHostToDevice);
-  cudaMemset(E.d.tq, 0, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(double));
+  cudaMemset(E.d.tq, 0, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(float));
   cudaMemset(E.d.tyf, 0, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(float));
   cudaMemset(E.d.tyb, 0, (size_t)ntile * NPVM * TILE_SLOTS * sizeof(float));
   cudaMemset(E.d.trf, 0, (size_t)ntile * NTR * TILE_SLOTS * sizeof(float));
