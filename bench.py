@@ -409,7 +409,9 @@ def main():
     res0 = [eng.residual(n)["res"] for n in range(nb)] if prec == abi.MIXED else None
     for w in range(args.warmup):
         eng.iterate(1, w + 1, 0.0)
-    shapes = eng.autotune(3) if not args.no_autotune else None
+    if not args.no_autotune:
+        eng.autotune(3)
+    shapes = eng.launch_shapes()
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:
@@ -444,8 +446,9 @@ def main():
         "dtype": "f64" if prec == abi.FP64 else "f32+f64", "data": "synthetic",
         "config": {"workload": describe(case, ncell), "cells": ncell, "precision": args.precision, "blocks": nb,
                    "l2": "working set >> 129 MB L2 (no flush needed)", "parallelism": "replicas" if ws > 1 else "1 GPU",
-                   "launch_shapes": None if shapes is None else {"face_threads": shapes[0], "rhs_threads": shapes[1],
-                                                                 "sweep_ctas_per_sm": shapes[2]}},
+                   "launch_shapes": {"face_threads": shapes[0], "rhs_threads": shapes[1],
+                                     "sweep_ctas_per_sm": shapes[2], "face_residual_pipeline_groups": shapes[3],
+                                     "autotuned": not args.no_autotune}},
         "roofline": {"bound": "hbm", "achieved": achieved_it, "peak": peak, "unit": "GB/s", "frac": achieved_it / peak,
                      "peak_kind": peak_kind,
                      "traffic": ITER_TRAFFIC_PER_CELL * ncell if (prec == abi.MIXED and args.case == "large") else None,

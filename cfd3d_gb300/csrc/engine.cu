@@ -767,9 +767,15 @@ __device__ void csf_cell(const DevPtr& d, long long g, long long sj, long long s
 // gravity and the surface-tension sources (a separate instantiation, so that the plain kernel carries none of their
 // code)
 template <bool MX, bool REC = true, bool XS = false>
-__global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= d.nint) return;
+// The mixed form at 2 CTAs of 256 threads per SM: its residual is latency-bound (the FP64
+// pipe about a third busy), and the occupancy buys more than the registers' few spills
+// cost.  store_res: the residual, icav and itt planes are written (the residual query and
+// the explicit schemes read them); the mixed form's LU-SGS iteration keeps them in
+// registers, and only the sweep record and x0 carry them on.
+__global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c, long long t0, long long t1, int store_res) {
+  long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= t1) return;
+  const bool out = !(MX && REC) || store_res != 0;
   int b = find_block_interior(d.blk, d.nblk, t), i, j, k;
   const BlockGeom& B = d.blk[b];
   long long g = interior_cell(B, t - B.int_off, i, j, k);
@@ -913,7 +919,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
       }
       const CavOutT<float> o = cavsource_t<float>(c, p2f, dvf, vol, (float)c.uref, (float)c.c_v, (float)c.c_c, sat);
       res[5] = res[5] + (double)o.r_v - (double)o.r_c;
-      for (int q = 0; q < 4; ++q) { d.icav[q * n + g] = o.icav[q]; icf[q] = o.icav[q]; }
+      for (int q = 0; q < 4; ++q) { if (out) d.icav[q * n + g] = o.icav[q]; icf[q] = o.icav[q]; }
       d.rcav[g] = o.r_c;
       d.rcav[n + g] = o.r_v;
     } else {
@@ -972,7 +978,7 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
       const float f1 = (1.0f - 0.5f * (1.0f - l1)) - 0.5f * (1.0f - l1);
       const float f2 = (1.0f - 0.5f * (1.0f - l2)) - 0.5f * (1.0f - l2);
       itf[0] = it0 * f1; itf[1] = it1 * f1; itf[2] = it2 * f2; itf[3] = it3 * f2;
-      for (int q = 0; q < 4; ++q) d.itt[q * n + g] = itf[q];
+      if (out) for (int q = 0; q < 4; ++q) d.itt[q * n + g] = itf[q];
     } else {
       double tv[3];
       for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
@@ -1041,12 +1047,12 @@ __global__ void __launch_bounds__(256) k_rhs(DevPtr d, Par c) {
     ke_source<double>(gr, gsk, pv2[7], pv2[8], dv[0], d.tv[g], d.tv[2 * n + g], vol, rk, itk);
     res[7] = res[7] + rk[0];
     res[8] = res[8] + rk[1];
-    for (int q = 0; q < 4; ++q) { d.itt[q * n + g] = itk[q]; itf[q] = (float)itk[q]; }
+    for (int q = 0; q < 4; ++q) { if (out) d.itt[q * n + g] = itk[q]; itf[q] = (float)itk[q]; }
     d.ocut[g] = 0.0;
   }
 #pragma unroll
   for (int v = 0; v < NPVM; ++v)
-    if (v < npv) d.res[v * n + g] = res[v];
+    if (out && v < npv) d.res[v * n + g] = res[v];
   if constexpr (!REC) return;   // the explicit schemes need no sweep records
   if (c.rot) {
     // the implicit operator's enthalpy is the rothalpy (lhs%getenthalpy, jac%getenthalpy):
@@ -1878,28 +1884,70 @@ constexpr long long SWEEP_SPIN = 1ll << 22;
 
 // k_rhs in the instantiation of the form (mixed / FP64), the time integrator (sweep records
 // for LU-SGS) and the extended sources (DES length scale, gravity)
+// (over the interior cells of blocks [b0, b1))
 template <bool REC>
-void launch_rhs_rec(const Engine& E, cudaStream_t s, int T) {
+void launch_rhs_rec(const Engine& E, cudaStream_t s, int T, int b0, int b1, int store_res) {
   const Par& c = E.par;
-  const unsigned g = nblk_of(E.nint, T);
+  const int nb = (int)E.blk.size();
+  const long long t0 = E.blk[b0].int_off, t1 = (b1 < nb) ? E.blk[b1].int_off : E.nint;
+  const unsigned g = nblk_of(std::max<long long>(t1 - t0, 1), T);
   const bool xs = (c.iturb == 0 && c.ides != 0) || c.gravity != 0 || c.csf != 0 || c.rot != 0;
   if (c.mixed) {
-    if (xs) k_rhs<true, REC, true><<<g, T, 0, s>>>(E.d, c);
-    else k_rhs<true, REC, false><<<g, T, 0, s>>>(E.d, c);
+    if (xs) k_rhs<true, REC, true><<<g, T, 0, s>>>(E.d, c, t0, t1, store_res);
+    else k_rhs<true, REC, false><<<g, T, 0, s>>>(E.d, c, t0, t1, store_res);
   } else {
-    if (xs) k_rhs<false, REC, true><<<g, T, 0, s>>>(E.d, c);
-    else k_rhs<false, REC, false><<<g, T, 0, s>>>(E.d, c);
+    if (xs) k_rhs<false, REC, true><<<g, T, 0, s>>>(E.d, c, t0, t1, store_res);
+    else k_rhs<false, REC, false><<<g, T, 0, s>>>(E.d, c, t0, t1, store_res);
   }
 }
-void launch_rhs(const Engine& E, cudaStream_t s, int T, bool rec) {
-  if (rec) launch_rhs_rec<true>(E, s, T);
-  else launch_rhs_rec<false>(E, s, T);
+void launch_rhs(const Engine& E, cudaStream_t s, int T, bool rec, bool store_res, int b0 = 0, int b1 = -1) {
+  if (b1 < 0) b1 = (int)E.blk.size();
+  if (rec) launch_rhs_rec<true>(E, s, T, b0, b1, store_res ? 1 : 0);
+  else launch_rhs_rec<false>(E, s, T, b0, b1, store_res ? 1 : 0);
+}
+
+// The face stage and the residual of one pseudo-iteration.  The mixed form with more than
+// one group pipelines them over groups of consecutive blocks: the residual of group q runs on
+// st2 beside the face stage of group q + 1 on s (the face kernels keep the FP32 pipes busy,
+// the residual the FP64 pipe; a block's faces and residual touch only its own padded cells,
+// faces and tiles).  st2 forks from s and joins it again, so the stage is one unit of s.
+void launch_face_rhs(const Engine& E, cudaStream_t s, bool rec, bool store_res) {
+  const Par& c = E.par;
+  const int nb = (int)E.blk.size();
+  const int ng = std::min(std::max(E.pipe_groups, 1), std::min(nb, Engine::MAX_PIPE));
+  if (!c.mixed) {
+    launch_face_flux(E, s);
+    launch_rhs(E, s, E.tpb_rhs, rec, store_res);
+    return;
+  }
+  if (ng <= 1) {
+    launch_face_flux_mixed(E, s, 0, nb);
+    launch_rhs(E, s, E.tpb_rhs, rec, store_res);
+    return;
+  }
+  cudaEventRecord(E.pipe_ev[0], s);
+  cudaStreamWaitEvent(E.st2, E.pipe_ev[0], 0);
+  for (int q = 0; q < ng; ++q) {
+    const int b0 = (int)((long long)nb * q / ng), b1 = (int)((long long)nb * (q + 1) / ng);
+    launch_face_flux_mixed(E, s, b0, b1);
+    cudaEventRecord(E.pipe_ev[1 + q], s);
+    cudaStreamWaitEvent(E.st2, E.pipe_ev[1 + q], 0);
+    launch_rhs(E, E.st2, E.tpb_rhs, rec, store_res, b0, b1);
+  }
+  cudaEventRecord(E.pipe_ev[Engine::MAX_PIPE + 1], E.st2);
+  cudaStreamWaitEvent(s, E.pipe_ev[Engine::MAX_PIPE + 1], 0);
 }
 
 // launches of the face fluxes and the residual: the FP64 form's three face kernels, or the
 // mixed form's shadow, its reconstruction and flux kernels of each direction (with the j and
 // k faces' column reconstruction under MUSCL), and k_rhs
-int face_rhs_launches(const Par& c) { return c.mixed ? (8 + (c.nmuscl > 0 ? 2 : 0)) : 4; }
+int face_rhs_launches(const Engine& E) {
+  const Par& c = E.par;
+  if (!c.mixed) return 4;
+  const int nb = (int)E.blk.size();
+  const int ng = std::min(std::max(E.pipe_groups, 1), std::min(nb, Engine::MAX_PIPE));
+  return ng * (8 + (c.nmuscl > 0 ? 2 : 0));
+}
 
 // The boundary program -- the total-pressure pools, then faces + halos, edges, corners -- and,
 // with the surface-tension source, calvfg and setbc_vfg after it, as timeinteg calls them
@@ -1938,12 +1986,19 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
   stage(1);
   n += launch_boundary(E, s);
   stage(2);
-  if (c.mixed) launch_face_flux_mixed(E, s);
-  else launch_face_flux(E, s);
-  stage(3);
-  launch_rhs(E, s, E.tpb_rhs, c.timemethod == 3);
+  // (the residual planes are written when the residual is queried: full = false)
+  if (c.mixed && E.pipe_groups > 1) {
+    // pipelined: the stage's end only (its face and residual parts overlap)
+    launch_face_rhs(E, s, c.timemethod == 3, !full);
+    stage(3);
+  } else {
+    if (c.mixed) launch_face_flux_mixed(E, s, 0, (int)E.blk.size());
+    else launch_face_flux(E, s);
+    stage(3);
+    launch_rhs(E, s, E.tpb_rhs, c.timemethod == 3, !full);
+  }
   stage(4);
-  n += face_rhs_launches(c);
+  n += face_rhs_launches(E);
   if (!full) { E.launches_per_iter = n; return; }
   if (c.timemethod != 3) {
     // explicit Euler (one stage) or RK3 (three; the time step is taken at the first only):
@@ -1952,10 +2007,8 @@ void launch_iteration(Engine& E, bool full, cudaEvent_t* mark = nullptr) {
     for (int m = 1; m <= nstage; ++m) {
       if (m > 1) {
         n += launch_boundary(E, s);
-        if (c.mixed) launch_face_flux_mixed(E, s);
-        else launch_face_flux(E, s);
-        launch_rhs(E, s, E.tpb_rhs, false);
-        n += face_rhs_launches(c);
+        launch_face_rhs(E, s, false, true);
+        n += face_rhs_launches(E);
       }
       if (m == nstage) { stage(5); stage(6); }
       if (c.mixed) k_update<true, true><<<E.red_grid, T, 0, s>>>(d, c, m);
@@ -2277,6 +2330,8 @@ int cfd3d_create(const cfd3d_config* cfg, int nblocks, const cfd3d_block_desc* b
   E.ncell = off; E.nint = ioff;
   for (int q = 0; q < 3; ++q) { E.nface[q] = foff[q]; E.ncol[q] = coff[q]; }
   CFD_CUDA(cudaStreamCreateWithFlags(&E.st, cudaStreamNonBlocking));
+  CFD_CUDA(cudaStreamCreateWithFlags(&E.st2, cudaStreamNonBlocking));
+  for (auto& e : E.pipe_ev) CFD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   // device buffers
   const Par& c = E.par;
   const long long n = E.ncell;
@@ -2487,6 +2542,8 @@ void cfd3d_destroy(cfd3d_handle* h) {
   for (auto e : h->bev) cudaEventDestroy(e);
   if (h->cp) cudaStreamDestroy(h->cp);
   for (auto e : h->ev) if (e) cudaEventDestroy(e);
+  for (auto e : E.pipe_ev) if (e) cudaEventDestroy(e);
+  if (E.st2) cudaStreamDestroy(E.st2);
   if (E.st) cudaStreamDestroy(E.st);
   delete h;
 }
@@ -3138,7 +3195,7 @@ int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
   for (int T : cands) {
     E.tpb_face = T;
     const float t = time_calls(E, reps, [&] {
-      if (c.mixed) launch_face_flux_mixed(E, E.st);
+      if (c.mixed) launch_face_flux_mixed(E, E.st, 0, (int)E.blk.size());
       else launch_face_flux(E, E.st);
     });
     if (t < tbest) { tbest = t; best = T; }
@@ -3149,11 +3206,24 @@ int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
   tbest = 1e30f;
   for (int T : cands) {
     const float t = time_calls(E, reps, [&] {
-      launch_rhs(E, E.st, T, c.timemethod == 3);
+      launch_rhs(E, E.st, T, c.timemethod == 3, false);
     });
     if (t < tbest) { tbest = t; best = T; }
   }
   E.tpb_rhs = best;
+  // groups of blocks of the mixed form's face / residual pipeline: 1, 2, 4, ... up to the
+  // block count
+  if (c.mixed) {
+    const int nb = (int)E.blk.size();
+    int bestp = 1;
+    tbest = 1e30f;
+    for (int q = 1; q <= std::min(nb, Engine::MAX_PIPE); q *= 2) {
+      E.pipe_groups = q;
+      const float t = time_calls(E, reps, [&] { launch_face_rhs(E, E.st, c.timemethod == 3, false); });
+      if (t < tbest) { tbest = t; bestp = q; }
+    }
+    E.pipe_groups = bestp;
+  }
   // persistent CTAs per SM of the dataflow sweeps (up to the occupancy limit)
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
@@ -3280,7 +3350,12 @@ int cfd3d_profile_iterate(cfd3d_handle* h, double* stage_ms) {
   cudaEvent_t ev[9];
   for (int q = 0; q < 9; ++q) CFD_CUDA(cudaEventCreate(&ev[q]));
   CFD_CUDA(cudaStreamSynchronize(E.st));
+  // the stages in sequence: the face / residual pipeline off, so that the face stage and
+  // the residual are timed apart
+  const int groups = E.pipe_groups;
+  E.pipe_groups = 1;
   launch_iteration(E, true, ev);
+  E.pipe_groups = groups;
   CFD_CUDA(cudaEventSynchronize(ev[8]));
   for (int q = 0; q < CFD3D_NSTAGES; ++q) {
     float f = 0.0f;
@@ -3289,6 +3364,46 @@ int cfd3d_profile_iterate(cfd3d_handle* h, double* stage_ms) {
   }
   for (int q = 0; q < 9; ++q) cudaEventDestroy(ev[q]);
   CFD_CUDA(cudaGetLastError());
+  return CFD3D_OK;
+}
+
+int cfd3d_launch_shapes(const cfd3d_handle* h, int* shapes) {
+  if (!h || !shapes) return CFD3D_ERR_ARG;
+  const Engine& E = h->E;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nb = (int)E.blk.size();
+  shapes[0] = E.tpb_face;
+  shapes[1] = E.tpb_rhs;
+  shapes[2] = (E.sweep_grid + nsm - 1) / std::max(nsm, 1);
+  shapes[3] = E.par.mixed ? std::min(std::max(E.pipe_groups, 1), std::min(nb, Engine::MAX_PIPE)) : 1;
+  return CFD3D_OK;
+}
+
+int cfd3d_set_launch_shapes(cfd3d_handle* h, const int* shapes) {
+  if (!h || !shapes) return CFD3D_ERR_ARG;
+  Engine& E = h->E;
+  const Par& c = E.par;
+  auto threads_ok = [](int T) { return T == 64 || T == 128 || T == 256; };
+  if (!threads_ok(shapes[0]) || !threads_ok(shapes[1])) { E.err = "threads per CTA must be 64, 128 or 256"; return CFD3D_ERR_ARG; }
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (c.mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_tile<true>, 32, TILE_SMEM);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_df<true>, SW_CH, 0);
+  if (shapes[2] < 1 || shapes[2] > std::max(per, 1)) { E.err = "sweep CTAs per SM outside 1 .. the occupancy limit"; return CFD3D_ERR_ARG; }
+  const int nb = (int)E.blk.size();
+  if (shapes[3] < 1 || shapes[3] > std::min(nb, Engine::MAX_PIPE) || (!c.mixed && shapes[3] != 1)) {
+    E.err = "pipeline groups outside 1 .. min(blocks, 16) (1 in the FP64 form)";
+    return CFD3D_ERR_ARG;
+  }
+  E.tpb_face = shapes[0];
+  E.tpb_rhs = shapes[1];
+  const int nwork = c.mixed ? E.d.ntile : E.d.nchunk;
+  if (!E.sweep_planes) E.sweep_grid = std::max(1, std::min(shapes[2] * nsm, nwork));
+  E.pipe_groups = shapes[3];
+  E.graph_ready = 0;
   return CFD3D_OK;
 }
 

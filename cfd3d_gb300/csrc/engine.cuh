@@ -231,7 +231,13 @@ struct Engine {
   // launch shapes chosen by cfd3d_autotune: threads per CTA of the face kernels and of the
   // residual kernel (64, 128 or 256)
   int tpb_face = 128, tpb_rhs = 128;
-  cudaStream_t st = nullptr;
+  // mixed form: the face stage and the residual pipelined over groups of blocks (the
+  // residual of group q on st2 beside the face stage of group q + 1 on st): pipe_groups
+  // groups, 1 = no pipelining
+  int pipe_groups = 1;
+  static constexpr int MAX_PIPE = 16;
+  cudaStream_t st = nullptr, st2 = nullptr;
+  cudaEvent_t pipe_ev[MAX_PIPE + 2] = {};
   cudaGraphExec_t graph = nullptr;
   int graph_ready = 0;
   int launches_per_iter = 0;
@@ -336,7 +342,7 @@ constexpr int SW_CH = 32;
 
 // face-flux launchers (flux.cu: FP64 form; flux_mixed.cu: mixed form)
 void launch_face_flux(const Engine& E, cudaStream_t s);
-void launch_face_flux_mixed(const Engine& E, cudaStream_t s);
+void launch_face_flux_mixed(const Engine& E, cudaStream_t s, int b0, int b1);
 // discrete adjoint (adjoint.cu): buffers (allocated once, zeroed per call), the reverse
 // pass, and release
 int adjoint_buffers(Engine& E);

@@ -23,12 +23,12 @@ namespace cfd {
 // d(1/rho_l)/d(p, T) = -drho_l/d(p, T) / rho_l^2, dh_l/dp = dh/dp / (1 - y2) (the gas's h
 // does not depend on p) and dh_l/dT = (dh/dT - y2 cp_g) / (1 - y2).  The mixture's rho -
 // rhoref and h - href are formed in FP64 and stored in FP32, as the face records keep them.
-__global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c) {
+__global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c, long long g0, long long g1) {
   const long long n = d.ncell;
   const long long stride = (long long)gridDim.x * blockDim.x;
   const int npv = c.npv;
   const double off[NPVM] = {0.0, c.uref_vec[0], c.uref_vec[1], c.uref_vec[2], c.tref, 0.0, 0.0, 0.0, 0.0};
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += stride) {
+  for (long long g = g0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; g < g1; g += stride) {
     float sh[NPVM];
 #pragma unroll
     for (int v = 0; v < NPVM; ++v) {
@@ -139,11 +139,11 @@ __device__ __forceinline__ FaceIdx face_of(const DevPtr& d, long long t) {
 // The warp runs along i, so every plane load is a coalesced row.  Writes the face states,
 // before the clips, into frec; k_recon_mx<DIR, true> clips them and forms the face EOS.
 template <int DIR>
-__global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long ncol) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long c0, long long c1) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x, ncol = c1 - c0;
   const int v = (int)(t / ncol);
   if (v >= c.npv) return;
-  const long long col = t - (long long)v * ncol;
+  const long long col = c0 + (t - (long long)v * ncol);
   int b = 0;
   while (b + 1 < d.nblk && col >= d.blk[b + 1].col_off[DIR]) ++b;
   const BlockGeom& B = d.blk[b];
@@ -200,8 +200,10 @@ __global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long 
 // are the cells' own.  (The per-variable loops run over the compile-time bound, guarded by
 // npv, so that the arrays stay in registers.)
 template <int DIR, bool MARCH = false>
-__global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
-  const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+__global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c, long long t0, long long t1) {
+  const long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= t1) return;
+  const FaceIdx f = face_of<DIR>(d, t);
   if (!f.ok) return;
   const long long n = d.ncell, g = f.g, gr = g + f.sn;
   const int npv = c.npv;
@@ -271,8 +273,10 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c) {
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(256, 2) k_flux_mx(DevPtr d, Par c) {
-  const FaceIdx f = face_of<DIR>(d, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+__global__ void __launch_bounds__(256, 2) k_flux_mx(DevPtr d, Par c, long long t0, long long t1) {
+  const long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= t1) return;
+  const FaceIdx f = face_of<DIR>(d, t);
   if (!f.ok) return;
   const long long n = d.ncell, g = f.g, gr = g + f.sn;
   const long long sn = f.sn, s1 = f.s1, s2 = f.s2;
@@ -417,26 +421,37 @@ __global__ void __launch_bounds__(256, 2) k_flux_mx(DevPtr d, Par c) {
     if (v < npv) fvo[v * n + g] = fv[v];
 }
 
-void launch_face_flux_mixed(const Engine& E, cudaStream_t s) {
+// the face stage of blocks [b0, b1): their padded cells, faces and columns are contiguous
+// ranges of the flat numberings
+void launch_face_flux_mixed(const Engine& E, cudaStream_t s, int b0, int b1) {
   const int T = E.tpb_face;
-  auto nb = [T](long long n) { return (unsigned)((n + T - 1) / T); };
+  const int nb = (int)E.blk.size();
+  auto nblk = [T](long long n) { return (unsigned)std::max<long long>((n + T - 1) / T, 1); };
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  k_shadow<<<std::max(nsm, 1) * 8, 256, 0, s>>>(E.d, E.par);
+  const long long g0 = E.blk[b0].off, g1 = (b1 < nb) ? E.blk[b1].off : E.ncell;
+  long long f0[3], f1[3], c0[3], c1[3];
+  for (int q = 0; q < 3; ++q) {
+    f0[q] = E.blk[b0].face_off[q]; f1[q] = (b1 < nb) ? E.blk[b1].face_off[q] : E.nface[q];
+    c0[q] = E.blk[b0].col_off[q]; c1[q] = (b1 < nb) ? E.blk[b1].col_off[q] : E.ncol[q];
+  }
+  const long long share = (long long)(b1 - b0) * std::max(nsm, 1) * 8 / std::max(nb, 1);
+  k_shadow<<<(unsigned)std::max<long long>(share, 1), 256, 0, s>>>(E.d, E.par, g0, g1);
   // the i faces from their 38-cell stencils, the j and k faces by columns (k_muscl_march)
   // under MUSCL; then the clips and the face EOS
   const bool march = E.par.nmuscl > 0;
-  k_recon_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  k_flux_mx<0><<<nb(E.nface[0]), T, 0, s>>>(E.d, E.par);
-  if (march) k_muscl_march<1><<<(unsigned)((E.ncol[1] * E.par.npv + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[1]);
-  if (march) k_recon_mx<1, true><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
-  else k_recon_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
-  k_flux_mx<1><<<nb(E.nface[1]), T, 0, s>>>(E.d, E.par);
-  if (march) k_muscl_march<2><<<(unsigned)((E.ncol[2] * E.par.npv + 127) / 128), 128, 0, s>>>(E.d, E.par, E.ncol[2]);
-  if (march) k_recon_mx<2, true><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
-  else k_recon_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
-  k_flux_mx<2><<<nb(E.nface[2]), T, 0, s>>>(E.d, E.par);
+  auto cols = [&](int q) { return (unsigned)(((c1[q] - c0[q]) * E.par.npv + 127) / 128); };
+  k_recon_mx<0><<<nblk(f1[0] - f0[0]), T, 0, s>>>(E.d, E.par, f0[0], f1[0]);
+  k_flux_mx<0><<<nblk(f1[0] - f0[0]), T, 0, s>>>(E.d, E.par, f0[0], f1[0]);
+  if (march) k_muscl_march<1><<<cols(1), 128, 0, s>>>(E.d, E.par, c0[1], c1[1]);
+  if (march) k_recon_mx<1, true><<<nblk(f1[1] - f0[1]), T, 0, s>>>(E.d, E.par, f0[1], f1[1]);
+  else k_recon_mx<1><<<nblk(f1[1] - f0[1]), T, 0, s>>>(E.d, E.par, f0[1], f1[1]);
+  k_flux_mx<1><<<nblk(f1[1] - f0[1]), T, 0, s>>>(E.d, E.par, f0[1], f1[1]);
+  if (march) k_muscl_march<2><<<cols(2), 128, 0, s>>>(E.d, E.par, c0[2], c1[2]);
+  if (march) k_recon_mx<2, true><<<nblk(f1[2] - f0[2]), T, 0, s>>>(E.d, E.par, f0[2], f1[2]);
+  else k_recon_mx<2><<<nblk(f1[2] - f0[2]), T, 0, s>>>(E.d, E.par, f0[2], f1[2]);
+  k_flux_mx<2><<<nblk(f1[2] - f0[2]), T, 0, s>>>(E.d, E.par, f0[2], f1[2]);
 }
 
 }  // namespace cfd

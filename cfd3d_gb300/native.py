@@ -64,6 +64,8 @@ def lib():
     L.cfd3d_eos_eval.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
     L.cfd3d_eos_eval_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp]
     L.cfd3d_stats.argtypes = [H, C.POINTER(C.c_int64), ip]
+    L.cfd3d_launch_shapes.argtypes = [H, ip]
+    L.cfd3d_set_launch_shapes.argtypes = [H, ip]
     L.cfd3d_time_iterate.argtypes = [H, C.c_int, dp]
     L.cfd3d_profile_iterate.argtypes = [H, dp]
     L.cfd3d_set_device.argtypes = [C.c_int]
@@ -75,7 +77,7 @@ def lib():
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
            "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_upload_primitives", "cfd3d_upload_primitives_all", "cfd3d_download_state_all", "cfd3d_download_csf", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
            "cfd3d_iterate", "cfd3d_iterate_n",
-           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats",
+           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats", "cfd3d_launch_shapes", "cfd3d_set_launch_shapes",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device", "cfd3d_fp64_peak"]
 STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
 
@@ -269,6 +271,18 @@ class Engine:
         ch = (C.c_int * 3)()
         self._check(lib().cfd3d_autotune(self.h, reps, ch))
         return tuple(ch)
+
+    def launch_shapes(self):
+        """cfd3d_launch_shapes: (face threads per CTA, residual threads per CTA, sweep CTAs
+        per SM, face / residual pipeline groups) in use."""
+        sh = (C.c_int * 4)()
+        self._check(lib().cfd3d_launch_shapes(self.h, sh))
+        return tuple(sh)
+
+    def set_launch_shapes(self, shapes):
+        """cfd3d_set_launch_shapes: the four shapes of launch_shapes()."""
+        sh = (C.c_int * 4)(*[int(x) for x in shapes])
+        self._check(lib().cfd3d_set_launch_shapes(self.h, sh))
 
     def sweep_stall_test(self):
         """cfd3d_sweep_stall_test: the status code (CFD3D_ERR_TIMEOUT expected)."""

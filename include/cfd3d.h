@@ -244,12 +244,25 @@ int  cfd3d_residual_vjp(cfd3d_handle *h, const double *cot, double *g_state, dou
 
 /* Launch-shape autotuner (no counterpart in the reference).  On the current state it
  * times, with CUDA events over `reps` calls each, the face-flux kernels and the residual
- * kernel at 64, 128 and 256 threads per CTA and the dataflow sweeps at 1, 2, 4, ... persistent
- * CTAs per SM (up to the occupancy limit), keeps the fastest of each, and re-captures the
+ * kernel at 64, 128 and 256 threads per CTA, the mixed form's face / residual pipeline at
+ * 1, 2, 4, ... block groups and the sweeps at 1, 2, 3, 4, 6, ... persistent CTAs per SM (up
+ * to the occupancy limit), keeps the fastest of each, and re-captures the
  * iteration graph at the next iteration.  choice (may be NULL) receives the threads per
  * CTA of the face and residual kernels and the sweep CTAs per SM.  Results do not depend on
  * the shapes: each thread's arithmetic is unchanged. */
 int  cfd3d_autotune(cfd3d_handle *h, int reps, int *choice);
+
+/* The launch shapes in use (no counterpart in the reference): shapes[0..3] receive the
+ * threads per CTA of the face and residual kernels, the sweep CTAs per SM, and the number
+ * of block groups over which the mixed form pipelines its face stage and residual (the
+ * residual of one group beside the face stage of the next, on a second stream; 1 = none).
+ * The autotuner chooses all four; results do not depend on them. */
+int  cfd3d_launch_shapes(const cfd3d_handle *h, int *shapes);
+/* Sets the four launch shapes of cfd3d_launch_shapes (for instance those a tuning run
+ * found): threads per CTA 64, 128 or 256; sweep CTAs per SM from 1 to the occupancy limit;
+ * pipeline groups from 1 to min(blocks, 16), 1 in the FP64 form.  CFD3D_ERR_ARG otherwise,
+ * with nothing changed.  The iteration graph is re-captured at the next iteration. */
+int  cfd3d_set_launch_shapes(cfd3d_handle *h, const int *shapes);
 
 /* Test hook of the dataflow sweeps' bounded waits (no counterpart in the reference): one
  * forward sweep on the current state's records in which the first chunk of cells never
@@ -304,7 +317,8 @@ int  cfd3d_set_device(int device);
  * niter back-to-back pseudo-iterations.  No reference counterpart (measurement only). */
 int  cfd3d_time_iterate(cfd3d_handle *h, int niter, double *ms);
 
-/* One pseudo-iteration launched stage by stage with CUDA events between the stages;
+/* One pseudo-iteration launched stage by stage with CUDA events between the stages (the
+ * mixed form's face / residual pipeline off, so that the two are timed apart);
  * stage_ms[CFD3D_NSTAGES] receives: time step, boundary program, face fluxes, residual
  * + sources, forward sweep, backward sweep, update + EOS, eddy + norms.
  * No reference counterpart (measurement only). */
