@@ -767,12 +767,12 @@ __device__ void csf_cell(const DevPtr& d, long long g, long long sj, long long s
 // gravity and the surface-tension sources (a separate instantiation, so that the plain kernel carries none of their
 // code)
 template <bool MX, bool REC = true, bool XS = false>
-// The mixed form at 2 CTAs of 256 threads per SM: its residual is latency-bound (the FP64
-// pipe about a third busy), and the occupancy buys more than the registers' few spills
-// cost.  store_res: the residual, icav and itt planes are written (the residual query and
+// The mixed form at 3 CTAs of 256 threads per SM: its residual is latency-bound (the FP64
+// pipe about a third busy), and the occupancy buys more than the registers' spills cost
+// (measured: 10.8 ms at 1 CTA, 8.1 at 2, 7.3 at 3 on the 14.2 M-cell case).  store_res: the residual, icav and itt planes are written (the residual query and
 // the explicit schemes read them); the mixed form's LU-SGS iteration keeps them in
 // registers, and only the sweep record and x0 carry them on.
-__global__ void __launch_bounds__(256, MX ? 2 : 1) k_rhs(DevPtr d, Par c, long long t0, long long t1, int store_res) {
+__global__ void __launch_bounds__(256, MX ? 3 : 1) k_rhs(DevPtr d, Par c, long long t0, long long t1, int store_res) {
   long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= t1) return;
   const bool out = !(MX && REC) || store_res != 0;
@@ -1348,10 +1348,10 @@ __global__ void __launch_bounds__(SW_CH) k_sweep_df(DevPtr d, Par c, long long s
 // the neighbours' FP32 products:
 //   forward   dq* = D^-1 (res + sum A+ dq*)  = x0 + y_f,   y_f = D^-1 (sum A+ dq*),   x0 = D^-1 res
 //   backward  dq  = D^-1 (dcv - sum A- dq)   = dq* + y_b,  y_b = D^-1 (- sum A- dq)   (D^-1 dcv = dq*)
-// k_rhs writes x0 in FP64 (tq) and in FP32 within the cell's tile record; the sweeps work
-// in FP32 alone -- the products take dq in FP32 -- and store their corrections y_f, y_b;
-// the update forms dq = x0 + y_f + y_b in FP64.  (On a GB300 each FP64 instruction holds a
-// warp for tens of cycles: none stays on the sweeps' dependency chain.)  One warp sweeps one tile at a
+// k_rhs writes x0 (FP32) into tq and into the cell's tile record; the sweeps work in FP32
+// alone -- the products take dq in FP32 -- and store their corrections y_f, y_b; the update
+// forms dq = x0 + y_f + y_b and adds it to pv in FP64.  (On a GB300 each FP64 instruction
+// holds a warp for tens of cycles: none stays on the sweeps' dependency chain.)  One warp sweeps one tile at a
 // time (tiles from a ticket counter in tile-hyperplane order, reversed for the backward
 // sweep): it stages the tile's records in shared memory with one bulk copy per array
 // (cp.async.bulk, completion on an mbarrier), waits for the done flags of the (at most
@@ -1584,8 +1584,15 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
         old[v] = p[v] = 0.0;
         if (v >= npv) continue;
         old[v] = d.pv[v * n + g];
-        p[v] = old[v] + (MX ? (double)d.tq[tq_at(pq, v)] + (double)d.tyf[tq_at(pq, v)] + (double)d.tyb[tq_at(pq, v)]
-                            : d.dqs[v * d.nint + pq]);
+        if (MX) {
+          // dq = x0 + y_f + y_b in FP32: each part is an FP32 result of the FP32 operator, so
+          // an FP64 sum would add digits none of them carries
+          const long long q = tq_at(pq, v);
+          const float dqf = (d.tq[q] + d.tyf[q]) + d.tyb[q];
+          p[v] = old[v] + (double)dqf;
+        } else {
+          p[v] = old[v] + d.dqs[v * d.nint + pq];
+        }
       }
     } else {
       double cur[NPVM], dvc[NDV], r[NPVM], x[NPVM];
@@ -1610,7 +1617,7 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
     }
 #pragma unroll
     for (int v = 0; v < NPVM; ++v)
-      if (v < npv && !isfinite(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
+      if (v < npv && !finite_bits(p[v])) bad = 1;   // checked before the clips, which would hide a NaN (fmax/fmin)
     p[0] = fmax(-c.pref + 1.0e1, p[0]);
     p[5] = fmin(1.0, fmax(0.0, p[5]));
     p[6] = fmin(1.0, fmax(0.0, p[6]));
@@ -1625,8 +1632,7 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
       if (v >= npv) continue;
       d.pv[v * n + g] = p[v];
       double df = fabs(old[v] - p[v]);
-      sq_[v] += df * df;
-      if (!isfinite(p[v])) bad = 1;
+      sq_[v] += df * df;   // (the clips keep a finite p finite)
     }
     double dp = fabs(old[0] - p[0]);
     if (dp > dpmax) { dpmax = dp; dpidx = t; }   // t increases: ties keep the first cell
@@ -1639,7 +1645,7 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
     else deteos<false>(c.fluid, c.with_prop, pe, te, y1, y2, dv, tv, &d.sc->snd2_fallbacks);
     for (int v = 0; v < NDV; ++v) {
       d.dv[v * n + g] = dv[v];
-      if (!isfinite(dv[v])) bad = 1;
+      if (!finite_bits(dv[v])) bad = 1;
     }
 #pragma unroll
     for (int v = 0; v < 3; ++v)
@@ -1946,7 +1952,7 @@ int face_rhs_launches(const Engine& E) {
   if (!c.mixed) return 4;
   const int nb = (int)E.blk.size();
   const int ng = std::min(std::max(E.pipe_groups, 1), std::min(nb, Engine::MAX_PIPE));
-  return ng * (8 + (c.nmuscl > 0 ? 2 : 0));
+  return ng * (8 + (c.nmuscl > 0 ? 2 : 0) + (c.iturb != -3 ? 3 : 0));
 }
 
 // The boundary program -- the total-pressure pools, then faces + halos, edges, corners -- and,

@@ -177,8 +177,7 @@ struct DevPtr {
   float *recf, *dqsf;
   // mixed form: the tile sweeps (setup_tiles).  tiles in forward ticket order; trf the FP32
   // tile records; tq the own part D^-1 res per slot (k_rhs, an FP32 solve); tyf / tyb the
-  // FP32 corrections of the forward / backward sweep, so that dq = tq + tyf + tyb, summed in
-  // FP64 (k_update);
+  // FP32 corrections of the forward / backward sweep, so that dq = tq + tyf + tyb (k_update);
   // tin the contributions entering each tile (written by the neighbouring tiles during a
   // sweep); done flags per tile
   int ntile;

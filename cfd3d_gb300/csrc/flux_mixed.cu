@@ -7,7 +7,8 @@
 //                     near its cell the liquid by first-order expansion), written to the
 //                     face record frec
 //   k_flux_mx<DIR>    per face: FP32 Roe-average sound speed, inviscid flux with FP64
-//                     leading-order terms, FP32 viscous flux; stores F - Phi.n dl in FP32
+//                     leading-order terms; stores F - Phi.n dl in FP32
+//   k_visc_mx<DIR>    per face: the FP32 viscous flux
 // Splitting reconstruction + EOS from the flux keeps each kernel's code within the
 // instruction cache (the expanded df64 Gibbs sums are large) and its registers low.
 // Same faces, stencils and formulas as the FP64 form (flux.cu); the precision choices are
@@ -273,12 +274,12 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c, long long t0,
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(256, 2) k_flux_mx(DevPtr d, Par c, long long t0, long long t1) {
+__global__ void __launch_bounds__(256) k_flux_mx(DevPtr d, Par c, long long t0, long long t1) {
   const long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= t1) return;
   const FaceIdx f = face_of<DIR>(d, t);
   if (!f.ok) return;
-  const long long n = d.ncell, g = f.g, gr = g + f.sn;
+  const long long n = d.ncell, g = f.g;
   const long long sn = f.sn, s1 = f.s1, s2 = f.s2;
   const int npv = c.npv;
   const float* P = d.pvf;
@@ -331,8 +332,23 @@ __global__ void __launch_bounds__(256, 2) k_flux_mx(DevPtr d, Par c, long long t
 #pragma unroll
   for (int v = 0; v < NPVM; ++v)
     if (v < npv) fo[v * n + g] = fx[v];
-  if (c.iturb == -3) return;
-  // ---- viscous flux in FP32 (vsflux_laminar / vsflux_turbulent, src/vsflux_module.f90:182-425)
+}
+
+// The viscous flux of the DIR faces in FP32 (vsflux_laminar / vsflux_turbulent,
+// src/vsflux_module.f90:182-425): a kernel of its own, so that its 18-cell gradient stencils
+// run with the warps its few registers allow rather than under the inviscid flux's df64
+// register budget.  Writes fv32.
+template <int DIR>
+__global__ void __launch_bounds__(256) k_visc_mx(DevPtr d, Par c, long long t0, long long t1) {
+  const long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= t1) return;
+  const FaceIdx f = face_of<DIR>(d, t);
+  if (!f.ok) return;
+  const long long n = d.ncell, g = f.g, gr = g + f.sn;
+  const long long sn = f.sn, s1 = f.s1, s2 = f.s2;
+  const int npv = c.npv;
+  const float* P = d.pvf;
+  const int fplane = (DIR == 0) ? GM_CX : (DIR == 1 ? GM_EX : GM_TX);
   const bool turb = (c.iturb >= -1);
   const int ep = (DIR == 0) ? GM_EX : (DIR == 1 ? GM_TX : GM_CX);
   const int tp = (DIR == 0) ? GM_TX : (DIR == 1 ? GM_CX : GM_EX);
@@ -440,18 +456,21 @@ void launch_face_flux_mixed(const Engine& E, cudaStream_t s, int b0, int b1) {
   k_shadow<<<(unsigned)std::max<long long>(share, 1), 256, 0, s>>>(E.d, E.par, g0, g1);
   // the i faces from their 38-cell stencils, the j and k faces by columns (k_muscl_march)
   // under MUSCL; then the clips and the face EOS
-  const bool march = E.par.nmuscl > 0;
+  const bool march = E.par.nmuscl > 0, visc = E.par.iturb != -3;
   auto cols = [&](int q) { return (unsigned)(((c1[q] - c0[q]) * E.par.npv + 127) / 128); };
   k_recon_mx<0><<<nblk(f1[0] - f0[0]), T, 0, s>>>(E.d, E.par, f0[0], f1[0]);
   k_flux_mx<0><<<nblk(f1[0] - f0[0]), T, 0, s>>>(E.d, E.par, f0[0], f1[0]);
+  if (visc) k_visc_mx<0><<<nblk(f1[0] - f0[0]), T, 0, s>>>(E.d, E.par, f0[0], f1[0]);
   if (march) k_muscl_march<1><<<cols(1), 128, 0, s>>>(E.d, E.par, c0[1], c1[1]);
   if (march) k_recon_mx<1, true><<<nblk(f1[1] - f0[1]), T, 0, s>>>(E.d, E.par, f0[1], f1[1]);
   else k_recon_mx<1><<<nblk(f1[1] - f0[1]), T, 0, s>>>(E.d, E.par, f0[1], f1[1]);
   k_flux_mx<1><<<nblk(f1[1] - f0[1]), T, 0, s>>>(E.d, E.par, f0[1], f1[1]);
+  if (visc) k_visc_mx<1><<<nblk(f1[1] - f0[1]), T, 0, s>>>(E.d, E.par, f0[1], f1[1]);
   if (march) k_muscl_march<2><<<cols(2), 128, 0, s>>>(E.d, E.par, c0[2], c1[2]);
   if (march) k_recon_mx<2, true><<<nblk(f1[2] - f0[2]), T, 0, s>>>(E.d, E.par, f0[2], f1[2]);
   else k_recon_mx<2><<<nblk(f1[2] - f0[2]), T, 0, s>>>(E.d, E.par, f0[2], f1[2]);
   k_flux_mx<2><<<nblk(f1[2] - f0[2]), T, 0, s>>>(E.d, E.par, f0[2], f1[2]);
+  if (visc) k_visc_mx<2><<<nblk(f1[2] - f0[2]), T, 0, s>>>(E.d, E.par, f0[2], f1[2]);
 }
 
 }  // namespace cfd

@@ -580,6 +580,11 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
   }
 }
 
+// isfinite by the exponent bits (integer instructions: the FP64 pipe is the scarce one)
+__device__ __forceinline__ bool finite_bits(double x) {
+  return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000;
+}
+
 // ------------------------------------------------------------------ MUSCL / MLP
 // Products and sums without FMA contraction.  A reconstructed state often lands exactly
 // on a clip bound (y1 = 0 next to a cell without vapour, when the MLP factor is exactly 2),
