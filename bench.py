@@ -66,24 +66,27 @@ def algorithmic_bytes(cfg):
 
 
 def rhs_bytes(cfg, mixed):
-    """Algorithmic bytes per cell of the residual kernel k_rhs (each datum once per cell).
-    Reads: the cell's + face fluxes (inviscid and viscous), pv, dv, tv, its + face vectors,
-    volume and wall distance, the BDF history, dt; the mixed form reads the fluxes in FP32
-    and adds the free-stream closure, the FP32 shadow of the SST gradients and the FP32
-    metric copy.  Writes: the residual, icav, itt, the omega bound, rcav, and the LU-SGS
-    record -- 66 FP64 values in the FP64 form; in the mixed form the 75-value FP32 tile
-    record and the own part x0 of dq in FP64."""
+    """Algorithmic bytes per cell of the residual kernel k_rhs in the LU-SGS iteration (each
+    datum once per cell).  FP64 form -- reads: the cell's + face fluxes (inviscid and
+    viscous), pv, dv, tv, its + face vectors, volume and wall distance, the BDF history, dt;
+    writes: the residual, icav, itt, the omega bound, rcav and the 66-value FP64 sweep
+    record.  Mixed form -- reads: the FP32 fluxes, pv, dv, tv, the volume, the BDF history,
+    dt, the free-stream closure, the FP32 shadow of the SST variables and the FP32 metrics
+    (+ face vectors, volume, wall distance); writes: the omega bound, rcav, the 74-value FP32
+    tile record and the FP32 own part x0 (the residual, icav and itt stay in registers)."""
     from cfd3d_gb300.abi import sizes
     npv, ntv, nqq, ngrd = sizes(cfg)
     vis = cfg.get("iturb", 0) != -3
-    fw = 4 if mixed else 8
-    rd = 3 * (2 if vis else 1) * npv * fw + 8 * npv + 8 * 18 + 8 * ntv + 8 * (9 + 2) + 8 * nqq * npv + 8
-    wr = 8 * npv + 8 * (4 + 4 + 1 + 2)
-    if mixed:
-        rd += 8 * npv + 4 * 5 + 4 * (9 + 2)
-        wr += 4 * 75 + 8 * npv
-    else:
-        wr += 8 * 66
+    sst = cfg.get("iturb", 0) == 0
+    cav = cfg.get("ncav", 0) != 0
+    ndv = 18
+    if not mixed:
+        rd = 3 * (2 if vis else 1) * npv * 8 + 8 * npv + 8 * ndv + 8 * ntv + 8 * (9 + 2) + 8 * nqq * npv + 8
+        wr = 8 * npv + 8 * (4 + 4 + 1 + 2) + 8 * 66
+        return rd + wr
+    rd = (3 * (2 if vis else 1) * npv * 4 + 8 * npv + 8 * ndv + 8 * ntv + 8 + 8 * nqq * npv + 8 + 8 * npv
+          + (4 * 5 if sst else 0) + 4 * (9 + 2))
+    wr = (8 if sst else 0) + (16 if cav else 0) + 4 * 74 + 4 * npv
     return rd + wr
 
 

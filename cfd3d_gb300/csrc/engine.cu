@@ -767,12 +767,12 @@ __device__ void csf_cell(const DevPtr& d, long long g, long long sj, long long s
 // gravity and the surface-tension sources (a separate instantiation, so that the plain kernel carries none of their
 // code)
 template <bool MX, bool REC = true, bool XS = false>
-// The mixed form at 3 CTAs of 256 threads per SM: its residual is latency-bound (the FP64
+// The mixed form at 4 CTAs of 256 threads per SM: its residual is latency-bound (the FP64
 // pipe about a third busy), and the occupancy buys more than the registers' spills cost
-// (measured: 10.8 ms at 1 CTA, 8.1 at 2, 7.3 at 3 on the 14.2 M-cell case).  store_res: the residual, icav and itt planes are written (the residual query and
+// (measured: 10.8 ms at 1 CTA, 8.1 at 2, 7.4 at 3, 6.6 at 4 on the 14.2 M-cell case).  store_res: the residual, icav and itt planes are written (the residual query and
 // the explicit schemes read them); the mixed form's LU-SGS iteration keeps them in
 // registers, and only the sweep record and x0 carry them on.
-__global__ void __launch_bounds__(256, MX ? 3 : 1) k_rhs(DevPtr d, Par c, long long t0, long long t1, int store_res) {
+__global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long long t0, long long t1, int store_res) {
   long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= t1) return;
   const bool out = !(MX && REC) || store_res != 0;
