@@ -195,8 +195,32 @@ __global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long 
   };
 #pragma unroll
   for (int q = 0; q < 5; ++q) load(q, q - 1);
+  // the plane a face needs last (m + 3) is fetched one face ahead, so that its loads are in
+  // flight while the face before it is formed
+  float pre[9];   // [3 (t1 + 1) + (t2 + 1)]
+  auto fetch = [&](int m) {
+    const long long gc = gm1 + sn * (m + 1);
+    if (mlp) {
+#pragma unroll
+      for (int p1 = 0; p1 < 3; ++p1)
+#pragma unroll
+        for (int p2 = 0; p2 < 3; ++p2) pre[3 * p1 + p2] = P[gc + (p1 - 1) * s1 + (p2 - 1) * s2];
+    } else {
+      pre[4] = P[gc];
+    }
+  };
+  fetch(4);
   for (int m = 1; m <= nmax; ++m) {
-    load(5, m + 3);
+    cc[5] = pre[4];
+    if (mlp) {
+      dt[5] = pre[7] - pre[1];
+      dr[5] = pre[5] - pre[3];
+      float lo = pre[0], hi = pre[0];
+#pragma unroll
+      for (int q = 1; q < 9; ++q) { lo = fminf(lo, pre[q]); hi = fmaxf(hi, pre[q]); }
+      mn[5] = lo; mx[5] = hi;
+    }
+    if (m < nmax) fetch(m + 4);
     const float mnr[4] = {mn[1], mn[2], mn[3], mn[4]}, mxr[4] = {mx[1], mx[2], mx[3], mx[4]};
     float xl, xr;
     muscl_reduced(c, cc[0], cc[1], cc[2], cc[3], cc[4], cc[5], dt[2], dr[2], dt[3], dr[3], mnr, mxr, xl, xr);
