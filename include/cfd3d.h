@@ -252,6 +252,14 @@ int  cfd3d_residual_vjp(cfd3d_handle *h, const double *cot, double *g_state, dou
  * the shapes: each thread's arithmetic is unchanged. */
 int  cfd3d_autotune(cfd3d_handle *h, int reps, int *choice);
 
+/* Self-test of the float <-> double conversions the mixed form runs on the integer pipes
+ * (no counterpart in the reference; on a GB300 the hardware conversions take FP64-pipe
+ * slots): n seeded bit patterns -- random ones over the double range, exact halfway cases,
+ * the ends of the float range, signed zeros, ordinary magnitudes -- converted by them and by
+ * the hardware.  mismatches[0] / [1] receive the number of double -> float / float -> double
+ * results whose bits differ (0 expected). */
+int  cfd3d_convert_selftest(long long n, unsigned long long seed, long long *mismatches);
+
 /* The launch shapes in use (no counterpart in the reference): shapes[0..3] receive the
  * threads per CTA of the face and residual kernels, the sweep CTAs per SM, and the number
  * of block groups over which the mixed form pipelines its face stage and residual (the
