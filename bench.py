@@ -433,6 +433,7 @@ def main():
         dist.barrier()
         return 0
     fp64_tflops = native.fp64_peak(1.0)
+    conv = native.convert_rate()
     peak, peak_kind = measured_peaks()
     bpc = algorithmic_bytes(cfg)
     achieved_it = ncell * bpc / (ms_step * 1e-3) / 1e9
@@ -462,7 +463,10 @@ def main():
                                 "frac": achieved_rhs / peak, "kernel_ms": rhs_ms, "algorithmic_bytes_per_cell": rb,
                                 "traffic": RHS_TRAFFIC_PER_CELL * ncell if (prec == abi.MIXED and args.case == "large") else None},
                      "fp64": {"peak_tflops": fp64_tflops,
-                              "peak_kind": "measured: cfd3d_fp64_peak, independent DFMA chains, 1 s"}},
+                              "peak_kind": "measured: cfd3d_fp64_peak, independent DFMA chains, 1 s",
+                              "conversions_gps": {k: round(v, 1) for k, v in conv.items()},
+                              "conversions_kind": "measured: cfd3d_convert_rate, float <-> double by the "
+                                                  "hardware (FP64 pipe) and on the integer pipes"}},
         "e2e": e2e,
         "gpu_launches": stats["launches_per_iter"] * args.steps,
         "setup_s": {"create": t_create - t_setup, "initialize": t_init - t_create,

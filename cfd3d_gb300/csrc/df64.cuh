@@ -14,10 +14,13 @@ namespace cfd {
 
 // float <-> double conversions on the integer pipes.  On a GB300 the hardware conversions
 // issue on the FP64 pipe at its rate (2 per clock per SM, measured: 625 G conversions/s
-// either way), so in the FP64-bound kernels every cast takes the slot of a DFMA.  These give
-// the same bits -- IEEE 754 round to nearest, ties to even -- from integer instructions for
-// the normal range and signed zeros (measured 1.5 / 2.2 T conversions/s), and hand the rest
-// (subnormals, infinities, NaNs, values outside the float range) to the hardware conversion.
+// either way).  These give the same bits -- IEEE 754 round to nearest, ties to even -- from
+// integer instructions for the normal range and signed zeros (measured 1.5 / 2.2 T
+// conversions/s alone), and hand the rest (subnormals, infinities, NaNs, values outside the
+// float range) to the hardware conversion.  Inside a kernel they cost a dozen integer
+// instructions, two branches and registers per cast: the eddy viscosity, whose work is
+// mostly casts of its neighbours' states, gains from them; the update, the residual and
+// the time step measured slower with them, and keep the hardware's.
 __device__ __forceinline__ float to_f32(double x) {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
   const int e = (int)((hi >> 20) & 0x7ffu) - 896;             // the float's biased exponent
@@ -42,20 +45,12 @@ struct df64 {
   float hi, lo;
   __device__ __forceinline__ df64() {}
   __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
-  // (from a constant: the compiler folds the hardware conversions; a run-time value takes
-  // split_f64, below)
   __device__ __forceinline__ explicit df64(double a) {
     hi = static_cast<float>(a);
     lo = static_cast<float>(a - static_cast<double>(hi));
   }
-  __device__ __forceinline__ explicit operator double() const { return to_f64(hi) + to_f64(lo); }
+  __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
 };
-
-// a run-time double as hi + lo, with the conversions on the integer pipes
-__device__ __forceinline__ df64 split_f64(double a) {
-  const float h = to_f32(a);
-  return df64(h, to_f32(a - to_f64(h)));
-}
 
 __device__ __forceinline__ df64 two_sum(float a, float b) {
   float s = __fadd_rn(a, b);

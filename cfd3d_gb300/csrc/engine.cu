@@ -167,10 +167,10 @@ __global__ void k_timestep(DevPtr d, Par c) {
       dtv = c.cfl;
     } else if (MX) {
       const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
-      const float u = to_f32(d.pv[n + g]), v = to_f32(d.pv[2 * n + g]), w = to_f32(d.pv[3 * n + g]);
+      const float u = (float)d.pv[n + g], v = (float)d.pv[2 * n + g], w = (float)d.pv[3 * n + g];
       float dvf[12], tvf[3] = {0.0f, 0.0f, 0.0f};
-      for (int q = 0; q < 12; ++q) dvf[q] = to_f32(d.dv[q * n + g]);
-      for (int q = 0; q < c.ntv; ++q) tvf[q] = to_f32(d.tv[q * n + g]);
+      for (int q = 0; q < 12; ++q) dvf[q] = (float)d.dv[q * n + g];
+      for (int q = 0; q < c.ntv; ++q) tvf[q] = (float)d.tv[q * n + g];
       const float* G = d.gmf;
       const float vol = G[GM_GRD * n + g];
       float cs[3][3];
@@ -191,7 +191,7 @@ __global__ void k_timestep(DevPtr d, Par c) {
         ss += s2;
       }
       const float ev = eigenvis_f(c, dvf, tvf) * ss / vol;
-      dtv = to_f64(to_f32(c.cfl) * vol / (eig + 4.0f * ev));
+      dtv = (double)((float)c.cfl * vol / (eig + 4.0f * ev));
     } else {
       const long long n = d.ncell, sj = B.ni, sk = (long long)B.ni * B.nj;
       double u = d.pv[n + g], v = d.pv[2 * n + g], w = d.pv[3 * n + g];
@@ -802,7 +802,7 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
           r += V[g] - V[g - st[q]];
         }
       }
-      res[v] = to_f64(r);
+      res[v] = (double)r;
     }
   }
   for (int v = 0; v < npv && !MX; ++v) {
@@ -899,12 +899,12 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
   float icf[4] = {0.0f, 0.0f, 0.0f, 0.0f}, itf[4] = {0.0f, 0.0f, 0.0f, 0.0f};
   if (MX) {
 #pragma unroll
-    for (int q = 0; q < NPVM; ++q) p2f[q] = to_f32(pv2[q]);
+    for (int q = 0; q < NPVM; ++q) p2f[q] = (float)pv2[q];
 #pragma unroll
-    for (int q = 0; q < NDV; ++q) dvf[q] = to_f32(dv[q]);
+    for (int q = 0; q < NDV; ++q) dvf[q] = (float)dv[q];
 #pragma unroll
     for (int q = 0; q < 3; ++q)
-      if (q < c.ntv) tvf[q] = to_f32(d.tv[q * n + g]);
+      if (q < c.ntv) tvf[q] = (float)d.tv[q * n + g];
   }
   const float volf = MX ? d.gmf[GM_GRD * n + g] : 0.0f;
   if (c.ncav) {
@@ -918,10 +918,10 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
         else sat[0] = h2o_pww(pv2[4]);
       }
       const CavOutT<float> o = cavsource_t<float>(c, p2f, dvf, vol, (float)c.uref, (float)c.c_v, (float)c.c_c, sat);
-      res[5] = res[5] + to_f64(o.r_v) - to_f64(o.r_c);
-      for (int q = 0; q < 4; ++q) { if (out) d.icav[q * n + g] = to_f64(o.icav[q]); icf[q] = o.icav[q]; }
-      d.rcav[g] = to_f64(o.r_c);
-      d.rcav[n + g] = to_f64(o.r_v);
+      res[5] = res[5] + (double)o.r_v - (double)o.r_c;
+      for (int q = 0; q < 4; ++q) { if (out) d.icav[q * n + g] = o.icav[q]; icf[q] = o.icav[q]; }
+      d.rcav[g] = o.r_c;
+      d.rcav[n + g] = o.r_v;
     } else {
       CavOut o = cavsource(c, pv2, dv, vol);
       res[5] = res[5] + o.r_v - o.r_c;
@@ -958,12 +958,12 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
       const float kf = p2f[7], of = p2f[8], rho = dvf[0];
       const SstOut<float> sf = sst_source_f(grf, kf, of, rho, tvf[0], tvf[2], d.gmf[(GM_GRD + 4) * n + g], volf,
                                             XS ? c.ides : 0, hmax);
-      res[7] = res[7] + to_f64(sf.r7);
-      res[8] = res[8] + to_f64(sf.r8);
+      res[7] = res[7] + (double)sf.r7;
+      res[8] = res[8] + (double)sf.r8;
       // the implicit coefficients and the omega bound of the update: FP32
       const float pf = sf.prod, df_ = sf.dest, dvf_ = sf.div, pkf = sf.pkw, bf = sf.bigf;
       const float taf = sf.talpha, tbf = sf.tbeta;
-      d.ocut[g] = to_f64(sqrtf(sf.strain - (2.0f / 3.0f) * dvf_ * dvf_));
+      d.ocut[g] = (double)sqrtf(sf.strain - (2.0f / 3.0f) * dvf_ * dvf_);
       const float ki = 1.0f / kf, oi = 1.0f / of, ei = 1.0f / tvf[2];
       const float dpdk = pf * ki;
       const float dpdo = -((pf + (2.0f / 3.0f) * rho * kf * dvf_) * oi);
@@ -978,7 +978,7 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
       const float f1 = (1.0f - 0.5f * (1.0f - l1)) - 0.5f * (1.0f - l1);
       const float f2 = (1.0f - 0.5f * (1.0f - l2)) - 0.5f * (1.0f - l2);
       itf[0] = it0 * f1; itf[1] = it1 * f1; itf[2] = it2 * f2; itf[3] = it3 * f2;
-      if (out) for (int q = 0; q < 4; ++q) d.itt[q * n + g] = to_f64(itf[q]);
+      if (out) for (int q = 0; q < 4; ++q) d.itt[q * n + g] = itf[q];
     } else {
       double tv[3];
       for (int q = 0; q < 3; ++q) tv[q] = d.tv[q * n + g];
@@ -1084,14 +1084,14 @@ __global__ void __launch_bounds__(256, MX ? 4 : 1) k_rhs(DevPtr d, Par c, long l
     float lam_fs[2];
     diag_spectral_f(c, p2f, dvf[5], fcf, lam_fs);
     const float evf = eigenvis_f(c, dvf, tvf);
-    diag_prepare_t<float>(c, p2f, dvf, evf, fcf, volf, to_f32(d.dt[g]), icf, itf, Df, lam_fs);
+    diag_prepare_t<float>(c, p2f, dvf, evf, fcf, volf, (float)d.dt[g], icf, itf, Df, lam_fs);
     // the cell's tile record (FP32) and the forward sweep's own part x0 = D^-1 res, at its
     // tile slot: consecutive i are consecutive slots.  x0 is an FP32 solve of the FP64
     // residual (rounded once): an inexact step of the iteration, not of its fixed point.
     const long long sl = d.pos[g];
     float rf[NPVM], xf[NPVM];
 #pragma unroll
-    for (int v = 0; v < NPVM; ++v) { rf[v] = (v < npv) ? to_f32(res[v]) : 0.0f; xf[v] = 0.0f; }
+    for (int v = 0; v < NPVM; ++v) { rf[v] = (v < npv) ? (float)res[v] : 0.0f; xf[v] = 0.0f; }
     diag_solve_t<float>(c, Df, p2f, dvf, rf, xf);
     float* R = d.trf + trf_at(sl, 0);
 #pragma unroll
@@ -1589,7 +1589,7 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
           // an FP64 sum would add digits none of them carries
           const long long q = tq_at(pq, v);
           const float dqf = (d.tq[q] + d.tyf[q]) + d.tyb[q];
-          p[v] = old[v] + to_f64(dqf);
+          p[v] = old[v] + (double)dqf;
         } else {
           p[v] = old[v] + d.dqs[v * d.nint + pq];
         }
@@ -1688,7 +1688,8 @@ __global__ void __launch_bounds__(128, 3) k_update(DevPtr d, Par c, int stage) {
   }
 }
 
-// MX: FP32, with the velocity gradients formed from u - U (exact differences)
+// MX: FP32, with the velocity gradients formed from u - U (exact differences), its casts of
+// the neighbours' states on the integer pipes (to_f32, to_f64)
 template <bool MX>
 // if_changed: only when an upload changed some pv (the eddy viscosity is a function of the
 // cell's and its neighbours' pv)

@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c, long long g0, l
 #pragma unroll
     for (int v = 0; v < NPVM; ++v) {
       if (v < npv) {
-        sh[v] = to_f32(d.pv[v * n + g] - off[v]);
+        sh[v] = (float)(d.pv[v * n + g] - off[v]);
         d.pvf[v * n + g] = sh[v];
       }
     }
@@ -56,18 +56,18 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c, long long g0, l
     const double y1 = d.pv[5 * n + g], rl = d.dv[2 * n + g];
     if (c.fluid == 2 && y1 == 0.0 && rl > 0.0) {
       const double y2 = d.pv[6 * n + g], rho = d.dv[g], h = d.dv[n + g];
-      const float ilf = to_f32(1.0 / rl), iyl = 1.0f / (1.0f - to_f32(y2));
-      q[LQ_VP] = -to_f32(d.dv[16 * n + g]) * ilf * ilf;
-      q[LQ_VT] = -to_f32(d.dv[17 * n + g]) * ilf * ilf;
-      q[LQ_HP] = to_f32(d.dv[10 * n + g]) * iyl;
-      q[LQ_HT] = (to_f32(d.dv[11 * n + g]) - to_f32(y2) * 1004.64f) * iyl;
-      q[LQ_RP] = to_f32(d.pv[g] - to_f64(sh[0]));
-      q[LQ_RT] = to_f32((d.pv[4 * n + g] - c.tref) - to_f64(sh[4]));
-      q[LQ_RDEV] = to_f32(rho - c.rhoref);
-      q[LQ_HDEV] = to_f32(h - c.href);
-      q[LQ_RHO] = to_f32(rho);
+      const float ilf = (float)(1.0 / rl), iyl = 1.0f / (1.0f - (float)y2);
+      q[LQ_VP] = -(float)d.dv[16 * n + g] * ilf * ilf;
+      q[LQ_VT] = -(float)d.dv[17 * n + g] * ilf * ilf;
+      q[LQ_HP] = (float)d.dv[10 * n + g] * iyl;
+      q[LQ_HT] = ((float)d.dv[11 * n + g] - (float)y2 * 1004.64f) * iyl;
+      q[LQ_RP] = (float)(d.pv[g] - (double)sh[0]);
+      q[LQ_RT] = (float)((d.pv[4 * n + g] - c.tref) - (double)sh[4]);
+      q[LQ_RDEV] = (float)(rho - c.rhoref);
+      q[LQ_HDEV] = (float)(h - c.href);
+      q[LQ_RHO] = (float)rho;
       q[LQ_VL] = ilf;
-      q[LQ_HLG] = -to_f32(d.dv[13 * n + g]);   // h_l - h_g = -(dh/dy2)
+      q[LQ_HLG] = -(float)d.dv[13 * n + g];   // h_l - h_g = -(dh/dy2)
     }
 #pragma unroll
     for (int m = 0; m < NLQ; ++m) d.lqf[m * n + g] = q[m];
@@ -404,13 +404,13 @@ __global__ void __launch_bounds__(256, 4) k_visc_mx(DevPtr d, Par c, long long t
   float tvl[3] = {0, 0, 0}, tvr[3] = {0, 0, 0};
 #pragma unroll
   for (int q = 0; q < 3; ++q)
-    if (q < c.ntv) { tvl[q] = to_f32(d.tv[q * n + g]); tvr[q] = to_f32(d.tv[q * n + gr]); }
+    if (q < c.ntv) { tvl[q] = (float)d.tv[q * n + g]; tvr[q] = (float)d.tv[q * n + gr]; }
   float vis = 0.5f * (tvl[0] + tvr[0]);
   float con = 0.5f * (tvl[1] + tvr[1]);
   float emut = 0.0f, tcon = 0.0f;
   if (turb) {
     emut = 0.5f * (tvl[2] + tvr[2]);
-    tcon = 0.5f * (tvl[2] * to_f32(d.dv[11 * n + g]) + tvr[2] * to_f32(d.dv[11 * n + gr])) / 0.9f;
+    tcon = 0.5f * (tvl[2] * (float)d.dv[11 * n + g] + tvr[2] * (float)d.dv[11 * n + gr]) / 0.9f;
   }
   const int vars[6] = {1, 2, 3, 4, 7, 8};
   float gx[6], gy[6], gz[6], cc[6];
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(256, 4) k_visc_mx(DevPtr d, Par c, long long t
     fv[8] = (vis + emut * (1.0f / 1.3f)) * (gx[5] * nx[0] + gy[5] * nx[1] + gz[5] * nx[2]);
   } else if (turb) {
     float pkw = gx[4] * gx[5] + gy[4] * gy[5] + gz[4] * gz[5];
-    float rho = to_f32(0.5 * (d.dv[g] + d.dv[gr]));
+    float rho = (float)(0.5 * (d.dv[g] + d.dv[gr]));
     float ydns = 0.5f * (GF[(GM_GRD + 4) * n + g] + GF[(GM_GRD + 4) * n + gr]);
     float kf = cc[4], of = cc[5];
     float cdkw = fmaxf(1.712f * rho / of * pkw, 1.0e-10f);

@@ -18,7 +18,6 @@
 // single-precision constants (src/eos_module.f90:1367,1370,1371,1457); they are kept.
 #pragma once
 #include <utility>
-#include "df64.cuh"
 
 namespace cfd {
 
@@ -165,7 +164,7 @@ __device__ __forceinline__ T h2o_pww(T t) {
 // below 7e-6 over 273-647 K), the FP64 one only where p lies within 1e-4 of it.  (An FP64
 // saturation pressure is a division, a square root and a quotient on the FP64 pipe.)
 __device__ __forceinline__ bool above_psat(double p, double t) {
-  const float psf = h2o_pww<float>(to_f32(t)), pf = to_f32(p);
+  const float psf = h2o_pww<float>((float)t), pf = (float)p;
   if (fabsf(pf - psf) > 1.0e-4f * psf) return pf > psf;
   return p > h2o_pww<double>(t);
 }

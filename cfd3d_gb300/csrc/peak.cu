@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "cfd3d.h"
+#include "df64.cuh"
 
 namespace {
 
@@ -24,7 +25,85 @@ __global__ void __launch_bounds__(256) k_dfma_peak(double* out, int iters, doubl
   if (s == -1.0) out[0] = s;   // never true: keeps every chain live
 }
 
+// conversion throughput: each thread converts `reps` values of ordinary magnitude, the
+// next one derived from the last by integer operations only; MODE 0 the hardware
+// conversion, 1 the integer-pipe one (to_f32 / to_f64)
+__global__ void k_fill_ordinary(double* p, long long n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  unsigned long long z = 99ull + (unsigned long long)t * 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  p[t] = __longlong_as_double((long long)((z & 0x800fffffffffffffull) | ((unsigned long long)(1003 + (int)(z % 40)) << 52)));
+}
+template <int MODE>
+__global__ void k_d2f_rate(const double* in, float* out, long long n, int reps) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double x = in[t];
+  float acc = 0.0f;
+  for (int r = 0; r < reps; ++r) {
+    acc += MODE ? cfd::to_f32(x) : __double2float_rn(x);
+    x = __hiloint2double(__double2hiint(x), __double2loint(x) ^ (r + 1));
+  }
+  out[t] = acc;
+}
+template <int MODE>
+__global__ void k_f2d_rate(const float* in, double* out, long long n, int reps) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  float x = in[t];
+  unsigned acc = 0u;
+  for (int r = 0; r < reps; ++r) {
+    const double d = MODE ? cfd::to_f64(x) : (double)x;
+    acc ^= (unsigned)__double2loint(d) ^ (unsigned)__double2hiint(d);
+    x = __uint_as_float(__float_as_uint(x) ^ (unsigned)(r & 7));
+  }
+  out[t] = (double)acc;
+}
+
 }  // namespace
+
+extern "C" int cfd3d_convert_rate(double* rates) {
+  if (!rates) return CFD3D_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CFD3D_ERR_NODEVICE;
+  const long long n = 1ll << 24;
+  const int reps = 64, T = 256;
+  const unsigned G = (unsigned)((n + T - 1) / T);
+  double *d64 = nullptr, *o64 = nullptr;
+  float *f32 = nullptr;
+  if (cudaMalloc(&d64, n * 8) != cudaSuccess || cudaMalloc(&o64, n * 8) != cudaSuccess ||
+      cudaMalloc(&f32, n * 4) != cudaSuccess) {
+    cudaFree(d64); cudaFree(o64); cudaFree(f32);
+    return CFD3D_ERR_NOMEM;
+  }
+  k_fill_ordinary<<<G, T>>>(d64, n);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rc = CFD3D_OK;
+  auto time = [&](auto launch) -> double {
+    launch();   // (warm-up)
+    cudaEventRecord(e0);
+    launch();
+    cudaEventRecord(e1);
+    if (cudaEventSynchronize(e1) != cudaSuccess) { rc = CFD3D_ERR_CUDA; return 0.0; }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return (double)n * reps / (ms * 1e-3) / 1e9;
+  };
+  rates[0] = time([&] { k_d2f_rate<0><<<G, T>>>(d64, f32, n, reps); });
+  rates[1] = time([&] { k_d2f_rate<1><<<G, T>>>(d64, f32, n, reps); });
+  rates[2] = time([&] { k_f2d_rate<0><<<G, T>>>(f32, o64, n, reps); });
+  rates[3] = time([&] { k_f2d_rate<1><<<G, T>>>(f32, o64, n, reps); });
+  if (cudaGetLastError() != cudaSuccess) rc = CFD3D_ERR_CUDA;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d64); cudaFree(o64); cudaFree(f32);
+  return rc;
+}
 
 extern "C" int cfd3d_fp64_peak(double seconds, double* tflops) {
   if (!tflops || !(seconds > 0.0) || seconds > 60.0) return CFD3D_ERR_ARG;

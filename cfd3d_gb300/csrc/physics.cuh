@@ -254,7 +254,7 @@ __device__ __forceinline__ void if97_r2_rh(df64 P, df64 T, bool meta, df64& gp, 
 // out-of-line copy per FULL flag keeps the expanded sums out of every caller
 template <bool FULL>
 __device__ __noinline__ void iapws_pair_df64(double p, double t, bool meta, Phase<double>& l, Phase<double>& v) {
-  const df64 P = split_f64(p), T = split_f64(t);
+  const df64 P(p), T(t);
   if constexpr (FULL) {
     Phase<df64> lx, vx;
     iapws_l<df64, FULL>(P, T, lx);
@@ -280,12 +280,12 @@ template <bool FULL>
 __device__ __noinline__ void iapws_liq_df64(double p, double t, Phase<double>& l) {
   if constexpr (FULL) {
     Phase<df64> lx;
-    iapws_l<df64, FULL>(split_f64(p), split_f64(t), lx);
+    iapws_l<df64, FULL>(df64(p), df64(t), lx);
     l.rho = (double)lx.rho; l.h = (double)lx.h;
     l.drdp = (double)lx.drdp; l.drdt = (double)lx.drdt; l.dhdp = (double)lx.dhdp; l.dhdt = (double)lx.dhdt;
   } else {
     df64 gp, gt, tau;
-    if97_r1_rh(split_f64(p), split_f64(t), gp, gt, tau);
+    if97_r1_rh(df64(p), df64(t), gp, gt, tau);
     l.rho = (double)(df64((double)25.841246054191803727f) * tau / gp);
     l.h = (double)(df64(639675.036) * gt);
   }
@@ -298,7 +298,7 @@ template <bool VAP>
 __device__ __noinline__ void iapws_inv_df64(double p, double t, bool meta, double* il, double* hl, double* iv,
                                             double* hv) {
   // 1/rho = gamma_pi / (c tau) = gamma_pi T / (c T* ): no division beyond tau's
-  const df64 P = split_f64(p), T = split_f64(t);
+  const df64 P(p), T(t);
   df64 gp, gt, tau;
   if97_r1_rh(P, T, gp, gt, tau);
   *il = (double)(gp * T * df64(1.0 / ((double)25.841246054191803727f * 1386.0)));
@@ -388,22 +388,22 @@ __device__ __forceinline__ void mixture_split(double il, double hl, double iv, d
   const double irho = yl * il + y1 * iv + y2 * ig;
   dv[0] = 1.0 / irho;
   dv[1] = yl * hl + y1 * hv + y2 * hg;
-  const float fil = to_f32(il), fiv = to_f32(iv), fig = to_f32(ig);
+  const float fil = (float)il, fiv = (float)iv, fig = (float)ig;
   const float rl = 1.0f / fil, rv = 1.0f / fiv, rg = 1.0f / fig;
-  dv[2] = to_f64(rl); dv[3] = to_f64(rv); dv[4] = to_f64(rg);
-  const float r0 = to_f32(dv[0]), fyl = to_f32(yl), fy1 = to_f32(y1), fy2 = to_f32(y2);
+  dv[2] = rl; dv[3] = rv; dv[4] = rg;
+  const float r0 = (float)dv[0], fyl = (float)yl, fy1 = (float)y1, fy2 = (float)y2;
   const float r2 = r0 * r0;
   const float il2 = fil * fil, iv2 = fiv * fiv, ig2 = fig * fig;
   const float d6 = r2 * (fyl * il2 * lf.drdp + fy1 * iv2 * vf.drdp + fy2 * ig2 * gf.drdp);
   const float d7 = r2 * (fyl * il2 * lf.drdt + fy1 * iv2 * vf.drdt + fy2 * ig2 * gf.drdt);
   const float d10 = fyl * lf.dhdp + fy1 * vf.dhdp + fy2 * gf.dhdp;
   const float d11 = fyl * lf.dhdt + fy1 * vf.dhdt + fy2 * gf.dhdt;
-  dv[6] = to_f64(d6); dv[7] = to_f64(d7);
-  dv[8] = to_f64(r2 * (fil - fiv));
-  dv[9] = to_f64(r2 * (fil - fig));
-  dv[10] = to_f64(d10); dv[11] = to_f64(d11);
-  dv[12] = to_f64(to_f32(hv - hl));
-  dv[13] = to_f64(to_f32(hg - hl));
+  dv[6] = d6; dv[7] = d7;
+  dv[8] = r2 * (fil - fiv);
+  dv[9] = r2 * (fil - fig);
+  dv[10] = d10; dv[11] = d11;
+  dv[12] = (float)(hv - hl);
+  dv[13] = (float)(hg - hl);
   float c2 = r0 * d11 / (r0 * d6 * d11 + d7 * (1.0f - r0 * d10));
   if (c2 <= 0.0f) {  // the reference's "alternative calculation for snd2"
     if (fallbacks) atomicAdd(fallbacks, 1ull);
@@ -412,8 +412,8 @@ __device__ __forceinline__ void mixture_split(double il, double hl, double iv, d
     const float ic2g = (rg * gf.drdp * gf.dhdt + gf.drdt * (1.0f - rg * gf.dhdp)) / (rg * gf.dhdt);
     c2 = 1.0f / (r2 * (fyl * ic2l * il2 + fy1 * ic2v * iv2 + fy2 * ic2g * ig2));
   }
-  dv[5] = to_f64(c2);
-  dv[14] = to_f64(vf.drdp); dv[15] = to_f64(vf.drdt); dv[16] = to_f64(lf.drdp); dv[17] = to_f64(lf.drdt);
+  dv[5] = c2;
+  dv[14] = vf.drdp; dv[15] = vf.drdt; dv[16] = lf.drdp; dv[17] = lf.drdt;
 }
 
 // Phase properties and the mixture EOS in a generic scalar (the adjoint's dual numbers);
@@ -470,7 +470,7 @@ __device__ __forceinline__ void deteos_simple(int fluid, double p, double t, dou
 // t / (p r1) in df64, the mixture sums and its one reciprocal in FP64
 __device__ __forceinline__ void mix_face_mx(double p, double t, double y1, double y2, double il, double hl, double iv,
                                             double hv, double& rho, double& h) {
-  const double ig = (double)(split_f64(t) / (split_f64(p) * df64(0.00348383500557)));
+  const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
   const double yl = 1.0 - y1 - y2;
   rho = 1.0 / (yl * il + y1 * iv + y2 * ig);
   h = yl * hl + y1 * hv + y2 * (1004.64 * t);
@@ -532,7 +532,7 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
                                              double* dv, double* tv, unsigned long long* fb) {
   double il, hl, iv, hv;
   Phase<float> lf, vf, gf;
-  const float pf = to_f32(p), tf = to_f32(t);
+  const float pf = (float)p, tf = (float)t;
   if (fluid == 1) {
     Phase<double> l, v;
     stiffened(p, t, l);
@@ -552,13 +552,13 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
       // enthalpy difference and derivatives the implicit operator and the cavitation
       // source read
       iapws_inv_df64<false>(p, t, meta, &il, &hl, &iv, &hv);
-      iv = to_f64(1.0f / vf.rho);
-      hv = to_f64(vf.h);
+      iv = (double)(1.0f / vf.rho);
+      hv = (double)vf.h;
     }
   }
   ideal_gas<float>(pf, tf, gf);
   // the gas: 1/rho = T / (p r1) in df64, h = cp T
-  const double ig = (double)(split_f64(t) / (split_f64(p) * df64(0.00348383500557)));
+  const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
   const double hg = 1004.64 * t;
   mixture_split(il, hl, iv, hv, ig, hg, lf, vf, gf, y1, y2, dv, fb);
   if (with_prop) {
@@ -569,14 +569,14 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
       lv = stiffened_vis<float>(tf); lc = 4598.0f * lv;
       vv = ideal_vis<float>(tf); vc = 1395.333333f * vv;
     } else {
-      iapws_transport<float>(tf, to_f32(dv[2]), lv, lc);
-      iapws_transport<float>(tf, to_f32(dv[3]), vv, vc);
+      iapws_transport<float>(tf, (float)dv[2], lv, lc);
+      iapws_transport<float>(tf, (float)dv[3], vv, vc);
     }
     float gv = ideal_vis<float>(tf), gc = 1395.333333f * gv;
-    const float r0 = to_f32(dv[0]), fyl = to_f32(1.0 - y1 - y2), fy1 = to_f32(y1), fy2 = to_f32(y2);
-    const float fil = to_f32(il), fiv = to_f32(iv), fig = to_f32(ig);
-    tv[0] = to_f64(r0 * (lv * fyl * fil + vv * fy1 * fiv + gv * fy2 * fig));
-    tv[1] = to_f64(r0 * (lc * fyl * fil + vc * fy1 * fiv + gc * fy2 * fig));
+    const float r0 = (float)dv[0], fyl = (float)(1.0 - y1 - y2), fy1 = (float)y1, fy2 = (float)y2;
+    const float fil = (float)il, fiv = (float)iv, fig = (float)ig;
+    tv[0] = r0 * (lv * fyl * fil + vv * fy1 * fiv + gv * fy2 * fig);
+    tv[1] = r0 * (lc * fyl * fil + vc * fy1 * fiv + gc * fy2 * fig);
   }
 }
 

@@ -67,6 +67,7 @@ def lib():
     L.cfd3d_launch_shapes.argtypes = [H, ip]
     L.cfd3d_set_launch_shapes.argtypes = [H, ip]
     L.cfd3d_convert_selftest.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
+    L.cfd3d_convert_rate.argtypes = [dp]
     L.cfd3d_time_iterate.argtypes = [H, C.c_int, dp]
     L.cfd3d_profile_iterate.argtypes = [H, dp]
     L.cfd3d_set_device.argtypes = [C.c_int]
@@ -78,7 +79,7 @@ def lib():
 EXPORTS = ["cfd3d_create", "cfd3d_destroy", "cfd3d_last_error", "cfd3d_sizes", "cfd3d_initialize",
            "cfd3d_upload_state", "cfd3d_download_state", "cfd3d_upload_primitives", "cfd3d_upload_primitives_all", "cfd3d_download_state_all", "cfd3d_download_csf", "cfd3d_checkpoint_write", "cfd3d_checkpoint_read",
            "cfd3d_iterate", "cfd3d_iterate_n",
-           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats", "cfd3d_launch_shapes", "cfd3d_set_launch_shapes", "cfd3d_convert_selftest",
+           "cfd3d_unsteady_shift", "cfd3d_residual", "cfd3d_residual_vjp", "cfd3d_sweep_stall_test", "cfd3d_autotune", "cfd3d_grid_metrics", "cfd3d_eos_eval", "cfd3d_eos_eval_noalloc", "cfd3d_stats", "cfd3d_launch_shapes", "cfd3d_set_launch_shapes", "cfd3d_convert_selftest", "cfd3d_convert_rate",
            "cfd3d_time_iterate", "cfd3d_profile_iterate", "cfd3d_set_device", "cfd3d_fp64_peak"]
 STAGES = ["timestep", "boundary", "face_flux", "residual", "sweep_fwd", "sweep_bwd", "update_eos", "eddy_norms"]
 
@@ -111,6 +112,16 @@ def convert_selftest(n, seed=1):
     if rc:
         raise Cfd3dError(rc, "cfd3d_convert_selftest failed")
     return out[0], out[1]
+
+
+def convert_rate():
+    """cfd3d_convert_rate: G conversions/s of double -> float (hardware, integer pipes) and
+    float -> double (hardware, integer pipes) on the current device."""
+    out = (C.c_double * 4)()
+    rc = lib().cfd3d_convert_rate(out)
+    if rc:
+        raise Cfd3dError(rc, "cfd3d_convert_rate failed")
+    return {"d2f_hw": out[0], "d2f_int": out[1], "f2d_hw": out[2], "f2d_int": out[3]}
 
 
 def eos_eval(p, t, y1, y2, fluid=2, prop=False):

@@ -339,6 +339,12 @@ int  cfd3d_profile_iterate(cfd3d_handle *h, double *stage_ms);
  * kernels.  No reference counterpart (measurement only). */
 int  cfd3d_fp64_peak(double seconds, double *tflops);
 
+/* Throughput of float <-> double conversions on the current device, in G conversions/s:
+ * rates[0] / [1] double -> float by the hardware / on the integer pipes (the mixed form's),
+ * rates[2] / [3] float -> double likewise; 2^24 threads of 64 conversions each, timed with
+ * CUDA events.  No reference counterpart (measurement only). */
+int  cfd3d_convert_rate(double *rates);
+
 #ifdef __cplusplus
 }
 #endif

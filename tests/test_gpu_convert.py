@@ -18,3 +18,9 @@ def test_integer_conversions_match_hardware(seed):
 def test_convert_selftest_rejects_bad_arguments():
     with pytest.raises(native.Cfd3dError):
         native.convert_selftest(0)
+
+
+def test_convert_rate_measures():
+    r = native.convert_rate()
+    assert set(r) == {"d2f_hw", "d2f_int", "f2d_hw", "f2d_int"}
+    assert all(v > 0.0 for v in r.values())
