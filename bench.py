@@ -48,12 +48,11 @@ UNIT = "Mcell-iter/s"
 
 
 # DRAM bytes per cell of one k_rhs launch, dram__bytes_read.sum + dram__bytes_write.sum
-# of an ncu capture of the mixed form on the large case at 1/2 resolution (1769472 cells),
-# divided by the cells; the capture grows in proportion to the cells
-RHS_TRAFFIC_PER_CELL = (3.174136e9 + 1.794411e9) / 1769472
-# the same for one whole pseudo-iteration of that workload: dram read + write summed over
-# the 19 launches of its third iteration, divided by the cells
-ITER_TRAFFIC_PER_CELL = (11.845088e9 + 5.483316e9) / 1769472
+# of a one-pass ncu capture of the mixed form on the large case itself (14155776 cells, the
+# launch list of one pseudo-iteration), divided by the cells
+RHS_TRAFFIC_PER_CELL = (19.983611e9 + 11.175133e9) / 14155776
+# the same for the whole pseudo-iteration: dram read + write summed over its 22 launches
+ITER_TRAFFIC_PER_CELL = (72.269954e9 + 33.385758e9) / 14155776
 
 
 def algorithmic_bytes(cfg):

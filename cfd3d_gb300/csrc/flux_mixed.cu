@@ -28,7 +28,9 @@ __device__ __forceinline__ bool padded_interior(const DevPtr& d, long long g) {
 }
 
 // Per padded cell: the FP32 gauge shadow, and (interior cells) its EOS state as the base of
-// the face states' expansion.  With y1 = 0 the mixture holds only liquid and gas, so the liquid's 1/rho and h
+// the face states' expansion.  The kernel is mostly casts of FP64 state to FP32: they run on
+// the integer pipes (to_f32, to_f64), and the liquid's 1/rho in FP32, to spare the FP64
+// pipe.  With y1 = 0 the mixture holds only liquid and gas, so the liquid's 1/rho and h
 // follow from dv: 1/rho_l = 1/dv(3), h_l = h - y2 (h_g - h_l), and its derivatives
 // d(1/rho_l)/d(p, T) = -drho_l/d(p, T) / rho_l^2, dh_l/dp = dh/dp / (1 - y2) (the gas's h
 // does not depend on p) and dh_l/dT = (dh/dT - y2 cp_g) / (1 - y2).  The mixture's rho -
@@ -43,7 +45,7 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c, long long g0, l
 #pragma unroll
     for (int v = 0; v < NPVM; ++v) {
       if (v < npv) {
-        sh[v] = (float)(d.pv[v * n + g] - off[v]);
+        sh[v] = to_f32(d.pv[v * n + g] - off[v]);
         d.pvf[v * n + g] = sh[v];
       }
     }
@@ -56,18 +58,18 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c, long long g0, l
     const double y1 = d.pv[5 * n + g], rl = d.dv[2 * n + g];
     if (c.fluid == 2 && y1 == 0.0 && rl > 0.0) {
       const double y2 = d.pv[6 * n + g], rho = d.dv[g], h = d.dv[n + g];
-      const float ilf = (float)(1.0 / rl), iyl = 1.0f / (1.0f - (float)y2);
-      q[LQ_VP] = -(float)d.dv[16 * n + g] * ilf * ilf;
-      q[LQ_VT] = -(float)d.dv[17 * n + g] * ilf * ilf;
-      q[LQ_HP] = (float)d.dv[10 * n + g] * iyl;
-      q[LQ_HT] = ((float)d.dv[11 * n + g] - (float)y2 * 1004.64f) * iyl;
-      q[LQ_RP] = (float)(d.pv[g] - (double)sh[0]);
-      q[LQ_RT] = (float)((d.pv[4 * n + g] - c.tref) - (double)sh[4]);
-      q[LQ_RDEV] = (float)(rho - c.rhoref);
-      q[LQ_HDEV] = (float)(h - c.href);
-      q[LQ_RHO] = (float)rho;
+      const float ilf = 1.0f / to_f32(rl), iyl = 1.0f / (1.0f - to_f32(y2));
+      q[LQ_VP] = -to_f32(d.dv[16 * n + g]) * ilf * ilf;
+      q[LQ_VT] = -to_f32(d.dv[17 * n + g]) * ilf * ilf;
+      q[LQ_HP] = to_f32(d.dv[10 * n + g]) * iyl;
+      q[LQ_HT] = (to_f32(d.dv[11 * n + g]) - to_f32(y2) * 1004.64f) * iyl;
+      q[LQ_RP] = to_f32(d.pv[g] - to_f64(sh[0]));
+      q[LQ_RT] = to_f32((d.pv[4 * n + g] - c.tref) - to_f64(sh[4]));
+      q[LQ_RDEV] = to_f32(rho - c.rhoref);
+      q[LQ_HDEV] = to_f32(h - c.href);
+      q[LQ_RHO] = to_f32(rho);
       q[LQ_VL] = ilf;
-      q[LQ_HLG] = -(float)d.dv[13 * n + g];   // h_l - h_g = -(dh/dy2)
+      q[LQ_HLG] = -to_f32(d.dv[13 * n + g]);   // h_l - h_g = -(dh/dy2)
     }
 #pragma unroll
     for (int m = 0; m < NLQ; ++m) d.lqf[m * n + g] = q[m];
@@ -251,18 +253,28 @@ __global__ void __launch_bounds__(256) k_recon_mx(DevPtr d, Par c, long long t0,
   if (c.nmuscl > 0) {
     float c9[NPVM], c10[NPVM];
 #pragma unroll
-    for (int v = 0; v < NPVM; ++v) {
-      gl[v] = gR[v] = c9[v] = c10[v] = 0.0f;
-      if (v >= npv) continue;
-      if (MARCH) {
+    for (int v = 0; v < NPVM; ++v) gl[v] = gR[v] = c9[v] = c10[v] = 0.0f;
+    if (MARCH) {
+#pragma unroll
+      for (int v = 0; v < NPVM; ++v) {
+        if (v >= npv) continue;
         gl[v] = d.frec[v * n + g]; gR[v] = d.frec[(FREC_SIDE + v) * n + g];
         c9[v] = P[v * n + g]; c10[v] = P[v * n + gr];
-      } else {
+      }
+    } else {
+      // one rolled loop over the variables (a 38-cell stencil and the limiter each: unrolled
+      // nine times the kernel outgrows the instruction cache); its results reach the
+      // register arrays by predicated selects
+#pragma unroll 1
+      for (int v = 0; v < npv; ++v) {
         float x[38];
 #pragma unroll
         for (int l = 0; l < 38; ++l) x[l] = P[v * n + stencil_cell(l, g, f.sn, f.s1, f.s2)];
-        muscl_var<float>(c, x, gl[v], gR[v]);
-        c9[v] = x[8]; c10[v] = x[9];
+        float xl, xr;
+        muscl_var<float>(c, x, xl, xr);
+#pragma unroll
+        for (int u = 0; u < NPVM; ++u)
+          if (u == v) { gl[u] = xl; gR[u] = xr; c9[u] = x[8]; c10[u] = x[9]; }
       }
     }
     muscl_clip_mx(c, c9, c10, gl, gR);
