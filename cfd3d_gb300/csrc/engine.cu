@@ -3269,7 +3269,7 @@ int cfd3d_autotune(cfd3d_handle* h, int reps, int* choice) {
   int bestg = E.sweep_grid;
   tbest = 1e30f;
   for (int m = 1; c.timemethod == 3 && m <= std::max(per, 1); ++m) {   // (no sweeps in the explicit schemes)
-    if (m > 4 && m % 2) continue;   // 1, 2, 3, 4, 6, 8, ...
+    if (m > 4 && m % 2 && m != per) continue;   // 1, 2, 3, 4, 6, 8, ... and the occupancy limit
     const int grid = std::max(1, std::min(m * nsm, nwork));
     // (the timed sweeps run on the records of the iteration launched above; the forward one
     // rewrites the right-hand side it reads, which changes the values but not the work)
