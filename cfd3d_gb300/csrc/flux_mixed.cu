@@ -239,9 +239,9 @@ __global__ void __launch_bounds__(128) k_muscl_march(DevPtr d, Par c, long long 
 // are the cells' own.  (The per-variable loops run over the compile-time bound, guarded by
 // npv, so that the arrays stay in registers.)
 template <int DIR, bool MARCH = false>
-// (the column-fed instantiations at 4 CTAs of 256 threads per SM: 0.55 ms faster over the
-// j and k faces than the compiler's choice; the stencil one at 2, the compiler's)
-__global__ void __launch_bounds__(256, MARCH ? 4 : 2) k_recon_mx(DevPtr d, Par c, long long t0, long long t1) {
+// (the column-fed instantiations at 4 CTAs of 256 threads per SM, the stencil one at 3:
+// 0.55 and 0.65 ms faster than at the compiler's choice of 2)
+__global__ void __launch_bounds__(256, MARCH ? 4 : 3) k_recon_mx(DevPtr d, Par c, long long t0, long long t1) {
   const long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= t1) return;
   const FaceIdx f = face_of<DIR>(d, t);
