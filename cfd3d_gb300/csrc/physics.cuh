@@ -293,12 +293,14 @@ __device__ __noinline__ void iapws_liq_df64(double p, double t, Phase<double>& l
 
 // The mixed form's face-state EOS: 1/rho and h of the liquid (and of the vapour when VAP)
 // from the df64 sums, the reciprocal also taken in df64 (on the FP32 pipes: an FP64
-// division costs a GB300 far more)
+// division costs a GB300 far more), and the gas's 1/rho = t / (p r1) from the same df64
+// splits of p and t (each split costs FP64-pipe conversions)
 template <bool VAP>
 __device__ __noinline__ void iapws_inv_df64(double p, double t, bool meta, double* il, double* hl, double* iv,
-                                            double* hv) {
+                                            double* hv, double* ig) {
   // 1/rho = gamma_pi / (c tau) = gamma_pi T / (c T* ): no division beyond tau's
   const df64 P(p), T(t);
+  *ig = (double)(T / (P * df64(0.00348383500557)));
   df64 gp, gt, tau;
   if97_r1_rh(P, T, gp, gt, tau);
   *il = (double)(gp * T * df64(1.0 / ((double)25.841246054191803727f * 1386.0)));
@@ -468,9 +470,8 @@ __device__ __forceinline__ void deteos_simple(int fluid, double p, double t, dou
 // the reconstructed face states; the same operations as the rho, h of deteos_simple
 // the mixed form's face mixture from the phases' 1/rho and h: the gas's reciprocal as
 // t / (p r1) in df64, the mixture sums and its one reciprocal in FP64
-__device__ __forceinline__ void mix_face_mx(double p, double t, double y1, double y2, double il, double hl, double iv,
-                                            double hv, double& rho, double& h) {
-  const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
+__device__ __forceinline__ void mix_face_mx(double t, double y1, double y2, double il, double hl, double iv,
+                                            double hv, double ig, double& rho, double& h) {
   const double yl = 1.0 - y1 - y2;
   rho = 1.0 / (yl * il + y1 * iv + y2 * ig);
   h = yl * hl + y1 * hv + y2 * (1004.64 * t);
@@ -481,10 +482,10 @@ __device__ __forceinline__ void eos_rho_h(int fluid, double p, double t, double 
   if constexpr (MX) {
     if (fluid != 1) {
       // phase reciprocals in df64
-      double il, hl, iv = 0.0, hv = 0.0;
-      if (y1 != 0.0) iapws_inv_df64<true>(p, t, above_psat(p, t), &il, &hl, &iv, &hv);
-      else iapws_inv_df64<false>(p, t, false, &il, &hl, &iv, &hv);
-      mix_face_mx(p, t, y1, y2, il, hl, iv, hv, rho, h);
+      double il, hl, iv = 0.0, hv = 0.0, ig;
+      if (y1 != 0.0) iapws_inv_df64<true>(p, t, above_psat(p, t), &il, &hl, &iv, &hv, &ig);
+      else iapws_inv_df64<false>(p, t, false, &il, &hl, &iv, &hv, &ig);
+      mix_face_mx(t, y1, y2, il, hl, iv, hv, ig, rho, h);
       return;
     }
   }
@@ -530,7 +531,7 @@ __device__ __forceinline__ void deteos(int fluid, int with_prop, double p, doubl
 // operator, the preconditioning speed and the FP32 viscous fluxes); mixture in FP64.
 __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p, double t, double y1, double y2,
                                              double* dv, double* tv, unsigned long long* fb) {
-  double il, hl, iv, hv;
+  double il, hl, iv, hv, ig;
   Phase<float> lf, vf, gf;
   const float pf = (float)p, tf = (float)t;
   if (fluid == 1) {
@@ -538,28 +539,28 @@ __device__ __forceinline__ void deteos_split(int fluid, int with_prop, double p,
     stiffened(p, t, l);
     ideal_gas(p, t, v);
     il = 1.0 / l.rho; hl = l.h; iv = 1.0 / v.rho; hv = v.h;
+    ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));   // the gas: t / (p r1)
     lf.drdp = (float)l.drdp; lf.drdt = (float)l.drdt; lf.dhdp = (float)l.dhdp; lf.dhdt = (float)l.dhdt;
     vf.drdp = (float)v.drdp; vf.drdt = (float)v.drdt; vf.dhdp = (float)v.dhdp; vf.dhdt = (float)v.dhdt;
   } else {
+    // (the gas's 1/rho = t / (p r1) comes with the phases, from the same df64 splits)
     const bool meta = above_psat(p, t);
     iapws_l<float, true>(pf, tf, lf);
     iapws_v_meta<float, true>(pf, tf, meta, vf);
     if (y1 != 0.0) {
-      iapws_inv_df64<true>(p, t, meta, &il, &hl, &iv, &hv);
+      iapws_inv_df64<true>(p, t, meta, &il, &hl, &iv, &hv, &ig);
     } else {
       // without vapour the vapour's 1/rho and h enter the mixture with the factor y1 = 0:
       // its df64 sums are skipped, and the phase's FP32 values serve the vapour density,
       // enthalpy difference and derivatives the implicit operator and the cavitation
       // source read
-      iapws_inv_df64<false>(p, t, meta, &il, &hl, &iv, &hv);
+      iapws_inv_df64<false>(p, t, meta, &il, &hl, &iv, &hv, &ig);
       iv = (double)(1.0f / vf.rho);
       hv = (double)vf.h;
     }
   }
   ideal_gas<float>(pf, tf, gf);
-  // the gas: 1/rho = T / (p r1) in df64, h = cp T
-  const double ig = (double)(df64(t) / (df64(p) * df64(0.00348383500557)));
-  const double hg = 1004.64 * t;
+  const double hg = 1004.64 * t;   // the gas's h = cp T
   mixture_split(il, hl, iv, hv, ig, hg, lf, vf, gf, y1, y2, dv, fb);
   if (with_prop) {
     // the transport properties in FP32: they feed the FP32 viscous fluxes, the SST terms
