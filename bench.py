@@ -50,9 +50,9 @@ UNIT = "Mcell-iter/s"
 # DRAM bytes per cell of one k_rhs launch, dram__bytes_read.sum + dram__bytes_write.sum
 # of a one-pass ncu capture of the mixed form on the large case itself (14155776 cells, the
 # launch list of one pseudo-iteration), divided by the cells
-RHS_TRAFFIC_PER_CELL = (19.982660e9 + 11.177230e9) / 14155776
+RHS_TRAFFIC_PER_CELL = (19.984210e9 + 11.177800e9) / 14155776
 # the same for the whole pseudo-iteration: dram read + write summed over its 22 launches
-ITER_TRAFFIC_PER_CELL = (72.283070e9 + 33.747710e9) / 14155776
+ITER_TRAFFIC_PER_CELL = (72.270140e9 + 33.714040e9) / 14155776
 
 
 def algorithmic_bytes(cfg):
