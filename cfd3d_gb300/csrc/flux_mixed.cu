@@ -40,9 +40,6 @@ __global__ void __launch_bounds__(256) k_shadow(DevPtr d, Par c, long long g0, l
   const long long stride = (long long)gridDim.x * blockDim.x;
   const int npv = c.npv;
   const double off[NPVM] = {0.0, c.uref_vec[0], c.uref_vec[1], c.uref_vec[2], c.tref, 0.0, 0.0, 0.0, 0.0};
-  // (two cells per pass: every thread is resident, so the loads two cells put in flight are
-  // the memory parallelism the kernel has)
-#pragma unroll 2
   for (long long g = g0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; g < g1; g += stride) {
     float sh[NPVM];
 #pragma unroll
