@@ -293,19 +293,29 @@ def pinned(shape):
 
 def run_e2e(eng, case, steps, it0):
     """The drop-in mode: per step, pv and qq up from pinned host memory (dv, tv derived on
-    the device), one iteration, pv, dv, tv down.  Returns (ms per step, H2D, D2H bytes)."""
+    the device), one iteration, pv, dv, tv down.  Returns (ms per step, H2D, D2H bytes).
+    The host arrays are carved from one pinned arena (2 MiB-aligned views): on a host whose
+    memory is fragmented, dozens of separately pinned arrays measured the device-to-host
+    copies 40 % slower than one pinned allocation."""
     import torch
+    states = [eng.download(n) for n in range(len(case["blocks"]))]
+    keys = [k for k in ("pv", "dv", "tv", "qq")
+            if not ((k == "qq" and not eng.nqq) or (k == "tv" and eng.ntv == 0))]
+    align = (2 << 20) // 8
+    words = sum(-(-st[k].size // align) * align for st in states for k in keys)
+    arena_t = torch.empty(words, dtype=torch.float64, pin_memory=True)
+    arena = arena_t.numpy()
     bufs = []
     h2d = d2h = 0
-    for n in range(len(case["blocks"])):
-        st = eng.download(n)
+    off = 0
+    for st in states:
         keep = {}
-        for k in ("pv", "dv", "tv", "qq"):
-            if (k == "qq" and not eng.nqq) or (k == "tv" and eng.ntv == 0):
-                continue
-            t, a = pinned(np.ascontiguousarray(st[k]).shape)
-            a[...] = st[k]
-            keep[k] = (t, a)
+        for k in keys:
+            src = np.ascontiguousarray(st[k])
+            a = arena[off:off + src.size].reshape(src.shape)
+            off += -(-src.size // align) * align
+            a[...] = src
+            keep[k] = (arena_t, a)
             if k in ("pv", "qq"):
                 h2d += a.nbytes
             if k != "qq":
